@@ -1,0 +1,344 @@
+"""Throughput of the GB300 kick-drift SPH step (particle-steps/s) at ~1M particles.
+
+Workload (one "step" = one kick-drift step of the whole domain): elastoplastic
+cylinder upsetting, R = 10 mm, L = 30 mm, dx = 0.2112 mm (982,072 particles),
+h = 1.2 dx cubic spline, steel E = 200 GPa, bilinear sigma_y = 300 MPa,
+Et = 1.5 GPa, bottom two layers fixed, top two layers at -1 m/s, Monaghan
+viscosity alpha = 1, dt = 0.4 h / Cs, seeded +-1e-3 dx position jitter.  The
+state (~1 GB) is far larger than the 129 MB L2, so no flush is needed between
+steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+The default arm runs the CUDA library; ``--impl reference`` times the CPU
+restatement of the reference's OpenMP structure (per-thread pair lists and the
+Nishimura gather, built from oracle/) on all host cores, on the same workload.
+N > 1 runs N independent replicas (the path does not shard across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s @1M: mixed vs FP64 on GB300 at ≤1e-4 err; adjoint/fwd time"
+R, L = 0.010, 0.030
+DX_1M = 0.2112e-3
+
+# Compulsory HBM bytes per particle of each gather kernel in the plain FP64
+# form (fields read once per pass, state read+written once, 4-byte neighbour
+# index per entry + 4-byte row length): see the design doc's traffic model.
+ALG_BYTES = {
+    "k_accel": lambda nnz: 144 + 4 * nnz + 4,           # x,v,rho,m,h,Sigma(6) -> a
+    "k_density_drift": lambda nnz: 272 + 4 * nnz + 4,   # x,v,a,rho,m,h -> v,rho ; x,v,a -> x,v
+    "k_rate_stress": lambda nnz: 440 + 4 * nnz + 4,     # x,v,rho,m,h,tau,eps,eps_p,pl,sy -> tau,Sigma,eps,...
+    "k_energy": lambda nnz: 88 + 4 * nnz + 4,           # x,v,p,rho,m,h -> dkin ; tau,SR -> dint
+}
+# FP64 operations per neighbour entry / per particle of the same kernels.
+ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (55, 250), "k_energy": (35, 20)}
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            j = json.load(open(p))
+            return float(j["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms in a thread."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([c.strip() for c in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in self.rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def build_domain(dom, dx=DX_1M):
+    from weldform_gb300 import configs
+    return configs.cylinder_upsetting(dom, R=R, L=L, dx=dx, v_top=-1.0)
+
+
+def _workload(n, precision):
+    return {"workload": f"cylinder upsetting R=10mm L=30mm dx={DX_1M * 1e3:.4f}mm N={n}, bilinear steel, "
+                        f"v_top=-1 m/s, alpha=1, dt=0.4h/Cs",
+            "particles": n, "form": precision, "l2": "state > 129 MB L2 (no flush needed)",
+            "parallelism": "replicas"}
+
+
+def time_form(wfmod, precision, steps, warmup, gpu):
+    """Headline timing of one precision form: graph-replayed steps between CUDA events."""
+    d = wfmod.Domain()
+    d.set("device", gpu)
+    d.set("precision", precision)
+    case = build_domain(d)
+    d.prepare(case.dt)
+    d.step(max(warmup, 3))
+    ms, launches = d.step_timed(steps)
+    nnz = 2.0 * d.geti("pair_count") / case.n
+    return d, case, ms, launches, nnz
+
+
+def roofline(d, case, nnz, steps, peak_gbs, peak_kind):
+    prof = d.profile_steps(max(2, min(steps, 10)))
+    kernels = {k: v for k, v in prof.items() if k in ALG_BYTES}
+    tot = sum(v[0] for v in prof.values())
+    top = max(kernels.items(), key=lambda kv: kv[1][0])
+    name, (ms_tot, cnt) = top
+    ms = ms_tot / cnt
+    alg = ALG_BYTES[name](nnz) * case.n
+    achieved = alg / (ms * 1e-3) / 1e9
+    per_nb, per_p = ALG_FLOPS[name]
+    flops = (per_nb * nnz + per_p) * case.n
+    shares = {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:8]}
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    if os.path.exists(tp):
+        for line in open(tp):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == name:
+                try:
+                    traffic = float(parts[1]) * case.n
+                except ValueError:
+                    pass
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 2), "peak": peak_gbs, "unit": "GB/s",
+            "frac": round(achieved / peak_gbs, 4), "peak_source": peak_kind, "traffic": traffic,
+            "alg_bytes_per_launch": alg, "ms_per_launch": round(ms, 4),
+            "fp64_tflops": round(flops / (ms * 1e-3) / 1e12, 4), "kernel_time_shares": shares}
+
+
+def e2e(wfmod, precision, steps, gpu, pinned):
+    """Through the C ABI with host buffers: upload x, v, Sigma; K steps; download x, Sigma."""
+    d = wfmod.Domain()
+    d.set("device", gpu)
+    d.set("precision", precision)
+    case = build_domain(d)
+    d.prepare(case.dt)
+    d.step(3)
+    x = pinned(d.get_array("x"))
+    v = pinned(d.get_array("v"))
+    t0 = time.perf_counter()
+    d.set_array("x", x)
+    d.set_array("v", v)
+    d.step(steps)
+    xo = d.get_array("x")
+    so = d.get_array("Sigma")
+    el = time.perf_counter() - t0
+    h2d = (x.nbytes + v.nbytes) / steps
+    d2h = (xo.nbytes + so.nbytes) / steps
+    d.close()
+    return {"value": case.n * steps / el, "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h)}
+
+
+def cpu_baseline(steps=2):
+    """The reference-structured CPU restatement on all host threads, 1M workload."""
+    import ctypes
+    import __graft_entry__ as ge
+    import weldform_gb300 as wf
+    path = os.path.join(ge.ORACLE_BUILD, "libwf_oracle.so")
+    if not os.path.exists(path):
+        ge.build_oracle()
+    lib = wf.bind(ctypes.CDLL(path), "wfo_")
+    threads = os.cpu_count() or 1
+    d = wf.Domain(lib=lib, prefix="wfo_")
+    d.set("cpu_mode", 1)
+    d.set("cpu_threads", threads)
+    case = build_domain(d)
+    d.prepare(case.dt)
+    d.step(1)  # first step carries the neighbour search
+    ms, _ = d.step_timed(steps)
+    d.close()
+    return {"value": case.n * steps / (ms * 1e-3), "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} steady kick-drift steps of the {case.n}-particle workload after the first "
+                      f"(search) step, reference-structured OpenMP restatement, {threads} threads"}
+
+
+def dist_setup(n):
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def reduce_max(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    warmup = max(a.warmup, 3)
+    rank, world, local, pg = dist_setup(a.gpus)
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        import ctypes
+        import __graft_entry__ as ge
+        import weldform_gb300 as wf
+        path = os.path.join(ge.ORACLE_BUILD, "libwf_oracle.so")
+        if not os.path.exists(path):
+            ge.build_oracle()
+        lib = wf.bind(ctypes.CDLL(path), "wfo_")
+        threads = os.cpu_count() or 1
+        d = wf.Domain(lib=lib, prefix="wfo_")
+        d.set("cpu_mode", 1)
+        d.set("cpu_threads", threads)
+        case = build_domain(d)
+        d.prepare(case.dt)
+        d.step(1)
+        steps = max(1, min(a.steps, 10))
+        wsteps = max(0, min(warmup, 2))
+        d.step(wsteps)
+        ms, _ = d.step_timed(steps)
+        val = case.n * steps / (ms * 1e-3)
+        line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": a.gpus, "steps": steps,
+                "warmup": wsteps + 1, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": _workload(case.n, "reference OpenMP structure (CPU)"),
+                "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                                 "sample": f"{steps} steps of the full {case.n}-particle workload"},
+                "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import weldform_gb300 as wfmod
+    try:
+        import torch
+        def pinned(arr):
+            t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
+            return t.numpy()
+        have_torch_cuda = torch.cuda.is_available()
+    except Exception:
+        torch = None
+        have_torch_cuda = False
+        def pinned(arr):
+            return np.ascontiguousarray(arr)
+
+    gpu = local if world > 1 else 0
+    peak, peak_kind = measured_peaks()
+    headline = wfmod.PRECISION_FP64
+    forms = {}
+    try:
+        wfmod.Domain().close()
+    except Exception as e:
+        print(json.dumps({"metric": METRIC, "error": str(e)}))
+        raise
+    # Headline form (timed region with barrier + synchronize on both sides).
+    d, case, _, _, nnz = time_form(wfmod, headline, 1, warmup, gpu)
+    barrier(pg)
+    if have_torch_cuda:
+        torch.cuda.synchronize()
+    with ClockSampler(gpu) as clk:
+        ms, launches = d.step_timed(a.steps)
+    if have_torch_cuda:
+        torch.cuda.synchronize()
+    barrier(pg)
+    ms_max = reduce_max(pg, ms)
+    value = world * case.n * a.steps / (ms_max * 1e-3)
+    rl = roofline(d, case, nnz, a.steps, peak, peak_kind)
+    d.close()
+    ee = e2e(wfmod, headline, a.steps, gpu, pinned)
+    ee["value"] *= world
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": a.steps,
+            "warmup": warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lattice jitter)",
+            "config": _workload(case.n, "plain FP64"), "gpu_launches": launches, "clocks": clk.summary(),
+            "roofline": rl, "e2e": ee, "neighbours_per_particle": round(nnz, 3)}
+    line["forms"] = {"fp64": {"value": value, "ms_per_step": ms_max / a.steps}}
+    if rank == 0 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,205 @@
+/*
+ * weldform_gb300 — C ABI of the GB300 (sm_103a) explicit SPH solid step.
+ *
+ * This is the drop-in boundary for WeldForm's kick-drift solid path.  The
+ * reference has no plugin or FFI layer: its "API" is the public members of
+ * SPH::Domain, SPH::Particle, the Material_ classes and TriMesh, compiled into
+ * each executable.  Every entry point below names the reference member it
+ * replaces (paths relative to the WeldForm source tree).
+ *
+ * Conventions
+ *  - Every call returns an int status (WF_OK == 0).  wf_last_error() gives a
+ *    human-readable message for the last failing call on this thread.
+ *    No exception ever crosses the ABI (the reference throws `new Fatal`,
+ *    External/fatal.h:58-63, or calls abort(), Functions.cpp:64-70).
+ *  - Particles are addressed in the reference's insertion order ("original
+ *    index"); the library reorders them internally (cell-sorted) and maps
+ *    indices back on every host transfer.
+ *  - Vectors are passed as double[3]; per-particle arrays as flat host
+ *    buffers (n * components, row-major).  The library copies inputs and
+ *    never keeps a caller pointer.
+ *  - One host thread per domain; one CUDA stream per domain.
+ *  - SI units, exactly as the reference (no unit conversion anywhere).
+ */
+#ifndef WELDFORM_GB300_H
+#define WELDFORM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define WF_OK               0
+#define WF_ERR_ARG          1  /* invalid argument / unknown field name          */
+#define WF_ERR_CUDA         2  /* CUDA runtime error or no device                 */
+#define WF_ERR_NAN          3  /* non-finite value detected in the state          */
+#define WF_ERR_NBR_OVERFLOW 4  /* a particle exceeds the neighbour cap (100,
+                                  MAX_NB_PER_PART, Source/Domain.h:49)           */
+#define WF_ERR_TIMEOUT      5  /* a bounded device wait gave up                   */
+#define WF_ERR_STATE        6  /* call not valid in the current solver state      */
+#define WF_ERR_NOMEM        7  /* device or host allocation failed                */
+#define WF_ERR_UNSUPPORTED  8  /* reference feature outside this build's scope   */
+
+/* ---- precision forms ------------------------------------------------------ */
+#define WF_PRECISION_FP64   0  /* plain form: FP64 throughout                     */
+#define WF_PRECISION_MIXED  1  /* FP32 Kahan pair sums, FP64 integration/return   */
+
+/* ---- material models (Source/Particle.h:34-37) ---------------------------- */
+#define WF_BILINEAR      0
+#define WF_HOLLOMON      1
+#define WF_JOHNSON_COOK  2
+
+/* ---- contact stiffness laws ------------------------------------------------ */
+#define WF_CONTACT_WANG    0  /* kij = 2 m / dt^2, Source/Contact_Wang.cpp:187      */
+#define WF_CONTACT_PENALTY 1  /* kij = PFAC * cont_stiff, Source/Contact.cpp:423;
+                                 cont_stiff per Source/SolverKickDrift.cpp:79-84   */
+#define WF_CONTACT_AREA    2  /* kij = PFAC * (m/rho)^(2/3): a pressure-per-length
+                                 penalty times the particle contact area
+                                 (Source/Contact_Wang.cpp:248 gives the area)     */
+
+typedef struct wf_domain wf_domain;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int wf_version(void);
+/* Message of the last failing call on this thread ("" if none). */
+const char* wf_last_error(void);
+
+/* Domain::Domain (Source/Domain.cpp:78-175).  dimension must be 3. */
+int wf_domain_create(int dimension, wf_domain** out);
+/* Domain::~Domain (Source/Domain.cpp:177-181).  Frees host and device state. */
+int wf_domain_destroy(wf_domain* d);
+
+/* Domain scalar fields (Source/Domain.h:113-537).  Names are the reference
+ * member names: "Cellfac", "pl_work_heat_frac", "friction_sta",
+ * "friction_dyn", "PFAC", "DFAC", "DomMax.x|y|z", "DomMin.x|y|z",
+ * "contact_force_factor".  Integer fields: "Nproc", "ts_nb_inc", "auto_ts",
+ * "nonlock_sum", "pl_heating", "thermal_solver", "contact",
+ * "contact_mesh_auto_update", "GradientType", "contact_alg" (WF_CONTACT_*),
+ * "precision" (WF_PRECISION_*), "device" (CUDA device ordinal, before the
+ * prologue), "use_graph" (replay each step as one CUDA graph, default 1),
+ * "cpu_threads" (unused on the GPU path). */
+int wf_set_domain_f64(wf_domain* d, const char* name, double value);
+int wf_set_domain_i32(wf_domain* d, const char* name, int value);
+/* Read-back of scalars: "Time", "deltat", "hmax", "int_energy_sum",
+ * "kin_energy_sum", "plastic_work", "contact_force_sum",
+ * "contact_reaction_sum", "ext_forces_work", "max_pl_strain", "m_maxT",
+ * "m_minT"; integers: "particle_count", "solid_part_count", "steps",
+ * "pair_count", "contact_pair_count", "nb_searches", "CellNo.x|y|z",
+ * "surface_count". */
+int wf_get_domain_f64(wf_domain* d, const char* name, double* value);
+int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* value);
+
+/* Domain::Kernel_Set (Source/Domain.cpp:190-194).  Only Qubic_Spline (0). */
+int wf_kernel_set(wf_domain* d, int kernel_type);
+
+/* Domain::AddBoxLength (Source/Domain.h:127-128, Source/Domain.cpp:326-599).
+ * 3D packings: type 1 cubic, type 0 hexagonal close packing. */
+int wf_add_box_length(wf_domain* d, int tag, const double V[3], double Lx, double Ly,
+                      double Lz, double r, double density, double h, int type,
+                      int rotation, int random, int fixed);
+/* Domain::AddCylinderLength (Source/Domain.h:130-131, Source/Domain.cpp:708-860). */
+int wf_add_cylinder_length(wf_domain* d, int tag, const double V[3], double Rxy,
+                           double Lz, double r, double density, double h, int fixed,
+                           int ghost);
+/* Domain::AssignZone (Source/Domain.h:495, Source/Domain.cpp:691-706). */
+int wf_assign_zone(wf_domain* d, const double start[3], const double end[3], int id,
+                   int64_t* count);
+
+/* Per-particle public fields (Source/Particle.h:50-265) for every particle
+ * whose ID equals `zone`, or all particles when zone < 0.
+ * f64 fields: "G", "Cs", "Sigmay", "Ep", "Alpha", "Beta", "TI", "TIInitDist",
+ * "k_T", "cp_T", "T", "th_exp", "Density", "RefDensity", "Mass", "h", "P0",
+ * "q_source".  i32 fields: "PresEq", "Fail", "Material_model", "mat",
+ * "Material", "ID", "IsFree", "print_history". */
+int wf_set_particle_f64(wf_domain* d, const char* field, int zone, double value);
+int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value);
+/* Whole-array transfer in original particle order.  Vector fields ("x", "v",
+ * "a", "Displacement", "normal", "contforce") take 3 values per particle;
+ * tensor fields ("Sigma", "ShearStress", "StrainRate", "RotationRate",
+ * "Strain", "Strain_pl") 9 (row-major, full 3x3, as the reference stores
+ * them); scalars 1 ("Density", "Pressure", "pl_strain", "Sigmay", "T",
+ * "dTdt", "eff_strain_rate", "q_plheat", "Mass", "h", "delta_pl_strain",
+ * "dDensity").  n is the total number of doubles. */
+int wf_set_particle_array_f64(wf_domain* d, const char* field, const double* src,
+                              int64_t n);
+int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int64_t n);
+/* Integer arrays: "ID", "Nb", "IsFree". */
+int wf_get_particle_array_i32(wf_domain* d, const char* field, int32_t* dst, int64_t n);
+
+/* Materials (Source/Material.h:64-224, Source/Material.cpp:6-72).
+ * model WF_BILINEAR: params {E, nu}            (hardening via particle Ep)
+ * model WF_HOLLOMON: params {E, nu, sy0, K, m} (Material.cpp:48-57)
+ * model WF_JOHNSON_COOK: params {E, nu, A, B, n, C, eps_0, m, T_m, T_t}
+ *   (JohnsonCook ctor order, Material.h:124-131).
+ * Returns the material index to put in the particle field "mat". */
+int wf_add_material(wf_domain* d, int model, const double* params, int nparams,
+                    int* mat_id);
+
+/* Amplitude table (SPH::amplitude, Source/Domain.h:69-89). */
+int wf_add_amplitude(wf_domain* d, int id, const double* time, const double* value,
+                     int n);
+/* Velocity boundary condition in the form the JSON driver's UserAcc applies
+ * (Source/WeldForm.cpp:51-120): particles with ID == zone get a = 0 and
+ * v = value (value_type 0) or amp_factor * amplitude(t) * value (value_type 1);
+ * a rigid mesh whose id == zone gets m_v (and m_w = value_ang). The callback
+ * runs at the three reference call sites (Source/SolverKickDrift.cpp:208,231,267). */
+int wf_add_velocity_bc(wf_domain* d, int zone, const double value[3],
+                       const double value_ang[3], int value_type, int amp_id,
+                       double amp_factor);
+
+/* Rigid plane contact surface: TriMesh::AxisPlaneMesh (Source/Mesh.cpp:82-203),
+ * TriMesh::CalcSpheres (Mesh.cpp:206-220) and Domain::AddTrimeshParticles
+ * (Source/Contact.cpp:10-38) in one call.  Returns the mesh index. */
+int wf_add_rigid_plane(wf_domain* d, int axis, int positaxisorent, const double p1[3],
+                       const double p2[3], int dens, double hfac, int zone_id,
+                       int* mesh_id);
+/* TriMesh::SetVel / SetRotAxisVel (Source/Mesh.h:68-69). */
+int wf_set_mesh_velocity(wf_domain* d, int mesh, const double v[3], const double w[3]);
+/* Domain::m_contact_force[mesh] (Source/Contact_Wang.cpp:312). */
+int wf_get_contact_force(wf_domain* d, int mesh, double out[3]);
+
+/* Domain::SolveDiffUpdateKickDrift (Source/Domain.h:199,
+ * Source/SolverKickDrift.cpp:23-401) without file output: runs the prologue
+ * (if not yet run) and steps while Time <= tf && idx_out <= maxidx. */
+int wf_solve_kickdrift(wf_domain* d, double tf, double dt, double dtOut, int64_t maxidx);
+/* The solver prologue only (SolverKickDrift.cpp:23-115) with time step dt. */
+int wf_prepare_kickdrift(wf_domain* d, double dt);
+/* Advance exactly nsteps kick-drift steps (SolverKickDrift.cpp:117-393). */
+int wf_step(wf_domain* d, int64_t nsteps);
+
+/* Neighbour search at the current positions (Neighbour.cpp:141-257 cell
+ * assignment + Neighbour.cpp:346-477 search + CalcPairPosList :617-694).
+ * Valid after wf_prepare_kickdrift. */
+int wf_neighbour_search(wf_domain* d);
+/* The current same-material pair list (SMPairs) as CSR in original indices,
+ * each row in canonical order: j > i ascending, then j < i ascending (the
+ * Anei layout, Neighbour.cpp:672-675).  offsets has particle_count+1 entries;
+ * idx holds at most cap entries (call with idx == NULL to get the size in
+ * offsets[particle_count]). */
+int wf_get_neighbours(wf_domain* d, int64_t* offsets, int32_t* idx, int64_t cap);
+/* Contact pairs (ContPairs, Contact.cpp:57-132): row = solid particle,
+ * entries = rigid-mesh particles, ascending; same calling convention. */
+int wf_get_contact_pairs(wf_domain* d, int64_t* offsets, int32_t* idx, int64_t cap);
+
+/* Blocks until the domain's stream is idle and reports deferred device
+ * status (non-finite state, neighbour overflow, bounded-wait timeout). */
+int wf_synchronize(wf_domain* d);
+
+/* ---- measurement helpers (no counterpart in the reference) ---------------
+ * wf_step_timed: nsteps steps bracketed by CUDA events recorded on the
+ * domain's stream (synchronised before and after); elapsed_ms is the event
+ * time, kernel_launches the number of this library's kernels launched.
+ * wf_profile_steps: nsteps steps launched one kernel at a time with an event
+ * after every kernel; per distinct kernel name (at most cap, name_len bytes
+ * each in names) the summed milliseconds and launch count. */
+int wf_step_timed(wf_domain* d, int64_t nsteps, double* elapsed_ms, int64_t* kernel_launches);
+int wf_profile_steps(wf_domain* d, int64_t nsteps, char* names, int name_len, double* total_ms,
+                     int64_t* launches, int cap, int* nkernels);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WELDFORM_GB300_H */

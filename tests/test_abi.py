@@ -1,0 +1,59 @@
+"""C-ABI surface checks that need no GPU: every declared entry point is
+exported by the CUDA library and mirrored by the oracle, and the library
+fails loudly (WF_ERR_CUDA) when no device is present."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import __graft_entry__ as ge
+import weldform_gb300 as wf
+
+HEADER = os.path.join(ge.ROOT, "include", "weldform_gb300.h")
+
+
+def declared():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(wf_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def cuda_lib_path():
+    p = wf.LIB_PATH
+    if not os.path.exists(p):
+        ge.build_cuda()
+    return p
+
+
+def test_header_declares_every_bound_entry_point():
+    names = declared()
+    for e in wf.EXPORTS:
+        assert "wf_" + e in names, e
+
+
+def test_library_exports_every_declared_symbol(cuda_lib_path):
+    lib = ctypes.CDLL(cuda_lib_path)
+    for name in declared():
+        assert hasattr(lib, name), name
+    wf.bind(lib, "wf_")
+
+
+def test_oracle_mirrors_the_abi():
+    from tests._support import oracle_lib
+    lib = oracle_lib()
+    for name in declared():
+        assert hasattr(lib, "wfo_" + name[3:]), name
+
+
+def test_no_device_is_a_loud_error(cuda_lib_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = wf.bind(ctypes.CDLL(cuda_lib_path), "wf_")
+    h = ctypes.c_void_p()
+    rc = lib.wf_domain_create(3, ctypes.byref(h))
+    assert rc == 2  # WF_ERR_CUDA
+    assert b"device" in lib.wf_last_error()
+    with pytest.raises(wf.WFError):
+        wf.Domain()

@@ -1,0 +1,164 @@
+"""GPU (sm_103a) kick-drift path against the CPU oracle, through the C ABI.
+
+Bar: neighbour lists bit-exact (same sets, same canonical row order);
+floating-point state within 1e-9 relative L2 (the plain FP64 form's
+tolerance), after the stated number of steps.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests._support import gpu_domain, oracle_domain, rel_l2
+from weldform_gb300 import configs, JOHNSON_COOK
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9
+THREADS = os.cpu_count() or 1
+
+
+def _pair(build, steps, fields, scalars=(), **kw):
+    out = {}
+    for name in ("gpu", "oracle"):
+        d = gpu_domain() if name == "gpu" else oracle_domain()
+        if name == "oracle":
+            d.set("cpu_threads", THREADS)
+        case = build(d, **kw)
+        d.prepare(case.dt)
+        d.step(steps)
+        out[name] = {f: d.get_array(f) for f in fields}
+        for s in scalars:
+            out[name][s] = d.get(s)
+        out[name]["searches"] = d.geti("nb_searches")
+        out[name]["nbr"] = d.neighbours()
+        if case.mesh is not None:
+            out[name]["cf"] = d.contact_force(case.mesh)
+            out[name]["cp"] = d.contact_pairs()
+        d.close()
+    return out["gpu"], out["oracle"]
+
+
+def _check(g, o, fields, scalars=(), tol=TOL):
+    for f in fields:
+        e = rel_l2(g[f], o[f])
+        assert e <= tol, f"{f}: relative L2 {e:.3e}"
+    for s in scalars:
+        e = abs(g[s] - o[s]) / max(abs(o[s]), 1e-300)
+        assert e <= 1e-8, f"{s}: {g[s]!r} vs {o[s]!r}"
+    assert g["searches"] == o["searches"]
+    assert np.array_equal(g["nbr"][0], o["nbr"][0]) and np.array_equal(g["nbr"][1], o["nbr"][1])
+
+
+def test_neighbour_search_bit_exact_cylinder():
+    res = {}
+    for name in ("gpu", "oracle"):
+        d = gpu_domain() if name == "gpu" else oracle_domain()
+        case = configs.cylinder_upsetting(d, R=0.004, L=0.010, dx=0.0004)
+        d.prepare(case.dt)
+        d.neighbour_search()
+        res[name] = (d.neighbours(), d.get_array("Nb"))
+    (go, gi), gnb = res["gpu"]
+    (oo, oi), onb = res["oracle"]
+    assert np.array_equal(go, oo)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gnb, onb)
+
+
+def test_neighbour_search_reference_table():
+    """The 12,144-particle case of the reference's recorded table (particle 2000)."""
+    import json
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reduction_particle2000.json")))
+    c = g["case"]
+    d = gpu_domain()
+    d.Kernel_Set(0)
+    d.AddCylinderLength(1, c["V"], c["R"], c["Lz"], c["dx"] / 2.0, c["rho"], c["dx"] * c["hfac"], False)
+    d.set_f64("DomMax.x", c["DomMax.x"])
+    d.set_f64("DomMin.x", c["DomMin.x"])
+    d.set_particles("Cs", 1000.0)
+    d.prepare(1e-7)
+    d.neighbour_search()
+    off, idx = d.neighbours()
+    p = g["particle"]
+    assert list(idx[off[p]:off[p + 1]]) == sorted(g["j_greater"]) + sorted(g["j_smaller"])
+    o = oracle_domain()
+    o.Kernel_Set(0)
+    o.AddCylinderLength(1, c["V"], c["R"], c["Lz"], c["dx"] / 2.0, c["rho"], c["dx"] * c["hfac"], False)
+    o.set_f64("DomMax.x", c["DomMax.x"])
+    o.set_f64("DomMin.x", c["DomMin.x"])
+    o.prepare(1e-7)
+    o.neighbour_search()
+    oo, oi = o.neighbours()
+    assert np.array_equal(off, oo) and np.array_equal(idx, oi)
+
+
+@pytest.mark.parametrize("packing,random", [(1, False), (1, True), (0, False)])
+def test_neighbour_search_bit_exact_box(packing, random):
+    res = {}
+    for name in ("gpu", "oracle"):
+        d = gpu_domain() if name == "gpu" else oracle_domain()
+        d.Kernel_Set(0)
+        d.AddBoxLength(0, (0.0, 0.0, 0.0), 0.006, 0.005, 0.004, 0.00025, 7850.0, 0.0006, packing, 0, random, False)
+        d.set_particles("Cs", 4600.0)
+        d.prepare(1e-8)
+        d.neighbour_search()
+        res[name] = (d.get_array("x"), d.neighbours())
+    assert np.array_equal(res["gpu"][0], res["oracle"][0])
+    assert np.array_equal(res["gpu"][1][0], res["oracle"][1][0])
+    assert np.array_equal(res["gpu"][1][1], res["oracle"][1][1])
+
+
+FIELDS = ("x", "v", "Density", "Sigma", "ShearStress", "pl_strain", "Sigmay", "Strain", "Displacement")
+SCALARS = ("int_energy_sum",)
+
+
+def test_elastic_cylinder_steps():
+    g, o = _pair(configs.cylinder_upsetting, 60, FIELDS, SCALARS, R=0.005, L=0.010, dx=0.0005)
+    _check(g, o, FIELDS, SCALARS)
+
+
+def test_yielding_bilinear_with_rebuilds():
+    g, o = _pair(configs.cylinder_upsetting, 80, FIELDS + ("Strain_pl", "eff_strain_rate"), SCALARS,
+                 R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    assert o["pl_strain"].max() > 1e-3 and o["searches"] > 10
+    _check(g, o, FIELDS + ("Strain_pl", "eff_strain_rate"), SCALARS)
+
+
+def test_johnson_cook_thermal():
+    f = FIELDS + ("T", "dTdt", "q_plheat")
+    g, o = _pair(configs.cylinder_upsetting, 80, f, SCALARS + ("plastic_work",), R=0.004, L=0.008, dx=0.0005,
+                 v_top=-30.0, model=JOHNSON_COOK, thermal=True)
+    assert o["T"].max() > 300.0
+    _check(g, o, f, SCALARS + ("plastic_work",))
+
+
+@pytest.mark.parametrize("stiffness", ["wang", "area"])
+def test_rigid_plane_contact(stiffness):
+    f = FIELDS + ("contforce", "T")
+    g, o = _pair(configs.contact_upsetting, 60, f, ("int_energy_sum", "contact_force_sum", "ext_forces_work"),
+                 R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, stiffness=stiffness, gap=-0.3 * 0.00036)
+    assert np.array_equal(g["cp"][0], o["cp"][0]) and np.array_equal(g["cp"][1], o["cp"][1])
+    assert len(o["cp"][1]) > 0
+    assert np.linalg.norm(o["cf"]) > 0
+    assert rel_l2(g["cf"], o["cf"]) <= 1e-8
+    _check(g, o, f, ("int_energy_sum", "contact_force_sum", "ext_forces_work"))
+
+
+def test_solve_loop_matches_reference_loop_control():
+    res = {}
+    for name in ("gpu", "oracle"):
+        d = gpu_domain() if name == "gpu" else oracle_domain()
+        case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005)
+        d.SolveDiffUpdateKickDrift(25 * case.dt, case.dt, 5 * case.dt)
+        res[name] = (d.geti("steps"), d.Time, d.get_array("x"))
+    assert res["gpu"][0] == res["oracle"][0]
+    assert res["gpu"][1] == res["oracle"][1]
+    assert rel_l2(res["gpu"][2], res["oracle"][2]) <= TOL
+
+
+@pytest.mark.slow
+def test_config1_full_1000_steps():
+    """8,004-particle elastic cylinder, 1000 steps (the small plain-FP64 case)."""
+    g, o = _pair(configs.cylinder_upsetting, 1000, FIELDS, SCALARS)
+    assert g["x"].shape[0] == 8004
+    _check(g, o, FIELDS, SCALARS)

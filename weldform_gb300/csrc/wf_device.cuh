@@ -1,0 +1,163 @@
+// Device-side data layout of the GB300 kick-drift SPH step (host + device).
+//
+// Particle state lives in one structure-of-arrays arena in HBM, one column of
+// N values per scalar component, in cell-sorted order.  The host keeps the map
+// between this order and the reference's particle order ("original index").
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wf {
+
+// ---- double columns -------------------------------------------------------
+// Symmetric tensors are stored as 6 components in the order xx yy zz xy xz yz;
+// the reference stores full 3x3 matrices whose off-diagonal pairs agree to the
+// last bit except for rounding-order asymmetries of the Jaumann update.
+enum F64Col : int {
+  C_X = 0,                 // position (3)
+  C_V = 3,                 // velocity (3)
+  C_RHO = 6,               // Density
+  C_A = 7,                 // acceleration (3)
+  C_DISP = 10,             // Displacement (3)
+  C_MASS = 13, C_RHO0, C_H, C_CS, C_P0, C_G, C_P,
+  C_SIG = 20,              // Sigma (6)
+  C_TAU = 26,              // ShearStress (6)
+  C_EPS = 32,              // Strain (6)
+  C_EPL = 38,              // Strain_pl (6)
+  C_EPLI = 44,             // Strain_pl_incr (6)
+  C_SR = 50,               // StrainRate (6)
+  C_PLS = 56, C_DPLS, C_SY, C_EP, C_ESR, C_T, C_DTDT, C_KT, C_CPT, C_THEXP, C_QPL, C_QSRC, C_ALPHA, C_BETA, C_PSEN,
+  C_NORMAL = 71,           // normal (3)
+  C_CF = 74,               // contforce (3)
+  C_DCONT = 77,
+  C_DKIN = 78, C_DINT = 79, C_DRHO = 80,
+  C_RR = 81,               // RotationRate, antisymmetric part (xy xz yz)
+  C_SRHO = 84,             // Sigma / Density^2 (6), for the acceleration pair term
+  C_MRHO = 90,             // Mass / Density
+  C_PR2 = 91,              // Pressure / Density^2
+  NF64_PERSIST = 92,
+  // scratch columns (not permuted): next-step buffers
+  C_XN = 92, C_VN = 95, C_RHON = 98, C_MRHON = 99,
+  NF64 = 100
+};
+enum I32Col : int {
+  I_ID = 0, I_IDORIG, I_NWS, I_MAT, I_MODEL, I_FAIL, I_MATERIAL, I_NB, I_KIND, I_ELEM, I_MESH, I_ORIG,
+  NI32_PERSIST = 12,
+  I_CELL = 12,             // scratch: cell key
+  NI32 = 13
+};
+
+struct MaterialDev {
+  int model;
+  double E;
+  double K, m, eps0, eps1, sy0;                         // Hollomon
+  double A, B, C, n, jm, eps_0, T_m, T_t;               // Johnson-Cook
+};
+struct BCDev {
+  int zone, value_type, amp_id;
+  double value[3], value_ang[3];
+  double amp_factor;
+};
+struct AmpDev {
+  int id, n, offset;  // points [offset, offset+n) of the amplitude tables
+};
+
+constexpr int MAX_MATERIALS = 16;
+constexpr int MAX_BCS = 32;
+constexpr int MAX_AMPS = 16;
+constexpr int MAX_AMP_POINTS = 512;
+constexpr int MAX_MESHES = 8;
+constexpr int MAX_NB = 100;  // MAX_NB_PER_PART, Source/Domain.h:49
+constexpr int MAX_CP = 64;   // contact pairs per particle
+
+// Tables that are read by a few threads only; kept in device memory.
+struct DomainTables {
+  MaterialDev mat[MAX_MATERIALS];
+  BCDev bc[MAX_BCS];
+  AmpDev amp[MAX_AMPS];
+  double amp_t[MAX_AMP_POINTS], amp_v[MAX_AMP_POINTS];
+  int nmat, nbc, namp;
+};
+
+// Error bits raised by kernels (read by the host at synchronisation points).
+constexpr int ERR_NBR_OVERFLOW = 1;
+constexpr int ERR_NAN = 2;
+constexpr int ERR_TIMEOUT = 4;
+constexpr int ERR_CONTACT_OVERFLOW = 8;
+constexpr int ERR_NO_SURFACE = 16;
+
+// Reduction slots (per-block partials, deterministic tree order).
+enum Slot : int {
+  S_DINT = 0, S_DKIN, S_PLW, S_MAXPL, S_MAXT, S_MINT, S_CFSUM, S_CRSUM, S_EXTW,
+  S_CFVEC = 9,  // 3 per mesh
+  NSLOTS = 9 + 3 * MAX_MESHES
+};
+
+// Scalars that evolve on the device, so a whole step runs without a host sync.
+struct StepState {
+  double Time, deltat;
+  double int_energy_sum, kin_energy_sum, plastic_work, contact_force_sum, contact_reaction_sum, ext_forces_work;
+  double max_pl;       // max pl_strain at the start of the current step
+  double max_pl_next;  // max pl_strain after the current step's stress update
+  double m_maxT, m_minT;
+  double mesh_v[MAX_MESHES][3];         // TriMesh::m_v set by the velocity BCs
+  double mesh_w[MAX_MESHES][3];         // TriMesh::m_w
+  double contact_force[MAX_MESHES][3];  // Domain::m_contact_force
+  long long steps, nb_searches;
+  unsigned long long pair_count, contact_pair_count;
+  int isfirst, isyielding, ts_i, nb_cleared;
+  int do_search;       // set by the schedule kernel for the current step
+  int errors;
+  int surface_count;
+};
+
+// Per-domain constants (set once at the solver prologue; small, by value).
+struct DomainConst {
+  int N, Nsolid, nbc_particles;
+  double Cellfac, hmax, dt;
+  double BLPF[3], CellSize[3];
+  int CellNo[3];
+  int ncells;
+  float pre_eps;       // relative margin of the FP32 neighbour prefilter
+  int ts_nb_inc, pl_heating, thermal_solver, contact, contact_mesh_auto_update, contact_alg;
+  double pl_work_heat_frac, friction_sta, friction_dyn, PFAC, DFAC;
+  double totmass_mean;
+  int id_free_surf;
+  int nmeshes;
+  int contact_surf_id[MAX_MESHES];
+  int nblocks;         // blocks of the per-particle kernels (partials stride)
+};
+
+// Device pointers, passed by value to every kernel.
+struct DevPtrs {
+  double* f;         // F64 arena: column c at f + c * N
+  int* i;            // I32 arena
+  StepState* st;
+  const DomainTables* tab;
+  const int* cell_rank;   // linear cell -> Morton rank
+  int* cell_start;        // ncells + 1
+  int* cell_count;        // ncells (histogram / cursor)
+  int* perm;              // new sorted position -> old sorted position
+  int* inv;               // original index -> sorted position
+  float* xs;              // FP32 prefilter coordinates (x - BLPF, 3 columns) and h
+  int* row_len;           // neighbours per particle
+  int* row_split;         // neighbours with larger original index (row prefix)
+  int* nbr;               // ELL: entry k of particle i at k * N + i
+  int* cp_len;            // contact pairs per particle
+  int* cp;                // ELL, width MAX_CP
+  const int* bc_list;     // original indices of particles carrying a BC zone id
+  // rigid meshes
+  double* node;           // 3 * nnodes (SoA: x[nnodes], y, z)
+  double* node_v;
+  const int* elem_node;   // 3 * nelem
+  double* elem_normal;    // 3 * nelem
+  double* elem_pplane;    // nelem
+  const int* elem_mesh;   // nelem
+  int* elem_particle;     // nelem -> sorted particle index
+  const int* node_mesh;   // nnodes
+  int nnodes, nelem;
+  double* partials;       // NSLOTS * nblocks
+  long long* scan_tmp;
+};
+
+}  // namespace wf

@@ -1,0 +1,1163 @@
+// Host side of the GB300 kick-drift SPH library: the SPH::Domain façade
+// (Source/Domain.h:113-537) over the C ABI declared in include/weldform_gb300.h.
+//
+// Before the solver prologue the domain is a host-side particle set in the
+// reference's insertion order (generators, zones, per-particle fields).  The
+// prologue uploads it into the device arena, builds the cell grid
+// (CellInitiate, Neighbour.cpp:10-139) and from then on all state lives in
+// HBM in cell-sorted order; host transfers map through the original index.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/weldform_gb300.h"
+#include "wf_device.cuh"
+#include "wf_launch.h"
+
+namespace {
+
+thread_local std::string g_err;
+int set_err(int code, const std::string& m) { g_err = m; return code; }
+
+struct CudaError { int code; std::string msg; };
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) throw CudaError{WF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+
+const double PI = 3.14159265358979323846;
+
+struct Vec { double c[3]; };
+inline Vec vec(double a, double b, double c) { return Vec{{a, b, c}}; }
+
+struct HostMaterial { int model; std::vector<double> p; wf::MaterialDev dev; };
+struct HostAmp { int id; std::vector<double> t, v; };
+struct HostBC { int zone; double value[3], ang[3]; int vt, amp; double fac; };
+struct HostMesh {
+  std::vector<Vec> node;
+  std::vector<int> en;          // 3 per element
+  std::vector<Vec> centroid, normal;
+  std::vector<double> pplane, radius;
+  int id = 0, first = 0;
+  Vec mv = vec(0, 0, 0), mw = vec(0, 0, 0);
+};
+
+// Particle field table: name -> host vector (original order).
+struct HostParticles {
+  std::vector<double> f[wf::NF64_PERSIST];
+  std::vector<int> i[wf::NI32_PERSIST];
+  int N = 0;
+};
+
+int col_f64(const std::string& n, int* ncomp) {
+  using namespace wf;
+  struct E { const char* n; int c, k; };
+  static const E tab[] = {
+      {"x", C_X, 3}, {"v", C_V, 3}, {"a", C_A, 3}, {"Displacement", C_DISP, 3}, {"normal", C_NORMAL, 3},
+      {"contforce", C_CF, 3}, {"Density", C_RHO, 1}, {"RefDensity", C_RHO0, 1}, {"Mass", C_MASS, 1}, {"h", C_H, 1},
+      {"Cs", C_CS, 1}, {"P0", C_P0, 1}, {"G", C_G, 1}, {"Pressure", C_P, 1}, {"pl_strain", C_PLS, 1},
+      {"delta_pl_strain", C_DPLS, 1}, {"Sigmay", C_SY, 1}, {"Ep", C_EP, 1}, {"eff_strain_rate", C_ESR, 1},
+      {"T", C_T, 1}, {"dTdt", C_DTDT, 1}, {"k_T", C_KT, 1}, {"cp_T", C_CPT, 1}, {"th_exp", C_THEXP, 1},
+      {"q_plheat", C_QPL, 1}, {"q_source", C_QSRC, 1}, {"Alpha", C_ALPHA, 1}, {"Beta", C_BETA, 1},
+      {"ps_energy", C_PSEN, 1}, {"delta_cont", C_DCONT, 1}, {"dkin_energy_dt", C_DKIN, 1},
+      {"dint_energy_dt", C_DINT, 1}, {"dDensity", C_DRHO, 1}, {"Sigma", C_SIG, 6}, {"ShearStress", C_TAU, 6},
+      {"Strain", C_EPS, 6}, {"Strain_pl", C_EPL, 6}, {"Strain_pl_incr", C_EPLI, 6}, {"StrainRate", C_SR, 6},
+      {"RotationRate", C_RR, 3}};
+  for (const E& e : tab)
+    if (n == e.n) { *ncomp = e.k; return e.c; }
+  return -1;
+}
+int col_i32(const std::string& n) {
+  using namespace wf;
+  if (n == "ID") return I_ID;
+  if (n == "mat") return I_MAT;
+  if (n == "Material_model") return I_MODEL;
+  if (n == "Fail") return I_FAIL;
+  if (n == "Material") return I_MATERIAL;
+  if (n == "Nb") return I_NB;
+  return -1;
+}
+// Fields that exist in the reference but are fixed in this build's scope.
+bool fixed_i32(const std::string& n, int v, std::string* why) {
+  if (n == "PresEq") { if (v != 0) { *why = "only PresEq = 0 is supported"; return false; } return true; }
+  if (n == "IsFree") { if (v != 1) { *why = "fixed (non-free) particles are not supported"; return false; } return true; }
+  if (n == "print_history") return true;
+  *why = "unknown particle i32 field " + n;
+  return false;
+}
+
+// Morton code of a cell (10 bits per axis, interleaved).
+uint64_t spread3(uint64_t v) {
+  v &= 0x1fffff;
+  v = (v | v << 32) & 0x1f00000000ffffULL;
+  v = (v | v << 16) & 0x1f0000ff0000ffULL;
+  v = (v | v << 8) & 0x100f00f00f00f00fULL;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+  v = (v | v << 2) & 0x1249249249249249ULL;
+  return v;
+}
+
+}  // namespace
+
+struct wf_domain {
+  int dim = 3;
+  // Domain defaults (Source/Domain.cpp:78-175)
+  double Cellfac = 2.0, pl_work_heat_frac = 0.9, friction_sta = 0.0, friction_dyn = 0.0, PFAC = 0.0, DFAC = 0.0;
+  double DomMax[3] = {-100000000000.0, -100000000000.0, -100000000000.0};
+  double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
+  int ts_nb_inc = 5, pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1, contact_alg = 0;
+  int precision = WF_PRECISION_FP64, use_graph = 1, device = 0;
+  int solid_part_count = -1;
+
+  HostParticles hp;
+  std::vector<HostMaterial> mats;
+  std::vector<HostAmp> amps;
+  std::vector<HostBC> bcs;
+  std::vector<HostMesh> meshes;
+
+  // device
+  bool prepared = false;
+  cudaStream_t stream = nullptr;
+  wf::DevPtrs P{};
+  wf::DomainConst K{};
+  double* d_f = nullptr;
+  int* d_i = nullptr;
+  double* d_fscratch = nullptr;
+  int* d_iscratch = nullptr;
+  std::vector<void*> allocs;
+  cudaGraphExec_t graph = nullptr;
+  int graph_precision = -1;
+  long long launches_per_step = 0;
+  double hmax = 0;
+  double BLPF[3] = {0, 0, 0}, TRPR[3] = {0, 0, 0};
+  int CellNo[3] = {0, 0, 0};
+
+  ~wf_domain() { release(); }
+  void release() {
+    if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
+    prepared = false;
+  }
+  template <class T> T* dalloc(size_t n) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) throw CudaError{WF_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    allocs.push_back(p);
+    return (T*)p;
+  }
+
+  // ------------------------------------------------------------ particles
+  void push(int tag, Vec x, double m0, double dens, double h, int kind) {
+    using namespace wf;
+    for (int c = 0; c < NF64_PERSIST; ++c) hp.f[c].push_back(0.0);
+    for (int c = 0; c < NI32_PERSIST; ++c) hp.i[c].push_back(0);
+    int p = hp.N++;
+    for (int d = 0; d < 3; ++d) hp.f[C_X + d][p] = x.c[d];
+    hp.f[C_RHO][p] = dens; hp.f[C_RHO0][p] = dens; hp.f[C_MASS][p] = m0; hp.f[C_H][p] = h;
+    hp.i[I_ID][p] = tag; hp.i[I_IDORIG][p] = tag; hp.i[I_MAT][p] = -1; hp.i[I_KIND][p] = kind;
+    hp.i[I_ELEM][p] = -1; hp.i[I_MESH][p] = -1; hp.i[I_ORIG][p] = p;
+  }
+  double& F(int c, int p) { return hp.f[c][p]; }
+
+  // Domain::AddCylinderLength, Source/Domain.cpp:708-860 (3D, no ghost rows).
+  static int half_part_count(double r, double R, int xinc) {  // calcHalfPartCount, Domain.cpp:674-689
+    int count = -1;
+    if (xinc > 0) {
+      count = 1;
+      double yp = r;
+      double xp = r + (double)(xinc - 1) * 2. * r;
+      double rad = std::sqrt(yp * yp + xp * xp);
+      while (rad <= R - r) {
+        yp += 2. * r;
+        rad = std::sqrt(yp * yp + xp * xp);
+        count++;
+      }
+      count -= 1;
+    }
+    return count;
+  }
+  void add_cylinder(int tag, const double V[3], double Rxy, double Lz, double r, double dens, double h) {
+    int nxy = half_part_count(r, Rxy, 1);
+    for (double zp = V[2] + r; zp <= (V[2] + Lz - r); zp += 2. * r) {
+      double yp = V[1] - r - (2. * r * (nxy - 1));
+      int yinc = nxy, ysign = -1;
+      for (int j = 0; j < 2 * nxy; j++) {
+        int nx = half_part_count(r, Rxy, yinc);
+        double xp = V[0] - r - (2. * r * (nx - 1));
+        for (int i = 0; i < 2 * nx; i++) {
+          push(tag, vec(xp, yp, zp), 0.0, dens, h, 0);
+          xp += 2. * r;
+        }
+        yp += 2. * r;
+        yinc += ysign;
+        if (yinc < 1) { yinc = 1; ysign = 1; }
+      }
+    }
+    solid_part_count = hp.N;
+    double Mass = PI * Rxy * Rxy * Lz * dens / hp.N;
+    for (int p = 0; p < hp.N; ++p) F(wf::C_MASS, p) = Mass;
+  }
+  // Domain::AddBoxLength, Source/Domain.cpp:326-599 (3D packings).
+  void add_box(int tag, const double V[3], double Lx, double Ly, double Lz, double r, double dens, double h, int type,
+               bool random) {
+    int first = hp.N;
+    const double qin = 0.03;
+    srand(100);
+    auto emit = [&](double x, double y, double z) {
+      if (random) {
+        double a = qin * r * double(rand()) / RAND_MAX;
+        double b = qin * r * double(rand()) / RAND_MAX;
+        double c = qin * r * double(rand()) / RAND_MAX;
+        push(tag, vec(x + a, y + b, z + c), 0.0, dens, h, 0);
+      } else {
+        push(tag, vec(x, y, z), 0.0, dens, h, 0);
+      }
+    };
+    if (type == 0) {  // hexagonal close packing
+      size_t k = 0;
+      double zp = V[2];
+      while (zp <= (V[2] + Lz - r)) {
+        size_t j = 0;
+        double yp = V[1];
+        while (yp <= (V[1] + Ly - r)) {
+          size_t i = 0;
+          double xp = V[0];
+          while (xp <= (V[0] + Lx - r)) {
+            double x;
+            if ((k % 2 != 0) && (j % 2 != 0)) x = V[0] + (2 * i + (j % 2) + (k % 2) - 1) * r;
+            else x = V[0] + (2 * i + (j % 2) + (k % 2) + 1) * r;
+            double y = V[1] + (std::sqrt(3.0) * (j + (1.0 / 3.0) * (k % 2)) + 1) * r;
+            double z = V[2] + ((2 * std::sqrt(6.0) / 3) * k + 1) * r;
+            emit(x, y, z);
+            i++;
+            if ((k % 2 != 0) && (j % 2 != 0)) xp = V[0] + (2 * i + (j % 2) + (k % 2) - 1) * r;
+            else xp = V[0] + (2 * i + (j % 2) + (k % 2) + 1) * r;
+          }
+          j++;
+          yp = V[1] + (std::sqrt(3.0) * (j + (1.0 / 3.0) * (k % 2)) + 1) * r;
+        }
+        k++;
+        zp = V[2] + ((2 * std::sqrt(6.0) / 3) * k + 1) * r;
+      }
+    } else {  // cubic packing
+      size_t k = 0;
+      double zp = V[2];
+      while (zp <= (V[2] + Lz - r)) {
+        size_t j = 0;
+        double yp = V[1];
+        while (yp <= (V[1] + Ly - r)) {
+          size_t i = 0;
+          double xp = V[0];
+          while (xp <= (V[0] + Lx - r)) {
+            emit(V[0] + (2.0 * i + 1) * r, V[1] + (2.0 * j + 1) * r, V[2] + (2.0 * k + 1) * r);
+            i++;
+            xp = V[0] + (2 * i + 1) * r;
+          }
+          j++;
+          yp = V[1] + (2.0 * j + 1) * r;
+        }
+        k++;
+        zp = V[2] + (2.0 * k + 1) * r;
+      }
+    }
+    double mx[3] = {V[0], V[1], V[2]};
+    for (int p = first; p < hp.N; ++p)
+      for (int d = 0; d < 3; ++d) mx[d] = std::max(mx[d], F(wf::C_X + d, p));
+    double t[3];
+    for (int d = 0; d < 3; ++d) t[d] = (mx[d] + r) - V[d];
+    double Mass = t[0] * t[1] * t[2] * dens / (hp.N - first);
+    for (int p = 0; p < hp.N; ++p) F(wf::C_MASS, p) = Mass;  // every particle, as Domain.cpp:461-469
+    solid_part_count = hp.N;
+  }
+  // TriMesh::AxisPlaneMesh (Mesh.cpp:82-203), CalcSpheres (:206-220) and
+  // Domain::AddTrimeshParticles (Contact.cpp:10-38).
+  int add_plane(int axis, bool posit, const double p1[3], const double p2[3], int dens, double hfac, int zone) {
+    HostMesh M;
+    int dir[3];
+    if (axis == 0) { dir[0] = 1; dir[1] = 2; } else if (axis == 1) { dir[0] = 0; dir[1] = 2; } else { dir[0] = 0; dir[1] = 1; }
+    dir[2] = axis;
+    double dl = (p2[dir[0]] - p1[dir[0]]) / dens;
+    double x2 = p1[dir[1]];
+    for (int j = 0; j < dens + 1; j++) {
+      double x1 = p1[dir[0]];
+      for (int i = 0; i < dens + 1; i++) {
+        Vec q; q.c[dir[0]] = x1; q.c[dir[1]] = x2; q.c[dir[2]] = p1[dir[2]];
+        M.node.push_back(q);
+        x1 += dl;
+      }
+      x2 += dl;
+    }
+    for (int j = 0; j < dens; j++)
+      for (int i = 0; i < dens; i++) {
+        int n0 = (dens + 1) * j + i, n1 = n0 + 1, n2 = (dens + 1) * (j + 1) + i, n3 = n2 + 1;
+        int tri[2][3] = {{n0, n1, n2}, {n1, n3, n2}};
+        if (!posit) { tri[0][1] = n2; tri[0][2] = n1; tri[1][0] = n1; tri[1][1] = n2; tri[1][2] = n3; }
+        for (int e = 0; e < 2; ++e) {
+          for (int k = 0; k < 3; ++k) M.en.push_back(tri[e][k]);
+          Vec s;
+          for (int d = 0; d < 3; ++d) s.c[d] = (M.node[tri[e][0]].c[d] + M.node[tri[e][1]].c[d] + M.node[tri[e][2]].c[d]) / 3.;
+          M.centroid.push_back(s);
+        }
+      }
+    int ne = (int)M.centroid.size();
+    for (int e = 0; e < ne; ++e) {  // CalcNormals
+      const Vec& a = M.node[M.en[3 * e]]; const Vec& b = M.node[M.en[3 * e + 1]]; const Vec& c = M.node[M.en[3 * e + 2]];
+      double u[3], w[3];
+      for (int d = 0; d < 3; ++d) { u[d] = b.c[d] - a.c[d]; w[d] = c.c[d] - a.c[d]; }
+      double cr[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+      double ln = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+      Vec n = vec(cr[0] / ln, cr[1] / ln, cr[2] / ln);
+      if (posit) n = vec(-n.c[0], -n.c[1], -n.c[2]);
+      M.normal.push_back(n);
+    }
+    for (int e = 0; e < ne; ++e) {  // CalcSpheres: radius = farthest node; plane through the last node
+      double mx = 0.;
+      for (int k = 0; k < 3; ++k) {
+        const Vec& q = M.node[M.en[3 * e + k]];
+        double r2[3] = {q.c[0] - M.centroid[e].c[0], q.c[1] - M.centroid[e].c[1], q.c[2] - M.centroid[e].c[2]};
+        double nr = std::sqrt(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+        if (nr > mx) mx = nr;
+      }
+      M.radius.push_back(mx);
+      const Vec& q = M.node[M.en[3 * e + 2]];
+      M.pplane.push_back(q.c[0] * M.normal[e].c[0] + q.c[1] * M.normal[e].c[1] + q.c[2] * M.normal[e].c[2]);
+    }
+    M.id = zone;
+    M.first = hp.N;
+    int mi = (int)meshes.size();
+    int ebase = 0;
+    for (auto& m : meshes) ebase += (int)m.centroid.size();
+    for (int e = 0; e < ne; ++e) {
+      double h = (double)(float)hfac * M.radius[e];  // hfac is a float parameter (Contact.cpp:10)
+      push(zone, M.centroid[e], 0.0, 0.0, h, 1);
+      int p = hp.N - 1;
+      for (int d = 0; d < 3; ++d) F(wf::C_NORMAL + d, p) = M.normal[e].c[d];
+      hp.i[wf::I_ELEM][p] = ebase + e;
+      hp.i[wf::I_MESH][p] = mi;
+    }
+    meshes.push_back(M);
+    return mi;
+  }
+
+  // ------------------------------------------------------------ prologue
+  void prepare(double dt) {
+    using namespace wf;
+    int N = hp.N;
+    if (N == 0) throw CudaError{WF_ERR_STATE, "no particles"};
+    if (!meshes.empty() && !contact) throw CudaError{WF_ERR_ARG, "rigid meshes need contact = 1"};
+    if ((int)meshes.size() > MAX_MESHES) throw CudaError{WF_ERR_UNSUPPORTED, "too many rigid meshes"};
+    if (solid_part_count < 0) solid_part_count = N;
+    for (int p = 0; p < N; ++p) {
+      if (hp.i[I_KIND][p] == 0 && p >= solid_part_count)
+        throw CudaError{WF_ERR_UNSUPPORTED, "solid particles must precede rigid-mesh particles"};
+    }
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    // CellInitiate (Neighbour.cpp:10-139): bbox of all particles, hmax, pad, cell counts.
+    for (int d = 0; d < 3; ++d) { BLPF[d] = F(C_X + d, 0); TRPR[d] = F(C_X + d, 0); }
+    hmax = F(C_H, 0);
+    double hmin = F(C_H, 0);
+    for (int p = 0; p < N; ++p) {
+      for (int d = 0; d < 3; ++d) {
+        if (F(C_X + d, p) > TRPR[d]) TRPR[d] = F(C_X + d, p);
+        if (F(C_X + d, p) < BLPF[d]) BLPF[d] = F(C_X + d, p);
+      }
+      if (F(C_H, p) > hmax) hmax = F(C_H, p);
+      if (F(C_H, p) < hmin) hmin = F(C_H, p);
+    }
+    for (int d = 0; d < 3; ++d) {
+      if (DomMax[d] > TRPR[d]) TRPR[d] = DomMax[d];
+      if (DomMin[d] < BLPF[d]) BLPF[d] = DomMin[d];
+    }
+    for (int d = 0; d < 3; ++d) { TRPR[d] += hmax / 2; BLPF[d] -= hmax / 2; }
+    double cs[3];
+    long long ncells = 1;
+    for (int d = 0; d < 3; ++d) {
+      double t = (TRPR[d] - BLPF[d]) / (Cellfac * hmax);
+      CellNo[d] = (double(std::ceil(t) - t) < (hmax / 10.0)) ? int(std::ceil(t)) : int(std::floor(t));
+      if (CellNo[d] <= 0) throw CudaError{WF_ERR_ARG, "CellInitiate: domain extent smaller than one cell"};
+      cs[d] = (TRPR[d] - BLPF[d]) / CellNo[d];
+      ncells *= CellNo[d];
+    }
+    if (ncells > (1LL << 30)) throw CudaError{WF_ERR_UNSUPPORTED, "cell grid too large"};
+    // Morton rank of each cell (linear index (i * ny + j) * nz + k).
+    std::vector<std::pair<uint64_t, int>> mc((size_t)ncells);
+    for (int a = 0; a < CellNo[0]; ++a)
+      for (int b = 0; b < CellNo[1]; ++b)
+        for (int c = 0; c < CellNo[2]; ++c) {
+          int lin = (a * CellNo[1] + b) * CellNo[2] + c;
+          mc[lin] = {spread3(a) | (spread3(b) << 1) | (spread3(c) << 2), lin};
+        }
+    std::sort(mc.begin(), mc.end());
+    std::vector<int> rank((size_t)ncells);
+    for (long long r = 0; r < ncells; ++r) rank[mc[r].second] = (int)r;
+
+    // Device allocations.
+    size_t n = N;
+    d_f = dalloc<double>((size_t)NF64 * n);
+    d_i = dalloc<int>((size_t)NI32 * n);
+    d_fscratch = dalloc<double>((size_t)NF64_PERSIST * n);
+    d_iscratch = dalloc<int>((size_t)NI32_PERSIST * n);
+    CK(cudaMemsetAsync(d_f, 0, sizeof(double) * NF64 * n, stream));
+    CK(cudaMemsetAsync(d_i, 0, sizeof(int) * NI32 * n, stream));
+    for (int c = 0; c < NF64_PERSIST; ++c)
+      CK(cudaMemcpyAsync(d_f + (size_t)c * n, hp.f[c].data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream));
+    for (int c = 0; c < NI32_PERSIST; ++c)
+      CK(cudaMemcpyAsync(d_i + (size_t)c * n, hp.i[c].data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream));
+    P.f = d_f; P.i = d_i;
+    P.st = dalloc<StepState>(1);
+    DomainTables* tab = dalloc<DomainTables>(1);
+    P.tab = tab;
+    int* crank = dalloc<int>(ncells);
+    CK(cudaMemcpyAsync(crank, rank.data(), sizeof(int) * ncells, cudaMemcpyHostToDevice, stream));
+    P.cell_rank = crank;
+    P.cell_start = dalloc<int>(ncells + 1);
+    P.cell_count = dalloc<int>(ncells);
+    P.perm = dalloc<int>(n);
+    P.inv = dalloc<int>(n);
+    P.xs = dalloc<float>(4 * n);
+    P.row_len = dalloc<int>(n);
+    P.row_split = dalloc<int>(n);
+    P.nbr = dalloc<int>((size_t)MAX_NB * n);
+    CK(cudaMemsetAsync(P.row_len, 0, sizeof(int) * n, stream));
+    CK(cudaMemsetAsync(P.row_split, 0, sizeof(int) * n, stream));
+    P.cp_len = dalloc<int>(n);
+    CK(cudaMemsetAsync(P.cp_len, 0, sizeof(int) * n, stream));
+    P.cp = contact ? dalloc<int>((size_t)MAX_CP * n) : dalloc<int>(1);
+    std::vector<int> inv0(n);
+    std::iota(inv0.begin(), inv0.end(), 0);
+    CK(cudaMemcpyAsync(P.inv, inv0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream));
+    // Tables.
+    DomainTables ht;
+    memset(&ht, 0, sizeof(ht));
+    ht.nmat = (int)mats.size();
+    for (size_t m = 0; m < mats.size(); ++m) ht.mat[m] = mats[m].dev;
+    ht.nbc = (int)bcs.size();
+    for (size_t b = 0; b < bcs.size(); ++b) {
+      BCDev& B = ht.bc[b];
+      B.zone = bcs[b].zone; B.value_type = bcs[b].vt; B.amp_id = bcs[b].amp; B.amp_factor = bcs[b].fac;
+      for (int d = 0; d < 3; ++d) { B.value[d] = bcs[b].value[d]; B.value_ang[d] = bcs[b].ang[d]; }
+    }
+    ht.namp = (int)amps.size();
+    int off = 0;
+    for (size_t a = 0; a < amps.size(); ++a) {
+      ht.amp[a].id = amps[a].id; ht.amp[a].n = (int)amps[a].t.size(); ht.amp[a].offset = off;
+      for (size_t k = 0; k < amps[a].t.size(); ++k) { ht.amp_t[off + k] = amps[a].t[k]; ht.amp_v[off + k] = amps[a].v[k]; }
+      off += (int)amps[a].t.size();
+    }
+    CK(cudaMemcpyAsync(tab, &ht, sizeof(ht), cudaMemcpyHostToDevice, stream));
+    // BC particle list (original indices).
+    std::vector<int> bl;
+    bool any_surface_bc = false;
+    for (auto& b : bcs) if (b.zone == 1) any_surface_bc = true;
+    for (int p = 0; p < N; ++p) {
+      bool hit = any_surface_bc && hp.i[I_KIND][p] == 0;
+      for (auto& b : bcs) if (hp.i[I_ID][p] == b.zone) hit = true;
+      if (hit) bl.push_back(p);
+    }
+    int* dbl = dalloc<int>(bl.size());
+    if (!bl.empty()) CK(cudaMemcpyAsync(dbl, bl.data(), sizeof(int) * bl.size(), cudaMemcpyHostToDevice, stream));
+    P.bc_list = dbl;
+    // Rigid meshes.
+    int nn = 0, ne = 0;
+    for (auto& m : meshes) { nn += (int)m.node.size(); ne += (int)m.centroid.size(); }
+    P.nnodes = nn; P.nelem = ne;
+    std::vector<double> hnode(3 * (size_t)std::max(nn, 1), 0.0), hnorm(3 * (size_t)std::max(ne, 1), 0.0),
+        hpp(std::max(ne, 1), 0.0);
+    std::vector<int> hen(3 * (size_t)std::max(ne, 1), 0), hem(std::max(ne, 1), 0), hnm(std::max(nn, 1), 0),
+        hep(std::max(ne, 1), 0);
+    int nb0 = 0, eb0 = 0;
+    for (size_t mi = 0; mi < meshes.size(); ++mi) {
+      auto& m = meshes[mi];
+      for (size_t k = 0; k < m.node.size(); ++k) {
+        for (int d = 0; d < 3; ++d) hnode[d * nn + nb0 + k] = m.node[k].c[d];
+        hnm[nb0 + k] = (int)mi;
+      }
+      for (size_t e = 0; e < m.centroid.size(); ++e) {
+        for (int k = 0; k < 3; ++k) hen[3 * (eb0 + e) + k] = nb0 + m.en[3 * e + k];
+        for (int d = 0; d < 3; ++d) hnorm[d * ne + eb0 + e] = m.normal[e].c[d];
+        hpp[eb0 + e] = m.pplane[e];
+        hem[eb0 + e] = (int)mi;
+        hep[eb0 + e] = m.first + (int)e;
+      }
+      nb0 += (int)m.node.size();
+      eb0 += (int)m.centroid.size();
+    }
+    P.node = dalloc<double>(hnode.size()); P.node_v = dalloc<double>(hnode.size());
+    int* den = dalloc<int>(hen.size()); P.elem_node = den;
+    P.elem_normal = dalloc<double>(hnorm.size()); P.elem_pplane = dalloc<double>(hpp.size());
+    int* dem = dalloc<int>(hem.size()); P.elem_mesh = dem;
+    P.elem_particle = dalloc<int>(hep.size());
+    int* dnm = dalloc<int>(hnm.size()); P.node_mesh = dnm;
+    CK(cudaMemcpyAsync(P.node, hnode.data(), sizeof(double) * hnode.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(P.node_v, 0, sizeof(double) * hnode.size(), stream));
+    CK(cudaMemcpyAsync(den, hen.data(), sizeof(int) * hen.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(P.elem_normal, hnorm.data(), sizeof(double) * hnorm.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(P.elem_pplane, hpp.data(), sizeof(double) * hpp.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(dem, hem.data(), sizeof(int) * hem.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(P.elem_particle, hep.data(), sizeof(int) * hep.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(dnm, hnm.data(), sizeof(int) * hnm.size(), cudaMemcpyHostToDevice, stream));
+    // Constants.
+    K.N = N; K.Nsolid = solid_part_count; K.nbc_particles = (int)bl.size();
+    K.Cellfac = Cellfac; K.hmax = hmax; K.dt = dt;
+    for (int d = 0; d < 3; ++d) { K.BLPF[d] = BLPF[d]; K.CellSize[d] = cs[d]; K.CellNo[d] = CellNo[d]; }
+    K.ncells = (int)ncells;
+    double ext = 0;
+    for (int d = 0; d < 3; ++d) ext = std::max(ext, TRPR[d] - BLPF[d]);
+    double R = Cellfac * hmin;
+    double eps = 4.0 * std::sqrt(3.0) * std::ldexp(1.0, -23) * (2.0 * ext) / R + 20.0 * std::ldexp(1.0, -24);
+    K.pre_eps = (float)(eps < 0.05 ? std::max(eps, 1e-5) : 2.0);
+    K.ts_nb_inc = ts_nb_inc; K.pl_heating = pl_heating; K.thermal_solver = thermal_solver; K.contact = contact;
+    K.contact_mesh_auto_update = contact_mesh_auto_update; K.contact_alg = contact_alg;
+    K.pl_work_heat_frac = pl_work_heat_frac; K.friction_sta = friction_sta; K.friction_dyn = friction_dyn;
+    K.PFAC = PFAC; K.DFAC = DFAC;
+    double tm = 0;
+    for (int p = 0; p < N; ++p) tm += F(C_MASS, p);
+    K.totmass_mean = tm / N;
+    K.id_free_surf = -999999;
+    K.nmeshes = (int)meshes.size();
+    for (size_t m = 0; m < meshes.size(); ++m) K.contact_surf_id[m] = meshes[m].id;
+    K.nblocks = (N + 255) / 256;
+    P.partials = dalloc<double>((size_t)NSLOTS * K.nblocks);
+    P.scan_tmp = dalloc<long long>((ncells + 4095) / 4096 + 1);
+    // Step state.
+    StepState st;
+    memset(&st, 0, sizeof(st));
+    st.deltat = dt; st.isfirst = 1; st.m_minT = 1000.;
+    for (size_t m = 0; m < meshes.size(); ++m)
+      for (int d = 0; d < 3; ++d) { st.mesh_v[m][d] = meshes[m].mv.c[d]; st.mesh_w[m][d] = meshes[m].mw.c[d]; }
+    CK(cudaMemcpyAsync(P.st, &st, sizeof(st), cudaMemcpyHostToDevice, stream));
+    launch_prologue(P, K, stream);
+    // SolverKickDrift.cpp:72-96: with contact, a search + CalculateSurface(1)
+    // before the loop; the first step searches again (ClearNbData).
+    if (contact) {
+      launch_force_search(P, stream);
+      launch_neighbour_search(P, K, d_fscratch, d_iscratch, stream);
+      K.id_free_surf = 1;
+    }
+    StepState* stp = P.st;
+    int one = 1, zero = 0;
+    CK(cudaMemcpyAsync(&stp->nb_cleared, &one, sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(&stp->do_search, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaGetLastError());
+    prepared = true;
+    check_errors();
+  }
+
+  void use_device() { if (prepared) CK(cudaSetDevice(device)); }
+  wf::StepState read_state() {
+    use_device();
+    wf::StepState st;
+    CK(cudaMemcpyAsync(&st, P.st, sizeof(st), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return st;
+  }
+  void check_errors() {
+    wf::StepState st = read_state();
+    if (st.errors & wf::ERR_NBR_OVERFLOW) throw CudaError{WF_ERR_NBR_OVERFLOW, "a particle has more than 100 neighbours (MAX_NB_PER_PART)"};
+    if (st.errors & wf::ERR_CONTACT_OVERFLOW) throw CudaError{WF_ERR_NBR_OVERFLOW, "a particle has more than 64 contact pairs"};
+    if (st.errors & wf::ERR_TIMEOUT) throw CudaError{WF_ERR_TIMEOUT, "a bounded device wait gave up"};
+    if (contact && st.nb_searches > 0 && st.surface_count == 0)
+      throw CudaError{WF_ERR_STATE, "No external particles found. Please check particle masses"};
+  }
+
+  void launch_one_step() {
+    if (precision == WF_PRECISION_MIXED) throw CudaError{WF_ERR_UNSUPPORTED, "mixed form not built yet"};
+    wf::launch_step_fp64(P, K, d_fscratch, d_iscratch, stream);
+  }
+  void step(long long n) {
+    if (!prepared) throw CudaError{WF_ERR_STATE, "wf_step before wf_prepare_kickdrift"};
+    use_device();
+    if (use_graph) {
+      if (!graph || graph_precision != precision) {
+        if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        long long l0 = wf::g_launches;
+        launch_one_step();
+        launches_per_step = wf::g_launches - l0;
+        CK(cudaStreamEndCapture(stream, &g));
+        CK(cudaGraphInstantiate(&graph, g, 0));
+        CK(cudaGraphDestroy(g));
+        graph_precision = precision;
+      }
+      for (long long s = 0; s < n; ++s) CK(cudaGraphLaunch(graph, stream));
+    } else {
+      for (long long s = 0; s < n; ++s) launch_one_step();
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    check_errors();
+  }
+  double step_timed(long long n, long long* launches) {
+    use_device();
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaStreamSynchronize(stream));
+    if (use_graph && (!graph || graph_precision != precision)) step(0);
+    long long l0 = wf::g_launches;
+    CK(cudaEventRecord(a, stream));
+    if (use_graph) {
+      for (long long s = 0; s < n; ++s) CK(cudaGraphLaunch(graph, stream));
+    } else {
+      for (long long s = 0; s < n; ++s) launch_one_step();
+    }
+    CK(cudaEventRecord(b, stream));
+    CK(cudaEventSynchronize(b));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *launches = use_graph ? launches_per_step * n : wf::g_launches - l0;
+    check_errors();
+    return ms;
+  }
+  struct ProfRow { std::string name; double ms; long long count; };
+  std::vector<ProfRow> profile(long long n) {
+    use_device();
+    const int cap = 64 * (int)std::max<long long>(n, 1) + 8;
+    std::vector<cudaEvent_t> ev(cap);
+    std::vector<const char*> names(cap);
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    wf::KernelTimer t;
+    t.ev = ev.data(); t.names = names.data(); t.cap = cap; t.n = 0;
+    CK(cudaStreamSynchronize(stream));
+    wf::g_timer = &t;
+    wf::mark(stream, "begin");
+    try {
+      for (long long s = 0; s < n; ++s) launch_one_step();
+    } catch (...) { wf::g_timer = nullptr; throw; }
+    wf::g_timer = nullptr;
+    CK(cudaStreamSynchronize(stream));
+    std::vector<ProfRow> rows;
+    for (int k = 1; k < t.n; ++k) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, ev[k - 1], ev[k]));
+      auto it = std::find_if(rows.begin(), rows.end(), [&](const ProfRow& r) { return r.name == names[k]; });
+      if (it == rows.end()) rows.push_back(ProfRow{names[k], ms, 1});
+      else { it->ms += ms; it->count += 1; }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    check_errors();
+    return rows;
+  }
+  void search_now() {
+    if (!prepared) throw CudaError{WF_ERR_STATE, "neighbour search before the solver prologue"};
+    use_device();
+    wf::launch_force_search(P, stream);
+    wf::launch_neighbour_search(P, K, d_fscratch, d_iscratch, stream);
+    int zero = 0;
+    CK(cudaMemcpyAsync(&P.st->do_search, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    check_errors();
+  }
+
+  // ------------------------------------------------------------ transfers
+  void get_f64(int c, int ncomp, double* dst) {
+    size_t n = hp.N;
+    if (!prepared) {
+      for (size_t p = 0; p < n; ++p)
+        for (int k = 0; k < ncomp; ++k) dst[p * ncomp + k] = hp.f[c + k][p];
+      return;
+    }
+    use_device();
+    double* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, sizeof(double) * n * ncomp, stream));
+    wf::launch_gather_orig(P, K, d_f + (size_t)c * n, tmp, ncomp, stream);
+    CK(cudaMemcpyAsync(dst, tmp, sizeof(double) * n * ncomp, cudaMemcpyDeviceToHost, stream));
+    CK(cudaFreeAsync(tmp, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  void set_f64(int c, int ncomp, const double* src) {
+    size_t n = hp.N;
+    if (!prepared) {
+      for (size_t p = 0; p < n; ++p)
+        for (int k = 0; k < ncomp; ++k) hp.f[c + k][p] = src[p * ncomp + k];
+      return;
+    }
+    use_device();
+    double* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, sizeof(double) * n * ncomp, stream));
+    CK(cudaMemcpyAsync(tmp, src, sizeof(double) * n * ncomp, cudaMemcpyHostToDevice, stream));
+    wf::launch_scatter_orig(P, K, tmp, d_f + (size_t)c * n, ncomp, stream);
+    CK(cudaFreeAsync(tmp, stream));
+    wf::launch_refresh_derived(P, K, stream);
+    CK(cudaStreamSynchronize(stream));
+  }
+  void get_i32(int c, int* dst) {
+    size_t n = hp.N;
+    if (!prepared) { for (size_t p = 0; p < n; ++p) dst[p] = hp.i[c][p]; return; }
+    use_device();
+    int* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, sizeof(int) * n, stream));
+    wf::launch_gather_orig_i32(P, K, d_i + (size_t)c * n, tmp, stream);
+    CK(cudaMemcpyAsync(dst, tmp, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaFreeAsync(tmp, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  // Canonical-order rows (ELL on device) as CSR over original indices.
+  void get_rows(const int* d_len, const int* d_ell, int width, std::vector<long long>& off, std::vector<int>& idx) {
+    use_device();
+    size_t n = hp.N;
+    std::vector<int> len(n), orig(n), ell;
+    CK(cudaMemcpyAsync(len.data(), d_len, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(orig.data(), d_i + (size_t)wf::I_ORIG * n, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    int mx = 0;
+    for (int l : len) mx = std::max(mx, l);
+    mx = std::min(mx, width);
+    ell.resize((size_t)mx * n);
+    if (mx) CK(cudaMemcpyAsync(ell.data(), d_ell, sizeof(int) * mx * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    std::vector<int> sorted_of(n);
+    for (size_t i = 0; i < n; ++i) sorted_of[orig[i]] = (int)i;
+    off.assign(n + 1, 0);
+    for (size_t o = 0; o < n; ++o) off[o + 1] = off[o] + std::min(len[sorted_of[o]], width);
+    idx.assign(off[n], 0);
+    for (size_t o = 0; o < n; ++o) {
+      int i = sorted_of[o];
+      int l = std::min(len[i], width);
+      for (int k = 0; k < l; ++k) idx[off[o] + k] = orig[ell[(size_t)k * n + i]];
+    }
+  }
+};
+
+// ============================================================================ C ABI
+namespace {
+template <class F> int guard(F&& f) {
+  try {
+    return f();
+  } catch (const CudaError& e) {
+    return set_err(e.code, e.msg);
+  } catch (const std::exception& e) {
+    return set_err(WF_ERR_ARG, e.what());
+  } catch (...) {
+    return set_err(WF_ERR_ARG, "unknown error");
+  }
+}
+#define NEED(d) if (!(d)) return set_err(WF_ERR_ARG, "null domain")
+}  // namespace
+
+extern "C" {
+
+int wf_version(void) { return 10000; }
+const char* wf_last_error(void) { return g_err.c_str(); }
+
+int wf_domain_create(int dimension, wf_domain** out) {
+  if (!out) return set_err(WF_ERR_ARG, "null out");
+  if (dimension != 3) return set_err(WF_ERR_UNSUPPORTED, "only Dimension = 3 is supported");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_err(WF_ERR_CUDA, "no CUDA device available");
+  *out = new wf_domain();
+  return WF_OK;
+}
+int wf_domain_destroy(wf_domain* d) { delete d; return WF_OK; }
+
+int wf_set_domain_f64(wf_domain* d, const char* name, double v) {
+  NEED(d);
+  std::string n(name ? name : "");
+  if (d->prepared && n != "contact_force_factor") return set_err(WF_ERR_STATE, "domain fields are fixed after the prologue");
+  if (n == "Cellfac") d->Cellfac = v;
+  else if (n == "pl_work_heat_frac") d->pl_work_heat_frac = v;
+  else if (n == "friction_sta") d->friction_sta = v;
+  else if (n == "friction_dyn") d->friction_dyn = v;
+  else if (n == "PFAC") d->PFAC = v;
+  else if (n == "DFAC") d->DFAC = v;
+  else if (n == "contact_force_factor") {}
+  else if (n.size() == 8 && n.rfind("DomMax.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') d->DomMax[n[7] - 'x'] = v;
+  else if (n.size() == 8 && n.rfind("DomMin.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') d->DomMin[n[7] - 'x'] = v;
+  else return set_err(WF_ERR_ARG, "unknown domain f64 field " + n);
+  return WF_OK;
+}
+int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
+  NEED(d);
+  std::string n(name ? name : "");
+  if (n == "precision") {
+    if (v != WF_PRECISION_FP64 && v != WF_PRECISION_MIXED) return set_err(WF_ERR_ARG, "precision must be 0 or 1");
+    d->precision = v;
+    return WF_OK;
+  }
+  if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }
+  if (n == "device") {
+    if (d->prepared) return set_err(WF_ERR_STATE, "the device is fixed after the prologue");
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || v < 0 || v >= nd) return set_err(WF_ERR_ARG, "no such CUDA device");
+    d->device = v;
+    return WF_OK;
+  }
+  if (n == "cpu_threads" || n == "Nproc" || n == "cpu_mode") return WF_OK;
+  if (d->prepared) return set_err(WF_ERR_STATE, "domain fields are fixed after the prologue");
+  if (n == "ts_nb_inc") { if (v < 1) return set_err(WF_ERR_ARG, "ts_nb_inc >= 1"); d->ts_nb_inc = v; }
+  else if (n == "pl_heating") d->pl_heating = v;
+  else if (n == "thermal_solver") d->thermal_solver = v;
+  else if (n == "contact") d->contact = v;
+  else if (n == "contact_mesh_auto_update") d->contact_mesh_auto_update = v;
+  else if (n == "contact_alg") { if (v < 0 || v > 2) return set_err(WF_ERR_ARG, "contact_alg"); d->contact_alg = v; }
+  else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
+  else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
+  else if (n == "GradientType") { if (v) return set_err(WF_ERR_UNSUPPORTED, "only GradientType 0 is supported"); }
+  else return set_err(WF_ERR_ARG, "unknown domain i32 field " + n);
+  return WF_OK;
+}
+int wf_get_domain_f64(wf_domain* d, const char* name, double* v) {
+  NEED(d);
+  return guard([&] {
+    std::string n(name ? name : "");
+    if (!d->prepared) {
+      if (n == "Time" || n.find("sum") != std::string::npos || n == "plastic_work" || n == "ext_forces_work" ||
+          n == "max_pl_strain" || n == "m_maxT" || n == "m_minT") { *v = 0.0; return WF_OK; }
+      if (n == "hmax") { *v = 0.0; return WF_OK; }
+      if (n == "deltat") { *v = 0.0; return WF_OK; }
+      return set_err(WF_ERR_ARG, "unknown domain f64 read " + n);
+    }
+    wf::StepState st = d->read_state();
+    if (n == "Time") *v = st.Time;
+    else if (n == "deltat") *v = st.deltat;
+    else if (n == "hmax") *v = d->hmax;
+    else if (n == "int_energy_sum") *v = st.int_energy_sum;
+    else if (n == "kin_energy_sum") *v = st.kin_energy_sum;
+    else if (n == "plastic_work") *v = st.plastic_work;
+    else if (n == "contact_force_sum") *v = st.contact_force_sum;
+    else if (n == "contact_reaction_sum") *v = st.contact_reaction_sum;
+    else if (n == "ext_forces_work") *v = st.ext_forces_work;
+    else if (n == "max_pl_strain") *v = st.max_pl;
+    else if (n == "m_maxT") *v = st.m_maxT;
+    else if (n == "m_minT") *v = st.m_minT;
+    else return set_err(WF_ERR_ARG, "unknown domain f64 read " + n);
+    return WF_OK;
+  });
+}
+int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
+  NEED(d);
+  return guard([&] {
+    std::string n(name ? name : "");
+    if (n == "particle_count") { *v = d->hp.N; return WF_OK; }
+    if (n == "solid_part_count") { *v = d->solid_part_count; return WF_OK; }
+    if (n.size() == 8 && n.rfind("CellNo.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') { *v = d->CellNo[n[7] - 'x']; return WF_OK; }
+    if (!d->prepared) { *v = 0; return WF_OK; }
+    wf::StepState st = d->read_state();
+    if (n == "steps") *v = st.steps;
+    else if (n == "pair_count") *v = st.pair_count / 2;
+    else if (n == "contact_pair_count") *v = st.contact_pair_count;
+    else if (n == "nb_searches") *v = st.nb_searches;
+    else if (n == "surface_count") *v = st.surface_count;
+    else return set_err(WF_ERR_ARG, "unknown domain i32 read " + n);
+    return WF_OK;
+  });
+}
+int wf_kernel_set(wf_domain* d, int kt) {
+  NEED(d);
+  if (kt != 0) return set_err(WF_ERR_UNSUPPORTED, "only the cubic spline kernel (0) is supported");
+  d->Cellfac = 2.0;
+  return WF_OK;
+}
+int wf_add_box_length(wf_domain* d, int tag, const double V[3], double Lx, double Ly, double Lz, double r,
+                      double density, double h, int type, int rotation, int random, int fixed) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "particles are fixed after the prologue");
+  if (!(type == 0 || type == 1)) return set_err(WF_ERR_ARG, "AddBoxLength: packing type must be 0 or 1");
+  if (!(rotation == 0 || rotation == 90)) return set_err(WF_ERR_ARG, "AddBoxLength: rotation must be 0 or 90");
+  if (fixed) return set_err(WF_ERR_UNSUPPORTED, "fixed (non-free) particles are not supported");
+  if (!(r > 0) || !(h > 0)) return set_err(WF_ERR_ARG, "r and h must be positive");
+  if (!d->meshes.empty()) return set_err(WF_ERR_STATE, "add solid particles before rigid meshes");
+  d->add_box(tag, V, Lx, Ly, Lz, r, density, h, type, random != 0);
+  return WF_OK;
+}
+int wf_add_cylinder_length(wf_domain* d, int tag, const double V[3], double Rxy, double Lz, double r, double density,
+                           double h, int fixed, int ghost) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "particles are fixed after the prologue");
+  if (ghost) return set_err(WF_ERR_UNSUPPORTED, "ghost rows are not supported");
+  if (fixed) return set_err(WF_ERR_UNSUPPORTED, "fixed (non-free) particles are not supported");
+  if (!(r > 0) || !(h > 0)) return set_err(WF_ERR_ARG, "r and h must be positive");
+  if (!d->meshes.empty()) return set_err(WF_ERR_STATE, "add solid particles before rigid meshes");
+  d->add_cylinder(tag, V, Rxy, Lz, r, density, h);
+  return WF_OK;
+}
+int wf_assign_zone(wf_domain* d, const double s[3], const double e[3], int id, int64_t* count) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "zones are fixed after the prologue");
+  int64_t c = 0;
+  for (int p = 0; p < d->hp.N; ++p) {
+    bool in = true;
+    for (int k = 0; k < 3; ++k)
+      if (d->hp.f[wf::C_X + k][p] < s[k] || d->hp.f[wf::C_X + k][p] > e[k]) in = false;
+    if (in) { d->hp.i[wf::I_ID][p] = id; d->hp.i[wf::I_IDORIG][p] = id; d->hp.i[wf::I_NWS][p] = 1; ++c; }
+  }
+  if (count) *count = c;
+  return WF_OK;
+}
+int wf_set_particle_f64(wf_domain* d, const char* field, int zone, double value) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "use wf_set_particle_array_f64 after the prologue");
+  std::string f(field ? field : "");
+  if (f == "TI") {  // tensile-instability term (InteractionAlt.cpp:106-110) is outside this build
+    if (value != 0.0) return set_err(WF_ERR_UNSUPPORTED, "tensile instability (TI > 0) is not supported");
+    return WF_OK;
+  }
+  if (f == "TIInitDist") return WF_OK;  // only used by the TI term
+  int nc = 0;
+  int c = col_f64(f, &nc);
+  if (c < 0 || nc != 1) return set_err(WF_ERR_ARG, "unknown particle f64 field " + f);
+  for (int p = 0; p < d->hp.N; ++p)
+    if (zone < 0 || d->hp.i[wf::I_ID][p] == zone) d->hp.f[c][p] = value;
+  return WF_OK;
+}
+int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "particle fields are fixed after the prologue");
+  std::string f(field ? field : "");
+  int c = col_i32(f);
+  if (c < 0 || c == wf::I_NB) {
+    std::string why;
+    if (!fixed_i32(f, value, &why)) return set_err(c == wf::I_NB ? WF_ERR_ARG : (why.rfind("unknown", 0) == 0 ? WF_ERR_ARG : WF_ERR_UNSUPPORTED), why);
+    return WF_OK;
+  }
+  if (f == "Fail" && value > 1) return set_err(WF_ERR_UNSUPPORTED, "Undefined failure criteria for solids");
+  if (f == "Material_model" && (value < 0 || value > 2)) return set_err(WF_ERR_UNSUPPORTED, "material model");
+  for (int p = 0; p < d->hp.N; ++p)
+    if (zone < 0 || d->hp.i[wf::I_ID][p] == zone) {
+      d->hp.i[c][p] = value;
+      if (c == wf::I_ID) d->hp.i[wf::I_IDORIG][p] = value;
+    }
+  return WF_OK;
+}
+int wf_set_particle_array_f64(wf_domain* d, const char* field, const double* src, int64_t n) {
+  NEED(d);
+  return guard([&] {
+    std::string f(field ? field : "");
+    int nc = 0;
+    int c = col_f64(f, &nc);
+    if (c < 0) return set_err(WF_ERR_ARG, "unknown particle array " + f);
+    if (n != (int64_t)d->hp.N * nc) return set_err(WF_ERR_ARG, "array size mismatch for " + f);
+    if (nc == 6 || (nc == 3 && c == wf::C_RR))
+      return set_err(WF_ERR_ARG, "tensor fields are set as 9 values per particle");
+    d->set_f64(c, nc, src);
+    return WF_OK;
+  });
+}
+int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int64_t n) {
+  NEED(d);
+  return guard([&] {
+    std::string f(field ? field : "");
+    int nc = 0;
+    int c = col_f64(f, &nc);
+    if (c < 0) return set_err(WF_ERR_ARG, "unknown particle array " + f);
+    size_t N = d->hp.N;
+    if (nc == 6 || c == wf::C_RR) {
+      if (n != (int64_t)N * 9) return set_err(WF_ERR_ARG, "array size mismatch for " + f);
+      std::vector<double> t(N * nc);
+      d->get_f64(c, nc, t.data());
+      for (size_t p = 0; p < N; ++p) {
+        double* o = dst + 9 * p;
+        const double* s = t.data() + nc * p;
+        if (nc == 6) {
+          o[0] = s[0]; o[4] = s[1]; o[8] = s[2]; o[1] = o[3] = s[3]; o[2] = o[6] = s[4]; o[5] = o[7] = s[5];
+        } else {
+          o[0] = o[4] = o[8] = 0.0; o[1] = s[0]; o[3] = -s[0]; o[2] = s[1]; o[6] = -s[1]; o[5] = s[2]; o[7] = -s[2];
+        }
+      }
+      return WF_OK;
+    }
+    if (n != (int64_t)N * nc) return set_err(WF_ERR_ARG, "array size mismatch for " + f);
+    d->get_f64(c, nc, dst);
+    return WF_OK;
+  });
+}
+int wf_get_particle_array_i32(wf_domain* d, const char* field, int32_t* dst, int64_t n) {
+  NEED(d);
+  return guard([&] {
+    std::string f(field ? field : "");
+    if (n != d->hp.N) return set_err(WF_ERR_ARG, "array size mismatch");
+    if (f == "IsFree") { for (int p = 0; p < d->hp.N; ++p) dst[p] = 1; return WF_OK; }
+    int c = col_i32(f);
+    if (c < 0) return set_err(WF_ERR_ARG, "unknown particle i32 array " + f);
+    d->get_i32(c, dst);
+    return WF_OK;
+  });
+}
+int wf_add_material(wf_domain* d, int model, const double* q, int np, int* mat_id) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "materials are fixed after the prologue");
+  if ((int)d->mats.size() >= wf::MAX_MATERIALS) return set_err(WF_ERR_UNSUPPORTED, "too many materials");
+  HostMaterial M;
+  M.model = model;
+  memset(&M.dev, 0, sizeof(M.dev));
+  M.dev.model = model;
+  if (model == WF_BILINEAR) {
+    if (np < 2) return set_err(WF_ERR_ARG, "bilinear needs {E, nu}");
+    M.dev.E = q[0];
+  } else if (model == WF_HOLLOMON) {
+    if (np < 5) return set_err(WF_ERR_ARG, "hollomon needs {E, nu, sy0, K, m}");
+    M.dev.E = q[0]; M.dev.sy0 = q[2]; M.dev.K = q[3]; M.dev.m = q[4];
+    M.dev.eps0 = q[2] / q[0];                    // Material.cpp:48-57
+    M.dev.eps1 = std::pow(q[2] / q[3], 1. / q[4]);
+    if (M.dev.eps0 > M.dev.eps1) return set_err(WF_ERR_ARG, "Hollomon material bad definition");
+  } else if (model == WF_JOHNSON_COOK) {
+    if (np < 10) return set_err(WF_ERR_ARG, "johnson-cook needs {E, nu, A, B, n, C, eps_0, m, T_m, T_t}");
+    M.dev.E = q[0]; M.dev.A = q[2]; M.dev.B = q[3]; M.dev.n = q[4]; M.dev.C = q[5]; M.dev.eps_0 = q[6];
+    M.dev.jm = q[7]; M.dev.T_m = q[8]; M.dev.T_t = q[9];
+  } else {
+    return set_err(WF_ERR_UNSUPPORTED, "unknown material model");
+  }
+  M.p.assign(q, q + np);
+  d->mats.push_back(M);
+  *mat_id = (int)d->mats.size() - 1;
+  return WF_OK;
+}
+int wf_add_amplitude(wf_domain* d, int id, const double* t, const double* v, int n) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "amplitudes are fixed after the prologue");
+  if (n < 2) return set_err(WF_ERR_ARG, "amplitude needs at least two points");
+  int tot = n;
+  for (auto& a : d->amps) tot += (int)a.t.size();
+  if ((int)d->amps.size() >= wf::MAX_AMPS || tot > wf::MAX_AMP_POINTS) return set_err(WF_ERR_UNSUPPORTED, "amplitude table full");
+  d->amps.push_back(HostAmp{id, std::vector<double>(t, t + n), std::vector<double>(v, v + n)});
+  return WF_OK;
+}
+int wf_add_velocity_bc(wf_domain* d, int zone, const double value[3], const double value_ang[3], int value_type,
+                       int amp_id, double amp_factor) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "boundary conditions are fixed after the prologue");
+  if ((int)d->bcs.size() >= wf::MAX_BCS) return set_err(WF_ERR_UNSUPPORTED, "too many boundary conditions");
+  if (value_type != 0 && value_type != 1) return set_err(WF_ERR_ARG, "value_type must be 0 or 1");
+  HostBC b;
+  b.zone = zone; b.vt = value_type; b.amp = amp_id; b.fac = amp_factor;
+  for (int k = 0; k < 3; ++k) { b.value[k] = value[k]; b.ang[k] = value_ang ? value_ang[k] : 0.0; }
+  d->bcs.push_back(b);
+  return WF_OK;
+}
+int wf_add_rigid_plane(wf_domain* d, int axis, int posit, const double p1[3], const double p2[3], int dens,
+                       double hfac, int zone_id, int* mesh_id) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "meshes are fixed after the prologue");
+  if (dens <= 0 || axis < 0 || axis > 2) return set_err(WF_ERR_ARG, "bad plane arguments");
+  if ((int)d->meshes.size() >= wf::MAX_MESHES) return set_err(WF_ERR_UNSUPPORTED, "too many rigid meshes");
+  if (d->solid_part_count < 0) d->solid_part_count = d->hp.N;
+  int m = d->add_plane(axis, posit != 0, p1, p2, dens, hfac, zone_id);
+  if (mesh_id) *mesh_id = m;
+  return WF_OK;
+}
+int wf_set_mesh_velocity(wf_domain* d, int mesh, const double v[3], const double w[3]) {
+  NEED(d);
+  if (mesh < 0 || mesh >= (int)d->meshes.size()) return set_err(WF_ERR_ARG, "mesh index");
+  if (d->prepared) return set_err(WF_ERR_STATE, "set the mesh velocity through a velocity BC after the prologue");
+  d->meshes[mesh].mv = vec(v[0], v[1], v[2]);
+  if (w) d->meshes[mesh].mw = vec(w[0], w[1], w[2]);
+  return WF_OK;
+}
+int wf_get_contact_force(wf_domain* d, int mesh, double out[3]) {
+  NEED(d);
+  return guard([&] {
+    if (mesh < 0 || mesh >= (int)d->meshes.size()) return set_err(WF_ERR_ARG, "mesh index");
+    if (!d->prepared) { out[0] = out[1] = out[2] = 0.0; return WF_OK; }
+    wf::StepState st = d->read_state();
+    for (int k = 0; k < 3; ++k) out[k] = st.contact_force[mesh][k];
+    return WF_OK;
+  });
+}
+int wf_prepare_kickdrift(wf_domain* d, double dt) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "the prologue already ran");
+  if (!(dt > 0)) return set_err(WF_ERR_ARG, "dt must be positive");
+  return guard([&] { d->prepare(dt); return WF_OK; });
+}
+int wf_step(wf_domain* d, int64_t n) {
+  NEED(d);
+  if (n < 0) return set_err(WF_ERR_ARG, "negative step count");
+  return guard([&] { d->step(n); return WF_OK; });
+}
+int wf_solve_kickdrift(wf_domain* d, double tf, double dt, double dtOut, int64_t maxidx) {
+  NEED(d);
+  return guard([&] {
+    if (!d->prepared) d->prepare(dt);
+    // Same loop control as SolverKickDrift.cpp:117,333-346 with Time advanced
+    // on the host in the same order as on the device.
+    wf::StepState st = d->read_state();
+    double Time = st.Time, tout = st.Time;
+    int64_t idx_out = 1;
+    int64_t pending = 0;
+    while (Time <= tf && idx_out <= maxidx) {
+      ++pending;
+      Time += st.deltat;
+      if (Time >= tout) { idx_out++; tout += dtOut; }
+    }
+    d->step(pending);
+    return WF_OK;
+  });
+}
+int wf_neighbour_search(wf_domain* d) {
+  NEED(d);
+  return guard([&] { d->search_now(); return WF_OK; });
+}
+static int rows_out(wf_domain* d, bool contact_rows, int64_t* off, int32_t* idx, int64_t cap) {
+  return guard([&] {
+    if (!d->prepared) return set_err(WF_ERR_STATE, "no neighbour list yet");
+    std::vector<long long> o;
+    std::vector<int> ix;
+    if (contact_rows) d->get_rows(d->P.cp_len, d->P.cp, d->contact ? wf::MAX_CP : 0, o, ix);
+    else d->get_rows(d->P.row_len, d->P.nbr, wf::MAX_NB, o, ix);
+    for (size_t k = 0; k < o.size(); ++k) off[k] = o[k];
+    if (idx) {
+      if (cap < (int64_t)ix.size()) return set_err(WF_ERR_ARG, "idx capacity");
+      for (size_t k = 0; k < ix.size(); ++k) idx[k] = ix[k];
+    }
+    return WF_OK;
+  });
+}
+int wf_get_neighbours(wf_domain* d, int64_t* off, int32_t* idx, int64_t cap) { NEED(d); return rows_out(d, false, off, idx, cap); }
+int wf_get_contact_pairs(wf_domain* d, int64_t* off, int32_t* idx, int64_t cap) { NEED(d); return rows_out(d, true, off, idx, cap); }
+int wf_step_timed(wf_domain* d, int64_t n, double* ms, int64_t* launches) {
+  NEED(d);
+  return guard([&] {
+    if (!d->prepared) return set_err(WF_ERR_STATE, "wf_step_timed before wf_prepare_kickdrift");
+    long long l = 0;
+    *ms = d->step_timed(n, &l);
+    if (launches) *launches = l;
+    return WF_OK;
+  });
+}
+int wf_profile_steps(wf_domain* d, int64_t n, char* names, int name_len, double* total_ms, int64_t* launches,
+                     int cap, int* nk) {
+  NEED(d);
+  return guard([&] {
+    if (!d->prepared) return set_err(WF_ERR_STATE, "wf_profile_steps before wf_prepare_kickdrift");
+    auto rows = d->profile(n);
+    int k = 0;
+    for (auto& r : rows) {
+      if (k >= cap) break;
+      if (names && name_len > 0) {
+        strncpy(names + (size_t)k * name_len, r.name.c_str(), name_len - 1);
+        names[(size_t)k * name_len + name_len - 1] = 0;
+      }
+      total_ms[k] = r.ms;
+      launches[k] = r.count;
+      ++k;
+    }
+    *nk = k;
+    return WF_OK;
+  });
+}
+int wf_synchronize(wf_domain* d) {
+  NEED(d);
+  return guard([&] {
+    if (!d->prepared) return WF_OK;
+    d->use_device();
+    CK(cudaStreamSynchronize(d->stream));
+    d->check_errors();
+    return WF_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,52 @@
+// Host-side launch entry points of the device kernels (one stream per domain).
+#pragma once
+#include "wf_device.cuh"
+
+namespace wf {
+
+// Launch bookkeeping: every kernel launch of a step is followed by mark(),
+// which counts launches and, during an instrumented run, records a CUDA event
+// on the launching stream so each kernel's duration can be read back.
+struct KernelTimer {
+  cudaEvent_t* ev = nullptr;
+  const char** names = nullptr;
+  int cap = 0, n = 0;
+};
+extern thread_local KernelTimer* g_timer;
+extern thread_local long long g_launches;
+inline void mark(cudaStream_t s, const char* name) {
+  ++g_launches;
+  KernelTimer* t = g_timer;
+  if (t && t->n < t->cap) {
+    cudaEventRecord(t->ev[t->n], s);
+    t->names[t->n] = name;
+    ++t->n;
+  }
+}
+
+// Neighbour search pipeline (wf_nbsearch.cu); every kernel is gated on
+// StepState::do_search.
+void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch,
+                             cudaStream_t s);
+// Forces the search on the next launch (solver prologue and explicit calls).
+void launch_force_search(const DevPtrs& P, cudaStream_t s);
+
+// One kick-drift step of the plain FP64 form (wf_step_fp64.cu).
+void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
+// One kick-drift step of the mixed FP32/FP64 form (wf_step_mixed.cu).
+void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
+
+// Prologue helpers: derived columns (Sigma/rho^2, m/rho, p/rho^2), initial
+// pressure (InitialChecks, Domain.cpp:2097-2113) and max pl_strain.
+void launch_prologue(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
+// Host-transfer helpers: scatter/gather between original and sorted order.
+void launch_gather_orig(const DevPtrs& P, const DomainConst& K, const double* col, double* out_orig, int ncomp,
+                        cudaStream_t s);
+void launch_scatter_orig(const DevPtrs& P, const DomainConst& K, const double* in_orig, double* col, int ncomp,
+                         cudaStream_t s);
+void launch_gather_orig_i32(const DevPtrs& P, const DomainConst& K, const int* col, int* out_orig, cudaStream_t s);
+void launch_scatter_orig_i32(const DevPtrs& P, const DomainConst& K, const int* in_orig, int* col, cudaStream_t s);
+// Recompute derived columns after a host write of state (x, v, rho, Sigma...).
+void launch_refresh_derived(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
+
+}  // namespace wf

@@ -1,0 +1,418 @@
+// Neighbour search of the kick-drift step on sm_103a.
+//
+// Replaces the reference's linked-list cell search (Neighbour.cpp:10-477) and
+// pair-list flattening (CalcPairPosList, Neighbour.cpp:617-694):
+//   1. k_cell_keys   — reference cell index (ListGenerate, Neighbour.cpp:183-227:
+//                      floor((x - BLPF) / CellSize), clamped) mapped to the cell's
+//                      Morton rank; histogram per cell.
+//   2. exclusive scan of the histogram -> cell start offsets.
+//   3. k_scatter + k_sort_cells — counting-sort scatter, then each cell's slots
+//                      ordered by original particle index (deterministic order).
+//   4. k_permute / k_copy_back — every persistent state column reordered.
+//   5. k_nbr_fill    — one thread per particle scans the 27 neighbouring cells,
+//                      applies the reference pair rules (AllocateNbPair,
+//                      Neighbour.cpp:374-417: contact-surface pairs, radius test
+//                      CheckRadius :361-372, free + same material) and writes its
+//                      row in canonical order (j > i ascending, then j < i
+//                      ascending by original index) into an ELL array
+//                      (entry k of particle i at k * N + i).
+// The radius test rij / h <= Cellfac is decided bit-exactly: an FP32 distance
+// prefilter with a proven-safe relative margin accepts or rejects clear cases,
+// and everything inside the margin is decided by the reference's FP64
+// expression evaluated with non-contracted IEEE operations.
+//
+// Every kernel checks st->do_search first, so the search can sit inside a
+// captured step and cost only an empty launch on steps that do not rebuild.
+#include "wf_device.cuh"
+#include "wf_launch.h"
+
+namespace wf {
+
+__device__ __forceinline__ bool searching(const DevPtrs& P) { return P.st->do_search != 0; }
+
+__global__ void k_cell_keys(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= K.N) return;
+  int c[3];
+  for (int d = 0; d < 3; ++d) {
+    double xd = P.f[(C_X + d) * (size_t)K.N + p];
+    int q = (int)floor(__ddiv_rn(__dsub_rn(xd, K.BLPF[d]), K.CellSize[d]));
+    if (q < 0) q = 0;
+    if (q >= K.CellNo[d]) q = K.CellNo[d] - 1;
+    c[d] = q;
+  }
+  int lin = (c[0] * K.CellNo[1] + c[1]) * K.CellNo[2] + c[2];
+  int key = P.cell_rank[lin];
+  P.i[I_CELL * (size_t)K.N + p] = key;
+  atomicAdd(&P.cell_count[key], 1);
+}
+
+__global__ void k_zero_int(DevPtrs P, int* a, long long n, int gate) {
+  if (gate && !searching(P)) return;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) a[k] = 0;
+}
+
+// ---- exclusive scan of an int array into an int array (three phases) ------
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ long long block_exclusive_scan(long long v, long long* sh, long long* total) {
+  // Hillis-Steele over a power-of-two block; deterministic.
+  int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int off = 1; off < blockDim.x; off <<= 1) {
+    long long add = (t >= off) ? sh[t - off] : 0;
+    __syncthreads();
+    sh[t] += add;
+    __syncthreads();
+  }
+  long long incl = sh[t];
+  *total = sh[blockDim.x - 1];
+  __syncthreads();
+  return incl - v;
+}
+
+__global__ void k_scan_reduce(DevPtrs P, const int* in, long long n, long long* tot) {
+  if (!searching(P)) return;
+  __shared__ long long sh[SCAN_THREADS];
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  long long s = 0;
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    long long idx = base + (long long)threadIdx.x * SCAN_ITEMS + k;
+    if (idx < n) s += in[idx];
+  }
+  long long total;
+  block_exclusive_scan(s, sh, &total);
+  if (threadIdx.x == 0) tot[blockIdx.x] = total;
+}
+__global__ void k_scan_top(DevPtrs P, long long* tot, int nb) {
+  if (!searching(P)) return;
+  __shared__ long long sh[SCAN_THREADS];
+  long long carry = 0;
+  for (int base = 0; base < nb; base += SCAN_THREADS) {
+    int idx = base + threadIdx.x;
+    long long v = (idx < nb) ? tot[idx] : 0;
+    long long total;
+    long long ex = block_exclusive_scan(v, sh, &total);
+    if (idx < nb) tot[idx] = ex + carry;
+    carry += total;
+    __syncthreads();
+  }
+}
+__global__ void k_scan_down(DevPtrs P, const int* in, long long n, const long long* tot, int* out, int* total_out) {
+  if (!searching(P)) return;
+  __shared__ long long sh[SCAN_THREADS];
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  long long vals[SCAN_ITEMS];
+  long long s = 0;
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    long long idx = base + (long long)threadIdx.x * SCAN_ITEMS + k;
+    vals[k] = (idx < n) ? in[idx] : 0;
+    s += vals[k];
+  }
+  long long total;
+  long long ex = block_exclusive_scan(s, sh, &total) + tot[blockIdx.x];
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    long long idx = base + (long long)threadIdx.x * SCAN_ITEMS + k;
+    if (idx < n) out[idx] = (int)ex;
+    ex += vals[k];
+  }
+  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) *total_out = (int)ex;
+}
+
+__global__ void k_scatter(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= K.N) return;
+  int key = P.i[I_CELL * (size_t)K.N + p];
+  int pos = P.cell_start[key] + atomicAdd(&P.cell_count[key], 1);
+  P.perm[pos] = p;
+}
+
+// Order each cell's slots by original particle index (insertion sort; cells
+// hold ~10-20 particles).
+__global__ void k_sort_cells(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= K.ncells) return;
+  int b = P.cell_start[c], e = P.cell_start[c + 1];
+  const int* orig = P.i + I_ORIG * (size_t)K.N;
+  for (int k = b + 1; k < e; ++k) {
+    int v = P.perm[k];
+    int ov = orig[v];
+    int m = k - 1;
+    while (m >= b && orig[P.perm[m]] > ov) { P.perm[m + 1] = P.perm[m]; --m; }
+    P.perm[m + 1] = v;
+  }
+}
+
+// Gather every persistent column into the scratch arenas (new order).
+__global__ void k_permute(DevPtrs P, DomainConst K, double* fdst, int* idst) {
+  if (!searching(P)) return;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  int col = blockIdx.y;
+  if (p >= K.N) return;
+  int src = P.perm[p];
+  if (col < NF64_PERSIST) fdst[col * (size_t)K.N + p] = P.f[col * (size_t)K.N + src];
+  else {
+    int c = col - NF64_PERSIST;
+    idst[c * (size_t)K.N + p] = P.i[c * (size_t)K.N + src];
+  }
+}
+__global__ void k_copy_back(DevPtrs P, DomainConst K, const double* fsrc, const int* isrc) {
+  if (!searching(P)) return;
+  size_t nf = (size_t)NF64_PERSIST * K.N, ni = (size_t)NI32_PERSIST * K.N;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < nf + ni; k += (size_t)gridDim.x * blockDim.x) {
+    if (k < nf) P.f[k] = fsrc[k];
+    else P.i[k - nf] = isrc[k - nf];
+  }
+}
+
+// Map original -> sorted index, element -> mesh particle, and the FP32
+// prefilter coordinates (relative to BLPF, plus h).
+__global__ void k_after_permute(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= K.N) return;
+  size_t N = K.N;
+  int o = P.i[I_ORIG * N + p];
+  P.inv[o] = p;
+  if (P.i[I_KIND * N + p] == 1) P.elem_particle[P.i[I_ELEM * N + p]] = p;
+  for (int d = 0; d < 3; ++d) P.xs[d * N + p] = (float)(P.f[(C_X + d) * N + p] - K.BLPF[d]);
+  P.xs[3 * N + p] = (float)P.f[C_H * N + p];
+}
+
+__device__ __forceinline__ bool is_contact_id(const DomainConst& K, int id) {
+  for (int m = 0; m < K.nmeshes; ++m)
+    if (id == K.contact_surf_id[m]) return true;
+  return false;
+}
+
+// CheckRadius (Neighbour.cpp:361-372) exactly: rij / ((hi + hj) / 2) <= Cellfac
+// with rij = sqrt(dx*dx + dy*dy + dz*dz) summed left to right, no contraction.
+__device__ __forceinline__ bool radius_exact(const DevPtrs& P, size_t N, int i, int j, double Cellfac) {
+  double hh = __ddiv_rn(__dadd_rn(P.f[C_H * N + i], P.f[C_H * N + j]), 2.0);
+  double dx = __dsub_rn(P.f[(C_X + 0) * N + i], P.f[(C_X + 0) * N + j]);
+  double dy = __dsub_rn(P.f[(C_X + 1) * N + i], P.f[(C_X + 1) * N + j]);
+  double dz = __dsub_rn(P.f[(C_X + 2) * N + i], P.f[(C_X + 2) * N + j]);
+  double s = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  double rij = __dsqrt_rn(s);
+  return __ddiv_rn(rij, hh) <= Cellfac;
+}
+
+// Radius test: FP32 prefilter, exact FP64 decision inside the margin.
+__device__ __forceinline__ bool radius_ok(const DevPtrs& P, const DomainConst& K, size_t N, int i, int j, float xi,
+                                          float yi, float zi, float hi) {
+  float dx = xi - P.xs[j], dy = yi - P.xs[N + j], dz = zi - P.xs[2 * N + j];
+  float d2 = dx * dx + dy * dy + dz * dz;
+  float R = (float)K.Cellfac * 0.5f * (hi + P.xs[3 * N + j]);
+  float R2 = R * R;
+  if (d2 < R2 * (1.0f - K.pre_eps)) return true;
+  if (d2 > R2 * (1.0f + K.pre_eps)) return false;
+  return radius_exact(P, N, i, j, K.Cellfac);
+}
+
+// One thread per particle: SM neighbour row in canonical order; the flag of
+// "was a free-surface particle at search time" for the contact pair rule.
+__global__ void __launch_bounds__(128) k_nbr_fill(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  const int* ID = P.i + I_ID * N;
+  const int* orig = P.i + I_ORIG * N;
+  const int* kind = P.i + I_KIND * N;
+  const int* material = P.i + I_MATERIAL * N;
+  int row[MAX_NB];
+  unsigned keys[MAX_NB];
+  int cnt = 0, split = 0;
+  bool overflow = false;
+  if (kind[i] == 0) {
+    float xi = P.xs[i], yi = P.xs[N + i], zi = P.xs[2 * N + i], hi = P.xs[3 * N + i];
+    int c[3];
+    for (int d = 0; d < 3; ++d) {
+      int q = (int)floor(__ddiv_rn(__dsub_rn(P.f[(C_X + d) * N + i], K.BLPF[d]), K.CellSize[d]));
+      c[d] = q < 0 ? 0 : (q >= K.CellNo[d] ? K.CellNo[d] - 1 : q);
+    }
+    int idi = ID[i], oi = orig[i], mi = material[i];
+    bool ci = K.contact && is_contact_id(K, idi);
+    for (int a = c[0] - 1; a <= c[0] + 1; ++a) {
+      if (a < 0 || a >= K.CellNo[0]) continue;
+      for (int b = c[1] - 1; b <= c[1] + 1; ++b) {
+        if (b < 0 || b >= K.CellNo[1]) continue;
+        for (int e = c[2] - 1; e <= c[2] + 1; ++e) {
+          if (e < 0 || e >= K.CellNo[2]) continue;
+          int key = P.cell_rank[(a * K.CellNo[1] + b) * K.CellNo[2] + e];
+          int s0 = P.cell_start[key], s1 = P.cell_start[key + 1];
+          for (int j = s0; j < s1; ++j) {
+            if (j == i) continue;
+            int idj = ID[j];
+            if (K.contact && (ci || is_contact_id(K, idj))) continue;  // RIG or dropped pair
+            if (kind[j] != 0 || material[j] != mi) continue;
+            if (!radius_ok(P, K, N, i, j, xi, yi, zi, hi)) continue;
+            unsigned kk = (unsigned)(orig[j] - oi - 1);
+            if (orig[j] > oi) ++split;
+            if (cnt < MAX_NB) {
+              int m = cnt - 1;
+              while (m >= 0 && keys[m] > kk) { keys[m + 1] = keys[m]; row[m + 1] = row[m]; --m; }
+              keys[m + 1] = kk; row[m + 1] = j;
+              ++cnt;
+            } else overflow = true;
+          }
+        }
+      }
+    }
+  }
+  for (int k = 0; k < cnt; ++k) P.nbr[(size_t)k * N + i] = row[k];
+  P.row_len[i] = cnt;
+  P.row_split[i] = split < cnt ? split : cnt;
+  P.i[I_NB * N + i] = cnt;
+  if (K.contact) P.i[I_NWS * N + i] = (P.i[I_NWS * N + i] & 1) | ((ID[i] == K.id_free_surf) ? 2 : 0);
+  if (overflow) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
+  // pair count (each unordered pair counted from both ends)
+  atomicAdd(&P.st->pair_count, (unsigned long long)cnt);
+}
+
+// CalculateSurface (Domain.cpp:1415-1491): n_i = sum_j m_j (x_i - x_j) in row
+// order; |n| / totmass >= 0.25 h and Nb <= 46 marks the free surface (ID 1).
+__global__ void k_surface(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  if (P.i[I_KIND * N + i] != 0) return;
+  double xi = P.f[C_X * N + i], yi = P.f[(C_X + 1) * N + i], zi = P.f[(C_X + 2) * N + i];
+  double n0 = 0, n1 = 0, n2 = 0;
+  int len = P.row_len[i];
+  for (int k = 0; k < len; ++k) {
+    int j = P.nbr[(size_t)k * N + i];
+    double mj = P.f[C_MASS * N + j];
+    n0 = __dadd_rn(n0, __dmul_rn(mj, __dsub_rn(xi, P.f[C_X * N + j])));
+    n1 = __dadd_rn(n1, __dmul_rn(mj, __dsub_rn(yi, P.f[(C_X + 1) * N + j])));
+    n2 = __dadd_rn(n2, __dmul_rn(mj, __dsub_rn(zi, P.f[(C_X + 2) * N + j])));
+  }
+  double s = __ddiv_rn(1.0, K.totmass_mean);
+  n0 = __dmul_rn(s, n0); n1 = __dmul_rn(s, n1); n2 = __dmul_rn(s, n2);
+  P.f[C_NORMAL * N + i] = n0; P.f[(C_NORMAL + 1) * N + i] = n1; P.f[(C_NORMAL + 2) * N + i] = n2;
+  int id = P.i[I_IDORIG * N + i];
+  double nn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(n0, n0), __dmul_rn(n1, n1)), __dmul_rn(n2, n2)));
+  bool surf = (nn >= __dmul_rn(0.25, P.f[C_H * N + i])) && (len <= 46);
+  if (surf) {
+    if (!(P.i[I_NWS * N + i] & 1)) id = 1;
+    atomicAdd(&P.st->surface_count, 1);
+  }
+  P.i[I_ID * N + i] = id;
+}
+
+// ContactNbSearch (Contact.cpp:57-132): surface particle (at search time and
+// now) within h1 + h2 of a rigid-mesh particle in a neighbouring cell.
+// Row sorted by the mesh particle's original index.
+__global__ void k_contact_pairs(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  int cnt = 0;
+  bool overflow = false;
+  int row[MAX_CP];
+  int keys[MAX_CP];
+  int idi = P.i[I_ID * N + i];
+  bool ok = P.i[I_KIND * N + i] == 0 && (P.i[I_NWS * N + i] & 2) && idi == K.id_free_surf;
+  if (ok) {
+    double xi = P.f[C_X * N + i], yi = P.f[(C_X + 1) * N + i], zi = P.f[(C_X + 2) * N + i];
+    double hi = P.f[C_H * N + i];
+    int c[3];
+    for (int d = 0; d < 3; ++d) {
+      int q = (int)floor(__ddiv_rn(__dsub_rn(P.f[(C_X + d) * N + i], K.BLPF[d]), K.CellSize[d]));
+      c[d] = q < 0 ? 0 : (q >= K.CellNo[d] ? K.CellNo[d] - 1 : q);
+    }
+    for (int a = c[0] - 1; a <= c[0] + 1; ++a) {
+      if (a < 0 || a >= K.CellNo[0]) continue;
+      for (int b = c[1] - 1; b <= c[1] + 1; ++b) {
+        if (b < 0 || b >= K.CellNo[1]) continue;
+        for (int e = c[2] - 1; e <= c[2] + 1; ++e) {
+          if (e < 0 || e >= K.CellNo[2]) continue;
+          int key = P.cell_rank[(a * K.CellNo[1] + b) * K.CellNo[2] + e];
+          for (int j = P.cell_start[key]; j < P.cell_start[key + 1]; ++j) {
+            if (P.i[I_KIND * N + j] != 1) continue;
+            if (!is_contact_id(K, P.i[I_ID * N + j])) continue;
+            double dx = __dsub_rn(xi, P.f[C_X * N + j]), dy = __dsub_rn(yi, P.f[(C_X + 1) * N + j]),
+                   dz = __dsub_rn(zi, P.f[(C_X + 2) * N + j]);
+            double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            if (!(r < __dadd_rn(hi, P.f[C_H * N + j]))) continue;
+            int kk = P.i[I_ORIG * N + j];
+            if (cnt < MAX_CP) {
+              int m = cnt - 1;
+              while (m >= 0 && keys[m] > kk) { keys[m + 1] = keys[m]; row[m + 1] = row[m]; --m; }
+              keys[m + 1] = kk; row[m + 1] = j;
+              ++cnt;
+            } else overflow = true;
+          }
+        }
+      }
+    }
+  }
+  for (int k = 0; k < cnt; ++k) P.cp[(size_t)k * N + i] = row[k];
+  P.cp_len[i] = cnt;
+  if (overflow) atomicOr(&P.st->errors, ERR_CONTACT_OVERFLOW);
+  if (cnt) atomicAdd(&P.st->contact_pair_count, (unsigned long long)cnt);
+}
+
+__global__ void k_force_search(DevPtrs P) { P.st->do_search = 1; }
+void launch_force_search(const DevPtrs& P, cudaStream_t s) { k_force_search<<<1, 1, 0, s>>>(P); }
+
+__global__ void k_search_begin(DevPtrs P) {
+  if (!searching(P)) return;
+  P.st->pair_count = 0;
+  P.st->contact_pair_count = 0;
+  P.st->surface_count = 0;
+  P.st->nb_searches += 1;
+}
+
+// ---------------------------------------------------------------- host side
+static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch,
+                             cudaStream_t s) {
+  const int T = 256;
+  int nz = nblk(K.ncells, T) > 4096 ? 4096 : nblk(K.ncells, T);
+  k_search_begin<<<1, 1, 0, s>>>(P);
+  mark(s, "k_search_begin");
+  k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, K.ncells, 1);
+  mark(s, "k_zero_int");
+  k_cell_keys<<<nblk(K.N, T), T, 0, s>>>(P, K);
+  mark(s, "k_cell_keys");
+  int nb = nblk(K.ncells, SCAN_TILE);
+  k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(P, P.cell_count, K.ncells, P.scan_tmp);
+  mark(s, "k_scan_reduce");
+  k_scan_top<<<1, SCAN_THREADS, 0, s>>>(P, P.scan_tmp, nb);
+  mark(s, "k_scan_top");
+  k_scan_down<<<nb, SCAN_THREADS, 0, s>>>(P, P.cell_count, K.ncells, P.scan_tmp, P.cell_start, P.cell_start + K.ncells);
+  mark(s, "k_scan_down");
+  k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, K.ncells, 1);
+  mark(s, "k_zero_int");
+  k_scatter<<<nblk(K.N, T), T, 0, s>>>(P, K);
+  mark(s, "k_scatter");
+  k_sort_cells<<<nblk(K.ncells, T), T, 0, s>>>(P, K);
+  mark(s, "k_sort_cells");
+  dim3 g(nblk(K.N, T), NF64_PERSIST + NI32_PERSIST);
+  k_permute<<<g, T, 0, s>>>(P, K, fscratch, iscratch);
+  mark(s, "k_permute");
+  k_copy_back<<<152 * 8, 512, 0, s>>>(P, K, fscratch, iscratch);
+  mark(s, "k_copy_back");
+  k_after_permute<<<nblk(K.N, T), T, 0, s>>>(P, K);
+  mark(s, "k_after_permute");
+  k_nbr_fill<<<nblk(K.N, 128), 128, 0, s>>>(P, K);
+  mark(s, "k_nbr_fill");
+  if (K.contact) {
+    k_surface<<<nblk(K.N, T), T, 0, s>>>(P, K);
+    mark(s, "k_surface");
+    k_contact_pairs<<<nblk(K.N, 128), 128, 0, s>>>(P, K);
+    mark(s, "k_contact_pairs");
+  }
+}
+
+}  // namespace wf

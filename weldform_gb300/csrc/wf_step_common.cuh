@@ -1,0 +1,136 @@
+// Device helpers shared by the plain and mixed step kernels.
+#pragma once
+#include "wf_device.cuh"
+
+namespace wf {
+
+constexpr double WF_PI = 3.14159265358979323846;
+constexpr double MIN_PS_FOR_NBSEARCH = 1.e-6;  // Source/Domain.cpp:28
+constexpr int BLOCK = 256;                      // threads of the per-particle kernels
+
+__device__ __forceinline__ double col(const DevPtrs& P, int c, size_t N, int i) { return P.f[(size_t)c * N + i]; }
+__device__ __forceinline__ double& colw(const DevPtrs& P, int c, size_t N, int i) { return P.f[(size_t)c * N + i]; }
+__device__ __forceinline__ int icol(const DevPtrs& P, int c, size_t N, int i) { return P.i[(size_t)c * N + i]; }
+
+// Deterministic block reduction (fixed shuffle tree, then fixed order across
+// warps) of one value per thread; the result is valid in thread 0.
+template <int OP>  // 0 sum, 1 max, 2 min
+__device__ __forceinline__ double block_reduce(double v, double* sh) {
+  for (int off = 16; off > 0; off >>= 1) {
+    double o = __shfl_down_sync(0xffffffffu, v, off);
+    v = (OP == 0) ? v + o : (OP == 1 ? fmax(v, o) : fmin(v, o));
+  }
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nw = blockDim.x >> 5;
+    double r = sh[0];
+    for (int k = 1; k < nw; ++k) r = (OP == 0) ? r + sh[k] : (OP == 1 ? fmax(r, sh[k]) : fmin(r, sh[k]));
+    v = r;
+  }
+  return v;
+}
+
+// Amplitude lookup (SPH::amplitude::getValAtTime, Source/Domain.h:69-89).
+__device__ __forceinline__ double amp_value(const DomainTables* T, int amp_id, double t, bool* found) {
+  for (int k = 0; k < T->namp; ++k) {
+    if (T->amp[k].id != amp_id) continue;
+    *found = true;
+    const double* tt = T->amp_t + T->amp[k].offset;
+    const double* vv = T->amp_v + T->amp[k].offset;
+    int i = T->amp[k].n - 1;
+    bool end = false;
+    while (!end) { i--; if (i == 0 || t > tt[i]) end = true; }
+    return vv[i] + (vv[i + 1] - vv[i]) / (tt[i + 1] - tt[i]) * (t - tt[i]);
+  }
+  return 0.0;
+}
+
+// Johnson-Cook flow stress (Source/Material.cpp:6-25).
+__device__ __forceinline__ double jc_yield(const MaterialDev& M, double strain, double strain_rate, double temp) {
+  double T_h = (temp - M.T_t) / (M.T_m - M.T_t);
+  double f = 1.0;
+  if (strain_rate > M.eps_0) f = (1.0 + M.C * log(strain_rate / M.eps_0));
+  return (M.A + M.B * pow(strain, M.n)) * f * (1.0 - pow(T_h, M.jm));
+}
+// Hollomon flow stress with plateau (Source/Material.cpp:59-64).
+__device__ __forceinline__ double hollomon_yield(const MaterialDev& M, double strain) {
+  if (strain + M.eps0 > M.eps1) return M.K * pow(strain + M.eps0, M.m);
+  return M.sy0;
+}
+
+// Radial-return constitutive update of one particle, Particle::CalcStressStrain
+// (Source/Particle.cpp:960-1067), on symmetric storage (xx yy zz xy xz yz).
+// sr: strain rate (6), rr: rotation rate (xy xz yz of the antisymmetric part).
+// Returns dep (plastic strain increment).
+struct StressIO {
+  double tau[6], sig[6], eps[6], epl[6], epli[6];
+  double pressure, pl_strain, delta_pl_strain, sigmay, Ep, esr;
+};
+__device__ __forceinline__ double stress_update(StressIO& s, const double sr[6], const double rr[3], double rho,
+                                                double rho0, double Cs, double P0, double G, double T, int fail,
+                                                int model, const MaterialDev* M, double dt) {
+  s.pressure = P0 + (Cs * Cs) * (rho - rho0);  // EOS case 0, Functions.cpp:206-212
+  // Full matrices: S (symmetric tau), W (antisymmetric rotation rate).
+  double S[3][3] = {{s.tau[0], s.tau[3], s.tau[4]}, {s.tau[3], s.tau[1], s.tau[5]}, {s.tau[4], s.tau[5], s.tau[2]}};
+  double W[3][3] = {{0.0, rr[0], rr[1]}, {-rr[0], 0.0, rr[2]}, {-rr[1], -rr[2], 0.0}};
+  // SRT = S W^T, RS = W S; entries summed k = 2, 1, 0 (matvec.h Mult order).
+  const int ui[6] = {0, 1, 2, 0, 0, 1}, uj[6] = {0, 1, 2, 1, 2, 2};
+  double tr = sr[0] + sr[1] + sr[2];
+  double s3 = 1.0 / 3.0 * tr;
+  double twoG = 2.0 * G;
+  double t6[6];
+  for (int c = 0; c < 6; ++c) {
+    int a = ui[c], b = uj[c];
+    double srt = S[a][2] * W[b][2] + S[a][1] * W[b][1] + S[a][0] * W[b][0];
+    double rs = W[a][2] * S[2][b] + W[a][1] * S[1][b] + W[a][0] * S[0][b];
+    double dev = sr[c] - (c < 3 ? s3 : 0.0);
+    t6[c] = dt * (twoG * dev + srt + rs) + s.tau[c];
+  }
+  double d01 = sr[0] - sr[1], d12 = sr[1] - sr[2], d20 = sr[2] - sr[0];
+  s.esr = sqrt(0.5 * (d01 * d01 + d12 * d12 + d20 * d20) + 3.0 * (sr[3] * sr[3] + sr[5] * sr[5] + sr[4] * sr[4]));
+  double dep = 0.0;
+  if (fail == 1) {
+    double J2 = 0.5 * (t6[0] * t6[0] + 2.0 * t6[3] * t6[3] + 2.0 * t6[4] * t6[4] + t6[1] * t6[1] +
+                       2.0 * t6[5] * t6[5] + t6[2] * t6[2]);
+    double sig_trial = sqrt(3.0 * J2);
+    double ratio = s.sigmay / sig_trial;
+    double sc = (1.0 < ratio) ? 1.0 : ratio;  // std::min(ratio, 1.0)
+    for (int c = 0; c < 6; ++c) t6[c] = sc * t6[c];
+    if (model == 1 && M) s.sigmay = hollomon_yield(*M, s.pl_strain);
+    else if (model == 2 && M) s.sigmay = jc_yield(*M, s.pl_strain, s.esr, T);
+    if (sig_trial > s.sigmay) {
+      if (s.Ep < 0) s.Ep = M ? M->E : 0.0;
+      dep = (sig_trial - s.sigmay) / (3. * G + s.Ep);
+      s.pl_strain += dep;
+      s.delta_pl_strain = dep;
+      if (model == 0) s.sigmay += dep * s.Ep;
+    }
+  }
+  for (int c = 0; c < 6; ++c) s.tau[c] = t6[c];
+  for (int c = 0; c < 6; ++c) s.sig[c] = (c < 3 ? -s.pressure : 0.0) + t6[c];
+  if (dep > 0.0) {
+    double f = dep / s.sigmay;
+    s.epli[0] = f * (s.sig[0] - 0.5 * (s.sig[1] + s.sig[2]));
+    s.epli[1] = f * (s.sig[1] - 0.5 * (s.sig[0] + s.sig[2]));
+    s.epli[2] = f * (s.sig[2] - 0.5 * (s.sig[0] + s.sig[1]));
+    s.epli[3] = 1.5 * f * s.sig[3];
+    s.epli[4] = 1.5 * f * s.sig[4];
+    s.epli[5] = 1.5 * f * s.sig[5];
+    for (int c = 0; c < 6; ++c) s.epl[c] = s.epl[c] + s.epli[c];
+  }
+  for (int c = 0; c < 6; ++c) s.eps[c] = dt * sr[c] + s.eps[c];
+  return dep;
+}
+
+// Plastic work heat source (Particle::CalcPlasticWorkHeat, Particle.cpp:922-939):
+// q = Sigma : (Strain_pl_incr / dt) with the off-diagonal pairs doubled.
+__device__ __forceinline__ double plastic_heat(const double sig[6], const double epli[6], double dt) {
+  double f = 1. / dt;
+  return sig[0] * (f * epli[0]) + 2.0 * sig[3] * (f * epli[3]) + 2.0 * sig[4] * (f * epli[4]) + sig[1] * (f * epli[1]) +
+         2.0 * sig[5] * (f * epli[5]) + sig[2] * (f * epli[2]);
+}
+
+}  // namespace wf

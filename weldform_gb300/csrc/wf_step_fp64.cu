@@ -1,0 +1,669 @@
+// Plain FP64 form of one kick-drift step (Domain::SolveDiffUpdateKickDrift,
+// Source/SolverKickDrift.cpp:117-393) on sm_103a.
+//
+// Launch sequence of one step (all on the domain's stream, no host sync):
+//   k_schedule          neighbour-search decision (SolverKickDrift.cpp:153-186)
+//   [search pipeline]   gated on the decision (wf_nbsearch.cu)
+//   k_accel             CalcAccel + AccelReduction (InteractionAlt.cpp:12-260)
+//   k_bc                GeneralAfter (WeldForm.cpp:51-120)
+//   k_contact_kick      CalcContactForcesWang (Contact_Wang.cpp:15-348) + v += a dt/2
+//   k_bc
+//   k_density_drift     CalcDensInc + DensReduction (InteractionAlt.cpp:483-640),
+//                       rho += dt drho, x += v dt, v += a dt/2 (SolverKickDrift.cpp:236-265)
+//   k_bc                (on the next-step velocity buffer)
+//   k_rate_stress       CalcRateTensors + RateTensorsReduction (InteractionAlt.cpp:263-479),
+//                       CalcStressStrain (Particle.cpp:960-1067), CalcPlasticWorkHeat
+//                       (ThermalStuct.cpp:14-39), T += dt dTdt (Thermal.cpp:727-734)
+//   k_energy            CalcTempInc (Thermal.cpp:53-219), CalcThermalExpStrainRate,
+//                       CalcKinEnergyEqn / CalcIntEnergyEqn (Domain.cpp:1752-1829)
+//   k_finalize          deterministic reduction of the per-block partial sums
+//   k_mesh_*            TriMesh::Update (Mesh.cpp:273-293), UpdateContactParticles
+//                       (Contact.cpp:41-55)
+//   k_step_end          Time += dt and the neighbour-clear schedule (:299-324)
+//
+// Each gather kernel runs one thread per particle over its neighbour row in
+// canonical order; a pair term is evaluated from the particle's own side
+// (x_i - x_j), which equals the reference's (min, max)-ordered pair value
+// with the reduction's sign applied.
+#include "wf_step_common.cuh"
+#include "wf_launch.h"
+
+namespace wf {
+
+thread_local KernelTimer* g_timer = nullptr;
+thread_local long long g_launches = 0;
+
+static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------- schedule
+__global__ void k_schedule(DevPtrs P, DomainConst K) {
+  StepState* s = P.st;
+  double mx = s->max_pl_next;
+  s->max_pl = mx;
+  int search = 0;
+  if (mx > MIN_PS_FOR_NBSEARCH && !s->isyielding) {  // first yield
+    search = 1;
+    s->isyielding = 1;
+  } else if ((mx > MIN_PS_FOR_NBSEARCH || s->isfirst) && s->ts_i == 0 && s->nb_cleared) {
+    search = 1;
+  }
+  if (search) s->nb_cleared = 0;
+  s->do_search = search;
+}
+
+__global__ void k_step_end(DevPtrs P, DomainConst K) {
+  StepState* s = P.st;
+  s->steps += 1;
+  s->Time += s->deltat;
+  s->isfirst = 0;
+  if (s->max_pl > MIN_PS_FOR_NBSEARCH) {
+    if (s->ts_i == (K.ts_nb_inc - 1)) s->nb_cleared = 1;
+    s->ts_i++;
+    if (s->ts_i > (K.ts_nb_inc - 1)) s->ts_i = 0;
+  }
+  s->do_search = 0;
+}
+
+// ---------------------------------------------------------------- geometry
+struct PairGeo {
+  double x0, x1, x2;  // x_i - x_j
+  double r2, r, hh, GK;
+};
+// Pair geometry: h = (hi + hj) / 2, q = rij / h, cubic-spline GradKernel
+// (Functions.cpp:74-87) evaluated as (C / h) * g(q) with g(q) = -3 + 9/4 q for
+// q < 1 and -3/4 (2 - q)^2 / q for 1 <= q < 2.
+__device__ __forceinline__ PairGeo pair_geo(double xi0, double xi1, double xi2, double hi, double xj0, double xj1,
+                                           double xj2, double hj) {
+  PairGeo g;
+  g.x0 = xi0 - xj0; g.x1 = xi1 - xj1; g.x2 = xi2 - xj2;
+  g.r2 = g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2;
+  g.r = sqrt(g.r2);
+  g.hh = (hi + hj) / 2;
+  double inv_h = 1.0 / g.hh;
+  double q = g.r * inv_h;
+  double h2 = g.hh * g.hh;
+  double C = 1.0 / (h2 * h2 * WF_PI);
+  if (q == 0.0) g.GK = C * inv_h * -3.0;
+  else if (q < 1.0) g.GK = C * inv_h * (-3.0 + 2.25 * q);
+  else if (q < 2.0) { double t = 2.0 - q; g.GK = C / (q * g.hh) * (-0.75 * t * t); }
+  else g.GK = 0.0;
+  return g;
+}
+
+// ---------------------------------------------------------------- accel
+__global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  if (icol(P, I_KIND, N, i) != 0) {  // StartAcceleration resets a for every particle
+    colw(P, C_A, N, i) = 0.0; colw(P, C_A + 1, N, i) = 0.0; colw(P, C_A + 2, N, i) = 0.0;
+    return;
+  }
+  double xi0 = col(P, C_X, N, i), xi1 = col(P, C_X + 1, N, i), xi2 = col(P, C_X + 2, N, i);
+  double vi0 = col(P, C_V, N, i), vi1 = col(P, C_V + 1, N, i), vi2 = col(P, C_V + 2, N, i);
+  double hi = col(P, C_H, N, i), rhoi = col(P, C_RHO, N, i), csi = col(P, C_CS, N, i);
+  double ai = col(P, C_ALPHA, N, i), bi = col(P, C_BETA, N, i);
+  double Si[6];
+  for (int c = 0; c < 6; ++c) Si[c] = col(P, C_SRHO + c, N, i);
+  double a0 = 0, a1 = 0, a2 = 0;
+  int len = P.row_len[i];
+  for (int k = 0; k < len; ++k) {
+    int j = P.nbr[(size_t)k * N + i];
+    PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+                         col(P, C_H, N, j));
+    double Alpha = (ai + col(P, C_ALPHA, N, j)) / 2.0, Beta = (bi + col(P, C_BETA, N, j)) / 2.0;
+    double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
+    double PIs = 0.0;
+    if (Alpha != 0.0 || Beta != 0.0) {
+      double dvx = v0 * g.x0 + v1 * g.x1 + v2 * g.x2;
+      if (dvx < 0) {
+        double MU = g.hh * dvx / (g.r * g.r + 0.01 * g.hh * g.hh);
+        double Cij = 0.5 * (csi + col(P, C_CS, N, j));
+        PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5 * (rhoi + col(P, C_RHO, N, j)));
+      }
+    }
+    double S0 = Si[0] + col(P, C_SRHO + 0, N, j) + PIs;
+    double S1 = Si[1] + col(P, C_SRHO + 1, N, j) + PIs;
+    double S2 = Si[2] + col(P, C_SRHO + 2, N, j) + PIs;
+    double S3 = Si[3] + col(P, C_SRHO + 3, N, j);
+    double S4 = Si[4] + col(P, C_SRHO + 4, N, j);
+    double S5 = Si[5] + col(P, C_SRHO + 5, N, j);
+    double g0 = g.GK * g.x0, g1 = g.GK * g.x1, g2 = g.GK * g.x2;
+    double t0 = g0 * S0 + g1 * S3 + g2 * S4;
+    double t1 = g0 * S3 + g1 * S1 + g2 * S5;
+    double t2 = g0 * S4 + g1 * S5 + g2 * S2;
+    double mj = col(P, C_MASS, N, j);
+    a0 += mj * t0; a1 += mj * t1; a2 += mj * t2;
+  }
+  colw(P, C_A, N, i) = a0; colw(P, C_A + 1, N, i) = a1; colw(P, C_A + 2, N, i) = a2;
+}
+
+// ---------------------------------------------------------------- BCs
+// GeneralAfter: particles whose ID matches a velocity BC get a = 0 and
+// v = value (constant or amplitude); rigid meshes with that id get m_v.
+__global__ void k_bc(DevPtrs P, DomainConst K, int vcol) {
+  const DomainTables* T = P.tab;
+  double t = P.st->Time;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && K.contact) {
+    for (int b = 0; b < T->nbc; ++b)
+      for (int m = 0; m < K.nmeshes; ++m)
+        if (K.contact_surf_id[m] == T->bc[b].zone) {
+          if (T->bc[b].value_type == 0) {
+            for (int d = 0; d < 3; ++d) { P.st->mesh_v[m][d] = T->bc[b].value[d]; P.st->mesh_w[m][d] = T->bc[b].value_ang[d]; }
+          } else {
+            bool found = false;
+            double val = T->bc[b].amp_factor * amp_value(T, T->bc[b].amp_id, t, &found);
+            if (found) for (int d = 0; d < 3; ++d) P.st->mesh_v[m][d] = val * T->bc[b].value[d];
+          }
+        }
+  }
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K.nbc_particles) return;
+  size_t N = K.N;
+  int i = P.inv[P.bc_list[k]];
+  int id = icol(P, I_ID, N, i);
+  for (int b = 0; b < T->nbc; ++b) {
+    if (T->bc[b].zone != id) continue;
+    if (T->bc[b].value_type == 0) {
+      for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = T->bc[b].value[d]; }
+    } else {
+      bool found = false;
+      double val = T->bc[b].amp_factor * amp_value(T, T->bc[b].amp_id, t, &found);
+      if (found)
+        for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = val * T->bc[b].value[d]; }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- contact + kick
+__device__ __forceinline__ double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+__device__ __forceinline__ double norm3(const double a[3]) { return sqrt(dot3(a, a)); }
+
+__global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K) {
+  __shared__ double sh[32];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  size_t N = K.N;
+  double dt = K.dt;
+  double cfsum = 0, crsum = 0, extw = 0;
+  double cfv[MAX_MESHES][3];
+  for (int m = 0; m < MAX_MESHES; ++m) cfv[m][0] = cfv[m][1] = cfv[m][2] = 0.0;
+  if (i < K.N) {
+    int kind = icol(P, I_KIND, N, i);
+    double a[3] = {col(P, C_A, N, i), col(P, C_A + 1, N, i), col(P, C_A + 2, N, i)};
+    if (K.contact) {
+      double cf[3] = {0, 0, 0}, dcont = 0.0;
+      int ncp = kind == 0 ? P.cp_len[i] : 0;
+      if (ncp > 0) {
+        double x[3] = {col(P, C_X, N, i), col(P, C_X + 1, N, i), col(P, C_X + 2, N, i)};
+        double v[3] = {col(P, C_V, N, i), col(P, C_V + 1, N, i), col(P, C_V + 2, N, i)};
+        double m1 = col(P, C_MASS, N, i), h1 = col(P, C_H, N, i);
+        for (int k = 0; k < ncp; ++k) {
+          int p2 = P.cp[(size_t)k * N + i];
+          double n2[3] = {col(P, C_NORMAL, N, p2), col(P, C_NORMAL + 1, N, p2), col(P, C_NORMAL + 2, N, p2)};
+          double v2[3] = {col(P, C_V, N, p2), col(P, C_V + 1, N, p2), col(P, C_V + 2, N, p2)};
+          double vr[3] = {v[0] - v2[0], v[1] - v2[1], v[2] - v2[2]};
+          double delta_ = -dot3(n2, vr);
+          int e = icol(P, I_ELEM, N, p2);
+          int m = icol(P, I_MESH, N, p2);
+          double xp[3];
+          for (int d = 0; d < 3; ++d) xp[d] = x[d] + v[d] * dt + a[d] * dt * dt / 2.0;
+          double dist = dot3(n2, xp) - P.elem_pplane[e];
+          if (!(dist < h1)) continue;
+          double qj[3] = {x[0] - dist * n2[0], x[1] - dist * n2[1], x[2] - dist * n2[2]};
+          bool inside = true;
+          for (int ii = 0; ii < 3 && inside; ++ii) {
+            int jj = ii + 1; if (jj > 2) jj = 0;
+            int na = P.elem_node[3 * e + ii], nb = P.elem_node[3 * e + jj];
+            double pa[3] = {P.node[na], P.node[P.nnodes + na], P.node[2 * P.nnodes + na]};
+            double pb[3] = {P.node[nb], P.node[P.nnodes + nb], P.node[2 * P.nnodes + nb]};
+            double u[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+            double w[3] = {qj[0] - pa[0], qj[1] - pa[1], qj[2] - pa[2]};
+            double c[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+            if (dot3(c, n2) < 0.0) inside = false;
+          }
+          if (!inside) continue;
+          double delta = h1 - dist;
+          double kij;
+          if (K.contact_alg == 1) {
+            double rho1 = col(P, C_RHO0, N, i), cs = col(P, C_CS, N, i), G = col(P, C_G, N, i);
+            double bulk = cs * cs * rho1;
+            double dS = pow(m1 / rho1, 0.33333);
+            kij = K.PFAC * (9. * bulk * G / (3. * bulk + G) * dS);
+          } else if (K.contact_alg == 2) {
+            kij = K.PFAC * pow(m1 / col(P, C_RHO, N, i), 2.0 / 3.0);
+          } else {
+            kij = 2.0 * m1 / (dt * dt);
+          }
+          double omega = sqrt(kij / m1);
+          double psi = 2. * m1 * omega * K.DFAC;
+          double s = kij * delta - psi * delta_;
+          for (int d = 0; d < 3; ++d) cf[d] = s * n2[d];
+          dcont = delta;
+          for (int d = 0; d < 3; ++d) a[d] = a[d] + cf[d] / m1;
+          if (K.friction_sta > 0.) {
+            double du[3];
+            for (int d = 0; d < 3; ++d) du[d] = (xp[d] - x[d]) - v2[d] * dt;
+            double dn = dot3(du, n2);
+            double tg[3];
+            for (int d = 0; d < 3; ++d) tg[d] = kij * (du[d] - dn * n2[d]);
+            double ntg = norm3(tg), ncf = norm3(cf);
+            if (ntg < K.friction_sta * ncf) {
+              for (int d = 0; d < 3; ++d) { double q = tg[d] / m1; cf[d] -= q; a[d] -= q; }
+            } else {
+              double fs = K.friction_dyn * ncf;
+              for (int d = 0; d < 3; ++d) { double td = fs * tg[d] / ntg; cf[d] -= td; a[d] -= td / m1; }
+            }
+          }
+          cfsum += norm3(cf);
+          if (m < MAX_MESHES) for (int d = 0; d < 3; ++d) cfv[m][d] += cf[d];
+          crsum += dot3(a, n2) * m1;
+          extw += dot3(cf, v2);
+        }
+      }
+      for (int d = 0; d < 3; ++d) colw(P, C_CF + d, N, i) = cf[d];
+      colw(P, C_DCONT, N, i) = dcont;
+      for (int d = 0; d < 3; ++d) colw(P, C_A + d, N, i) = a[d];
+    }
+    if (kind == 0) {  // half kick v += a * 0.5 * dt (rigid-mesh particles have a = 0)
+      for (int d = 0; d < 3; ++d) colw(P, C_V + d, N, i) = col(P, C_V + d, N, i) + a[d] * 0.5 * dt;
+    }
+  }
+  if (K.contact) {
+    double r;
+    r = block_reduce<0>(cfsum, sh); if (threadIdx.x == 0) P.partials[S_CFSUM * K.nblocks + blockIdx.x] = r;
+    r = block_reduce<0>(crsum, sh); if (threadIdx.x == 0) P.partials[S_CRSUM * K.nblocks + blockIdx.x] = r;
+    r = block_reduce<0>(extw, sh); if (threadIdx.x == 0) P.partials[S_EXTW * K.nblocks + blockIdx.x] = r;
+    for (int m = 0; m < K.nmeshes && m < MAX_MESHES; ++m)
+      for (int d = 0; d < 3; ++d) {
+        r = block_reduce<0>(cfv[m][d], sh);
+        if (threadIdx.x == 0) P.partials[(S_CFVEC + 3 * m + d) * K.nblocks + blockIdx.x] = r;
+      }
+  }
+}
+
+// ---------------------------------------------------------------- density + drift + kick
+__global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  double dt = K.dt;
+  double xi0 = col(P, C_X, N, i), xi1 = col(P, C_X + 1, N, i), xi2 = col(P, C_X + 2, N, i);
+  double vi0 = col(P, C_V, N, i), vi1 = col(P, C_V + 1, N, i), vi2 = col(P, C_V + 2, N, i);
+  double rhoi = col(P, C_RHO, N, i);
+  double dd = 0.0;
+  if (icol(P, I_KIND, N, i) == 0) {
+    double hi = col(P, C_H, N, i);
+    int len = P.row_len[i];
+    for (int k = 0; k < len; ++k) {
+      int j = P.nbr[(size_t)k * N + i];
+      PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+                           col(P, C_H, N, j));
+      double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
+      double pd = v0 * (g.GK * g.x0) + v1 * (g.GK * g.x1) + v2 * (g.GK * g.x2);
+      dd += col(P, C_MRHO, N, j) * pd;
+    }
+    dd *= rhoi;
+  }
+  colw(P, C_DRHO, N, i) = dd;
+  double rn = rhoi + dt * dd;
+  colw(P, C_RHON, N, i) = rn;
+  colw(P, C_MRHON, N, i) = icol(P, I_KIND, N, i) == 0 ? col(P, C_MASS, N, i) / rn : 0.0;
+  double v[3] = {vi0, vi1, vi2}, x[3] = {xi0, xi1, xi2};
+  for (int d = 0; d < 3; ++d) {
+    double du = v[d] * dt;
+    colw(P, C_DISP + d, N, i) = col(P, C_DISP + d, N, i) + du;
+    colw(P, C_XN + d, N, i) = x[d] + du;
+    colw(P, C_VN + d, N, i) = v[d] + col(P, C_A + d, N, i) * dt / 2.;
+  }
+}
+
+// ---------------------------------------------------------------- rate + stress
+__global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K) {
+  __shared__ double sh[32];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  size_t N = K.N;
+  double dt = K.dt;
+  double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300;
+  if (i < K.N) {
+    // Next-step buffers become the current state for this particle.
+    double x[3], v[3];
+    for (int d = 0; d < 3; ++d) { x[d] = col(P, C_XN + d, N, i); v[d] = col(P, C_VN + d, N, i); }
+    double rho = col(P, C_RHON, N, i);
+    for (int d = 0; d < 3; ++d) { colw(P, C_X + d, N, i) = x[d]; colw(P, C_V + d, N, i) = v[d]; }
+    colw(P, C_RHO, N, i) = rho;
+    colw(P, C_MRHO, N, i) = col(P, C_MRHON, N, i);
+    maxpl = col(P, C_PLS, N, i);
+    if (icol(P, I_KIND, N, i) == 0) {
+      double hi = col(P, C_H, N, i);
+      double sr[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};
+      int len = P.row_len[i];
+      for (int k = 0; k < len; ++k) {
+        int j = P.nbr[(size_t)k * N + i];
+        PairGeo g = pair_geo(x[0], x[1], x[2], hi, col(P, C_XN, N, j), col(P, C_XN + 1, N, j), col(P, C_XN + 2, N, j),
+                             col(P, C_H, N, j));
+        double b0 = v[0] - col(P, C_VN, N, j), b1 = v[1] - col(P, C_VN + 1, N, j), b2 = v[2] - col(P, C_VN + 2, N, j);
+        double f = -0.5 * g.GK;
+        double w = col(P, C_MRHON, N, j);
+        sr[0] += w * (f * (2.0 * b0 * g.x0));
+        sr[1] += w * (f * (2.0 * b1 * g.x1));
+        sr[2] += w * (f * (2.0 * b2 * g.x2));
+        sr[3] += w * (f * (b0 * g.x1 + b1 * g.x0));
+        sr[4] += w * (f * (b0 * g.x2 + b2 * g.x0));
+        sr[5] += w * (f * (b1 * g.x2 + b2 * g.x1));
+        rr[0] += w * (f * (b0 * g.x1 - b1 * g.x0));
+        rr[1] += w * (f * (b0 * g.x2 - b2 * g.x0));
+        rr[2] += w * (f * (b1 * g.x2 - b2 * g.x1));
+      }
+      StressIO s;
+      for (int c = 0; c < 6; ++c) {
+        s.tau[c] = col(P, C_TAU + c, N, i); s.eps[c] = col(P, C_EPS + c, N, i);
+        s.epl[c] = col(P, C_EPL + c, N, i); s.epli[c] = col(P, C_EPLI + c, N, i);
+      }
+      s.pl_strain = col(P, C_PLS, N, i); s.delta_pl_strain = col(P, C_DPLS, N, i);
+      s.sigmay = col(P, C_SY, N, i); s.Ep = col(P, C_EP, N, i);
+      int mi = icol(P, I_MAT, N, i);
+      const MaterialDev* M = (mi >= 0 && mi < P.tab->nmat) ? &P.tab->mat[mi] : nullptr;
+      double T = col(P, C_T, N, i);
+      stress_update(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i), col(P, C_G, N, i), T,
+                    icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), M, dt);
+      for (int c = 0; c < 6; ++c) {
+        colw(P, C_TAU + c, N, i) = s.tau[c]; colw(P, C_SIG + c, N, i) = s.sig[c];
+        colw(P, C_EPS + c, N, i) = s.eps[c]; colw(P, C_EPL + c, N, i) = s.epl[c];
+        colw(P, C_EPLI + c, N, i) = s.epli[c]; colw(P, C_SR + c, N, i) = sr[c];
+      }
+      for (int c = 0; c < 3; ++c) colw(P, C_RR + c, N, i) = rr[c];
+      colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
+      colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = s.esr;
+      maxpl = s.pl_strain;
+      double c2 = 1.0 / (rho * rho);
+      for (int c = 0; c < 6; ++c) colw(P, C_SRHO + c, N, i) = c2 * s.sig[c];
+      colw(P, C_PR2, N, i) = s.pressure / (rho * rho);
+      if (K.pl_heating) {
+        double q = col(P, C_QPL, N, i);
+        if (s.delta_pl_strain > 0.0) q = plastic_heat(s.sig, s.epli, dt);
+        colw(P, C_QPL, N, i) = q;
+        colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + q * dt;
+        plw = col(P, C_MASS, N, i) / rho * q;
+      }
+      if (K.thermal_solver) {
+        T += dt * col(P, C_DTDT, N, i);
+        colw(P, C_T, N, i) = T;
+        maxT = T; minT = T;
+      }
+    }
+  }
+  double r;
+  r = block_reduce<1>(maxpl, sh); if (threadIdx.x == 0) P.partials[S_MAXPL * K.nblocks + blockIdx.x] = r;
+  if (K.pl_heating) { r = block_reduce<0>(plw, sh); if (threadIdx.x == 0) P.partials[S_PLW * K.nblocks + blockIdx.x] = r; }
+  if (K.thermal_solver) {
+    r = block_reduce<1>(maxT, sh); if (threadIdx.x == 0) P.partials[S_MAXT * K.nblocks + blockIdx.x] = r;
+    r = block_reduce<2>(minT, sh); if (threadIdx.x == 0) P.partials[S_MINT * K.nblocks + blockIdx.x] = r;
+  }
+}
+
+// ---------------------------------------------------------------- energies (+ conduction)
+__global__ void __launch_bounds__(BLOCK) k_energy(DevPtrs P, DomainConst K) {
+  __shared__ double sh[32];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  size_t N = K.N;
+  double dkin = 0.0, dint = 0.0;
+  if (i < K.N && icol(P, I_KIND, N, i) == 0) {
+    double x0 = col(P, C_X, N, i), x1 = col(P, C_X + 1, N, i), x2 = col(P, C_X + 2, N, i);
+    double v0 = col(P, C_V, N, i), v1 = col(P, C_V + 1, N, i), v2 = col(P, C_V + 2, N, i);
+    double hi = col(P, C_H, N, i), mi = col(P, C_MASS, N, i), mrhoi = col(P, C_MRHO, N, i);
+    double pri = col(P, C_PR2, N, i);
+    double Ti = col(P, C_T, N, i), ki = col(P, C_KT, N, i);
+    double cond = 0.0;
+    int len = P.row_len[i], split = P.row_split[i];
+    for (int k = 0; k < len; ++k) {
+      int j = P.nbr[(size_t)k * N + i];
+      PairGeo g = pair_geo(x0, x1, x2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+                           col(P, C_H, N, j));
+      double b0 = v0 - col(P, C_V, N, j), b1 = v1 - col(P, C_V + 1, N, j), b2 = v2 - col(P, C_V + 2, N, j);
+      double dv = b0 * (g.GK * g.x0) + b1 * (g.GK * g.x1) + b2 * (g.GK * g.x2);
+      bool up = k < split;  // original index of j larger than i's
+      // CalcKinEnergyEqn pair (P1 = smaller original index): 0.5 m_P2 (p1/d1^2 + p2/d2^2) v12.(GK x12)
+      double pk = 0.5 * (up ? col(P, C_MASS, N, j) : mi) * (pri + col(P, C_PR2, N, j)) * dv;
+      dkin += up ? pk : -pk;
+      if (K.thermal_solver) {
+        double kj = col(P, C_KT, N, j);
+        double w = up ? col(P, C_MRHO, N, j) : mrhoi;  // m_P2 / rho_P2 for both ends
+        double dxx = g.x0 * (g.GK * g.x0) + g.x1 * (g.GK * g.x1) + g.x2 * (g.GK * g.x2);
+        cond += w * 4. * (ki * kj) / (ki + kj) * (Ti - col(P, C_T, N, j)) * dxx / (g.r * g.r);
+      }
+    }
+    double sr[6];
+    for (int c = 0; c < 6; ++c) sr[c] = col(P, C_SR + c, N, i);
+    if (K.thermal_solver) {
+      double rho = col(P, C_RHO, N, i);
+      double f = 1. / (rho * col(P, C_CPT, N, i));
+      double dTdt = f * (cond + 0.0 + col(P, C_QSRC, N, i) + col(P, C_QPL, N, i) * K.pl_work_heat_frac + 0.0);
+      colw(P, C_DTDT, N, i) = dTdt;
+      double s = col(P, C_THEXP, N, i) * dTdt;
+      for (int c = 0; c < 3; ++c) { sr[c] = sr[c] + s; colw(P, C_SR + c, N, i) = sr[c]; }
+    }
+    double t[6];
+    for (int c = 0; c < 6; ++c) t[c] = col(P, C_TAU + c, N, i);
+    dint = mrhoi * (t[0] * sr[0] + 2.0 * t[3] * sr[3] + 2.0 * t[4] * sr[4] + t[1] * sr[1] + 2.0 * t[5] * sr[5] +
+                    t[2] * sr[2]);
+    colw(P, C_DKIN, N, i) = dkin;
+    colw(P, C_DINT, N, i) = dint;
+  }
+  double r;
+  r = block_reduce<0>(dkin, sh); if (threadIdx.x == 0) P.partials[S_DKIN * K.nblocks + blockIdx.x] = r;
+  r = block_reduce<0>(dint, sh); if (threadIdx.x == 0) P.partials[S_DINT * K.nblocks + blockIdx.x] = r;
+}
+
+// ---------------------------------------------------------------- reductions
+// One block per slot; each thread sums a fixed strided subset, then a fixed tree.
+__global__ void k_finalize(DevPtrs P, DomainConst K) {
+  __shared__ double sh[1024];
+  int slot = blockIdx.x;
+  bool active = (slot == S_DINT || slot == S_DKIN || slot == S_MAXPL) ||
+                (K.pl_heating && slot == S_PLW) || (K.thermal_solver && (slot == S_MAXT || slot == S_MINT)) ||
+                (K.contact && (slot == S_CFSUM || slot == S_CRSUM || slot == S_EXTW ||
+                               (slot >= S_CFVEC && slot < S_CFVEC + 3 * K.nmeshes)));
+  if (!active) return;
+  int op = (slot == S_MAXPL || slot == S_MAXT) ? 1 : (slot == S_MINT ? 2 : 0);
+  double acc = op == 1 ? -1e300 : (op == 2 ? 1e300 : 0.0);
+  const double* src = P.partials + (size_t)slot * K.nblocks;
+  for (int b = threadIdx.x; b < K.nblocks; b += blockDim.x) {
+    double v = src[b];
+    acc = op == 0 ? acc + v : (op == 1 ? fmax(acc, v) : fmin(acc, v));
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      double a = sh[threadIdx.x], b = sh[threadIdx.x + s];
+      sh[threadIdx.x] = op == 0 ? a + b : (op == 1 ? fmax(a, b) : fmin(a, b));
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  double v = sh[0];
+  StepState* st = P.st;
+  double dt = st->deltat;
+  switch (slot) {
+    case S_DINT: st->int_energy_sum += v * dt; break;
+    case S_DKIN: st->kin_energy_sum += v * dt; break;
+    case S_PLW: st->plastic_work += v * dt; break;
+    case S_MAXPL: st->max_pl_next = v; break;
+    case S_MAXT: st->m_maxT = v > 0.0 ? v : 0.0; break;
+    case S_MINT: st->m_minT = v < 1000. ? v : 1000.; break;
+    case S_CFSUM: st->contact_force_sum = v; break;
+    case S_CRSUM: st->contact_reaction_sum = v; break;
+    case S_EXTW: st->ext_forces_work += v * dt; break;
+    default: {
+      int q = slot - S_CFVEC;
+      st->contact_force[q / 3][q % 3] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- rigid meshes
+// TriMesh::Update: node_v = m_v + m_w x node; node += node_v dt.
+__global__ void k_mesh_nodes(DevPtrs P, DomainConst K) {
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nnodes) return;
+  int m = P.node_mesh[n];
+  const double* mv = P.st->mesh_v[m];
+  const double* mw = P.st->mesh_w[m];
+  double p[3] = {P.node[n], P.node[P.nnodes + n], P.node[2 * P.nnodes + n]};
+  double vr[3] = {mw[1] * p[2] - mw[2] * p[1], mw[2] * p[0] - mw[0] * p[2], mw[0] * p[1] - mw[1] * p[0]};
+  if (!K.contact_mesh_auto_update) return;
+  for (int d = 0; d < 3; ++d) {
+    double nv = mv[d] + vr[d];
+    P.node_v[d * P.nnodes + n] = nv;
+    P.node[d * P.nnodes + n] = p[d] + nv * K.dt;
+  }
+}
+// CalcNormals + UpdatePlaneCoeff per element (Mesh.cpp:222-256), then
+// UpdateContactParticles (Contact.cpp:41-55) for the element's particle.
+__global__ void k_mesh_elems(DevPtrs P, DomainConst K) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.nelem) return;
+  int nn = P.nnodes;
+  int n0 = P.elem_node[3 * e], n1 = P.elem_node[3 * e + 1], n2 = P.elem_node[3 * e + 2];
+  size_t N = K.N;
+  int p = P.elem_particle[e];
+  double nrm[3] = {P.elem_normal[e], P.elem_normal[P.nelem + e], P.elem_normal[2 * P.nelem + e]};
+  if (K.contact_mesh_auto_update) {
+    double a[3] = {P.node[n0], P.node[nn + n0], P.node[2 * nn + n0]};
+    double b[3] = {P.node[n1], P.node[nn + n1], P.node[2 * nn + n1]};
+    double c[3] = {P.node[n2], P.node[nn + n2], P.node[2 * nn + n2]};
+    double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, w[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    double cr[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+    double ln = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    for (int d = 0; d < 3; ++d) { nrm[d] = cr[d] / ln; P.elem_normal[d * P.nelem + e] = nrm[d]; }
+    P.elem_pplane[e] = c[0] * nrm[0] + c[1] * nrm[1] + c[2] * nrm[2];  // nfar = last node
+  }
+  for (int d = 0; d < 3; ++d) {
+    double s = 0.0;
+    s = s + P.node_v[d * nn + n0]; s = s + P.node_v[d * nn + n1]; s = s + P.node_v[d * nn + n2];
+    colw(P, C_V + d, N, p) = s / 3;
+    colw(P, C_A + d, N, p) = 0.0;
+    colw(P, C_NORMAL + d, N, p) = nrm[d];
+  }
+}
+
+// ---------------------------------------------------------------- prologue helpers
+__global__ void k_refresh_derived(DevPtrs P, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  if (icol(P, I_KIND, N, i) != 0) {  // rigid-mesh particles carry no mass or density
+    for (int c = 0; c < 6; ++c) colw(P, C_SRHO + c, N, i) = 0.0;
+    colw(P, C_MRHO, N, i) = 0.0;
+    colw(P, C_PR2, N, i) = 0.0;
+    return;
+  }
+  double rho = col(P, C_RHO, N, i);
+  double c2 = 1.0 / (rho * rho);
+  for (int c = 0; c < 6; ++c) colw(P, C_SRHO + c, N, i) = c2 * col(P, C_SIG + c, N, i);
+  colw(P, C_MRHO, N, i) = col(P, C_MASS, N, i) / rho;
+  colw(P, C_PR2, N, i) = col(P, C_P, N, i) / (rho * rho);
+}
+__global__ void k_initial_pressure(DevPtrs P, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  double cs = col(P, C_CS, N, i);
+  colw(P, C_P, N, i) = col(P, C_P0, N, i) + (cs * cs) * (col(P, C_RHO, N, i) - col(P, C_RHO0, N, i));
+}
+__global__ void k_max_pl(DevPtrs P, DomainConst K) {
+  __shared__ double sh[32];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = (i < K.N) ? col(P, C_PLS, (size_t)K.N, i) : 0.0;
+  double r = block_reduce<1>(v, sh);
+  if (threadIdx.x == 0) P.partials[S_MAXPL * K.nblocks + blockIdx.x] = r;
+}
+__global__ void k_max_pl_final(DevPtrs P, DomainConst K) {
+  if (threadIdx.x || blockIdx.x) return;
+  double m = 0.0;
+  for (int b = 0; b < K.nblocks; ++b) m = fmax(m, P.partials[S_MAXPL * K.nblocks + b]);
+  P.st->max_pl_next = m;
+}
+
+void launch_prologue(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
+  k_initial_pressure<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  k_refresh_derived<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  k_max_pl<<<K.nblocks, BLOCK, 0, s>>>(P, K);
+  k_max_pl_final<<<1, 1, 0, s>>>(P, K);
+}
+void launch_refresh_derived(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
+  k_refresh_derived<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+}
+
+// ---------------------------------------------------------------- host transfers
+__global__ void k_gather_orig(DevPtrs P, DomainConst K, const double* colp, double* out, int ncomp) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= K.N) return;
+  int i = P.inv[o];
+  for (int c = 0; c < ncomp; ++c) out[(size_t)o * ncomp + c] = colp[(size_t)c * K.N + i];
+}
+__global__ void k_scatter_orig(DevPtrs P, DomainConst K, const double* in, double* colp, int ncomp) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= K.N) return;
+  int i = P.inv[o];
+  for (int c = 0; c < ncomp; ++c) colp[(size_t)c * K.N + i] = in[(size_t)o * ncomp + c];
+}
+__global__ void k_gather_orig_i32(DevPtrs P, DomainConst K, const int* colp, int* out) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= K.N) return;
+  out[o] = colp[P.inv[o]];
+}
+__global__ void k_scatter_orig_i32(DevPtrs P, DomainConst K, const int* in, int* colp) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= K.N) return;
+  colp[P.inv[o]] = in[o];
+}
+void launch_gather_orig(const DevPtrs& P, const DomainConst& K, const double* c, double* o, int n, cudaStream_t s) {
+  k_gather_orig<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, c, o, n);
+}
+void launch_scatter_orig(const DevPtrs& P, const DomainConst& K, const double* in, double* c, int n, cudaStream_t s) {
+  k_scatter_orig<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, in, c, n);
+}
+void launch_gather_orig_i32(const DevPtrs& P, const DomainConst& K, const int* c, int* o, cudaStream_t s) {
+  k_gather_orig_i32<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, c, o);
+}
+void launch_scatter_orig_i32(const DevPtrs& P, const DomainConst& K, const int* in, int* c, cudaStream_t s) {
+  k_scatter_orig_i32<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, in, c);
+}
+
+// ---------------------------------------------------------------- one step
+void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
+  int nb = nblk(K.N, BLOCK);
+  int nbc = nblk(K.nbc_particles > 0 ? K.nbc_particles : 1, BLOCK);
+  k_schedule<<<1, 1, 0, s>>>(P, K);
+  mark(s, "k_schedule");
+  launch_neighbour_search(P, K, fscratch, iscratch, s);
+  k_accel<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_accel");
+  k_bc<<<nbc, BLOCK, 0, s>>>(P, K, C_V);
+  mark(s, "k_bc");
+  k_contact_kick<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_contact_kick");
+  k_bc<<<nbc, BLOCK, 0, s>>>(P, K, C_V);
+  mark(s, "k_bc");
+  k_density_drift<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_density_drift");
+  k_bc<<<nbc, BLOCK, 0, s>>>(P, K, C_VN);
+  mark(s, "k_bc");
+  k_rate_stress<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_rate_stress");
+  k_energy<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_energy");
+  k_finalize<<<NSLOTS, 1024, 0, s>>>(P, K);
+  mark(s, "k_finalize");
+  if (K.contact && P.nelem > 0) {
+    k_mesh_nodes<<<nblk(P.nnodes, BLOCK), BLOCK, 0, s>>>(P, K);
+    mark(s, "k_mesh_nodes");
+    k_mesh_elems<<<nblk(P.nelem, BLOCK), BLOCK, 0, s>>>(P, K);
+    mark(s, "k_mesh_elems");
+  }
+  k_step_end<<<1, 1, 0, s>>>(P, K);
+  mark(s, "k_step_end");
+}
+
+}  // namespace wf
