@@ -1,0 +1,67 @@
+"""CPU checks of the oracle and the host-side helpers (no GPU)."""
+import numpy as np
+import pytest
+
+from tests._support import oracle_domain, rel_l2
+from weldform_gb300 import configs
+
+
+def test_cylinder_count_matches_generator():
+    for R, L, dx in ((0.010, 0.030, 0.001), (0.004, 0.008, 0.0005), (0.003, 0.006, 0.0003)):
+        d = oracle_domain()
+        d.AddCylinderLength(0, (0, 0, 0), R, L, dx / 2, 7850.0, 1.2 * dx, False)
+        assert d.particle_count == configs.cylinder_count(R, L, dx)
+    # 276 particles per layer x 29 layers at dx = 1 mm (the 30th layer is lost to
+    # the accumulated zp += 2r, Domain.cpp:749-752)
+    assert configs.cylinder_count(0.010, 0.030, 0.001) == 8004
+
+
+def test_jitter_is_deterministic_and_bounded():
+    a = configs.jitter(1000, 0.001)
+    b = configs.jitter(1000, 0.001)
+    assert np.array_equal(a, b)
+    assert np.abs(a).max() <= 1e-6 and np.abs(a).max() > 0.9e-6
+    assert not np.array_equal(a, configs.jitter(1000, 0.001, seed=1))
+
+
+def _run(mode, steps, **kw):
+    d = oracle_domain()
+    d.set("cpu_mode", mode)
+    d.set("cpu_threads", 4)
+    case = configs.cylinder_upsetting(d, **kw)
+    d.prepare(case.dt)
+    d.step(steps)
+    return {f: d.get_array(f) for f in ("x", "Sigma", "pl_strain", "Density")}, d
+
+
+def test_reference_structured_mode_agrees_with_canonical_mode():
+    """Per-thread pair lists + Nishimura gather (the timed CPU baseline) against
+    the canonical gather: only the summation order differs."""
+    kw = dict(R=0.003, L=0.006, dx=0.0005, v_top=-20.0)
+    a, _ = _run(0, 40, **kw)
+    b, _ = _run(1, 40, **kw)
+    assert a["pl_strain"].max() > 0
+    for f in a:
+        assert rel_l2(b[f], a[f]) < 1e-9, f
+
+
+def test_kinetic_energy_rate_cancels_pairwise():
+    """CalcKinEnergyEqn adds +temp / -temp to the two particles of every pair
+    (Domain.cpp:1775-1791), so its global sum is zero up to rounding."""
+    _, d = _run(0, 20, R=0.003, L=0.006, dx=0.0005, v_top=-5.0)
+    assert abs(d.get("kin_energy_sum")) < 1e-9 * max(abs(d.get("int_energy_sum")), 1e-12)
+
+
+def test_yield_triggers_rebuild_schedule():
+    """First yield searches at once; afterwards every ts_nb_inc = 5 steps."""
+    _, d = _run(0, 30, R=0.003, L=0.006, dx=0.0005, v_top=-20.0)
+    n = d.geti("nb_searches")
+    assert 5 <= n <= 8
+
+
+def test_unsupported_features_are_rejected():
+    d = oracle_domain()
+    d.AddCylinderLength(0, (0, 0, 0), 0.003, 0.006, 0.00025, 7850.0, 0.0006, False)
+    d.set_particles("TI", 0.3)
+    with pytest.raises(Exception):
+        d.prepare(1e-8)
