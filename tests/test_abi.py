@@ -43,6 +43,8 @@ def test_oracle_mirrors_the_abi():
     from tests._support import oracle_lib
     lib = oracle_lib()
     for name in declared():
+        if name == "wf_neighbour_list_static":  # product-only helper, no reference counterpart
+            continue
         assert hasattr(lib, "wfo_" + name[3:]), name
 
 

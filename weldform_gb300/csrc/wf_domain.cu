@@ -24,6 +24,14 @@ namespace {
 thread_local std::string g_err;
 int set_err(int code, const std::string& m) { g_err = m; return code; }
 
+}  // namespace
+
+namespace wf {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace wf
+
+namespace {
+
 struct CudaError { int code; std::string msg; };
 #define CK(call)                                                                                    \
   do {                                                                                              \
