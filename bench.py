@@ -36,16 +36,22 @@ METRIC = "particle-steps/s @1M: mixed vs FP64 on GB300 at ≤1e-4 err; adjoint/f
 R, L = 0.010, 0.030
 DX_1M = 0.2112e-3
 
-# Compulsory HBM bytes per particle of each gather kernel in the plain FP64
-# form (fields read once per pass, state read+written once, 4-byte neighbour
-# index per entry + 4-byte row length): see the design doc's traffic model.
+# Compulsory HBM bytes per particle of each gather kernel (fields read once
+# per pass, state read + written once, 4-byte neighbour index per entry and a
+# 4-byte row length), at each form's storage widths: FP64 state; the mixed
+# form's gathers read FP32 float-float shadows (x, v: 24 B each) and FP32
+# Sigma/rho^2, m, rho, h.  the design doc section 5 lists the field sets.
 ALG_BYTES = {
-    "k_accel": lambda nnz: 144 + 4 * nnz + 4,           # x,v,rho,m,h,Sigma(6) -> a
-    "k_density_drift": lambda nnz: 272 + 4 * nnz + 4,   # x,v,a,rho,m,h -> v,rho ; x,v,a -> x,v
-    "k_rate_stress": lambda nnz: 440 + 4 * nnz + 4,     # x,v,rho,m,h,tau,eps,eps_p,pl,sy -> tau,Sigma,eps,...
-    "k_energy": lambda nnz: 88 + 4 * nnz + 4,           # x,v,p,rho,m,h -> dkin ; tau,SR -> dint
+    "k_accel": lambda nnz: 144 + 4 * nnz + 4,             # x,v,rho,m,h,Sigma(6) -> a
+    "k_density_drift": lambda nnz: 272 + 4 * nnz + 4,     # x,v,a,rho,m,h -> v,rho ; x,v,a -> x,v
+    "k_rate_stress": lambda nnz: 440 + 4 * nnz + 4,       # x,v,rho,m,h,tau,eps,eps_p,pl,sy -> tau,Sigma,...
+    "k_energy": lambda nnz: 88 + 4 * nnz + 4,             # x,v,p,rho,m,h -> dkin ; tau,SR -> dint
+    "k_accel_mx": lambda nnz: 108 + 4 * nnz + 4,          # ff x,v; f32 rho,m,h,Sigma/rho^2 -> a (f64)
+    "k_density_drift_mx": lambda nnz: 320 + 4 * nnz + 4,  # f64 integration + ff shadows of x,v written
+    "k_rate_stress_mx": lambda nnz: 440 + 4 * nnz + 4,    # f64 stress state, ff gathers
+    "k_energy_mx": lambda nnz: 60 + 4 * nnz + 4,          # ff x,v; f32 p/rho^2,m -> dkin ; tau,SR -> dint
 }
-# FP64 operations per neighbour entry / per particle of the same kernels.
+# FP64 operations per neighbour entry / per particle (plain form).
 ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (55, 250), "k_energy": (35, 20)}
 
 
@@ -155,7 +161,7 @@ def roofline(d, case, nnz, steps, peak_gbs, peak_kind):
     ms = ms_tot / cnt
     alg = ALG_BYTES[name](nnz) * case.n
     achieved = alg / (ms * 1e-3) / 1e9
-    per_nb, per_p = ALG_FLOPS[name]
+    per_nb, per_p = ALG_FLOPS.get(name, (0, 0))
     flops = (per_nb * nnz + per_p) * case.n
     shares = {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:8]}
     traffic = None
@@ -171,7 +177,8 @@ def roofline(d, case, nnz, steps, peak_gbs, peak_kind):
     return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 2), "peak": peak_gbs, "unit": "GB/s",
             "frac": round(achieved / peak_gbs, 4), "peak_source": peak_kind, "traffic": traffic,
             "alg_bytes_per_launch": alg, "ms_per_launch": round(ms, 4),
-            "fp64_tflops": round(flops / (ms * 1e-3) / 1e12, 4), "kernel_time_shares": shares}
+            "fp64_tflops": round(flops / (ms * 1e-3) / 1e12, 4) if flops else None,
+            "kernel_time_shares": shares}
 
 
 def e2e(wfmod, precision, steps, gpu, pinned):
@@ -292,7 +299,7 @@ def main():
 
     import weldform_gb300 as wfmod
     try:
-        import torch
+        import torch  # noqa: F811
         def pinned(arr):
             t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
             return t.numpy()
@@ -305,35 +312,53 @@ def main():
 
     gpu = local if world > 1 else 0
     peak, peak_kind = measured_peaks()
-    headline = wfmod.PRECISION_FP64
-    forms = {}
     try:
         wfmod.Domain().close()
     except Exception as e:
         print(json.dumps({"metric": METRIC, "error": str(e)}))
         raise
-    # Headline form (timed region with barrier + synchronize on both sides).
-    d, case, _, _, nnz = time_form(wfmod, headline, 1, warmup, gpu)
-    barrier(pg)
-    if have_torch_cuda:
-        torch.cuda.synchronize()
-    with ClockSampler(gpu) as clk:
-        ms, launches = d.step_timed(a.steps)
-    if have_torch_cuda:
-        torch.cuda.synchronize()
-    barrier(pg)
-    ms_max = reduce_max(pg, ms)
-    value = world * case.n * a.steps / (ms_max * 1e-3)
-    rl = roofline(d, case, nnz, a.steps, peak, peak_kind)
-    d.close()
-    ee = e2e(wfmod, headline, a.steps, gpu, pinned)
+    forms = {}
+    head = None
+    for name, prec in (("mixed", wfmod.PRECISION_MIXED), ("fp64", wfmod.PRECISION_FP64)):
+        d, case, _, _, nnz = time_form(wfmod, prec, 1, warmup, gpu)
+        steps = a.steps
+        barrier(pg)
+        if have_torch_cuda:
+            torch.cuda.synchronize()
+        with ClockSampler(gpu) as clk:
+            ms, launches = d.step_timed(steps)
+        if have_torch_cuda:
+            torch.cuda.synchronize()
+        barrier(pg)
+        ms_max = reduce_max(pg, ms)
+        val = world * case.n * steps / (ms_max * 1e-3)
+        rl = roofline(d, case, nnz, steps, peak, peak_kind)
+        forms[name] = {"value": val, "ms_per_step": ms_max / steps, "steps": steps, "roofline": rl,
+                       "gpu_launches": launches, "clocks": clk.summary()}
+        if name == "mixed":
+            head = (case, nnz)
+            xm, sm = d.get_array("Displacement"), d.get_array("Sigma")
+        else:
+            xf, sf = d.get_array("Displacement"), d.get_array("Sigma")
+        d.close()
+    case, nnz = head
+    mixed = forms["mixed"]
+    ee = e2e(wfmod, wfmod.PRECISION_MIXED, a.steps, gpu, pinned)
     ee["value"] *= world
-    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": a.steps,
-            "warmup": warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lattice jitter)",
-            "config": _workload(case.n, "plain FP64"), "gpu_launches": launches, "clocks": clk.summary(),
-            "roofline": rl, "e2e": ee, "neighbours_per_particle": round(nnz, 3)}
-    line["forms"] = {"fp64": {"value": value, "ms_per_step": ms_max / a.steps}}
+    line = {"metric": METRIC, "value": mixed["value"], "unit": "particle-steps/s", "n_gpus": world,
+            "steps": a.steps, "warmup": warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair sums + f64 integration (mixed form)",
+            "data": "synthetic (seeded lattice jitter)", "config": _workload(case.n, "mixed FP32/FP64"),
+            "gpu_launches": mixed["gpu_launches"], "clocks": mixed["clocks"], "roofline": mixed["roofline"],
+            "e2e": ee, "neighbours_per_particle": round(nnz, 3),
+            "forms": {k: {kk: v for kk, v in f.items() if kk not in ("clocks",)} for k, f in forms.items()},
+            "mixed_over_fp64": mixed["value"] / forms["fp64"]["value"]}
+    # Same steps from the same start on both forms: the mixed form's drift from
+    # the plain FP64 form (itself within 1e-9 of the CPU oracle).
+    if forms["fp64"]["steps"] == mixed["steps"]:
+        line["mixed_vs_fp64_rel_l2"] = {
+            "Displacement": float(np.linalg.norm(xm - xf) / max(np.linalg.norm(xf), 1e-300)),
+            "Sigma": float(np.linalg.norm(sm - sf) / max(np.linalg.norm(sf), 1e-300))}
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:

@@ -1,0 +1,84 @@
+"""Mixed FP32/FP64 form against the FP64 oracle, through the C ABI.
+
+Bar (the benchmark spec): relative L2 error <= 1e-4 in stress and reaction force
+after the stated steps; the same bound is applied to displacement, plastic
+strain, density and temperature.  Neighbour lists stay bit-exact (the search
+is shared with the plain form and runs on FP64 positions).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests._support import gpu_domain, oracle_domain, rel_l2
+from weldform_gb300 import configs, JOHNSON_COOK, PRECISION_MIXED
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+THREADS = os.cpu_count() or 1
+
+
+def _run(build, steps, fields, scalars=(), **kw):
+    out = {}
+    for name in ("mixed", "oracle"):
+        d = gpu_domain() if name == "mixed" else oracle_domain()
+        if name == "mixed":
+            d.set("precision", PRECISION_MIXED)
+        else:
+            d.set("cpu_threads", THREADS)
+        case = build(d, **kw)
+        d.prepare(case.dt)
+        d.step(steps)
+        out[name] = {f: d.get_array(f) for f in fields}
+        for s in scalars:
+            out[name][s] = d.get(s)
+        out[name]["nbr"] = d.neighbours()
+        if case.mesh is not None:
+            out[name]["cf"] = d.contact_force(case.mesh)
+        d.close()
+    return out["mixed"], out["oracle"]
+
+
+def _check(m, o, fields, tol=TOL):
+    errs = {f: rel_l2(m[f], o[f]) for f in fields}
+    for f, e in errs.items():
+        assert e <= tol, f"{f}: relative L2 {e:.3e} (all: {errs})"
+    return errs
+
+
+FIELDS = ("Displacement", "Sigma", "Density", "v")
+
+
+def test_mixed_elastic_config1_1000_steps():
+    m, o = _run(configs.cylinder_upsetting, 1000, FIELDS, ("int_energy_sum",))
+    _check(m, o, FIELDS)
+    assert abs(m["int_energy_sum"] - o["int_energy_sum"]) <= TOL * abs(o["int_energy_sum"])
+    assert np.array_equal(m["nbr"][1], o["nbr"][1])
+
+
+def test_mixed_yielding_bilinear():
+    f = FIELDS + ("pl_strain", "Strain_pl")
+    m, o = _run(configs.cylinder_upsetting, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    assert o["pl_strain"].max() > 1e-2
+    _check(m, o, f)
+
+
+def test_mixed_johnson_cook_thermal():
+    f = FIELDS + ("pl_strain", "T")
+    m, o = _run(configs.cylinder_upsetting, 200, f, ("plastic_work",), R=0.004, L=0.008, dx=0.0005, v_top=-30.0,
+                model=JOHNSON_COOK, thermal=True)
+    _check(m, o, f + ())
+    dT_m = m["T"] - 300.0
+    dT_o = o["T"] - 300.0
+    assert rel_l2(dT_m, dT_o) <= TOL
+    assert abs(m["plastic_work"] - o["plastic_work"]) <= TOL * abs(o["plastic_work"])
+
+
+def test_mixed_contact_reaction_force():
+    f = FIELDS + ("pl_strain",)
+    m, o = _run(configs.contact_upsetting, 150, f, ("contact_force_sum",), R=0.003, L=0.006, dx=0.0003,
+                v_punch=-10.0, gap=0.0)
+    assert abs(o["cf"][2]) > 0
+    assert abs(m["cf"][2] - o["cf"][2]) <= TOL * abs(o["cf"][2])
+    _check(m, o, f)

@@ -47,6 +47,19 @@ enum I32Col : int {
   NI32 = 13
 };
 
+// ---- float shadow columns of the mixed form --------------------------------
+// Positions, velocities and temperature as float-float pairs (hi = fl(v),
+// lo = fl(v - hi)): the difference of two pairs gives x_i - x_j to FP32
+// accuracy even when |x| >> |x_i - x_j|, with FP32 arithmetic only.
+enum F32Col : int {
+  G_XH = 0, G_XL = 3, G_VH = 6, G_VL = 9,
+  G_SRHO = 12,             // Sigma / rho^2 (6)
+  G_MRHO = 18, G_RHO = 19, G_PR2 = 20, G_TH = 21, G_TL = 22,
+  G_H = 23, G_M = 24, G_CS = 25, G_ALPHA = 26, G_BETA = 27, G_KT = 28,
+  G_XHN = 29, G_XLN = 32, G_VHN = 35, G_VLN = 38, G_MRHON = 41, G_RHON = 42,
+  NF32 = 43
+};
+
 struct MaterialDev {
   int model;
   double E;
@@ -126,12 +139,14 @@ struct DomainConst {
   int nmeshes;
   int contact_surf_id[MAX_MESHES];
   int nblocks;         // blocks of the per-particle kernels (partials stride)
+  int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
 };
 
 // Device pointers, passed by value to every kernel.
 struct DevPtrs {
   double* f;         // F64 arena: column c at f + c * N
   int* i;            // I32 arena
+  float* g;          // F32 shadow arena of the mixed form (column c at g + c * N)
   StepState* st;
   const DomainTables* tab;
   const int* cell_rank;   // linear cell -> Morton rank

@@ -141,6 +141,7 @@ struct wf_domain {
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
   int graph_precision = -1;
+  bool shadows_valid = false;  // float shadows of the mixed form match the FP64 state
   long long launches_per_step = 0;
   double hmax = 0;
   double BLPF[3] = {0, 0, 0}, TRPR[3] = {0, 0, 0};
@@ -414,6 +415,8 @@ struct wf_domain {
     d_f = dalloc<double>((size_t)NF64 * n);
     d_i = dalloc<int>((size_t)NI32 * n);
     d_fscratch = dalloc<double>((size_t)NF64_PERSIST * n);
+    P.g = dalloc<float>((size_t)NF32 * n);
+    CK(cudaMemsetAsync(P.g, 0, sizeof(float) * NF32 * n, stream));
     d_iscratch = dalloc<int>((size_t)NI32_PERSIST * n);
     CK(cudaMemsetAsync(d_f, 0, sizeof(double) * NF64 * n, stream));
     CK(cudaMemsetAsync(d_i, 0, sizeof(int) * NI32 * n, stream));
@@ -580,12 +583,25 @@ struct wf_domain {
   }
 
   void launch_one_step() {
-    if (precision == WF_PRECISION_MIXED) throw CudaError{WF_ERR_UNSUPPORTED, "mixed form not built yet"};
-    wf::launch_step_fp64(P, K, d_fscratch, d_iscratch, stream);
+    wf::DomainConst k = K;
+    k.mixed = precision == WF_PRECISION_MIXED;
+    if (k.mixed) wf::launch_step_mixed(P, k, d_fscratch, d_iscratch, stream);
+    else wf::launch_step_fp64(P, k, d_fscratch, d_iscratch, stream);
+  }
+  // Before running mixed steps: rebuild the float shadows from the FP64 state
+  // if plain steps or host writes have touched it since.
+  void ensure_shadows() {
+    if (precision != WF_PRECISION_MIXED) { shadows_valid = false; return; }
+    if (shadows_valid) return;
+    wf::DomainConst k = K;
+    k.mixed = 1;
+    wf::launch_refresh_shadows(P, k, 1, stream);
+    shadows_valid = true;
   }
   void step(long long n) {
     if (!prepared) throw CudaError{WF_ERR_STATE, "wf_step before wf_prepare_kickdrift"};
     use_device();
+    ensure_shadows();
     if (use_graph) {
       if (!graph || graph_precision != precision) {
         if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
@@ -614,6 +630,7 @@ struct wf_domain {
     CK(cudaEventCreate(&b));
     CK(cudaStreamSynchronize(stream));
     if (use_graph && (!graph || graph_precision != precision)) step(0);
+    ensure_shadows();
     long long l0 = wf::g_launches;
     CK(cudaEventRecord(a, stream));
     if (use_graph) {
@@ -640,6 +657,7 @@ struct wf_domain {
     for (auto& e : ev) CK(cudaEventCreate(&e));
     wf::KernelTimer t;
     t.ev = ev.data(); t.names = names.data(); t.cap = cap; t.n = 0;
+    ensure_shadows();
     CK(cudaStreamSynchronize(stream));
     wf::g_timer = &t;
     wf::mark(stream, "begin");
@@ -701,6 +719,7 @@ struct wf_domain {
     wf::launch_scatter_orig(P, K, tmp, d_f + (size_t)c * n, ncomp, stream);
     CK(cudaFreeAsync(tmp, stream));
     wf::launch_refresh_derived(P, K, stream);
+    shadows_valid = false;
     CK(cudaStreamSynchronize(stream));
   }
   void get_i32(int c, int* dst) {

@@ -31,6 +31,17 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
 // Forces the search on the next launch (solver prologue and explicit calls).
 void launch_force_search(const DevPtrs& P, cudaStream_t s);
 
+// Pieces shared by both forms (wf_step_fp64.cu): schedule + gated search;
+// velocity BCs on a velocity column; contact + first half kick; reductions,
+// rigid-mesh update and schedule bookkeeping.
+void launch_step_head(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
+void launch_bc(const DevPtrs& P, const DomainConst& K, int vcol, cudaStream_t s);
+void launch_contact_kick(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
+void launch_step_tail(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
+// Float shadows of the mixed form from the FP64 state (gated on the search
+// flag unless force is set).
+void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, cudaStream_t s);
+
 // One kick-drift step of the plain FP64 form (wf_step_fp64.cu).
 void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
 // One kick-drift step of the mixed FP32/FP64 form (wf_step_mixed.cu).

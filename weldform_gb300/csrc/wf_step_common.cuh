@@ -33,6 +33,19 @@ __device__ __forceinline__ double block_reduce(double v, double* sh) {
   return v;
 }
 
+__device__ __forceinline__ float& gcol(const DevPtrs& P, int c, size_t N, int i) { return P.g[(size_t)c * N + i]; }
+// Float-float split of a double: hi = fl(v), lo = fl(v - hi).
+__device__ __forceinline__ void ff_split(double v, float& hi, float& lo) {
+  hi = __double2float_rn(v);
+  lo = __double2float_rn(v - (double)hi);
+}
+__device__ __forceinline__ void store_ff(const DevPtrs& P, int chi, int clo, size_t N, int i, double v) {
+  float h, l;
+  ff_split(v, h, l);
+  P.g[(size_t)chi * N + i] = h;
+  P.g[(size_t)clo * N + i] = l;
+}
+
 // Amplitude lookup (SPH::amplitude::getValAtTime, Source/Domain.h:69-89).
 __device__ __forceinline__ double amp_value(const DomainTables* T, int amp_id, double t, bool* found) {
   for (int k = 0; k < T->namp; ++k) {

@@ -173,6 +173,10 @@ __global__ void k_bc(DevPtrs P, DomainConst K, int vcol) {
         for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = val * T->bc[b].value[d]; }
     }
   }
+  if (K.mixed) {  // keep the float-float velocity shadow in step with the FP64 value
+    int hc = vcol == C_VN ? G_VHN : G_VH, lc = vcol == C_VN ? G_VLN : G_VL;
+    for (int d = 0; d < 3; ++d) store_ff(P, hc + d, lc + d, N, i, col(P, vcol + d, N, i));
+  }
 }
 
 // ---------------------------------------------------------------- contact + kick
@@ -265,7 +269,11 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
       for (int d = 0; d < 3; ++d) colw(P, C_A + d, N, i) = a[d];
     }
     if (kind == 0) {  // half kick v += a * 0.5 * dt (rigid-mesh particles have a = 0)
-      for (int d = 0; d < 3; ++d) colw(P, C_V + d, N, i) = col(P, C_V + d, N, i) + a[d] * 0.5 * dt;
+      for (int d = 0; d < 3; ++d) {
+        double vn = col(P, C_V + d, N, i) + a[d] * 0.5 * dt;
+        colw(P, C_V + d, N, i) = vn;
+        if (K.mixed) store_ff(P, G_VH + d, G_VL + d, N, i, vn);
+      }
     }
   }
   if (K.contact) {
@@ -544,6 +552,7 @@ __global__ void k_mesh_elems(DevPtrs P, DomainConst K) {
     colw(P, C_V + d, N, p) = s / 3;
     colw(P, C_A + d, N, p) = 0.0;
     colw(P, C_NORMAL + d, N, p) = nrm[d];
+    if (K.mixed) store_ff(P, G_VH + d, G_VL + d, N, p, s / 3);
   }
 }
 
@@ -632,28 +641,21 @@ void launch_scatter_orig_i32(const DevPtrs& P, const DomainConst& K, const int* 
 }
 
 // ---------------------------------------------------------------- one step
-void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
-  int nb = nblk(K.N, BLOCK);
-  int nbc = nblk(K.nbc_particles > 0 ? K.nbc_particles : 1, BLOCK);
+void launch_step_head(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
   k_schedule<<<1, 1, 0, s>>>(P, K);
   mark(s, "k_schedule");
   launch_neighbour_search(P, K, fscratch, iscratch, s);
-  k_accel<<<nb, BLOCK, 0, s>>>(P, K);
-  mark(s, "k_accel");
-  k_bc<<<nbc, BLOCK, 0, s>>>(P, K, C_V);
+}
+void launch_bc(const DevPtrs& P, const DomainConst& K, int vcol, cudaStream_t s) {
+  int nbc = nblk(K.nbc_particles > 0 ? K.nbc_particles : 1, BLOCK);
+  k_bc<<<nbc, BLOCK, 0, s>>>(P, K, vcol);
   mark(s, "k_bc");
-  k_contact_kick<<<nb, BLOCK, 0, s>>>(P, K);
+}
+void launch_contact_kick(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
+  k_contact_kick<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
   mark(s, "k_contact_kick");
-  k_bc<<<nbc, BLOCK, 0, s>>>(P, K, C_V);
-  mark(s, "k_bc");
-  k_density_drift<<<nb, BLOCK, 0, s>>>(P, K);
-  mark(s, "k_density_drift");
-  k_bc<<<nbc, BLOCK, 0, s>>>(P, K, C_VN);
-  mark(s, "k_bc");
-  k_rate_stress<<<nb, BLOCK, 0, s>>>(P, K);
-  mark(s, "k_rate_stress");
-  k_energy<<<nb, BLOCK, 0, s>>>(P, K);
-  mark(s, "k_energy");
+}
+void launch_step_tail(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
   k_finalize<<<NSLOTS, 1024, 0, s>>>(P, K);
   mark(s, "k_finalize");
   if (K.contact && P.nelem > 0) {
@@ -664,6 +666,24 @@ void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, 
   }
   k_step_end<<<1, 1, 0, s>>>(P, K);
   mark(s, "k_step_end");
+}
+
+void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
+  int nb = nblk(K.N, BLOCK);
+  launch_step_head(P, K, fscratch, iscratch, s);
+  k_accel<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_accel");
+  launch_bc(P, K, C_V, s);
+  launch_contact_kick(P, K, s);
+  launch_bc(P, K, C_V, s);
+  k_density_drift<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_density_drift");
+  launch_bc(P, K, C_VN, s);
+  k_rate_stress<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_rate_stress");
+  k_energy<<<nb, BLOCK, 0, s>>>(P, K);
+  mark(s, "k_energy");
+  launch_step_tail(P, K, s);
 }
 
 }  // namespace wf
