@@ -57,7 +57,8 @@ enum F32Col : int {
   G_MRHO = 18, G_RHO = 19, G_PR2 = 20, G_TH = 21, G_TL = 22,
   G_H = 23, G_M = 24, G_CS = 25, G_ALPHA = 26, G_BETA = 27, G_KT = 28,
   G_XHN = 29, G_XLN = 32, G_VHN = 35, G_VLN = 38, G_MRHON = 41, G_RHON = 42,
-  NF32 = 43
+  G_RATES = 43,            // StrainRate (6) + RotationRate (3) between the gather and the update
+  NF32 = 52
 };
 
 struct MaterialDev {

@@ -149,17 +149,21 @@ __global__ void k_sort_cells(DevPtrs P, DomainConst K) {
   }
 }
 
-// Gather every persistent column into the scratch arenas (new order).
+// Gather every persistent column into the scratch arenas (new order).  A
+// fixed grid strides over (column, particle) so the launch costs nothing on
+// steps that do not search.
 __global__ void k_permute(DevPtrs P, DomainConst K, double* fdst, int* idst) {
   if (!searching(P)) return;
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  int col = blockIdx.y;
-  if (p >= K.N) return;
-  int src = P.perm[p];
-  if (col < NF64_PERSIST) fdst[col * (size_t)K.N + p] = P.f[col * (size_t)K.N + src];
-  else {
-    int c = col - NF64_PERSIST;
-    idst[c * (size_t)K.N + p] = P.i[c * (size_t)K.N + src];
+  size_t N = K.N;
+  size_t total = (size_t)(NF64_PERSIST + NI32_PERSIST) * N;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    size_t col = k / N, p = k - col * N;
+    int src = P.perm[p];
+    if (col < (size_t)NF64_PERSIST) fdst[col * N + p] = P.f[col * N + src];
+    else {
+      size_t c = col - NF64_PERSIST;
+      idst[c * N + p] = P.i[c * N + src];
+    }
   }
 }
 __global__ void k_copy_back(DevPtrs P, DomainConst K, const double* fsrc, const int* isrc) {
@@ -398,8 +402,7 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   mark(s, "k_scatter");
   k_sort_cells<<<nblk(K.ncells, T), T, 0, s>>>(P, K);
   mark(s, "k_sort_cells");
-  dim3 g(nblk(K.N, T), NF64_PERSIST + NI32_PERSIST);
-  k_permute<<<g, T, 0, s>>>(P, K, fscratch, iscratch);
+  k_permute<<<152 * 8, 512, 0, s>>>(P, K, fscratch, iscratch);
   mark(s, "k_permute");
   k_copy_back<<<152 * 8, 512, 0, s>>>(P, K, fscratch, iscratch);
   mark(s, "k_copy_back");

@@ -255,46 +255,72 @@ __device__ __forceinline__ double stress_update_mx(StressIO& s, const float sr[6
   return dep;
 }
 
-__global__ void __launch_bounds__(BLOCK) k_rate_stress_mx(DevPtrs P, DomainConst K) {
+// Gather half: strain-rate and rotation-rate sums (InteractionAlt.cpp:263-479),
+// written as float columns for the elementwise update below.  Kept lean so the
+// gather runs at high occupancy.
+__global__ void __launch_bounds__(BLOCK) k_rate_mx(DevPtrs P, DomainConst K, float* rates) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (icol(P, I_KIND, N, i) == 0) {
+    float xh0 = gcol(P, G_XHN, N, i), xh1 = gcol(P, G_XHN + 1, N, i), xh2 = gcol(P, G_XHN + 2, N, i);
+    float xl0 = gcol(P, G_XLN, N, i), xl1 = gcol(P, G_XLN + 1, N, i), xl2 = gcol(P, G_XLN + 2, N, i);
+    float vh0 = gcol(P, G_VHN, N, i), vh1 = gcol(P, G_VHN + 1, N, i), vh2 = gcol(P, G_VHN + 2, N, i);
+    float vl0 = gcol(P, G_VLN, N, i), vl1 = gcol(P, G_VLN + 1, N, i), vl2 = gcol(P, G_VLN + 2, N, i);
+    float hi = gcol(P, G_H, N, i);
+    KSum M[9];  // sum_j (m_j/rho_j) (-GK/2) (v_i - v_j)_k (x_i - x_j)_l
+    int len = P.row_len[i];
+    for (int k = 0; k < len; ++k) {
+      int j = P.nbr[(size_t)k * N + i];
+      GeoF g = geo_f(P, N, G_XHN, G_XLN, xh0, xh1, xh2, xl0, xl1, xl2, hi, j);
+      float b0 = (vh0 - gcol(P, G_VHN, N, j)) + (vl0 - gcol(P, G_VLN, N, j));
+      float b1 = (vh1 - gcol(P, G_VHN + 1, N, j)) + (vl1 - gcol(P, G_VLN + 1, N, j));
+      float b2 = (vh2 - gcol(P, G_VHN + 2, N, j)) + (vl2 - gcol(P, G_VLN + 2, N, j));
+      float w = gcol(P, G_MRHON, N, j) * (-0.5f * g.GK);
+      float wb0 = w * b0, wb1 = w * b1, wb2 = w * b2;
+      M[0].add(wb0 * g.x0); M[1].add(wb0 * g.x1); M[2].add(wb0 * g.x2);
+      M[3].add(wb1 * g.x0); M[4].add(wb1 * g.x1); M[5].add(wb1 * g.x2);
+      M[6].add(wb2 * g.x0); M[7].add(wb2 * g.x1); M[8].add(wb2 * g.x2);
+    }
+    double m[9];
+    for (int c = 0; c < 9; ++c) m[c] = M[c].value();
+    // StrainRate = symmetric part (InteractionAlt.cpp:338-351), RotationRate
+    // = antisymmetric part (355-361)
+    out[0] = (float)(2.0 * m[0]); out[1] = (float)(2.0 * m[4]); out[2] = (float)(2.0 * m[8]);
+    out[3] = (float)(m[1] + m[3]); out[4] = (float)(m[2] + m[6]); out[5] = (float)(m[5] + m[7]);
+    out[6] = (float)(m[1] - m[3]); out[7] = (float)(m[2] - m[6]); out[8] = (float)(m[5] - m[7]);
+  }
+  for (int c = 0; c < 9; ++c) rates[(size_t)c * N + i] = out[c];
+}
+
+// Elementwise half: constitutive update, heating, temperature, and the
+// next-step buffers becoming current.
+__global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K, const float* rates) {
   __shared__ double sh[32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
   double dt = K.dt;
   double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300;
   if (i < K.N) {
-    double x[3], v[3];
-    for (int d = 0; d < 3; ++d) { x[d] = col(P, C_XN + d, N, i); v[d] = col(P, C_VN + d, N, i); }
+    for (int d = 0; d < 3; ++d) {
+      colw(P, C_X + d, N, i) = col(P, C_XN + d, N, i);
+      colw(P, C_V + d, N, i) = col(P, C_VN + d, N, i);
+      gcol(P, G_XH + d, N, i) = gcol(P, G_XHN + d, N, i);
+      gcol(P, G_XL + d, N, i) = gcol(P, G_XLN + d, N, i);
+      gcol(P, G_VH + d, N, i) = gcol(P, G_VHN + d, N, i);
+      gcol(P, G_VL + d, N, i) = gcol(P, G_VLN + d, N, i);
+    }
     double rho = col(P, C_RHON, N, i);
-    for (int d = 0; d < 3; ++d) { colw(P, C_X + d, N, i) = x[d]; colw(P, C_V + d, N, i) = v[d]; }
     colw(P, C_RHO, N, i) = rho;
     colw(P, C_MRHO, N, i) = col(P, C_MRHON, N, i);
-    float xh0 = gcol(P, G_XHN, N, i), xh1 = gcol(P, G_XHN + 1, N, i), xh2 = gcol(P, G_XHN + 2, N, i);
-    float xl0 = gcol(P, G_XLN, N, i), xl1 = gcol(P, G_XLN + 1, N, i), xl2 = gcol(P, G_XLN + 2, N, i);
-    float vh0 = gcol(P, G_VHN, N, i), vh1 = gcol(P, G_VHN + 1, N, i), vh2 = gcol(P, G_VHN + 2, N, i);
-    float vl0 = gcol(P, G_VLN, N, i), vl1 = gcol(P, G_VLN + 1, N, i), vl2 = gcol(P, G_VLN + 2, N, i);
+    gcol(P, G_MRHO, N, i) = gcol(P, G_MRHON, N, i);
+    gcol(P, G_RHO, N, i) = gcol(P, G_RHON, N, i);
     maxpl = col(P, C_PLS, N, i);
     if (icol(P, I_KIND, N, i) == 0) {
-      float hi = gcol(P, G_H, N, i);
-      KSum M[9];  // sum_j (m_j/rho_j) (-GK/2) (v_i - v_j)_k (x_i - x_j)_l
-      int len = P.row_len[i];
-      for (int k = 0; k < len; ++k) {
-        int j = P.nbr[(size_t)k * N + i];
-        GeoF g = geo_f(P, N, G_XHN, G_XLN, xh0, xh1, xh2, xl0, xl1, xl2, hi, j);
-        float b0 = (vh0 - gcol(P, G_VHN, N, j)) + (vl0 - gcol(P, G_VLN, N, j));
-        float b1 = (vh1 - gcol(P, G_VHN + 1, N, j)) + (vl1 - gcol(P, G_VLN + 1, N, j));
-        float b2 = (vh2 - gcol(P, G_VHN + 2, N, j)) + (vl2 - gcol(P, G_VLN + 2, N, j));
-        float w = gcol(P, G_MRHON, N, j) * (-0.5f * g.GK);
-        float wb0 = w * b0, wb1 = w * b1, wb2 = w * b2;
-        M[0].add(wb0 * g.x0); M[1].add(wb0 * g.x1); M[2].add(wb0 * g.x2);
-        M[3].add(wb1 * g.x0); M[4].add(wb1 * g.x1); M[5].add(wb1 * g.x2);
-        M[6].add(wb2 * g.x0); M[7].add(wb2 * g.x1); M[8].add(wb2 * g.x2);
-      }
-      double m[9];
-      for (int c = 0; c < 9; ++c) m[c] = M[c].value();
-      // StrainRate = sym part (InteractionAlt.cpp:338-351), RotationRate = antisym (355-361)
-      float sr[6] = {(float)(2.0 * m[0]), (float)(2.0 * m[4]), (float)(2.0 * m[8]), (float)(m[1] + m[3]),
-                     (float)(m[2] + m[6]), (float)(m[5] + m[7])};
-      float rr[3] = {(float)(m[1] - m[3]), (float)(m[2] - m[6]), (float)(m[5] - m[7])};
+      float sr[6], rr[3];
+      for (int c = 0; c < 6; ++c) sr[c] = rates[(size_t)c * N + i];
+      for (int c = 0; c < 3; ++c) rr[c] = rates[(size_t)(6 + c) * N + i];
       StressIO s;
       for (int c = 0; c < 6; ++c) {
         s.tau[c] = col(P, C_TAU + c, N, i); s.eps[c] = col(P, C_EPS + c, N, i);
@@ -333,13 +359,6 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress_mx(DevPtrs P, DomainConst
         maxT = T; minT = T;
       }
     }
-    // next-step shadows become current for this particle
-    gcol(P, G_XH, N, i) = xh0; gcol(P, G_XH + 1, N, i) = xh1; gcol(P, G_XH + 2, N, i) = xh2;
-    gcol(P, G_XL, N, i) = xl0; gcol(P, G_XL + 1, N, i) = xl1; gcol(P, G_XL + 2, N, i) = xl2;
-    gcol(P, G_VH, N, i) = vh0; gcol(P, G_VH + 1, N, i) = vh1; gcol(P, G_VH + 2, N, i) = vh2;
-    gcol(P, G_VL, N, i) = vl0; gcol(P, G_VL + 1, N, i) = vl1; gcol(P, G_VL + 2, N, i) = vl2;
-    gcol(P, G_MRHO, N, i) = gcol(P, G_MRHON, N, i);
-    gcol(P, G_RHO, N, i) = gcol(P, G_RHON, N, i);
   }
   double r;
   r = block_reduce<1>(maxpl, sh); if (threadIdx.x == 0) P.partials[S_MAXPL * K.nblocks + blockIdx.x] = r;
@@ -422,8 +441,11 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   k_density_drift_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  k_rate_stress_mx<<<nb, BLOCK, 0, s>>>(P, K);
-  mark(s, "k_rate_stress_mx");
+  float* rates = P.g + (size_t)G_RATES * K.N;
+  k_rate_mx<<<nb, BLOCK, 0, s>>>(P, K, rates);
+  mark(s, "k_rate_mx");
+  k_stress_mx<<<nb, BLOCK, 0, s>>>(P, K, rates);
+  mark(s, "k_stress_mx");
   k_energy_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_energy_mx");
   launch_step_tail(P, K, s);
