@@ -47,10 +47,9 @@ ALG_BYTES = {
     "k_rate_stress": lambda nnz: 440 + 4 * nnz + 4,       # x,v,rho,m,h,tau,eps,eps_p,pl,sy -> tau,Sigma,...
     "k_energy": lambda nnz: 88 + 4 * nnz + 4,             # x,v,p,rho,m,h -> dkin ; tau,SR -> dint
     "k_accel_mx": lambda nnz: 108 + 4 * nnz + 4,          # ff x,v; f32 rho,m,h,Sigma/rho^2 -> a (f64)
-    "k_density_drift_mx": lambda nnz: 320 + 4 * nnz + 4,  # f64 integration + ff shadows of x,v written
-    "k_rate_mx": lambda nnz: 56 + 4 * nnz + 4,            # ff x,v; f32 h, m/rho -> 9 rate floats
+    "k_density_drift_mx": lambda nnz: 336 + 4 * nnz + 4,  # f64 integration; next-step record written
+    "k_rate_mx": lambda nnz: 72 + 4 * nnz + 4,            # next record -> 9 rates, dkin, conduction
     "k_stress_mx": lambda nnz: 440,                       # f64 stress state read + written
-    "k_energy_mx": lambda nnz: 60 + 4 * nnz + 4,          # ff x,v; f32 p/rho^2,m -> dkin ; tau,SR -> dint
 }
 # FP64 operations per neighbour entry / per particle (plain form).
 ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (55, 250), "k_energy": (35, 20)}

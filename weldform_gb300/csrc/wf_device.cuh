@@ -47,19 +47,34 @@ enum I32Col : int {
   NI32 = 13
 };
 
-// ---- float shadow columns of the mixed form --------------------------------
-// Positions, velocities and temperature as float-float pairs (hi = fl(v),
+// ---- float4 field groups of the mixed form -----------------------------------
+// The FP32 data a neighbour's gather reads is packed four fields to a float4,
+// one float4 column per group (group q of particle i at rc[q * N + i]).  In
+// cell-sorted order the k-th neighbours of a warp's 32 consecutive particles
+// have nearly consecutive indices, so each 16-byte load coalesces into a few
+// lines — better than one column per field (more load instructions) and
+// better than one record per particle (one line per lane).  Positions,
+// velocities and temperature are float-float pairs (hi = fl(v),
 // lo = fl(v - hi)): the difference of two pairs gives x_i - x_j to FP32
-// accuracy even when |x| >> |x_i - x_j|, with FP32 arithmetic only.
-enum F32Col : int {
-  G_XH = 0, G_XL = 3, G_VH = 6, G_VL = 9,
-  G_SRHO = 12,             // Sigma / rho^2 (6)
-  G_MRHO = 18, G_RHO = 19, G_PR2 = 20, G_TH = 21, G_TL = 22,
-  G_H = 23, G_M = 24, G_CS = 25, G_ALPHA = 26, G_BETA = 27, G_KT = 28,
-  G_XHN = 29, G_XLN = 32, G_VHN = 35, G_VLN = 38, G_MRHON = 41, G_RHON = 42,
-  G_RATES = 43,            // StrainRate (6) + RotationRate (3) between the gather and the update
-  NF32 = 52
+// accuracy even when |x| >> |x_i - x_j|.
+enum RecCur : int {        // current-state groups
+  RC_XH = 0,               // x hi (xyz), h
+  RC_XL = 1,               // x lo (xyz), mass
+  RC_VH = 2,               // v hi (xyz), rho
+  RC_VL = 3,               // v lo (xyz), m/rho
+  RC_S0 = 4,               // Sigma/rho^2 xx yy zz xy
+  RC_S1 = 5,               // Sigma/rho^2 xz yz, p/rho^2, Cs
+  RC_MISC = 6,             // alpha, beta, k_T, T hi
+  RC_T2 = 7,               // T lo
+  RC_N = 8
 };
+enum RecNext : int {       // next-step groups
+  RN_XH = 0, RN_XL = 1,    // as RC_XH / RC_XL at x(n+1)
+  RN_VH = 2, RN_VL = 3,    // v(n+1) hi/lo, rho(n+1), m/rho(n+1)
+  RN_E = 4,                // p/rho^2 at rho(n+1), k_T, T(n+1) hi, T(n+1) lo
+  RN_N = 5
+};
+constexpr int NF32 = 4 * (RC_N + RN_N) + 9;  // floats per particle: records + 9 rate columns
 
 struct MaterialDev {
   int model;
@@ -147,7 +162,10 @@ struct DomainConst {
 struct DevPtrs {
   double* f;         // F64 arena: column c at f + c * N
   int* i;            // I32 arena
-  float* g;          // F32 shadow arena of the mixed form (column c at g + c * N)
+  float* g;          // F32 arena of the mixed form: current groups, next groups, 9 rate columns
+  float4* rc;        // current-state float4 groups (RC_N columns of N)
+  float4* rn;        // next-step float4 groups (RN_N columns of N)
+  float* rates;      // StrainRate (6) + RotationRate (3) columns
   StepState* st;
   const DomainTables* tab;
   const int* cell_rank;   // linear cell -> Morton rank

@@ -417,6 +417,9 @@ struct wf_domain {
     d_fscratch = dalloc<double>((size_t)NF64_PERSIST * n);
     P.g = dalloc<float>((size_t)NF32 * n);
     CK(cudaMemsetAsync(P.g, 0, sizeof(float) * NF32 * n, stream));
+    P.rc = reinterpret_cast<float4*>(P.g);
+    P.rn = reinterpret_cast<float4*>(P.g + (size_t)4 * RC_N * n);
+    P.rates = P.g + (size_t)4 * (RC_N + RN_N) * n;
     d_iscratch = dalloc<int>((size_t)NI32_PERSIST * n);
     CK(cudaMemsetAsync(d_f, 0, sizeof(double) * NF64 * n, stream));
     CK(cudaMemsetAsync(d_i, 0, sizeof(int) * NI32 * n, stream));

@@ -219,22 +219,31 @@ __device__ __forceinline__ bool radius_ok(const DevPtrs& P, const DomainConst& K
   return radius_exact(P, N, i, j, K.Cellfac);
 }
 
-// One thread per particle: SM neighbour row in canonical order; the flag of
-// "was a free-surface particle at search time" for the contact pair rule.
-__global__ void __launch_bounds__(128) k_nbr_fill(DevPtrs P, DomainConst K) {
+// SM neighbour rows in canonical order: one warp per particle, 32 consecutive
+// particles per block.  Lanes test the candidates of each of the 27 cells in
+// parallel; accepted ones are compacted with a ballot into the warp's shared
+// buffer, sorted there by the canonical key (bitonic, 128 slots), and the
+// block writes its 32 rows to the ELL array one coalesced line per entry
+// index.  Also sets Nb and the "free surface at search time" flag used by the
+// contact pair rule.
+constexpr int FILL_WARPS = 32;
+constexpr int FILL_SLOTS = 128;
+__global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
+  __shared__ unsigned s_key[FILL_WARPS][FILL_SLOTS];
+  __shared__ int s_idx[FILL_WARPS][FILL_SLOTS];
+  __shared__ int s_len[FILL_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i0 = blockIdx.x * FILL_WARPS;
+  const int i = i0 + w;
   size_t N = K.N;
   const int* ID = P.i + I_ID * N;
   const int* orig = P.i + I_ORIG * N;
   const int* kind = P.i + I_KIND * N;
   const int* material = P.i + I_MATERIAL * N;
-  int row[MAX_NB];
-  unsigned keys[MAX_NB];
   int cnt = 0, split = 0;
   bool overflow = false;
-  if (kind[i] == 0) {
+  if (i < K.N && kind[i] == 0) {
     float xi = P.xs[i], yi = P.xs[N + i], zi = P.xs[2 * N + i], hi = P.xs[3 * N + i];
     int c[3];
     for (int d = 0; d < 3; ++d) {
@@ -251,33 +260,75 @@ __global__ void __launch_bounds__(128) k_nbr_fill(DevPtrs P, DomainConst K) {
           if (e < 0 || e >= K.CellNo[2]) continue;
           int key = P.cell_rank[(a * K.CellNo[1] + b) * K.CellNo[2] + e];
           int s0 = P.cell_start[key], s1 = P.cell_start[key + 1];
-          for (int j = s0; j < s1; ++j) {
-            if (j == i) continue;
-            int idj = ID[j];
-            if (K.contact && (ci || is_contact_id(K, idj))) continue;  // RIG or dropped pair
-            if (kind[j] != 0 || material[j] != mi) continue;
-            if (!radius_ok(P, K, N, i, j, xi, yi, zi, hi)) continue;
-            unsigned kk = (unsigned)(orig[j] - oi - 1);
-            if (orig[j] > oi) ++split;
-            if (cnt < MAX_NB) {
-              int m = cnt - 1;
-              while (m >= 0 && keys[m] > kk) { keys[m + 1] = keys[m]; row[m + 1] = row[m]; --m; }
-              keys[m + 1] = kk; row[m + 1] = j;
-              ++cnt;
-            } else overflow = true;
+          for (int base = s0; base < s1; base += 32) {
+            int j = base + lane;
+            bool ok = false;
+            unsigned kk = 0;
+            if (j < s1 && j != i) {
+              int idj = ID[j];
+              ok = !(K.contact && (ci || is_contact_id(K, idj))) && kind[j] == 0 && material[j] == mi &&
+                   radius_ok(P, K, N, i, j, xi, yi, zi, hi);
+              if (ok) kk = (unsigned)(orig[j] - oi - 1);
+            }
+            unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+              int pos = cnt + __popc(m & ((1u << lane) - 1u));
+              if (pos < FILL_SLOTS) { s_key[w][pos] = kk; s_idx[w][pos] = j; }
+            }
+            cnt += __popc(m);
           }
         }
       }
     }
+    if (cnt > MAX_NB) overflow = true;
+    if (cnt > FILL_SLOTS) cnt = FILL_SLOTS;
   }
-  for (int k = 0; k < cnt; ++k) P.nbr[(size_t)k * N + i] = row[k];
-  P.row_len[i] = cnt;
-  P.row_split[i] = split < cnt ? split : cnt;
-  P.i[I_NB * N + i] = cnt;
-  if (K.contact) P.i[I_NWS * N + i] = (P.i[I_NWS * N + i] & 1) | ((ID[i] == K.id_free_surf) ? 2 : 0);
-  if (overflow) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
-  // pair count (each unordered pair counted from both ends)
-  atomicAdd(&P.st->pair_count, (unsigned long long)cnt);
+  // Pad and sort the warp's slots by key (bitonic, ascending).
+  for (int e = lane; e < FILL_SLOTS; e += 32)
+    if (e >= cnt) { s_key[w][e] = 0xffffffffu; s_idx[w][e] = -1; }
+  __syncwarp();
+  for (int k = 2; k <= FILL_SLOTS; k <<= 1) {
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int e = lane; e < FILL_SLOTS; e += 32) {
+        int p = e ^ jj;
+        if (p > e) {
+          bool up = (e & k) == 0;
+          unsigned ke = s_key[w][e], kp = s_key[w][p];
+          if ((ke > kp) == up) {
+            s_key[w][e] = kp; s_key[w][p] = ke;
+            int t = s_idx[w][e]; s_idx[w][e] = s_idx[w][p]; s_idx[w][p] = t;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (cnt > MAX_NB) cnt = MAX_NB;
+  if (i < K.N) {
+    // keys below N - 1 - oi belong to neighbours with a larger original index
+    int oi = orig[i];
+    for (int e = lane; e < cnt; e += 32) split += s_key[w][e] < (unsigned)(K.N - 1 - oi) ? 1 : 0;
+    for (int off = 16; off > 0; off >>= 1) split += __shfl_down_sync(0xffffffffu, split, off);
+    if (lane == 0) {
+      s_len[w] = cnt;
+      P.row_len[i] = cnt;
+      P.row_split[i] = split;
+      P.i[I_NB * N + i] = cnt;
+      if (K.contact) P.i[I_NWS * N + i] = (P.i[I_NWS * N + i] & 1) | ((ID[i] == K.id_free_surf) ? 2 : 0);
+      if (overflow) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
+      atomicAdd(&P.st->pair_count, (unsigned long long)cnt);
+    }
+  } else if (lane == 0) {
+    s_len[w] = 0;
+  }
+  __syncthreads();
+  // Block-wide coalesced ELL write: thread (k, t) stores entry k of particle i0 + t.
+  int maxlen = 0;
+  for (int t = 0; t < FILL_WARPS; ++t) maxlen = max(maxlen, s_len[t]);
+  for (int q = threadIdx.x; q < maxlen * FILL_WARPS; q += blockDim.x) {
+    int k = q / FILL_WARPS, t = q - k * FILL_WARPS;
+    if (k < s_len[t]) P.nbr[(size_t)k * N + i0 + t] = s_idx[t][k];
+  }
 }
 
 // CalculateSurface (Domain.cpp:1415-1491): n_i = sum_j m_j (x_i - x_j) in row
@@ -408,7 +459,7 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   mark(s, "k_copy_back");
   k_after_permute<<<nblk(K.N, T), T, 0, s>>>(P, K);
   mark(s, "k_after_permute");
-  k_nbr_fill<<<nblk(K.N, 128), 128, 0, s>>>(P, K);
+  k_nbr_fill<<<nblk(K.N, FILL_WARPS), FILL_WARPS * 32, 0, s>>>(P, K);
   mark(s, "k_nbr_fill");
   if (K.contact) {
     k_surface<<<nblk(K.N, T), T, 0, s>>>(P, K);

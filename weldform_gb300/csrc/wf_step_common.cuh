@@ -33,17 +33,23 @@ __device__ __forceinline__ double block_reduce(double v, double* sh) {
   return v;
 }
 
-__device__ __forceinline__ float& gcol(const DevPtrs& P, int c, size_t N, int i) { return P.g[(size_t)c * N + i]; }
 // Float-float split of a double: hi = fl(v), lo = fl(v - hi).
 __device__ __forceinline__ void ff_split(double v, float& hi, float& lo) {
   hi = __double2float_rn(v);
   lo = __double2float_rn(v - (double)hi);
 }
-__device__ __forceinline__ void store_ff(const DevPtrs& P, int chi, int clo, size_t N, int i, double v) {
+__device__ __forceinline__ float* rc_f(const DevPtrs& P, size_t N, int i, int q) {
+  return reinterpret_cast<float*>(P.rc + (size_t)q * N + i);
+}
+__device__ __forceinline__ float* rn_f(const DevPtrs& P, size_t N, int i, int q) {
+  return reinterpret_cast<float*>(P.rn + (size_t)q * N + i);
+}
+// Velocity component d of particle i into the current (next) float4 groups.
+__device__ __forceinline__ void rec_set_v(const DevPtrs& P, size_t N, int i, int d, double v, bool next) {
   float h, l;
   ff_split(v, h, l);
-  P.g[(size_t)chi * N + i] = h;
-  P.g[(size_t)clo * N + i] = l;
+  if (next) { rn_f(P, N, i, RN_VH)[d] = h; rn_f(P, N, i, RN_VL)[d] = l; }
+  else { rc_f(P, N, i, RC_VH)[d] = h; rc_f(P, N, i, RC_VL)[d] = l; }
 }
 
 // Amplitude lookup (SPH::amplitude::getValAtTime, Source/Domain.h:69-89).

@@ -173,10 +173,8 @@ __global__ void k_bc(DevPtrs P, DomainConst K, int vcol) {
         for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = val * T->bc[b].value[d]; }
     }
   }
-  if (K.mixed) {  // keep the float-float velocity shadow in step with the FP64 value
-    int hc = vcol == C_VN ? G_VHN : G_VH, lc = vcol == C_VN ? G_VLN : G_VL;
-    for (int d = 0; d < 3; ++d) store_ff(P, hc + d, lc + d, N, i, col(P, vcol + d, N, i));
-  }
+  if (K.mixed)  // keep the float-float velocity in the records in step with the FP64 value
+    for (int d = 0; d < 3; ++d) rec_set_v(P, N, i, d, col(P, vcol + d, N, i), vcol == C_VN);
 }
 
 // ---------------------------------------------------------------- contact + kick
@@ -272,7 +270,7 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
       for (int d = 0; d < 3; ++d) {
         double vn = col(P, C_V + d, N, i) + a[d] * 0.5 * dt;
         colw(P, C_V + d, N, i) = vn;
-        if (K.mixed) store_ff(P, G_VH + d, G_VL + d, N, i, vn);
+        if (K.mixed) rec_set_v(P, N, i, d, vn, false);
       }
     }
   }
@@ -552,7 +550,7 @@ __global__ void k_mesh_elems(DevPtrs P, DomainConst K) {
     colw(P, C_V + d, N, p) = s / 3;
     colw(P, C_A + d, N, p) = 0.0;
     colw(P, C_NORMAL + d, N, p) = nrm[d];
-    if (K.mixed) store_ff(P, G_VH + d, G_VL + d, N, p, s / 3);
+    if (K.mixed) rec_set_v(P, N, p, d, s / 3, false);
   }
 }
 

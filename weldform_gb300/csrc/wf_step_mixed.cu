@@ -1,17 +1,22 @@
 // Mixed FP32/FP64 form of the kick-drift step on sm_103a.
 //
-// Same launch sequence and reference semantics as the plain form
-// (wf_step_fp64.cu); what changes is the arithmetic of the pair gathers:
-//  * relative positions, velocities and temperatures are formed from
-//    float-float shadows (hi = fl(v), lo = fl(v - hi)) as
-//    (hi_i - hi_j) + (lo_i - lo_j): accurate to FP32 rounding of the
-//    difference itself, the accuracy an FP64 difference cast to FP32 has, with
-//    FP32 instructions only (GB300 issues FP64 at 1/72 of its FP32 rate);
-//  * kernel gradients, viscosity and pair terms in FP32;
-//  * every per-particle pair sum is Kahan-compensated in FP32;
-//  * FP64 stays in: position/velocity/density integration, the stress
-//    accumulation and its radial-return yield check and scale factor, the
-//    temperature update, and all global reductions.
+// Same step, same reference semantics as the plain form (wf_step_fp64.cu);
+// what changes is how the pair gathers compute and what they read:
+//  * each particle's FP32 gather data sits in one 128-byte record (one cache
+//    line per neighbour), so a neighbour costs a few vector loads from one
+//    line instead of one scalar load from each of ~20 separate columns;
+//  * relative positions, velocities and temperatures come from float-float
+//    pairs, (hi_i - hi_j) + (lo_i - lo_j): accurate to FP32 rounding of the
+//    difference itself — the accuracy of an FP64 difference cast to FP32 —
+//    with FP32 instructions only (GB300 issues FP64 at 1/72 of its FP32 rate);
+//  * kernel gradients, viscosity and pair terms in FP32, every per-particle
+//    pair sum Kahan-compensated;
+//  * FP64 stays in position/velocity/density/temperature integration, the
+//    stress accumulation with its radial-return yield check and scale factor,
+//    and all global reductions.
+// Three gathers per step: acceleration; density (+ drift and second kick);
+// rate tensors fused with the kinetic-energy and conduction sums, which use
+// the same positions, velocities and the pressure of the updated density.
 #include "wf_step_common.cuh"
 #include "wf_launch.h"
 
@@ -33,59 +38,52 @@ struct KSum {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-// Pair geometry in FP32 from float-float positions.  GK as in
-// Functions.cpp:74-87 (cubic spline, 3D).
-struct GeoF {
-  float x0, x1, x2, r2, r, hh, GK;
-};
-__device__ __forceinline__ GeoF geo_f(const DevPtrs& P, size_t N, int hcol, int lcol, float xh0, float xh1, float xh2,
-                                      float xl0, float xl1, float xl2, float hi, int j) {
-  GeoF g;
-  g.x0 = (xh0 - P.g[(size_t)(hcol + 0) * N + j]) + (xl0 - P.g[(size_t)(lcol + 0) * N + j]);
-  g.x1 = (xh1 - P.g[(size_t)(hcol + 1) * N + j]) + (xl1 - P.g[(size_t)(lcol + 1) * N + j]);
-  g.x2 = (xh2 - P.g[(size_t)(hcol + 2) * N + j]) + (xl2 - P.g[(size_t)(lcol + 2) * N + j]);
-  g.r2 = g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2;
-  float rinv = rsqrtf(g.r2);
-  g.r = g.r2 * rinv;
-  float hj = P.g[(size_t)G_H * N + j];
-  g.hh = 0.5f * (hi + hj);
-  float inv_h = 1.0f / g.hh;
-  float q = g.r * inv_h;
+__device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+
+// Cubic-spline gradient factor GK (Functions.cpp:74-87, 3D) from r^2 and the
+// pair smoothing length hh = (hi + hj) / 2.
+__device__ __forceinline__ float grad_kernel_f(float r2, float hh, float* r_out) {
+  float rinv = rsqrtf(r2);
+  float r = r2 * rinv;
+  float inv_h = 1.0f / hh;
+  float q = r * inv_h;
   float ih2 = inv_h * inv_h;
-  float C = INV_PI_F * ih2 * ih2;
+  float C = INV_PI_F * ih2 * ih2 * inv_h;
   float w;
   if (q < 1.0f) w = -3.0f + 2.25f * q;
-  else if (q < 2.0f) { float t = 2.0f - q; w = -0.75f * t * t * (g.hh * rinv); }
+  else if (q < 2.0f) { float t = 2.0f - q; w = -0.75f * t * t * (hh * rinv); }
   else w = 0.0f;
-  if (g.r2 == 0.0f) { w = -3.0f; g.r = 0.0f; }
-  g.GK = C * inv_h * w;
-  return g;
+  if (r2 == 0.0f) { w = -3.0f; r = 0.0f; }
+  *r_out = r;
+  return C * w;
 }
 
-// ---------------------------------------------------------------- shadows
-__global__ void k_refresh_shadows(DevPtrs P, DomainConst K, int force) {
+// ---------------------------------------------------------------- records
+__global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
   if (!force && !P.st->do_search) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
   size_t N = K.N;
-  for (int d = 0; d < 3; ++d) {
-    store_ff(P, G_XH + d, G_XL + d, N, i, col(P, C_X + d, N, i));
-    store_ff(P, G_VH + d, G_VL + d, N, i, col(P, C_V + d, N, i));
-  }
-  store_ff(P, G_TH, G_TL, N, i, col(P, C_T, N, i));
   bool solid = icol(P, I_KIND, N, i) == 0;
   double rho = col(P, C_RHO, N, i);
   double c2 = solid ? 1.0 / (rho * rho) : 0.0;
-  for (int c = 0; c < 6; ++c) gcol(P, G_SRHO + c, N, i) = (float)(c2 * col(P, C_SIG + c, N, i));
-  gcol(P, G_MRHO, N, i) = solid ? (float)(col(P, C_MASS, N, i) / rho) : 0.f;
-  gcol(P, G_RHO, N, i) = (float)rho;
-  gcol(P, G_PR2, N, i) = (float)(c2 * col(P, C_P, N, i));
-  gcol(P, G_H, N, i) = (float)col(P, C_H, N, i);
-  gcol(P, G_M, N, i) = (float)col(P, C_MASS, N, i);
-  gcol(P, G_CS, N, i) = (float)col(P, C_CS, N, i);
-  gcol(P, G_ALPHA, N, i) = (float)col(P, C_ALPHA, N, i);
-  gcol(P, G_BETA, N, i) = (float)col(P, C_BETA, N, i);
-  gcol(P, G_KT, N, i) = (float)col(P, C_KT, N, i);
+  float xh[3], xl[3], vh[3], vl[3], th, tl;
+  for (int d = 0; d < 3; ++d) {
+    ff_split(col(P, C_X + d, N, i), xh[d], xl[d]);
+    ff_split(col(P, C_V + d, N, i), vh[d], vl[d]);
+  }
+  ff_split(col(P, C_T, N, i), th, tl);
+  float4* r = P.rc + i;
+  r[(size_t)RC_XH * N] = make_float4(xh[0], xh[1], xh[2], (float)col(P, C_H, N, i));
+  r[(size_t)RC_XL * N] = make_float4(xl[0], xl[1], xl[2], (float)col(P, C_MASS, N, i));
+  r[(size_t)RC_VH * N] = make_float4(vh[0], vh[1], vh[2], (float)rho);
+  r[(size_t)RC_VL * N] = make_float4(vl[0], vl[1], vl[2], solid ? (float)(col(P, C_MASS, N, i) / rho) : 0.f);
+  r[(size_t)RC_S0 * N] = make_float4((float)(c2 * col(P, C_SIG, N, i)), (float)(c2 * col(P, C_SIG + 1, N, i)),
+                         (float)(c2 * col(P, C_SIG + 2, N, i)), (float)(c2 * col(P, C_SIG + 3, N, i)));
+  r[(size_t)RC_S1 * N] = make_float4((float)(c2 * col(P, C_SIG + 4, N, i)), (float)(c2 * col(P, C_SIG + 5, N, i)),
+                         (float)(c2 * col(P, C_P, N, i)), (float)col(P, C_CS, N, i));
+  r[(size_t)RC_MISC * N] = make_float4((float)col(P, C_ALPHA, N, i), (float)col(P, C_BETA, N, i), (float)col(P, C_KT, N, i), th);
+  r[(size_t)RC_T2 * N] = make_float4(tl, 0.f, 0.f, 0.f);
 }
 
 // ---------------------------------------------------------------- accel
@@ -97,40 +95,36 @@ __global__ void __launch_bounds__(BLOCK) k_accel_mx(DevPtrs P, DomainConst K) {
     colw(P, C_A, N, i) = 0.0; colw(P, C_A + 1, N, i) = 0.0; colw(P, C_A + 2, N, i) = 0.0;
     return;
   }
-  float xh0 = gcol(P, G_XH, N, i), xh1 = gcol(P, G_XH + 1, N, i), xh2 = gcol(P, G_XH + 2, N, i);
-  float xl0 = gcol(P, G_XL, N, i), xl1 = gcol(P, G_XL + 1, N, i), xl2 = gcol(P, G_XL + 2, N, i);
-  float vh0 = gcol(P, G_VH, N, i), vh1 = gcol(P, G_VH + 1, N, i), vh2 = gcol(P, G_VH + 2, N, i);
-  float vl0 = gcol(P, G_VL, N, i), vl1 = gcol(P, G_VL + 1, N, i), vl2 = gcol(P, G_VL + 2, N, i);
-  float hi = gcol(P, G_H, N, i), rhoi = gcol(P, G_RHO, N, i), csi = gcol(P, G_CS, N, i);
-  float ai = gcol(P, G_ALPHA, N, i), bi = gcol(P, G_BETA, N, i);
-  float Si[6];
-  for (int c = 0; c < 6; ++c) Si[c] = gcol(P, G_SRHO + c, N, i);
+  const float4* ri = P.rc + i;
+  float4 xh = ld4(ri + (size_t)RC_XH * N), xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
+  float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1 = ld4(ri + (size_t)RC_S1 * N), mi = ld4(ri + (size_t)RC_MISC * N);
   KSum a0, a1, a2;
   int len = P.row_len[i];
+  const int* nb = P.nbr + i;
   for (int k = 0; k < len; ++k) {
-    int j = P.nbr[(size_t)k * N + i];
-    GeoF g = geo_f(P, N, G_XH, G_XL, xh0, xh1, xh2, xl0, xl1, xl2, hi, j);
-    float Alpha = 0.5f * (ai + gcol(P, G_ALPHA, N, j)), Beta = 0.5f * (bi + gcol(P, G_BETA, N, j));
-    float v0 = (vh0 - gcol(P, G_VH, N, j)) + (vl0 - gcol(P, G_VL, N, j));
-    float v1 = (vh1 - gcol(P, G_VH + 1, N, j)) + (vl1 - gcol(P, G_VL + 1, N, j));
-    float v2 = (vh2 - gcol(P, G_VH + 2, N, j)) + (vl2 - gcol(P, G_VL + 2, N, j));
+    int j = nb[(size_t)k * N];
+    const float4* rj = P.rc + j;
+    float4 jxh = ld4(rj + (size_t)RC_XH * N), jxl = ld4(rj + (size_t)RC_XL * N), jvh = ld4(rj + (size_t)RC_VH * N), jvl = ld4(rj + (size_t)RC_VL * N);
+    float4 js0 = ld4(rj + (size_t)RC_S0 * N), js1 = ld4(rj + (size_t)RC_S1 * N), jmi = ld4(rj + (size_t)RC_MISC * N);
+    float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
+    float v0 = (vh.x - jvh.x) + (vl.x - jvl.x), v1 = (vh.y - jvh.y) + (vl.y - jvl.y), v2 = (vh.z - jvh.z) + (vl.z - jvl.z);
+    float hh = 0.5f * (xh.w + jxh.w);
+    float r2 = x0 * x0 + x1 * x1 + x2 * x2, r;
+    float GK = grad_kernel_f(r2, hh, &r);
+    float Alpha = 0.5f * (mi.x + jmi.x), Beta = 0.5f * (mi.y + jmi.y);
     float PIs = 0.f;
     if (Alpha != 0.f || Beta != 0.f) {
-      float dvx = v0 * g.x0 + v1 * g.x1 + v2 * g.x2;
-      if (dvx < 0.f) {
-        float MU = g.hh * dvx / (g.r * g.r + 0.01f * g.hh * g.hh);
-        float Cij = 0.5f * (csi + gcol(P, G_CS, N, j));
-        PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5f * (rhoi + gcol(P, G_RHO, N, j)));
+      float dvx = v0 * x0 + v1 * x1 + v2 * x2;
+      if (dvx < 0.f) {  // Monaghan viscosity (InteractionAlt.cpp:74-94)
+        float MU = hh * dvx / (r * r + 0.01f * hh * hh);
+        float Cij = 0.5f * (s1.w + js1.w);
+        PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5f * (vh.w + jvh.w));
       }
     }
-    float S0 = Si[0] + gcol(P, G_SRHO + 0, N, j) + PIs;
-    float S1 = Si[1] + gcol(P, G_SRHO + 1, N, j) + PIs;
-    float S2 = Si[2] + gcol(P, G_SRHO + 2, N, j) + PIs;
-    float S3 = Si[3] + gcol(P, G_SRHO + 3, N, j);
-    float S4 = Si[4] + gcol(P, G_SRHO + 4, N, j);
-    float S5 = Si[5] + gcol(P, G_SRHO + 5, N, j);
-    float g0 = g.GK * g.x0, g1 = g.GK * g.x1, g2 = g.GK * g.x2;
-    float mj = gcol(P, G_M, N, j);
+    float S0 = s0.x + js0.x + PIs, S1 = s0.y + js0.y + PIs, S2 = s0.z + js0.z + PIs;
+    float S3 = s0.w + js0.w, S4 = s1.x + js1.x, S5 = s1.y + js1.y;
+    float g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
+    float mj = jxl.w;
     a0.add(mj * (g0 * S0 + g1 * S3 + g2 * S4));
     a1.add(mj * (g0 * S3 + g1 * S1 + g2 * S5));
     a2.add(mj * (g0 * S4 + g1 * S5 + g2 * S2));
@@ -147,21 +141,22 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift_mx(DevPtrs P, DomainCon
   double rhoi = col(P, C_RHO, N, i);
   double dd = 0.0;
   bool solid = icol(P, I_KIND, N, i) == 0;
+  const float4* ri = P.rc + i;
+  float4 xh = ld4(ri + (size_t)RC_XH * N);
   if (solid) {
-    float xh0 = gcol(P, G_XH, N, i), xh1 = gcol(P, G_XH + 1, N, i), xh2 = gcol(P, G_XH + 2, N, i);
-    float xl0 = gcol(P, G_XL, N, i), xl1 = gcol(P, G_XL + 1, N, i), xl2 = gcol(P, G_XL + 2, N, i);
-    float vh0 = gcol(P, G_VH, N, i), vh1 = gcol(P, G_VH + 1, N, i), vh2 = gcol(P, G_VH + 2, N, i);
-    float vl0 = gcol(P, G_VL, N, i), vl1 = gcol(P, G_VL + 1, N, i), vl2 = gcol(P, G_VL + 2, N, i);
-    float hi = gcol(P, G_H, N, i);
+    float4 xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
     KSum s;
     int len = P.row_len[i];
+    const int* nb = P.nbr + i;
     for (int k = 0; k < len; ++k) {
-      int j = P.nbr[(size_t)k * N + i];
-      GeoF g = geo_f(P, N, G_XH, G_XL, xh0, xh1, xh2, xl0, xl1, xl2, hi, j);
-      float v0 = (vh0 - gcol(P, G_VH, N, j)) + (vl0 - gcol(P, G_VL, N, j));
-      float v1 = (vh1 - gcol(P, G_VH + 1, N, j)) + (vl1 - gcol(P, G_VL + 1, N, j));
-      float v2 = (vh2 - gcol(P, G_VH + 2, N, j)) + (vl2 - gcol(P, G_VL + 2, N, j));
-      s.add(gcol(P, G_MRHO, N, j) * (g.GK * (v0 * g.x0 + v1 * g.x1 + v2 * g.x2)));
+      int j = nb[(size_t)k * N];
+      const float4* rj = P.rc + j;
+      float4 jxh = ld4(rj + (size_t)RC_XH * N), jxl = ld4(rj + (size_t)RC_XL * N), jvh = ld4(rj + (size_t)RC_VH * N), jvl = ld4(rj + (size_t)RC_VL * N);
+      float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
+      float v0 = (vh.x - jvh.x) + (vl.x - jvl.x), v1 = (vh.y - jvh.y) + (vl.y - jvl.y), v2 = (vh.z - jvh.z) + (vl.z - jvl.z);
+      float r;
+      float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
+      s.add(jvl.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
     }
     dd = s.value() * rhoi;
   }
@@ -170,8 +165,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift_mx(DevPtrs P, DomainCon
   colw(P, C_RHON, N, i) = rn;
   double mrn = solid ? col(P, C_MASS, N, i) / rn : 0.0;
   colw(P, C_MRHON, N, i) = mrn;
-  gcol(P, G_MRHON, N, i) = (float)mrn;
-  gcol(P, G_RHON, N, i) = (float)rn;
+  float nxh[3], nxl[3], nvh[3], nvl[3];
   for (int d = 0; d < 3; ++d) {
     double v = col(P, C_V + d, N, i);
     double du = v * dt;
@@ -180,15 +174,83 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift_mx(DevPtrs P, DomainCon
     double vn = v + col(P, C_A + d, N, i) * dt / 2.;
     colw(P, C_XN + d, N, i) = xn;
     colw(P, C_VN + d, N, i) = vn;
-    store_ff(P, G_XHN + d, G_XLN + d, N, i, xn);
-    store_ff(P, G_VHN + d, G_VLN + d, N, i, vn);
+    ff_split(xn, nxh[d], nxl[d]);
+    ff_split(vn, nvh[d], nvl[d]);
   }
+  // Pressure of the updated density (EOS case 0, Functions.cpp:206-212) and the
+  // temperature after this step's update (Thermal.cpp:727-734): both depend only
+  // on this particle, so the fused rate/energy gather can read them.
+  double cs = col(P, C_CS, N, i);
+  double pn = col(P, C_P0, N, i) + (cs * cs) * (rn - col(P, C_RHO0, N, i));
+  double Tn = col(P, C_T, N, i) + (K.thermal_solver ? dt * col(P, C_DTDT, N, i) : 0.0);
+  float th, tl;
+  ff_split(Tn, th, tl);
+  float4* r = P.rn + i;
+  r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], xh.w);
+  r[(size_t)RN_XL * N] = make_float4(nxl[0], nxl[1], nxl[2], (float)col(P, C_MASS, N, i));
+  r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], (float)rn);
+  r[(size_t)RN_VL * N] = make_float4(nvl[0], nvl[1], nvl[2], (float)mrn);
+  r[(size_t)RN_E * N] = make_float4(solid ? (float)(pn / (rn * rn)) : 0.f, ri[(size_t)RC_MISC * N].z, th, tl);
 }
 
-// ---------------------------------------------------------------- rate + stress
-// Radial return with the Jaumann increment formed in FP32 and accumulated
-// into the FP64 deviatoric stress; the yield check, scale factor and plastic
-// strain increment are FP64 (Particle.cpp:960-1067).
+// ---------------------------------------------------------------- rates + energy + conduction
+// Gather at x(n+1), v(n+1): strain/rotation rate sums (InteractionAlt.cpp:263-479),
+// the kinetic-energy pair sum (Domain.cpp:1752-1808) and conduction (Thermal.cpp:53-219).
+__global__ void __launch_bounds__(BLOCK) k_rate_mx(DevPtrs P, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double dkin = 0.0, cond = 0.0;
+  if (icol(P, I_KIND, N, i) == 0) {
+    const float4* ri = P.rn + i;
+    float4 xh = ld4(ri + (size_t)RN_XH * N), xl = ld4(ri + (size_t)RN_XL * N), vh = ld4(ri + (size_t)RN_VH * N), vl = ld4(ri + (size_t)RN_VL * N), e = ld4(ri + (size_t)RN_E * N);
+    KSum M[9];  // sum_j (m_j / rho_j) (-GK / 2) (v_i - v_j)_k (x_i - x_j)_l
+    KSum kin, cnd;
+    int len = P.row_len[i], split = P.row_split[i];
+    const int* nb = P.nbr + i;
+    bool thermal = K.thermal_solver;
+    for (int k = 0; k < len; ++k) {
+      int j = nb[(size_t)k * N];
+      const float4* rj = P.rn + j;
+      float4 jxh = ld4(rj + (size_t)RN_XH * N), jxl = ld4(rj + (size_t)RN_XL * N), jvh = ld4(rj + (size_t)RN_VH * N), jvl = ld4(rj + (size_t)RN_VL * N);
+      float4 je = ld4(rj + (size_t)RN_E * N);
+      float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
+      float b0 = (vh.x - jvh.x) + (vl.x - jvl.x), b1 = (vh.y - jvh.y) + (vl.y - jvl.y), b2 = (vh.z - jvh.z) + (vl.z - jvl.z);
+      float r;
+      float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
+      float w = jvl.w * (-0.5f * GK);
+      float wb0 = w * b0, wb1 = w * b1, wb2 = w * b2;
+      M[0].add(wb0 * x0); M[1].add(wb0 * x1); M[2].add(wb0 * x2);
+      M[3].add(wb1 * x0); M[4].add(wb1 * x1); M[5].add(wb1 * x2);
+      M[6].add(wb2 * x0); M[7].add(wb2 * x1); M[8].add(wb2 * x2);
+      bool up = k < split;  // original index of j larger than i's
+      float dv = GK * (b0 * x0 + b1 * x1 + b2 * x2);
+      float pk = 0.5f * (up ? jxl.w : xl.w) * (e.x + je.x) * dv;
+      kin.add(up ? pk : -pk);
+      if (thermal) {
+        float wt = up ? jvl.w : vl.w;  // m_P2 / rho_P2 for both ends of the pair
+        float dT = (e.z - je.z) + (e.w - je.w);
+        cnd.add(wt * 4.f * (e.y * je.y) / (e.y + je.y) * dT * GK);
+      }
+    }
+    double m[9];
+    for (int c = 0; c < 9; ++c) m[c] = M[c].value();
+    out[0] = (float)(2.0 * m[0]); out[1] = (float)(2.0 * m[4]); out[2] = (float)(2.0 * m[8]);
+    out[3] = (float)(m[1] + m[3]); out[4] = (float)(m[2] + m[6]); out[5] = (float)(m[5] + m[7]);
+    out[6] = (float)(m[1] - m[3]); out[7] = (float)(m[2] - m[6]); out[8] = (float)(m[5] - m[7]);
+    dkin = kin.value();
+    cond = cnd.value();
+  }
+  for (int c = 0; c < 9; ++c) P.rates[(size_t)c * N + i] = out[c];
+  colw(P, C_DKIN, N, i) = dkin;
+  colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
+}
+
+// ---------------------------------------------------------------- elementwise update
+// Radial return with the Jaumann increment formed in FP32 and accumulated into
+// the FP64 deviatoric stress; yield check, scale factor and plastic increment
+// in FP64 (Particle.cpp:960-1067).
 __device__ __forceinline__ double stress_update_mx(StressIO& s, const float sr[6], const float rr[3], double rho,
                                                    double rho0, double Cs, double P0, double G, double T, int fail,
                                                    int model, const MaterialDev* M, double dt) {
@@ -206,8 +268,7 @@ __device__ __forceinline__ double stress_update_mx(StressIO& s, const float sr[6
     float srt = S[a][2] * W[b][2] + S[a][1] * W[b][1] + S[a][0] * W[b][0];
     float rs = W[a][2] * S[2][b] + W[a][1] * S[1][b] + W[a][0] * S[0][b];
     float dev = sr[c] - (c < 3 ? s3 : 0.f);
-    float inc = dtf * (twoG * dev + srt + rs);
-    t6[c] = s.tau[c] + (double)inc;
+    t6[c] = s.tau[c] + (double)(dtf * (twoG * dev + srt + rs));
   }
   float d01 = sr[0] - sr[1], d12 = sr[1] - sr[2], d20 = sr[2] - sr[0];
   float esr = sqrtf(0.5f * (d01 * d01 + d12 * d12 + d20 * d20) + 3.0f * (sr[3] * sr[3] + sr[5] * sr[5] + sr[4] * sr[4]));
@@ -218,12 +279,12 @@ __device__ __forceinline__ double stress_update_mx(StressIO& s, const float sr[6
                        2.0 * t6[5] * t6[5] + t6[2] * t6[2]);
     double sig_trial = sqrt(3.0 * J2);
     double ratio = s.sigmay / sig_trial;
-    double sc = (1.0 < ratio) ? 1.0 : ratio;
-    if (sc < 1.0)
+    double sc = (1.0 < ratio) ? 1.0 : ratio;  // std::min(ratio, 1.0)
+    if (sc != 1.0)
       for (int c = 0; c < 6; ++c) t6[c] = sc * t6[c];
     if (model == 1 && M) {
-      s.sigmay = (double)(M->K * powf((float)(s.pl_strain + M->eps0), (float)M->m));
-      if (!(s.pl_strain + M->eps0 > M->eps1)) s.sigmay = M->sy0;
+      if (s.pl_strain + M->eps0 > M->eps1) s.sigmay = (double)((float)M->K * powf((float)(s.pl_strain + M->eps0), (float)M->m));
+      else s.sigmay = M->sy0;
     } else if (model == 2 && M) {
       float Th = (float)((T - M->T_t) / (M->T_m - M->T_t));
       float f = 1.0f;
@@ -255,72 +316,32 @@ __device__ __forceinline__ double stress_update_mx(StressIO& s, const float sr[6
   return dep;
 }
 
-// Gather half: strain-rate and rotation-rate sums (InteractionAlt.cpp:263-479),
-// written as float columns for the elementwise update below.  Kept lean so the
-// gather runs at high occupancy.
-__global__ void __launch_bounds__(BLOCK) k_rate_mx(DevPtrs P, DomainConst K, float* rates) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
-  size_t N = K.N;
-  float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  if (icol(P, I_KIND, N, i) == 0) {
-    float xh0 = gcol(P, G_XHN, N, i), xh1 = gcol(P, G_XHN + 1, N, i), xh2 = gcol(P, G_XHN + 2, N, i);
-    float xl0 = gcol(P, G_XLN, N, i), xl1 = gcol(P, G_XLN + 1, N, i), xl2 = gcol(P, G_XLN + 2, N, i);
-    float vh0 = gcol(P, G_VHN, N, i), vh1 = gcol(P, G_VHN + 1, N, i), vh2 = gcol(P, G_VHN + 2, N, i);
-    float vl0 = gcol(P, G_VLN, N, i), vl1 = gcol(P, G_VLN + 1, N, i), vl2 = gcol(P, G_VLN + 2, N, i);
-    float hi = gcol(P, G_H, N, i);
-    KSum M[9];  // sum_j (m_j/rho_j) (-GK/2) (v_i - v_j)_k (x_i - x_j)_l
-    int len = P.row_len[i];
-    for (int k = 0; k < len; ++k) {
-      int j = P.nbr[(size_t)k * N + i];
-      GeoF g = geo_f(P, N, G_XHN, G_XLN, xh0, xh1, xh2, xl0, xl1, xl2, hi, j);
-      float b0 = (vh0 - gcol(P, G_VHN, N, j)) + (vl0 - gcol(P, G_VLN, N, j));
-      float b1 = (vh1 - gcol(P, G_VHN + 1, N, j)) + (vl1 - gcol(P, G_VLN + 1, N, j));
-      float b2 = (vh2 - gcol(P, G_VHN + 2, N, j)) + (vl2 - gcol(P, G_VLN + 2, N, j));
-      float w = gcol(P, G_MRHON, N, j) * (-0.5f * g.GK);
-      float wb0 = w * b0, wb1 = w * b1, wb2 = w * b2;
-      M[0].add(wb0 * g.x0); M[1].add(wb0 * g.x1); M[2].add(wb0 * g.x2);
-      M[3].add(wb1 * g.x0); M[4].add(wb1 * g.x1); M[5].add(wb1 * g.x2);
-      M[6].add(wb2 * g.x0); M[7].add(wb2 * g.x1); M[8].add(wb2 * g.x2);
-    }
-    double m[9];
-    for (int c = 0; c < 9; ++c) m[c] = M[c].value();
-    // StrainRate = symmetric part (InteractionAlt.cpp:338-351), RotationRate
-    // = antisymmetric part (355-361)
-    out[0] = (float)(2.0 * m[0]); out[1] = (float)(2.0 * m[4]); out[2] = (float)(2.0 * m[8]);
-    out[3] = (float)(m[1] + m[3]); out[4] = (float)(m[2] + m[6]); out[5] = (float)(m[5] + m[7]);
-    out[6] = (float)(m[1] - m[3]); out[7] = (float)(m[2] - m[6]); out[8] = (float)(m[5] - m[7]);
-  }
-  for (int c = 0; c < 9; ++c) rates[(size_t)c * N + i] = out[c];
-}
-
-// Elementwise half: constitutive update, heating, temperature, and the
-// next-step buffers becoming current.
-__global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K, const float* rates) {
+__global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K) {
   __shared__ double sh[32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
   double dt = K.dt;
-  double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300;
+  double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300, dkin = 0.0, dint = 0.0;
   if (i < K.N) {
     for (int d = 0; d < 3; ++d) {
       colw(P, C_X + d, N, i) = col(P, C_XN + d, N, i);
       colw(P, C_V + d, N, i) = col(P, C_VN + d, N, i);
-      gcol(P, G_XH + d, N, i) = gcol(P, G_XHN + d, N, i);
-      gcol(P, G_XL + d, N, i) = gcol(P, G_XLN + d, N, i);
-      gcol(P, G_VH + d, N, i) = gcol(P, G_VHN + d, N, i);
-      gcol(P, G_VL + d, N, i) = gcol(P, G_VLN + d, N, i);
     }
     double rho = col(P, C_RHON, N, i);
     colw(P, C_RHO, N, i) = rho;
     colw(P, C_MRHO, N, i) = col(P, C_MRHON, N, i);
-    gcol(P, G_MRHO, N, i) = gcol(P, G_MRHON, N, i);
-    gcol(P, G_RHO, N, i) = gcol(P, G_RHON, N, i);
+    const float4* rn = P.rn + i;
+    float4* rc = P.rc + i;
+    float4 nxh = rn[(size_t)RN_XH * N], nxl = rn[(size_t)RN_XL * N], nvh = rn[(size_t)RN_VH * N], nvl = rn[(size_t)RN_VL * N], ne = rn[(size_t)RN_E * N];
+    rc[(size_t)RC_XH * N] = nxh; rc[(size_t)RC_XL * N] = nxl; rc[(size_t)RC_VH * N] = nvh; rc[(size_t)RC_VL * N] = nvl;
+    float4 s1 = rc[(size_t)RC_S1 * N];
+    float4 misc = rc[(size_t)RC_MISC * N];
     maxpl = col(P, C_PLS, N, i);
+    dkin = col(P, C_DKIN, N, i);
     if (icol(P, I_KIND, N, i) == 0) {
       float sr[6], rr[3];
-      for (int c = 0; c < 6; ++c) sr[c] = rates[(size_t)c * N + i];
-      for (int c = 0; c < 3; ++c) rr[c] = rates[(size_t)(6 + c) * N + i];
+      for (int c = 0; c < 6; ++c) sr[c] = P.rates[(size_t)c * N + i];
+      for (int c = 0; c < 3; ++c) rr[c] = P.rates[(size_t)(6 + c) * N + i];
       StressIO s;
       for (int c = 0; c < 6; ++c) {
         s.tau[c] = col(P, C_TAU + c, N, i); s.eps[c] = col(P, C_EPS + c, N, i);
@@ -333,18 +354,8 @@ __global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K, c
       double T = col(P, C_T, N, i);
       stress_update_mx(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i),
                        col(P, C_G, N, i), T, icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), Mt, dt);
-      for (int c = 0; c < 6; ++c) {
-        colw(P, C_TAU + c, N, i) = s.tau[c]; colw(P, C_SIG + c, N, i) = s.sig[c];
-        colw(P, C_EPS + c, N, i) = s.eps[c]; colw(P, C_EPL + c, N, i) = s.epl[c];
-        colw(P, C_EPLI + c, N, i) = s.epli[c]; colw(P, C_SR + c, N, i) = (double)sr[c];
-      }
-      for (int c = 0; c < 3; ++c) colw(P, C_RR + c, N, i) = (double)rr[c];
-      colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
-      colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = s.esr;
-      maxpl = s.pl_strain;
-      float c2 = 1.0f / ((float)rho * (float)rho);
-      for (int c = 0; c < 6; ++c) gcol(P, G_SRHO + c, N, i) = c2 * (float)s.sig[c];
-      gcol(P, G_PR2, N, i) = c2 * (float)s.pressure;
+      double srd[6];
+      for (int c = 0; c < 6; ++c) srd[c] = (double)sr[c];
       if (K.pl_heating) {
         double q = col(P, C_QPL, N, i);
         if (s.delta_pl_strain > 0.0) q = plastic_heat(s.sig, s.epli, dt);
@@ -352,16 +363,40 @@ __global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K, c
         colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + q * dt;
         plw = col(P, C_MASS, N, i) / rho * q;
       }
-      if (K.thermal_solver) {
+      if (K.thermal_solver) {  // T(n+1) (already in the next record), then CalcTempInc's dTdt
         T += dt * col(P, C_DTDT, N, i);
         colw(P, C_T, N, i) = T;
-        store_ff(P, G_TH, G_TL, N, i, T);
         maxT = T; minT = T;
+        double f = 1. / (rho * col(P, C_CPT, N, i));
+        double dTdt = f * (col(P, C_DINT, N, i) + col(P, C_QSRC, N, i) + col(P, C_QPL, N, i) * K.pl_work_heat_frac);
+        colw(P, C_DTDT, N, i) = dTdt;
+        double st = col(P, C_THEXP, N, i) * dTdt;  // CalcThermalExpStrainRate
+        for (int c = 0; c < 3; ++c) srd[c] = srd[c] + st;
       }
+      for (int c = 0; c < 6; ++c) {
+        colw(P, C_TAU + c, N, i) = s.tau[c]; colw(P, C_SIG + c, N, i) = s.sig[c];
+        colw(P, C_EPS + c, N, i) = s.eps[c]; colw(P, C_EPL + c, N, i) = s.epl[c];
+        colw(P, C_EPLI + c, N, i) = s.epli[c]; colw(P, C_SR + c, N, i) = srd[c];
+      }
+      for (int c = 0; c < 3; ++c) colw(P, C_RR + c, N, i) = (double)rr[c];
+      colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
+      colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = s.esr;
+      maxpl = s.pl_strain;
+      // CalcIntEnergyEqn (Particle.cpp:941-950)
+      dint = col(P, C_MRHO, N, i) * (s.tau[0] * srd[0] + 2.0 * s.tau[3] * srd[3] + 2.0 * s.tau[4] * srd[4] +
+                                     s.tau[1] * srd[1] + 2.0 * s.tau[5] * srd[5] + s.tau[2] * srd[2]);
+      colw(P, C_DINT, N, i) = dint;
+      float c2 = 1.0f / ((float)rho * (float)rho);
+      rc[(size_t)RC_S0 * N] = make_float4(c2 * (float)s.sig[0], c2 * (float)s.sig[1], c2 * (float)s.sig[2], c2 * (float)s.sig[3]);
+      rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], c2 * (float)s.pressure, s1.w);
     }
+    rc[(size_t)RC_MISC * N] = make_float4(misc.x, misc.y, misc.z, ne.z);
+    rc[(size_t)RC_T2 * N] = make_float4(ne.w, 0.f, 0.f, 0.f);
   }
   double r;
   r = block_reduce<1>(maxpl, sh); if (threadIdx.x == 0) P.partials[S_MAXPL * K.nblocks + blockIdx.x] = r;
+  r = block_reduce<0>(dkin, sh); if (threadIdx.x == 0) P.partials[S_DKIN * K.nblocks + blockIdx.x] = r;
+  r = block_reduce<0>(dint, sh); if (threadIdx.x == 0) P.partials[S_DINT * K.nblocks + blockIdx.x] = r;
   if (K.pl_heating) { r = block_reduce<0>(plw, sh); if (threadIdx.x == 0) P.partials[S_PLW * K.nblocks + blockIdx.x] = r; }
   if (K.thermal_solver) {
     r = block_reduce<1>(maxT, sh); if (threadIdx.x == 0) P.partials[S_MAXT * K.nblocks + blockIdx.x] = r;
@@ -369,64 +404,9 @@ __global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K, c
   }
 }
 
-// ---------------------------------------------------------------- energies (+ conduction)
-__global__ void __launch_bounds__(BLOCK) k_energy_mx(DevPtrs P, DomainConst K) {
-  __shared__ double sh[32];
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  size_t N = K.N;
-  double dkin = 0.0, dint = 0.0;
-  if (i < K.N && icol(P, I_KIND, N, i) == 0) {
-    float xh0 = gcol(P, G_XH, N, i), xh1 = gcol(P, G_XH + 1, N, i), xh2 = gcol(P, G_XH + 2, N, i);
-    float xl0 = gcol(P, G_XL, N, i), xl1 = gcol(P, G_XL + 1, N, i), xl2 = gcol(P, G_XL + 2, N, i);
-    float vh0 = gcol(P, G_VH, N, i), vh1 = gcol(P, G_VH + 1, N, i), vh2 = gcol(P, G_VH + 2, N, i);
-    float vl0 = gcol(P, G_VL, N, i), vl1 = gcol(P, G_VL + 1, N, i), vl2 = gcol(P, G_VL + 2, N, i);
-    float hi = gcol(P, G_H, N, i), mi = gcol(P, G_M, N, i), mrhoi = gcol(P, G_MRHO, N, i), pri = gcol(P, G_PR2, N, i);
-    float thi = gcol(P, G_TH, N, i), tli = gcol(P, G_TL, N, i), ki = gcol(P, G_KT, N, i);
-    KSum kin, cond;
-    int len = P.row_len[i], split = P.row_split[i];
-    for (int k = 0; k < len; ++k) {
-      int j = P.nbr[(size_t)k * N + i];
-      GeoF g = geo_f(P, N, G_XH, G_XL, xh0, xh1, xh2, xl0, xl1, xl2, hi, j);
-      float b0 = (vh0 - gcol(P, G_VH, N, j)) + (vl0 - gcol(P, G_VL, N, j));
-      float b1 = (vh1 - gcol(P, G_VH + 1, N, j)) + (vl1 - gcol(P, G_VL + 1, N, j));
-      float b2 = (vh2 - gcol(P, G_VH + 2, N, j)) + (vl2 - gcol(P, G_VL + 2, N, j));
-      float dv = g.GK * (b0 * g.x0 + b1 * g.x1 + b2 * g.x2);
-      bool up = k < split;
-      float pk = 0.5f * (up ? gcol(P, G_M, N, j) : mi) * (pri + gcol(P, G_PR2, N, j)) * dv;
-      kin.add(up ? pk : -pk);
-      if (K.thermal_solver) {
-        float kj = gcol(P, G_KT, N, j);
-        float w = up ? gcol(P, G_MRHO, N, j) : mrhoi;
-        float dT = (thi - gcol(P, G_TH, N, j)) + (tli - gcol(P, G_TL, N, j));
-        cond.add(w * 4.f * (ki * kj) / (ki + kj) * dT * g.GK);
-      }
-    }
-    dkin = kin.value();
-    double sr[6];
-    for (int c = 0; c < 6; ++c) sr[c] = col(P, C_SR + c, N, i);
-    if (K.thermal_solver) {
-      double rho = col(P, C_RHO, N, i);
-      double f = 1. / (rho * col(P, C_CPT, N, i));
-      double dTdt = f * (cond.value() + col(P, C_QSRC, N, i) + col(P, C_QPL, N, i) * K.pl_work_heat_frac);
-      colw(P, C_DTDT, N, i) = dTdt;
-      double s = col(P, C_THEXP, N, i) * dTdt;
-      for (int c = 0; c < 3; ++c) { sr[c] = sr[c] + s; colw(P, C_SR + c, N, i) = sr[c]; }
-    }
-    double t[6];
-    for (int c = 0; c < 6; ++c) t[c] = col(P, C_TAU + c, N, i);
-    dint = col(P, C_MRHO, N, i) *
-           (t[0] * sr[0] + 2.0 * t[3] * sr[3] + 2.0 * t[4] * sr[4] + t[1] * sr[1] + 2.0 * t[5] * sr[5] + t[2] * sr[2]);
-    colw(P, C_DKIN, N, i) = dkin;
-    colw(P, C_DINT, N, i) = dint;
-  }
-  double r;
-  r = block_reduce<0>(dkin, sh); if (threadIdx.x == 0) P.partials[S_DKIN * K.nblocks + blockIdx.x] = r;
-  r = block_reduce<0>(dint, sh); if (threadIdx.x == 0) P.partials[S_DINT * K.nblocks + blockIdx.x] = r;
-}
-
 void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, cudaStream_t s) {
-  k_refresh_shadows<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, force);
-  mark(s, "k_refresh_shadows");
+  k_refresh_records<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, force);
+  mark(s, "k_refresh_records");
 }
 
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
@@ -441,13 +421,10 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   k_density_drift_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  float* rates = P.g + (size_t)G_RATES * K.N;
-  k_rate_mx<<<nb, BLOCK, 0, s>>>(P, K, rates);
+  k_rate_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_rate_mx");
-  k_stress_mx<<<nb, BLOCK, 0, s>>>(P, K, rates);
+  k_stress_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_stress_mx");
-  k_energy_mx<<<nb, BLOCK, 0, s>>>(P, K);
-  mark(s, "k_energy_mx");
   launch_step_tail(P, K, s);
 }
 
