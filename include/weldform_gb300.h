@@ -127,6 +127,10 @@ int wf_set_particle_array_f64(wf_domain* d, const char* field, const double* src
 int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int64_t n);
 /* Integer arrays: "ID", "Nb", "IsFree". */
 int wf_get_particle_array_i32(wf_domain* d, const char* field, int32_t* dst, int64_t n);
+/* Per-particle integer fields as whole arrays, before the prologue: "ID",
+ * "mat", "Material_model", "Fail", "Material", "not_write_surf_ID"
+ * (Particle.h:50-265; the array form of assigning them in a loop). */
+int wf_set_particle_array_i32(wf_domain* d, const char* field, const int32_t* src, int64_t n);
 
 /* Materials (Source/Material.h:64-224, Source/Material.cpp:6-72).
  * model WF_BILINEAR: params {E, nu}            (hardening via particle Ep)
@@ -186,6 +190,23 @@ int wf_get_contact_pairs(wf_domain* d, int64_t* offsets, int32_t* idx, int64_t c
 /* Blocks until the domain's stream is idle and reports deferred device
  * status (non-finite state, neighbour overflow, bounded-wait timeout). */
 int wf_synchronize(wf_domain* d);
+
+/* ---- device checkpoints ----------------------------------------------------
+ * The reference's restart reads positions only (Input.cpp:4-97); these keep
+ * the complete solver state (particle arena, neighbour and contact lists,
+ * rigid meshes, step scalars) in device memory, in up to 16 slots, so a run
+ * can be rewound (recompute-based adjoints, tuning runs, what-if branches).
+ * A slot is allocated on its first save and reused afterwards. */
+int wf_checkpoint_save(wf_domain* d, int slot);
+int wf_checkpoint_restore(wf_domain* d, int slot);
+int wf_checkpoint_free(wf_domain* d, int slot);
+
+/* Chooses the thread-block size of the mixed form's three gather kernels
+ * (64, 128, 256 or 512 threads) by timing `steps` steps with each from a
+ * checkpoint of the current state, restores that state, keeps the fastest
+ * and returns it; results are cached per size bucket (particles rounded to a
+ * power of two) for later domains in the process. */
+int wf_autotune(wf_domain* d, int steps, int* block);
 
 /* ---- measurement helpers (no counterpart in the reference) ---------------
  * wf_step_timed: nsteps steps bracketed by CUDA events recorded on the

@@ -1401,6 +1401,18 @@ int wfo_get_particle_array_i32(wfo_domain* p, const char* field, int32_t* dst, i
   for (int i = 0; i < d->N; ++i) dst[i] = (*f)[i];
   return WF_OK;
 }
+int wfo_set_particle_array_i32(wfo_domain* p, const char* field, const int32_t* src, int64_t n) {
+  Domain* d = D(p);
+  std::string fn(field ? field : "");
+  if (n != d->N) return set_err(WF_ERR_ARG, "size");
+  std::vector<int>* f = fn == "not_write_surf_ID" ? &d->not_write_surf : i32_field(d, fn);
+  if (!f || fn == "Nb" || fn == "IsFree") return set_err(WF_ERR_ARG, "unknown settable particle i32 array " + fn);
+  for (int i = 0; i < d->N; ++i) {
+    (*f)[i] = src[i];
+    if (fn == "ID") d->ID_orig[i] = src[i];
+  }
+  return WF_OK;
+}
 int wfo_add_material(wfo_domain* p, int model, const double* q, int np, int* mat_id) {
   Material M; M.model = model;
   if (model == 0) { if (np < 2) return set_err(WF_ERR_ARG, "bilinear needs {E, nu}"); M.E = q[0]; M.nu = q[1]; }
@@ -1492,6 +1504,28 @@ int wfo_get_contact_pairs(wfo_domain* p, int64_t* off, int32_t* idx, int64_t cap
   return WF_OK;
 }
 int wfo_synchronize(wfo_domain*) { return WF_OK; }
+// Checkpoints of the whole oracle state (a copy of the Domain object).
+static std::vector<Domain*> g_slots[1];
+int wfo_checkpoint_save(wfo_domain* p, int slot) {
+  if (slot < 0 || slot > 15) return set_err(WF_ERR_ARG, "slot");
+  auto& v = g_slots[0];
+  if ((int)v.size() <= slot) v.resize(slot + 1, nullptr);
+  delete v[slot];
+  v[slot] = new Domain(*D(p));
+  return WF_OK;
+}
+int wfo_checkpoint_restore(wfo_domain* p, int slot) {
+  auto& v = g_slots[0];
+  if (slot < 0 || slot >= (int)v.size() || !v[slot]) return set_err(WF_ERR_STATE, "checkpoint slot is empty");
+  *D(p) = *v[slot];
+  return WF_OK;
+}
+int wfo_checkpoint_free(wfo_domain*, int slot) {
+  auto& v = g_slots[0];
+  if (slot >= 0 && slot < (int)v.size()) { delete v[slot]; v[slot] = nullptr; }
+  return WF_OK;
+}
+int wfo_autotune(wfo_domain*, int, int* block) { if (block) *block = 0; return WF_OK; }
 int wfo_step_timed(wfo_domain* p, int64_t n, double* ms, int64_t* launches) {
   auto t0 = std::chrono::steady_clock::now();
   int rc = wfo_step(p, n);

@@ -82,3 +82,13 @@ def test_mixed_contact_reaction_force():
     assert abs(o["cf"][2]) > 0
     assert abs(m["cf"][2] - o["cf"][2]) <= TOL * abs(o["cf"][2])
     _check(m, o, f)
+
+
+@pytest.mark.slow
+def test_mixed_250k_1000_steps_against_oracle():
+    """The 240,300-particle configuration of the mixed-precision study
+    (dx = 0.3353 mm) after 1000 steps, against the FP64 oracle."""
+    m, o = _run(configs.cylinder_upsetting, 1000, FIELDS, ("int_energy_sum",), dx=0.3353e-3)
+    assert m["v"].shape[0] == 240300
+    errs = _check(m, o, FIELDS)
+    print("mixed vs oracle, 240300 particles, 1000 steps:", errs)

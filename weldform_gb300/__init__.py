@@ -75,6 +75,7 @@ _SIGS = {
     "set_particle_array_f64": [_P, _S, _DP, _I64],
     "get_particle_array_f64": [_P, _S, _DP, _I64],
     "get_particle_array_i32": [_P, _S, _IP, _I64],
+    "set_particle_array_i32": [_P, _S, _IP, _I64],
     "add_material": [_P, _I, _DP, _I, ctypes.POINTER(_I)],
     "add_amplitude": [_P, _I, _DP, _DP, _I],
     "add_velocity_bc": [_P, _I, _DP, _DP, _I, _I, _D],
@@ -89,6 +90,10 @@ _SIGS = {
     "get_contact_pairs": [_P, _I64P, _IP, _I64],
     "synchronize": [_P],
     "step_timed": [_P, _I64, _DP, _I64P],
+    "checkpoint_save": [_P, _I],
+    "checkpoint_restore": [_P, _I],
+    "checkpoint_free": [_P, _I],
+    "autotune": [_P, _I, ctypes.POINTER(_I)],
     "profile_steps": [_P, _I64, ctypes.c_char_p, _I, _DP, _I64P, _I, ctypes.POINTER(_I)],
 }
 EXPORTS = ["version", "last_error"] + list(_SIGS)
@@ -271,6 +276,21 @@ class Domain:
     def synchronize(self):
         self._call("synchronize", self._h)
 
+    def checkpoint_save(self, slot: int = 0):
+        self._call("checkpoint_save", self._h, int(slot))
+
+    def checkpoint_restore(self, slot: int = 0):
+        self._call("checkpoint_restore", self._h, int(slot))
+
+    def checkpoint_free(self, slot: int = 0):
+        self._call("checkpoint_free", self._h, int(slot))
+
+    def autotune(self, steps: int = 5) -> int:
+        """Pick the gather kernels' block size by timing; returns it."""
+        b = ctypes.c_int()
+        self._call("autotune", self._h, int(steps), ctypes.byref(b))
+        return b.value
+
     def step_timed(self, n: int):
         """n steps between CUDA events on the domain's stream: (ms, kernel launches)."""
         ms = ctypes.c_double()
@@ -306,6 +326,10 @@ class Domain:
         return out.reshape(n, comps) if comps > 1 else out
 
     def set_array(self, field: str, values):
+        if field in ("ID", "mat", "Material_model", "Fail", "Material", "not_write_surf_ID"):
+            a = np.ascontiguousarray(values, dtype=np.int32).ravel()
+            self._call("set_particle_array_i32", self._h, field.encode(), a.ctypes.data_as(_IP), a.size)
+            return
         a = np.ascontiguousarray(values, dtype=np.float64).ravel()
         self._call("set_particle_array_f64", self._h, field.encode(), a.ctypes.data_as(_DP), a.size)
 

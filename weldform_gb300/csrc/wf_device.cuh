@@ -91,8 +91,8 @@ struct AmpDev {
   int id, n, offset;  // points [offset, offset+n) of the amplitude tables
 };
 
-constexpr int MAX_MATERIALS = 16;
-constexpr int MAX_BCS = 32;
+constexpr int MAX_MATERIALS = 512;
+constexpr int MAX_BCS = 520;
 constexpr int MAX_AMPS = 16;
 constexpr int MAX_AMP_POINTS = 512;
 constexpr int MAX_MESHES = 8;
@@ -156,6 +156,7 @@ struct DomainConst {
   int contact_surf_id[MAX_MESHES];
   int nblocks;         // blocks of the per-particle kernels (partials stride)
   int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
+  int gblock;          // thread-block size of the mixed form's gather kernels
 };
 
 // Device pointers, passed by value to every kernel.

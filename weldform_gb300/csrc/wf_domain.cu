@@ -8,6 +8,8 @@
 // HBM in cell-sorted order; host transfers map through the original index.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -141,6 +143,11 @@ struct wf_domain {
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
   int graph_precision = -1;
+  int graph_block = -1;
+  int gblock = 256;
+  struct Region { void* p; size_t bytes; };
+  std::vector<Region> regions;           // every mutable device region of the state
+  std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
   bool shadows_valid = false;  // float shadows of the mixed form match the FP64 state
   long long launches_per_step = 0;
   double hmax = 0;
@@ -149,6 +156,9 @@ struct wf_domain {
 
   ~wf_domain() { release(); }
   void release() {
+    for (auto& sl : slots)
+      for (void* p : sl) cudaFree(p);
+    slots.clear();
     if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
@@ -550,6 +560,12 @@ struct wf_domain {
     for (size_t m = 0; m < meshes.size(); ++m)
       for (int d = 0; d < 3; ++d) { st.mesh_v[m][d] = meshes[m].mv.c[d]; st.mesh_w[m][d] = meshes[m].mw.c[d]; }
     CK(cudaMemcpyAsync(P.st, &st, sizeof(st), cudaMemcpyHostToDevice, stream));
+    regions = {{d_f, sizeof(double) * NF64 * n}, {d_i, sizeof(int) * NI32 * n}, {P.g, sizeof(float) * NF32 * n},
+               {P.st, sizeof(StepState)}, {P.inv, sizeof(int) * n}, {P.row_len, sizeof(int) * n},
+               {P.row_split, sizeof(int) * n}, {P.nbr, sizeof(int) * MAX_NB * n}, {P.cp_len, sizeof(int) * n},
+               {P.cp, contact ? sizeof(int) * MAX_CP * n : sizeof(int)}, {P.node, sizeof(double) * hnode.size()},
+               {P.node_v, sizeof(double) * hnode.size()}, {P.elem_normal, sizeof(double) * hnorm.size()},
+               {P.elem_pplane, sizeof(double) * hpp.size()}, {P.elem_particle, sizeof(int) * hep.size()}};
     launch_prologue(P, K, stream);
     // SolverKickDrift.cpp:72-96: with contact, a search + CalculateSurface(1)
     // before the loop; the first step searches again (ClearNbData).
@@ -588,6 +604,7 @@ struct wf_domain {
   void launch_one_step() {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
+    k.gblock = gblock;
     if (k.mixed) wf::launch_step_mixed(P, k, d_fscratch, d_iscratch, stream);
     else wf::launch_step_fp64(P, k, d_fscratch, d_iscratch, stream);
   }
@@ -606,8 +623,9 @@ struct wf_domain {
     use_device();
     ensure_shadows();
     if (use_graph) {
-      if (!graph || graph_precision != precision) {
+      if (!graph || graph_precision != precision || graph_block != gblock) {
         if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+        graph_block = gblock;
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         long long l0 = wf::g_launches;
@@ -632,7 +650,7 @@ struct wf_domain {
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
     CK(cudaStreamSynchronize(stream));
-    if (use_graph && (!graph || graph_precision != precision)) step(0);
+    if (use_graph && (!graph || graph_precision != precision || graph_block != gblock)) step(0);
     ensure_shadows();
     long long l0 = wf::g_launches;
     CK(cudaEventRecord(a, stream));
@@ -680,6 +698,67 @@ struct wf_domain {
     for (auto& e : ev) cudaEventDestroy(e);
     check_errors();
     return rows;
+  }
+  void checkpoint_save(int slot) {
+    use_device();
+    if ((int)slots.size() <= slot) slots.resize(slot + 1);
+    auto& sl = slots[slot];
+    if (sl.empty())
+      for (auto& r : regions) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, r.bytes);
+        if (e != cudaSuccess) {
+          for (void* q : sl) cudaFree(q);
+          sl.clear();
+          throw CudaError{WF_ERR_NOMEM, std::string("checkpoint: ") + cudaGetErrorString(e)};
+        }
+        sl.push_back(p);
+      }
+    for (size_t k = 0; k < regions.size(); ++k)
+      CK(cudaMemcpyAsync(sl[k], regions[k].p, regions[k].bytes, cudaMemcpyDeviceToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  void checkpoint_restore(int slot) {
+    use_device();
+    if ((int)slots.size() <= slot || slots[slot].empty()) throw CudaError{WF_ERR_STATE, "checkpoint slot is empty"};
+    auto& sl = slots[slot];
+    for (size_t k = 0; k < regions.size(); ++k)
+      CK(cudaMemcpyAsync(regions[k].p, sl[k], regions[k].bytes, cudaMemcpyDeviceToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  void checkpoint_free(int slot) {
+    if ((int)slots.size() <= slot) return;
+    for (void* p : slots[slot]) cudaFree(p);
+    slots[slot].clear();
+  }
+  int autotune(int steps) {
+    static std::mutex mu;
+    static std::map<int, int> cache;  // size bucket -> block
+    int bucket = 0;
+    while ((1LL << bucket) < hp.N) ++bucket;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      auto it = cache.find(bucket);
+      if (it != cache.end()) { gblock = it->second; return gblock; }
+    }
+    const int slot = 15;
+    checkpoint_save(slot);
+    int best = 256;
+    double best_ms = 1e300;
+    for (int b : {64, 128, 256, 512}) {
+      gblock = b;
+      long long l = 0;
+      step(1);  // capture + warm
+      checkpoint_restore(slot);
+      double ms = step_timed(steps, &l);
+      checkpoint_restore(slot);
+      if (ms < best_ms) { best_ms = ms; best = b; }
+    }
+    gblock = best;
+    checkpoint_free(slot);
+    std::lock_guard<std::mutex> lk(mu);
+    cache[bucket] = best;
+    return best;
   }
   void search_now() {
     if (!prepared) throw CudaError{WF_ERR_STATE, "neighbour search before the solver prologue"};
@@ -1017,6 +1096,24 @@ int wf_get_particle_array_i32(wf_domain* d, const char* field, int32_t* dst, int
     return WF_OK;
   });
 }
+int wf_set_particle_array_i32(wf_domain* d, const char* field, const int32_t* src, int64_t n) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "integer particle fields are fixed after the prologue");
+  std::string f(field ? field : "");
+  if (n != d->hp.N) return set_err(WF_ERR_ARG, "array size mismatch");
+  int c = f == "not_write_surf_ID" ? wf::I_NWS : col_i32(f);
+  if (c < 0 || c == wf::I_NB) return set_err(WF_ERR_ARG, "unknown settable particle i32 array " + f);
+  for (int p = 0; p < d->hp.N; ++p) {
+    int v = src[p];
+    if (f == "Fail" && v > 1) return set_err(WF_ERR_UNSUPPORTED, "Undefined failure criteria for solids");
+    if (f == "Material_model" && (v < 0 || v > 2)) return set_err(WF_ERR_UNSUPPORTED, "material model");
+  }
+  for (int p = 0; p < d->hp.N; ++p) {
+    d->hp.i[c][p] = c == wf::I_NWS ? (src[p] ? 1 : 0) : src[p];
+    if (c == wf::I_ID) d->hp.i[wf::I_IDORIG][p] = src[p];
+  }
+  return WF_OK;
+}
 int wf_add_material(wf_domain* d, int model, const double* q, int np, int* mat_id) {
   NEED(d);
   if (d->prepared) return set_err(WF_ERR_STATE, "materials are fixed after the prologue");
@@ -1176,6 +1273,40 @@ int wf_profile_steps(wf_domain* d, int64_t n, char* names, int name_len, double*
       ++k;
     }
     *nk = k;
+    return WF_OK;
+  });
+}
+int wf_checkpoint_save(wf_domain* d, int slot) {
+  NEED(d);
+  if (slot < 0 || slot > 15) return set_err(WF_ERR_ARG, "checkpoint slot must be 0..15");
+  return guard([&] {
+    if (!d->prepared) return set_err(WF_ERR_STATE, "checkpoint before the prologue");
+    d->checkpoint_save(slot);
+    return WF_OK;
+  });
+}
+int wf_checkpoint_restore(wf_domain* d, int slot) {
+  NEED(d);
+  if (slot < 0 || slot > 15) return set_err(WF_ERR_ARG, "checkpoint slot must be 0..15");
+  return guard([&] {
+    if (!d->prepared) return set_err(WF_ERR_STATE, "checkpoint before the prologue");
+    d->checkpoint_restore(slot);
+    return WF_OK;
+  });
+}
+int wf_checkpoint_free(wf_domain* d, int slot) {
+  NEED(d);
+  if (slot < 0 || slot > 15) return set_err(WF_ERR_ARG, "checkpoint slot must be 0..15");
+  d->checkpoint_free(slot);
+  return WF_OK;
+}
+int wf_autotune(wf_domain* d, int steps, int* block) {
+  NEED(d);
+  if (steps < 1) return set_err(WF_ERR_ARG, "steps >= 1");
+  return guard([&] {
+    if (!d->prepared) return set_err(WF_ERR_STATE, "autotune before the prologue");
+    int b = d->autotune(steps);
+    if (block) *block = b;
     return WF_OK;
   });
 }

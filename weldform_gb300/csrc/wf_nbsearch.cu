@@ -32,8 +32,7 @@ __device__ __forceinline__ bool searching(const DevPtrs& P) { return P.st->do_se
 
 __global__ void k_cell_keys(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= K.N) return;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
   int c[3];
   for (int d = 0; d < 3; ++d) {
     double xd = P.f[(C_X + d) * (size_t)K.N + p];
@@ -46,6 +45,7 @@ __global__ void k_cell_keys(DevPtrs P, DomainConst K) {
   int key = P.cell_rank[lin];
   P.i[I_CELL * (size_t)K.N + p] = key;
   atomicAdd(&P.cell_count[key], 1);
+  }
 }
 
 __global__ void k_zero_int(DevPtrs P, int* a, long long n, int gate) {
@@ -125,19 +125,18 @@ __global__ void k_scan_down(DevPtrs P, const int* in, long long n, const long lo
 
 __global__ void k_scatter(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= K.N) return;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
   int key = P.i[I_CELL * (size_t)K.N + p];
   int pos = P.cell_start[key] + atomicAdd(&P.cell_count[key], 1);
   P.perm[pos] = p;
+  }
 }
 
 // Order each cell's slots by original particle index (insertion sort; cells
 // hold ~10-20 particles).
 __global__ void k_sort_cells(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= K.ncells) return;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < K.ncells; c += gridDim.x * blockDim.x) {
   int b = P.cell_start[c], e = P.cell_start[c + 1];
   const int* orig = P.i + I_ORIG * (size_t)K.N;
   for (int k = b + 1; k < e; ++k) {
@@ -146,6 +145,7 @@ __global__ void k_sort_cells(DevPtrs P, DomainConst K) {
     int m = k - 1;
     while (m >= b && orig[P.perm[m]] > ov) { P.perm[m + 1] = P.perm[m]; --m; }
     P.perm[m + 1] = v;
+  }
   }
 }
 
@@ -175,25 +175,32 @@ __global__ void k_copy_back(DevPtrs P, DomainConst K, const double* fsrc, const 
   }
 }
 
-// Map original -> sorted index, element -> mesh particle, and the FP32
-// prefilter coordinates (relative to BLPF, plus h).
-__global__ void k_after_permute(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= K.N) return;
-  size_t N = K.N;
-  int o = P.i[I_ORIG * N + p];
-  P.inv[o] = p;
-  if (P.i[I_KIND * N + p] == 1) P.elem_particle[P.i[I_ELEM * N + p]] = p;
-  for (int d = 0; d < 3; ++d) P.xs[d * N + p] = (float)(P.f[(C_X + d) * N + p] - K.BLPF[d]);
-  P.xs[3 * N + p] = (float)P.f[C_H * N + p];
-}
-
 __device__ __forceinline__ bool is_contact_id(const DomainConst& K, int id) {
   for (int m = 0; m < K.nmeshes; ++m)
     if (id == K.contact_surf_id[m]) return true;
   return false;
 }
+
+// Map original -> sorted index, element -> mesh particle, and the FP32
+// prefilter coordinates (relative to BLPF, plus h).
+__global__ void k_after_permute(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
+  size_t N = K.N;
+  int o = P.i[I_ORIG * N + p];
+  P.inv[o] = p;
+  int kind = P.i[I_KIND * N + p];
+  if (kind == 1) P.elem_particle[P.i[I_ELEM * N + p]] = p;
+  reinterpret_cast<float4*>(P.xs)[p] =
+      make_float4((float)(P.f[(C_X + 0) * N + p] - K.BLPF[0]), (float)(P.f[(C_X + 1) * N + p] - K.BLPF[1]),
+                  (float)(P.f[(C_X + 2) * N + p] - K.BLPF[2]), (float)P.f[C_H * N + p]);
+  // class word for the pair rules: bit 0 rigid-mesh particle, bit 1 carries a
+  // contact-surface id, bits 2.. material index (the cell-key scratch column is
+  // free once the particles are scattered)
+  P.i[I_CELL * N + p] = kind | (is_contact_id(K, P.i[I_ID * N + p]) ? 2 : 0) | (P.i[I_MATERIAL * N + p] << 2);
+  }
+}
+
 
 // CheckRadius (Neighbour.cpp:361-372) exactly: rij / ((hi + hj) / 2) <= Cellfac
 // with rij = sqrt(dx*dx + dy*dy + dz*dz) summed left to right, no contraction.
@@ -209,10 +216,10 @@ __device__ __forceinline__ bool radius_exact(const DevPtrs& P, size_t N, int i, 
 
 // Radius test: FP32 prefilter, exact FP64 decision inside the margin.
 __device__ __forceinline__ bool radius_ok(const DevPtrs& P, const DomainConst& K, size_t N, int i, int j, float xi,
-                                          float yi, float zi, float hi) {
-  float dx = xi - P.xs[j], dy = yi - P.xs[N + j], dz = zi - P.xs[2 * N + j];
+                                          float yi, float zi, float hi, float4 pj) {
+  float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
   float d2 = dx * dx + dy * dy + dz * dz;
-  float R = (float)K.Cellfac * 0.5f * (hi + P.xs[3 * N + j]);
+  float R = (float)K.Cellfac * 0.5f * (hi + pj.w);
   float R2 = R * R;
   if (d2 < R2 * (1.0f - K.pre_eps)) return true;
   if (d2 > R2 * (1.0f + K.pre_eps)) return false;
@@ -234,9 +241,11 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   __shared__ int s_idx[FILL_WARPS][FILL_SLOTS];
   __shared__ int s_len[FILL_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i0 = blockIdx.x * FILL_WARPS;
-  const int i = i0 + w;
   size_t N = K.N;
+  const int ngroups = (K.N + FILL_WARPS - 1) / FILL_WARPS;
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+  const int i0 = grp * FILL_WARPS;
+  const int i = i0 + w;
   const int* ID = P.i + I_ID * N;
   const int* orig = P.i + I_ORIG * N;
   const int* kind = P.i + I_KIND * N;
@@ -244,7 +253,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   int cnt = 0, split = 0;
   bool overflow = false;
   if (i < K.N && kind[i] == 0) {
-    float xi = P.xs[i], yi = P.xs[N + i], zi = P.xs[2 * N + i], hi = P.xs[3 * N + i];
+    float4 pi = reinterpret_cast<const float4*>(P.xs)[i];
     int c[3];
     for (int d = 0; d < 3; ++d) {
       int q = (int)floor(__ddiv_rn(__dsub_rn(P.f[(C_X + d) * N + i], K.BLPF[d]), K.CellSize[d]));
@@ -252,33 +261,53 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     }
     int idi = ID[i], oi = orig[i], mi = material[i];
     bool ci = K.contact && is_contact_id(K, idi);
-    for (int a = c[0] - 1; a <= c[0] + 1; ++a) {
-      if (a < 0 || a >= K.CellNo[0]) continue;
-      for (int b = c[1] - 1; b <= c[1] + 1; ++b) {
-        if (b < 0 || b >= K.CellNo[1]) continue;
-        for (int e = c[2] - 1; e <= c[2] + 1; ++e) {
-          if (e < 0 || e >= K.CellNo[2]) continue;
-          int key = P.cell_rank[(a * K.CellNo[1] + b) * K.CellNo[2] + e];
-          int s0 = P.cell_start[key], s1 = P.cell_start[key + 1];
-          for (int base = s0; base < s1; base += 32) {
-            int j = base + lane;
-            bool ok = false;
-            unsigned kk = 0;
-            if (j < s1 && j != i) {
-              int idj = ID[j];
-              ok = !(K.contact && (ci || is_contact_id(K, idj))) && kind[j] == 0 && material[j] == mi &&
-                   radius_ok(P, K, N, i, j, xi, yi, zi, hi);
-              if (ok) kk = (unsigned)(orig[j] - oi - 1);
-            }
-            unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) {
-              int pos = cnt + __popc(m & ((1u << lane) - 1u));
-              if (pos < FILL_SLOTS) { s_key[w][pos] = kk; s_idx[w][pos] = j; }
-            }
-            cnt += __popc(m);
-          }
+    const int* cls = P.i + I_CELL * N;
+    // Lane c < 27 fetches the range of neighbour cell c; a warp scan of the
+    // counts flattens the candidates so all lanes work on every iteration.
+    int cs = 0, cc = 0;
+    if (lane < 27) {
+      int a = c[0] + lane / 9 - 1, b = c[1] + (lane / 3) % 3 - 1, e = c[2] + lane % 3 - 1;
+      if (a >= 0 && a < K.CellNo[0] && b >= 0 && b < K.CellNo[1] && e >= 0 && e < K.CellNo[2]) {
+        int key = P.cell_rank[(a * K.CellNo[1] + b) * K.CellNo[2] + e];
+        cs = P.cell_start[key];
+        cc = P.cell_start[key + 1] - cs;
+      }
+    }
+    int incl = cc;
+    for (int off = 1; off < 32; off <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += v;
+    }
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    int excl = incl - cc;
+    for (int base = 0; base < total; base += 32) {
+      int t = base + lane;
+      // cell of flat candidate t: the last lane whose exclusive prefix <= t
+      int cell = 0;
+      for (int q = 0; q < 27; ++q) {
+        int ex = __shfl_sync(0xffffffffu, excl, q);
+        if (ex <= t) cell = q;
+      }
+      int cstart = __shfl_sync(0xffffffffu, cs, cell);
+      int cexcl = __shfl_sync(0xffffffffu, excl, cell);
+      bool ok = false;
+      unsigned kk = 0;
+      int j = -1;
+      if (t < total) {
+        j = cstart + (t - cexcl);
+        if (j != i) {
+          int cj = cls[j];
+          ok = !(K.contact && (ci || (cj & 2))) && (cj & 1) == 0 && (cj >> 2) == mi &&
+               radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, reinterpret_cast<const float4*>(P.xs)[j]);
+          if (ok) kk = (unsigned)(orig[j] - oi - 1);
         }
       }
+      unsigned m = __ballot_sync(0xffffffffu, ok);
+      if (ok) {
+        int pos = cnt + __popc(m & ((1u << lane) - 1u));
+        if (pos < FILL_SLOTS) { s_key[w][pos] = kk; s_idx[w][pos] = j; }
+      }
+      cnt += __popc(m);
     }
     if (cnt > MAX_NB) overflow = true;
     if (cnt > FILL_SLOTS) cnt = FILL_SLOTS;
@@ -329,16 +358,17 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     int k = q / FILL_WARPS, t = q - k * FILL_WARPS;
     if (k < s_len[t]) P.nbr[(size_t)k * N + i0 + t] = s_idx[t][k];
   }
+  __syncthreads();  // the shared buffers are reused by the next group
+  }
 }
 
 // CalculateSurface (Domain.cpp:1415-1491): n_i = sum_j m_j (x_i - x_j) in row
 // order; |n| / totmass >= 0.25 h and Nb <= 46 marks the free surface (ID 1).
 __global__ void k_surface(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
   size_t N = K.N;
-  if (P.i[I_KIND * N + i] != 0) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
+  if (P.i[I_KIND * N + i] != 0) continue;
   double xi = P.f[C_X * N + i], yi = P.f[(C_X + 1) * N + i], zi = P.f[(C_X + 2) * N + i];
   double n0 = 0, n1 = 0, n2 = 0;
   int len = P.row_len[i];
@@ -360,6 +390,7 @@ __global__ void k_surface(DevPtrs P, DomainConst K) {
     atomicAdd(&P.st->surface_count, 1);
   }
   P.i[I_ID * N + i] = id;
+  }
 }
 
 // ContactNbSearch (Contact.cpp:57-132): surface particle (at search time and
@@ -367,9 +398,8 @@ __global__ void k_surface(DevPtrs P, DomainConst K) {
 // Row sorted by the mesh particle's original index.
 __global__ void k_contact_pairs(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
   size_t N = K.N;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
   int cnt = 0;
   bool overflow = false;
   int row[MAX_CP];
@@ -414,6 +444,7 @@ __global__ void k_contact_pairs(DevPtrs P, DomainConst K) {
   P.cp_len[i] = cnt;
   if (overflow) atomicOr(&P.st->errors, ERR_CONTACT_OVERFLOW);
   if (cnt) atomicAdd(&P.st->contact_pair_count, (unsigned long long)cnt);
+  }
 }
 
 __global__ void k_force_search(DevPtrs P) { P.st->do_search = 1; }
@@ -433,12 +464,16 @@ static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch,
                              cudaStream_t s) {
   const int T = 256;
-  int nz = nblk(K.ncells, T) > 4096 ? 4096 : nblk(K.ncells, T);
+  // Gated kernels run on fixed grids with grid-stride loops: on steps that do
+  // not search, each launch is a handful of blocks that exit at once.
+  const int G = 152 * 4;
+  auto grid = [&](long long n) { int b = nblk(n, T); return b < G ? b : G; };
+  int nz = grid(K.ncells);
   k_search_begin<<<1, 1, 0, s>>>(P);
   mark(s, "k_search_begin");
   k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, K.ncells, 1);
   mark(s, "k_zero_int");
-  k_cell_keys<<<nblk(K.N, T), T, 0, s>>>(P, K);
+  k_cell_keys<<<grid(K.N), T, 0, s>>>(P, K);
   mark(s, "k_cell_keys");
   int nb = nblk(K.ncells, SCAN_TILE);
   k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(P, P.cell_count, K.ncells, P.scan_tmp);
@@ -449,22 +484,22 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   mark(s, "k_scan_down");
   k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, K.ncells, 1);
   mark(s, "k_zero_int");
-  k_scatter<<<nblk(K.N, T), T, 0, s>>>(P, K);
+  k_scatter<<<grid(K.N), T, 0, s>>>(P, K);
   mark(s, "k_scatter");
-  k_sort_cells<<<nblk(K.ncells, T), T, 0, s>>>(P, K);
+  k_sort_cells<<<grid(K.ncells), T, 0, s>>>(P, K);
   mark(s, "k_sort_cells");
-  k_permute<<<152 * 8, 512, 0, s>>>(P, K, fscratch, iscratch);
+  k_permute<<<152 * 4, 512, 0, s>>>(P, K, fscratch, iscratch);
   mark(s, "k_permute");
-  k_copy_back<<<152 * 8, 512, 0, s>>>(P, K, fscratch, iscratch);
+  k_copy_back<<<152 * 4, 512, 0, s>>>(P, K, fscratch, iscratch);
   mark(s, "k_copy_back");
-  k_after_permute<<<nblk(K.N, T), T, 0, s>>>(P, K);
+  k_after_permute<<<grid(K.N), T, 0, s>>>(P, K);
   mark(s, "k_after_permute");
-  k_nbr_fill<<<nblk(K.N, FILL_WARPS), FILL_WARPS * 32, 0, s>>>(P, K);
+  k_nbr_fill<<<nblk(K.N, FILL_WARPS) < 152 ? nblk(K.N, FILL_WARPS) : 152, FILL_WARPS * 32, 0, s>>>(P, K);
   mark(s, "k_nbr_fill");
   if (K.contact) {
-    k_surface<<<nblk(K.N, T), T, 0, s>>>(P, K);
+    k_surface<<<grid(K.N), T, 0, s>>>(P, K);
     mark(s, "k_surface");
-    k_contact_pairs<<<nblk(K.N, 128), 128, 0, s>>>(P, K);
+    k_contact_pairs<<<grid(K.N), 128, 0, s>>>(P, K);
     mark(s, "k_contact_pairs");
   }
 }

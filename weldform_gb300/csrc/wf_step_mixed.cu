@@ -61,9 +61,8 @@ __device__ __forceinline__ float grad_kernel_f(float r2, float hh, float* r_out)
 // ---------------------------------------------------------------- records
 __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
   if (!force && !P.st->do_search) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
   size_t N = K.N;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
   bool solid = icol(P, I_KIND, N, i) == 0;
   double rho = col(P, C_RHO, N, i);
   double c2 = solid ? 1.0 / (rho * rho) : 0.0;
@@ -84,10 +83,11 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
                          (float)(c2 * col(P, C_P, N, i)), (float)col(P, C_CS, N, i));
   r[(size_t)RC_MISC * N] = make_float4((float)col(P, C_ALPHA, N, i), (float)col(P, C_BETA, N, i), (float)col(P, C_KT, N, i), th);
   r[(size_t)RC_T2 * N] = make_float4(tl, 0.f, 0.f, 0.f);
+  }
 }
 
 // ---------------------------------------------------------------- accel
-__global__ void __launch_bounds__(BLOCK) k_accel_mx(DevPtrs P, DomainConst K) {
+__global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
   size_t N = K.N;
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(BLOCK) k_accel_mx(DevPtrs P, DomainConst K) {
 }
 
 // ---------------------------------------------------------------- density + drift + kick
-__global__ void __launch_bounds__(BLOCK) k_density_drift_mx(DevPtrs P, DomainConst K) {
+__global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
   size_t N = K.N;
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift_mx(DevPtrs P, DomainCon
 // ---------------------------------------------------------------- rates + energy + conduction
 // Gather at x(n+1), v(n+1): strain/rotation rate sums (InteractionAlt.cpp:263-479),
 // the kinetic-energy pair sum (Domain.cpp:1752-1808) and conduction (Thermal.cpp:53-219).
-__global__ void __launch_bounds__(BLOCK) k_rate_mx(DevPtrs P, DomainConst K) {
+__global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
   size_t N = K.N;
@@ -405,23 +405,26 @@ __global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K) {
 }
 
 void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, cudaStream_t s) {
-  k_refresh_records<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, force);
+  int b = nblk(K.N, BLOCK);
+  k_refresh_records<<<b < 152 * 4 ? b : 152 * 4, BLOCK, 0, s>>>(P, K, force);
   mark(s, "k_refresh_records");
 }
 
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
   int nb = nblk(K.N, BLOCK);
+  int gb = (K.gblock == 64 || K.gblock == 128 || K.gblock == 512) ? K.gblock : 256;
+  int ng = nblk(K.N, gb);
   launch_step_head(P, K, fscratch, iscratch, s);
   launch_refresh_shadows(P, K, 0, s);
-  k_accel_mx<<<nb, BLOCK, 0, s>>>(P, K);
+  k_accel_mx<<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
-  k_density_drift_mx<<<nb, BLOCK, 0, s>>>(P, K);
+  k_density_drift_mx<<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  k_rate_mx<<<nb, BLOCK, 0, s>>>(P, K);
+  k_rate_mx<<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_rate_mx");
   k_stress_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_stress_mx");

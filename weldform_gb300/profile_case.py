@@ -19,6 +19,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--precision", type=int, default=0)
     ap.add_argument("--v-top", type=float, default=-1.0)
+    ap.add_argument("--kernels", action="store_true", help="print per-kernel CUDA-event times of the steps")
     a = ap.parse_args()
     dx = configs.dx_for_count(0.010, 0.030, a.n)
     d = Domain()
@@ -28,7 +29,13 @@ def main():
     t = time.perf_counter()
     d.step(a.steps)
     el = time.perf_counter() - t
-    print(f"n={case.n} dx={dx:.6e} steps={a.steps} s/step={el / max(a.steps, 1):.4e}")
+    print(f"n={case.n} dx={dx:.6e} steps={a.steps} s/step={el / max(a.steps, 1):.4e} "
+          f"searches={d.geti('nb_searches')} max_pl={d.get('max_pl_strain'):.3e}")
+    if a.kernels:
+        prof = d.profile_steps(a.steps)
+        tot = sum(v[0] for v in prof.values())
+        for k, (ms, n) in sorted(prof.items(), key=lambda kv: -kv[1][0]):
+            print(f"  {k:24s} {n:4d} launches {ms:9.3f} ms  {100 * ms / tot:5.1f} %")
     d.close()
 
 
