@@ -208,6 +208,37 @@ int wf_checkpoint_free(wf_domain* d, int slot);
  * power of two) for later domains in the process. */
 int wf_autotune(wf_domain* d, int steps, int* block);
 
+/* ---- reaction-force adjoint (no counterpart in the reference) ------------
+ * Gradient of the loss
+ *     L = (1/S) sum_s (F(s) - target[s])^2,
+ * F(s) = component `axis` of the contact force on rigid mesh `mesh`
+ * (Domain::m_contact_force, Contact_Wang.cpp:312) after step (s+1)*every of a
+ * run of `steps` steps from the current state, S = ntarget,
+ * with respect to the parameters (grad[WF_NPARAM], in this order):
+ *   WF_P_E     Young's modulus, through G = E/(2(1+nu)) and
+ *              Cs = sqrt(E/(3(1-2nu)rho0)) of every particle (dt fixed)
+ *   WF_P_SY0   initial Sigmay of bilinear / Hollomon particles
+ *   WF_P_EP    Ep of every particle (bilinear hardening modulus)
+ *   WF_P_A .. WF_P_M   Johnson-Cook A, B, n, C, m of every material, including
+ *              their effect on the initial Sigmay = CalcYieldStress(0, 0, T0)
+ *              (WeldForm.cpp:905-906)
+ *   WF_P_MU    friction_sta = friction_dyn
+ *   WF_P_PFAC  contact stiffness factor (contact_alg 1 and 2)
+ * The plain FP64 step (precision 0) is differentiated in reverse mode with the
+ * neighbour and contact lists of each step frozen.  The forward run stores a
+ * device checkpoint every `checkpoint_every` steps; the reverse sweep
+ * recomputes one segment at a time, taping its steps, and runs the adjoint
+ * kernels backwards over it.  On return the domain holds the state after
+ * `steps` steps, as if wf_step had run them.  curve (optional, ntarget values)
+ * receives F(s); fwd_ms / adj_ms (optional) the wall time of the forward run
+ * and of the reverse sweep.  Errors: WF_ERR_UNSUPPORTED for the mixed form or
+ * particles with Ep < 0. */
+#define WF_NPARAM 10
+enum { WF_P_E = 0, WF_P_SY0, WF_P_EP, WF_P_A, WF_P_B, WF_P_N, WF_P_C, WF_P_M, WF_P_MU, WF_P_PFAC };
+int wf_adjoint_reaction_loss(wf_domain* d, int64_t steps, int every, int mesh, int axis, const double* target,
+                             int64_t ntarget, int checkpoint_every, double* loss, double* grad, double* curve,
+                             double* fwd_ms, double* adj_ms);
+
 /* ---- measurement helpers (no counterpart in the reference) ---------------
  * wf_step_timed: nsteps steps bracketed by CUDA events recorded on the
  * domain's stream (synchronised before and after); elapsed_ms is the event

@@ -237,6 +237,7 @@ struct Domain {
   double int_energy_sum = 0, kin_energy_sum = 0, plastic_work = 0, contact_force_sum = 0, contact_reaction_sum = 0,
          ext_forces_work = 0, m_maxT = 0, m_minT = 0, max_pl = 0;
   int surface_count = 0;
+  double tangent_mismatch = 0;  // largest relative value difference seen by the tangent run
 
   void push_particle(int tag, const V3& xx, double m0, double dens, double hh, bool fixed) {
     // Particle.cpp:28-157 constructor defaults
@@ -1142,6 +1143,13 @@ struct Domain {
     return WF_OK;
   }
   int step() {  // SolverKickDrift.cpp:117-393
+    int rc = begin_step();
+    if (rc) return rc;
+    finish_step();
+    return WF_OK;
+  }
+  // StartAcceleration and the neighbour-search schedule (SolverKickDrift.cpp:117-186).
+  int begin_step() {
     int rc;
     // StartAcceleration (Domain.cpp:1519-1597) for free particles with TI = 0
     for (int i = 0; i < N; i++) { a[i] = v3(0, 0, 0); dDensity[i] = 0.; srate[i] = zero3(); rrate[i] = zero3(); }
@@ -1164,6 +1172,10 @@ struct Domain {
         if ((rc = neighbour_search())) return rc;
         if (contact && (rc = contact_nb_update())) return rc;
       }
+    return WF_OK;
+  }
+  // The rest of the step (force passes, kicks, drift, stress, thermal, bookkeeping).
+  void finish_step() {
     pass_accel();
     general_after();
     if (contact) contact_wang();
@@ -1193,14 +1205,15 @@ struct Domain {
       if (contact_mesh_auto_update) for (auto& M : meshes) M.update(deltat);
       update_contact_particles();
     }
-    if (mx > MIN_PS_FOR_NBSEARCH) {
+    if (max_pl > MIN_PS_FOR_NBSEARCH) {  // max pl_strain at the start of the step
       if (ts_i == (ts_nb_inc - 1)) nb_cleared = true;  // ClearNbData
       ts_i++;
       if (ts_i > (ts_nb_inc - 1)) ts_i = 0;
     }
-    return WF_OK;
   }
 };
+
+#include "wf_tangent.inc"
 
 // ---------------------------------------------------------------- field maps
 double* f64_scalar(Domain* d, const std::string& f) {
@@ -1327,6 +1340,7 @@ int wfo_get_domain_f64(wfo_domain* p, const char* name, double* v) {
   else if (n == "max_pl_strain") *v = d->max_pl;
   else if (n == "m_maxT") *v = d->m_maxT;
   else if (n == "m_minT") *v = d->m_minT;
+  else if (n == "tangent_mismatch") *v = d->tangent_mismatch;
   else return set_err(WF_ERR_ARG, "unknown domain f64 read " + n);
   return WF_OK;
 }
@@ -1526,6 +1540,51 @@ int wfo_checkpoint_free(wfo_domain*, int slot) {
   return WF_OK;
 }
 int wfo_autotune(wfo_domain*, int, int* block) { if (block) *block = 0; return WF_OK; }
+// The gradient of the reaction-force loss by the FP64 tangent-linear run
+// (forward mode, one dual direction per parameter) in canonical mode: the
+// reference against which the GPU's reverse-mode adjoint is checked.  Same
+// arguments and loss as the library's entry point; checkpoint_every has no
+// effect (forward mode needs no recompute); adj_ms is 0.
+int wfo_adjoint_reaction_loss(wfo_domain* p, int64_t steps, int every, int mesh, int axis, const double* target,
+                              int64_t ntarget, int checkpoint_every, double* loss, double* grad, double* curve,
+                              double* fwd_ms, double* adj_ms) {
+  Domain* d = D(p);
+  (void)checkpoint_every;
+  if (!d->prepared) return set_err(WF_ERR_STATE, "adjoint before wf_prepare_kickdrift");
+  if (d->mode != 0) return set_err(WF_ERR_UNSUPPORTED, "the tangent run needs cpu_mode 0");
+  if (!d->contact || mesh < 0 || mesh >= (int)d->meshes.size())
+    return set_err(WF_ERR_ARG, "the reaction-force loss needs a rigid mesh");
+  if (axis < 0 || axis > 2 || every < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps || !target || !loss ||
+      !grad)
+    return set_err(WF_ERR_ARG, "adjoint: bad steps / sampling / target arguments");
+  for (int i = 0; i < d->N; ++i)
+    if (d->Ep[i] < 0.0) return set_err(WF_ERR_UNSUPPORTED, "adjoint: particles with Ep < 0 are not supported");
+  auto t0 = std::chrono::steady_clock::now();
+  Tangent T(*d);
+  T.init();
+  double L = 0.0;
+  for (int k = 0; k < NPAR; ++k) grad[k] = 0.0;
+  for (int64_t st = 0; st < steps; ++st) {
+    int rc = d->begin_step();
+    if (rc) return rc;
+    T.step();
+    d->finish_step();
+    if ((st + 1) % every == 0 && (st + 1) / every <= ntarget) {
+      int64_t s = (st + 1) / every - 1;
+      const Dd& F = T.mcf[mesh].c[axis];
+      double r = F.v - target[s];
+      L += r * r;
+      for (int k = 0; k < NPAR; ++k) grad[k] += 2.0 * r / (double)ntarget * F.d[k];
+      if (curve) curve[s] = F.v;
+    }
+    T.sync();
+  }
+  *loss = L / (double)ntarget;
+  d->tangent_mismatch = T.mismatch;
+  if (fwd_ms) *fwd_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (adj_ms) *adj_ms = 0.0;
+  return WF_OK;
+}
 int wfo_step_timed(wfo_domain* p, int64_t n, double* ms, int64_t* launches) {
   auto t0 = std::chrono::steady_clock::now();
   int rc = wfo_step(p, n);

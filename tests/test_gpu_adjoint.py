@@ -1,0 +1,145 @@
+"""Reverse-mode adjoint of the plain FP64 step (GPU) against the oracle's FP64
+tangent-linear run and against central finite differences on the GPU.
+
+Bars: every parameter the loss depends on agrees with the tangent-linear
+gradient to 1e-6 relative (the GPU and oracle trajectories differ by ~1e-12)
+and with central differences (relative step 1e-6) to 1e-4; the gradient does
+not depend on the checkpoint interval (bit-identical); the domain ends in
+the same state as after plain steps."""
+import os
+
+import numpy as np
+import pytest
+
+from tests._support import gpu_domain, oracle_domain
+from weldform_gb300 import BILINEAR, JOHNSON_COOK, PARAMS
+from weldform_gb300 import adjoint as adj
+
+pytestmark = pytest.mark.gpu
+THREADS = os.cpu_count() or 1
+
+JC = adj.ContactCase(R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, model=JOHNSON_COOK, thermal=True, stiffness="area")
+BL = adj.ContactCase(R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, model=BILINEAR, thermal=False, stiffness="wang")
+
+
+def _oracle():
+    d = oracle_domain()
+    d.set("cpu_threads", THREADS)
+    return d
+
+
+def _run(make, case, steps, every, target, k=10):
+    d = make()
+    mesh = adj.build(d, case, case.nominal())
+    d.prepare(case.dt)
+    r = d.adjoint_reaction_loss(steps, every, target, mesh=mesh, checkpoint_every=k)
+    r["x"] = d.get_array("x")
+    r["Sigma"] = d.get_array("Sigma")
+    d.close()
+    return r
+
+
+def _target(case, steps, every):
+    return adj.perturbed_jc_target(case, steps, every) * 0.9
+
+
+@pytest.mark.parametrize("case,must", [(JC, ("E", "A", "B", "n", "C", "PFAC")), (BL, ("E", "sy0", "Ep"))],
+                         ids=["jc_thermal_area", "bilinear_wang"])
+def test_adjoint_matches_tangent_linear(case, must):
+    steps, every = 60, 5
+    t = _target(case, steps, every)
+    g = _run(gpu_domain, case, steps, every, t)
+    o = _run(_oracle, case, steps, every, t)
+    assert abs(g["loss"] - o["loss"]) <= 1e-9 * abs(o["loss"])
+    s = case.scale()
+    gg, go = g["grad"] * s, o["grad"] * s
+    big = np.abs(go).max()
+    for p in must:
+        k = PARAMS.index(p)
+        assert abs(gg[k] - go[k]) <= 1e-6 * abs(go[k]), (p, gg[k], go[k])
+    for k, p in enumerate(PARAMS):
+        assert abs(gg[k] - go[k]) <= 1e-8 * big, (p, gg[k], go[k])
+
+
+def test_adjoint_matches_finite_differences():
+    steps, every = 60, 5
+    t = _target(JC, steps, every)
+    prob = adj.Problem(JC, steps, every, t)
+    loss, g = prob.loss_grad(np.zeros(len(PARAMS)))
+    fd = adj.central_fd(prob)
+    for p in ("E", "A", "B", "n", "C", "PFAC"):
+        k = PARAMS.index(p)
+        assert abs(g[k] - fd[k]) <= 1e-4 * abs(fd[k]), (p, g[k], fd[k])
+
+
+def test_checkpoint_interval_does_not_change_the_gradient():
+    steps, every = 60, 5
+    t = _target(JC, steps, every)
+    rs = [_run(gpu_domain, JC, steps, every, t, k) for k in (3, 7, 60)]
+    for r in rs[1:]:
+        assert r["loss"] == rs[0]["loss"]
+        assert np.array_equal(r["grad"], rs[0]["grad"])
+
+
+def test_adjoint_leaves_the_state_of_a_plain_run():
+    steps, every = 30, 5
+    t = _target(JC, steps, every)
+    r = _run(gpu_domain, JC, steps, every, t, 7)
+    d = gpu_domain()
+    adj.build(d, JC, JC.nominal())
+    d.prepare(JC.dt)
+    d.step(steps)
+    assert np.array_equal(r["x"], d.get_array("x"))
+    assert np.array_equal(r["Sigma"], d.get_array("Sigma"))
+    d.close()
+
+
+def test_gradcheck_through_autograd_function():
+    torch = pytest.importorskip("torch")
+    case = adj.ContactCase(R=0.0025, L=0.005, dx=0.0005, v_punch=-20.0)
+    steps, every = 30, 5
+    prob = adj.Problem(case, steps, every, _target(case, steps, every))
+    u = torch.zeros(len(PARAMS), dtype=torch.float64, requires_grad=True)
+    fn = adj.ReactionLoss
+    assert torch.autograd.gradcheck(lambda v: fn.apply(v, prob), (u,), eps=1e-6, atol=1e-7, rtol=1e-3)
+
+
+def test_mixed_precision_is_rejected():
+    from weldform_gb300 import PRECISION_MIXED
+    d = gpu_domain()
+    d.set("precision", PRECISION_MIXED)
+    mesh = adj.build(d, JC, JC.nominal())
+    d.prepare(JC.dt)
+    with pytest.raises(Exception):
+        d.adjoint_reaction_loss(10, 5, np.zeros(2), mesh=mesh)
+    d.close()
+
+
+@pytest.mark.slow
+def test_penalty_contact_workload_53k():
+    """The 53,352-particle penalty-contact workload (dx = 0.55 mm), 400 steps,
+    loss over 40 samples: adjoint against the FP64 tangent-linear run and
+    against central differences, for checkpoint intervals 10, 20 and 50."""
+    case = adj.ContactCase()
+    steps, every = 400, 10
+    t = adj.perturbed_jc_target(case, steps, every)
+    o = _run(_oracle, case, steps, every, t)
+    s = case.scale()
+    go = o["grad"] * s
+    big = np.abs(go).max()
+    for k in (10, 20, 50):
+        g = _run(gpu_domain, case, steps, every, t, k)
+        gg = g["grad"] * s
+        rel = np.abs(gg - go) / np.maximum(np.abs(go), 1e-300)
+        print(f"k={k} adjoint vs tangent-linear, relative per parameter:", dict(zip(PARAMS, rel.round(12))))
+        for p in ("E", "A", "B", "n", "C", "PFAC"):
+            q = PARAMS.index(p)
+            assert rel[q] <= 1e-6, (p, gg[q], go[q])
+        assert np.all(np.abs(gg - go) <= 1e-8 * big)
+    prob = adj.Problem(case, steps, every, t)
+    fd = adj.central_fd(prob)
+    ga = go * prob.norm
+    print("tangent-linear vs central differences:", dict(zip(PARAMS, (np.abs(ga - fd) / np.abs(fd)).round(8))))
+    for p in ("E", "A", "B", "n", "C", "PFAC"):
+        q = PARAMS.index(p)
+        assert abs(ga[q] - fd[q]) <= 1e-3 * abs(fd[q]), (p, ga[q], fd[q])

@@ -24,7 +24,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 __all__ = ["Domain", "WFError", "load_library", "LIB_PATH", "PRECISION_FP64", "PRECISION_MIXED",
-           "BILINEAR", "HOLLOMON", "JOHNSON_COOK", "CONTACT_WANG", "CONTACT_PENALTY", "CONTACT_AREA"]
+           "BILINEAR", "HOLLOMON", "JOHNSON_COOK", "CONTACT_WANG", "CONTACT_PENALTY", "CONTACT_AREA", "PARAMS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libweldform_gb300.so")
@@ -33,6 +33,8 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 BILINEAR, HOLLOMON, JOHNSON_COOK = 0, 1, 2
 CONTACT_WANG, CONTACT_PENALTY, CONTACT_AREA = 0, 1, 2
+# Parameters of the reaction-force adjoint, in the order of its gradient.
+PARAMS = ("E", "sy0", "Ep", "A", "B", "n", "C", "m", "mu", "PFAC")
 
 _ERRNAMES = {1: "WF_ERR_ARG", 2: "WF_ERR_CUDA", 3: "WF_ERR_NAN", 4: "WF_ERR_NBR_OVERFLOW", 5: "WF_ERR_TIMEOUT",
              6: "WF_ERR_STATE", 7: "WF_ERR_NOMEM", 8: "WF_ERR_UNSUPPORTED"}
@@ -95,6 +97,7 @@ _SIGS = {
     "checkpoint_free": [_P, _I],
     "autotune": [_P, _I, ctypes.POINTER(_I)],
     "profile_steps": [_P, _I64, ctypes.c_char_p, _I, _DP, _I64P, _I, ctypes.POINTER(_I)],
+    "adjoint_reaction_loss": [_P, _I64, _I, _I, _I, _DP, _I64, _I, _DP, _DP, _DP, _DP, _DP],
 }
 EXPORTS = ["version", "last_error"] + list(_SIGS)
 
@@ -311,6 +314,24 @@ class Domain:
             nm = names.raw[k * L:(k + 1) * L].split(b"\0", 1)[0].decode()
             out[nm] = (tot[k], int(cnt[k]))
         return out
+
+    def adjoint_reaction_loss(self, steps: int, every: int, target, mesh: int = 0, axis: int = 2,
+                              checkpoint_every: int = 20):
+        """Loss (1/S) sum_s (F_s - target_s)^2 of the mesh's reaction force
+        sampled every `every` steps, and its gradient with respect to PARAMS by
+        the reverse-mode adjoint (plain FP64 form, checkpoint every
+        `checkpoint_every` steps).  Returns a dict with loss, grad (PARAMS
+        order), curve (the sampled F_s), fwd_ms and adj_ms; the domain ends
+        `steps` steps later."""
+        t = np.ascontiguousarray(target, dtype=np.float64).ravel()
+        loss = ctypes.c_double()
+        grad = np.zeros(len(PARAMS))
+        curve = np.zeros(t.size)
+        fms, ams = ctypes.c_double(), ctypes.c_double()
+        self._call("adjoint_reaction_loss", self._h, int(steps), int(every), int(mesh), int(axis),
+                   t.ctypes.data_as(_DP), t.size, int(checkpoint_every), ctypes.byref(loss),
+                   grad.ctypes.data_as(_DP), curve.ctypes.data_as(_DP), ctypes.byref(fms), ctypes.byref(ams))
+        return {"loss": loss.value, "grad": grad, "curve": curve, "fwd_ms": fms.value, "adj_ms": ams.value}
 
     # ------------------------------------------------------------ arrays
     def get_array(self, field: str) -> np.ndarray:

@@ -193,6 +193,21 @@ struct DevPtrs {
   int nnodes, nelem;
   double* partials;       // NSLOTS * nblocks
   long long* scan_tmp;
+  double* tx;             // step tape of the adjoint's recompute (TapeCol columns), null otherwise
+};
+
+// Per-step values the plain form writes for the adjoint when DevPtrs::tx is
+// set: the inputs of the contact and density passes and the branch record of
+// the radial return, so the reverse pass takes exactly the forward branches.
+enum TapeCol : int {
+  TX_APRE = 0,             // acceleration entering the contact pass (after the first BC pass) (3)
+  TX_VH = 3,               // half-step velocity entering the density pass (3)
+  TX_SR = 6,               // StrainRate before the thermal-expansion term (6)
+  TX_RR = 12,              // RotationRate (xy xz yz)
+  TX_SC = 15,              // radial-return scale min(Sigmay / sig_trial, 1)
+  TX_SYN = 16,             // flow stress recomputed in the step (JC / Hollomon; Sigmay otherwise)
+  TX_DEP = 17,             // plastic strain increment (0 when elastic)
+  NTX = 18
 };
 
 }  // namespace wf

@@ -7,6 +7,7 @@
 // (CellInitiate, Neighbour.cpp:10-139) and from then on all state lives in
 // HBM in cell-sorted order; host transfers map through the original index.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -18,6 +19,7 @@
 #include <vector>
 
 #include "../../include/weldform_gb300.h"
+#include "wf_adjoint.cuh"
 #include "wf_device.cuh"
 #include "wf_launch.h"
 
@@ -699,10 +701,7 @@ struct wf_domain {
     check_errors();
     return rows;
   }
-  void checkpoint_save(int slot) {
-    use_device();
-    if ((int)slots.size() <= slot) slots.resize(slot + 1);
-    auto& sl = slots[slot];
+  void save_to(std::vector<void*>& sl) {
     if (sl.empty())
       for (auto& r : regions) {
         void* p = nullptr;
@@ -718,18 +717,239 @@ struct wf_domain {
       CK(cudaMemcpyAsync(sl[k], regions[k].p, regions[k].bytes, cudaMemcpyDeviceToDevice, stream));
     CK(cudaStreamSynchronize(stream));
   }
-  void checkpoint_restore(int slot) {
-    use_device();
-    if ((int)slots.size() <= slot || slots[slot].empty()) throw CudaError{WF_ERR_STATE, "checkpoint slot is empty"};
-    auto& sl = slots[slot];
+  void restore_from(const std::vector<void*>& sl) {
     for (size_t k = 0; k < regions.size(); ++k)
       CK(cudaMemcpyAsync(regions[k].p, sl[k], regions[k].bytes, cudaMemcpyDeviceToDevice, stream));
     CK(cudaStreamSynchronize(stream));
+  }
+  void checkpoint_save(int slot) {
+    use_device();
+    if ((int)slots.size() <= slot) slots.resize(slot + 1);
+    save_to(slots[slot]);
+  }
+  void checkpoint_restore(int slot) {
+    use_device();
+    if ((int)slots.size() <= slot || slots[slot].empty()) throw CudaError{WF_ERR_STATE, "checkpoint slot is empty"};
+    restore_from(slots[slot]);
   }
   void checkpoint_free(int slot) {
     if ((int)slots.size() <= slot) return;
     for (void* p : slots[slot]) cudaFree(p);
     slots[slot].clear();
+  }
+  // ------------------------------------------------------------ adjoint
+  // Device buffers owned by one adjoint call (freed when it returns).
+  struct Scratch {
+    std::vector<void*> ps;
+    ~Scratch() { for (void* p : ps) cudaFree(p); }
+    template <class T> T* get(size_t n) {
+      void* p = nullptr;
+      cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+      if (e != cudaSuccess) throw CudaError{WF_ERR_NOMEM, std::string("adjoint tape: ") + cudaGetErrorString(e)};
+      ps.push_back(p);
+      return (T*)p;
+    }
+  };
+  // Fixed-size buffers reused across the segments of one adjoint call.
+  template <class T> struct Pool {
+    Scratch* sc = nullptr;
+    size_t n = 0, used = 0;
+    std::vector<T*> bufs;
+    T* get() {
+      if (used == bufs.size()) bufs.push_back(sc->get<T>(n));
+      return bufs[used++];
+    }
+  };
+  struct TapeStep {
+    double *start = nullptr, *end = nullptr, *tx = nullptr, *mesh = nullptr;
+    int* topo = nullptr;
+    bool searched = false;
+    double time = 0.0;
+  };
+  // Topology record layout (ints of N): perm, int arena, row_len, row_split,
+  // neighbour rows (MAX_NB), contact count, contact rows (MAX_CP).
+  size_t topo_ints() const {
+    return (size_t)(3 + wf::NI32_PERSIST + wf::MAX_NB + 1 + (contact ? wf::MAX_CP : 0)) * hp.N;
+  }
+
+  // Gradient of a reaction-force loss by the reverse-mode adjoint of the plain
+  // FP64 step with checkpoint-and-recompute (see include/weldform_gb300.h).
+  void adjoint_reaction(long long steps, int every, int mesh, int axis, const double* target, long long ntarget,
+                        int kchk, double* loss, double* grad, double* curve, double* fwd_ms, double* adj_ms) {
+    using namespace wf;
+    if (!prepared) throw CudaError{WF_ERR_STATE, "adjoint before wf_prepare_kickdrift"};
+    if (precision != WF_PRECISION_FP64)
+      throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint runs on the plain FP64 form (precision 0)"};
+    if (!contact || mesh < 0 || mesh >= (int)meshes.size())
+      throw CudaError{WF_ERR_ARG, "the reaction-force loss needs a rigid mesh"};
+    if (axis < 0 || axis > 2 || every < 1 || kchk < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps ||
+        !target || !loss || !grad)
+      throw CudaError{WF_ERR_ARG, "adjoint: bad steps / sampling / target arguments"};
+    size_t n = hp.N;
+    {
+      std::vector<double> ep(n);
+      get_f64(C_EP, 1, ep.data());
+      for (double e : ep)
+        if (e < 0.0) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: particles with Ep < 0 are not supported"};
+    }
+    use_device();
+    if (use_graph && (!graph || graph_precision != precision || graph_block != gblock)) step(0);
+    Scratch sc;
+    double* f0 = sc.get<double>((size_t)NF64_PERSIST * n);
+    int* i0 = sc.get<int>((size_t)NI32_PERSIST * n);
+    CK(cudaMemcpyAsync(f0, d_f, sizeof(double) * NF64_PERSIST * n, cudaMemcpyDeviceToDevice, stream));
+    CK(cudaMemcpyAsync(i0, d_i, sizeof(int) * NI32_PERSIST * n, cudaMemcpyDeviceToDevice, stream));
+    double* dF = sc.get<double>(steps);
+    long long nseg = (steps + kchk - 1) / kchk;
+    std::vector<std::vector<void*>> chk((size_t)nseg + 1);
+    struct FreeChk {
+      std::vector<std::vector<void*>>& c;
+      ~FreeChk() { for (auto& v : c) for (void* p : v) cudaFree(p); }
+    } free_chk{chk};
+    DomainConst k = K;
+    k.mixed = 0;
+    k.gblock = gblock;
+
+    // ---- forward pass: loss curve and a checkpoint every kchk steps
+    auto t0 = std::chrono::steady_clock::now();
+    for (long long c = 0; c < nseg; ++c) {
+      save_to(chk[c]);
+      long long s1 = std::min(steps, (c + 1) * kchk);
+      for (long long st = c * kchk; st < s1; ++st) {
+        if (use_graph) CK(cudaGraphLaunch(graph, stream));
+        else launch_one_step();
+        launch_record_force(P, mesh, axis, dF, st, stream);
+      }
+    }
+    save_to(chk[nseg]);
+    check_errors();
+    auto t1 = std::chrono::steady_clock::now();
+    std::vector<double> F(steps);
+    CK(cudaMemcpyAsync(F.data(), dF, sizeof(double) * steps, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    double L = 0.0;
+    std::vector<double> seed(steps, 0.0);
+    for (long long s = 0; s < ntarget; ++s) {
+      long long st = (s + 1) * every - 1;
+      double r = F[st] - target[s];
+      L += r * r;
+      seed[st] = 2.0 * r / (double)ntarget;
+      if (curve) curve[s] = F[st];
+    }
+    *loss = L / (double)ntarget;
+
+    // ---- reverse sweep, one recomputed segment at a time
+    double* Lin = sc.get<double>((size_t)NA_STATE * n);
+    double* Lout = sc.get<double>((size_t)NA_STATE * n);
+    double* Tb = sc.get<double>((size_t)NA_TMP * n);
+    double* Q = sc.get<double>((size_t)NQ * n);
+    double* Q2 = sc.get<double>((size_t)NQ * n);
+    int* derr = sc.get<int>(1);
+    CK(cudaMemsetAsync(Lin, 0, sizeof(double) * NA_STATE * n, stream));
+    CK(cudaMemsetAsync(Q, 0, sizeof(double) * NQ * n, stream));
+    CK(cudaMemsetAsync(derr, 0, sizeof(int), stream));
+    Pool<double> snaps{&sc, (size_t)NF64_PERSIST * n}, txs{&sc, (size_t)NTX * n},
+        meshp{&sc, (size_t)3 * P.nnodes + P.nelem};
+    Pool<int> topos{&sc, topo_ints()};
+    std::vector<TapeStep> tape((size_t)std::min<long long>(kchk, steps));
+    int nn = P.nnodes, ne = P.nelem;
+    auto topo_view = [&](int* t, DevPtrs& S) {
+      S.perm = t;
+      S.i = t + n;
+      S.row_len = S.i + (size_t)NI32_PERSIST * n;
+      S.row_split = S.row_len + n;
+      S.nbr = S.row_split + n;
+      S.cp_len = S.nbr + (size_t)MAX_NB * n;
+      S.cp = S.cp_len + n;
+    };
+    for (long long c = nseg - 1; c >= 0; --c) {
+      restore_from(chk[c]);
+      snaps.used = txs.used = meshp.used = topos.used = 0;
+      long long s0 = c * kchk, s1 = std::min(steps, (c + 1) * kchk);
+      double* prev_end = nullptr;
+      int* cur_topo = nullptr;
+      for (long long st = s0; st < s1; ++st) {
+        TapeStep& T = tape[st - s0];
+        launch_step_head(P, k, d_fscratch, d_iscratch, stream);
+        StepState ss = read_state();
+        T.searched = ss.do_search != 0;
+        T.time = ss.Time;
+        if (T.searched || st == s0) {
+          T.topo = topos.get();
+          DevPtrs V{};
+          topo_view(T.topo, V);
+          CK(cudaMemcpyAsync(V.perm, P.perm, sizeof(int) * n, cudaMemcpyDeviceToDevice, stream));
+          CK(cudaMemcpyAsync(V.i, d_i, sizeof(int) * NI32_PERSIST * n, cudaMemcpyDeviceToDevice, stream));
+          CK(cudaMemcpyAsync(V.row_len, P.row_len, sizeof(int) * n, cudaMemcpyDeviceToDevice, stream));
+          CK(cudaMemcpyAsync(V.row_split, P.row_split, sizeof(int) * n, cudaMemcpyDeviceToDevice, stream));
+          CK(cudaMemcpyAsync(V.nbr, P.nbr, sizeof(int) * MAX_NB * n, cudaMemcpyDeviceToDevice, stream));
+          CK(cudaMemcpyAsync(V.cp_len, P.cp_len, sizeof(int) * n, cudaMemcpyDeviceToDevice, stream));
+          if (contact) CK(cudaMemcpyAsync(V.cp, P.cp, sizeof(int) * MAX_CP * n, cudaMemcpyDeviceToDevice, stream));
+          cur_topo = T.topo;
+          T.start = snaps.get();
+          CK(cudaMemcpyAsync(T.start, d_f, sizeof(double) * NF64_PERSIST * n, cudaMemcpyDeviceToDevice, stream));
+        } else {
+          T.topo = cur_topo;
+          T.start = prev_end;
+        }
+        T.mesh = meshp.get();
+        if (nn) CK(cudaMemcpyAsync(T.mesh, P.node, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, stream));
+        if (ne) CK(cudaMemcpyAsync(T.mesh + 3 * nn, P.elem_pplane, sizeof(double) * ne, cudaMemcpyDeviceToDevice, stream));
+        T.tx = txs.get();
+        DevPtrs Pt = P;
+        Pt.tx = T.tx;
+        launch_step_fp64_body(Pt, k, stream);
+        T.end = snaps.get();
+        CK(cudaMemcpyAsync(T.end, d_f, sizeof(double) * NF64_PERSIST * n, cudaMemcpyDeviceToDevice, stream));
+        prev_end = T.end;
+      }
+      for (long long st = s1 - 1; st >= s0; --st) {
+        TapeStep& T = tape[st - s0];
+        AdjPtrs A;
+        A.S = P;
+        A.S.f = T.start;
+        A.S.tx = nullptr;
+        topo_view(T.topo, A.S);
+        A.S.node = T.mesh;
+        A.S.elem_pplane = T.mesh + 3 * nn;
+        A.fe = T.end;
+        A.tx = T.tx;
+        A.Lin = Lin;
+        A.Lout = Lout;
+        A.Tmp = Tb;
+        A.Q = Q;
+        A.err = derr;
+        A.time = T.time;
+        for (int d = 0; d < 3; ++d) A.seed[d] = 0.0;
+        A.seed_mesh = -1;
+        if (seed[st] != 0.0) { A.seed[axis] = seed[st]; A.seed_mesh = mesh; }
+        launch_adjoint_step(A, k, stream);
+        if (T.searched) {
+          launch_unpermute(A.S.perm, Lout, Lin, NA_STATE, (int)n, stream);
+          launch_unpermute(A.S.perm, Q, Q2, NQ, (int)n, stream);
+          std::swap(Q, Q2);
+        } else {
+          std::swap(Lin, Lout);
+        }
+      }
+    }
+    DevPtrs P0 = P;
+    P0.f = f0;
+    P0.i = i0;
+    double* dgrad = sc.get<double>(ADJ_NPARAM);
+    double* parts = sc.get<double>((size_t)ADJ_NPARAM * ((n + ADJ_BLOCK - 1) / ADJ_BLOCK));
+    launch_adjoint_finish(P0, K, Lin, Q, parts, dgrad, stream);
+    CK(cudaMemcpyAsync(grad, dgrad, sizeof(double) * ADJ_NPARAM, cudaMemcpyDeviceToHost, stream));
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaGetLastError());
+    auto t2 = std::chrono::steady_clock::now();
+    restore_from(chk[nseg]);
+    if (herr & ERR_ADJ_CONTACT)
+      throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: a particle had more than 8 inside contact pairs in one step"};
+    if (fwd_ms) *fwd_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    if (adj_ms) *adj_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
   }
   int autotune(int steps) {
     static std::mutex mu;
@@ -1307,6 +1527,16 @@ int wf_autotune(wf_domain* d, int steps, int* block) {
     if (!d->prepared) return set_err(WF_ERR_STATE, "autotune before the prologue");
     int b = d->autotune(steps);
     if (block) *block = b;
+    return WF_OK;
+  });
+}
+int wf_adjoint_reaction_loss(wf_domain* d, int64_t steps, int every, int mesh, int axis, const double* target,
+                             int64_t ntarget, int checkpoint_every, double* loss, double* grad, double* curve,
+                             double* fwd_ms, double* adj_ms) {
+  NEED(d);
+  return guard([&] {
+    d->adjoint_reaction(steps, every, mesh, axis, target, ntarget, checkpoint_every, loss, grad, curve, fwd_ms,
+                        adj_ms);
     return WF_OK;
   });
 }

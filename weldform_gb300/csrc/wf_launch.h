@@ -42,8 +42,11 @@ void launch_step_tail(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
 // flag unless force is set).
 void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, cudaStream_t s);
 
-// One kick-drift step of the plain FP64 form (wf_step_fp64.cu).
+// One kick-drift step of the plain FP64 form (wf_step_fp64.cu), and the part
+// of it after the schedule and search (the adjoint's recompute snapshots the
+// state between the two).
 void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
+void launch_step_fp64_body(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
 // One kick-drift step of the mixed FP32/FP64 form (wf_step_mixed.cu).
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
 

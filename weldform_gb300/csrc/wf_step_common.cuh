@@ -87,6 +87,7 @@ __device__ __forceinline__ double hollomon_yield(const MaterialDev& M, double st
 struct StressIO {
   double tau[6], sig[6], eps[6], epl[6], epli[6];
   double pressure, pl_strain, delta_pl_strain, sigmay, Ep, esr;
+  double sc = 1.0, sy_new = 0.0;  // branch record: scale factor and the step's flow stress
 };
 __device__ __forceinline__ double stress_update(StressIO& s, const double sr[6], const double rr[3], double rho,
                                                 double rho0, double Cs, double P0, double G, double T, int fail,
@@ -120,6 +121,8 @@ __device__ __forceinline__ double stress_update(StressIO& s, const double sr[6],
     for (int c = 0; c < 6; ++c) t6[c] = sc * t6[c];
     if (model == 1 && M) s.sigmay = hollomon_yield(*M, s.pl_strain);
     else if (model == 2 && M) s.sigmay = jc_yield(*M, s.pl_strain, s.esr, T);
+    s.sc = sc;
+    s.sy_new = s.sigmay;
     if (sig_trial > s.sigmay) {
       if (s.Ep < 0) s.Ep = M ? M->E : 0.0;
       dep = (sig_trial - s.sigmay) / (3. * G + s.Ep);

@@ -192,6 +192,8 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
   if (i < K.N) {
     int kind = icol(P, I_KIND, N, i);
     double a[3] = {col(P, C_A, N, i), col(P, C_A + 1, N, i), col(P, C_A + 2, N, i)};
+    if (P.tx)
+      for (int d = 0; d < 3; ++d) P.tx[(size_t)(TX_APRE + d) * N + i] = a[d];
     if (K.contact) {
       double cf[3] = {0, 0, 0}, dcont = 0.0;
       int ncp = kind == 0 ? P.cp_len[i] : 0;
@@ -297,6 +299,10 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
   double vi0 = col(P, C_V, N, i), vi1 = col(P, C_V + 1, N, i), vi2 = col(P, C_V + 2, N, i);
   double rhoi = col(P, C_RHO, N, i);
   double dd = 0.0;
+  if (P.tx) {
+    P.tx[(size_t)(TX_VH + 0) * N + i] = vi0; P.tx[(size_t)(TX_VH + 1) * N + i] = vi1;
+    P.tx[(size_t)(TX_VH + 2) * N + i] = vi2;
+  }
   if (icol(P, I_KIND, N, i) == 0) {
     double hi = col(P, C_H, N, i);
     int len = P.row_len[i];
@@ -370,8 +376,15 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
       int mi = icol(P, I_MAT, N, i);
       const MaterialDev* M = (mi >= 0 && mi < P.tab->nmat) ? &P.tab->mat[mi] : nullptr;
       double T = col(P, C_T, N, i);
-      stress_update(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i), col(P, C_G, N, i), T,
-                    icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), M, dt);
+      double dep = stress_update(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i),
+                                 col(P, C_G, N, i), T, icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), M, dt);
+      if (P.tx) {
+        for (int c = 0; c < 6; ++c) P.tx[(size_t)(TX_SR + c) * N + i] = sr[c];
+        for (int c = 0; c < 3; ++c) P.tx[(size_t)(TX_RR + c) * N + i] = rr[c];
+        P.tx[(size_t)TX_SC * N + i] = s.sc;
+        P.tx[(size_t)TX_SYN * N + i] = s.sy_new;
+        P.tx[(size_t)TX_DEP * N + i] = dep;
+      }
       for (int c = 0; c < 6; ++c) {
         colw(P, C_TAU + c, N, i) = s.tau[c]; colw(P, C_SIG + c, N, i) = s.sig[c];
         colw(P, C_EPS + c, N, i) = s.eps[c]; colw(P, C_EPL + c, N, i) = s.epl[c];
@@ -667,8 +680,12 @@ void launch_step_tail(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
 }
 
 void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
-  int nb = nblk(K.N, BLOCK);
   launch_step_head(P, K, fscratch, iscratch, s);
+  launch_step_fp64_body(P, K, s);
+}
+
+void launch_step_fp64_body(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
+  int nb = nblk(K.N, BLOCK);
   k_accel<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_accel");
   launch_bc(P, K, C_V, s);
