@@ -228,6 +228,35 @@ def cpu_baseline(steps=2):
                       f"(search) step, reference-structured OpenMP restatement, {threads} threads"}
 
 
+def adjoint_leg(wfmod, steps=400, every=10, k=20):
+    """Reaction-force adjoint on the 53,352-particle penalty-contact workload
+    (R = 10 mm, L = 30 mm, dx = 0.55 mm, JC + conduction + plastic heating,
+    rigid plane at -20 m/s, friction 0.2, PFAC = 0.1 E / h), 400 steps, loss
+    over 40 samples against the curve of JC constants perturbed by N(0, 5%):
+    wall time of the adjoint (forward with checkpoints, reverse sweep) over a
+    plain FP64 forward run of the same steps (CUDA graph)."""
+    from weldform_gb300 import adjoint as adj
+    case = adj.ContactCase()
+    target = adj.perturbed_jc_target(case, steps, every)
+    d = wfmod.Domain()
+    mesh = adj.build(d, case, case.nominal())
+    d.prepare(case.dt)
+    d.checkpoint_save(0)
+    d.step(1)
+    d.checkpoint_restore(0)
+    fwd_ms, _ = d.step_timed(steps)
+    d.checkpoint_restore(0)
+    r = d.adjoint_reaction_loss(steps, every, target, mesh=mesh, checkpoint_every=k)
+    n = d.particle_count
+    d.close()
+    return {"workload": "penalty-contact cylinder R=10mm L=30mm dx=0.55mm, JC+thermal, plane -20 m/s",
+            "particles": n, "steps": steps, "samples": steps // every, "checkpoint_every": k, "form": "fp64",
+            "forward_ms": fwd_ms, "adjoint_forward_ms": r["fwd_ms"], "reverse_ms": r["adj_ms"],
+            "adjoint_over_forward": r["adj_ms"] / fwd_ms,
+            "gradient_over_forward": (r["fwd_ms"] + r["adj_ms"]) / fwd_ms,
+            "loss": r["loss"], "grad": dict(zip(wfmod.PARAMS, r["grad"].tolist()))}
+
+
 def dist_setup(n):
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
@@ -261,6 +290,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     a = ap.parse_args()
     warmup = max(a.warmup, 3)
     rank, world, local, pg = dist_setup(a.gpus)
@@ -359,6 +389,8 @@ def main():
         line["mixed_vs_fp64_rel_l2"] = {
             "Displacement": float(np.linalg.norm(xm - xf) / max(np.linalg.norm(xf), 1e-300)),
             "Sigma": float(np.linalg.norm(sm - sf) / max(np.linalg.norm(sf), 1e-300))}
+    if rank == 0 and not a.no_adjoint:
+        line["adjoint"] = adjoint_leg(wfmod)
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
