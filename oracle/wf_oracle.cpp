@@ -99,6 +99,59 @@ inline double grad_kernel(int dim, double q, double h) {
   else if (q < 2.0) return C / (q * h) * ((-3.0 / 4.0) * (2.0 - q) * (2.0 - q));
   return 0.0;
 }
+// Functions.cpp:25-36 Kernel, cubic spline (KernelType 0).
+inline double kernel_w(int dim, double q, double h) {
+  double C = (dim == 2) ? 10.0 / (7.0 * h * h * PI) : 1.0 / (h * h * h * PI);
+  if (q < 1.0) return C * (1.0 - (3.0 / 2.0) * q * q + (3.0 / 4.0) * q * q * q);
+  else if (q < 2.0) return C * ((1.0 / 4.0) * (2.0 - q) * (2.0 - q) * (2.0 - q));
+  return 0.0;
+}
+// Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations, standing in
+// for gsl_eigen_symmv (matvec.h:776-803, GSL not available here): eigenvalues
+// L (ascending, as Rotation's SortAsc) and eigenvectors as the columns of V.
+// Functions of the spectrum that do not depend on the eigenvector basis (the
+// tensile-instability stress below) agree with any backward-stable solver to
+// rounding.
+inline void eig_sym3(const M3& M, double L[3], M3& V) {
+  double a[3][3];
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) a[i][j] = 0.5 * (at(M, i, j) + at(M, j, i));
+  double v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (off <= 1e-36 * diag || off == 0.0) break;
+    const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (auto& e : pq) {
+      int p = e[0], q = e[1];
+      if (a[p][q] == 0.0) continue;
+      double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+      double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+      double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+      for (int k = 0; k < 3; ++k) {  // A <- A J (columns p, q)
+        double akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - sn * akq;
+        a[k][q] = sn * akp + c * akq;
+      }
+      for (int k = 0; k < 3; ++k) {  // A <- J^T A (rows p, q)
+        double apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - sn * aqk;
+        a[q][k] = sn * apk + c * aqk;
+      }
+      for (int k = 0; k < 3; ++k) {
+        double vkp = v[k][p], vkq = v[k][q];
+        v[k][p] = c * vkp - sn * vkq;
+        v[k][q] = sn * vkp + c * vkq;
+      }
+    }
+  }
+  int ord[3] = {0, 1, 2};
+  std::sort(ord, ord + 3, [&](int x, int y) { return a[x][x] < a[y][y]; });
+  for (int k = 0; k < 3; ++k) {
+    L[k] = a[ord[k]][ord[k]];
+    for (int r = 0; r < 3; ++r) at(V, r, k) = v[r][ord[k]];
+  }
+}
+
 // Functions.cpp:206-212 EOS case 0.
 inline double eos0(double Cs, double P0, double rho, double rho0) { return P0 + (Cs * Cs) * (rho - rho0); }
 
@@ -195,8 +248,8 @@ struct Domain {
   std::vector<V3> x, v, a, x_prev, disp, normal, contforce;
   std::vector<double> rho, rho0, mass, h, Cs, P0, G, pressure, pl_strain, delta_pl_strain, sigmay, Ep,
       eff_strain_rate, T, dTdt, k_T, cp_T, th_exp, q_plheat, q_conv, q_source, q_cont_conv, ps_energy, alpha,
-      beta, TI, TIInitDist, dDensity, cont_stiff, delta_cont, dkin, dint;
-  std::vector<M3> sigma, tau, srate, rrate, strain, strain_pl, strain_pl_incr;
+      beta, TI, TIn, TIInitDist, dDensity, cont_stiff, delta_cont, dkin, dint;
+  std::vector<M3> sigma, tau, srate, rrate, strain, strain_pl, strain_pl_incr, TIR;
   std::vector<int> ID, ID_orig, not_write_surf, is_free, material_idx, mat, model, fail_crit, pres_eq, Nb, mesh_of, elem_of;
 
   std::vector<Material> materials;
@@ -248,10 +301,10 @@ struct Domain {
     Ep.push_back(0); eff_strain_rate.push_back(0); T.push_back(0); dTdt.push_back(0); k_T.push_back(0);
     cp_T.push_back(0); th_exp.push_back(0); q_plheat.push_back(0); q_conv.push_back(0); q_source.push_back(0);
     q_cont_conv.push_back(0); ps_energy.push_back(0); alpha.push_back(0); beta.push_back(0); TI.push_back(0);
-    TIInitDist.push_back(0); dDensity.push_back(0); cont_stiff.push_back(0); delta_cont.push_back(0);
+    TIn.push_back(4.0); TIInitDist.push_back(0); dDensity.push_back(0); cont_stiff.push_back(0); delta_cont.push_back(0);
     dkin.push_back(0); dint.push_back(0);
     sigma.push_back(zero3()); tau.push_back(zero3()); srate.push_back(zero3()); rrate.push_back(zero3());
-    strain.push_back(zero3()); strain_pl.push_back(zero3()); strain_pl_incr.push_back(zero3());
+    strain.push_back(zero3()); strain_pl.push_back(zero3()); strain_pl_incr.push_back(zero3()); TIR.push_back(zero3());
     ID.push_back(tag); ID_orig.push_back(tag); not_write_surf.push_back(0); is_free.push_back(fixed ? 0 : 1);
     material_idx.push_back(0); mat.push_back(-1); model.push_back(0); fail_crit.push_back(0); pres_eq.push_back(0);
     Nb.push_back(0); mesh_of.push_back(-1); elem_of.push_back(-1);
@@ -725,12 +778,21 @@ struct Domain {
       double Cij = 0.5 * (Cs[P1] + Cs[P2]);  // SoundSpeed case 0 returns Cs (Functions.cpp:232-238)
       if (dot(vij, xij) < 0) { PI_s = (Alpha * Cij * MUij + Beta * MUij * MUij) / (0.5 * (di + dj)); has_pi = true; }
     }
+    // Tensile instability (InteractionAlt.cpp:102-109):
+    // TIij = (W(rij/h) / W(dinit/h))^((n1+n2)/2) (TIR1 + TIR2)
+    bool has_ti = TI[P1] > 0.0 || TI[P2] > 0.0;
+    double fti = 0.0;
+    if (has_ti) {
+      double K = kernel_w(dim, rij / hh, hh);
+      fti = std::pow((K / kernel_w(dim, (TIInitDist[P1] + TIInitDist[P2]) / (2.0 * hh), hh)), (TIn[P1] + TIn[P2]) / 2.0);
+    }
     M3 S;
     double ci = 1.0 / (di * di), cj = 1.0 / (dj * dj);
     for (int k = 0; k < 3; ++k)
       for (int l = 0; l < 3; ++l) {
         double s = ci * at(sigma[P1], k, l) + cj * at(sigma[P2], k, l);
         if (has_pi) s = s + PI_s * I3(k, l);
+        if (has_ti) s = s + fti * (at(TIR[P1], k, l) + at(TIR[P2], k, l));
         at(S, k, l) = s;
       }
     return vecmat(scl(GK, xij), S);
@@ -1116,7 +1178,6 @@ struct Domain {
     if (dim != 3) return set_err(WF_ERR_UNSUPPORTED, "only Dimension = 3 is supported");
     for (int i = 0; i < N; ++i) {
       if (!is_free[i]) return set_err(WF_ERR_UNSUPPORTED, "fixed (non-free) particles are not supported");
-      if (TI[i] > 0.0) return set_err(WF_ERR_UNSUPPORTED, "tensile instability (TI > 0) is not supported");
       if (pres_eq[i] != 0) return set_err(WF_ERR_UNSUPPORTED, "only PresEq = 0 is supported");
     }
     if (solid_part_count < 0) solid_part_count = N;
@@ -1151,7 +1212,21 @@ struct Domain {
   // StartAcceleration and the neighbour-search schedule (SolverKickDrift.cpp:117-186).
   int begin_step() {
     int rc;
-    // StartAcceleration (Domain.cpp:1519-1597) for free particles with TI = 0
+    // StartAcceleration (Domain.cpp:1519-1597) for free particles: the
+    // tensile-instability stress TIR = V diag(f(L)) V^T of Sigma with
+    // f(l) = -TI l / rho^2 for l > 0, else 0 (3D branch, :1557-1569).
+    for (int i = 0; i < N; i++) {
+      if (TI[i] > 0.0) {
+        double rho2 = rho[i] * rho[i];
+        double pc = TI[i] / (rho2);
+        double L[3];
+        M3 V;
+        eig_sym3(sigma[i], L, V);
+        M3 Val = zero3();
+        for (int k = 0; k < 3; ++k) at(Val, k, k) = (L[k] > 0) ? -pc * L[k] : 0.0;
+        TIR[i] = matmul(matmul(V, Val), trans(V));
+      }
+    }
     for (int i = 0; i < N; i++) { a[i] = v3(0, 0, 0); dDensity[i] = 0.; srate[i] = zero3(); rrate[i] = zero3(); }
     double mx = 0;
     for (int i = 0; i < N; i++) if (pl_strain[i] > mx) mx = pl_strain[i];
@@ -1228,6 +1303,7 @@ std::vector<double>* f64_field(Domain* d, const std::string& f) {
   if (f == "Beta") return &d->beta;
   if (f == "TI") return &d->TI;
   if (f == "TIInitDist") return &d->TIInitDist;
+  if (f == "TIn") return &d->TIn;
   if (f == "k_T") return &d->k_T;
   if (f == "cp_T") return &d->cp_T;
   if (f == "T") return &d->T;
@@ -1263,6 +1339,7 @@ std::vector<M3>* m3_field(Domain* d, const std::string& f) {
   if (f == "RotationRate") return &d->rrate;
   if (f == "Strain") return &d->strain;
   if (f == "Strain_pl") return &d->strain_pl;
+  if (f == "TIR") return &d->TIR;
   return nullptr;
 }
 std::vector<int>* i32_field(Domain* d, const std::string& f) {
@@ -1557,8 +1634,10 @@ int wfo_adjoint_reaction_loss(wfo_domain* p, int64_t steps, int every, int mesh,
   if (axis < 0 || axis > 2 || every < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps || !target || !loss ||
       !grad)
     return set_err(WF_ERR_ARG, "adjoint: bad steps / sampling / target arguments");
-  for (int i = 0; i < d->N; ++i)
+  for (int i = 0; i < d->N; ++i) {
     if (d->Ep[i] < 0.0) return set_err(WF_ERR_UNSUPPORTED, "adjoint: particles with Ep < 0 are not supported");
+    if (d->TI[i] > 0.0) return set_err(WF_ERR_UNSUPPORTED, "adjoint: tensile instability (TI > 0) is not supported");
+  }
   auto t0 = std::chrono::steady_clock::now();
   Tangent T(*d);
   T.init();

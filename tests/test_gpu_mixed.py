@@ -92,3 +92,9 @@ def test_mixed_250k_1000_steps_against_oracle():
     assert m["v"].shape[0] == 240300
     errs = _check(m, o, FIELDS)
     print("mixed vs oracle, 240300 particles, 1000 steps:", errs)
+
+
+def test_mixed_tensile_instability():
+    from tests.test_gpu_parity import _tensile
+    m, o = _run(_tensile, 100, FIELDS, R=0.004, L=0.008, dx=0.0005, v_top=20.0)
+    _check(m, o, FIELDS)

@@ -168,3 +168,20 @@ def test_config1_full_1000_steps():
     g, o = _pair(configs.cylinder_upsetting, 1000, FIELDS, SCALARS)
     assert g["x"].shape[0] == 8004
     _check(g, o, FIELDS, SCALARS)
+
+
+def _tensile(dom, **kw):
+    """Cylinder pulled at the top (tension), tensile-instability term on
+    (TI = 0.3, TIInitDist = dx, TIn = 4: the JSON driver's defaults,
+    WeldForm.cpp:368, 900-901)."""
+    case = configs.cylinder_upsetting(dom, **kw)
+    dom.set_particles("TI", 0.3)
+    dom.set_particles("TIInitDist", case.dx)
+    return case
+
+
+def test_tensile_instability():
+    f = FIELDS + ("TIR",)
+    g, o = _pair(_tensile, 100, f, SCALARS, R=0.004, L=0.008, dx=0.0005, v_top=20.0)
+    assert np.abs(o["TIR"]).max() > 0
+    _check(g, o, f, SCALARS)

@@ -62,6 +62,31 @@ def test_yield_triggers_rebuild_schedule():
 def test_unsupported_features_are_rejected():
     d = oracle_domain()
     d.AddCylinderLength(0, (0, 0, 0), 0.003, 0.006, 0.00025, 7850.0, 0.0006, False)
-    d.set_particles("TI", 0.3)
+    d.set_particles("PresEq", 1)
     with pytest.raises(Exception):
         d.prepare(1e-8)
+
+
+def test_tensile_instability_stress_is_the_positive_spectral_part():
+    """StartAcceleration's TIR (Domain.cpp:1557-1569) from the stress at the
+    start of the step: -TI/rho^2 times the positive spectral part of Sigma,
+    checked against numpy's symmetric eigen-decomposition."""
+    d = oracle_domain()
+    d.AddCylinderLength(0, (0, 0, 0), 0.002, 0.004, 0.00025, 7850.0, 0.0006, False)
+    n = d.particle_count
+    rng = np.random.default_rng(7)
+    A = rng.normal(size=(n, 3, 3)) * 1e8
+    S = A + A.transpose(0, 2, 1)
+    S[::3] = np.diag([2e8, -1e8, 3e8])         # diagonal and
+    S[1::5] = np.diag([1e8, 1e8, -2e8])        # repeated eigenvalues
+    d.set_array("Sigma", S.reshape(n, 9))
+    d.set_particles("G", 76.9e9)
+    d.set_particles("Cs", 4607.8)
+    d.set_particles("TI", 0.3)
+    d.prepare(1e-9)
+    d.step(1)
+    tir = d.get_array("TIR").reshape(n, 3, 3)
+    w, V = np.linalg.eigh(S)
+    f = np.where(w > 0, -0.3 * w / 7850.0 ** 2, 0.0)
+    ref = np.einsum("nij,nj,nkj->nik", V, f, V)
+    assert np.abs(tir - ref).max() <= 1e-12 * np.abs(ref).max()

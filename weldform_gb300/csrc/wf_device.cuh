@@ -35,10 +35,12 @@ enum F64Col : int {
   C_SRHO = 84,             // Sigma / Density^2 (6), for the acceleration pair term
   C_MRHO = 90,             // Mass / Density
   C_PR2 = 91,              // Pressure / Density^2
-  NF64_PERSIST = 92,
-  // scratch columns (not permuted): next-step buffers
-  C_XN = 92, C_VN = 95, C_RHON = 98, C_MRHON = 99,
-  NF64 = 100
+  C_TI = 92, C_TIN, C_TIDIST,  // tensile instability: TI, TIn, TIInitDist (Particle.h:146-149)
+  NF64_PERSIST = 95,
+  // scratch columns (not permuted): next-step buffers and the
+  // tensile-instability stress TIR (6), recomputed at every step start
+  C_XN = 95, C_VN = 98, C_RHON = 101, C_MRHON = 102, C_TIR = 103,
+  NF64 = 109
 };
 enum I32Col : int {
   I_ID = 0, I_IDORIG, I_NWS, I_MAT, I_MODEL, I_FAIL, I_MATERIAL, I_NB, I_KIND, I_ELEM, I_MESH, I_ORIG,
@@ -66,7 +68,9 @@ enum RecCur : int {        // current-state groups
   RC_S1 = 5,               // Sigma/rho^2 xz yz, p/rho^2, Cs
   RC_MISC = 6,             // alpha, beta, k_T, T hi
   RC_T2 = 7,               // T lo
-  RC_N = 8
+  RC_TI0 = 8,              // TIR xx yy zz xy (tensile instability, when any TI > 0)
+  RC_TI1 = 9,              // TIR xz yz, TIn, TIInitDist
+  RC_N = 10
 };
 enum RecNext : int {       // next-step groups
   RN_XH = 0, RN_XL = 1,    // as RC_XH / RC_XL at x(n+1)
@@ -157,6 +161,7 @@ struct DomainConst {
   int nblocks;         // blocks of the per-particle kernels (partials stride)
   int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
   int gblock;          // thread-block size of the mixed form's gather kernels
+  int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
 };
 
 // Device pointers, passed by value to every kernel.

@@ -78,7 +78,8 @@ int col_f64(const std::string& n, int* ncomp) {
       {"T", C_T, 1}, {"dTdt", C_DTDT, 1}, {"k_T", C_KT, 1}, {"cp_T", C_CPT, 1}, {"th_exp", C_THEXP, 1},
       {"q_plheat", C_QPL, 1}, {"q_source", C_QSRC, 1}, {"Alpha", C_ALPHA, 1}, {"Beta", C_BETA, 1},
       {"ps_energy", C_PSEN, 1}, {"delta_cont", C_DCONT, 1}, {"dkin_energy_dt", C_DKIN, 1},
-      {"dint_energy_dt", C_DINT, 1}, {"dDensity", C_DRHO, 1}, {"Sigma", C_SIG, 6}, {"ShearStress", C_TAU, 6},
+      {"dint_energy_dt", C_DINT, 1}, {"dDensity", C_DRHO, 1}, {"TI", C_TI, 1}, {"TIn", C_TIN, 1},
+      {"TIInitDist", C_TIDIST, 1}, {"TIR", C_TIR, 6}, {"Sigma", C_SIG, 6}, {"ShearStress", C_TAU, 6},
       {"Strain", C_EPS, 6}, {"Strain_pl", C_EPL, 6}, {"Strain_pl_incr", C_EPLI, 6}, {"StrainRate", C_SR, 6},
       {"RotationRate", C_RR, 3}};
   for (const E& e : tab)
@@ -186,6 +187,7 @@ struct wf_domain {
     hp.f[C_RHO][p] = dens; hp.f[C_RHO0][p] = dens; hp.f[C_MASS][p] = m0; hp.f[C_H][p] = h;
     hp.i[I_ID][p] = tag; hp.i[I_IDORIG][p] = tag; hp.i[I_MAT][p] = -1; hp.i[I_KIND][p] = kind;
     hp.i[I_ELEM][p] = -1; hp.i[I_MESH][p] = -1; hp.i[I_ORIG][p] = p;
+    hp.f[C_TIN][p] = 4.0;  // Particle.cpp:47
   }
   double& F(int c, int p) { return hp.f[c][p]; }
 
@@ -550,6 +552,9 @@ struct wf_domain {
     for (int p = 0; p < N; ++p) tm += F(C_MASS, p);
     K.totmass_mean = tm / N;
     K.id_free_surf = -999999;
+    K.ti = 0;
+    for (int p = 0; p < N; ++p)
+      if (hp.i[I_KIND][p] == 0 && F(C_TI, p) > 0.0) K.ti = 1;
     K.nmeshes = (int)meshes.size();
     for (size_t m = 0; m < meshes.size(); ++m) K.contact_surf_id[m] = meshes[m].id;
     K.nblocks = (N + 255) / 256;
@@ -780,6 +785,7 @@ struct wf_domain {
     if (!prepared) throw CudaError{WF_ERR_STATE, "adjoint before wf_prepare_kickdrift"};
     if (precision != WF_PRECISION_FP64)
       throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint runs on the plain FP64 form (precision 0)"};
+    if (K.ti) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: tensile instability (TI > 0) is not supported"};
     if (!contact || mesh < 0 || mesh >= (int)meshes.size())
       throw CudaError{WF_ERR_ARG, "the reaction-force loss needs a rigid mesh"};
     if (axis < 0 || axis > 2 || every < 1 || kchk < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps ||
@@ -1231,11 +1237,6 @@ int wf_set_particle_f64(wf_domain* d, const char* field, int zone, double value)
   NEED(d);
   if (d->prepared) return set_err(WF_ERR_STATE, "use wf_set_particle_array_f64 after the prologue");
   std::string f(field ? field : "");
-  if (f == "TI") {  // tensile-instability term (InteractionAlt.cpp:106-110) is outside this build
-    if (value != 0.0) return set_err(WF_ERR_UNSUPPORTED, "tensile instability (TI > 0) is not supported");
-    return WF_OK;
-  }
-  if (f == "TIInitDist") return WF_OK;  // only used by the TI term
   int nc = 0;
   int c = col_f64(f, &nc);
   if (c < 0 || nc != 1) return set_err(WF_ERR_ARG, "unknown particle f64 field " + f);

@@ -47,6 +47,8 @@ void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, c
 // state between the two).
 void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
 void launch_step_fp64_body(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
+// Tensile-instability stress TIR of every particle (no-op unless K.ti).
+void launch_tensile(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
 // One kick-drift step of the mixed FP32/FP64 form (wf_step_mixed.cu).
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s);
 

@@ -80,6 +80,52 @@ __device__ __forceinline__ double hollomon_yield(const MaterialDev& M, double st
   return M.sy0;
 }
 
+// Cubic-spline kernel W(q) (Functions.cpp:25-36, 3D) without its constant
+// 1/(pi h^3): the tensile-instability term only uses ratios of W.
+__device__ __forceinline__ double kernel_shape(double q) {
+  if (q < 1.0) return 1.0 - (3.0 / 2.0) * q * q + (3.0 / 4.0) * q * q * q;
+  else if (q < 2.0) return (1.0 / 4.0) * (2.0 - q) * (2.0 - q) * (2.0 - q);
+  return 0.0;
+}
+
+// Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations (a published
+// method; the reference calls GSL's gsl_eigen_symmv through Rotation,
+// Functions.cpp:381-395).  s: xx yy zz xy xz yz.  Returns the eigenvalues in
+// L and the eigenvectors as columns of V.  The sweep count is bounded.
+__device__ __forceinline__ void eig_sym3(const double s[6], double L[3], double V[3][3]) {
+  double a[3][3] = {{s[0], s[3], s[4]}, {s[3], s[1], s[5]}, {s[4], s[5], s[2]}};
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) V[r][c] = (r == c) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (off == 0.0 || off <= 1e-36 * diag) break;
+    for (int e = 0; e < 3; ++e) {
+      int p = e == 2 ? 1 : 0, q = e == 0 ? 1 : 2;
+      if (a[p][q] == 0.0) continue;
+      double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+      double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+      double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+      for (int k = 0; k < 3; ++k) {
+        double akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - sn * akq;
+        a[k][q] = sn * akp + c * akq;
+      }
+      for (int k = 0; k < 3; ++k) {
+        double apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - sn * aqk;
+        a[q][k] = sn * apk + c * aqk;
+      }
+      for (int k = 0; k < 3; ++k) {
+        double vkp = V[k][p], vkq = V[k][q];
+        V[k][p] = c * vkp - sn * vkq;
+        V[k][q] = sn * vkp + c * vkq;
+      }
+    }
+  }
+  for (int k = 0; k < 3; ++k) L[k] = a[k][k];
+}
+
 // Radial-return constitutive update of one particle, Particle::CalcStressStrain
 // (Source/Particle.cpp:960-1067), on symmetric storage (xx yy zz xy xz yz).
 // sr: strain rate (6), rr: rotation rate (xy xz yz of the antisymmetric part).

@@ -90,6 +90,40 @@ __device__ __forceinline__ PairGeo pair_geo(double xi0, double xi1, double xi2, 
   return g;
 }
 
+// ---------------------------------------------------------------- tensile instability
+// StartAcceleration's TIR (Domain.cpp:1557-1569): TIR = V diag(f(L)) V^T for
+// the eigen-decomposition of Sigma, f(l) = -TI l / rho^2 for l > 0, else 0;
+// products summed k = 2, 1, 0 as matvec.h's Mult.  Also fills the mixed
+// form's FP32 groups.
+__global__ void k_tensile(DevPtrs P, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  double tir[6] = {0, 0, 0, 0, 0, 0};
+  double ti = col(P, C_TI, N, i);
+  if (icol(P, I_KIND, N, i) == 0 && ti > 0.0) {
+    double rho = col(P, C_RHO, N, i);
+    double rho2 = rho * rho;
+    double pc = ti / (rho2);
+    double sg[6], L[3], V[3][3];
+    for (int c = 0; c < 6; ++c) sg[c] = col(P, C_SIG + c, N, i);
+    eig_sym3(sg, L, V);
+    double f[3];
+    for (int k = 0; k < 3; ++k) f[k] = (L[k] > 0) ? -pc * L[k] : 0.0;
+    const int ui[6] = {0, 1, 2, 0, 0, 1}, uj[6] = {0, 1, 2, 1, 2, 2};
+    for (int c = 0; c < 6; ++c) {
+      int a = ui[c], b = uj[c];
+      tir[c] = (V[a][2] * f[2]) * V[b][2] + (V[a][1] * f[1]) * V[b][1] + (V[a][0] * f[0]) * V[b][0];
+    }
+  }
+  for (int c = 0; c < 6; ++c) colw(P, C_TIR + c, N, i) = tir[c];
+  if (K.mixed) {
+    P.rc[(size_t)RC_TI0 * N + i] = make_float4((float)tir[0], (float)tir[1], (float)tir[2], (float)tir[3]);
+    P.rc[(size_t)RC_TI1 * N + i] =
+        make_float4((float)tir[4], (float)tir[5], (float)col(P, C_TIN, N, i), (float)col(P, C_TIDIST, N, i));
+  }
+}
+
 // ---------------------------------------------------------------- accel
 __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -103,6 +137,7 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
   double vi0 = col(P, C_V, N, i), vi1 = col(P, C_V + 1, N, i), vi2 = col(P, C_V + 2, N, i);
   double hi = col(P, C_H, N, i), rhoi = col(P, C_RHO, N, i), csi = col(P, C_CS, N, i);
   double ai = col(P, C_ALPHA, N, i), bi = col(P, C_BETA, N, i);
+  double tii = K.ti ? col(P, C_TI, N, i) : 0.0;
   double Si[6];
   for (int c = 0; c < 6; ++c) Si[c] = col(P, C_SRHO + c, N, i);
   double a0 = 0, a1 = 0, a2 = 0;
@@ -128,6 +163,17 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
     double S3 = Si[3] + col(P, C_SRHO + 3, N, j);
     double S4 = Si[4] + col(P, C_SRHO + 4, N, j);
     double S5 = Si[5] + col(P, C_SRHO + 5, N, j);
+    if (K.ti && (tii > 0.0 || col(P, C_TI, N, j) > 0.0)) {
+      // TIij = (W(rij/h) / W(dinit/h))^((n_i + n_j)/2) (TIR_i + TIR_j) (InteractionAlt.cpp:102-109)
+      double q0 = (col(P, C_TIDIST, N, i) + col(P, C_TIDIST, N, j)) / (2.0 * g.hh);
+      double f = pow((kernel_shape(g.r / g.hh) / kernel_shape(q0)), (col(P, C_TIN, N, i) + col(P, C_TIN, N, j)) / 2.0);
+      S0 = S0 + f * (col(P, C_TIR + 0, N, i) + col(P, C_TIR + 0, N, j));
+      S1 = S1 + f * (col(P, C_TIR + 1, N, i) + col(P, C_TIR + 1, N, j));
+      S2 = S2 + f * (col(P, C_TIR + 2, N, i) + col(P, C_TIR + 2, N, j));
+      S3 = S3 + f * (col(P, C_TIR + 3, N, i) + col(P, C_TIR + 3, N, j));
+      S4 = S4 + f * (col(P, C_TIR + 4, N, i) + col(P, C_TIR + 4, N, j));
+      S5 = S5 + f * (col(P, C_TIR + 5, N, i) + col(P, C_TIR + 5, N, j));
+    }
     double g0 = g.GK * g.x0, g1 = g.GK * g.x1, g2 = g.GK * g.x2;
     double t0 = g0 * S0 + g1 * S3 + g2 * S4;
     double t1 = g0 * S3 + g1 * S1 + g2 * S5;
@@ -684,8 +730,15 @@ void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, 
   launch_step_fp64_body(P, K, s);
 }
 
+void launch_tensile(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
+  if (!K.ti) return;
+  k_tensile<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  mark(s, "k_tensile");
+}
+
 void launch_step_fp64_body(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
   int nb = nblk(K.N, BLOCK);
+  launch_tensile(P, K, s);
   k_accel<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_accel");
   launch_bc(P, K, C_V, s);

@@ -87,6 +87,7 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
 }
 
 // ---------------------------------------------------------------- accel
+template <bool TI>
 __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
@@ -98,6 +99,9 @@ __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
   const float4* ri = P.rc + i;
   float4 xh = ld4(ri + (size_t)RC_XH * N), xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
   float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1 = ld4(ri + (size_t)RC_S1 * N), mi = ld4(ri + (size_t)RC_MISC * N);
+  float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
+  float tii = 0.f;
+  if (TI) { t0 = ld4(ri + (size_t)RC_TI0 * N); t1 = ld4(ri + (size_t)RC_TI1 * N); tii = (float)col(P, C_TI, N, i); }
   KSum a0, a1, a2;
   int len = P.row_len[i];
   const int* nb = P.nbr + i;
@@ -123,6 +127,18 @@ __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
     }
     float S0 = s0.x + js0.x + PIs, S1 = s0.y + js0.y + PIs, S2 = s0.z + js0.z + PIs;
     float S3 = s0.w + js0.w, S4 = s1.x + js1.x, S5 = s1.y + js1.y;
+    if (TI) {  // tensile instability (InteractionAlt.cpp:102-109); TIR = 0 where TI = 0
+      float4 jt0 = ld4(rj + (size_t)RC_TI0 * N), jt1 = ld4(rj + (size_t)RC_TI1 * N);
+      if (tii > 0.f || (float)col(P, C_TI, N, j) > 0.f) {
+        float q = r / hh, q0 = (t1.w + jt1.w) / (2.f * hh);
+        float wq = q < 1.f ? 1.f - 1.5f * q * q + 0.75f * q * q * q : (q < 2.f ? 0.25f * (2.f - q) * (2.f - q) * (2.f - q) : 0.f);
+        float w0 = q0 < 1.f ? 1.f - 1.5f * q0 * q0 + 0.75f * q0 * q0 * q0
+                            : (q0 < 2.f ? 0.25f * (2.f - q0) * (2.f - q0) * (2.f - q0) : 0.f);
+        float f = powf(wq / w0, 0.5f * (t1.z + jt1.z));
+        S0 += f * (t0.x + jt0.x); S1 += f * (t0.y + jt0.y); S2 += f * (t0.z + jt0.z);
+        S3 += f * (t0.w + jt0.w); S4 += f * (t1.x + jt1.x); S5 += f * (t1.y + jt1.y);
+      }
+    }
     float g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
     float mj = jxl.w;
     a0.add(mj * (g0 * S0 + g1 * S3 + g2 * S4));
@@ -416,7 +432,9 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   int ng = nblk(K.N, gb);
   launch_step_head(P, K, fscratch, iscratch, s);
   launch_refresh_shadows(P, K, 0, s);
-  k_accel_mx<<<ng, gb, 0, s>>>(P, K);
+  launch_tensile(P, K, s);
+  if (K.ti) k_accel_mx<true><<<ng, gb, 0, s>>>(P, K);
+  else k_accel_mx<false><<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
