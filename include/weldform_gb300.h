@@ -77,6 +77,7 @@ int wf_domain_destroy(wf_domain* d);
  * "contact_force_factor".  Integer fields: "Nproc", "ts_nb_inc", "auto_ts",
  * "nonlock_sum", "pl_heating", "thermal_solver", "contact",
  * "contact_mesh_auto_update", "GradientType", "contact_alg" (WF_CONTACT_*),
+ * "integrator" (0 kick-drift, 1 leapfrog; before the prologue),
  * "precision" (WF_PRECISION_*), "device" (CUDA device ordinal, before the
  * prologue), "use_graph" (replay each step as one CUDA graph, default 1),
  * "cpu_threads" (unused on the GPU path). */
@@ -109,7 +110,7 @@ int wf_assign_zone(wf_domain* d, const double start[3], const double end[3], int
 
 /* Per-particle public fields (Source/Particle.h:50-265) for every particle
  * whose ID equals `zone`, or all particles when zone < 0.
- * f64 fields: "G", "Cs", "Sigmay", "Ep", "Alpha", "Beta", "TI", "TIInitDist",
+ * f64 fields: "G", "Cs", "Sigmay", "Ep", "Alpha", "Beta", "TI", "TIn", "TIInitDist",
  * "k_T", "cp_T", "T", "th_exp", "Density", "RefDensity", "Mass", "h", "P0",
  * "q_source".  i32 fields: "PresEq", "Fail", "Material_model", "mat",
  * "Material", "ID", "IsFree", "print_history". */
@@ -118,7 +119,7 @@ int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value);
 /* Whole-array transfer in original particle order.  Vector fields ("x", "v",
  * "a", "Displacement", "normal", "contforce") take 3 values per particle;
  * tensor fields ("Sigma", "ShearStress", "StrainRate", "RotationRate",
- * "Strain", "Strain_pl") 9 (row-major, full 3x3, as the reference stores
+ * "Strain", "Strain_pl", "TIR" read-only) 9 (row-major, full 3x3, as the reference stores
  * them); scalars 1 ("Density", "Pressure", "pl_strain", "Sigmay", "T",
  * "dTdt", "eff_strain_rate", "q_plheat", "Mass", "h", "delta_pl_strain",
  * "dDensity").  n is the total number of doubles. */
@@ -168,7 +169,15 @@ int wf_get_contact_force(wf_domain* d, int mesh, double out[3]);
  * Source/SolverKickDrift.cpp:23-401) without file output: runs the prologue
  * (if not yet run) and steps while Time <= tf && idx_out <= maxidx. */
 int wf_solve_kickdrift(wf_domain* d, double tf, double dt, double dtOut, int64_t maxidx);
-/* The solver prologue only (SolverKickDrift.cpp:23-115) with time step dt. */
+/* Domain::SolveDiffUpdateLeapFrog (Source/Domain.h:200,
+ * Source/SolverLeapfrog.cpp:24-451): the same prologue and rebuild schedule
+ * with the leapfrog update (velocities at half steps: the first step starts
+ * from v - a dt/2, then v += a dt; density and drift with v(n+1/2), rates at
+ * x(n+1), v(n+1/2)).  Equivalent to wf_set_domain_i32(d, "integrator", 1)
+ * before the prologue followed by wf_solve_kickdrift. */
+int wf_solve_leapfrog(wf_domain* d, double tf, double dt, double dtOut, int64_t maxidx);
+/* The solver prologue only (SolverKickDrift.cpp:23-115, identical for the
+ * leapfrog solver) with time step dt. */
 int wf_prepare_kickdrift(wf_domain* d, double dt);
 /* Advance exactly nsteps kick-drift steps (SolverKickDrift.cpp:117-393). */
 int wf_step(wf_domain* d, int64_t nsteps);

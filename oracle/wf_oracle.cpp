@@ -241,6 +241,7 @@ struct Domain {
   double DomMax[3] = {-100000000000.0, -100000000000.0, -100000000000.0};
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int mode = 0;       // 0 canonical, 1 reference-structured
+  int integrator = 0; // 0 kick-drift (SolverKickDrift.cpp), 1 leapfrog (SolverLeapfrog.cpp)
   int nthreads = 1;
 
   // particles (SoA, original order)
@@ -1254,6 +1255,28 @@ struct Domain {
     pass_accel();
     general_after();
     if (contact) contact_wang();
+    if (integrator == 1) {
+      // SolverLeapfrog.cpp:233-260: velocities at half steps; the first step
+      // starts from v - a dt/2, then v += a (dt_prev + dt)/2.
+      if (isfirst)
+        for (int i = 0; i < N; i++) v[i] = sub(v[i], v3(a[i].c[0] * 0.5 * deltat, a[i].c[1] * 0.5 * deltat, a[i].c[2] * 0.5 * deltat));
+      general_after();
+      prev_deltat = deltat;
+      for (int i = 0; i < N; i++) {
+        double f = 0.5 * (prev_deltat + deltat);
+        v[i] = add(v[i], v3(a[i].c[0] * f, a[i].c[1] * f, a[i].c[2] * f));
+      }
+      general_after();
+      pass_density();  // SolverLeapfrog.cpp:263-275 (x at n, v at n+1/2)
+      for (int i = 0; i < N; i++) rho[i] += deltat * dDensity[i];
+      for (int i = 0; i < N; i++) {
+        x_prev[i] = x[i];
+        V3 du = scl(deltat, v[i]);
+        disp[i] = add(disp[i], du);
+        x[i] = add(x[i], du);
+      }
+      pass_rates();  // x at n+1, v at n+1/2 (:287-291)
+    } else {
     prev_deltat = deltat;
     for (int i = 0; i < N; i++) v[i] = add(v[i], scl(0.5 * prev_deltat, a[i]));
     general_after();
@@ -1268,6 +1291,7 @@ struct Domain {
     for (int i = 0; i < N; i++) v[i] = add(v[i], v3(a[i].c[0] * deltat / 2., a[i].c[1] * deltat / 2., a[i].c[2] * deltat / 2.));
     general_after();
     pass_rates();
+    }
 #pragma omp parallel for schedule(static) num_threads(nthreads)
     for (int i = 0; i < solid_part_count; i++) if (!is_mesh(i)) stress_strain(i, deltat);
     plastic_work_heat(deltat);
@@ -1395,6 +1419,7 @@ int wfo_set_domain_i32(wfo_domain* p, const char* name, int v) {
   else if (n == "contact_mesh_auto_update") d->contact_mesh_auto_update = v;
   else if (n == "contact_alg") d->contact_alg = v;
   else if (n == "cpu_mode") d->mode = v;
+  else if (n == "integrator") d->integrator = v;
   else if (n == "cpu_threads" || n == "Nproc") d->nthreads = v > 0 ? v : 1;
   else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
@@ -1573,6 +1598,14 @@ int wfo_solve_kickdrift(wfo_domain* p, double tf, double dt, double dtOut, int64
   }
   return WF_OK;
 }
+// Domain::SolveDiffUpdateLeapFrog (SolverLeapfrog.cpp:24-451): the same
+// prologue and schedule as the kick-drift loop with the leapfrog update.
+int wfo_solve_leapfrog(wfo_domain* p, double tf, double dt, double dtOut, int64_t maxidx) {
+  Domain* d = D(p);
+  if (d->prepared && d->integrator != 1) return set_err(WF_ERR_STATE, "the domain was prepared for kick-drift");
+  d->integrator = 1;
+  return wfo_solve_kickdrift(p, tf, dt, dtOut, maxidx);
+}
 int wfo_neighbour_search(wfo_domain* p) { return D(p)->neighbour_search(); }
 int wfo_get_neighbours(wfo_domain* p, int64_t* off, int32_t* idx, int64_t cap) {
   Domain* d = D(p);
@@ -1629,6 +1662,7 @@ int wfo_adjoint_reaction_loss(wfo_domain* p, int64_t steps, int every, int mesh,
   (void)checkpoint_every;
   if (!d->prepared) return set_err(WF_ERR_STATE, "adjoint before wf_prepare_kickdrift");
   if (d->mode != 0) return set_err(WF_ERR_UNSUPPORTED, "the tangent run needs cpu_mode 0");
+  if (d->integrator != 0) return set_err(WF_ERR_UNSUPPORTED, "the adjoint differentiates the kick-drift step");
   if (!d->contact || mesh < 0 || mesh >= (int)d->meshes.size())
     return set_err(WF_ERR_ARG, "the reaction-force loss needs a rigid mesh");
   if (axis < 0 || axis > 2 || every < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps || !target || !loss ||

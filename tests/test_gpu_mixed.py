@@ -98,3 +98,10 @@ def test_mixed_tensile_instability():
     from tests.test_gpu_parity import _tensile
     m, o = _run(_tensile, 100, FIELDS, R=0.004, L=0.008, dx=0.0005, v_top=20.0)
     _check(m, o, FIELDS)
+
+
+def test_mixed_leapfrog():
+    from tests.test_gpu_parity import _leapfrog
+    f = FIELDS + ("pl_strain",)
+    m, o = _run(_leapfrog, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    _check(m, o, f)

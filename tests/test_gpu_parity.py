@@ -185,3 +185,30 @@ def test_tensile_instability():
     g, o = _pair(_tensile, 100, f, SCALARS, R=0.004, L=0.008, dx=0.0005, v_top=20.0)
     assert np.abs(o["TIR"]).max() > 0
     _check(g, o, f, SCALARS)
+
+
+def _leapfrog(dom, **kw):
+    dom.set("integrator", 1)
+    return configs.cylinder_upsetting(dom, **kw)
+
+
+def _leapfrog_contact(dom, **kw):
+    dom.set("integrator", 1)
+    return configs.contact_upsetting(dom, **kw)
+
+
+def test_leapfrog_yielding():
+    """SolveDiffUpdateLeapFrog's update (SolverLeapfrog.cpp:203-291) with
+    rebuilds every 5 steps once yielding."""
+    f = FIELDS + ("Strain_pl",)
+    g, o = _pair(_leapfrog, 80, f, SCALARS, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    assert o["pl_strain"].max() > 1e-3
+    _check(g, o, f, SCALARS)
+
+
+def test_leapfrog_contact_thermal():
+    f = FIELDS + ("T",)
+    g, o = _pair(_leapfrog_contact, 100, f, SCALARS, R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, gap=0.0,
+                 stiffness="area")
+    _check(g, o, f, SCALARS)
+    assert abs(g["cf"][2] - o["cf"][2]) <= 1e-9 * abs(o["cf"][2])

@@ -90,3 +90,21 @@ def test_tensile_instability_stress_is_the_positive_spectral_part():
     f = np.where(w > 0, -0.3 * w / 7850.0 ** 2, 0.0)
     ref = np.einsum("nij,nj,nkj->nik", V, f, V)
     assert np.abs(tir - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_leapfrog_first_step_matches_kickdrift_half_kick():
+    """Both integrators start from v(1/2) = v(0) + a(0) dt/2; afterwards the
+    leapfrog keeps velocities at half steps, so the states part."""
+    out = {}
+    for integ in (0, 1):
+        d = oracle_domain()
+        d.set("integrator", integ)
+        case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_top=-5.0)
+        d.prepare(case.dt)
+        d.step(1)
+        x1 = d.get_array("x")
+        d.step(10)
+        out[integ] = (x1, d.get_array("x"), d.get_array("v"))
+        d.close()
+    assert rel_l2(out[1][0], out[0][0]) <= 1e-15  # x(1) = x(0) + dt v(1/2) in both
+    assert rel_l2(out[1][2], out[0][2]) > 1e-6    # v(n+1/2) against v(n+1)

@@ -85,6 +85,7 @@ _SIGS = {
     "set_mesh_velocity": [_P, _I, _DP, _DP],
     "get_contact_force": [_P, _I, _DP],
     "solve_kickdrift": [_P, _D, _D, _D, _I64],
+    "solve_leapfrog": [_P, _D, _D, _D, _I64],
     "prepare_kickdrift": [_P, _D],
     "step": [_P, _I64],
     "neighbour_search": [_P],
@@ -272,6 +273,9 @@ class Domain:
 
     def SolveDiffUpdateKickDrift(self, tf: float, dt: float, dtOut: float, TheFileKey=None, maxidx: int = 1000000):
         self._call("solve_kickdrift", self._h, float(tf), float(dt), float(dtOut), int(maxidx))
+
+    def SolveDiffUpdateLeapFrog(self, tf: float, dt: float, dtOut: float, TheFileKey=None, maxidx: int = 1000000):
+        self._call("solve_leapfrog", self._h, float(tf), float(dt), float(dtOut), int(maxidx))
 
     def neighbour_search(self):
         self._call("neighbour_search", self._h)

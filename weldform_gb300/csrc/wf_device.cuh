@@ -162,6 +162,7 @@ struct DomainConst {
   int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
   int gblock;          // thread-block size of the mixed form's gather kernels
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
+  int leapfrog;        // 1: SolveDiffUpdateLeapFrog's update (velocities at half steps)
 };
 
 // Device pointers, passed by value to every kernel.

@@ -126,6 +126,7 @@ struct wf_domain {
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int ts_nb_inc = 5, pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1, contact_alg = 0;
   int precision = WF_PRECISION_FP64, use_graph = 1, device = 0;
+  int integrator = 0;  // 0 kick-drift, 1 leapfrog
   int solid_part_count = -1;
 
   HostParticles hp;
@@ -552,6 +553,7 @@ struct wf_domain {
     for (int p = 0; p < N; ++p) tm += F(C_MASS, p);
     K.totmass_mean = tm / N;
     K.id_free_surf = -999999;
+    K.leapfrog = integrator;
     K.ti = 0;
     for (int p = 0; p < N; ++p)
       if (hp.i[I_KIND][p] == 0 && F(C_TI, p) > 0.0) K.ti = 1;
@@ -786,6 +788,7 @@ struct wf_domain {
     if (precision != WF_PRECISION_FP64)
       throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint runs on the plain FP64 form (precision 0)"};
     if (K.ti) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: tensile instability (TI > 0) is not supported"};
+    if (K.leapfrog) throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint differentiates the kick-drift step"};
     if (!contact || mesh < 0 || mesh >= (int)meshes.size())
       throw CudaError{WF_ERR_ARG, "the reaction-force loss needs a rigid mesh"};
     if (axis < 0 || axis > 2 || every < 1 || kchk < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps ||
@@ -1139,6 +1142,10 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   else if (n == "contact") d->contact = v;
   else if (n == "contact_mesh_auto_update") d->contact_mesh_auto_update = v;
   else if (n == "contact_alg") { if (v < 0 || v > 2) return set_err(WF_ERR_ARG, "contact_alg"); d->contact_alg = v; }
+  else if (n == "integrator") {  // 0 SolveDiffUpdateKickDrift, 1 SolveDiffUpdateLeapFrog
+    if (v != 0 && v != 1) return set_err(WF_ERR_ARG, "integrator must be 0 (kick-drift) or 1 (leapfrog)");
+    d->integrator = v;
+  }
   else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
   else if (n == "GradientType") { if (v) return set_err(WF_ERR_UNSUPPORTED, "only GradientType 0 is supported"); }
@@ -1444,6 +1451,12 @@ int wf_solve_kickdrift(wf_domain* d, double tf, double dt, double dtOut, int64_t
     d->step(pending);
     return WF_OK;
   });
+}
+int wf_solve_leapfrog(wf_domain* d, double tf, double dt, double dtOut, int64_t maxidx) {
+  NEED(d);
+  if (d->prepared && d->integrator != 1) return set_err(WF_ERR_STATE, "the domain was prepared for kick-drift");
+  d->integrator = 1;
+  return wf_solve_kickdrift(d, tf, dt, dtOut, maxidx);
 }
 int wf_neighbour_search(wf_domain* d) {
   NEED(d);

@@ -314,7 +314,14 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
       colw(P, C_DCONT, N, i) = dcont;
       for (int d = 0; d < 3; ++d) colw(P, C_A + d, N, i) = a[d];
     }
-    if (kind == 0) {  // half kick v += a * 0.5 * dt (rigid-mesh particles have a = 0)
+    if (K.leapfrog) {  // first leapfrog step starts from v - a dt/2 (SolverLeapfrog.cpp:233-236)
+      if (P.st->isfirst)
+        for (int d = 0; d < 3; ++d) {
+          double vn = col(P, C_V + d, N, i) - a[d] * 0.5 * dt;
+          colw(P, C_V + d, N, i) = vn;
+          if (K.mixed) rec_set_v(P, N, i, d, vn, false);
+        }
+    } else if (kind == 0) {  // half kick v += a * 0.5 * dt (rigid-mesh particles have a = 0)
       for (int d = 0; d < 3; ++d) {
         double vn = col(P, C_V + d, N, i) + a[d] * 0.5 * dt;
         colw(P, C_V + d, N, i) = vn;
@@ -371,7 +378,21 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
     double du = v[d] * dt;
     colw(P, C_DISP + d, N, i) = col(P, C_DISP + d, N, i) + du;
     colw(P, C_XN + d, N, i) = x[d] + du;
-    colw(P, C_VN + d, N, i) = v[d] + col(P, C_A + d, N, i) * dt / 2.;
+    colw(P, C_VN + d, N, i) = K.leapfrog ? v[d] : v[d] + col(P, C_A + d, N, i) * dt / 2.;
+  }
+}
+
+// Leapfrog kick v(n+1/2) = v(n-1/2) + a (dt_prev + dt)/2 for every particle
+// (SolverLeapfrog.cpp:247-254; dt is fixed, so the factor is dt).
+__global__ void k_kick_leapfrog(DevPtrs P, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  size_t N = K.N;
+  double f = 0.5 * (K.dt + K.dt);
+  for (int d = 0; d < 3; ++d) {
+    double vn = col(P, C_V + d, N, i) + col(P, C_A + d, N, i) * f;
+    colw(P, C_V + d, N, i) = vn;
+    if (K.mixed) rec_set_v(P, N, i, d, vn, false);
   }
 }
 
@@ -711,6 +732,11 @@ void launch_bc(const DevPtrs& P, const DomainConst& K, int vcol, cudaStream_t s)
 void launch_contact_kick(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
   k_contact_kick<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
   mark(s, "k_contact_kick");
+  if (K.leapfrog) {  // GeneralAfter, then the full kick (the caller's next BC pass follows)
+    launch_bc(P, K, C_V, s);
+    k_kick_leapfrog<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+    mark(s, "k_kick_leapfrog");
+  }
 }
 void launch_step_tail(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
   k_finalize<<<NSLOTS, 1024, 0, s>>>(P, K);

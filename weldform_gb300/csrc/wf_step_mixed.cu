@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst
     double du = v * dt;
     colw(P, C_DISP + d, N, i) = col(P, C_DISP + d, N, i) + du;
     double xn = col(P, C_X + d, N, i) + du;
-    double vn = v + col(P, C_A + d, N, i) * dt / 2.;
+    double vn = K.leapfrog ? v : v + col(P, C_A + d, N, i) * dt / 2.;
     colw(P, C_XN + d, N, i) = xn;
     colw(P, C_VN + d, N, i) = vn;
     ff_split(xn, nxh[d], nxl[d]);
