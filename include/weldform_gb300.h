@@ -156,7 +156,10 @@ int wf_add_velocity_bc(wf_domain* d, int zone, const double value[3],
 
 /* Rigid plane contact surface: TriMesh::AxisPlaneMesh (Source/Mesh.cpp:82-203),
  * TriMesh::CalcSpheres (Mesh.cpp:206-220) and Domain::AddTrimeshParticles
- * (Source/Contact.cpp:10-38) in one call.  Returns the mesh index. */
+ * (Source/Contact.cpp:10-38) in one call.  Returns the mesh index.  zone_id
+ * may not be 1: the solver marks free-surface particles with id 1
+ * (CalculateSurface(1), SolverKickDrift.cpp:94), and a mesh with that id would
+ * pair surface particles with each other (WF_ERR_ARG). */
 int wf_add_rigid_plane(wf_domain* d, int axis, int positaxisorent, const double p1[3],
                        const double p2[3], int dens, double hfac, int zone_id,
                        int* mesh_id);

@@ -1562,6 +1562,7 @@ int wfo_add_velocity_bc(wfo_domain* p, int zone, const double value[3], const do
 int wfo_add_rigid_plane(wfo_domain* p, int axis, int posit, const double p1[3], const double p2[3], int dens,
                         double hfac, int zone_id, int* mesh_id) {
   if (dens <= 0 || axis < 0 || axis > 2) return set_err(WF_ERR_ARG, "bad plane arguments");
+  if (zone_id == 1) return set_err(WF_ERR_ARG, "zone id 1 marks the free surface (CalculateSurface(1))");
   int m = D(p)->add_plane(axis, posit != 0, v3(p1[0], p1[1], p1[2]), v3(p2[0], p2[1], p2[2]), dens, hfac, zone_id);
   if (mesh_id) *mesh_id = m;
   return WF_OK;

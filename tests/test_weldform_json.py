@@ -1,0 +1,150 @@
+"""WeldForm JSON front-end and WriteCSV output (weldform_gb300/weldform_json.py).
+
+The inputs below are written for these tests in the reference's input schema
+(Source/WeldForm.cpp:147-940).  CPU tests drive the oracle; the GPU test runs
+the same input on the library and compares with the oracle."""
+import copy
+import math
+import os
+
+import numpy as np
+import pytest
+
+from tests._support import gpu_domain, oracle_domain, rel_l2
+from weldform_gb300 import BILINEAR, WFError
+from weldform_gb300 import weldform_json as wj
+
+R, L, r = 0.003, 0.006, 0.00025
+E, nu, rho = 200e9, 0.3, 7850.0
+CS = math.sqrt(E / (3 * (1 - 2 * nu)) / rho)
+DT = 0.4 * (2 * r * 1.2) / CS
+
+COMPRESSION = {
+    "Configuration": {"Nproc": 4, "particleRadius": r, "hFactor": 1.2, "cflMethod": 1, "cflFactor": 0.4,
+                      "outTime": 5 * DT, "simTime": 20 * DT, "autoTS": [False, False, False],
+                      "solver": "Mech", "tensileInstability": 0.0},
+    "Materials": [{"type": "Bilinear", "density0": rho, "youngsModulus": E, "poissonsRatio": nu,
+                   "yieldStress0": 300e6, "const": [1.5e9]}],
+    "DomainBlocks": [{"type": "Cylinder", "zoneId": 0, "start": [0, 0, 0], "dim": [2 * R, 2 * R, L]}],
+    "DomainZones": [{"id": 2, "start": [-1, -1, -1], "end": [1, 1, 2 * r]},
+                    {"id": 3, "start": [-1, -1, L - 4 * r], "end": [1, 1, 1]}],
+    "BoundaryConditions": [{"zoneId": 2, "valueType": 0, "value": [0, 0, 0]},
+                           {"zoneId": 3, "valueType": 0, "value": [0, 0, -20.0]}],
+}
+
+CONTACT = {
+    "Configuration": {"particleRadius": r, "hFactor": 1.2, "cflMethod": 1, "cflFactor": 0.4,
+                      "outTime": 10 * DT, "simTime": 30 * DT, "autoTS": [False, False, False],
+                      "solver": "Mech-Thermal"},
+    "Materials": [{"type": "JohnsonCook", "density0": rho, "youngsModulus": E, "poissonsRatio": nu,
+                   "const": [350e6, 275e6, 0.36, 0.022, 1.0, 1.0, 1793.0, 300.0], "plasticHeat": True,
+                   "thermalCond": 50.0, "thermalHeatCap": 460.0}],
+    "DomainBlocks": [{"type": "Cylinder", "start": [0, 0, 0], "dim": [2 * R, 2 * R, L]}],
+    "DomainZones": [{"id": 2, "start": [-1, -1, -1], "end": [1, 1, 2 * r]}],
+    # the generator's top layer is at L - 3r (the z accumulation drops the last
+    # layer); the plane starts one smoothing length above it
+    "RigidBodies": [{"type": "Plane", "zoneId": 10, "start": [-R - 2 * r, -R - 2 * r, L - 3 * r + 2 * r * 1.2],
+                     "dim": [2 * R + 4 * r, 2 * R + 4 * r, 0], "partSide": 14}],
+    "Contact": [{"fricCoeffStatic": 0.2, "fricCoeffDynamic": 0.2}],
+    "Amplitudes": [{"id": 1, "time": [0.0, 10 * DT, 1.0], "value": [0.0, 1.0, 1.0]}],
+    "BoundaryConditions": [{"zoneId": 2, "valueType": 0, "value": [0, 0, 0]},
+                           {"zoneId": 10, "valueType": 1, "amplitudeId": 1, "amplitudeFactor": 1.0,
+                            "value": [0, 0, -10.0]}],
+    "InitialConditions": [{"Temp": 300.0, "zoneId": -1}],
+}
+
+
+def _oracle():
+    d = oracle_domain()
+    d.set("cpu_threads", min(os.cpu_count() or 1, 8))
+    return d
+
+
+def _read_csv(path):
+    lines = open(path).read().splitlines()
+    return lines[0], np.array([[float(v) for v in ln.split(", ")] for ln in lines[1:]])
+
+
+def test_csv_layout_and_output_schedule(tmp_path):
+    paths = wj.run(COMPRESSION, str(tmp_path), make=_oracle)
+    assert [os.path.basename(p) for p in paths][:2] == ["test06_0001.csv", "test06_0002.csv"]
+    assert 4 <= len(paths) <= 6          # t = dt, then every 5 dt up to 20 dt
+    head, rows = _read_csv(paths[-1])
+    assert head == wj.CSV_HEADER
+    assert rows.shape[1] == 17
+    d = _oracle()
+    d.AddCylinderLength(0, (0, 0, 0), R, L, r, rho, 2 * r * 1.2, False)
+    assert rows.shape[0] == d.particle_count
+    assert set(np.unique(rows[:, 3]).astype(int)) <= {0, 2, 3}
+
+
+def test_json_build_equals_the_api_build():
+    """The same case built by hand through the Domain API, as the driver
+    would (G, Cs, Ep, Sigmay, Alpha/Beta, TIInitDist, DomMax/DomMin quirk)."""
+    run = wj.build(COMPRESSION, make=_oracle)
+    a = run.dom
+    a.prepare(run.dt)
+    a.step(15)
+    b = _oracle()
+    b.set("integrator", 1)
+    b.Kernel_Set(0)
+    b.set_f64("DomMax.x", L)
+    b.set_f64("DomMin.x", -L)
+    b.AddCylinderLength(0, (0, 0, 0), R, L, r, rho, 2 * r * 1.2, False)
+    b.AssignZone((-1, -1, -1), (1, 1, 2 * r), 2)
+    b.AssignZone((-1, -1, L - 4 * r), (1, 1, 1), 3)
+    b.add_velocity_bc(2, (0, 0, 0))
+    b.add_velocity_bc(3, (0, 0, -20.0))
+    mid = b.add_material(BILINEAR, [E, nu])
+    b.set_particles("mat", mid)
+    b.set_particles("Ep", E * 1.5e9 / (E - 1.5e9))
+    b.set_particles("Sigmay", 300e6)
+    b.set_particles("G", E / (2 * (1 + nu)))
+    b.set_particles("Cs", CS)
+    b.set_particles("Fail", 1)
+    b.set_particles("Alpha", 1.0)
+    b.set_particles("Beta", 0.0)
+    b.set_particles("TIInitDist", 2 * r)
+    b.prepare(run.dt)
+    b.step(15)
+    for f in ("x", "v", "Sigma", "pl_strain"):
+        assert np.array_equal(a.get_array(f), b.get_array(f)), f
+
+
+def test_contact_thermal_input_runs_in_the_oracle(tmp_path):
+    paths = wj.run(CONTACT, str(tmp_path), make=_oracle)
+    head, rows = _read_csv(paths[-1])
+    assert np.abs(rows[:, 14]).max() > 0      # CZFz: contact force on surface particles
+    assert rows[:, 16].max() >= 300.0
+
+
+@pytest.mark.parametrize("patch", [
+    ("Configuration", "solver", "Mech-Fraser"),
+    ("Configuration", "autoTS", [True, False, False]),
+    ("Configuration", "kernelGradCorr", True),
+    ("Materials", "damageModel", "Rankine"),
+    ("DomainBlocks", "gridCoordSys", "AxiSymmetric"),
+])
+def test_unsupported_inputs_are_rejected(patch):
+    j = copy.deepcopy(COMPRESSION)
+    sec, key, val = patch
+    tgt = j[sec][0] if isinstance(j[sec], list) else j[sec]
+    tgt[key] = val
+    with pytest.raises(WFError) as e:
+        wj.build(j, make=_oracle)
+    assert e.value.code == 8
+
+
+@pytest.mark.gpu
+def test_json_run_on_the_gpu_matches_the_oracle(tmp_path):
+    out = {}
+    for name, make in (("gpu", gpu_domain), ("oracle", _oracle)):
+        paths = wj.run(CONTACT, str(tmp_path / name), make=make)
+        out[name] = [_read_csv(p)[1] for p in paths]
+    assert len(out["gpu"]) == len(out["oracle"])
+    for g, o in zip(out["gpu"], out["oracle"]):
+        assert g.shape == o.shape
+        cols = [0, 1, 2, 4, 5, 6, 7, 8, 14, 15, 16]  # x, Sigma_eq, pl, v, CZFz, p, T
+        assert np.array_equal(g[:, 3], o[:, 3])
+        for c in cols:
+            assert rel_l2(g[:, c], o[:, c]) <= 2e-6, c   # 6 printed digits

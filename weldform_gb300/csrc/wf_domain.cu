@@ -1398,6 +1398,7 @@ int wf_add_rigid_plane(wf_domain* d, int axis, int posit, const double p1[3], co
   NEED(d);
   if (d->prepared) return set_err(WF_ERR_STATE, "meshes are fixed after the prologue");
   if (dens <= 0 || axis < 0 || axis > 2) return set_err(WF_ERR_ARG, "bad plane arguments");
+  if (zone_id == 1) return set_err(WF_ERR_ARG, "zone id 1 marks the free surface (CalculateSurface(1))");
   if ((int)d->meshes.size() >= wf::MAX_MESHES) return set_err(WF_ERR_UNSUPPORTED, "too many rigid meshes");
   if (d->solid_part_count < 0) d->solid_part_count = d->hp.N;
   int m = d->add_plane(axis, posit != 0, p1, p2, dens, hfac, zone_id);
