@@ -78,6 +78,9 @@ int wf_domain_destroy(wf_domain* d);
  * "nonlock_sum", "pl_heating", "thermal_solver", "contact",
  * "contact_mesh_auto_update", "GradientType", "contact_alg" (WF_CONTACT_*),
  * "integrator" (0 kick-drift, 1 leapfrog; before the prologue),
+ * "gradKernelCorr" (kernel-gradient correction, Domain.cpp:1832-1940; plain
+ * FP64 form; the correction matrix is recomputed at the first step and, for
+ * the leapfrog solver, after every rebuild),
  * "precision" (WF_PRECISION_*), "device" (CUDA device ordinal, before the
  * prologue), "use_graph" (replay each step as one CUDA graph, default 1),
  * "cpu_threads" (unused on the GPU path). */

@@ -242,6 +242,7 @@ struct Domain {
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int mode = 0;       // 0 canonical, 1 reference-structured
   int integrator = 0; // 0 kick-drift (SolverKickDrift.cpp), 1 leapfrog (SolverLeapfrog.cpp)
+  int grad_corr = 0;  // Domain::gradKernelCorr (Domain.cpp:130; forces the locking sums, SolverKickDrift.cpp:107-110)
   int nthreads = 1;
 
   // particles (SoA, original order)
@@ -250,7 +251,7 @@ struct Domain {
   std::vector<double> rho, rho0, mass, h, Cs, P0, G, pressure, pl_strain, delta_pl_strain, sigmay, Ep,
       eff_strain_rate, T, dTdt, k_T, cp_T, th_exp, q_plheat, q_conv, q_source, q_cont_conv, ps_energy, alpha,
       beta, TI, TIn, TIInitDist, dDensity, cont_stiff, delta_cont, dkin, dint;
-  std::vector<M3> sigma, tau, srate, rrate, strain, strain_pl, strain_pl_incr, TIR;
+  std::vector<M3> sigma, tau, srate, rrate, strain, strain_pl, strain_pl_incr, TIR, gcm;
   std::vector<int> ID, ID_orig, not_write_surf, is_free, material_idx, mat, model, fail_crit, pres_eq, Nb, mesh_of, elem_of;
 
   std::vector<Material> materials;
@@ -306,6 +307,7 @@ struct Domain {
     dkin.push_back(0); dint.push_back(0);
     sigma.push_back(zero3()); tau.push_back(zero3()); srate.push_back(zero3()); rrate.push_back(zero3());
     strain.push_back(zero3()); strain_pl.push_back(zero3()); strain_pl_incr.push_back(zero3()); TIR.push_back(zero3());
+    { M3 I = zero3(); at(I, 0, 0) = at(I, 1, 1) = at(I, 2, 2) = 1.0; gcm.push_back(I); }
     ID.push_back(tag); ID_orig.push_back(tag); not_write_surf.push_back(0); is_free.push_back(fixed ? 0 : 1);
     material_idx.push_back(0); mat.push_back(-1); model.push_back(0); fail_crit.push_back(0); pres_eq.push_back(0);
     Nb.push_back(0); mesh_of.push_back(-1); elem_of.push_back(-1);
@@ -665,6 +667,55 @@ struct Domain {
         ipair[i]++; jpair[j]++;
       }
   }
+  // Domain::CalcGradCorrMatrix (Domain.cpp:1832-1940): per particle
+  // M_i = -sum_j (m_j/rho_j) (GK x_ij) (x) x_ij over its neighbours (canonical
+  // row order), then gradCorrM_i = InvLog(M_i), the identity where the
+  // determinant is below 1e-10 (matvec.h:673-693).
+  void calc_grad_corr() {
+    int mx = contact ? first_fem[0] : N;
+    for (int i = 0; i < mx; i++) {
+      M3 t = zero3();
+      for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
+        int j = nb_idx[k];
+        int P1 = std::min(i, j), P2 = std::max(i, j);
+        V3 xij = sub(x[P1], x[P2]);
+        double hh = (h[P1] + h[P2]) / 2.0;
+        double GK = grad_kernel(dim, norm(xij) / hh, hh);
+        V3 g = scl(GK, xij);
+        double f = mass[j] / rho[j];
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) at(t, a, b) = at(t, a, b) - f * (g.c[a] * xij.c[b]);
+      }
+      double det = at(t, 0, 0) * (at(t, 1, 1) * at(t, 2, 2) - at(t, 1, 2) * at(t, 2, 1)) -
+                   at(t, 0, 1) * (at(t, 1, 0) * at(t, 2, 2) - at(t, 1, 2) * at(t, 2, 0)) +
+                   at(t, 0, 2) * (at(t, 1, 0) * at(t, 2, 1) - at(t, 1, 1) * at(t, 2, 0));
+      M3 m;
+      if (std::fabs(det) < 1.0e-10) {
+        m = zero3(); at(m, 0, 0) = at(m, 1, 1) = at(m, 2, 2) = 1.0;
+      } else {
+        at(m, 0, 0) = (at(t, 1, 1) * at(t, 2, 2) - at(t, 1, 2) * at(t, 2, 1)) / det;
+        at(m, 0, 1) = (at(t, 0, 2) * at(t, 2, 1) - at(t, 0, 1) * at(t, 2, 2)) / det;
+        at(m, 0, 2) = (at(t, 0, 1) * at(t, 1, 2) - at(t, 0, 2) * at(t, 1, 1)) / det;
+        at(m, 1, 0) = (at(t, 1, 2) * at(t, 2, 0) - at(t, 1, 0) * at(t, 2, 2)) / det;
+        at(m, 1, 1) = (at(t, 0, 0) * at(t, 2, 2) - at(t, 0, 2) * at(t, 2, 0)) / det;
+        at(m, 1, 2) = (at(t, 0, 2) * at(t, 1, 0) - at(t, 0, 0) * at(t, 1, 2)) / det;
+        at(m, 2, 0) = (at(t, 1, 0) * at(t, 2, 1) - at(t, 1, 1) * at(t, 2, 0)) / det;
+        at(m, 2, 1) = (at(t, 0, 1) * at(t, 2, 0) - at(t, 0, 0) * at(t, 2, 1)) / det;
+        at(m, 2, 2) = (at(t, 0, 0) * at(t, 1, 1) - at(t, 0, 1) * at(t, 1, 0)) / det;
+      }
+      gcm[i] = m;
+    }
+  }
+  // Corrected kernel gradient of end e of the pair (P1, P2):
+  // Mult(GK * gradCorrM_e, x12) (InteractionAlt.cpp:114-132).
+  V3 corr_grad(int e, double GK, const V3& x12) const {
+    M3 G;
+    for (int k = 0; k < 9; ++k) G.m[k] = GK * gcm[e].m[k];
+    V3 r;
+    for (int k = 0; k < 3; ++k) r.c[k] = x12.c[0] * at(G, k, 0) + x12.c[1] * at(G, k, 1) + x12.c[2] * at(G, k, 2);
+    return r;
+  }
+
   int neighbour_search() {
     if (!cells_ready) return set_err(WF_ERR_STATE, "neighbour search before the solver prologue");
     search_linked_list();
@@ -764,7 +815,7 @@ struct Domain {
 
   // -------------------------------------------------------------- pair terms
   // InteractionAlt.cpp:35-197, pair (P1, P2) as the Nishimura path orders them.
-  V3 pair_accel(int P1, int P2) const {
+  V3 pair_accel(int P1, int P2, int corr_end = -1) const {
     double hh = (h[P1] + h[P2]) / 2;
     V3 xij = sub(x[P1], x[P2]);
     double rij = norm(xij);
@@ -796,6 +847,7 @@ struct Domain {
         if (has_ti) s = s + fti * (at(TIR[P1], k, l) + at(TIR[P2], k, l));
         at(S, k, l) = s;
       }
+    if (corr_end >= 0) return vecmat(corr_grad(corr_end, GK, xij), S);  // temp_c (InteractionAlt.cpp:166-170)
     return vecmat(scl(GK, xij), S);
   }
   // InteractionAlt.cpp:505-565
@@ -836,12 +888,19 @@ struct Domain {
     for (int k = 0; k < 9; ++k) RR.m[k] = f * RR.m[k];
   }
   // Thermal.cpp:72-131 conduction pair term for (P1, P2)
-  double pair_conduction(int P1, int P2) const {
+  double pair_conduction(int P1, int P2, int corr_end = -1) const {
     V3 xij = sub(x[P1], x[P2]);
     double hh = (h[P1] + h[P2]) / 2.0;
     double GK = grad_kernel(dim, norm(xij) / hh, hh);
     double mj = mass[P2], dj = rho[P2];
-    return mj / dj * 4. * (k_T[P1] * k_T[P2]) / (k_T[P1] + k_T[P2]) * (T[P1] - T[P2]) * dot(xij, scl(GK, xij)) /
+    V3 g = scl(GK, xij);
+    if (corr_end >= 0) {  // Mult(gradCorrM_e, GK x12) (Thermal.cpp:90-107)
+      const M3& M = gcm[corr_end];
+      V3 c;
+      for (int k = 0; k < 3; ++k) c.c[k] = g.c[0] * at(M, k, 0) + g.c[1] * at(M, k, 1) + g.c[2] * at(M, k, 2);
+      g = c;
+    }
+    return mj / dj * 4. * (k_T[P1] * k_T[P2]) / (k_T[P1] + k_T[P2]) * (T[P1] - T[P2]) * dot(xij, g) /
            (norm(xij) * norm(xij));
   }
   // Domain.cpp:1775-1790 kinetic-energy pair term for (P1, P2)
@@ -881,10 +940,11 @@ struct Domain {
     for (int i = 0; i < ns; i++) {
       if (is_mesh(i)) continue;
       V3 ai = v3(0, 0, 0);
+      int ce = grad_corr ? i : -1;  // the locking sum's corrected gradient of this end
       for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
         int j = nb_idx[k];
-        if (j > i) ai = add(ai, scl(mass[j], pair_accel(i, j)));
-        else ai = sub(ai, scl(mass[j], pair_accel(j, i)));
+        if (j > i) ai = add(ai, scl(mass[j], pair_accel(i, j, ce)));
+        else ai = sub(ai, scl(mass[j], pair_accel(j, i, ce)));
       }
       a[i] = ai;
     }
@@ -918,6 +978,19 @@ struct Domain {
     for (int i = 0; i < ns; i++) {
       if (is_mesh(i)) continue;
       double dd = 0.;
+      if (grad_corr) {  // locking form: += m_j (rho_i / rho_j) v12 . Mult(GK M_i, x12) (InteractionAlt.cpp:589-605)
+        for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
+          int j = nb_idx[k];
+          int P1 = std::min(i, j), P2 = std::max(i, j);
+          double hh = (h[P1] + h[P2]) / 2;
+          V3 xij = sub(x[P1], x[P2]);
+          double GK = grad_kernel(dim, norm(xij) / hh, hh);
+          double t1 = dot(sub(v[P1], v[P2]), corr_grad(i, GK, xij));
+          dd += mass[j] * (rho[i] / rho[j]) * t1;
+        }
+        dDensity[i] = dd;
+        continue;
+      }
       for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
         int j = nb_idx[k];
         double pd = (j > i) ? this->pair_densinc(i, j) : this->pair_densinc(j, i);
@@ -955,6 +1028,25 @@ struct Domain {
     for (int i = 0; i < ns; i++) {
       if (is_mesh(i)) continue;
       M3& SRi = srate[i]; M3& RRi = rrate[i];
+      if (grad_corr) {  // locking form with corrected gradients (InteractionAlt.cpp:330-350, 425-450)
+        for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
+          int j = nb_idx[k];
+          int P1 = std::min(i, j), P2 = std::max(i, j);
+          double hh = (h[P1] + h[P2]) / 2;
+          V3 xij = sub(x[P1], x[P2]);
+          double GK = grad_kernel(dim, norm(xij) / hh, hh);
+          V3 vab = sub(v[P1], v[P2]);
+          V3 gk = corr_grad(i, GK, xij);
+          float mj_dj = mass[j] / rho[j];
+          for (int a2 = 0; a2 < 3; ++a2)
+            for (int b2 = 0; b2 < 3; ++b2) {
+              double g = vab.c[a2] * gk.c[b2], gt = vab.c[b2] * gk.c[a2];
+              at(SRi, a2, b2) = at(SRi, a2, b2) + mj_dj * (-0.5 * (g + gt));
+              at(RRi, a2, b2) = at(RRi, a2, b2) + mj_dj * (-0.5 * (g - gt));
+            }
+        }
+        continue;
+      }
       for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
         int j = nb_idx[k];
         M3 SR, RR;
@@ -1052,7 +1144,8 @@ struct Domain {
       double s = 0.;
       for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
         int j = nb_idx[k];
-        if (j > i) s += pair_conduction(i, j); else s -= pair_conduction(j, i);
+        int ce = grad_corr ? i : -1;
+        if (j > i) s += pair_conduction(i, j, ce); else s -= pair_conduction(j, i, ce);
       }
       tmp[i] = s;
     }
@@ -1177,6 +1270,8 @@ struct Domain {
   int prepare(double dt) {  // SolverKickDrift.cpp:23-115
     if (N == 0) return set_err(WF_ERR_STATE, "no particles");
     if (dim != 3) return set_err(WF_ERR_UNSUPPORTED, "only Dimension = 3 is supported");
+    if (grad_corr && mode == 1)
+      return set_err(WF_ERR_UNSUPPORTED, "kernel-gradient correction runs the locking sums (cpu_mode 0)");
     for (int i = 0; i < N; ++i) {
       if (!is_free[i]) return set_err(WF_ERR_UNSUPPORTED, "fixed (non-free) particles are not supported");
       if (pres_eq[i] != 0) return set_err(WF_ERR_UNSUPPORTED, "only PresEq = 0 is supported");
@@ -1243,11 +1338,17 @@ struct Domain {
       if (contact && (rc = contact_nb_update())) return rc;
       isyielding = true;
     }
+    bool regular = false;
     if (mx > MIN_PS_FOR_NBSEARCH || isfirst || check_nb_every_time)
       if (ts_i == 0 && nb_cleared) {
         if ((rc = neighbour_search())) return rc;
         if (contact && (rc = contact_nb_update())) return rc;
+        regular = true;
       }
+    // CalcGradCorrMatrix: the kick-drift solver at its first step only
+    // (SolverKickDrift.cpp:189-191); the leapfrog solver after every regular
+    // search and at the first step (SolverLeapfrog.cpp:186-204).
+    if (grad_corr && (isfirst || (integrator == 1 && regular))) calc_grad_corr();
     return WF_OK;
   }
   // The rest of the step (force passes, kicks, drift, stress, thermal, bookkeeping).
@@ -1364,6 +1465,7 @@ std::vector<M3>* m3_field(Domain* d, const std::string& f) {
   if (f == "Strain") return &d->strain;
   if (f == "Strain_pl") return &d->strain_pl;
   if (f == "TIR") return &d->TIR;
+  if (f == "gradCorrM") return &d->gcm;
   return nullptr;
 }
 std::vector<int>* i32_field(Domain* d, const std::string& f) {
@@ -1420,6 +1522,7 @@ int wfo_set_domain_i32(wfo_domain* p, const char* name, int v) {
   else if (n == "contact_alg") d->contact_alg = v;
   else if (n == "cpu_mode") d->mode = v;
   else if (n == "integrator") d->integrator = v;
+  else if (n == "gradKernelCorr") d->grad_corr = v;
   else if (n == "cpu_threads" || n == "Nproc") d->nthreads = v > 0 ? v : 1;
   else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
@@ -1664,6 +1767,7 @@ int wfo_adjoint_reaction_loss(wfo_domain* p, int64_t steps, int every, int mesh,
   if (!d->prepared) return set_err(WF_ERR_STATE, "adjoint before wf_prepare_kickdrift");
   if (d->mode != 0) return set_err(WF_ERR_UNSUPPORTED, "the tangent run needs cpu_mode 0");
   if (d->integrator != 0) return set_err(WF_ERR_UNSUPPORTED, "the adjoint differentiates the kick-drift step");
+  if (d->grad_corr) return set_err(WF_ERR_UNSUPPORTED, "adjoint: kernel-gradient correction is not supported");
   if (!d->contact || mesh < 0 || mesh >= (int)d->meshes.size())
     return set_err(WF_ERR_ARG, "the reaction-force loss needs a rigid mesh");
   if (axis < 0 || axis > 2 || every < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps || !target || !loss ||

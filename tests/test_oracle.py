@@ -108,3 +108,29 @@ def test_leapfrog_first_step_matches_kickdrift_half_kick():
         d.close()
     assert rel_l2(out[1][0], out[0][0]) <= 1e-15  # x(1) = x(0) + dt v(1/2) in both
     assert rel_l2(out[1][2], out[0][2]) > 1e-6    # v(n+1/2) against v(n+1)
+
+
+def test_kernel_gradient_correction_matrix():
+    """CalcGradCorrMatrix (Domain.cpp:1832-1940): isotropic (c I, the same c)
+    for interior particles of a regular lattice — at h = 1.2 dx the discrete
+    first moment -sum_j V_j grad W_ij (x) x_ij is 1.376 I, so c = 0.727 —
+    and anisotropic where the free surface truncates the neighbourhood; the
+    corrected step differs from the uncorrected one."""
+    out = {}
+    for corr in (0, 1):
+        d = oracle_domain()
+        d.set("gradKernelCorr", corr)
+        case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_top=-5.0, jitter_amp=0.0)
+        d.prepare(case.dt)
+        d.step(5)
+        out[corr] = (d.get_array("gradCorrM").reshape(-1, 3, 3), d.get_array("Nb"), d.get_array("x"))
+        d.close()
+    M, nb, _ = out[1]
+    c = M[:, 0, 0]
+    aniso = np.abs(M - c[:, None, None] * np.eye(3)).max(axis=(1, 2)) / np.abs(c)
+    full = nb == nb.max()
+    assert aniso[full].max() < 1e-12 and np.ptp(c[full]) < 1e-12 * abs(c[full][0])
+    assert 0.6 < c[full][0] < 0.8
+    assert aniso[nb < 0.6 * nb.max()].min() > 0.05
+    assert np.array_equal(out[0][0], np.broadcast_to(np.eye(3), out[0][0].shape))
+    assert rel_l2(out[1][2], out[0][2]) > 1e-12

@@ -121,7 +121,6 @@ def test_contact_thermal_input_runs_in_the_oracle(tmp_path):
 @pytest.mark.parametrize("patch", [
     ("Configuration", "solver", "Mech-Fraser"),
     ("Configuration", "autoTS", [True, False, False]),
-    ("Configuration", "kernelGradCorr", True),
     ("Materials", "damageModel", "Rankine"),
     ("DomainBlocks", "gridCoordSys", "AxiSymmetric"),
 ])

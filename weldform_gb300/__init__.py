@@ -39,7 +39,7 @@ PARAMS = ("E", "sy0", "Ep", "A", "B", "n", "C", "m", "mu", "PFAC")
 _ERRNAMES = {1: "WF_ERR_ARG", 2: "WF_ERR_CUDA", 3: "WF_ERR_NAN", 4: "WF_ERR_NBR_OVERFLOW", 5: "WF_ERR_TIMEOUT",
              6: "WF_ERR_STATE", 7: "WF_ERR_NOMEM", 8: "WF_ERR_UNSUPPORTED"}
 
-TENSOR_FIELDS = ("Sigma", "ShearStress", "StrainRate", "RotationRate", "Strain", "Strain_pl", "Strain_pl_incr", "TIR")
+TENSOR_FIELDS = ("Sigma", "ShearStress", "StrainRate", "RotationRate", "Strain", "Strain_pl", "Strain_pl_incr", "TIR", "gradCorrM")
 VECTOR_FIELDS = ("x", "v", "a", "Displacement", "normal", "contforce")
 
 

@@ -36,11 +36,12 @@ enum F64Col : int {
   C_MRHO = 90,             // Mass / Density
   C_PR2 = 91,              // Pressure / Density^2
   C_TI = 92, C_TIN, C_TIDIST,  // tensile instability: TI, TIn, TIInitDist (Particle.h:146-149)
-  NF64_PERSIST = 95,
+  C_GCM = 95,              // kernel-gradient correction matrix gradCorrM (9, row-major)
+  NF64_PERSIST = 104,
   // scratch columns (not permuted): next-step buffers and the
   // tensile-instability stress TIR (6), recomputed at every step start
-  C_XN = 95, C_VN = 98, C_RHON = 101, C_MRHON = 102, C_TIR = 103,
-  NF64 = 109
+  C_XN = 104, C_VN = 107, C_RHON = 110, C_MRHON = 111, C_TIR = 112,
+  NF64 = 118
 };
 enum I32Col : int {
   I_ID = 0, I_IDORIG, I_NWS, I_MAT, I_MODEL, I_FAIL, I_MATERIAL, I_NB, I_KIND, I_ELEM, I_MESH, I_ORIG,
@@ -140,6 +141,7 @@ struct StepState {
   unsigned long long pair_count, contact_pair_count;
   int isfirst, isyielding, ts_i, nb_cleared;
   int do_search;       // set by the schedule kernel for the current step
+  int do_gradcorr;     // recompute the kernel-gradient correction this step
   int errors;
   int surface_count;
 };
@@ -163,6 +165,7 @@ struct DomainConst {
   int gblock;          // thread-block size of the mixed form's gather kernels
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
   int leapfrog;        // 1: SolveDiffUpdateLeapFrog's update (velocities at half steps)
+  int gradcorr;        // 1: kernel-gradient correction (Domain::gradKernelCorr)
 };
 
 // Device pointers, passed by value to every kernel.

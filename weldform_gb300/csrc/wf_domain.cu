@@ -79,7 +79,7 @@ int col_f64(const std::string& n, int* ncomp) {
       {"q_plheat", C_QPL, 1}, {"q_source", C_QSRC, 1}, {"Alpha", C_ALPHA, 1}, {"Beta", C_BETA, 1},
       {"ps_energy", C_PSEN, 1}, {"delta_cont", C_DCONT, 1}, {"dkin_energy_dt", C_DKIN, 1},
       {"dint_energy_dt", C_DINT, 1}, {"dDensity", C_DRHO, 1}, {"TI", C_TI, 1}, {"TIn", C_TIN, 1},
-      {"TIInitDist", C_TIDIST, 1}, {"TIR", C_TIR, 6}, {"Sigma", C_SIG, 6}, {"ShearStress", C_TAU, 6},
+      {"TIInitDist", C_TIDIST, 1}, {"TIR", C_TIR, 6}, {"gradCorrM", C_GCM, 9}, {"Sigma", C_SIG, 6}, {"ShearStress", C_TAU, 6},
       {"Strain", C_EPS, 6}, {"Strain_pl", C_EPL, 6}, {"Strain_pl_incr", C_EPLI, 6}, {"StrainRate", C_SR, 6},
       {"RotationRate", C_RR, 3}};
   for (const E& e : tab)
@@ -127,6 +127,7 @@ struct wf_domain {
   int ts_nb_inc = 5, pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1, contact_alg = 0;
   int precision = WF_PRECISION_FP64, use_graph = 1, device = 0;
   int integrator = 0;  // 0 kick-drift, 1 leapfrog
+  int grad_corr = 0;   // Domain::gradKernelCorr
   int solid_part_count = -1;
 
   HostParticles hp;
@@ -189,6 +190,7 @@ struct wf_domain {
     hp.i[I_ID][p] = tag; hp.i[I_IDORIG][p] = tag; hp.i[I_MAT][p] = -1; hp.i[I_KIND][p] = kind;
     hp.i[I_ELEM][p] = -1; hp.i[I_MESH][p] = -1; hp.i[I_ORIG][p] = p;
     hp.f[C_TIN][p] = 4.0;  // Particle.cpp:47
+    hp.f[C_GCM][p] = hp.f[C_GCM + 4][p] = hp.f[C_GCM + 8][p] = 1.0;  // gradCorrM = I
   }
   double& F(int c, int p) { return hp.f[c][p]; }
 
@@ -554,6 +556,7 @@ struct wf_domain {
     K.totmass_mean = tm / N;
     K.id_free_surf = -999999;
     K.leapfrog = integrator;
+    K.gradcorr = grad_corr;
     K.ti = 0;
     for (int p = 0; p < N; ++p)
       if (hp.i[I_KIND][p] == 0 && F(C_TI, p) > 0.0) K.ti = 1;
@@ -611,6 +614,8 @@ struct wf_domain {
   }
 
   void launch_one_step() {
+    if (K.gradcorr && precision == WF_PRECISION_MIXED)
+      throw CudaError{WF_ERR_UNSUPPORTED, "kernel-gradient correction runs in the plain FP64 form"};
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
     k.gblock = gblock;
@@ -789,6 +794,7 @@ struct wf_domain {
       throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint runs on the plain FP64 form (precision 0)"};
     if (K.ti) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: tensile instability (TI > 0) is not supported"};
     if (K.leapfrog) throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint differentiates the kick-drift step"};
+    if (K.gradcorr) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: kernel-gradient correction is not supported"};
     if (!contact || mesh < 0 || mesh >= (int)meshes.size())
       throw CudaError{WF_ERR_ARG, "the reaction-force loss needs a rigid mesh"};
     if (axis < 0 || axis > 2 || every < 1 || kchk < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps ||
@@ -1146,6 +1152,7 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     if (v != 0 && v != 1) return set_err(WF_ERR_ARG, "integrator must be 0 (kick-drift) or 1 (leapfrog)");
     d->integrator = v;
   }
+  else if (n == "gradKernelCorr") d->grad_corr = v != 0;
   else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
   else if (n == "GradientType") { if (v) return set_err(WF_ERR_UNSUPPORTED, "only GradientType 0 is supported"); }

@@ -40,15 +40,19 @@ __global__ void k_schedule(DevPtrs P, DomainConst K) {
   StepState* s = P.st;
   double mx = s->max_pl_next;
   s->max_pl = mx;
-  int search = 0;
+  int search = 0, regular = 0;
   if (mx > MIN_PS_FOR_NBSEARCH && !s->isyielding) {  // first yield
     search = 1;
     s->isyielding = 1;
   } else if ((mx > MIN_PS_FOR_NBSEARCH || s->isfirst) && s->ts_i == 0 && s->nb_cleared) {
     search = 1;
+    regular = 1;
   }
   if (search) s->nb_cleared = 0;
   s->do_search = search;
+  // CalcGradCorrMatrix: kick-drift at its first step (SolverKickDrift.cpp:189-191),
+  // leapfrog after every regular search and at the first step (SolverLeapfrog.cpp:186-204)
+  s->do_gradcorr = K.gradcorr && (s->isfirst || (K.leapfrog && regular));
 }
 
 __global__ void k_step_end(DevPtrs P, DomainConst K) {
@@ -124,6 +128,49 @@ __global__ void k_tensile(DevPtrs P, DomainConst K) {
   }
 }
 
+// ---------------------------------------------------------------- kernel-gradient correction
+// Domain::CalcGradCorrMatrix (Domain.cpp:1832-1940): M_i = -sum_j (m_j/rho_j)
+// (GK x_ij) (x) x_ij over the particle's row, gradCorrM = InvLog(M_i)
+// (matvec.h:673-693; the identity when |det| < 1e-10).  The dyad is even in
+// x_ij, so each end's own x_i - x_j gives the reference's value.
+__global__ void k_grad_corr(DevPtrs P, DomainConst K) {
+  if (!P.st->do_gradcorr) return;
+  size_t N = K.N;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
+    if (icol(P, I_KIND, N, i) != 0) continue;
+    double xi0 = col(P, C_X, N, i), xi1 = col(P, C_X + 1, N, i), xi2 = col(P, C_X + 2, N, i), hi = col(P, C_H, N, i);
+    double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int len = P.row_len[i];
+    for (int k = 0; k < len; ++k) {
+      int j = P.nbr[(size_t)k * N + i];
+      PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+                           col(P, C_H, N, j));
+      double gv[3] = {g.GK * g.x0, g.GK * g.x1, g.GK * g.x2}, xv[3] = {g.x0, g.x1, g.x2};
+      double f = col(P, C_MASS, N, j) / col(P, C_RHO, N, j);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) t[3 * a + b] = t[3 * a + b] - f * (gv[a] * xv[b]);
+    }
+    double det = t[0] * (t[4] * t[8] - t[5] * t[7]) - t[1] * (t[3] * t[8] - t[5] * t[6]) +
+                 t[2] * (t[3] * t[7] - t[4] * t[6]);
+    double m[9];
+    if (fabs(det) < 1.0e-10) {
+      for (int c = 0; c < 9; ++c) m[c] = (c % 4 == 0) ? 1.0 : 0.0;
+    } else {
+      m[0] = (t[4] * t[8] - t[5] * t[7]) / det; m[1] = (t[2] * t[7] - t[1] * t[8]) / det; m[2] = (t[1] * t[5] - t[2] * t[4]) / det;
+      m[3] = (t[5] * t[6] - t[3] * t[8]) / det; m[4] = (t[0] * t[8] - t[2] * t[6]) / det; m[5] = (t[2] * t[3] - t[0] * t[5]) / det;
+      m[6] = (t[3] * t[7] - t[4] * t[6]) / det; m[7] = (t[1] * t[6] - t[0] * t[7]) / det; m[8] = (t[0] * t[4] - t[1] * t[3]) / det;
+    }
+    for (int c = 0; c < 9; ++c) colw(P, C_GCM + c, N, i) = m[c];
+  }
+}
+// Corrected gradient Mult(GK * gradCorrM_i, x) (InteractionAlt.cpp:114-132).
+__device__ __forceinline__ void corr_grad(const DevPtrs& P, size_t N, int i, double GK, double x0, double x1,
+                                          double x2, double out[3]) {
+  for (int k = 0; k < 3; ++k)
+    out[k] = x0 * (GK * col(P, C_GCM + 3 * k, N, i)) + x1 * (GK * col(P, C_GCM + 3 * k + 1, N, i)) +
+             x2 * (GK * col(P, C_GCM + 3 * k + 2, N, i));
+}
+
 // ---------------------------------------------------------------- accel
 __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -175,6 +222,11 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
       S5 = S5 + f * (col(P, C_TIR + 5, N, i) + col(P, C_TIR + 5, N, j));
     }
     double g0 = g.GK * g.x0, g1 = g.GK * g.x1, g2 = g.GK * g.x2;
+    if (K.gradcorr) {  // temp_c = Mult(vc_i, S) of the locking sum (InteractionAlt.cpp:166-170)
+      double vc[3];
+      corr_grad(P, N, i, g.GK, g.x0, g.x1, g.x2, vc);
+      g0 = vc[0]; g1 = vc[1]; g2 = vc[2];
+    }
     double t0 = g0 * S0 + g1 * S3 + g2 * S4;
     double t1 = g0 * S3 + g1 * S1 + g2 * S5;
     double t2 = g0 * S4 + g1 * S5 + g2 * S2;
@@ -364,10 +416,17 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
       PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                            col(P, C_H, N, j));
       double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
+      if (K.gradcorr) {  // locking form m_j (rho_i/rho_j) v_ij . vc_i (InteractionAlt.cpp:589-605)
+        double vc[3];
+        corr_grad(P, N, i, g.GK, g.x0, g.x1, g.x2, vc);
+        double t1 = v0 * vc[0] + v1 * vc[1] + v2 * vc[2];
+        dd += col(P, C_MASS, N, j) * (rhoi / col(P, C_RHO, N, j)) * t1;
+        continue;
+      }
       double pd = v0 * (g.GK * g.x0) + v1 * (g.GK * g.x1) + v2 * (g.GK * g.x2);
       dd += col(P, C_MRHO, N, j) * pd;
     }
-    dd *= rhoi;
+    if (!K.gradcorr) dd *= rhoi;
   }
   colw(P, C_DRHO, N, i) = dd;
   double rn = rhoi + dt * dd;
@@ -421,6 +480,21 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
         PairGeo g = pair_geo(x[0], x[1], x[2], hi, col(P, C_XN, N, j), col(P, C_XN + 1, N, j), col(P, C_XN + 2, N, j),
                              col(P, C_H, N, j));
         double b0 = v[0] - col(P, C_VN, N, j), b1 = v[1] - col(P, C_VN + 1, N, j), b2 = v[2] - col(P, C_VN + 2, N, j);
+        if (K.gradcorr) {  // locking form: (float)(m_j/rho_j) with v_ij (x) vc_i (InteractionAlt.cpp:330-350, 425-450)
+          double gk[3];
+          corr_grad(P, N, i, g.GK, g.x0, g.x1, g.x2, gk);
+          double bv[3] = {b0, b1, b2};
+          double wf = (double)(float)(col(P, C_MASS, N, j) / col(P, C_RHON, N, j));
+          const int ua[6] = {0, 1, 2, 0, 0, 1}, ub[6] = {0, 1, 2, 1, 2, 2};
+          for (int c = 0; c < 6; ++c) {
+            double gab = bv[ua[c]] * gk[ub[c]], gba = bv[ub[c]] * gk[ua[c]];
+            sr[c] += wf * (-0.5 * (gab + gba));
+          }
+          rr[0] += wf * (-0.5 * (bv[0] * gk[1] - bv[1] * gk[0]));
+          rr[1] += wf * (-0.5 * (bv[0] * gk[2] - bv[2] * gk[0]));
+          rr[2] += wf * (-0.5 * (bv[1] * gk[2] - bv[2] * gk[1]));
+          continue;
+        }
         double f = -0.5 * g.GK;
         double w = col(P, C_MRHON, N, j);
         sr[0] += w * (f * (2.0 * b0 * g.x0));
@@ -514,7 +588,15 @@ __global__ void __launch_bounds__(BLOCK) k_energy(DevPtrs P, DomainConst K) {
       if (K.thermal_solver) {
         double kj = col(P, C_KT, N, j);
         double w = up ? col(P, C_MRHO, N, j) : mrhoi;  // m_P2 / rho_P2 for both ends
-        double dxx = g.x0 * (g.GK * g.x0) + g.x1 * (g.GK * g.x1) + g.x2 * (g.GK * g.x2);
+        double gx[3] = {g.GK * g.x0, g.GK * g.x1, g.GK * g.x2};
+        if (K.gradcorr) {  // Mult(gradCorrM_i, GK x_ij) (Thermal.cpp:90-107)
+          double c3[3];
+          for (int q = 0; q < 3; ++q)
+            c3[q] = gx[0] * col(P, C_GCM + 3 * q, N, i) + gx[1] * col(P, C_GCM + 3 * q + 1, N, i) +
+                    gx[2] * col(P, C_GCM + 3 * q + 2, N, i);
+          gx[0] = c3[0]; gx[1] = c3[1]; gx[2] = c3[2];
+        }
+        double dxx = g.x0 * gx[0] + g.x1 * gx[1] + g.x2 * gx[2];
         cond += w * 4. * (ki * kj) / (ki + kj) * (Ti - col(P, C_T, N, j)) * dxx / (g.r * g.r);
       }
     }
@@ -723,6 +805,11 @@ void launch_step_head(const DevPtrs& P, const DomainConst& K, double* fscratch, 
   k_schedule<<<1, 1, 0, s>>>(P, K);
   mark(s, "k_schedule");
   launch_neighbour_search(P, K, fscratch, iscratch, s);
+  if (K.gradcorr) {
+    int b = nblk(K.N, BLOCK);
+    k_grad_corr<<<b < 152 * 4 ? b : 152 * 4, BLOCK, 0, s>>>(P, K);
+    mark(s, "k_grad_corr");
+  }
 }
 void launch_bc(const DevPtrs& P, const DomainConst& K, int vcol, cudaStream_t s) {
   int nbc = nblk(K.nbc_particles > 0 ? K.nbc_particles : 1, BLOCK);

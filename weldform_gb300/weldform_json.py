@@ -28,8 +28,9 @@ Supported input (everything the kick-drift / leapfrog path covers):
   coefficients, penaltyFactor).
 Anything else (Fraser or Thermal solvers, adaptive time step, GMT, damage,
 file or axisymmetric domains and meshes, 2D, heat-conduction contact,
-convection / temperature BCs, kernel-gradient correction, smoothing-length
-update) raises WFError(WF_ERR_UNSUPPORTED) before any step runs.
+convection / temperature BCs, smoothing-length update) raises
+WFError(WF_ERR_UNSUPPORTED) before any step runs.  kernelGradCorr is
+supported in the plain FP64 form.
 """
 from __future__ import annotations
 
@@ -135,8 +136,8 @@ def build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = N
     cont_alg = config.get("contAlgorithm", "Wang")
     if cont_alg not in ("Wang", "Fraser"):
         _unsupported(f"contact algorithm {cont_alg!r}")
-    if config.get("kernelGradCorr", False):
-        _unsupported("kernel-gradient correction")
+    if config.get("kernelGradCorr", False):  # the reference then sums with locks (SolverKickDrift.cpp:107-110)
+        dom.set("gradKernelCorr", 1)
     if int(config.get("stressGradType", 0)) != 0:
         _unsupported("stressGradType != 0")
     if config.get("smoothlenUpdate", False):
