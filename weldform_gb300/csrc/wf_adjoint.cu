@@ -114,13 +114,14 @@ __global__ void __launch_bounds__(BLOCK) k_adj_thermal_stress(AdjPtrs A, DomainC
     if (K.pl_heating) lqpl = K.pl_work_heat_frac * lci;
     double xi[3] = {FE(C_X, i), FE(C_X + 1, i), FE(C_X + 2, i)};
     double hi = col(S, C_H, N, i), ki = col(S, C_KT, N, i), Ti = FE(C_T, i), wi = FE(C_MRHO, i);
-    int len = S.row_len[i], split = S.row_split[i];
+    int len = S.row_len[i];
     for (int k = 0; k < len; ++k) {
-      int j = S.nbr[(size_t)k * N + i];
+      int e = S.nbr[(size_t)k * N + i];
+      int j = nb_index(e);
       GeoD g = geo_d(xi, hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
       double lcj = LIN(A_DTDT, j) / (FE(C_RHO, j) * col(S, C_CPT, N, j));
       double d = lci - lcj;
-      bool up = k < split;  // j has the larger original index: P2 = j
+      bool up = nb_up(e);  // j has the larger original index: P2 = j
       double w = up ? FE(C_MRHO, j) : wi;  // m_P2 / rho_P2 at both ends (Thermal.cpp:127-131)
       double kj = col(S, C_KT, N, j);
       double kk = 4. * (ki * kj) / (ki + kj);
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_rates_drift(AdjPtrs A, DomainCons
   double sumLT = 0.0;
   int len = S.row_len[i];
   for (int k = 0; k < len; ++k) {
-    int j = S.nbr[(size_t)k * N + i];
+    int j = nb_index(S.nbr[(size_t)k * N + i]);
     GeoD g = geo_d(xi, hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
     double b0 = vi[0] - FE(C_V, j), b1 = vi[1] - FE(C_V + 1, j), b2 = vi[2] - FE(C_V + 2, j);
     double wj = FE(C_MRHO, j);
@@ -377,7 +378,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_density_contact(AdjPtrs A, Domain
   double lx[3] = {0, 0, 0}, lrho = 0.0, D = 0.0;
   int len = S.row_len[i];
   for (int k = 0; k < len; ++k) {
-    int j = S.nbr[(size_t)k * N + i];
+    int j = nb_index(S.nbr[(size_t)k * N + i]);
     GeoD g = geo_d(xi, hi, col(S, C_X, N, j), col(S, C_X + 1, N, j), col(S, C_X + 2, N, j), col(S, C_H, N, j));
     double b0 = vh[0] - TXV(TX_VH, j), b1 = vh[1] - TXV(TX_VH + 1, j), b2 = vh[2] - TXV(TX_VH + 2, j);
     double bx = b0 * g.x0 + b1 * g.x1 + b2 * g.x2;
@@ -596,7 +597,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
   double lSs[6] = {0, 0, 0, 0, 0, 0};
   int len = S.row_len[i];
   for (int k = 0; k < len; ++k) {
-    int j = S.nbr[(size_t)k * N + i];
+    int j = nb_index(S.nbr[(size_t)k * N + i]);
     double mj = col(S, C_MASS, N, j);
     double Gm[3];
     for (int d = 0; d < 3; ++d) Gm[d] = mj * lai[d] - mi * TMP(J_AACC + d, j);

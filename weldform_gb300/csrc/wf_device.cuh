@@ -104,6 +104,16 @@ constexpr int MAX_MESHES = 8;
 constexpr int MAX_NB = 100;  // MAX_NB_PER_PART, Source/Domain.h:49
 constexpr int MAX_CP = 64;   // contact pairs per particle
 
+// Neighbour-row entries: the neighbour's index, bit 31 set when its original
+// index is larger than the row particle's (the P2 side of the reference's
+// (min, max) pair).  The plain FP64 form keeps rows in the reference's
+// canonical order (j > i ascending, then j < i ascending by original index);
+// the mixed form orders them by memory index, so the k-th neighbours of a
+// warp's consecutive particles sit close together in memory.
+constexpr unsigned NB_UP = 0x80000000u;
+__host__ __device__ __forceinline__ int nb_index(int e) { return e & 0x7fffffff; }
+__host__ __device__ __forceinline__ bool nb_up(int e) { return e < 0; }
+
 // Tables that are read by a few threads only; kept in device memory.
 struct DomainTables {
   MaterialDev mat[MAX_MATERIALS];
@@ -166,6 +176,8 @@ struct DomainConst {
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
   int leapfrog;        // 1: SolveDiffUpdateLeapFrog's update (velocities at half steps)
   int gradcorr;        // 1: kernel-gradient correction (Domain::gradKernelCorr)
+  int av_uniform;      // 1 when every solid particle has the same Alpha and Beta
+  float av_alpha, av_beta;  // those values (the mixed acceleration gather skips their loads)
 };
 
 // Device pointers, passed by value to every kernel.

@@ -556,6 +556,18 @@ struct wf_domain {
     K.totmass_mean = tm / N;
     K.id_free_surf = -999999;
     K.leapfrog = integrator;
+    {
+      K.av_uniform = 1;
+      bool first = true;
+      double a0 = 0, b0 = 0;
+      for (int p = 0; p < N; ++p) {
+        if (hp.i[I_KIND][p] != 0) continue;
+        if (first) { a0 = F(C_ALPHA, p); b0 = F(C_BETA, p); first = false; }
+        else if (F(C_ALPHA, p) != a0 || F(C_BETA, p) != b0) { K.av_uniform = 0; break; }
+      }
+      K.av_alpha = (float)a0;
+      K.av_beta = (float)b0;
+    }
     K.gradcorr = grad_corr;
     K.ti = 0;
     for (int p = 0; p < N; ++p)
@@ -583,7 +595,7 @@ struct wf_domain {
     // before the loop; the first step searches again (ClearNbData).
     if (contact) {
       launch_force_search(P, stream);
-      launch_neighbour_search(P, K, d_fscratch, d_iscratch, stream);
+      launch_neighbour_search(P, kconst(), d_fscratch, d_iscratch, stream);
       K.id_free_surf = 1;
     }
     StepState* stp = P.st;
@@ -613,12 +625,17 @@ struct wf_domain {
       throw CudaError{WF_ERR_STATE, "No external particles found. Please check particle masses"};
   }
 
-  void launch_one_step() {
-    if (K.gradcorr && precision == WF_PRECISION_MIXED)
-      throw CudaError{WF_ERR_UNSUPPORTED, "kernel-gradient correction runs in the plain FP64 form"};
+  // The constants of a launch: K plus the current form and gather block size.
+  wf::DomainConst kconst() const {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
     k.gblock = gblock;
+    return k;
+  }
+  void launch_one_step() {
+    if (K.gradcorr && precision == WF_PRECISION_MIXED)
+      throw CudaError{WF_ERR_UNSUPPORTED, "kernel-gradient correction runs in the plain FP64 form"};
+    wf::DomainConst k = kconst();
     if (k.mixed) wf::launch_step_mixed(P, k, d_fscratch, d_iscratch, stream);
     else wf::launch_step_fp64(P, k, d_fscratch, d_iscratch, stream);
   }
@@ -999,7 +1016,8 @@ struct wf_domain {
     if (!prepared) throw CudaError{WF_ERR_STATE, "neighbour search before the solver prologue"};
     use_device();
     wf::launch_force_search(P, stream);
-    wf::launch_neighbour_search(P, K, d_fscratch, d_iscratch, stream);
+    wf::launch_neighbour_search(P, kconst(), d_fscratch, d_iscratch, stream);
+    shadows_valid = false;  // the search reorders particles
     int zero = 0;
     CK(cudaMemcpyAsync(&P.st->do_search, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
@@ -1072,7 +1090,11 @@ struct wf_domain {
     for (size_t o = 0; o < n; ++o) {
       int i = sorted_of[o];
       int l = std::min(len[i], width);
-      for (int k = 0; k < l; ++k) idx[off[o] + k] = orig[ell[(size_t)k * n + i]];
+      for (int k = 0; k < l; ++k) idx[off[o] + k] = orig[wf::nb_index(ell[(size_t)k * n + i])];
+      // canonical order (j > i ascending, then j < i ascending), whatever the device order
+      unsigned oo = (unsigned)o;
+      std::sort(idx.begin() + off[o], idx.begin() + off[o + 1],
+                [oo](int a, int b) { return (unsigned)a - oo - 1u < (unsigned)b - oo - 1u; });
     }
   }
 };
@@ -1129,7 +1151,10 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   std::string n(name ? name : "");
   if (n == "precision") {
     if (v != WF_PRECISION_FP64 && v != WF_PRECISION_MIXED) return set_err(WF_ERR_ARG, "precision must be 0 or 1");
+    if (v == d->precision) return WF_OK;
     d->precision = v;
+    // the two forms order neighbour rows differently: rebuild them now
+    if (d->prepared) return guard([&] { d->search_now(); return WF_OK; });
     return WF_OK;
   }
   if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }

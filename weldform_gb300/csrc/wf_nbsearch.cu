@@ -282,11 +282,13 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     int excl = incl - cc;
     for (int base = 0; base < total; base += 32) {
       int t = base + lane;
-      // cell of flat candidate t: the last lane whose exclusive prefix <= t
+      // cell of flat candidate t: the last lane q < 27 whose exclusive prefix
+      // is <= t (prefixes are non-decreasing in q: binary search, 5 shuffles)
       int cell = 0;
-      for (int q = 0; q < 27; ++q) {
-        int ex = __shfl_sync(0xffffffffu, excl, q);
-        if (ex <= t) cell = q;
+      for (int step = 16; step > 0; step >>= 1) {
+        int q = cell + step;
+        int ex = __shfl_sync(0xffffffffu, excl, q < 27 ? q : 26);
+        if (q < 27 && ex <= t) cell = q;
       }
       int cstart = __shfl_sync(0xffffffffu, cs, cell);
       int cexcl = __shfl_sync(0xffffffffu, excl, cell);
@@ -299,26 +301,30 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
           int cj = cls[j];
           ok = !(K.contact && (ci || (cj & 2))) && (cj & 1) == 0 && (cj >> 2) == mi &&
                radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, reinterpret_cast<const float4*>(P.xs)[j]);
-          if (ok) kk = (unsigned)(orig[j] - oi - 1);
+          if (ok) kk = K.mixed ? (unsigned)j : (unsigned)(orig[j] - oi - 1);
         }
       }
       unsigned m = __ballot_sync(0xffffffffu, ok);
       if (ok) {
         int pos = cnt + __popc(m & ((1u << lane) - 1u));
-        if (pos < FILL_SLOTS) { s_key[w][pos] = kk; s_idx[w][pos] = j; }
+        // stored entry: the index, with bit 31 set when j has the larger
+        // original index (P2 of the reference's (min, max) pair)
+        if (pos < FILL_SLOTS) { s_key[w][pos] = kk; s_idx[w][pos] = (int)((unsigned)j | (orig[j] > oi ? NB_UP : 0u)); }
       }
       cnt += __popc(m);
     }
     if (cnt > MAX_NB) overflow = true;
     if (cnt > FILL_SLOTS) cnt = FILL_SLOTS;
   }
-  // Pad and sort the warp's slots by key (bitonic, ascending).
-  for (int e = lane; e < FILL_SLOTS; e += 32)
+  // Pad and sort the warp's slots by key (bitonic, ascending) over the
+  // smallest power of two >= the row length (32, 64 or 128; warp-uniform).
+  int nsort = cnt <= 32 ? 32 : (cnt <= 64 ? 64 : FILL_SLOTS);
+  for (int e = lane; e < nsort; e += 32)
     if (e >= cnt) { s_key[w][e] = 0xffffffffu; s_idx[w][e] = -1; }
   __syncwarp();
-  for (int k = 2; k <= FILL_SLOTS; k <<= 1) {
+  for (int k = 2; k <= nsort; k <<= 1) {
     for (int jj = k >> 1; jj > 0; jj >>= 1) {
-      for (int e = lane; e < FILL_SLOTS; e += 32) {
+      for (int e = lane; e < nsort; e += 32) {
         int p = e ^ jj;
         if (p > e) {
           bool up = (e & k) == 0;
@@ -334,9 +340,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   }
   if (cnt > MAX_NB) cnt = MAX_NB;
   if (i < K.N) {
-    // keys below N - 1 - oi belong to neighbours with a larger original index
-    int oi = orig[i];
-    for (int e = lane; e < cnt; e += 32) split += s_key[w][e] < (unsigned)(K.N - 1 - oi) ? 1 : 0;
+    for (int e = lane; e < cnt; e += 32) split += s_idx[w][e] < 0 ? 1 : 0;
     for (int off = 16; off > 0; off >>= 1) split += __shfl_down_sync(0xffffffffu, split, off);
     if (lane == 0) {
       s_len[w] = cnt;
@@ -373,7 +377,7 @@ __global__ void k_surface(DevPtrs P, DomainConst K) {
   double n0 = 0, n1 = 0, n2 = 0;
   int len = P.row_len[i];
   for (int k = 0; k < len; ++k) {
-    int j = P.nbr[(size_t)k * N + i];
+    int j = nb_index(P.nbr[(size_t)k * N + i]);
     double mj = P.f[C_MASS * N + j];
     n0 = __dadd_rn(n0, __dmul_rn(mj, __dsub_rn(xi, P.f[C_X * N + j])));
     n1 = __dadd_rn(n1, __dmul_rn(mj, __dsub_rn(yi, P.f[(C_X + 1) * N + j])));

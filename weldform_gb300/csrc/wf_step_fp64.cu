@@ -142,7 +142,7 @@ __global__ void k_grad_corr(DevPtrs P, DomainConst K) {
     double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     int len = P.row_len[i];
     for (int k = 0; k < len; ++k) {
-      int j = P.nbr[(size_t)k * N + i];
+      int j = nb_index(P.nbr[(size_t)k * N + i]);
       PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                            col(P, C_H, N, j));
       double gv[3] = {g.GK * g.x0, g.GK * g.x1, g.GK * g.x2}, xv[3] = {g.x0, g.x1, g.x2};
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
   double a0 = 0, a1 = 0, a2 = 0;
   int len = P.row_len[i];
   for (int k = 0; k < len; ++k) {
-    int j = P.nbr[(size_t)k * N + i];
+    int j = nb_index(P.nbr[(size_t)k * N + i]);
     PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                          col(P, C_H, N, j));
     double Alpha = (ai + col(P, C_ALPHA, N, j)) / 2.0, Beta = (bi + col(P, C_BETA, N, j)) / 2.0;
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
     double hi = col(P, C_H, N, i);
     int len = P.row_len[i];
     for (int k = 0; k < len; ++k) {
-      int j = P.nbr[(size_t)k * N + i];
+      int j = nb_index(P.nbr[(size_t)k * N + i]);
       PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                            col(P, C_H, N, j));
       double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
       double sr[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};
       int len = P.row_len[i];
       for (int k = 0; k < len; ++k) {
-        int j = P.nbr[(size_t)k * N + i];
+        int j = nb_index(P.nbr[(size_t)k * N + i]);
         PairGeo g = pair_geo(x[0], x[1], x[2], hi, col(P, C_XN, N, j), col(P, C_XN + 1, N, j), col(P, C_XN + 2, N, j),
                              col(P, C_H, N, j));
         double b0 = v[0] - col(P, C_VN, N, j), b1 = v[1] - col(P, C_VN + 1, N, j), b2 = v[2] - col(P, C_VN + 2, N, j);
@@ -574,14 +574,15 @@ __global__ void __launch_bounds__(BLOCK) k_energy(DevPtrs P, DomainConst K) {
     double pri = col(P, C_PR2, N, i);
     double Ti = col(P, C_T, N, i), ki = col(P, C_KT, N, i);
     double cond = 0.0;
-    int len = P.row_len[i], split = P.row_split[i];
+    int len = P.row_len[i];
     for (int k = 0; k < len; ++k) {
-      int j = P.nbr[(size_t)k * N + i];
+      int e = P.nbr[(size_t)k * N + i];
+      int j = nb_index(e);
       PairGeo g = pair_geo(x0, x1, x2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                            col(P, C_H, N, j));
       double b0 = v0 - col(P, C_V, N, j), b1 = v1 - col(P, C_V + 1, N, j), b2 = v2 - col(P, C_V + 2, N, j);
       double dv = b0 * (g.GK * g.x0) + b1 * (g.GK * g.x1) + b2 * (g.GK * g.x2);
-      bool up = k < split;  // original index of j larger than i's
+      bool up = nb_up(e);  // original index of j larger than i's
       // CalcKinEnergyEqn pair (P1 = smaller original index): 0.5 m_P2 (p1/d1^2 + p2/d2^2) v12.(GK x12)
       double pk = 0.5 * (up ? col(P, C_MASS, N, j) : mi) * (pri + col(P, C_PR2, N, j)) * dv;
       dkin += up ? pk : -pk;

@@ -106,16 +106,22 @@ __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
   int len = P.row_len[i];
   const int* nb = P.nbr + i;
   for (int k = 0; k < len; ++k) {
-    int j = nb[(size_t)k * N];
+    int j = nb_index(nb[(size_t)k * N]);
     const float4* rj = P.rc + j;
     float4 jxh = ld4(rj + (size_t)RC_XH * N), jxl = ld4(rj + (size_t)RC_XL * N), jvh = ld4(rj + (size_t)RC_VH * N), jvl = ld4(rj + (size_t)RC_VL * N);
-    float4 js0 = ld4(rj + (size_t)RC_S0 * N), js1 = ld4(rj + (size_t)RC_S1 * N), jmi = ld4(rj + (size_t)RC_MISC * N);
+    float4 js0 = ld4(rj + (size_t)RC_S0 * N), js1 = ld4(rj + (size_t)RC_S1 * N);
     float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
     float v0 = (vh.x - jvh.x) + (vl.x - jvl.x), v1 = (vh.y - jvh.y) + (vl.y - jvl.y), v2 = (vh.z - jvh.z) + (vl.z - jvl.z);
     float hh = 0.5f * (xh.w + jxh.w);
     float r2 = x0 * x0 + x1 * x1 + x2 * x2, r;
     float GK = grad_kernel_f(r2, hh, &r);
-    float Alpha = 0.5f * (mi.x + jmi.x), Beta = 0.5f * (mi.y + jmi.y);
+    float Alpha, Beta;
+    if (K.av_uniform) {  // the pair mean of equal values is the value itself
+      Alpha = K.av_alpha; Beta = K.av_beta;
+    } else {
+      float4 jmi = ld4(rj + (size_t)RC_MISC * N);
+      Alpha = 0.5f * (mi.x + jmi.x); Beta = 0.5f * (mi.y + jmi.y);
+    }
     float PIs = 0.f;
     if (Alpha != 0.f || Beta != 0.f) {
       float dvx = v0 * x0 + v1 * x1 + v2 * x2;
@@ -165,7 +171,7 @@ __global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
     for (int k = 0; k < len; ++k) {
-      int j = nb[(size_t)k * N];
+      int j = nb_index(nb[(size_t)k * N]);
       const float4* rj = P.rc + j;
       float4 jxh = ld4(rj + (size_t)RC_XH * N), jxl = ld4(rj + (size_t)RC_XL * N), jvh = ld4(rj + (size_t)RC_VH * N), jvl = ld4(rj + (size_t)RC_VL * N);
       float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
@@ -223,11 +229,12 @@ __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
     float4 xh = ld4(ri + (size_t)RN_XH * N), xl = ld4(ri + (size_t)RN_XL * N), vh = ld4(ri + (size_t)RN_VH * N), vl = ld4(ri + (size_t)RN_VL * N), e = ld4(ri + (size_t)RN_E * N);
     KSum M[9];  // sum_j (m_j / rho_j) (-GK / 2) (v_i - v_j)_k (x_i - x_j)_l
     KSum kin, cnd;
-    int len = P.row_len[i], split = P.row_split[i];
+    int len = P.row_len[i];
     const int* nb = P.nbr + i;
     bool thermal = K.thermal_solver;
     for (int k = 0; k < len; ++k) {
-      int j = nb[(size_t)k * N];
+      int ent = nb[(size_t)k * N];
+      int j = nb_index(ent);
       const float4* rj = P.rn + j;
       float4 jxh = ld4(rj + (size_t)RN_XH * N), jxl = ld4(rj + (size_t)RN_XL * N), jvh = ld4(rj + (size_t)RN_VH * N), jvl = ld4(rj + (size_t)RN_VL * N);
       float4 je = ld4(rj + (size_t)RN_E * N);
@@ -240,7 +247,7 @@ __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
       M[0].add(wb0 * x0); M[1].add(wb0 * x1); M[2].add(wb0 * x2);
       M[3].add(wb1 * x0); M[4].add(wb1 * x1); M[5].add(wb1 * x2);
       M[6].add(wb2 * x0); M[7].add(wb2 * x1); M[8].add(wb2 * x2);
-      bool up = k < split;  // original index of j larger than i's
+      bool up = nb_up(ent);  // original index of j larger than i's
       float dv = GK * (b0 * x0 + b1 * x1 + b2 * x2);
       float pk = 0.5f * (up ? jxl.w : xl.w) * (e.x + je.x) * dv;
       kin.add(up ? pk : -pk);
