@@ -1091,10 +1091,7 @@ struct wf_domain {
       int i = sorted_of[o];
       int l = std::min(len[i], width);
       for (int k = 0; k < l; ++k) idx[off[o] + k] = orig[wf::nb_index(ell[(size_t)k * n + i])];
-      // canonical order (j > i ascending, then j < i ascending), whatever the device order
-      unsigned oo = (unsigned)o;
-      std::sort(idx.begin() + off[o], idx.begin() + off[o + 1],
-                [oo](int a, int b) { return (unsigned)a - oo - 1u < (unsigned)b - oo - 1u; });
+
     }
   }
 };
@@ -1151,10 +1148,7 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   std::string n(name ? name : "");
   if (n == "precision") {
     if (v != WF_PRECISION_FP64 && v != WF_PRECISION_MIXED) return set_err(WF_ERR_ARG, "precision must be 0 or 1");
-    if (v == d->precision) return WF_OK;
     d->precision = v;
-    // the two forms order neighbour rows differently: rebuild them now
-    if (d->prepared) return guard([&] { d->search_now(); return WF_OK; });
     return WF_OK;
   }
   if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }

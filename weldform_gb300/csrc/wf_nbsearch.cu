@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
           int cj = cls[j];
           ok = !(K.contact && (ci || (cj & 2))) && (cj & 1) == 0 && (cj >> 2) == mi &&
                radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, reinterpret_cast<const float4*>(P.xs)[j]);
-          if (ok) kk = K.mixed ? (unsigned)j : (unsigned)(orig[j] - oi - 1);
+          if (ok) kk = (unsigned)(orig[j] - oi - 1);
         }
       }
       unsigned m = __ballot_sync(0xffffffffu, ok);
