@@ -150,6 +150,9 @@ struct wf_domain {
   int graph_precision = -1;
   int graph_block = -1;
   int gblock = 256;
+  int gsched = 0;    // gather schedule of the mixed form (0 per-tile blocks, 1 SM-chunked persistent)
+  int nchunks = 1;   // SM count of the device (chunks of the persistent schedule)
+  int graph_key() const { return gblock * 2 + gsched; }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
@@ -576,6 +579,13 @@ struct wf_domain {
     for (size_t m = 0; m < meshes.size(); ++m) K.contact_surf_id[m] = meshes[m].id;
     K.nblocks = (N + 255) / 256;
     P.partials = dalloc<double>((size_t)NSLOTS * K.nblocks);
+    {
+      int sms = 1;
+      CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+      nchunks = sms < 1 ? 1 : (sms > MAX_CHUNKS ? MAX_CHUNKS : sms);
+      P.tile_ctr = dalloc<int>((size_t)GATHER_KERNELS * MAX_CHUNKS);
+      CK(cudaMemsetAsync(P.tile_ctr, 0, sizeof(int) * GATHER_KERNELS * MAX_CHUNKS, stream));
+    }
     P.scan_tmp = dalloc<long long>((ncells + 4095) / 4096 + 1);
     // Step state.
     StepState st;
@@ -630,6 +640,8 @@ struct wf_domain {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
     k.gblock = gblock;
+    k.gsched = gsched;
+    k.nchunks = nchunks;
     return k;
   }
   void launch_one_step() {
@@ -654,9 +666,9 @@ struct wf_domain {
     use_device();
     ensure_shadows();
     if (use_graph) {
-      if (!graph || graph_precision != precision || graph_block != gblock) {
+      if (!graph || graph_precision != precision || graph_block != graph_key()) {
         if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
-        graph_block = gblock;
+        graph_block = graph_key();
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         long long l0 = wf::g_launches;
@@ -681,7 +693,7 @@ struct wf_domain {
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
     CK(cudaStreamSynchronize(stream));
-    if (use_graph && (!graph || graph_precision != precision || graph_block != gblock)) step(0);
+    if (use_graph && (!graph || graph_precision != precision || graph_block != graph_key())) step(0);
     ensure_shadows();
     long long l0 = wf::g_launches;
     CK(cudaEventRecord(a, stream));
@@ -825,7 +837,7 @@ struct wf_domain {
         if (e < 0.0) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: particles with Ep < 0 are not supported"};
     }
     use_device();
-    if (use_graph && (!graph || graph_precision != precision || graph_block != gblock)) step(0);
+    if (use_graph && (!graph || graph_precision != precision || graph_block != graph_key())) step(0);
     Scratch sc;
     double* f0 = sc.get<double>((size_t)NF64_PERSIST * n);
     int* i0 = sc.get<int>((size_t)NI32_PERSIST * n);
@@ -985,31 +997,35 @@ struct wf_domain {
   }
   int autotune(int steps) {
     static std::mutex mu;
-    static std::map<int, int> cache;  // size bucket -> block
+    static std::map<int, std::pair<int, int>> cache;  // size bucket -> (block, schedule)
     int bucket = 0;
     while ((1LL << bucket) < hp.N) ++bucket;
     {
       std::lock_guard<std::mutex> lk(mu);
       auto it = cache.find(bucket);
-      if (it != cache.end()) { gblock = it->second; return gblock; }
+      if (it != cache.end()) { gblock = it->second.first; gsched = it->second.second; return gblock; }
     }
     const int slot = 15;
     checkpoint_save(slot);
-    int best = 256;
+    int best = 256, best_sched = 0;
     double best_ms = 1e300;
-    for (int b : {64, 128, 256, 512}) {
-      gblock = b;
-      long long l = 0;
-      step(1);  // capture + warm
-      checkpoint_restore(slot);
-      double ms = step_timed(steps, &l);
-      checkpoint_restore(slot);
-      if (ms < best_ms) { best_ms = ms; best = b; }
+    for (int sc : {0, 1}) {
+      for (int b : {64, 128, 256, 512}) {
+        gblock = b;
+        gsched = sc;
+        long long l = 0;
+        step(1);  // capture + warm
+        checkpoint_restore(slot);
+        double ms = step_timed(steps, &l);
+        checkpoint_restore(slot);
+        if (ms < best_ms) { best_ms = ms; best = b; best_sched = sc; }
+      }
     }
     gblock = best;
+    gsched = best_sched;
     checkpoint_free(slot);
     std::lock_guard<std::mutex> lk(mu);
-    cache[bucket] = best;
+    cache[bucket] = {best, best_sched};
     return best;
   }
   void search_now() {
@@ -1152,6 +1168,16 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     return WF_OK;
   }
   if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }
+  if (n == "gather_schedule") {  // mixed-form gathers: 0 one block per tile, 1 SM-chunked persistent
+    if (v != 0 && v != 1) return set_err(WF_ERR_ARG, "gather_schedule must be 0 or 1");
+    d->gsched = v;
+    return WF_OK;
+  }
+  if (n == "gather_block") {
+    if (v != 64 && v != 128 && v != 256 && v != 512) return set_err(WF_ERR_ARG, "gather_block must be 64, 128, 256 or 512");
+    d->gblock = v;
+    return WF_OK;
+  }
   if (n == "device") {
     if (d->prepared) return set_err(WF_ERR_STATE, "the device is fixed after the prologue");
     int nd = 0;
@@ -1212,6 +1238,8 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     std::string n(name ? name : "");
     if (n == "particle_count") { *v = d->hp.N; return WF_OK; }
     if (n == "solid_part_count") { *v = d->solid_part_count; return WF_OK; }
+    if (n == "gather_schedule") { *v = d->gsched; return WF_OK; }
+    if (n == "gather_block") { *v = d->gblock; return WF_OK; }
     if (n.size() == 8 && n.rfind("CellNo.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') { *v = d->CellNo[n[7] - 'x']; return WF_OK; }
     if (!d->prepared) { *v = 0; return WF_OK; }
     wf::StepState st = d->read_state();

@@ -229,15 +229,26 @@ __device__ __forceinline__ bool radius_ok(const DevPtrs& P, const DomainConst& K
 // SM neighbour rows in canonical order: one warp per particle, 32 consecutive
 // particles per block.  Lanes test the candidates of each of the 27 cells in
 // parallel; accepted ones are compacted with a ballot into the warp's shared
-// buffer, sorted there by the canonical key (bitonic, 128 slots), and the
+// buffer (128 slots), placed there by the rank of their canonical key, and the
 // block writes its 32 rows to the ELL array one coalesced line per entry
 // index.  Also sets Nb and the "free surface at search time" flag used by the
 // contact pair rule.
+// rank[r] += number of keys in row[0, n4) below key[r], r < NK (n4 a multiple of 4).
+template <int NK>
+__device__ __forceinline__ void rank_row(const unsigned* row, int n4, const unsigned key[4], int rank[4]) {
+  for (int t = 0; t < n4; t += 4) {
+    uint4 q = *reinterpret_cast<const uint4*>(row + t);
+#pragma unroll
+    for (int r = 0; r < NK; ++r)
+      rank[r] += (int)(q.x < key[r]) + (int)(q.y < key[r]) + (int)(q.z < key[r]) + (int)(q.w < key[r]);
+  }
+}
+
 constexpr int FILL_WARPS = 32;
 constexpr int FILL_SLOTS = 128;
 __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  __shared__ unsigned s_key[FILL_WARPS][FILL_SLOTS];
+  __shared__ __align__(16) unsigned s_key[FILL_WARPS][FILL_SLOTS];
   __shared__ int s_idx[FILL_WARPS][FILL_SLOTS];
   __shared__ int s_len[FILL_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -316,28 +327,28 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     if (cnt > MAX_NB) overflow = true;
     if (cnt > FILL_SLOTS) cnt = FILL_SLOTS;
   }
-  // Pad and sort the warp's slots by key (bitonic, ascending) over the
-  // smallest power of two >= the row length (32, 64 or 128; warp-uniform).
-  int nsort = cnt <= 32 ? 32 : (cnt <= 64 ? 64 : FILL_SLOTS);
-  for (int e = lane; e < nsort; e += 32)
-    if (e >= cnt) { s_key[w][e] = 0xffffffffu; s_idx[w][e] = -1; }
+  // Order the warp's slots by key.  Keys are distinct (one per neighbour), so
+  // each entry's final slot is the number of smaller keys: every lane ranks
+  // its own (at most four) entries against the whole row, read four keys per
+  // broadcast load, then scatters them.  Pads above the row hold the largest
+  // key, which no real key reaches (orig[j] - oi - 1 != -1).
+  int cnt4 = (cnt + 3) & ~3;
+  for (int e = cnt + lane; e < cnt4; e += 32) s_key[w][e] = 0xffffffffu;
   __syncwarp();
-  for (int k = 2; k <= nsort; k <<= 1) {
-    for (int jj = k >> 1; jj > 0; jj >>= 1) {
-      for (int e = lane; e < nsort; e += 32) {
-        int p = e ^ jj;
-        if (p > e) {
-          bool up = (e & k) == 0;
-          unsigned ke = s_key[w][e], kp = s_key[w][p];
-          if ((ke > kp) == up) {
-            s_key[w][e] = kp; s_key[w][p] = ke;
-            int t = s_idx[w][e]; s_idx[w][e] = s_idx[w][p]; s_idx[w][p] = t;
-          }
-        }
-      }
-      __syncwarp();
-    }
+  const int nk = (cnt + 31) >> 5;  // warp-uniform
+  unsigned key[4];
+  int idx[4], rank[4] = {0, 0, 0, 0};
+  for (int r = 0; r < 4; ++r) {
+    int e = lane + 32 * r;
+    key[r] = e < cnt ? s_key[w][e] : 0xffffffffu;
+    idx[r] = e < cnt ? s_idx[w][e] : 0;
   }
+  if (nk <= 2) rank_row<2>(&s_key[w][0], cnt4, key, rank);
+  else rank_row<4>(&s_key[w][0], cnt4, key, rank);
+  __syncwarp();
+  for (int r = 0; r < 4; ++r)
+    if (lane + 32 * r < cnt) s_idx[w][rank[r]] = idx[r];
+  __syncwarp();
   if (cnt > MAX_NB) cnt = MAX_NB;
   if (i < K.N) {
     for (int e = lane; e < cnt; e += 32) split += s_idx[w][e] < 0 ? 1 : 0;

@@ -2,9 +2,10 @@
 //
 // Same step, same reference semantics as the plain form (wf_step_fp64.cu);
 // what changes is how the pair gathers compute and what they read:
-//  * each particle's FP32 gather data sits in one 128-byte record (one cache
-//    line per neighbour), so a neighbour costs a few vector loads from one
-//    line instead of one scalar load from each of ~20 separate columns;
+//  * the FP32 gather data sits in float4 field-group columns (group q of
+//    particle i at rc[q*N + i]), so a neighbour costs six 16-byte loads that
+//    coalesce across the warp's consecutive particles, instead of one scalar
+//    load from each of ~20 separate columns;
 //  * relative positions, velocities and temperatures come from float-float
 //    pairs, (hi_i - hi_j) + (lo_i - lo_j): accurate to FP32 rounding of the
 //    difference itself — the accuracy of an FP64 difference cast to FP32 —
@@ -39,6 +40,53 @@ struct KSum {
 };
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+
+// ---------------------------------------------------------------- gather schedule
+// Schedule 0: block b handles particles [b*B, (b+1)*B).  Schedule 1: a
+// persistent grid (resident blocks of every SM) where each SM owns a
+// contiguous chunk of tiles — a compact region in the Morton order — and its
+// blocks take the chunk's tiles in order from a cursor, so the neighbour
+// records that consecutive tiles share stay in that SM's L1.  A block whose
+// home chunk is exhausted moves on to the next chunk, so every tile is taken
+// exactly once whatever SMs the blocks land on.  Each particle's result does
+// not depend on which block computes it.
+__device__ __forceinline__ unsigned sm_id() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
+
+template <class Body>
+__device__ __forceinline__ void run_tiles(const DomainConst& K, int* ctr, Body body) {
+  if (!K.gsched) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < K.N) body(i);
+    return;
+  }
+  __shared__ int s_tile, s_chunk, s_seen;
+  const int nch = K.nchunks;
+  const int ntiles = (K.N + blockDim.x - 1) / blockDim.x;
+  if (threadIdx.x == 0) { s_chunk = (int)(sm_id() % (unsigned)nch); s_seen = 0; }
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int c = s_chunk, seen = s_seen, tile = -1;
+      while (seen < nch) {
+        int lo = (int)((long long)ntiles * c / nch), hi = (int)((long long)ntiles * (c + 1) / nch);
+        int t = lo + atomicAdd(&ctr[c], 1);
+        if (t < hi) { tile = t; break; }
+        c = (c + 1 == nch) ? 0 : c + 1;
+        ++seen;
+      }
+      s_chunk = c; s_seen = seen; s_tile = tile;
+    }
+    __syncthreads();
+    int tile = s_tile;
+    __syncthreads();
+    if (tile < 0) return;
+    int i = tile * blockDim.x + threadIdx.x;
+    if (i < K.N) body(i);
+  }
+}
 
 // Cubic-spline gradient factor GK (Functions.cpp:74-87, 3D) from r^2 and the
 // pair smoothing length hh = (hi + hj) / 2.
@@ -88,9 +136,7 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
 
 // ---------------------------------------------------------------- accel
 template <bool TI>
-__global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
+__device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   if (icol(P, I_KIND, N, i) != 0) {
     colw(P, C_A, N, i) = 0.0; colw(P, C_A + 1, N, i) = 0.0; colw(P, C_A + 2, N, i) = 0.0;
@@ -153,11 +199,13 @@ __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
   }
   colw(P, C_A, N, i) = a0.value(); colw(P, C_A + 1, N, i) = a1.value(); colw(P, C_A + 2, N, i) = a2.value();
 }
+template <bool TI>
+__global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
+  run_tiles(K, P.tile_ctr, [&](int i) { accel_mx<TI>(P, K, i); });
+}
 
 // ---------------------------------------------------------------- density + drift + kick
-__global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst K) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
+__device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   double dt = K.dt;
   double rhoi = col(P, C_RHO, N, i);
@@ -214,13 +262,14 @@ __global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst
   r[(size_t)RN_VL * N] = make_float4(nvl[0], nvl[1], nvl[2], (float)mrn);
   r[(size_t)RN_E * N] = make_float4(solid ? (float)(pn / (rn * rn)) : 0.f, ri[(size_t)RC_MISC * N].z, th, tl);
 }
+__global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst K) {
+  run_tiles(K, P.tile_ctr + K.nchunks, [&](int i) { density_drift_mx(P, K, i); });
+}
 
 // ---------------------------------------------------------------- rates + energy + conduction
 // Gather at x(n+1), v(n+1): strain/rotation rate sums (InteractionAlt.cpp:263-479),
 // the kinetic-energy pair sum (Domain.cpp:1752-1808) and conduction (Thermal.cpp:53-219).
-__global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
+__device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   double dkin = 0.0, cond = 0.0;
@@ -269,12 +318,27 @@ __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
   colw(P, C_DKIN, N, i) = dkin;
   colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
 }
+__global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
+  run_tiles(K, P.tile_ctr + 2 * K.nchunks, [&](int i) { rate_mx(P, K, i); });
+}
 
 // ---------------------------------------------------------------- elementwise update
+// Stress state of the radial return.  The strain columns (Strain, Strain_pl,
+// Strain_pl_incr) are not held here: the kernel streams them after the return,
+// which keeps the kernel's register footprint small.
+struct StressMx {
+  double tau[6], sig[6];
+  double pressure, pl_strain, delta_pl_strain, sigmay, Ep;
+  float esr;
+};
+
 // Radial return with the Jaumann increment formed in FP32 and accumulated into
 // the FP64 deviatoric stress; yield check, scale factor and plastic increment
-// in FP64 (Particle.cpp:960-1067).
-__device__ __forceinline__ double stress_update_mx(StressIO& s, const float sr[6], const float rr[3], double rho,
+// in FP64 (Particle.cpp:960-1067).  Returns the plastic increment.  The trial
+// stress sqrt(3 J2) and the ratio sigma_y / sigma_trial are formed only when
+// 3 J2 > sigma_y^2 (a particle inside the yield surface has scale factor 1 and
+// no plastic step), so elastic particles skip the FP64 sqrt and divide.
+__device__ __forceinline__ double stress_update_mx(StressMx& s, const float sr[6], const float rr[3], double rho,
                                                    double rho0, double Cs, double P0, double G, double T, int fail,
                                                    int model, const MaterialDev* M, double dt) {
   s.pressure = P0 + (Cs * Cs) * (rho - rho0);
@@ -294,52 +358,49 @@ __device__ __forceinline__ double stress_update_mx(StressIO& s, const float sr[6
     t6[c] = s.tau[c] + (double)(dtf * (twoG * dev + srt + rs));
   }
   float d01 = sr[0] - sr[1], d12 = sr[1] - sr[2], d20 = sr[2] - sr[0];
-  float esr = sqrtf(0.5f * (d01 * d01 + d12 * d12 + d20 * d20) + 3.0f * (sr[3] * sr[3] + sr[5] * sr[5] + sr[4] * sr[4]));
-  s.esr = esr;
+  s.esr = sqrtf(0.5f * (d01 * d01 + d12 * d12 + d20 * d20) + 3.0f * (sr[3] * sr[3] + sr[5] * sr[5] + sr[4] * sr[4]));
   double dep = 0.0;
   if (fail == 1) {
     double J2 = 0.5 * (t6[0] * t6[0] + 2.0 * t6[3] * t6[3] + 2.0 * t6[4] * t6[4] + t6[1] * t6[1] +
                        2.0 * t6[5] * t6[5] + t6[2] * t6[2]);
-    double sig_trial = sqrt(3.0 * J2);
-    double ratio = s.sigmay / sig_trial;
-    double sc = (1.0 < ratio) ? 1.0 : ratio;  // std::min(ratio, 1.0)
-    if (sc != 1.0)
-      for (int c = 0; c < 6; ++c) t6[c] = sc * t6[c];
+    double tJ2 = 3.0 * J2;
+    double sig_trial = -1.0;  // sqrt(3 J2), formed on demand
+    double sy = s.sigmay;
+    if (!(sy > 0.0 && tJ2 <= sy * sy)) {
+      sig_trial = sqrt(tJ2);
+      double ratio = sy / sig_trial;
+      double sc = (1.0 < ratio) ? 1.0 : ratio;  // std::min(ratio, 1.0)
+      if (sc != 1.0)
+        for (int c = 0; c < 6; ++c) t6[c] = sc * t6[c];
+    }
     if (model == 1 && M) {
       if (s.pl_strain + M->eps0 > M->eps1) s.sigmay = (double)((float)M->K * powf((float)(s.pl_strain + M->eps0), (float)M->m));
       else s.sigmay = M->sy0;
     } else if (model == 2 && M) {
       float Th = (float)((T - M->T_t) / (M->T_m - M->T_t));
       float f = 1.0f;
-      if (esr > (float)M->eps_0) f = 1.0f + (float)M->C * logf(esr / (float)M->eps_0);
+      if (s.esr > (float)M->eps_0) f = 1.0f + (float)M->C * logf(s.esr / (float)M->eps_0);
       s.sigmay = (double)(((float)M->A + (float)M->B * powf((float)s.pl_strain, (float)M->n)) * f *
                           (1.0f - powf(Th, (float)M->jm)));
     }
-    if (sig_trial > s.sigmay) {
-      if (s.Ep < 0) s.Ep = M ? M->E : 0.0;
-      dep = (sig_trial - s.sigmay) / (3. * G + s.Ep);
-      s.pl_strain += dep;
-      s.delta_pl_strain = dep;
-      if (model == 0) s.sigmay += dep * s.Ep;
+    sy = s.sigmay;
+    if (!(sy > 0.0 && tJ2 <= sy * sy)) {
+      if (sig_trial < 0.0) sig_trial = sqrt(tJ2);
+      if (sig_trial > sy) {
+        if (s.Ep < 0) s.Ep = M ? M->E : 0.0;
+        dep = (sig_trial - sy) / (3. * G + s.Ep);
+        s.pl_strain += dep;
+        s.delta_pl_strain = dep;
+        if (model == 0) s.sigmay += dep * s.Ep;
+      }
     }
   }
   for (int c = 0; c < 6; ++c) s.tau[c] = t6[c];
   for (int c = 0; c < 6; ++c) s.sig[c] = (c < 3 ? -s.pressure : 0.0) + t6[c];
-  if (dep > 0.0) {
-    double f = dep / s.sigmay;
-    s.epli[0] = f * (s.sig[0] - 0.5 * (s.sig[1] + s.sig[2]));
-    s.epli[1] = f * (s.sig[1] - 0.5 * (s.sig[0] + s.sig[2]));
-    s.epli[2] = f * (s.sig[2] - 0.5 * (s.sig[0] + s.sig[1]));
-    s.epli[3] = 1.5 * f * s.sig[3];
-    s.epli[4] = 1.5 * f * s.sig[4];
-    s.epli[5] = 1.5 * f * s.sig[5];
-    for (int c = 0; c < 6; ++c) s.epl[c] = s.epl[c] + s.epli[c];
-  }
-  for (int c = 0; c < 6; ++c) s.eps[c] = dt * (double)sr[c] + s.eps[c];
   return dep;
 }
 
-__global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K) {
+__global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K) {
   __shared__ double sh[32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
@@ -355,9 +416,11 @@ __global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K) {
     colw(P, C_MRHO, N, i) = col(P, C_MRHON, N, i);
     const float4* rn = P.rn + i;
     float4* rc = P.rc + i;
-    float4 nxh = rn[(size_t)RN_XH * N], nxl = rn[(size_t)RN_XL * N], nvh = rn[(size_t)RN_VH * N], nvl = rn[(size_t)RN_VL * N], ne = rn[(size_t)RN_E * N];
-    rc[(size_t)RC_XH * N] = nxh; rc[(size_t)RC_XL * N] = nxl; rc[(size_t)RC_VH * N] = nvh; rc[(size_t)RC_VL * N] = nvl;
-    float4 s1 = rc[(size_t)RC_S1 * N];
+    rc[(size_t)RC_XH * N] = rn[(size_t)RN_XH * N];
+    rc[(size_t)RC_XL * N] = rn[(size_t)RN_XL * N];
+    rc[(size_t)RC_VH * N] = rn[(size_t)RN_VH * N];
+    rc[(size_t)RC_VL * N] = rn[(size_t)RN_VL * N];
+    float4 ne = rn[(size_t)RN_E * N];
     float4 misc = rc[(size_t)RC_MISC * N];
     maxpl = col(P, C_PLS, N, i);
     dkin = col(P, C_DKIN, N, i);
@@ -365,23 +428,45 @@ __global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K) {
       float sr[6], rr[3];
       for (int c = 0; c < 6; ++c) sr[c] = P.rates[(size_t)c * N + i];
       for (int c = 0; c < 3; ++c) rr[c] = P.rates[(size_t)(6 + c) * N + i];
-      StressIO s;
-      for (int c = 0; c < 6; ++c) {
-        s.tau[c] = col(P, C_TAU + c, N, i); s.eps[c] = col(P, C_EPS + c, N, i);
-        s.epl[c] = col(P, C_EPL + c, N, i); s.epli[c] = col(P, C_EPLI + c, N, i);
-      }
+      StressMx s;
+      for (int c = 0; c < 6; ++c) s.tau[c] = col(P, C_TAU + c, N, i);
       s.pl_strain = col(P, C_PLS, N, i); s.delta_pl_strain = col(P, C_DPLS, N, i);
       s.sigmay = col(P, C_SY, N, i); s.Ep = col(P, C_EP, N, i);
       int mi = icol(P, I_MAT, N, i);
       const MaterialDev* Mt = (mi >= 0 && mi < P.tab->nmat) ? &P.tab->mat[mi] : nullptr;
       double T = col(P, C_T, N, i);
-      stress_update_mx(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i),
-                       col(P, C_G, N, i), T, icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), Mt, dt);
+      double dep = stress_update_mx(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i),
+                                    col(P, C_G, N, i), T, icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), Mt, dt);
+      for (int c = 0; c < 6; ++c) {
+        colw(P, C_TAU + c, N, i) = s.tau[c];
+        colw(P, C_SIG + c, N, i) = s.sig[c];
+        colw(P, C_EPS + c, N, i) = dt * (double)sr[c] + col(P, C_EPS + c, N, i);
+      }
+      // Strain_pl_incr = dep / sigma_y (sigma - tr-free part) and Strain_pl += it
+      // (Particle.cpp:1040-1058); kept from the last plastic step otherwise.
+      double epli[6];
+      if (dep > 0.0) {
+        double f = dep / s.sigmay;
+        epli[0] = f * (s.sig[0] - 0.5 * (s.sig[1] + s.sig[2]));
+        epli[1] = f * (s.sig[1] - 0.5 * (s.sig[0] + s.sig[2]));
+        epli[2] = f * (s.sig[2] - 0.5 * (s.sig[0] + s.sig[1]));
+        epli[3] = 1.5 * f * s.sig[3];
+        epli[4] = 1.5 * f * s.sig[4];
+        epli[5] = 1.5 * f * s.sig[5];
+        for (int c = 0; c < 6; ++c) {
+          colw(P, C_EPLI + c, N, i) = epli[c];
+          colw(P, C_EPL + c, N, i) = col(P, C_EPL + c, N, i) + epli[c];
+        }
+      }
       double srd[6];
       for (int c = 0; c < 6; ++c) srd[c] = (double)sr[c];
       if (K.pl_heating) {
         double q = col(P, C_QPL, N, i);
-        if (s.delta_pl_strain > 0.0) q = plastic_heat(s.sig, s.epli, dt);
+        if (s.delta_pl_strain > 0.0) {
+          if (!(dep > 0.0))
+            for (int c = 0; c < 6; ++c) epli[c] = col(P, C_EPLI + c, N, i);
+          q = plastic_heat(s.sig, epli, dt);
+        }
         colw(P, C_QPL, N, i) = q;
         colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + q * dt;
         plw = col(P, C_MASS, N, i) / rho * q;
@@ -396,22 +481,19 @@ __global__ void __launch_bounds__(BLOCK) k_stress_mx(DevPtrs P, DomainConst K) {
         double st = col(P, C_THEXP, N, i) * dTdt;  // CalcThermalExpStrainRate
         for (int c = 0; c < 3; ++c) srd[c] = srd[c] + st;
       }
-      for (int c = 0; c < 6; ++c) {
-        colw(P, C_TAU + c, N, i) = s.tau[c]; colw(P, C_SIG + c, N, i) = s.sig[c];
-        colw(P, C_EPS + c, N, i) = s.eps[c]; colw(P, C_EPL + c, N, i) = s.epl[c];
-        colw(P, C_EPLI + c, N, i) = s.epli[c]; colw(P, C_SR + c, N, i) = srd[c];
-      }
+      for (int c = 0; c < 6; ++c) colw(P, C_SR + c, N, i) = srd[c];
       for (int c = 0; c < 3; ++c) colw(P, C_RR + c, N, i) = (double)rr[c];
       colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
-      colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = s.esr;
+      colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = (double)s.esr;
       maxpl = s.pl_strain;
       // CalcIntEnergyEqn (Particle.cpp:941-950)
       dint = col(P, C_MRHO, N, i) * (s.tau[0] * srd[0] + 2.0 * s.tau[3] * srd[3] + 2.0 * s.tau[4] * srd[4] +
                                      s.tau[1] * srd[1] + 2.0 * s.tau[5] * srd[5] + s.tau[2] * srd[2]);
       colw(P, C_DINT, N, i) = dint;
       float c2 = 1.0f / ((float)rho * (float)rho);
+      float s1w = rc[(size_t)RC_S1 * N].w;
       rc[(size_t)RC_S0 * N] = make_float4(c2 * (float)s.sig[0], c2 * (float)s.sig[1], c2 * (float)s.sig[2], c2 * (float)s.sig[3]);
-      rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], c2 * (float)s.pressure, s1.w);
+      rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], c2 * (float)s.pressure, s1w);
     }
     rc[(size_t)RC_MISC * N] = make_float4(misc.x, misc.y, misc.z, ne.z);
     rc[(size_t)RC_T2 * N] = make_float4(ne.w, 0.f, 0.f, 0.f);
@@ -433,23 +515,46 @@ void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, c
   mark(s, "k_refresh_records");
 }
 
+__global__ void k_zero_cursors(int* c, int n) {
+  for (int k = threadIdx.x; k < n; k += blockDim.x) c[k] = 0;
+}
+
+// Blocks of a persistent launch: resident blocks per SM x SMs, at most `cap`.
+static int persistent_grid(const void* fn, int block, int sms, int cap) {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0) != cudaSuccess || per < 1) per = 1;
+  long long g = (long long)per * sms;
+  return (int)(g < cap ? g : cap);
+}
+
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
   int nb = nblk(K.N, BLOCK);
   int gb = (K.gblock == 64 || K.gblock == 128 || K.gblock == 512) ? K.gblock : 256;
   int ng = nblk(K.N, gb);
+  int ga = ng, gd = ng, gr = ng;
+  if (K.gsched) {  // persistent: the resident blocks of every SM, capped at one tile each
+    const void* fa = K.ti ? (const void*)k_accel_mx<true> : (const void*)k_accel_mx<false>;
+    ga = persistent_grid(fa, gb, K.nchunks, ng);
+    gd = persistent_grid((const void*)k_density_drift_mx, gb, K.nchunks, ng);
+    gr = persistent_grid((const void*)k_rate_mx, gb, K.nchunks, ng);
+  }
   launch_step_head(P, K, fscratch, iscratch, s);
   launch_refresh_shadows(P, K, 0, s);
   launch_tensile(P, K, s);
-  if (K.ti) k_accel_mx<true><<<ng, gb, 0, s>>>(P, K);
-  else k_accel_mx<false><<<ng, gb, 0, s>>>(P, K);
+  if (K.gsched) {
+    k_zero_cursors<<<1, 512, 0, s>>>(P.tile_ctr, GATHER_KERNELS * K.nchunks);
+    mark(s, "k_zero_cursors");
+  }
+  if (K.ti) k_accel_mx<true><<<ga, gb, 0, s>>>(P, K);
+  else k_accel_mx<false><<<ga, gb, 0, s>>>(P, K);
   mark(s, "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
-  k_density_drift_mx<<<ng, gb, 0, s>>>(P, K);
+  k_density_drift_mx<<<gd, gb, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  k_rate_mx<<<ng, gb, 0, s>>>(P, K);
+  k_rate_mx<<<gr, gb, 0, s>>>(P, K);
   mark(s, "k_rate_mx");
   k_stress_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_stress_mx");
