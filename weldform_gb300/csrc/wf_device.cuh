@@ -167,6 +167,7 @@ struct DomainConst {
   int CellNo[3];
   int ncells;
   float pre_eps;       // relative margin of the FP32 neighbour prefilter
+  double cell_skip_r2; // (Cellfac * hmax)^2 (1 + 1e-6): cells farther than this hold no neighbour
   int ts_nb_inc, pl_heating, thermal_solver, contact, contact_mesh_auto_update, contact_alg;
   double pl_work_heat_frac, friction_sta, friction_dyn, PFAC, DFAC;
   double totmass_mean;

@@ -543,6 +543,7 @@ struct wf_domain {
     // Constants.
     K.N = N; K.Nsolid = solid_part_count; K.nbc_particles = (int)bl.size();
     K.Cellfac = Cellfac; K.hmax = hmax; K.dt = dt;
+    K.cell_skip_r2 = (Cellfac * hmax) * (Cellfac * hmax) * (1.0 + 1e-6);
     for (int d = 0; d < 3; ++d) { K.BLPF[d] = BLPF[d]; K.CellSize[d] = cs[d]; K.CellNo[d] = CellNo[d]; }
     K.ncells = (int)ncells;
     double ext = 0;

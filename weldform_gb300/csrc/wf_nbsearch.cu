@@ -275,13 +275,29 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     const int* cls = P.i + I_CELL * N;
     // Lane c < 27 fetches the range of neighbour cell c; a warp scan of the
     // counts flattens the candidates so all lanes work on every iteration.
+    // A cell whose box lies farther from x_i than the largest pair radius
+    // Cellfac * hmax holds no neighbour and is left out (about a quarter of
+    // the candidates: most corner and some edge cells).  Boxes of the
+    // outermost cells extend to infinity outwards, since the cell index is
+    // clamped there.
     int cs = 0, cc = 0;
     if (lane < 27) {
-      int a = c[0] + lane / 9 - 1, b = c[1] + (lane / 3) % 3 - 1, e = c[2] + lane % 3 - 1;
-      if (a >= 0 && a < K.CellNo[0] && b >= 0 && b < K.CellNo[1] && e >= 0 && e < K.CellNo[2]) {
-        int key = P.cell_rank[(a * K.CellNo[1] + b) * K.CellNo[2] + e];
-        cs = P.cell_start[key];
-        cc = P.cell_start[key + 1] - cs;
+      int q3[3] = {c[0] + lane / 9 - 1, c[1] + (lane / 3) % 3 - 1, c[2] + lane % 3 - 1};
+      if (q3[0] >= 0 && q3[0] < K.CellNo[0] && q3[1] >= 0 && q3[1] < K.CellNo[1] && q3[2] >= 0 && q3[2] < K.CellNo[2]) {
+        double g2 = 0.0;
+        for (int d = 0; d < 3; ++d) {
+          double x = P.f[(C_X + d) * N + i];
+          double g = 0.0;
+          if (q3[d] > 0 && x < K.BLPF[d] + q3[d] * K.CellSize[d]) g = K.BLPF[d] + q3[d] * K.CellSize[d] - x;
+          if (q3[d] < K.CellNo[d] - 1 && x > K.BLPF[d] + (q3[d] + 1) * K.CellSize[d])
+            g = x - (K.BLPF[d] + (q3[d] + 1) * K.CellSize[d]);
+          g2 += g * g;
+        }
+        if (g2 <= K.cell_skip_r2) {
+          int key = P.cell_rank[(q3[0] * K.CellNo[1] + q3[1]) * K.CellNo[2] + q3[2]];
+          cs = P.cell_start[key];
+          cc = P.cell_start[key + 1] - cs;
+        }
       }
     }
     int incl = cc;

@@ -52,6 +52,18 @@ __device__ __forceinline__ void rec_set_v(const DevPtrs& P, size_t N, int i, int
   else { rc_f(P, N, i, RC_VH)[d] = h; rc_f(P, N, i, RC_VL)[d] = l; }
 }
 
+// The current velocity record of particle i from its three FP64 components,
+// written as whole 16-byte groups (the .w fields carried over).
+__device__ __forceinline__ void rec_set_v3(const DevPtrs& P, size_t N, int i, const double v[3]) {
+  float4* r = P.rc + i;
+  float4 h = r[(size_t)RC_VH * N], l = r[(size_t)RC_VL * N];
+  ff_split(v[0], h.x, l.x);
+  ff_split(v[1], h.y, l.y);
+  ff_split(v[2], h.z, l.z);
+  r[(size_t)RC_VH * N] = h;
+  r[(size_t)RC_VL * N] = l;
+}
+
 // Amplitude lookup (SPH::amplitude::getValAtTime, Source/Domain.h:69-89).
 __device__ __forceinline__ double amp_value(const DomainTables* T, int amp_id, double t, bool* found) {
   for (int k = 0; k < T->namp; ++k) {

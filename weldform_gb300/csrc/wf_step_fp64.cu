@@ -279,20 +279,26 @@ __global__ void k_bc(DevPtrs P, DomainConst K, int vcol) {
 __device__ __forceinline__ double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 __device__ __forceinline__ double norm3(const double a[3]) { return sqrt(dot3(a, a)); }
 
+// NM: per-mesh force accumulators a thread keeps — 0 without contact, 1 with
+// one rigid mesh (kept in registers), MAX_MESHES with several (indexed by the
+// pair's mesh, so they live in local memory).
+template <int NM>
 __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K) {
   __shared__ double sh[32];
+  constexpr bool CONTACT = NM > 0;
+  constexpr int NV = NM > 0 ? NM : 1;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
   double dt = K.dt;
   double cfsum = 0, crsum = 0, extw = 0;
-  double cfv[MAX_MESHES][3];
-  for (int m = 0; m < MAX_MESHES; ++m) cfv[m][0] = cfv[m][1] = cfv[m][2] = 0.0;
+  double cfv[NV][3];
+  for (int m = 0; m < NV; ++m) cfv[m][0] = cfv[m][1] = cfv[m][2] = 0.0;
   if (i < K.N) {
     int kind = icol(P, I_KIND, N, i);
     double a[3] = {col(P, C_A, N, i), col(P, C_A + 1, N, i), col(P, C_A + 2, N, i)};
     if (P.tx)
       for (int d = 0; d < 3; ++d) P.tx[(size_t)(TX_APRE + d) * N + i] = a[d];
-    if (K.contact) {
+    if (CONTACT) {
       double cf[3] = {0, 0, 0}, dcont = 0.0;
       int ncp = kind == 0 ? P.cp_len[i] : 0;
       if (ncp > 0) {
@@ -357,7 +363,8 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
             }
           }
           cfsum += norm3(cf);
-          if (m < MAX_MESHES) for (int d = 0; d < 3; ++d) cfv[m][d] += cf[d];
+          if (NM == 1) for (int d = 0; d < 3; ++d) cfv[0][d] += cf[d];  // the only mesh
+          else if (m < NV) for (int d = 0; d < 3; ++d) cfv[m][d] += cf[d];
           crsum += dot3(a, n2) * m1;
           extw += dot3(cf, v2);
         }
@@ -374,19 +381,20 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
           if (K.mixed) rec_set_v(P, N, i, d, vn, false);
         }
     } else if (kind == 0) {  // half kick v += a * 0.5 * dt (rigid-mesh particles have a = 0)
+      double vn[3];
       for (int d = 0; d < 3; ++d) {
-        double vn = col(P, C_V + d, N, i) + a[d] * 0.5 * dt;
-        colw(P, C_V + d, N, i) = vn;
-        if (K.mixed) rec_set_v(P, N, i, d, vn, false);
+        vn[d] = col(P, C_V + d, N, i) + a[d] * 0.5 * dt;
+        colw(P, C_V + d, N, i) = vn[d];
       }
+      if (K.mixed) rec_set_v3(P, N, i, vn);
     }
   }
-  if (K.contact) {
+  if (CONTACT) {
     double r;
     r = block_reduce<0>(cfsum, sh); if (threadIdx.x == 0) P.partials[S_CFSUM * K.nblocks + blockIdx.x] = r;
     r = block_reduce<0>(crsum, sh); if (threadIdx.x == 0) P.partials[S_CRSUM * K.nblocks + blockIdx.x] = r;
     r = block_reduce<0>(extw, sh); if (threadIdx.x == 0) P.partials[S_EXTW * K.nblocks + blockIdx.x] = r;
-    for (int m = 0; m < K.nmeshes && m < MAX_MESHES; ++m)
+    for (int m = 0; m < K.nmeshes && m < NV; ++m)
       for (int d = 0; d < 3; ++d) {
         r = block_reduce<0>(cfv[m][d], sh);
         if (threadIdx.x == 0) P.partials[(S_CFVEC + 3 * m + d) * K.nblocks + blockIdx.x] = r;
@@ -818,7 +826,9 @@ void launch_bc(const DevPtrs& P, const DomainConst& K, int vcol, cudaStream_t s)
   mark(s, "k_bc");
 }
 void launch_contact_kick(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
-  k_contact_kick<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  if (!K.contact) k_contact_kick<0><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  else if (K.nmeshes == 1) k_contact_kick<1><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  else k_contact_kick<MAX_MESHES><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
   mark(s, "k_contact_kick");
   if (K.leapfrog) {  // GeneralAfter, then the full kick (the caller's next BC pass follows)
     launch_bc(P, K, C_V, s);
