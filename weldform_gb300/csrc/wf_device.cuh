@@ -167,7 +167,8 @@ struct DomainConst {
   int CellNo[3];
   int ncells;
   float pre_eps;       // relative margin of the FP32 neighbour prefilter
-  double cell_skip_r2; // (Cellfac * hmax)^2 (1 + 1e-6): cells farther than this hold no neighbour
+  float cell_skip_r2;  // (Cellfac * hmax + FP32 rounding margin)^2: cells farther hold no neighbour
+  float BLPFf[3], CellSizef[3];  // FP32 copies of the grid origin and cell size
   int ts_nb_inc, pl_heating, thermal_solver, contact, contact_mesh_auto_update, contact_alg;
   double pl_work_heat_frac, friction_sta, friction_dyn, PFAC, DFAC;
   double totmass_mean;

@@ -543,8 +543,19 @@ struct wf_domain {
     // Constants.
     K.N = N; K.Nsolid = solid_part_count; K.nbc_particles = (int)bl.size();
     K.Cellfac = Cellfac; K.hmax = hmax; K.dt = dt;
-    K.cell_skip_r2 = (Cellfac * hmax) * (Cellfac * hmax) * (1.0 + 1e-6);
     for (int d = 0; d < 3; ++d) { K.BLPF[d] = BLPF[d]; K.CellSize[d] = cs[d]; K.CellNo[d] = CellNo[d]; }
+    {
+      // Largest pair radius plus a margin over the FP32 rounding of positions
+      // (up to the grid's extent) and of the cell bounds formed in FP32.
+      double ext = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        K.BLPFf[d] = (float)BLPF[d];
+        K.CellSizef[d] = (float)cs[d];
+        ext = std::max(ext, std::max(std::fabs(BLPF[d]), std::fabs(BLPF[d] + CellNo[d] * cs[d])));
+      }
+      double r = Cellfac * hmax * (1.0 + 1e-5) + 16.0 * 1.1920929e-7 * ext;
+      K.cell_skip_r2 = (float)(r * r * (1.0 + 1e-5));
+    }
     K.ncells = (int)ncells;
     double ext = 0;
     for (int d = 0; d < 3; ++d) ext = std::max(ext, TRPR[d] - BLPF[d]);

@@ -284,13 +284,15 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     if (lane < 27) {
       int q3[3] = {c[0] + lane / 9 - 1, c[1] + (lane / 3) % 3 - 1, c[2] + lane % 3 - 1};
       if (q3[0] >= 0 && q3[0] < K.CellNo[0] && q3[1] >= 0 && q3[1] < K.CellNo[1] && q3[2] >= 0 && q3[2] < K.CellNo[2]) {
-        double g2 = 0.0;
+        // FP32 (GB300 runs FP64 at 1/64 of the FP32 rate); the radius carries
+        // a margin above the FP32 rounding of positions and cell bounds.
+        const float xf[3] = {pi.x, pi.y, pi.z};
+        float g2 = 0.f;
         for (int d = 0; d < 3; ++d) {
-          double x = P.f[(C_X + d) * N + i];
-          double g = 0.0;
-          if (q3[d] > 0 && x < K.BLPF[d] + q3[d] * K.CellSize[d]) g = K.BLPF[d] + q3[d] * K.CellSize[d] - x;
-          if (q3[d] < K.CellNo[d] - 1 && x > K.BLPF[d] + (q3[d] + 1) * K.CellSize[d])
-            g = x - (K.BLPF[d] + (q3[d] + 1) * K.CellSize[d]);
+          float lo = K.BLPFf[d] + (float)q3[d] * K.CellSizef[d], hi = lo + K.CellSizef[d];
+          float g = 0.f;
+          if (q3[d] > 0 && xf[d] < lo) g = lo - xf[d];
+          if (q3[d] < K.CellNo[d] - 1 && xf[d] > hi) g = xf[d] - hi;
           g2 += g * g;
         }
         if (g2 <= K.cell_skip_r2) {
