@@ -545,13 +545,14 @@ struct wf_domain {
     K.Cellfac = Cellfac; K.hmax = hmax; K.dt = dt;
     for (int d = 0; d < 3; ++d) { K.BLPF[d] = BLPF[d]; K.CellSize[d] = cs[d]; K.CellNo[d] = CellNo[d]; }
     {
-      // Largest pair radius plus a margin over the FP32 rounding of positions
-      // (up to the grid's extent) and of the cell bounds formed in FP32.
+      // Largest pair radius plus a margin over the FP32 rounding of the
+      // prefilter coordinates x - BLPF (the grid's extent at most; clamped
+      // particles only sit in the outermost cells, whose boxes are unbounded)
+      // and of the cell bounds formed in FP32.
       double ext = 0.0;
       for (int d = 0; d < 3; ++d) {
-        K.BLPFf[d] = (float)BLPF[d];
         K.CellSizef[d] = (float)cs[d];
-        ext = std::max(ext, std::max(std::fabs(BLPF[d]), std::fabs(BLPF[d] + CellNo[d] * cs[d])));
+        ext = std::max(ext, CellNo[d] * cs[d]);
       }
       double r = Cellfac * hmax * (1.0 + 1e-5) + 16.0 * 1.1920929e-7 * ext;
       K.cell_skip_r2 = (float)(r * r * (1.0 + 1e-5));

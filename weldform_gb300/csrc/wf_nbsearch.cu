@@ -284,17 +284,21 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     if (lane < 27) {
       int q3[3] = {c[0] + lane / 9 - 1, c[1] + (lane / 3) % 3 - 1, c[2] + lane % 3 - 1};
       if (q3[0] >= 0 && q3[0] < K.CellNo[0] && q3[1] >= 0 && q3[1] < K.CellNo[1] && q3[2] >= 0 && q3[2] < K.CellNo[2]) {
-        // FP32 (GB300 runs FP64 at 1/64 of the FP32 rate); the radius carries
-        // a margin above the FP32 rounding of positions and cell bounds.
+        // FP32 on the prefilter coordinates x - BLPF (GB300 runs FP64 at 1/64
+        // of the FP32 rate); the radius carries a margin above the FP32
+        // rounding of those coordinates and of the cell bounds.
         const float xf[3] = {pi.x, pi.y, pi.z};
         float g2 = 0.f;
+        bool inside = true;  // a particle outside the grid (clamped cell) keeps all 27 cells
         for (int d = 0; d < 3; ++d) {
-          float lo = K.BLPFf[d] + (float)q3[d] * K.CellSizef[d], hi = lo + K.CellSizef[d];
+          float lo = (float)q3[d] * K.CellSizef[d], hi = lo + K.CellSizef[d];
           float g = 0.f;
           if (q3[d] > 0 && xf[d] < lo) g = lo - xf[d];
           if (q3[d] < K.CellNo[d] - 1 && xf[d] > hi) g = xf[d] - hi;
           g2 += g * g;
+          inside = inside && xf[d] >= 0.f && xf[d] <= (float)K.CellNo[d] * K.CellSizef[d];
         }
+        if (!inside) g2 = 0.f;
         if (g2 <= K.cell_skip_r2) {
           int key = P.cell_rank[(q3[0] * K.CellNo[1] + q3[1]) * K.CellNo[2] + q3[2]];
           cs = P.cell_start[key];
