@@ -46,8 +46,9 @@ enum F64Col : int {
 enum I32Col : int {
   I_ID = 0, I_IDORIG, I_NWS, I_MAT, I_MODEL, I_FAIL, I_MATERIAL, I_NB, I_KIND, I_ELEM, I_MESH, I_ORIG,
   NI32_PERSIST = 12,
-  I_CELL = 12,             // scratch: cell key
-  NI32 = 13
+  I_CELL = 12,             // scratch: cell key (Morton rank) of the particle at its pre-search position
+  I_CLASS = 13,            // scratch: pair-rule class word in sorted order
+  NI32 = 14
 };
 
 // ---- float4 field groups of the mixed form -----------------------------------
@@ -198,6 +199,7 @@ struct DevPtrs {
   StepState* st;
   const DomainTables* tab;
   const int* cell_rank;   // linear cell -> Morton rank
+  const int* cell_lin;    // Morton rank -> linear cell
   int* cell_start;        // ncells + 1
   int* cell_count;        // ncells (histogram / cursor)
   int* perm;              // new sorted position -> old sorted position

@@ -454,6 +454,14 @@ struct wf_domain {
     int* crank = dalloc<int>(ncells);
     CK(cudaMemcpyAsync(crank, rank.data(), sizeof(int) * ncells, cudaMemcpyHostToDevice, stream));
     P.cell_rank = crank;
+    {
+      std::vector<int> lin(ncells);
+      for (size_t c = 0; c < (size_t)ncells; ++c) lin[rank[c]] = (int)c;
+      int* clin = dalloc<int>(ncells);
+      CK(cudaMemcpyAsync(clin, lin.data(), sizeof(int) * ncells, cudaMemcpyHostToDevice, stream));
+      CK(cudaStreamSynchronize(stream));  // the host vector dies at the end of this scope
+      P.cell_lin = clin;
+    }
     P.cell_start = dalloc<int>(ncells + 1);
     P.cell_count = dalloc<int>(ncells);
     P.perm = dalloc<int>(n);

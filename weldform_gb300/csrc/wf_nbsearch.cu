@@ -195,9 +195,8 @@ __global__ void k_after_permute(DevPtrs P, DomainConst K) {
       make_float4((float)(P.f[(C_X + 0) * N + p] - K.BLPF[0]), (float)(P.f[(C_X + 1) * N + p] - K.BLPF[1]),
                   (float)(P.f[(C_X + 2) * N + p] - K.BLPF[2]), (float)P.f[C_H * N + p]);
   // class word for the pair rules: bit 0 rigid-mesh particle, bit 1 carries a
-  // contact-surface id, bits 2.. material index (the cell-key scratch column is
-  // free once the particles are scattered)
-  P.i[I_CELL * N + p] = kind | (is_contact_id(K, P.i[I_ID * N + p]) ? 2 : 0) | (P.i[I_MATERIAL * N + p] << 2);
+  // contact-surface id, bits 2.. material index
+  P.i[I_CLASS * N + p] = kind | (is_contact_id(K, P.i[I_ID * N + p]) ? 2 : 0) | (P.i[I_MATERIAL * N + p] << 2);
   }
 }
 
@@ -265,14 +264,14 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   bool overflow = false;
   if (i < K.N && kind[i] == 0) {
     float4 pi = reinterpret_cast<const float4*>(P.xs)[i];
-    int c[3];
-    for (int d = 0; d < 3; ++d) {
-      int q = (int)floor(__ddiv_rn(__dsub_rn(P.f[(C_X + d) * N + i], K.BLPF[d]), K.CellSize[d]));
-      c[d] = q < 0 ? 0 : (q >= K.CellNo[d] ? K.CellNo[d] - 1 : q);
-    }
+    // The particle's cell: the key it was sorted by (k_cell_keys evaluated the
+    // reference's FP64 cell formula once per particle), mapped back to grid
+    // coordinates.
+    int lin = P.cell_lin[P.i[I_CELL * N + P.perm[i]]];
+    int c[3] = {lin / (K.CellNo[1] * K.CellNo[2]), (lin / K.CellNo[2]) % K.CellNo[1], lin % K.CellNo[2]};
     int idi = ID[i], oi = orig[i], mi = material[i];
     bool ci = K.contact && is_contact_id(K, idi);
-    const int* cls = P.i + I_CELL * N;
+    const int* cls = P.i + I_CLASS * N;
     // Lane c < 27 fetches the range of neighbour cell c; a warp scan of the
     // counts flattens the candidates so all lanes work on every iteration.
     // A cell whose box lies farther from x_i than the largest pair radius
