@@ -228,6 +228,75 @@ def cpu_baseline(steps=2):
                       f"(search) step, reference-structured OpenMP restatement, {threads} threads"}
 
 
+def _oracle_lib():
+    import ctypes
+    import __graft_entry__ as ge
+    import weldform_gb300 as wf
+    path = os.path.join(ge.ORACLE_BUILD, "libwf_oracle.so")
+    if not os.path.exists(path):
+        ge.build_oracle()
+    return wf.bind(ctypes.CDLL(path), "wfo_")
+
+
+def config_table(gpu=0):
+    """Throughput of every synthetic configuration of the path: the plain FP64
+    and mixed GPU forms (CUDA-graph steps between CUDA events, after the
+    first step's search) and the reference-structured CPU restatement on all
+    host threads and on one thread (bounded samples of steady steps).  One
+    JSON object; rows in the order of the configurations."""
+    import weldform_gb300 as wfmod
+    from weldform_gb300 import configs
+    lib = _oracle_lib()
+    threads = os.cpu_count() or 1
+
+    def cyl(dx):
+        return lambda d: configs.cylinder_upsetting(d, R=R, L=L, dx=dx, v_top=-1.0)
+
+    def contact(d):
+        return configs.contact_upsetting(d, R=R, L=L, dx=0.2e-3, v_punch=-1.0, stiffness="area")
+
+    # (name, builder, GPU FP64 steps, GPU mixed steps, CPU all-thread steps, CPU one-thread steps)
+    rows_in = [
+        ("1: elastoplastic cylinder dx=1mm, bilinear", cyl(1e-3), 1000, 1000, 200, 20),
+        ("2: JC + conduction + penalty-contact plane (0.1E/h) dx=0.2mm, mu=0.2", contact, 50, 200, 2, 1),
+        ("3: cylinder dx=0.3353mm", cyl(0.3353e-3), 50, 200, 4, 1),
+        ("3: cylinder dx=0.2112mm", cyl(0.2112e-3), 20, 100, 2, 1),
+        ("3: cylinder dx=0.1331mm", cyl(0.1331e-3), 10, 50, 1, 0),
+    ]
+    out = []
+    for name, build, s64, smx, scpu, s1 in rows_in:
+        row = {"config": name}
+        for form, prec, steps in (("gpu_fp64", wfmod.PRECISION_FP64, s64), ("gpu_mixed", wfmod.PRECISION_MIXED, smx)):
+            d = wfmod.Domain()
+            d.set("device", gpu)
+            d.set("precision", prec)
+            case = build(d)
+            d.prepare(case.dt)
+            d.step(3)
+            ms, _ = d.step_timed(steps)
+            row["particles"] = case.n
+            row[form] = {"particle_steps_s": case.n * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                         "steps": steps}
+            d.close()
+        for form, nthr, steps in (("cpu_all_threads", threads, scpu), ("cpu_one_thread", 1, s1)):
+            if steps <= 0:
+                continue
+            d = wfmod.Domain(lib=lib, prefix="wfo_")
+            d.set("cpu_mode", 1)
+            d.set("cpu_threads", nthr)
+            case = build(d)
+            d.prepare(case.dt)
+            d.step(1)
+            ms, _ = d.step_timed(steps)
+            row[form] = {"particle_steps_s": case.n * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                         "steps": steps, "threads": nthr}
+            d.close()
+        row["mixed_over_fp64"] = row["gpu_mixed"]["particle_steps_s"] / row["gpu_fp64"]["particle_steps_s"]
+        out.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+    return {"table": out, "cpu_kind": "port (reference-structured OpenMP restatement)", "cpu_threads": threads}
+
+
 def adjoint_leg(wfmod, steps=400, every=10, k=20):
     """Reaction-force adjoint on the 53,352-particle penalty-contact workload
     (R = 10 mm, L = 30 mm, dx = 0.55 mm, JC + conduction + plastic heating,
@@ -291,7 +360,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--config-table", action="store_true",
+                    help="time every configuration (GPU forms and CPU restatement) and print one JSON table")
     a = ap.parse_args()
+    if a.config_table:
+        print(json.dumps(config_table()))
+        return
     warmup = max(a.warmup, 3)
     rank, world, local, pg = dist_setup(a.gpus)
 
