@@ -170,6 +170,7 @@ struct DomainConst {
   float pre_eps;       // relative margin of the FP32 neighbour prefilter
   float cell_skip_r2;  // (Cellfac * hmax + FP32 rounding margin)^2: cells farther hold no neighbour
   float CellSizef[3];  // FP32 copy of the cell size
+  float half_cellfac_f;  // 0.5 * Cellfac in FP32 (prefilter radius factor)
   int ts_nb_inc, pl_heating, thermal_solver, contact, contact_mesh_auto_update, contact_alg;
   double pl_work_heat_frac, friction_sta, friction_dyn, PFAC, DFAC;
   double totmass_mean;

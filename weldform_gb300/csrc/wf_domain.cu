@@ -564,6 +564,7 @@ struct wf_domain {
       }
       double r = Cellfac * hmax * (1.0 + 1e-5) + 16.0 * 1.1920929e-7 * ext;
       K.cell_skip_r2 = (float)(r * r * (1.0 + 1e-5));
+      K.half_cellfac_f = (float)K.Cellfac * 0.5f;
     }
     K.ncells = (int)ncells;
     double ext = 0;

@@ -218,7 +218,7 @@ __device__ __forceinline__ bool radius_ok(const DevPtrs& P, const DomainConst& K
                                           float yi, float zi, float hi, float4 pj) {
   float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
   float d2 = dx * dx + dy * dy + dz * dz;
-  float R = (float)K.Cellfac * 0.5f * (hi + pj.w);
+  float R = K.half_cellfac_f * (hi + pj.w);
   float R2 = R * R;
   if (d2 < R2 * (1.0f - K.pre_eps)) return true;
   if (d2 > R2 * (1.0f + K.pre_eps)) return false;
@@ -243,23 +243,32 @@ __device__ __forceinline__ void rank_row(const unsigned* row, int n4, const unsi
   }
 }
 
-constexpr int FILL_WARPS = 32;
+constexpr int FILL_WARPS = 8;                    // warps per block
+constexpr int FILL_ROWS = 32;                    // particles (rows) per block group
+constexpr int FILL_PER_WARP = FILL_ROWS / FILL_WARPS;
 constexpr int FILL_SLOTS = 128;
 __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  __shared__ __align__(16) unsigned s_key[FILL_WARPS][FILL_SLOTS];
-  __shared__ int s_idx[FILL_WARPS][FILL_SLOTS];
-  __shared__ int s_len[FILL_WARPS];
+  __shared__ __align__(16) unsigned s_key[FILL_ROWS][FILL_SLOTS];
+  __shared__ int s_idx[FILL_ROWS][FILL_SLOTS];
+  __shared__ int s_len[FILL_ROWS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   size_t N = K.N;
-  const int ngroups = (K.N + FILL_WARPS - 1) / FILL_WARPS;
-  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-  const int i0 = grp * FILL_WARPS;
-  const int i = i0 + w;
   const int* ID = P.i + I_ID * N;
   const int* orig = P.i + I_ORIG * N;
   const int* kind = P.i + I_KIND * N;
   const int* material = P.i + I_MATERIAL * N;
+  const int* cls = P.i + I_CLASS * N;
+  const int ngroups = (K.N + FILL_ROWS - 1) / FILL_ROWS;
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+  const int i0 = grp * FILL_ROWS;
+  // Each warp builds FILL_PER_WARP consecutive rows, one after the other, so
+  // the block barrier below averages the warps' row costs over several rows.
+  for (int rr = 0; rr < FILL_PER_WARP; ++rr) {
+  const int row = w * FILL_PER_WARP + rr;
+  const int i = i0 + row;
+  unsigned* rkey = &s_key[row][0];
+  int* ridx = &s_idx[row][0];
   int cnt = 0, split = 0;
   bool overflow = false;
   if (i < K.N && kind[i] == 0) {
@@ -271,7 +280,6 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     int c[3] = {lin / (K.CellNo[1] * K.CellNo[2]), (lin / K.CellNo[2]) % K.CellNo[1], lin % K.CellNo[2]};
     int idi = ID[i], oi = orig[i], mi = material[i];
     bool ci = K.contact && is_contact_id(K, idi);
-    const int* cls = P.i + I_CLASS * N;
     // Lane c < 27 fetches the range of neighbour cell c; a warp scan of the
     // counts flattens the candidates so all lanes work on every iteration.
     // A cell whose box lies farther from x_i than the largest pair radius
@@ -341,41 +349,41 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
         int pos = cnt + __popc(m & ((1u << lane) - 1u));
         // stored entry: the index, with bit 31 set when j has the larger
         // original index (P2 of the reference's (min, max) pair)
-        if (pos < FILL_SLOTS) { s_key[w][pos] = kk; s_idx[w][pos] = (int)((unsigned)j | (orig[j] > oi ? NB_UP : 0u)); }
+        if (pos < FILL_SLOTS) { rkey[pos] = kk; ridx[pos] = (int)((unsigned)j | (orig[j] > oi ? NB_UP : 0u)); }
       }
       cnt += __popc(m);
     }
     if (cnt > MAX_NB) overflow = true;
     if (cnt > FILL_SLOTS) cnt = FILL_SLOTS;
   }
-  // Order the warp's slots by key.  Keys are distinct (one per neighbour), so
+  // Order the row's slots by key.  Keys are distinct (one per neighbour), so
   // each entry's final slot is the number of smaller keys: every lane ranks
   // its own (at most four) entries against the whole row, read four keys per
   // broadcast load, then scatters them.  Pads above the row hold the largest
   // key, which no real key reaches (orig[j] - oi - 1 != -1).
   int cnt4 = (cnt + 3) & ~3;
-  for (int e = cnt + lane; e < cnt4; e += 32) s_key[w][e] = 0xffffffffu;
+  for (int e = cnt + lane; e < cnt4; e += 32) rkey[e] = 0xffffffffu;
   __syncwarp();
   const int nk = (cnt + 31) >> 5;  // warp-uniform
   unsigned key[4];
   int idx[4], rank[4] = {0, 0, 0, 0};
   for (int r = 0; r < 4; ++r) {
     int e = lane + 32 * r;
-    key[r] = e < cnt ? s_key[w][e] : 0xffffffffu;
-    idx[r] = e < cnt ? s_idx[w][e] : 0;
+    key[r] = e < cnt ? rkey[e] : 0xffffffffu;
+    idx[r] = e < cnt ? ridx[e] : 0;
   }
-  if (nk <= 2) rank_row<2>(&s_key[w][0], cnt4, key, rank);
-  else rank_row<4>(&s_key[w][0], cnt4, key, rank);
+  if (nk <= 2) rank_row<2>(rkey, cnt4, key, rank);
+  else rank_row<4>(rkey, cnt4, key, rank);
   __syncwarp();
   for (int r = 0; r < 4; ++r)
-    if (lane + 32 * r < cnt) s_idx[w][rank[r]] = idx[r];
+    if (lane + 32 * r < cnt) ridx[rank[r]] = idx[r];
   __syncwarp();
   if (cnt > MAX_NB) cnt = MAX_NB;
   if (i < K.N) {
-    for (int e = lane; e < cnt; e += 32) split += s_idx[w][e] < 0 ? 1 : 0;
+    for (int e = lane; e < cnt; e += 32) split += ridx[e] < 0 ? 1 : 0;
     for (int off = 16; off > 0; off >>= 1) split += __shfl_down_sync(0xffffffffu, split, off);
     if (lane == 0) {
-      s_len[w] = cnt;
+      s_len[row] = cnt;
       P.row_len[i] = cnt;
       P.row_split[i] = split;
       P.i[I_NB * N + i] = cnt;
@@ -384,14 +392,15 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
       atomicAdd(&P.st->pair_count, (unsigned long long)cnt);
     }
   } else if (lane == 0) {
-    s_len[w] = 0;
+    s_len[row] = 0;
   }
+  }  // rows of this warp
   __syncthreads();
   // Block-wide coalesced ELL write: thread (k, t) stores entry k of particle i0 + t.
   int maxlen = 0;
-  for (int t = 0; t < FILL_WARPS; ++t) maxlen = max(maxlen, s_len[t]);
-  for (int q = threadIdx.x; q < maxlen * FILL_WARPS; q += blockDim.x) {
-    int k = q / FILL_WARPS, t = q - k * FILL_WARPS;
+  for (int t = 0; t < FILL_ROWS; ++t) maxlen = max(maxlen, s_len[t]);
+  for (int q = threadIdx.x; q < maxlen * FILL_ROWS; q += blockDim.x) {
+    int k = q / FILL_ROWS, t = q - k * FILL_ROWS;
     if (k < s_len[t]) P.nbr[(size_t)k * N + i0 + t] = s_idx[t][k];
   }
   __syncthreads();  // the shared buffers are reused by the next group
@@ -530,7 +539,11 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   mark(s, "k_copy_back");
   k_after_permute<<<grid(K.N), T, 0, s>>>(P, K);
   mark(s, "k_after_permute");
-  k_nbr_fill<<<nblk(K.N, FILL_WARPS) < 152 ? nblk(K.N, FILL_WARPS) : 152, FILL_WARPS * 32, 0, s>>>(P, K);
+  {
+    // a few resident blocks per SM, striding over the row groups
+    int groups = nblk(K.N, FILL_ROWS), cap = 152 * 4;
+    k_nbr_fill<<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
+  }
   mark(s, "k_nbr_fill");
   if (K.contact) {
     k_surface<<<grid(K.N), T, 0, s>>>(P, K);
