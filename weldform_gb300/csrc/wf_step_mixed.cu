@@ -151,7 +151,6 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   KSum a0, a1, a2;
   int len = P.row_len[i];
   const int* nb = P.nbr + i;
-#pragma unroll 2
   for (int k = 0; k < len; ++k) {
     int j = nb_index(nb[(size_t)k * N]);
     const float4* rj = P.rc + j;
@@ -219,7 +218,6 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
     KSum s;
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
-#pragma unroll 2
     for (int k = 0; k < len; ++k) {
       int j = nb_index(nb[(size_t)k * N]);
       const float4* rj = P.rc + j;
@@ -283,7 +281,6 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
     bool thermal = K.thermal_solver;
-#pragma unroll 2
     for (int k = 0; k < len; ++k) {
       int ent = nb[(size_t)k * N];
       int j = nb_index(ent);
