@@ -44,15 +44,14 @@ DX_1M = 0.2112e-3
 ALG_BYTES = {
     "k_accel": lambda nnz: 144 + 4 * nnz + 4,             # x,v,rho,m,h,Sigma(6) -> a
     "k_density_drift": lambda nnz: 272 + 4 * nnz + 4,     # x,v,a,rho,m,h -> v,rho ; x,v,a -> x,v
-    "k_rate_stress": lambda nnz: 440 + 4 * nnz + 4,       # x,v,rho,m,h,tau,eps,eps_p,pl,sy -> tau,Sigma,...
-    "k_energy": lambda nnz: 88 + 4 * nnz + 4,             # x,v,p,rho,m,h -> dkin ; tau,SR -> dint
+    "k_rate_stress": lambda nnz: 456 + 4 * nnz + 4,       # x,v,rho,m,h,p,tau,eps,eps_p,pl,sy -> tau,Sigma,..,dkin,dint
     "k_accel_mx": lambda nnz: 108 + 4 * nnz + 4,          # ff x,v; f32 rho,m,h,Sigma/rho^2 -> a (f64)
     "k_density_drift_mx": lambda nnz: 336 + 4 * nnz + 4,  # f64 integration; next-step record written
     "k_rate_mx": lambda nnz: 72 + 4 * nnz + 4,            # next record -> 9 rates, dkin, conduction
     "k_stress_mx": lambda nnz: 440,                       # f64 stress state read + written
 }
 # FP64 operations per neighbour entry / per particle (plain form).
-ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (55, 250), "k_energy": (35, 20)}
+ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (70, 270)}
 
 
 def _env_int(k, d):

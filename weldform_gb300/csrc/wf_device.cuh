@@ -41,7 +41,9 @@ enum F64Col : int {
   // scratch columns (not permuted): next-step buffers and the
   // tensile-instability stress TIR (6), recomputed at every step start
   C_XN = 104, C_VN = 107, C_RHON = 110, C_MRHON = 111, C_TIR = 112,
-  NF64 = 118
+  C_PR2N = 118,            // next-step Pressure / Density^2 (plain form; read by the fused rate gather)
+  C_TN = 119,              // next-step temperature (plain form)
+  NF64 = 120
 };
 enum I32Col : int {
   I_ID = 0, I_IDORIG, I_NWS, I_MAT, I_MODEL, I_FAIL, I_MATERIAL, I_NB, I_KIND, I_ELEM, I_MESH, I_ORIG,

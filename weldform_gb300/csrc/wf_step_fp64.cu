@@ -9,13 +9,15 @@
 //   k_contact_kick      CalcContactForcesWang (Contact_Wang.cpp:15-348) + v += a dt/2
 //   k_bc
 //   k_density_drift     CalcDensInc + DensReduction (InteractionAlt.cpp:483-640),
-//                       rho += dt drho, x += v dt, v += a dt/2 (SolverKickDrift.cpp:236-265)
+//                       rho += dt drho, x += v dt, v += a dt/2 (SolverKickDrift.cpp:236-265);
+//                       next-step p/rho^2 and T for the rate gather
 //   k_bc                (on the next-step velocity buffer)
 //   k_rate_stress       CalcRateTensors + RateTensorsReduction (InteractionAlt.cpp:263-479),
 //                       CalcStressStrain (Particle.cpp:960-1067), CalcPlasticWorkHeat
-//                       (ThermalStuct.cpp:14-39), T += dt dTdt (Thermal.cpp:727-734)
-//   k_energy            CalcTempInc (Thermal.cpp:53-219), CalcThermalExpStrainRate,
-//                       CalcKinEnergyEqn / CalcIntEnergyEqn (Domain.cpp:1752-1829)
+//                       (ThermalStuct.cpp:14-39), T += dt dTdt (Thermal.cpp:727-734),
+//                       and in the same neighbour loop CalcTempInc (Thermal.cpp:53-219),
+//                       CalcKinEnergyEqn (Domain.cpp:1752-1808); then CalcThermalExpStrainRate
+//                       and CalcIntEnergyEqn (Domain.cpp:1810-1829)
 //   k_finalize          deterministic reduction of the per-block partial sums
 //   k_mesh_*            TriMesh::Update (Mesh.cpp:273-293), UpdateContactParticles
 //                       (Contact.cpp:41-55)
@@ -440,6 +442,15 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
   double rn = rhoi + dt * dd;
   colw(P, C_RHON, N, i) = rn;
   colw(P, C_MRHON, N, i) = icol(P, I_KIND, N, i) == 0 ? col(P, C_MASS, N, i) / rn : 0.0;
+  // Next-step pressure over density^2 (EOS case 0 of the updated density, the
+  // expression the stress update evaluates) and next-step temperature
+  // (Thermal.cpp:727-734): the fused rate gather reads both for neighbours.
+  {
+    double cs = col(P, C_CS, N, i);
+    double pn = col(P, C_P0, N, i) + (cs * cs) * (rn - col(P, C_RHO0, N, i));
+    colw(P, C_PR2N, N, i) = pn / (rn * rn);
+    if (K.thermal_solver) colw(P, C_TN, N, i) = col(P, C_T, N, i) + dt * col(P, C_DTDT, N, i);
+  }
   double v[3] = {vi0, vi1, vi2}, x[3] = {xi0, xi1, xi2};
   for (int d = 0; d < 3; ++d) {
     double du = v[d] * dt;
@@ -469,7 +480,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
   double dt = K.dt;
-  double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300;
+  double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300, dkin_b = 0.0, dint = 0.0;
   if (i < K.N) {
     // Next-step buffers become the current state for this particle.
     double x[3], v[3];
@@ -482,12 +493,40 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
     if (icol(P, I_KIND, N, i) == 0) {
       double hi = col(P, C_H, N, i);
       double sr[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};
+      // CalcKinEnergyEqn and CalcTempInc pair sums, on the same positions and
+      // velocities as the rates (Domain.cpp:1752-1808, Thermal.cpp:53-219)
+      double dkin = 0.0, cond = 0.0;
+      double massi = col(P, C_MASS, N, i), mrhoi = col(P, C_MRHON, N, i), pri = col(P, C_PR2N, N, i);
+      double Ti = 0.0, ki = 0.0;
+      if (K.thermal_solver) { Ti = col(P, C_TN, N, i); ki = col(P, C_KT, N, i); }
       int len = P.row_len[i];
       for (int k = 0; k < len; ++k) {
-        int j = nb_index(P.nbr[(size_t)k * N + i]);
+        int e = P.nbr[(size_t)k * N + i];
+        int j = nb_index(e);
         PairGeo g = pair_geo(x[0], x[1], x[2], hi, col(P, C_XN, N, j), col(P, C_XN + 1, N, j), col(P, C_XN + 2, N, j),
                              col(P, C_H, N, j));
         double b0 = v[0] - col(P, C_VN, N, j), b1 = v[1] - col(P, C_VN + 1, N, j), b2 = v[2] - col(P, C_VN + 2, N, j);
+        {
+          double dv = b0 * (g.GK * g.x0) + b1 * (g.GK * g.x1) + b2 * (g.GK * g.x2);
+          bool up = nb_up(e);  // original index of j larger than i's
+          // pair (P1 = smaller original index): 0.5 m_P2 (p1/d1^2 + p2/d2^2) v12.(GK x12)
+          double pk = 0.5 * (up ? col(P, C_MASS, N, j) : massi) * (pri + col(P, C_PR2N, N, j)) * dv;
+          dkin += up ? pk : -pk;
+          if (K.thermal_solver) {
+            double kj = col(P, C_KT, N, j);
+            double w = up ? col(P, C_MRHON, N, j) : mrhoi;  // m_P2 / rho_P2 for both ends
+            double gx[3] = {g.GK * g.x0, g.GK * g.x1, g.GK * g.x2};
+            if (K.gradcorr) {  // Mult(gradCorrM_i, GK x_ij) (Thermal.cpp:90-107)
+              double c3[3];
+              for (int q = 0; q < 3; ++q)
+                c3[q] = gx[0] * col(P, C_GCM + 3 * q, N, i) + gx[1] * col(P, C_GCM + 3 * q + 1, N, i) +
+                        gx[2] * col(P, C_GCM + 3 * q + 2, N, i);
+              gx[0] = c3[0]; gx[1] = c3[1]; gx[2] = c3[2];
+            }
+            double dxx = g.x0 * gx[0] + g.x1 * gx[1] + g.x2 * gx[2];
+            cond += w * 4. * (ki * kj) / (ki + kj) * (Ti - col(P, C_TN, N, j)) * dxx / (g.r * g.r);
+          }
+        }
         if (K.gradcorr) {  // locking form: (float)(m_j/rho_j) with v_ij (x) vc_i (InteractionAlt.cpp:330-350, 425-450)
           double gk[3];
           corr_grad(P, N, i, g.GK, g.x0, g.x1, g.x2, gk);
@@ -546,21 +585,37 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
       double c2 = 1.0 / (rho * rho);
       for (int c = 0; c < 6; ++c) colw(P, C_SRHO + c, N, i) = c2 * s.sig[c];
       colw(P, C_PR2, N, i) = s.pressure / (rho * rho);
+      double qpl = col(P, C_QPL, N, i);
       if (K.pl_heating) {
-        double q = col(P, C_QPL, N, i);
-        if (s.delta_pl_strain > 0.0) q = plastic_heat(s.sig, s.epli, dt);
-        colw(P, C_QPL, N, i) = q;
-        colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + q * dt;
-        plw = col(P, C_MASS, N, i) / rho * q;
+        if (s.delta_pl_strain > 0.0) qpl = plastic_heat(s.sig, s.epli, dt);
+        colw(P, C_QPL, N, i) = qpl;
+        colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + qpl * dt;
+        plw = col(P, C_MASS, N, i) / rho * qpl;
       }
+      double sre[6];
+      for (int c = 0; c < 6; ++c) sre[c] = sr[c];
       if (K.thermal_solver) {
         T += dt * col(P, C_DTDT, N, i);
         colw(P, C_T, N, i) = T;
         maxT = T; minT = T;
+        // CalcTempInc's dTdt and CalcThermalExpStrainRate (after the stress)
+        double f = 1. / (rho * col(P, C_CPT, N, i));
+        double dTdt = f * (cond + 0.0 + col(P, C_QSRC, N, i) + qpl * K.pl_work_heat_frac + 0.0);
+        colw(P, C_DTDT, N, i) = dTdt;
+        double st = col(P, C_THEXP, N, i) * dTdt;
+        for (int c = 0; c < 3; ++c) { sre[c] = sre[c] + st; colw(P, C_SR + c, N, i) = sre[c]; }
       }
+      // CalcIntEnergyEqn (Particle.cpp:941-950)
+      dint = mrhoi * (s.tau[0] * sre[0] + 2.0 * s.tau[3] * sre[3] + 2.0 * s.tau[4] * sre[4] + s.tau[1] * sre[1] +
+                      2.0 * s.tau[5] * sre[5] + s.tau[2] * sre[2]);
+      colw(P, C_DKIN, N, i) = dkin;
+      colw(P, C_DINT, N, i) = dint;
+      dkin_b = dkin;
     }
   }
   double r;
+  r = block_reduce<0>(dkin_b, sh); if (threadIdx.x == 0) P.partials[S_DKIN * K.nblocks + blockIdx.x] = r;
+  r = block_reduce<0>(dint, sh); if (threadIdx.x == 0) P.partials[S_DINT * K.nblocks + blockIdx.x] = r;
   r = block_reduce<1>(maxpl, sh); if (threadIdx.x == 0) P.partials[S_MAXPL * K.nblocks + blockIdx.x] = r;
   if (K.pl_heating) { r = block_reduce<0>(plw, sh); if (threadIdx.x == 0) P.partials[S_PLW * K.nblocks + blockIdx.x] = r; }
   if (K.thermal_solver) {
@@ -569,67 +624,6 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
   }
 }
 
-// ---------------------------------------------------------------- energies (+ conduction)
-__global__ void __launch_bounds__(BLOCK) k_energy(DevPtrs P, DomainConst K) {
-  __shared__ double sh[32];
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  size_t N = K.N;
-  double dkin = 0.0, dint = 0.0;
-  if (i < K.N && icol(P, I_KIND, N, i) == 0) {
-    double x0 = col(P, C_X, N, i), x1 = col(P, C_X + 1, N, i), x2 = col(P, C_X + 2, N, i);
-    double v0 = col(P, C_V, N, i), v1 = col(P, C_V + 1, N, i), v2 = col(P, C_V + 2, N, i);
-    double hi = col(P, C_H, N, i), mi = col(P, C_MASS, N, i), mrhoi = col(P, C_MRHO, N, i);
-    double pri = col(P, C_PR2, N, i);
-    double Ti = col(P, C_T, N, i), ki = col(P, C_KT, N, i);
-    double cond = 0.0;
-    int len = P.row_len[i];
-    for (int k = 0; k < len; ++k) {
-      int e = P.nbr[(size_t)k * N + i];
-      int j = nb_index(e);
-      PairGeo g = pair_geo(x0, x1, x2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
-                           col(P, C_H, N, j));
-      double b0 = v0 - col(P, C_V, N, j), b1 = v1 - col(P, C_V + 1, N, j), b2 = v2 - col(P, C_V + 2, N, j);
-      double dv = b0 * (g.GK * g.x0) + b1 * (g.GK * g.x1) + b2 * (g.GK * g.x2);
-      bool up = nb_up(e);  // original index of j larger than i's
-      // CalcKinEnergyEqn pair (P1 = smaller original index): 0.5 m_P2 (p1/d1^2 + p2/d2^2) v12.(GK x12)
-      double pk = 0.5 * (up ? col(P, C_MASS, N, j) : mi) * (pri + col(P, C_PR2, N, j)) * dv;
-      dkin += up ? pk : -pk;
-      if (K.thermal_solver) {
-        double kj = col(P, C_KT, N, j);
-        double w = up ? col(P, C_MRHO, N, j) : mrhoi;  // m_P2 / rho_P2 for both ends
-        double gx[3] = {g.GK * g.x0, g.GK * g.x1, g.GK * g.x2};
-        if (K.gradcorr) {  // Mult(gradCorrM_i, GK x_ij) (Thermal.cpp:90-107)
-          double c3[3];
-          for (int q = 0; q < 3; ++q)
-            c3[q] = gx[0] * col(P, C_GCM + 3 * q, N, i) + gx[1] * col(P, C_GCM + 3 * q + 1, N, i) +
-                    gx[2] * col(P, C_GCM + 3 * q + 2, N, i);
-          gx[0] = c3[0]; gx[1] = c3[1]; gx[2] = c3[2];
-        }
-        double dxx = g.x0 * gx[0] + g.x1 * gx[1] + g.x2 * gx[2];
-        cond += w * 4. * (ki * kj) / (ki + kj) * (Ti - col(P, C_T, N, j)) * dxx / (g.r * g.r);
-      }
-    }
-    double sr[6];
-    for (int c = 0; c < 6; ++c) sr[c] = col(P, C_SR + c, N, i);
-    if (K.thermal_solver) {
-      double rho = col(P, C_RHO, N, i);
-      double f = 1. / (rho * col(P, C_CPT, N, i));
-      double dTdt = f * (cond + 0.0 + col(P, C_QSRC, N, i) + col(P, C_QPL, N, i) * K.pl_work_heat_frac + 0.0);
-      colw(P, C_DTDT, N, i) = dTdt;
-      double s = col(P, C_THEXP, N, i) * dTdt;
-      for (int c = 0; c < 3; ++c) { sr[c] = sr[c] + s; colw(P, C_SR + c, N, i) = sr[c]; }
-    }
-    double t[6];
-    for (int c = 0; c < 6; ++c) t[c] = col(P, C_TAU + c, N, i);
-    dint = mrhoi * (t[0] * sr[0] + 2.0 * t[3] * sr[3] + 2.0 * t[4] * sr[4] + t[1] * sr[1] + 2.0 * t[5] * sr[5] +
-                    t[2] * sr[2]);
-    colw(P, C_DKIN, N, i) = dkin;
-    colw(P, C_DINT, N, i) = dint;
-  }
-  double r;
-  r = block_reduce<0>(dkin, sh); if (threadIdx.x == 0) P.partials[S_DKIN * K.nblocks + blockIdx.x] = r;
-  r = block_reduce<0>(dint, sh); if (threadIdx.x == 0) P.partials[S_DINT * K.nblocks + blockIdx.x] = r;
-}
 
 // ---------------------------------------------------------------- reductions
 // One block per slot; each thread sums a fixed strided subset, then a fixed tree.
@@ -873,8 +867,6 @@ void launch_step_fp64_body(const DevPtrs& P, const DomainConst& K, cudaStream_t 
   launch_bc(P, K, C_VN, s);
   k_rate_stress<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_rate_stress");
-  k_energy<<<nb, BLOCK, 0, s>>>(P, K);
-  mark(s, "k_energy");
   launch_step_tail(P, K, s);
 }
 
