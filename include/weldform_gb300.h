@@ -216,16 +216,12 @@ int wf_checkpoint_save(wf_domain* d, int slot);
 int wf_checkpoint_restore(wf_domain* d, int slot);
 int wf_checkpoint_free(wf_domain* d, int slot);
 
-/* Chooses the thread-block size (64, 128, 256 or 512 threads) and the
- * schedule of the mixed form's three gather kernels by timing `steps` steps
- * with each pair from a checkpoint of the current state, restores that
- * state, keeps the fastest and returns its block size; results are cached
- * per size bucket (particles rounded to a power of two) for later domains
- * in the process.  The schedule is domain field "gather_schedule": 0 one
- * block per tile of particles, 1 a persistent grid in which every SM sweeps
- * its own contiguous chunk of tiles (neighbour records shared by
- * consecutive tiles stay in that SM's L1).  Both fields can also be set
- * directly ("gather_block", "gather_schedule"), also after the prologue. */
+/* Chooses the thread-block size of the mixed form's three gather kernels
+ * (64, 128, 256 or 512 threads) by timing `steps` steps with each from a
+ * checkpoint of the current state, restores that state, keeps the fastest
+ * and returns it; results are cached per size bucket (particles rounded to a
+ * power of two) for later domains in the process.  The block size is also
+ * domain field "gather_block", settable after the prologue. */
 int wf_autotune(wf_domain* d, int steps, int* block);
 
 /* ---- reaction-force adjoint (no counterpart in the reference) ------------

@@ -107,19 +107,18 @@ def test_mixed_leapfrog():
     _check(m, o, f)
 
 
-def test_mixed_gather_schedules_agree_bitwise():
-    """Every gather schedule and block size computes each particle's sums in
-    the same order, so the yielding JC + thermal + contact run is bit-identical
-    across them (which SM or block handles a particle does not matter)."""
+def test_mixed_gather_block_sizes_agree_bitwise():
+    """Every gather block size computes each particle's sums in the same
+    order, so a yielding JC + thermal + contact run is bit-identical across
+    them (which block handles a particle does not matter)."""
     res = []
-    for sched, block in ((0, 256), (1, 256), (1, 64), (1, 512)):
+    for block in (256, 64, 128, 512):
         d = gpu_domain()
         d.set("precision", PRECISION_MIXED)
         case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, gap=0.0)
         d.prepare(case.dt)
-        d.set("gather_schedule", sched)
         d.set("gather_block", block)
-        assert d.geti("gather_schedule") == sched and d.geti("gather_block") == block
+        assert d.geti("gather_block") == block
         d.step(60)
         res.append({f: d.get_array(f) for f in ("x", "v", "Sigma", "pl_strain", "T")})
         d.close()

@@ -105,8 +105,7 @@ constexpr int MAX_AMPS = 16;
 constexpr int MAX_AMP_POINTS = 512;
 constexpr int MAX_MESHES = 8;
 constexpr int MAX_NB = 100;  // MAX_NB_PER_PART, Source/Domain.h:49
-constexpr int GATHER_KERNELS = 3;  // persistent gathers with their own tile cursors
-constexpr int MAX_CHUNKS = 1024;   // upper bound of the SM chunk count
+
 constexpr int MAX_CP = 64;   // contact pairs per particle
 
 // Neighbour-row entries: the neighbour's index, bit 31 set when its original
@@ -182,8 +181,6 @@ struct DomainConst {
   int nblocks;         // blocks of the per-particle kernels (partials stride)
   int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
   int gblock;          // thread-block size of the mixed form's gather kernels
-  int gsched;          // gather schedule: 0 one block per tile, 1 SM-chunked persistent blocks
-  int nchunks;         // SM chunks of the persistent schedule (the SM count)
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
   int leapfrog;        // 1: SolveDiffUpdateLeapFrog's update (velocities at half steps)
   int gradcorr;        // 1: kernel-gradient correction (Domain::gradKernelCorr)
@@ -225,7 +222,6 @@ struct DevPtrs {
   const int* node_mesh;   // nnodes
   int nnodes, nelem;
   double* partials;       // NSLOTS * nblocks
-  int* tile_ctr;          // GATHER_KERNELS * nchunks tile cursors of the persistent gathers
   long long* scan_tmp;
   double* tx;             // step tape of the adjoint's recompute (TapeCol columns), null otherwise
 };

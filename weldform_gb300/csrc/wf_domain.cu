@@ -150,9 +150,7 @@ struct wf_domain {
   int graph_precision = -1;
   int graph_block = -1;
   int gblock = 256;
-  int gsched = 0;    // gather schedule of the mixed form (0 per-tile blocks, 1 SM-chunked persistent)
-  int nchunks = 1;   // SM count of the device (chunks of the persistent schedule)
-  int graph_key() const { return gblock * 2 + gsched; }
+  int graph_key() const { return gblock; }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
@@ -601,13 +599,6 @@ struct wf_domain {
     for (size_t m = 0; m < meshes.size(); ++m) K.contact_surf_id[m] = meshes[m].id;
     K.nblocks = (N + 255) / 256;
     P.partials = dalloc<double>((size_t)NSLOTS * K.nblocks);
-    {
-      int sms = 1;
-      CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-      nchunks = sms < 1 ? 1 : (sms > MAX_CHUNKS ? MAX_CHUNKS : sms);
-      P.tile_ctr = dalloc<int>((size_t)GATHER_KERNELS * MAX_CHUNKS);
-      CK(cudaMemsetAsync(P.tile_ctr, 0, sizeof(int) * GATHER_KERNELS * MAX_CHUNKS, stream));
-    }
     P.scan_tmp = dalloc<long long>((ncells + 4095) / 4096 + 1);
     // Step state.
     StepState st;
@@ -662,8 +653,6 @@ struct wf_domain {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
     k.gblock = gblock;
-    k.gsched = gsched;
-    k.nchunks = nchunks;
     return k;
   }
   void launch_one_step() {
@@ -1019,35 +1008,31 @@ struct wf_domain {
   }
   int autotune(int steps) {
     static std::mutex mu;
-    static std::map<int, std::pair<int, int>> cache;  // size bucket -> (block, schedule)
+    static std::map<int, int> cache;  // size bucket -> block
     int bucket = 0;
     while ((1LL << bucket) < hp.N) ++bucket;
     {
       std::lock_guard<std::mutex> lk(mu);
       auto it = cache.find(bucket);
-      if (it != cache.end()) { gblock = it->second.first; gsched = it->second.second; return gblock; }
+      if (it != cache.end()) { gblock = it->second; return gblock; }
     }
     const int slot = 15;
     checkpoint_save(slot);
-    int best = 256, best_sched = 0;
+    int best = 256;
     double best_ms = 1e300;
-    for (int sc : {0, 1}) {
-      for (int b : {64, 128, 256, 512}) {
-        gblock = b;
-        gsched = sc;
-        long long l = 0;
-        step(1);  // capture + warm
-        checkpoint_restore(slot);
-        double ms = step_timed(steps, &l);
-        checkpoint_restore(slot);
-        if (ms < best_ms) { best_ms = ms; best = b; best_sched = sc; }
-      }
+    for (int b : {64, 128, 256, 512}) {
+      gblock = b;
+      long long l = 0;
+      step(1);  // capture + warm
+      checkpoint_restore(slot);
+      double ms = step_timed(steps, &l);
+      checkpoint_restore(slot);
+      if (ms < best_ms) { best_ms = ms; best = b; }
     }
     gblock = best;
-    gsched = best_sched;
     checkpoint_free(slot);
     std::lock_guard<std::mutex> lk(mu);
-    cache[bucket] = {best, best_sched};
+    cache[bucket] = best;
     return best;
   }
   void search_now() {
@@ -1190,11 +1175,6 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     return WF_OK;
   }
   if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }
-  if (n == "gather_schedule") {  // mixed-form gathers: 0 one block per tile, 1 SM-chunked persistent
-    if (v != 0 && v != 1) return set_err(WF_ERR_ARG, "gather_schedule must be 0 or 1");
-    d->gsched = v;
-    return WF_OK;
-  }
   if (n == "gather_block") {
     if (v != 64 && v != 128 && v != 256 && v != 512) return set_err(WF_ERR_ARG, "gather_block must be 64, 128, 256 or 512");
     d->gblock = v;
@@ -1260,7 +1240,6 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     std::string n(name ? name : "");
     if (n == "particle_count") { *v = d->hp.N; return WF_OK; }
     if (n == "solid_part_count") { *v = d->solid_part_count; return WF_OK; }
-    if (n == "gather_schedule") { *v = d->gsched; return WF_OK; }
     if (n == "gather_block") { *v = d->gblock; return WF_OK; }
     if (n.size() == 8 && n.rfind("CellNo.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') { *v = d->CellNo[n[7] - 'x']; return WF_OK; }
     if (!d->prepared) { *v = 0; return WF_OK; }

@@ -41,51 +41,11 @@ struct KSum {
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 
-// ---------------------------------------------------------------- gather schedule
-// Schedule 0: block b handles particles [b*B, (b+1)*B).  Schedule 1: a
-// persistent grid (resident blocks of every SM) where each SM owns a
-// contiguous chunk of tiles — a compact region in the Morton order — and its
-// blocks take the chunk's tiles in order from a cursor, so the neighbour
-// records that consecutive tiles share stay in that SM's L1.  A block whose
-// home chunk is exhausted moves on to the next chunk, so every tile is taken
-// exactly once whatever SMs the blocks land on.  Each particle's result does
-// not depend on which block computes it.
-__device__ __forceinline__ unsigned sm_id() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
-  return r;
-}
-
+// One thread per particle: block b handles particles [b*B, (b+1)*B).
 template <class Body>
-__device__ __forceinline__ void run_tiles(const DomainConst& K, int* ctr, Body body) {
-  if (!K.gsched) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < K.N) body(i);
-    return;
-  }
-  __shared__ int s_tile, s_chunk, s_seen;
-  const int nch = K.nchunks;
-  const int ntiles = (K.N + blockDim.x - 1) / blockDim.x;
-  if (threadIdx.x == 0) { s_chunk = (int)(sm_id() % (unsigned)nch); s_seen = 0; }
-  for (;;) {
-    if (threadIdx.x == 0) {
-      int c = s_chunk, seen = s_seen, tile = -1;
-      while (seen < nch) {
-        int lo = (int)((long long)ntiles * c / nch), hi = (int)((long long)ntiles * (c + 1) / nch);
-        int t = lo + atomicAdd(&ctr[c], 1);
-        if (t < hi) { tile = t; break; }
-        c = (c + 1 == nch) ? 0 : c + 1;
-        ++seen;
-      }
-      s_chunk = c; s_seen = seen; s_tile = tile;
-    }
-    __syncthreads();
-    int tile = s_tile;
-    __syncthreads();
-    if (tile < 0) return;
-    int i = tile * blockDim.x + threadIdx.x;
-    if (i < K.N) body(i);
-  }
+__device__ __forceinline__ void run_rows(const DomainConst& K, Body body) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < K.N) body(i);
 }
 
 // Cubic-spline gradient factor GK (Functions.cpp:74-87, 3D) from r^2 and the
@@ -135,7 +95,9 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
 }
 
 // ---------------------------------------------------------------- accel
-template <bool TI>
+// AVU: every solid particle has the same (alpha, beta), so the pair mean is
+// the value itself and the gather reads neither particle's misc group.
+template <bool TI, bool AVU>
 __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   if (icol(P, I_KIND, N, i) != 0) {
@@ -144,7 +106,8 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   }
   const float4* ri = P.rc + i;
   float4 xh = ld4(ri + (size_t)RC_XH * N), xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
-  float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1 = ld4(ri + (size_t)RC_S1 * N), mi = ld4(ri + (size_t)RC_MISC * N);
+  float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1 = ld4(ri + (size_t)RC_S1 * N);
+  float4 mi = AVU ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(ri + (size_t)RC_MISC * N);
   float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
   float tii = 0.f;
   if (TI) { t0 = ld4(ri + (size_t)RC_TI0 * N); t1 = ld4(ri + (size_t)RC_TI1 * N); tii = (float)col(P, C_TI, N, i); }
@@ -162,7 +125,7 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
     float r2 = x0 * x0 + x1 * x1 + x2 * x2, r;
     float GK = grad_kernel_f(r2, hh, &r);
     float Alpha, Beta;
-    if (K.av_uniform) {  // the pair mean of equal values is the value itself
+    if (AVU) {
       Alpha = K.av_alpha; Beta = K.av_beta;
     } else {
       float4 jmi = ld4(rj + (size_t)RC_MISC * N);
@@ -199,9 +162,9 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   }
   colw(P, C_A, N, i) = a0.value(); colw(P, C_A + 1, N, i) = a1.value(); colw(P, C_A + 2, N, i) = a2.value();
 }
-template <bool TI>
+template <bool TI, bool AVU>
 __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
-  run_tiles(K, P.tile_ctr, [&](int i) { accel_mx<TI>(P, K, i); });
+  run_rows(K, [&](int i) { accel_mx<TI, AVU>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- density + drift + kick
@@ -263,7 +226,7 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   r[(size_t)RN_E * N] = make_float4(solid ? (float)(pn / (rn * rn)) : 0.f, ri[(size_t)RC_MISC * N].z, th, tl);
 }
 __global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst K) {
-  run_tiles(K, P.tile_ctr + K.nchunks, [&](int i) { density_drift_mx(P, K, i); });
+  run_rows(K, [&](int i) { density_drift_mx(P, K, i); });
 }
 
 // ---------------------------------------------------------------- rates + energy + conduction
@@ -319,7 +282,7 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
   colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
 }
 __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
-  run_tiles(K, P.tile_ctr + 2 * K.nchunks, [&](int i) { rate_mx(P, K, i); });
+  run_rows(K, [&](int i) { rate_mx(P, K, i); });
 }
 
 // ---------------------------------------------------------------- elementwise update
@@ -515,46 +478,28 @@ void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, c
   mark(s, "k_refresh_records");
 }
 
-__global__ void k_zero_cursors(int* c, int n) {
-  for (int k = threadIdx.x; k < n; k += blockDim.x) c[k] = 0;
-}
-
-// Blocks of a persistent launch: resident blocks per SM x SMs, at most `cap`.
-static int persistent_grid(const void* fn, int block, int sms, int cap) {
-  int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0) != cudaSuccess || per < 1) per = 1;
-  long long g = (long long)per * sms;
-  return (int)(g < cap ? g : cap);
-}
-
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
   int nb = nblk(K.N, BLOCK);
   int gb = (K.gblock == 64 || K.gblock == 128 || K.gblock == 512) ? K.gblock : 256;
   int ng = nblk(K.N, gb);
-  int ga = ng, gd = ng, gr = ng;
-  if (K.gsched) {  // persistent: the resident blocks of every SM, capped at one tile each
-    const void* fa = K.ti ? (const void*)k_accel_mx<true> : (const void*)k_accel_mx<false>;
-    ga = persistent_grid(fa, gb, K.nchunks, ng);
-    gd = persistent_grid((const void*)k_density_drift_mx, gb, K.nchunks, ng);
-    gr = persistent_grid((const void*)k_rate_mx, gb, K.nchunks, ng);
-  }
   launch_step_head(P, K, fscratch, iscratch, s);
   launch_refresh_shadows(P, K, 0, s);
   launch_tensile(P, K, s);
-  if (K.gsched) {
-    k_zero_cursors<<<1, 512, 0, s>>>(P.tile_ctr, GATHER_KERNELS * K.nchunks);
-    mark(s, "k_zero_cursors");
+  if (K.ti) {
+    if (K.av_uniform) k_accel_mx<true, true><<<ng, gb, 0, s>>>(P, K);
+    else k_accel_mx<true, false><<<ng, gb, 0, s>>>(P, K);
+  } else {
+    if (K.av_uniform) k_accel_mx<false, true><<<ng, gb, 0, s>>>(P, K);
+    else k_accel_mx<false, false><<<ng, gb, 0, s>>>(P, K);
   }
-  if (K.ti) k_accel_mx<true><<<ga, gb, 0, s>>>(P, K);
-  else k_accel_mx<false><<<ga, gb, 0, s>>>(P, K);
   mark(s, "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
-  k_density_drift_mx<<<gd, gb, 0, s>>>(P, K);
+  k_density_drift_mx<<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  k_rate_mx<<<gr, gb, 0, s>>>(P, K);
+  k_rate_mx<<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_rate_mx");
   k_stress_mx<<<nb, BLOCK, 0, s>>>(P, K);
   mark(s, "k_stress_mx");

@@ -20,7 +20,6 @@ def main():
     ap.add_argument("--precision", type=int, default=0)
     ap.add_argument("--v-top", type=float, default=-1.0)
     ap.add_argument("--kernels", action="store_true", help="print per-kernel CUDA-event times of the steps")
-    ap.add_argument("--gather-schedule", type=int, default=None, help="mixed gathers: 0 per-tile blocks, 1 SM-chunked")
     ap.add_argument("--gather-block", type=int, default=None, help="mixed gathers: threads per block")
     a = ap.parse_args()
     dx = configs.dx_for_count(0.010, 0.030, a.n)
@@ -28,8 +27,6 @@ def main():
     d.set("precision", a.precision)
     case = configs.cylinder_upsetting(d, R=0.010, L=0.030, dx=dx, v_top=a.v_top)
     d.prepare(case.dt)
-    if a.gather_schedule is not None:
-        d.set("gather_schedule", a.gather_schedule)
     if a.gather_block is not None:
         d.set("gather_block", a.gather_block)
     t = time.perf_counter()
