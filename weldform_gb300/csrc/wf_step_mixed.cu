@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst
 // ---------------------------------------------------------------- rates + energy + conduction
 // Gather at x(n+1), v(n+1): strain/rotation rate sums (InteractionAlt.cpp:263-479),
 // the kinetic-energy pair sum (Domain.cpp:1752-1808) and conduction (Thermal.cpp:53-219).
+template <bool THERMAL>
 __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -243,7 +244,6 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
     KSum kin, cnd;
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
-    bool thermal = K.thermal_solver;
     for (int k = 0; k < len; ++k) {
       int ent = nb[(size_t)k * N];
       int j = nb_index(ent);
@@ -263,7 +263,7 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       float dv = GK * (b0 * x0 + b1 * x1 + b2 * x2);
       float pk = 0.5f * (up ? jxl.w : xl.w) * (e.x + je.x) * dv;
       kin.add(up ? pk : -pk);
-      if (thermal) {
+      if (THERMAL) {
         float wt = up ? jvl.w : vl.w;  // m_P2 / rho_P2 for both ends of the pair
         float dT = (e.z - je.z) + (e.w - je.w);
         cnd.add(wt * 4.f * (e.y * je.y) / (e.y + je.y) * dT * GK);
@@ -281,8 +281,9 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
   colw(P, C_DKIN, N, i) = dkin;
   colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
 }
+template <bool THERMAL>
 __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { rate_mx(P, K, i); });
+  run_rows(K, [&](int i) { rate_mx<THERMAL>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- elementwise update
@@ -363,6 +364,7 @@ __device__ __forceinline__ double stress_update_mx(StressMx& s, const float sr[6
   return dep;
 }
 
+template <bool HEAT, bool THERMAL>
 __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K) {
   __shared__ double sh[32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
       }
       double srd[6];
       for (int c = 0; c < 6; ++c) srd[c] = (double)sr[c];
-      if (K.pl_heating) {
+      if (HEAT) {
         double q = col(P, C_QPL, N, i);
         if (s.delta_pl_strain > 0.0) {
           if (!(dep > 0.0))
@@ -434,7 +436,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
         colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + q * dt;
         plw = col(P, C_MASS, N, i) / rho * q;
       }
-      if (K.thermal_solver) {  // T(n+1) (already in the next record), then CalcTempInc's dTdt
+      if (THERMAL) {  // T(n+1) (already in the next record), then CalcTempInc's dTdt
         T += dt * col(P, C_DTDT, N, i);
         colw(P, C_T, N, i) = T;
         maxT = T; minT = T;
@@ -465,8 +467,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
   r = block_reduce<1>(maxpl, sh); if (threadIdx.x == 0) P.partials[S_MAXPL * K.nblocks + blockIdx.x] = r;
   r = block_reduce<0>(dkin, sh); if (threadIdx.x == 0) P.partials[S_DKIN * K.nblocks + blockIdx.x] = r;
   r = block_reduce<0>(dint, sh); if (threadIdx.x == 0) P.partials[S_DINT * K.nblocks + blockIdx.x] = r;
-  if (K.pl_heating) { r = block_reduce<0>(plw, sh); if (threadIdx.x == 0) P.partials[S_PLW * K.nblocks + blockIdx.x] = r; }
-  if (K.thermal_solver) {
+  if (HEAT) { r = block_reduce<0>(plw, sh); if (threadIdx.x == 0) P.partials[S_PLW * K.nblocks + blockIdx.x] = r; }
+  if (THERMAL) {
     r = block_reduce<1>(maxT, sh); if (threadIdx.x == 0) P.partials[S_MAXT * K.nblocks + blockIdx.x] = r;
     r = block_reduce<2>(minT, sh); if (threadIdx.x == 0) P.partials[S_MINT * K.nblocks + blockIdx.x] = r;
   }
@@ -499,9 +501,16 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   k_density_drift_mx<<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  k_rate_mx<<<ng, gb, 0, s>>>(P, K);
+  if (K.thermal_solver) k_rate_mx<true><<<ng, gb, 0, s>>>(P, K);
+  else k_rate_mx<false><<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_rate_mx");
-  k_stress_mx<<<nb, BLOCK, 0, s>>>(P, K);
+  if (K.pl_heating) {
+    if (K.thermal_solver) k_stress_mx<true, true><<<nb, BLOCK, 0, s>>>(P, K);
+    else k_stress_mx<true, false><<<nb, BLOCK, 0, s>>>(P, K);
+  } else {
+    if (K.thermal_solver) k_stress_mx<false, true><<<nb, BLOCK, 0, s>>>(P, K);
+    else k_stress_mx<false, false><<<nb, BLOCK, 0, s>>>(P, K);
+  }
   mark(s, "k_stress_mx");
   launch_step_tail(P, K, s);
 }
