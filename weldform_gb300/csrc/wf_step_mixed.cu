@@ -225,7 +225,7 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   r[(size_t)RN_VL * N] = make_float4(nvl[0], nvl[1], nvl[2], (float)mrn);
   r[(size_t)RN_E * N] = make_float4(solid ? (float)(pn / (rn * rn)) : 0.f, ri[(size_t)RC_MISC * N].z, th, tl);
 }
-__global__ void __launch_bounds__(512) k_density_drift_mx(DevPtrs P, DomainConst K) {
+__global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainConst K) {
   run_rows(K, [&](int i) { density_drift_mx(P, K, i); });
 }
 
