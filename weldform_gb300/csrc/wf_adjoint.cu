@@ -33,29 +33,36 @@ namespace wf {
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 static_assert(ADJ_BLOCK == BLOCK, "the finish kernel's partials are sized by ADJ_BLOCK");
 
-// Cubic-spline gradient kernel (Functions.cpp:74-87) and its derivative in r.
+// Cubic-spline gradient kernel (Functions.cpp:74-87) and its derivative in r,
+// with C = 1 / (pi hh^4):
+//   q < 1:      GK = C/hh (-3 + 9/4 q),     dGK/dr = C/hh^2 9/4
+//   1 <= q < 2: GK = -3/4 C (2 - q)^2 / r,  dGK/dr = 3/4 C (4 - q^2) / r^2
+// formed with one division (1/r) per pair, plus 1/hh when the pair's
+// smoothing lengths differ (inv_hi = 1/h_i is the caller's).  The values
+// equal the forward's to rounding.
 struct GeoD {
   double x0, x1, x2, r, GK, dGr;  // dGr = (dGK/dr) / r
 };
-__device__ __forceinline__ GeoD geo_d(const double xi[3], double hi, double xj0, double xj1, double xj2, double hj) {
+__device__ __forceinline__ GeoD geo_d(const double xi[3], double hi, double inv_hi, double xj0, double xj1, double xj2,
+                                      double hj) {
   GeoD g;
   g.x0 = xi[0] - xj0; g.x1 = xi[1] - xj1; g.x2 = xi[2] - xj2;
   double r2 = g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2;
   g.r = sqrt(r2);
-  double hh = (hi + hj) / 2;
-  double inv_h = 1.0 / hh;
+  double inv_h = hj == hi ? inv_hi : 2.0 / (hi + hj);
   double q = g.r * inv_h;
-  double h2 = hh * hh;
-  double C = 1.0 / (h2 * h2 * WF_PI);
+  double ih2 = inv_h * inv_h;
+  double C = ih2 * ih2 * (1.0 / WF_PI);
+  double rinv = g.r > 0.0 ? 1.0 / g.r : 0.0;
   double dG = 0.0;
   if (q == 0.0) g.GK = C * inv_h * -3.0;
-  else if (q < 1.0) { g.GK = C * inv_h * (-3.0 + 2.25 * q); dG = C * inv_h * inv_h * 2.25; }
+  else if (q < 1.0) { g.GK = C * inv_h * (-3.0 + 2.25 * q); dG = C * ih2 * 2.25; }
   else if (q < 2.0) {
     double t = 2.0 - q;
-    g.GK = C / (q * hh) * (-0.75 * t * t);
-    dG = C * inv_h * inv_h * 0.75 * (4.0 - q * q) / (q * q);
+    g.GK = C * rinv * (-0.75 * t * t);
+    dG = C * 0.75 * (4.0 - q * q) * (rinv * rinv);
   } else g.GK = 0.0;
-  g.dGr = g.r > 0.0 ? dG / g.r : 0.0;
+  g.dGr = dG * rinv;
   return g;
 }
 
@@ -107,19 +114,20 @@ __global__ void __launch_bounds__(BLOCK) k_adj_thermal_stress(AdjPtrs A, DomainC
   double lqpl = 0.0;
   // ---- M: T' = T + dt dTdt, dTdt' = (cond + q_src + frac q_pl) / (rho' cp)
   if (K.thermal_solver) {
-    double cpi = col(S, C_CPT, N, i);
     double ldT = LIN(A_DTDT, i);
-    double lci = ldT / (rhoN * cpi);
-    lrhon += -FE(C_DTDT, i) * ldT / rhoN;
+    double lci = TMP(J_LC, i);
+    double inv_rhoN = 1.0 / rhoN;
+    lrhon += -FE(C_DTDT, i) * ldT * inv_rhoN;
     if (K.pl_heating) lqpl = K.pl_work_heat_frac * lci;
     double xi[3] = {FE(C_X, i), FE(C_X + 1, i), FE(C_X + 2, i)};
     double hi = col(S, C_H, N, i), ki = col(S, C_KT, N, i), Ti = FE(C_T, i), wi = FE(C_MRHO, i);
+    double inv_hi = 1.0 / hi;
     int len = S.row_len[i];
     for (int k = 0; k < len; ++k) {
       int e = S.nbr[(size_t)k * N + i];
       int j = nb_index(e);
-      GeoD g = geo_d(xi, hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
-      double lcj = LIN(A_DTDT, j) / (FE(C_RHO, j) * col(S, C_CPT, N, j));
+      GeoD g = geo_d(xi, hi, inv_hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
+      double lcj = TMP(J_LC, j);
       double d = lci - lcj;
       bool up = nb_up(e);  // j has the larger original index: P2 = j
       double w = up ? FE(C_MRHO, j) : wi;  // m_P2 / rho_P2 at both ends (Thermal.cpp:127-131)
@@ -129,7 +137,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_thermal_stress(AdjPtrs A, DomainC
       ltn += d * w * kk * g.GK;
       double cx = d * w * kk * dT * g.dGr;
       lxn[0] += cx * g.x0; lxn[1] += cx * g.x1; lxn[2] += cx * g.x2;
-      if (!up) lrhon += -d * w * kk * dT * g.GK / rhoN;
+      if (!up) lrhon += -d * w * kk * dT * g.GK * inv_rhoN;
     }
   }
   // ---- K + L: radial return (Particle.cpp:960-1067) and plastic-work heat
@@ -312,6 +320,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_rates_drift(AdjPtrs A, DomainCons
   double xi[3] = {FE(C_X, i), FE(C_X + 1, i), FE(C_X + 2, i)};
   double vi[3] = {FE(C_V, i), FE(C_V + 1, i), FE(C_V + 2, i)};
   double hi = col(S, C_H, N, i), wi = FE(C_MRHO, i), rhoN = FE(C_RHO, i);
+  double inv_hi = 1.0 / hi;
   double li[9];
   for (int c = 0; c < 6; ++c) li[c] = TMP(J_SR + c, i);
   for (int c = 0; c < 3; ++c) li[6 + c] = TMP(J_RR + c, i);
@@ -322,7 +331,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_rates_drift(AdjPtrs A, DomainCons
   int len = S.row_len[i];
   for (int k = 0; k < len; ++k) {
     int j = nb_index(S.nbr[(size_t)k * N + i]);
-    GeoD g = geo_d(xi, hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
+    GeoD g = geo_d(xi, hi, inv_hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
     double b0 = vi[0] - FE(C_V, j), b1 = vi[1] - FE(C_V + 1, j), b2 = vi[2] - FE(C_V + 2, j);
     double wj = FE(C_MRHO, j);
     double lj[9], L[9];
@@ -373,13 +382,14 @@ __global__ void __launch_bounds__(BLOCK) k_adj_density_contact(AdjPtrs A, Domain
   double xi[3] = {col(S, C_X, N, i), col(S, C_X + 1, N, i), col(S, C_X + 2, N, i)};
   double vh[3] = {TXV(TX_VH, i), TXV(TX_VH + 1, i), TXV(TX_VH + 2, i)};
   double hi = col(S, C_H, N, i), rhoi = col(S, C_RHO, N, i), wi = col(S, C_MRHO, N, i);
+  double inv_hi = 1.0 / hi, w_rho = -wi / rhoi;
   double ldr = TMP(J_DRHO, i);
   double lvh[3] = {TMP(J_VH, i), TMP(J_VH + 1, i), TMP(J_VH + 2, i)};
   double lx[3] = {0, 0, 0}, lrho = 0.0, D = 0.0;
   int len = S.row_len[i];
   for (int k = 0; k < len; ++k) {
     int j = nb_index(S.nbr[(size_t)k * N + i]);
-    GeoD g = geo_d(xi, hi, col(S, C_X, N, j), col(S, C_X + 1, N, j), col(S, C_X + 2, N, j), col(S, C_H, N, j));
+    GeoD g = geo_d(xi, hi, inv_hi, col(S, C_X, N, j), col(S, C_X + 1, N, j), col(S, C_X + 2, N, j), col(S, C_H, N, j));
     double b0 = vh[0] - TXV(TX_VH, j), b1 = vh[1] - TXV(TX_VH + 1, j), b2 = vh[2] - TXV(TX_VH + 2, j);
     double bx = b0 * g.x0 + b1 * g.x1 + b2 * g.x2;
     double pd = g.GK * bx;
@@ -389,7 +399,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_density_contact(AdjPtrs A, Domain
     lvh[0] += Lam * g.GK * g.x0; lvh[1] += Lam * g.GK * g.x1; lvh[2] += Lam * g.GK * g.x2;
     double c = Lam * bx * g.dGr;
     lx[0] += Lam * g.GK * b0 + c * g.x0; lx[1] += Lam * g.GK * b1 + c * g.x1; lx[2] += Lam * g.GK * b2 + c * g.x2;
-    lrho += ldj * rhoj * (-wi / rhoi) * pd;
+    lrho += ldj * rhoj * w_rho * pd;
   }
   lrho += ldr * D;
   // second BC pass and the first half kick vh = v1 + a1 dt/2
@@ -590,6 +600,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
   double vi[3] = {col(S, C_V, N, i), col(S, C_V + 1, N, i), col(S, C_V + 2, N, i)};
   double hi = col(S, C_H, N, i), rhoi = col(S, C_RHO, N, i), csi = col(S, C_CS, N, i), mi = col(S, C_MASS, N, i);
   double al = col(S, C_ALPHA, N, i), be = col(S, C_BETA, N, i);
+  double inv_hi = 1.0 / hi;
   double Si[6];
   for (int c = 0; c < 6; ++c) Si[c] = col(S, C_SRHO + c, N, i);
   double lai[3] = {TMP(J_AACC, i), TMP(J_AACC + 1, i), TMP(J_AACC + 2, i)};
@@ -601,20 +612,20 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
     double mj = col(S, C_MASS, N, j);
     double Gm[3];
     for (int d = 0; d < 3; ++d) Gm[d] = mj * lai[d] - mi * TMP(J_AACC + d, j);
-    GeoD g = geo_d(xi, hi, col(S, C_X, N, j), col(S, C_X + 1, N, j), col(S, C_X + 2, N, j), col(S, C_H, N, j));
+    GeoD g = geo_d(xi, hi, inv_hi, col(S, C_X, N, j), col(S, C_X + 1, N, j), col(S, C_X + 2, N, j), col(S, C_H, N, j));
     double b0 = vi[0] - col(S, C_V, N, j), b1 = vi[1] - col(S, C_V + 1, N, j), b2 = vi[2] - col(S, C_V + 2, N, j);
     double Alpha = (al + col(S, C_ALPHA, N, j)) / 2.0, Beta = (be + col(S, C_BETA, N, j)) / 2.0;
-    double PIs = 0.0, MU = 0.0, Dn = 0.0, Cij = 0.0, rbar = 0.0, hh = 0.0;
+    double PIs = 0.0, MU = 0.0, iDn = 0.0, Cij = 0.0, irbar = 0.0, hh = 0.0;
     bool av = false;
     if (Alpha != 0.0 || Beta != 0.0) {
       double dvx = b0 * g.x0 + b1 * g.x1 + b2 * g.x2;
       if (dvx < 0) {
         hh = (hi + col(S, C_H, N, j)) / 2;
-        Dn = g.r * g.r + 0.01 * hh * hh;
-        MU = hh * dvx / Dn;
+        iDn = 1.0 / (g.r * g.r + 0.01 * hh * hh);
+        MU = hh * dvx * iDn;
         Cij = 0.5 * (csi + col(S, C_CS, N, j));
-        rbar = 0.5 * (rhoi + col(S, C_RHO, N, j));
-        PIs = (Alpha * Cij * MU + Beta * MU * MU) / rbar;
+        irbar = 2.0 / (rhoi + col(S, C_RHO, N, j));
+        PIs = (Alpha * Cij * MU + Beta * MU * MU) * irbar;
         av = true;
       }
     }
@@ -634,10 +645,10 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
     lSs[5] += g.GK * (g.x1 * Gm[2] + g.x2 * Gm[1]);
     if (av) {
       double lPI = g.GK * (g.x0 * Gm[0] + g.x1 * Gm[1] + g.x2 * Gm[2]);
-      double lMU = lPI * (Alpha * Cij + 2.0 * Beta * MU) / rbar;
-      lcs += lPI * Alpha * MU / rbar * 0.5;
-      lrho += -lPI * PIs / rbar * 0.5;
-      double cb = lMU * hh / Dn, cx = -lMU * 2.0 * MU / Dn;
+      double lMU = lPI * (Alpha * Cij + 2.0 * Beta * MU) * irbar;
+      lcs += lPI * Alpha * MU * irbar * 0.5;
+      lrho += -lPI * PIs * irbar * 0.5;
+      double cb = lMU * hh * iDn, cx = -lMU * 2.0 * MU * iDn;
       lx[0] += cb * b0 + cx * g.x0; lx[1] += cb * b1 + cx * g.x1; lx[2] += cb * b2 + cx * g.x2;
       lv[0] += cb * g.x0; lv[1] += cb * g.x1; lv[2] += cb * g.x2;
     }
@@ -712,8 +723,22 @@ __global__ void k_record_force(const StepState* st, int mesh, int axis, double* 
   if (threadIdx.x == 0 && blockIdx.x == 0) out[n] = st->contact_force[mesh][axis];
 }
 
+// Per-particle factor of the conduction adjoint, d loss / d dTdt' / (rho' cp),
+// read by both ends of every pair in R1.
+__global__ void k_adj_conduction_factor(AdjPtrs A, DomainConst K) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  const DevPtrs& S = A.S;
+  size_t N = K.N;
+  TMP(J_LC, i) = icol(S, I_KIND, N, i) == 0 ? LIN(A_DTDT, i) / (FE(C_RHO, i) * col(S, C_CPT, N, i)) : 0.0;
+}
+
 void launch_adjoint_step(const AdjPtrs& A, const DomainConst& K, cudaStream_t s) {
   int nb = nblk(K.N, BLOCK);
+  if (K.thermal_solver) {
+    k_adj_conduction_factor<<<nb, BLOCK, 0, s>>>(A, K);
+    mark(s, "k_adj_conduction_factor");
+  }
   k_adj_thermal_stress<<<nb, BLOCK, 0, s>>>(A, K);
   mark(s, "k_adj_thermal_stress");
   k_adj_rates_drift<<<nb, BLOCK, 0, s>>>(A, K);

@@ -37,7 +37,8 @@ enum AdjTmp : int {
   J_AH = 19,   // acceleration of the second kick (3)
   J_DRHO = 22, // density rate
   J_AACC = 23, // acceleration from the pair sum (3)
-  NA_TMP = 26
+  J_LC = 26,   // adjoint of dTdt(n+1) over rho(n+1) cp (the conduction sum's factor)
+  NA_TMP = 27
 };
 // Per-particle accumulators of parameter adjoints (permuted with the state).
 enum AdjParamCol : int {

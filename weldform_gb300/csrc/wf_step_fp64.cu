@@ -76,22 +76,28 @@ struct PairGeo {
   double r2, r, hh, GK;
 };
 // Pair geometry: h = (hi + hj) / 2, q = rij / h, cubic-spline GradKernel
-// (Functions.cpp:74-87) evaluated as (C / h) * g(q) with g(q) = -3 + 9/4 q for
-// q < 1 and -3/4 (2 - q)^2 / q for 1 <= q < 2.
-__device__ __forceinline__ PairGeo pair_geo(double xi0, double xi1, double xi2, double hi, double xj0, double xj1,
-                                           double xj2, double hj) {
+// (Functions.cpp:74-87), C = 1 / (pi h^4):
+//   q < 1:      GK = C/h (-3 + 9/4 q)
+//   1 <= q < 2: GK = -3/4 C (2 - q)^2 / (q h) = -3/4 C (2 - q)^2 / r
+// GB300 runs FP64 division as a multi-instruction sequence at 1/64 of the
+// FP32 rate, so the pair takes one division (C / r, only for q >= 1) plus
+// 1/h when the two smoothing lengths differ; inv_hi = 1/h_i comes from the
+// caller.  Equal to the reference's expression to rounding.
+__device__ __forceinline__ PairGeo pair_geo(double xi0, double xi1, double xi2, double hi, double inv_hi, double xj0,
+                                           double xj1, double xj2, double hj) {
   PairGeo g;
   g.x0 = xi0 - xj0; g.x1 = xi1 - xj1; g.x2 = xi2 - xj2;
   g.r2 = g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2;
   g.r = sqrt(g.r2);
-  g.hh = (hi + hj) / 2;
-  double inv_h = 1.0 / g.hh;
+  double inv_h;
+  if (hj == hi) { g.hh = hi; inv_h = inv_hi; }
+  else { g.hh = (hi + hj) / 2; inv_h = 1.0 / g.hh; }
   double q = g.r * inv_h;
-  double h2 = g.hh * g.hh;
-  double C = 1.0 / (h2 * h2 * WF_PI);
+  double ih2 = inv_h * inv_h;
+  double C = ih2 * ih2 * (1.0 / WF_PI);
   if (q == 0.0) g.GK = C * inv_h * -3.0;
   else if (q < 1.0) g.GK = C * inv_h * (-3.0 + 2.25 * q);
-  else if (q < 2.0) { double t = 2.0 - q; g.GK = C / (q * g.hh) * (-0.75 * t * t); }
+  else if (q < 2.0) { double t = 2.0 - q; g.GK = C / g.r * (-0.75 * t * t); }
   else g.GK = 0.0;
   return g;
 }
@@ -141,11 +147,12 @@ __global__ void k_grad_corr(DevPtrs P, DomainConst K) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
     if (icol(P, I_KIND, N, i) != 0) continue;
     double xi0 = col(P, C_X, N, i), xi1 = col(P, C_X + 1, N, i), xi2 = col(P, C_X + 2, N, i), hi = col(P, C_H, N, i);
+    double inv_hi = 1.0 / hi;
     double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     int len = P.row_len[i];
     for (int k = 0; k < len; ++k) {
       int j = nb_index(P.nbr[(size_t)k * N + i]);
-      PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+      PairGeo g = pair_geo(xi0, xi1, xi2, hi, inv_hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                            col(P, C_H, N, j));
       double gv[3] = {g.GK * g.x0, g.GK * g.x1, g.GK * g.x2}, xv[3] = {g.x0, g.x1, g.x2};
       double f = col(P, C_MASS, N, j) / col(P, C_RHO, N, j);
@@ -185,6 +192,7 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
   double xi0 = col(P, C_X, N, i), xi1 = col(P, C_X + 1, N, i), xi2 = col(P, C_X + 2, N, i);
   double vi0 = col(P, C_V, N, i), vi1 = col(P, C_V + 1, N, i), vi2 = col(P, C_V + 2, N, i);
   double hi = col(P, C_H, N, i), rhoi = col(P, C_RHO, N, i), csi = col(P, C_CS, N, i);
+  double inv_hi = 1.0 / hi;
   double ai = col(P, C_ALPHA, N, i), bi = col(P, C_BETA, N, i);
   double tii = K.ti ? col(P, C_TI, N, i) : 0.0;
   double Si[6];
@@ -193,17 +201,18 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
   int len = P.row_len[i];
   for (int k = 0; k < len; ++k) {
     int j = nb_index(P.nbr[(size_t)k * N + i]);
-    PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+    PairGeo g = pair_geo(xi0, xi1, xi2, hi, inv_hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                          col(P, C_H, N, j));
     double Alpha = (ai + col(P, C_ALPHA, N, j)) / 2.0, Beta = (bi + col(P, C_BETA, N, j)) / 2.0;
     double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
     double PIs = 0.0;
     if (Alpha != 0.0 || Beta != 0.0) {
       double dvx = v0 * g.x0 + v1 * g.x1 + v2 * g.x2;
-      if (dvx < 0) {
-        double MU = g.hh * dvx / (g.r * g.r + 0.01 * g.hh * g.hh);
+      if (dvx < 0) {  // MU = h dvx / Dn, PIs = (Alpha Cij MU + Beta MU^2) / rho_bar in one division
+        double Dn = g.r * g.r + 0.01 * g.hh * g.hh;
+        double hv = g.hh * dvx;
         double Cij = 0.5 * (csi + col(P, C_CS, N, j));
-        PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5 * (rhoi + col(P, C_RHO, N, j)));
+        PIs = hv * (Alpha * Cij * Dn + Beta * hv) / (Dn * Dn * (0.5 * (rhoi + col(P, C_RHO, N, j))));
       }
     }
     double S0 = Si[0] + col(P, C_SRHO + 0, N, j) + PIs;
@@ -420,10 +429,11 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
   }
   if (icol(P, I_KIND, N, i) == 0) {
     double hi = col(P, C_H, N, i);
+    double inv_hi = 1.0 / hi;
     int len = P.row_len[i];
     for (int k = 0; k < len; ++k) {
       int j = nb_index(P.nbr[(size_t)k * N + i]);
-      PairGeo g = pair_geo(xi0, xi1, xi2, hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+      PairGeo g = pair_geo(xi0, xi1, xi2, hi, inv_hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                            col(P, C_H, N, j));
       double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
       if (K.gradcorr) {  // locking form m_j (rho_i/rho_j) v_ij . vc_i (InteractionAlt.cpp:589-605)
@@ -492,6 +502,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
     maxpl = col(P, C_PLS, N, i);
     if (icol(P, I_KIND, N, i) == 0) {
       double hi = col(P, C_H, N, i);
+      double inv_hi = 1.0 / hi;
       double sr[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};
       // CalcKinEnergyEqn and CalcTempInc pair sums, on the same positions and
       // velocities as the rates (Domain.cpp:1752-1808, Thermal.cpp:53-219)
@@ -503,7 +514,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
       for (int k = 0; k < len; ++k) {
         int e = P.nbr[(size_t)k * N + i];
         int j = nb_index(e);
-        PairGeo g = pair_geo(x[0], x[1], x[2], hi, col(P, C_XN, N, j), col(P, C_XN + 1, N, j), col(P, C_XN + 2, N, j),
+        PairGeo g = pair_geo(x[0], x[1], x[2], hi, inv_hi, col(P, C_XN, N, j), col(P, C_XN + 1, N, j), col(P, C_XN + 2, N, j),
                              col(P, C_H, N, j));
         double b0 = v[0] - col(P, C_VN, N, j), b1 = v[1] - col(P, C_VN + 1, N, j), b2 = v[2] - col(P, C_VN + 2, N, j);
         {
