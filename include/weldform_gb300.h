@@ -81,9 +81,14 @@ int wf_domain_destroy(wf_domain* d);
  * "gradKernelCorr" (kernel-gradient correction, Domain.cpp:1832-1940; plain
  * FP64 form; the correction matrix is recomputed at the first step and, for
  * the leapfrog solver, after every rebuild),
+ * "h_update" (Domain::h_update: UpdateSmoothingLength, Domain.cpp:2493-2510,
+ * after each regular rebuild; both solvers reach it with dDensity already
+ * zeroed by StartAcceleration, so h does not change: accepted, no effect),
  * "precision" (WF_PRECISION_*), "device" (CUDA device ordinal, before the
  * prologue), "use_graph" (replay each step as one CUDA graph, default 1),
- * "cpu_threads" (unused on the GPU path). */
+ * "gather_block" (threads per block of the mixed form's gathers: 64, 128,
+ * 256 or 512), "cpu_threads" (unused on the GPU path).  Read back with
+ * wf_get_domain_i32: "gather_block". */
 int wf_set_domain_f64(wf_domain* d, const char* name, double value);
 int wf_set_domain_i32(wf_domain* d, const char* name, int value);
 /* Read-back of scalars: "Time", "deltat", "hmax", "int_energy_sum",

@@ -242,13 +242,14 @@ struct Domain {
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int mode = 0;       // 0 canonical, 1 reference-structured
   int integrator = 0; // 0 kick-drift (SolverKickDrift.cpp), 1 leapfrog (SolverLeapfrog.cpp)
+  int h_update = 0;   // Domain::h_update (Domain.cpp:149; JSON "smoothlenUpdate", WeldForm.cpp:377-389)
   int grad_corr = 0;  // Domain::gradKernelCorr (Domain.cpp:130; forces the locking sums, SolverKickDrift.cpp:107-110)
   int nthreads = 1;
 
   // particles (SoA, original order)
   int N = 0, solid_part_count = -1;
   std::vector<V3> x, v, a, x_prev, disp, normal, contforce;
-  std::vector<double> rho, rho0, mass, h, Cs, P0, G, pressure, pl_strain, delta_pl_strain, sigmay, Ep,
+  std::vector<double> rho, rho0, mass, h, hini, Cs, P0, G, pressure, pl_strain, delta_pl_strain, sigmay, Ep,
       eff_strain_rate, T, dTdt, k_T, cp_T, th_exp, q_plheat, q_conv, q_source, q_cont_conv, ps_energy, alpha,
       beta, TI, TIn, TIInitDist, dDensity, cont_stiff, delta_cont, dkin, dint;
   std::vector<M3> sigma, tau, srate, rrate, strain, strain_pl, strain_pl_incr, TIR, gcm;
@@ -298,7 +299,7 @@ struct Domain {
     // Particle.cpp:28-157 constructor defaults
     x.push_back(xx); v.push_back(v3(0, 0, 0)); a.push_back(v3(0, 0, 0)); x_prev.push_back(xx);
     disp.push_back(v3(0, 0, 0)); normal.push_back(v3(0, 0, 0)); contforce.push_back(v3(0, 0, 0));
-    rho.push_back(dens); rho0.push_back(dens); mass.push_back(m0); h.push_back(hh); Cs.push_back(0); P0.push_back(0);
+    rho.push_back(dens); rho0.push_back(dens); mass.push_back(m0); h.push_back(hh); hini.push_back(hh); Cs.push_back(0); P0.push_back(0);
     G.push_back(0); pressure.push_back(0); pl_strain.push_back(0); delta_pl_strain.push_back(0); sigmay.push_back(0);
     Ep.push_back(0); eff_strain_rate.push_back(0); T.push_back(0); dTdt.push_back(0); k_T.push_back(0);
     cp_T.push_back(0); th_exp.push_back(0); q_plheat.push_back(0); q_conv.push_back(0); q_source.push_back(0);
@@ -1342,6 +1343,7 @@ struct Domain {
     if (mx > MIN_PS_FOR_NBSEARCH || isfirst || check_nb_every_time)
       if (ts_i == 0 && nb_cleared) {
         if ((rc = neighbour_search())) return rc;
+        if (h_update) update_smoothing_length();  // after CalcPairPosList (SolverKickDrift.cpp:169-171)
         if (contact && (rc = contact_nb_update())) return rc;
         regular = true;
       }
@@ -1350,6 +1352,16 @@ struct Domain {
     // search and at the first step (SolverLeapfrog.cpp:186-204).
     if (grad_corr && (isfirst || (integrator == 1 && regular))) calc_grad_corr();
     return WF_OK;
+  }
+  // UpdateSmoothingLength (Domain.cpp:2493-2510): h -= h/3 (dDensity/Density) dt
+  // within (hmin, hmax) = (h0/2, h0) (Particle.cpp:58-61).  Both solvers call
+  // it after StartAcceleration has zeroed dDensity (Domain.cpp:1586), so
+  // htent == h, which is never below hmax = h0 while h == h0: h stays h0.
+  void update_smoothing_length() {
+    for (int i = 0; i < solid_part_count; i++) {
+      double htent = h[i] - h[i] * 0.33333333 * dDensity[i] / rho[i] * deltat;
+      if (htent > 0.5 * hini[i] && htent < hini[i]) h[i] = htent;
+    }
   }
   // The rest of the step (force passes, kicks, drift, stress, thermal, bookkeeping).
   void finish_step() {
@@ -1523,6 +1535,7 @@ int wfo_set_domain_i32(wfo_domain* p, const char* name, int v) {
   else if (n == "cpu_mode") d->mode = v;
   else if (n == "integrator") d->integrator = v;
   else if (n == "gradKernelCorr") d->grad_corr = v;
+  else if (n == "h_update") d->h_update = v != 0;
   else if (n == "cpu_threads" || n == "Nproc") d->nthreads = v > 0 ? v : 1;
   else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }

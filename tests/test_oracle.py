@@ -134,3 +134,27 @@ def test_kernel_gradient_correction_matrix():
     assert aniso[nb < 0.6 * nb.max()].min() > 0.05
     assert np.array_equal(out[0][0], np.broadcast_to(np.eye(3), out[0][0].shape))
     assert rel_l2(out[1][2], out[0][2]) > 1e-12
+
+
+def test_smoothing_length_update_leaves_h_unchanged():
+    """UpdateSmoothingLength (Domain.cpp:2493-2510) runs after each regular
+    rebuild, but both solvers call it after StartAcceleration zeroed dDensity,
+    so htent == h and h never leaves h0: a yielding run with the flag set is
+    identical to one without, in both integrators."""
+    import numpy as np
+    from tests._support import oracle_domain
+    from weldform_gb300 import configs
+    for integ in (0, 1):
+        out = []
+        for flag in (0, 1):
+            d = oracle_domain()
+            d.set("integrator", integ)
+            d.set("h_update", flag)
+            case = configs.cylinder_upsetting(d, R=0.002, L=0.004, dx=0.0005, v_top=-20.0)
+            d.prepare(case.dt)
+            d.step(40)
+            assert d.geti("nb_searches") > 2
+            out.append((d.get_array("h"), d.get_array("x"), d.get_array("Sigma")))
+            d.close()
+        for a, b in zip(out[0], out[1]):
+            assert np.array_equal(a, b)

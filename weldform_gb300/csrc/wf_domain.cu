@@ -149,6 +149,7 @@ struct wf_domain {
   cudaGraphExec_t graph = nullptr;
   int graph_precision = -1;
   int graph_block = -1;
+  bool h_update = false;  // accepted; no effect in these solvers (see "h_update" in the setter)
   int gblock = 256;
   int graph_key() const { return gblock; }
   struct Region { void* p; size_t bytes; };
@@ -1200,6 +1201,12 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     d->integrator = v;
   }
   else if (n == "gradKernelCorr") d->grad_corr = v != 0;
+  // Domain::h_update (JSON "smoothlenUpdate"): UpdateSmoothingLength
+  // (Domain.cpp:2493-2510) runs after each regular search, but both solvers
+  // reach it after StartAcceleration zeroed dDensity (Domain.cpp:1586), so it
+  // forms htent = h, which fails htent < hmax = h0: h never changes.  The flag
+  // is accepted and the step is unchanged (the oracle restates the call).
+  else if (n == "h_update") d->h_update = v != 0;
   else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
   else if (n == "GradientType") { if (v) return set_err(WF_ERR_UNSUPPORTED, "only GradientType 0 is supported"); }

@@ -140,8 +140,8 @@ def build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = N
         dom.set("gradKernelCorr", 1)
     if int(config.get("stressGradType", 0)) != 0:
         _unsupported("stressGradType != 0")
-    if config.get("smoothlenUpdate", False):
-        _unsupported("smoothing-length update")
+    if config.get("smoothlenUpdate", False):  # WeldForm.cpp:377-389 (no effect on h in these solvers)
+        dom.set("h_update", 1)
     tensins = float(config.get("tensileInstability", 0.3))
     dom.set("ts_nb_inc", int(config.get("nbsearchFreq", 5)))
     # ---- Domain block (WeldForm.cpp:395-560)
