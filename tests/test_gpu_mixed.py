@@ -125,3 +125,16 @@ def test_mixed_gather_block_sizes_agree_bitwise():
     for r in res[1:]:
         for f in r:
             assert np.array_equal(r[f], res[0][f]), f
+
+
+@pytest.mark.parametrize("integrator", [0, 1], ids=["kickdrift", "leapfrog"])
+def test_mixed_kernel_gradient_correction(integrator):
+    """gradKernelCorr in the mixed form: corrected FP32 gradients in the
+    acceleration, density (locking form), rate and conduction gathers, the
+    matrix formed in FP64 on the solver's schedule."""
+    from tests.test_gpu_parity import _grad_corr, _grad_corr_leapfrog
+    build = _grad_corr if integrator == 0 else _grad_corr_leapfrog
+    f = FIELDS + ("pl_strain", "T")
+    m, o = _run(build, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0, model=JOHNSON_COOK, thermal=True)
+    assert o["pl_strain"].max() > 1e-2
+    _check(m, o, f)

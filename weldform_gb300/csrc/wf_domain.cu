@@ -657,8 +657,6 @@ struct wf_domain {
     return k;
   }
   void launch_one_step() {
-    if (K.gradcorr && precision == WF_PRECISION_MIXED)
-      throw CudaError{WF_ERR_UNSUPPORTED, "kernel-gradient correction runs in the plain FP64 form"};
     wf::DomainConst k = kconst();
     if (k.mixed) wf::launch_step_mixed(P, k, d_fscratch, d_iscratch, stream);
     else wf::launch_step_fp64(P, k, d_fscratch, d_iscratch, stream);

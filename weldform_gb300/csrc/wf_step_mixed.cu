@@ -66,6 +66,24 @@ __device__ __forceinline__ float grad_kernel_f(float r2, float hh, float* r_out)
   return C * w;
 }
 
+// Kernel-gradient correction of the locking sums (gradKernelCorr): the
+// corrected gradient Mult(GK gradCorrM_i, x_ij) (InteractionAlt.cpp:114-132),
+// with the particle's own matrix in FP32.
+struct CorrM {
+  float m[9];
+};
+__device__ __forceinline__ CorrM load_corr(const DevPtrs& P, size_t N, int i) {
+  CorrM c;
+  for (int k = 0; k < 9; ++k) c.m[k] = (float)col(P, C_GCM + k, N, i);
+  return c;
+}
+__device__ __forceinline__ void corr_gk(const CorrM& c, float GK, float x0, float x1, float x2, float& g0, float& g1,
+                                        float& g2) {
+  g0 = GK * (c.m[0] * x0 + c.m[1] * x1 + c.m[2] * x2);
+  g1 = GK * (c.m[3] * x0 + c.m[4] * x1 + c.m[5] * x2);
+  g2 = GK * (c.m[6] * x0 + c.m[7] * x1 + c.m[8] * x2);
+}
+
 // ---------------------------------------------------------------- records
 __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
   if (!force && !P.st->do_search) return;
@@ -97,7 +115,8 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
 // ---------------------------------------------------------------- accel
 // AVU: every solid particle has the same (alpha, beta), so the pair mean is
 // the value itself and the gather reads neither particle's misc group.
-template <bool TI, bool AVU>
+// GC: kernel-gradient correction (temp_c = Mult(vc_i, S), InteractionAlt.cpp:166-170).
+template <bool TI, bool AVU, bool GC>
 __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   if (icol(P, I_KIND, N, i) != 0) {
@@ -111,6 +130,8 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
   float tii = 0.f;
   if (TI) { t0 = ld4(ri + (size_t)RC_TI0 * N); t1 = ld4(ri + (size_t)RC_TI1 * N); tii = (float)col(P, C_TI, N, i); }
+  CorrM cm;
+  if (GC) cm = load_corr(P, N, i);
   KSum a0, a1, a2;
   int len = P.row_len[i];
   const int* nb = P.nbr + i;
@@ -155,6 +176,7 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
       }
     }
     float g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
+    if (GC) corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
     float mj = jxl.w;
     a0.add(mj * (g0 * S0 + g1 * S3 + g2 * S4));
     a1.add(mj * (g0 * S3 + g1 * S1 + g2 * S5));
@@ -162,12 +184,15 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   }
   colw(P, C_A, N, i) = a0.value(); colw(P, C_A + 1, N, i) = a1.value(); colw(P, C_A + 2, N, i) = a2.value();
 }
-template <bool TI, bool AVU>
+template <bool TI, bool AVU, bool GC>
 __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { accel_mx<TI, AVU>(P, K, i); });
+  run_rows(K, [&](int i) { accel_mx<TI, AVU, GC>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- density + drift + kick
+// GC: the locking sum with corrected gradients, m_j (rho_i / rho_j) v_ij . vc_i
+// (InteractionAlt.cpp:589-605), which carries rho_i inside the sum.
+template <bool GC>
 __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   double dt = K.dt;
@@ -178,6 +203,9 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   float4 xh = ld4(ri + (size_t)RC_XH * N);
   if (solid) {
     float4 xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
+    CorrM cm;
+    if (GC) cm = load_corr(P, N, i);
+    float rhoif = (float)rhoi;
     KSum s;
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
@@ -189,9 +217,15 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
       float v0 = (vh.x - jvh.x) + (vl.x - jvl.x), v1 = (vh.y - jvh.y) + (vl.y - jvl.y), v2 = (vh.z - jvh.z) + (vl.z - jvl.z);
       float r;
       float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
-      s.add(jvl.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
+      if (GC) {
+        float g0, g1, g2;
+        corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
+        s.add(jxl.w * (rhoif / jvh.w) * (v0 * g0 + v1 * g1 + v2 * g2));
+      } else {
+        s.add(jvl.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
+      }
     }
-    dd = s.value() * rhoi;
+    dd = GC ? s.value() : s.value() * rhoi;
   }
   colw(P, C_DRHO, N, i) = dd;
   double rn = rhoi + dt * dd;
@@ -225,14 +259,18 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   r[(size_t)RN_VL * N] = make_float4(nvl[0], nvl[1], nvl[2], (float)mrn);
   r[(size_t)RN_E * N] = make_float4(solid ? (float)(pn / (rn * rn)) : 0.f, ri[(size_t)RC_MISC * N].z, th, tl);
 }
+template <bool GC>
 __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { density_drift_mx(P, K, i); });
+  run_rows(K, [&](int i) { density_drift_mx<GC>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- rates + energy + conduction
 // Gather at x(n+1), v(n+1): strain/rotation rate sums (InteractionAlt.cpp:263-479),
 // the kinetic-energy pair sum (Domain.cpp:1752-1808) and conduction (Thermal.cpp:53-219).
-template <bool THERMAL>
+// GC: rates and conduction with corrected gradients (InteractionAlt.cpp:330-350,
+// 425-450; Thermal.cpp:90-107), weights (float)(m_j / rho_j); the kinetic-energy
+// pair term keeps the plain gradient, as the reference's.
+template <bool THERMAL, bool GC>
 __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -240,7 +278,9 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
   if (icol(P, I_KIND, N, i) == 0) {
     const float4* ri = P.rn + i;
     float4 xh = ld4(ri + (size_t)RN_XH * N), xl = ld4(ri + (size_t)RN_XL * N), vh = ld4(ri + (size_t)RN_VH * N), vl = ld4(ri + (size_t)RN_VL * N), e = ld4(ri + (size_t)RN_E * N);
-    KSum M[9];  // sum_j (m_j / rho_j) (-GK / 2) (v_i - v_j)_k (x_i - x_j)_l
+    CorrM cm;
+    if (GC) cm = load_corr(P, N, i);
+    KSum M[9];  // sum_j (m_j / rho_j) (-GK / 2) (v_i - v_j)_k (x_i - x_j)_l  (GC: gk_l for GK x_l)
     KSum kin, cnd;
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
@@ -254,11 +294,16 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       float b0 = (vh.x - jvh.x) + (vl.x - jvl.x), b1 = (vh.y - jvh.y) + (vl.y - jvl.y), b2 = (vh.z - jvh.z) + (vl.z - jvl.z);
       float r;
       float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
+      float y0 = x0, y1 = x1, y2 = x2;
       float w = jvl.w * (-0.5f * GK);
+      if (GC) {  // -1/2 (float)(m_j/rho_j) (v_ij (x) gk), gk = M_i GK x_ij
+        corr_gk(cm, GK, x0, x1, x2, y0, y1, y2);
+        w = jvl.w * -0.5f;
+      }
       float wb0 = w * b0, wb1 = w * b1, wb2 = w * b2;
-      M[0].add(wb0 * x0); M[1].add(wb0 * x1); M[2].add(wb0 * x2);
-      M[3].add(wb1 * x0); M[4].add(wb1 * x1); M[5].add(wb1 * x2);
-      M[6].add(wb2 * x0); M[7].add(wb2 * x1); M[8].add(wb2 * x2);
+      M[0].add(wb0 * y0); M[1].add(wb0 * y1); M[2].add(wb0 * y2);
+      M[3].add(wb1 * y0); M[4].add(wb1 * y1); M[5].add(wb1 * y2);
+      M[6].add(wb2 * y0); M[7].add(wb2 * y1); M[8].add(wb2 * y2);
       bool up = nb_up(ent);  // original index of j larger than i's
       float dv = GK * (b0 * x0 + b1 * x1 + b2 * x2);
       float pk = 0.5f * (up ? jxl.w : xl.w) * (e.x + je.x) * dv;
@@ -266,7 +311,9 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       if (THERMAL) {
         float wt = up ? jvl.w : vl.w;  // m_P2 / rho_P2 for both ends of the pair
         float dT = (e.z - je.z) + (e.w - je.w);
-        cnd.add(wt * 4.f * (e.y * je.y) / (e.y + je.y) * dT * GK);
+        // x.(GK x)/r^2 = GK; with the correction x.gk/r^2 (Thermal.cpp:90-107)
+        float gr = GC ? (x0 * y0 + x1 * y1 + x2 * y2) / (x0 * x0 + x1 * x1 + x2 * x2) : GK;
+        cnd.add(wt * 4.f * (e.y * je.y) / (e.y + je.y) * dT * gr);
       }
     }
     double m[9];
@@ -281,9 +328,9 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
   colw(P, C_DKIN, N, i) = dkin;
   colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
 }
-template <bool THERMAL>
+template <bool THERMAL, bool GC>
 __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { rate_mx<THERMAL>(P, K, i); });
+  run_rows(K, [&](int i) { rate_mx<THERMAL, GC>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- elementwise update
@@ -480,6 +527,12 @@ void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, c
   mark(s, "k_refresh_records");
 }
 
+template <bool TI, bool AVU>
+static void launch_accel_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
+  if (K.gradcorr) k_accel_mx<TI, AVU, true><<<ng, gb, 0, s>>>(P, K);
+  else k_accel_mx<TI, AVU, false><<<ng, gb, 0, s>>>(P, K);
+}
+
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
   int nb = nblk(K.N, BLOCK);
   int gb = (K.gblock == 64 || K.gblock == 128 || K.gblock == 512) ? K.gblock : 256;
@@ -488,21 +541,27 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   launch_refresh_shadows(P, K, 0, s);
   launch_tensile(P, K, s);
   if (K.ti) {
-    if (K.av_uniform) k_accel_mx<true, true><<<ng, gb, 0, s>>>(P, K);
-    else k_accel_mx<true, false><<<ng, gb, 0, s>>>(P, K);
+    if (K.av_uniform) launch_accel_mx<true, true>(P, K, ng, gb, s);
+    else launch_accel_mx<true, false>(P, K, ng, gb, s);
   } else {
-    if (K.av_uniform) k_accel_mx<false, true><<<ng, gb, 0, s>>>(P, K);
-    else k_accel_mx<false, false><<<ng, gb, 0, s>>>(P, K);
+    if (K.av_uniform) launch_accel_mx<false, true>(P, K, ng, gb, s);
+    else launch_accel_mx<false, false>(P, K, ng, gb, s);
   }
   mark(s, "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
-  k_density_drift_mx<<<ng, gb, 0, s>>>(P, K);
+  if (K.gradcorr) k_density_drift_mx<true><<<ng, gb, 0, s>>>(P, K);
+  else k_density_drift_mx<false><<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  if (K.thermal_solver) k_rate_mx<true><<<ng, gb, 0, s>>>(P, K);
-  else k_rate_mx<false><<<ng, gb, 0, s>>>(P, K);
+  if (K.thermal_solver) {
+    if (K.gradcorr) k_rate_mx<true, true><<<ng, gb, 0, s>>>(P, K);
+    else k_rate_mx<true, false><<<ng, gb, 0, s>>>(P, K);
+  } else {
+    if (K.gradcorr) k_rate_mx<false, true><<<ng, gb, 0, s>>>(P, K);
+    else k_rate_mx<false, false><<<ng, gb, 0, s>>>(P, K);
+  }
   mark(s, "k_rate_mx");
   if (K.pl_heating) {
     if (K.thermal_solver) k_stress_mx<true, true><<<nb, BLOCK, 0, s>>>(P, K);
