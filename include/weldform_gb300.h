@@ -73,14 +73,21 @@ int wf_domain_destroy(wf_domain* d);
 
 /* Domain scalar fields (Source/Domain.h:113-537).  Names are the reference
  * member names: "Cellfac", "pl_work_heat_frac", "friction_sta",
- * "friction_dyn", "PFAC", "DFAC", "DomMax.x|y|z", "DomMin.x|y|z",
- * "contact_force_factor".  Integer fields: "Nproc", "ts_nb_inc", "auto_ts",
+ * "friction_dyn", "PFAC", "DFAC", "CFL", "sqrt_h_a", "DomMax.x|y|z",
+ * "DomMin.x|y|z", "contact_force_factor".  Integer fields: "Nproc", "ts_nb_inc",
  * "nonlock_sum", "pl_heating", "thermal_solver", "contact",
  * "contact_mesh_auto_update", "GradientType", "contact_alg" (WF_CONTACT_*),
  * "integrator" (0 kick-drift, 1 leapfrog; before the prologue),
  * "gradKernelCorr" (kernel-gradient correction, Domain.cpp:1832-1940; plain
  * FP64 form; the correction matrix is recomputed at the first step and, for
  * the leapfrog solver, after every rebuild),
+ * "auto_ts", "auto_ts_acc", "auto_ts_cont" (adaptive time step after the
+ * contact pass, SolverKickDrift.cpp:216-219 / SolverLeapfrog.cpp:257-260:
+ * CheckMinTSVel, CheckMinTSAccel, AdaptiveTimeStep, Domain.cpp:206-319; the
+ * step never exceeds the solver's initial dt; auto_ts_cont with contact in
+ * the kick-drift solver is WF_ERR_UNSUPPORTED, as it reads a member nothing
+ * on that path sets; f64 fields "CFL" (default 0.7) and "sqrt_h_a" (0.0025)
+ * are the criteria's coefficients; read the current step with "deltat"),
  * "h_update" (Domain::h_update: UpdateSmoothingLength, Domain.cpp:2493-2510,
  * after each regular rebuild; both solvers reach it with dDensity already
  * zeroed by StartAcceleration, so h does not change: accepted, no effect),

@@ -242,6 +242,9 @@ struct Domain {
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int mode = 0;       // 0 canonical, 1 reference-structured
   int integrator = 0; // 0 kick-drift (SolverKickDrift.cpp), 1 leapfrog (SolverLeapfrog.cpp)
+  // adaptive time step (Domain.cpp:107-170 defaults; Domain.h:326-456)
+  int auto_ts = 0, auto_ts_acc = 0, auto_ts_cont = 0;
+  double CFL = 0.7, sqrt_h_a = 0.0025, deltatint = 0, deltatmin = 0;
   int h_update = 0;   // Domain::h_update (Domain.cpp:149; JSON "smoothlenUpdate", WeldForm.cpp:377-389)
   int grad_corr = 0;  // Domain::gradKernelCorr (Domain.cpp:130; forces the locking sums, SolverKickDrift.cpp:107-110)
   int nthreads = 1;
@@ -1278,7 +1281,11 @@ struct Domain {
       if (pres_eq[i] != 0) return set_err(WF_ERR_UNSUPPORTED, "only PresEq = 0 is supported");
     }
     if (solid_part_count < 0) solid_part_count = N;
-    deltat = dt;
+    if (auto_ts_cont && contact && integrator == 0)
+      return set_err(WF_ERR_UNSUPPORTED,
+                     "auto_ts_cont with contact: the kick-drift solver reads Domain::min_force_ts, which nothing "
+                     "on its contact path sets");
+    deltat = deltatint = deltatmin = dt;  // SolverKickDrift.cpp:30, SolverLeapfrog.cpp:33
     for (int i = 0; i < N; i++) pressure[i] = eos0(Cs[i], P0[i], rho[i], rho0[i]);  // InitialChecks
     int rc = cell_initiate();
     if (rc) return rc;
@@ -1363,6 +1370,49 @@ struct Domain {
       if (htent > 0.5 * hini[i] && htent < hini[i]) h[i] = htent;
     }
   }
+  // CheckMinTSVel (Domain.cpp:265-299): CFL * (shortest neighbour distance) /
+  // (Cs + |v|) over every particle (no neighbours: distance 1000).
+  void check_min_ts_vel() {
+    deltatmin = deltatint;
+    for (int i = 0; i < N; i++) {
+      double mn = 1000.;
+      for (int64_t k = nb_off[i]; k < nb_off[i + 1]; ++k) {
+        double d = norm(sub(x[nb_idx[k]], x[i]));
+        if (d < mn) mn = d;
+      }
+      double test = CFL * mn / (Cs[i] + norm(v[i]));
+      if (deltatmin > test) deltatmin = test;
+    }
+  }
+  // CheckMinTSAccel (Domain.cpp:304-319): sqrt_h_a sqrt(h / |a|); it restarts
+  // from deltatint, so with both criteria on only this one counts.
+  void check_min_ts_accel() {
+    deltatmin = deltatint;
+    for (int i = 0; i < N; i++) {
+      double test = sqrt_h_a * std::sqrt(h[i] / norm(a[i]));
+      if (deltatmin > test) deltatmin = test;
+    }
+  }
+  // AdaptiveTimeStep (Domain.cpp:206-239).  The contact term (auto_ts_cont)
+  // reads min_force_ts, which the leapfrog solver sets to the initial dt
+  // (SolverLeapfrog.cpp:95), never below deltat; the kick-drift solver is
+  // rejected at the prologue.  The floor manual_min_ts is an int member
+  // (Domain.h:328) holding 0, so it never applies.
+  void adaptive_time_step() {
+    if (deltatint > deltatmin) {
+      if (deltat < deltatmin) deltat = 2.0 * deltat * deltatmin / (deltat + deltatmin);
+      else deltat = deltatmin;
+    } else {
+      if (deltatint != deltat) deltat = 2.0 * deltat * deltatint / (deltat + deltatint);
+      else deltat = deltatint;
+    }
+  }
+  void time_step_control() {
+    prev_deltat = deltat;
+    if (auto_ts) check_min_ts_vel();
+    if (auto_ts_acc) check_min_ts_accel();
+    if (auto_ts || auto_ts_acc) adaptive_time_step();
+  }
   // The rest of the step (force passes, kicks, drift, stress, thermal, bookkeeping).
   void finish_step() {
     pass_accel();
@@ -1374,7 +1424,7 @@ struct Domain {
       if (isfirst)
         for (int i = 0; i < N; i++) v[i] = sub(v[i], v3(a[i].c[0] * 0.5 * deltat, a[i].c[1] * 0.5 * deltat, a[i].c[2] * 0.5 * deltat));
       general_after();
-      prev_deltat = deltat;
+      time_step_control();  // SolverLeapfrog.cpp:257-260
       for (int i = 0; i < N; i++) {
         double f = 0.5 * (prev_deltat + deltat);
         v[i] = add(v[i], v3(a[i].c[0] * f, a[i].c[1] * f, a[i].c[2] * f));
@@ -1390,7 +1440,7 @@ struct Domain {
       }
       pass_rates();  // x at n+1, v at n+1/2 (:287-291)
     } else {
-    prev_deltat = deltat;
+    time_step_control();  // SolverKickDrift.cpp:216-219
     for (int i = 0; i < N; i++) v[i] = add(v[i], scl(0.5 * prev_deltat, a[i]));
     general_after();
     pass_density();
@@ -1517,6 +1567,8 @@ int wfo_set_domain_f64(wfo_domain* p, const char* name, double v) {
   else if (n == "friction_sta") d->friction_sta = v;
   else if (n == "friction_dyn") d->friction_dyn = v;
   else if (n == "PFAC") d->PFAC = v;
+  else if (n == "CFL") d->CFL = v;
+  else if (n == "sqrt_h_a") d->sqrt_h_a = v;
   else if (n == "DFAC") d->DFAC = v;
   else if (n == "contact_force_factor") {}
   else if (n.rfind("DomMax.", 0) == 0 && n.size() == 8) d->DomMax[n[7] - 'x'] = v;
@@ -1537,7 +1589,9 @@ int wfo_set_domain_i32(wfo_domain* p, const char* name, int v) {
   else if (n == "gradKernelCorr") d->grad_corr = v;
   else if (n == "h_update") d->h_update = v != 0;
   else if (n == "cpu_threads" || n == "Nproc") d->nthreads = v > 0 ? v : 1;
-  else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
+  else if (n == "auto_ts") d->auto_ts = v != 0;
+  else if (n == "auto_ts_acc") d->auto_ts_acc = v != 0;
+  else if (n == "auto_ts_cont") d->auto_ts_cont = v != 0;
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
   else if (n == "GradientType") { if (v) return set_err(WF_ERR_UNSUPPORTED, "only GradientType 0 is supported"); }
   else if (n == "precision" || n == "device" || n == "use_graph") {}
@@ -1781,6 +1835,7 @@ int wfo_adjoint_reaction_loss(wfo_domain* p, int64_t steps, int every, int mesh,
   if (d->mode != 0) return set_err(WF_ERR_UNSUPPORTED, "the tangent run needs cpu_mode 0");
   if (d->integrator != 0) return set_err(WF_ERR_UNSUPPORTED, "the adjoint differentiates the kick-drift step");
   if (d->grad_corr) return set_err(WF_ERR_UNSUPPORTED, "adjoint: kernel-gradient correction is not supported");
+  if (d->auto_ts || d->auto_ts_acc) return set_err(WF_ERR_UNSUPPORTED, "adjoint: the time step must be fixed");
   if (!d->contact || mesh < 0 || mesh >= (int)d->meshes.size())
     return set_err(WF_ERR_ARG, "the reaction-force loss needs a rigid mesh");
   if (axis < 0 || axis > 2 || every < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps || !target || !loss ||

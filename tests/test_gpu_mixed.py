@@ -138,3 +138,14 @@ def test_mixed_kernel_gradient_correction(integrator):
     m, o = _run(build, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0, model=JOHNSON_COOK, thermal=True)
     assert o["pl_strain"].max() > 1e-2
     _check(m, o, f)
+
+
+def test_mixed_adaptive_time_step():
+    """Velocity-criterion adaptive step in the mixed form: the step, Time and
+    state stay within the mixed form's bar of the oracle."""
+    from tests.test_gpu_parity import _auto_ts
+    f = FIELDS + ("pl_strain",)
+    m, o = _run(_auto_ts(1, 0, 0), 200, f, ("deltat", "Time"), R=0.004, L=0.008, dx=0.0005, v_top=-20.0, cfl=0.8)
+    _check(m, o, f)
+    assert abs(m["deltat"] - o["deltat"]) <= TOL * o["deltat"]
+    assert abs(m["Time"] - o["Time"]) <= TOL * o["Time"]

@@ -245,3 +245,60 @@ def test_kernel_gradient_correction(build):
     g, o = _pair(build, 60, f, SCALARS, R=0.004, L=0.008, dx=0.0005, v_top=-20.0, model=JOHNSON_COOK, thermal=True)
     assert o["pl_strain"].max() > 1e-3
     _check(g, o, f, SCALARS)
+
+
+def _auto_ts(vel, acc, integrator):
+    def build(dom, **kw):
+        dom.set("auto_ts", vel)
+        dom.set("auto_ts_acc", acc)
+        dom.set("integrator", integrator)
+        return configs.cylinder_upsetting(dom, **kw)
+    return build
+
+
+@pytest.mark.parametrize("vel,acc,integrator", [(1, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 1)],
+                         ids=["velocity", "acceleration", "both", "leapfrog_velocity"])
+def test_adaptive_time_step(vel, acc, integrator):
+    """CheckMinTSVel / CheckMinTSAccel / AdaptiveTimeStep on the device:
+    with a step above the CFL bound (cfl 0.8) the step shrinks; the state,
+    the step size and Time follow the oracle."""
+    f = FIELDS
+    g, o = _pair(_auto_ts(vel, acc, integrator), 60, f, SCALARS + ("deltat", "Time"), R=0.004, L=0.008,
+                 dx=0.0005, v_top=-20.0, cfl=0.8)
+    h = 1.2 * 0.0005
+    assert o["deltat"] < 0.95 * 0.8 * h / configs.Steel().Cs
+    _check(g, o, f, SCALARS + ("deltat", "Time"))
+
+
+def test_adaptive_time_step_with_contact_leapfrog_and_solve_loop():
+    """The leapfrog solver with penalty contact and all three autoTS flags
+    (its min_force_ts is the initial dt, so the contact criterion is inert),
+    run through SolveDiffUpdateLeapFrog's loop control with outputs: step
+    count, Time and state follow the oracle."""
+    res = {}
+    for name in ("gpu", "oracle"):
+        d = gpu_domain() if name == "gpu" else oracle_domain()
+        if name == "oracle":
+            d.set("cpu_threads", THREADS)
+        for k in ("auto_ts", "auto_ts_acc", "auto_ts_cont"):
+            d.set(k, 1)
+        d.set("integrator", 1)
+        case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, gap=0.0, stiffness="area")
+        d.SolveDiffUpdateLeapFrog(20 * case.dt, case.dt, 5 * case.dt)
+        res[name] = (d.geti("steps"), d.Time, d.get("deltat"), d.get_array("x"), d.contact_force(case.mesh))
+        d.close()
+    g, o = res["gpu"], res["oracle"]
+    assert g[0] == o[0] and g[0] > 20
+    assert abs(g[1] - o[1]) <= 1e-9 * o[1] and abs(g[2] - o[2]) <= 1e-8 * o[2]
+    assert rel_l2(g[3], o[3]) <= TOL
+    assert abs(g[4][2] - o[4][2]) <= 1e-8 * abs(o[4][2])
+
+
+def test_kickdrift_contact_time_step_is_rejected():
+    from weldform_gb300 import WFError
+    d = gpu_domain()
+    d.set("auto_ts_cont", 1)
+    case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_punch=-10.0)
+    with pytest.raises(WFError):
+        d.prepare(case.dt)
+    d.close()

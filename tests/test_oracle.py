@@ -158,3 +158,17 @@ def test_smoothing_length_update_leaves_h_unchanged():
             d.close()
         for a, b in zip(out[0], out[1]):
             assert np.array_equal(a, b)
+
+
+def test_kickdrift_contact_time_step_is_rejected_by_the_oracle():
+    """auto_ts_cont with contact in the kick-drift solver reads
+    Domain::min_force_ts, which nothing on that path sets: rejected."""
+    import pytest
+    from tests._support import oracle_domain
+    from weldform_gb300 import configs, WFError
+    d = oracle_domain()
+    d.set("auto_ts_cont", 1)
+    case = configs.contact_upsetting(d, R=0.002, L=0.004, dx=0.0005, v_punch=-10.0)
+    with pytest.raises(WFError):
+        d.prepare(case.dt)
+    d.close()

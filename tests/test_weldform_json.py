@@ -120,7 +120,7 @@ def test_contact_thermal_input_runs_in_the_oracle(tmp_path):
 
 @pytest.mark.parametrize("patch", [
     ("Configuration", "solver", "Mech-Fraser"),
-    ("Configuration", "autoTS", [True, False, False]),
+    ("Materials", "type", "GMT"),
     ("Materials", "damageModel", "Rankine"),
     ("DomainBlocks", "gridCoordSys", "AxiSymmetric"),
 ])
@@ -132,6 +132,27 @@ def test_unsupported_inputs_are_rejected(patch):
     with pytest.raises(WFError) as e:
         wj.build(j, make=_oracle)
     assert e.value.code == 8
+
+
+def test_default_adaptive_time_step(tmp_path):
+    """Without an autoTS key the driver runs the velocity criterion
+    (WeldForm.cpp:350): with cflFactor 0.8 the CFL bound on the shortest
+    neighbour distance is below the input step, so the step shrinks and the
+    run needs more steps to reach simTime than the fixed-step loop."""
+    j = copy.deepcopy(COMPRESSION)
+    del j["Configuration"]["autoTS"]
+    j["Configuration"]["cflFactor"] = 0.8
+    j["Configuration"]["simTime"] = 10 * DT
+    j["Configuration"]["outTime"] = 5 * DT
+    r = wj.build(j, make=_oracle)
+    assert r.adaptive
+    r.dom.prepare(r.dt)
+    r.dom.step(3)
+    assert r.dom.get("deltat") < 0.9 * r.dt
+    paths = wj.run(j, str(tmp_path), make=_oracle)
+    assert len(paths) >= 2
+    head, rows = _read_csv(paths[-1])
+    assert head == wj.CSV_HEADER
 
 
 @pytest.mark.gpu

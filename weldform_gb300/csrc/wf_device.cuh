@@ -138,13 +138,17 @@ constexpr int ERR_NO_SURFACE = 16;
 // Reduction slots (per-block partials, deterministic tree order).
 enum Slot : int {
   S_DINT = 0, S_DKIN, S_PLW, S_MAXPL, S_MAXT, S_MINT, S_CFSUM, S_CRSUM, S_EXTW,
-  S_CFVEC = 9,  // 3 per mesh
-  NSLOTS = 9 + 3 * MAX_MESHES
+  S_DTV = 9,    // CheckMinTSVel's smallest candidate time step (block minima)
+  S_DTA = 10,   // CheckMinTSAccel's
+  S_CFVEC = 11, // 3 per mesh
+  NSLOTS = 11 + 3 * MAX_MESHES
 };
 
 // Scalars that evolve on the device, so a whole step runs without a host sync.
 struct StepState {
   double Time, deltat;
+  double prev_deltat;  // the step's time step before AdaptiveTimeStep (first kick; leapfrog kick)
+  double deltatint;    // the solver's initial time step (Domain::deltatint)
   double int_energy_sum, kin_energy_sum, plastic_work, contact_force_sum, contact_reaction_sum, ext_forces_work;
   double max_pl;       // max pl_strain at the start of the current step
   double max_pl_next;  // max pl_strain after the current step's stress update
@@ -184,6 +188,8 @@ struct DomainConst {
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
   int leapfrog;        // 1: SolveDiffUpdateLeapFrog's update (velocities at half steps)
   int gradcorr;        // 1: kernel-gradient correction (Domain::gradKernelCorr)
+  int auto_ts, auto_ts_acc;  // adaptive time step: velocity / acceleration criteria
+  double CFL, sqrt_h_a;      // their coefficients (Domain::CFL, Domain::sqrt_h_a)
   int av_uniform;      // 1 when every solid particle has the same Alpha and Beta
   float av_alpha, av_beta;  // those values (the mixed acceleration gather skips their loads)
 };

@@ -150,6 +150,9 @@ struct wf_domain {
   int graph_precision = -1;
   int graph_block = -1;
   bool h_update = false;  // accepted; no effect in these solvers (see "h_update" in the setter)
+  // adaptive time step (Domain.cpp:107-170 defaults)
+  int auto_ts = 0, auto_ts_acc = 0, auto_ts_cont = 0;
+  double CFL = 0.7, sqrt_h_a = 0.0025;
   int gblock = 256;
   int graph_key() const { return gblock; }
   struct Region { void* p; size_t bytes; };
@@ -593,6 +596,10 @@ struct wf_domain {
       K.av_beta = (float)b0;
     }
     K.gradcorr = grad_corr;
+    if (auto_ts_cont && contact && integrator == 0)
+      throw CudaError{WF_ERR_UNSUPPORTED, "auto_ts_cont with contact: the kick-drift solver reads Domain::min_force_ts, "
+                                          "which nothing on its contact path sets"};
+    K.auto_ts = auto_ts; K.auto_ts_acc = auto_ts_acc; K.CFL = CFL; K.sqrt_h_a = sqrt_h_a;
     K.ti = 0;
     for (int p = 0; p < N; ++p)
       if (hp.i[I_KIND][p] == 0 && F(C_TI, p) > 0.0) K.ti = 1;
@@ -604,7 +611,8 @@ struct wf_domain {
     // Step state.
     StepState st;
     memset(&st, 0, sizeof(st));
-    st.deltat = dt; st.isfirst = 1; st.m_minT = 1000.;
+    st.deltat = dt; st.prev_deltat = dt; st.deltatint = dt;  // SolverKickDrift.cpp:30
+    st.isfirst = 1; st.m_minT = 1000.;
     for (size_t m = 0; m < meshes.size(); ++m)
       for (int d = 0; d < 3; ++d) { st.mesh_v[m][d] = meshes[m].mv.c[d]; st.mesh_w[m][d] = meshes[m].mw.c[d]; }
     CK(cudaMemcpyAsync(P.st, &st, sizeof(st), cudaMemcpyHostToDevice, stream));
@@ -834,6 +842,7 @@ struct wf_domain {
     if (K.ti) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: tensile instability (TI > 0) is not supported"};
     if (K.leapfrog) throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint differentiates the kick-drift step"};
     if (K.gradcorr) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: kernel-gradient correction is not supported"};
+    if (K.auto_ts || K.auto_ts_acc) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: the time step must be fixed"};
     if (!contact || mesh < 0 || mesh >= (int)meshes.size())
       throw CudaError{WF_ERR_ARG, "the reaction-force loss needs a rigid mesh"};
     if (axis < 0 || axis > 2 || every < 1 || kchk < 1 || steps < 1 || ntarget < 1 || ntarget * every > steps ||
@@ -1158,6 +1167,8 @@ int wf_set_domain_f64(wf_domain* d, const char* name, double v) {
   else if (n == "friction_sta") d->friction_sta = v;
   else if (n == "friction_dyn") d->friction_dyn = v;
   else if (n == "PFAC") d->PFAC = v;
+  else if (n == "CFL") d->CFL = v;
+  else if (n == "sqrt_h_a") d->sqrt_h_a = v;
   else if (n == "DFAC") d->DFAC = v;
   else if (n == "contact_force_factor") {}
   else if (n.size() == 8 && n.rfind("DomMax.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') d->DomMax[n[7] - 'x'] = v;
@@ -1205,7 +1216,9 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   // forms htent = h, which fails htent < hmax = h0: h never changes.  The flag
   // is accepted and the step is unchanged (the oracle restates the call).
   else if (n == "h_update") d->h_update = v != 0;
-  else if (n == "auto_ts") { if (v) return set_err(WF_ERR_UNSUPPORTED, "auto_ts is not supported"); }
+  else if (n == "auto_ts") d->auto_ts = v != 0;          // CheckMinTSVel + AdaptiveTimeStep
+  else if (n == "auto_ts_acc") d->auto_ts_acc = v != 0;  // CheckMinTSAccel
+  else if (n == "auto_ts_cont") d->auto_ts_cont = v != 0;
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
   else if (n == "GradientType") { if (v) return set_err(WF_ERR_UNSUPPORTED, "only GradientType 0 is supported"); }
   else return set_err(WF_ERR_ARG, "unknown domain i32 field " + n);
@@ -1503,13 +1516,33 @@ int wf_solve_kickdrift(wf_domain* d, double tf, double dt, double dtOut, int64_t
     wf::StepState st = d->read_state();
     double Time = st.Time, tout = st.Time;
     int64_t idx_out = 1;
-    int64_t pending = 0;
+    if (!(d->K.auto_ts || d->K.auto_ts_acc)) {  // fixed dt: the whole loop is known up front
+      int64_t pending = 0;
+      while (Time <= tf && idx_out <= maxidx) {
+        ++pending;
+        Time += st.deltat;
+        if (Time >= tout) { idx_out++; tout += dtOut; }
+      }
+      d->step(pending);
+      return WF_OK;
+    }
+    // Adaptive dt never exceeds deltatint, so n = floor((limit - Time) / deltatint)
+    // further steps cannot carry Time past the next loop or output boundary:
+    // run them as one replay, then read Time back; single steps near a boundary.
     while (Time <= tf && idx_out <= maxidx) {
-      ++pending;
-      Time += st.deltat;
+      double lim = std::min(tf, tout);
+      int64_t n = Time < lim ? (int64_t)std::floor((lim - Time) / st.deltatint) : 0;
+      if (n > 1) {
+        d->step(n - 1);
+        st = d->read_state();
+        Time = st.Time;
+        continue;
+      }
+      d->step(1);
+      st = d->read_state();
+      Time = st.Time;
       if (Time >= tout) { idx_out++; tout += dtOut; }
     }
-    d->step(pending);
     return WF_OK;
   });
 }

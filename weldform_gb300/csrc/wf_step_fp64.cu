@@ -300,8 +300,9 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
   constexpr int NV = NM > 0 ? NM : 1;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
-  double dt = K.dt;
+  double dt = P.st->deltat;  // the step's time step before AdaptiveTimeStep (prev_deltat)
   double cfsum = 0, crsum = 0, extw = 0;
+  double dta = 1.0 / 0.0;  // CheckMinTSAccel candidate (kick-drift, after contact)
   double cfv[NV][3];
   for (int m = 0; m < NV; ++m) cfv[m][0] = cfv[m][1] = cfv[m][2] = 0.0;
   if (i < K.N) {
@@ -384,6 +385,8 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
       colw(P, C_DCONT, N, i) = dcont;
       for (int d = 0; d < 3; ++d) colw(P, C_A + d, N, i) = a[d];
     }
+    if (K.auto_ts_acc && !K.leapfrog)  // Domain.cpp:309
+      dta = K.sqrt_h_a * sqrt(col(P, C_H, N, i) / sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]));
     if (K.leapfrog) {  // first leapfrog step starts from v - a dt/2 (SolverLeapfrog.cpp:233-236)
       if (P.st->isfirst)
         for (int d = 0; d < 3; ++d) {
@@ -399,6 +402,10 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
       }
       if (K.mixed) rec_set_v3(P, N, i, vn);
     }
+  }
+  if (K.auto_ts_acc && !K.leapfrog) {
+    double r = block_reduce<2>(dta, sh);
+    if (threadIdx.x == 0) P.partials[S_DTA * K.nblocks + blockIdx.x] = r;
   }
   if (CONTACT) {
     double r;
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
   size_t N = K.N;
-  double dt = K.dt;
+  double dt = P.st->deltat;
   double xi0 = col(P, C_X, N, i), xi1 = col(P, C_X + 1, N, i), xi2 = col(P, C_X + 2, N, i);
   double vi0 = col(P, C_V, N, i), vi1 = col(P, C_V + 1, N, i), vi2 = col(P, C_V + 2, N, i);
   double rhoi = col(P, C_RHO, N, i);
@@ -471,12 +478,12 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
 }
 
 // Leapfrog kick v(n+1/2) = v(n-1/2) + a (dt_prev + dt)/2 for every particle
-// (SolverLeapfrog.cpp:247-254; dt is fixed, so the factor is dt).
+// (SolverLeapfrog.cpp:264-270).
 __global__ void k_kick_leapfrog(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
   size_t N = K.N;
-  double f = 0.5 * (K.dt + K.dt);
+  double f = 0.5 * (P.st->prev_deltat + P.st->deltat);
   for (int d = 0; d < 3; ++d) {
     double vn = col(P, C_V + d, N, i) + col(P, C_A + d, N, i) * f;
     colw(P, C_V + d, N, i) = vn;
@@ -489,7 +496,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
   __shared__ double sh[32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
-  double dt = K.dt;
+  double dt = P.st->deltat;
   double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300, dkin_b = 0.0, dint = 0.0;
   if (i < K.N) {
     // Next-step buffers become the current state for this particle.
@@ -697,7 +704,7 @@ __global__ void k_mesh_nodes(DevPtrs P, DomainConst K) {
   for (int d = 0; d < 3; ++d) {
     double nv = mv[d] + vr[d];
     P.node_v[d * P.nnodes + n] = nv;
-    P.node[d * P.nnodes + n] = p[d] + nv * K.dt;
+    P.node[d * P.nnodes + n] = p[d] + nv * P.st->deltat;
   }
 }
 // CalcNormals + UpdatePlaneCoeff per element (Mesh.cpp:222-256), then
@@ -825,20 +832,94 @@ void launch_step_head(const DevPtrs& P, const DomainConst& K, double* fscratch, 
     mark(s, "k_grad_corr");
   }
 }
+// ---------------------------------------------------------------- adaptive time step
+// CheckMinTSVel (Domain.cpp:265-299): CFL * (shortest neighbour distance, 1000
+// without neighbours) / (Cs + |v|); CheckMinTSAccel (:304-319):
+// sqrt_h_a * sqrt(h / |a|).  Every particle; block minima into S_DTV / S_DTA.
+__global__ void __launch_bounds__(BLOCK) k_dt_tests(DevPtrs P, DomainConst K, int vel, int acc) {
+  __shared__ double sh[32];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  size_t N = K.N;
+  double tv = 1.0 / 0.0, ta = 1.0 / 0.0;
+  if (i < K.N) {
+    if (vel) {
+      double xi[3] = {col(P, C_X, N, i), col(P, C_X + 1, N, i), col(P, C_X + 2, N, i)};
+      double mn = 1000.;
+      int len = P.row_len[i];
+      for (int k = 0; k < len; ++k) {
+        int j = nb_index(P.nbr[(size_t)k * N + i]);
+        double d0 = col(P, C_X, N, j) - xi[0], d1 = col(P, C_X + 1, N, j) - xi[1], d2 = col(P, C_X + 2, N, j) - xi[2];
+        double d = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        if (d < mn) mn = d;
+      }
+      double v0 = col(P, C_V, N, i), v1 = col(P, C_V + 1, N, i), v2 = col(P, C_V + 2, N, i);
+      tv = K.CFL * mn / (col(P, C_CS, N, i) + sqrt(v0 * v0 + v1 * v1 + v2 * v2));
+    }
+    if (acc) {
+      double a0 = col(P, C_A, N, i), a1 = col(P, C_A + 1, N, i), a2 = col(P, C_A + 2, N, i);
+      ta = K.sqrt_h_a * sqrt(col(P, C_H, N, i) / sqrt(a0 * a0 + a1 * a1 + a2 * a2));
+    }
+  }
+  double r;
+  if (vel) { r = block_reduce<2>(tv, sh); if (threadIdx.x == 0) P.partials[S_DTV * K.nblocks + blockIdx.x] = r; }
+  if (acc) { r = block_reduce<2>(ta, sh); if (threadIdx.x == 0) P.partials[S_DTA * K.nblocks + blockIdx.x] = r; }
+}
+
+// AdaptiveTimeStep (Domain.cpp:206-239) from the candidates' minimum.  Each
+// criterion starts from deltatint and the acceleration one runs second, so
+// with both on only it counts (CheckMinTSAccel resets deltatmin).  The
+// contact term cannot lower deltat here (the leapfrog solver's min_force_ts
+// is the initial dt; kick-drift with it is rejected) and the floor
+// manual_min_ts is an int member holding 0 (Domain.h:328).
+__global__ void k_adapt_dt(DevPtrs P, DomainConst K) {
+  __shared__ double sh[32];
+  double mv = 1.0 / 0.0, ma = 1.0 / 0.0;
+  for (int b = threadIdx.x; b < K.nblocks; b += blockDim.x) {
+    if (K.auto_ts) mv = fmin(mv, P.partials[S_DTV * K.nblocks + b]);
+    if (K.auto_ts_acc) ma = fmin(ma, P.partials[S_DTA * K.nblocks + b]);
+  }
+  mv = block_reduce<2>(mv, sh);
+  ma = block_reduce<2>(ma, sh);
+  if (threadIdx.x != 0) return;
+  StepState* st = P.st;
+  double dint = st->deltatint, dmin = dint;
+  if (K.auto_ts) dmin = fmin(dint, mv);
+  if (K.auto_ts_acc) dmin = fmin(dint, ma);
+  double dt = st->deltat;
+  st->prev_deltat = dt;
+  if (dint > dmin) dt = dt < dmin ? 2.0 * dt * dmin / (dt + dmin) : dmin;
+  else dt = dint != dt ? 2.0 * dt * dint / (dt + dint) : dint;
+  st->deltat = dt;
+}
+
 void launch_bc(const DevPtrs& P, const DomainConst& K, int vcol, cudaStream_t s) {
   int nbc = nblk(K.nbc_particles > 0 ? K.nbc_particles : 1, BLOCK);
   k_bc<<<nbc, BLOCK, 0, s>>>(P, K, vcol);
   mark(s, "k_bc");
 }
 void launch_contact_kick(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
+  bool adapt = K.auto_ts || K.auto_ts_acc;
+  if (K.auto_ts && !K.leapfrog) {  // kick-drift: the velocity criterion sees v before the first kick
+    k_dt_tests<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, 1, 0);
+    mark(s, "k_dt_tests");
+  }
   if (!K.contact) k_contact_kick<0><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
   else if (K.nmeshes == 1) k_contact_kick<1><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
   else k_contact_kick<MAX_MESHES><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
   mark(s, "k_contact_kick");
-  if (K.leapfrog) {  // GeneralAfter, then the full kick (the caller's next BC pass follows)
+  if (K.leapfrog) {  // GeneralAfter, time-step control, then the full kick (the caller's BC pass follows)
     launch_bc(P, K, C_V, s);
+    if (adapt) {
+      k_dt_tests<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, K.auto_ts, K.auto_ts_acc);
+      mark(s, "k_dt_tests");
+      k_adapt_dt<<<1, 256, 0, s>>>(P, K);
+      mark(s, "k_adapt_dt");
+    }
     k_kick_leapfrog<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
     mark(s, "k_kick_leapfrog");
+  } else if (adapt) {
+    k_adapt_dt<<<1, 256, 0, s>>>(P, K);
+    mark(s, "k_adapt_dt");
   }
 }
 void launch_step_tail(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
 template <bool GC>
 __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
-  double dt = K.dt;
+  double dt = P.st->deltat;
   double rhoi = col(P, C_RHO, N, i);
   double dd = 0.0;
   bool solid = icol(P, I_KIND, N, i) == 0;
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
   __shared__ double sh[32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   size_t N = K.N;
-  double dt = K.dt;
+  double dt = P.st->deltat;
   double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300, dkin = 0.0, dint = 0.0;
   if (i < K.N) {
     for (int d = 0; d < 3; ++d) {

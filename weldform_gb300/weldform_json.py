@@ -13,7 +13,8 @@ Supported input (everything the kick-drift / leapfrog path covers):
                  "Mech-Thermal-LeapFrog" -> SolveDiffUpdateLeapFrog;
                  "Mech-KickDrift", "Mech-Thermal-KickDrift" -> SolveDiffUpdateKickDrift),
                  particleRadius, hFactor, cflMethod/timeStepSize/cflFactor,
-                 outTime, simTime, autoTS (all false), artifViscAlpha/Beta,
+                 outTime, simTime, autoTS (velocity / acceleration criteria;
+                 the contact one with leapfrog), artifViscAlpha/Beta,
                  contAlgorithm ("Wang"; "Fraser" also selects Wang, as the
                  reference), tensileInstability (default 0.3), nbsearchFreq,
                  sumType "Nishimura", stressGradType 0
@@ -26,11 +27,11 @@ Supported input (everything the kick-drift / leapfrog path covers):
   amplitude, valueAng for rigid bodies), InitialConditions (velocity,
   temperature), RigidBodies of type Plane with Contact[0] (friction
   coefficients, penaltyFactor).
-Anything else (Fraser or Thermal solvers, adaptive time step, GMT, damage,
-file or axisymmetric domains and meshes, 2D, heat-conduction contact,
-convection / temperature BCs, smoothing-length update) raises
-WFError(WF_ERR_UNSUPPORTED) before any step runs.  kernelGradCorr is
-supported in the plain FP64 form.
+Anything else (Fraser or Thermal solvers, GMT, damage, file or axisymmetric
+domains and meshes, 2D, heat-conduction contact, convection / temperature
+BCs) raises WFError(WF_ERR_UNSUPPORTED) before any step runs.
+kernelGradCorr is supported in both forms; smoothlenUpdate is accepted (it
+cannot change h in these solvers).
 """
 from __future__ import annotations
 
@@ -62,6 +63,7 @@ class Run:
     sim_time: float
     out_time: float
     thermal: bool
+    adaptive: bool = False  # autoTS velocity or acceleration criterion on
 
 
 def _vec(v, n=3, default=0.0):
@@ -127,10 +129,13 @@ def build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = N
         timestep = float(config["cflFactor"]) * h / Cs
     output_time = float(config["outTime"])
     sim_time = float(config["simTime"])
+    # autoTS = [velocity, acceleration, contact] criteria, default [true, false,
+    # false] (WeldForm.cpp:350, 364, 379-381)
     auto_ts = config.get("autoTS", [True, False, False])
     auto_ts = auto_ts if isinstance(auto_ts, list) else [auto_ts]
-    if any(auto_ts):
-        _unsupported("adaptive time step (autoTS)")
+    auto_ts = (list(auto_ts) + [False, False, False])[:3]
+    for key, flag in zip(("auto_ts", "auto_ts_acc", "auto_ts_cont"), auto_ts):
+        dom.set(key, 1 if flag else 0)
     alpha = float(config.get("artifViscAlpha", 1.0))
     beta = float(config.get("artifViscBeta", 0.0))
     cont_alg = config.get("contAlgorithm", "Wang")
@@ -259,7 +264,8 @@ def build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = N
     if sy is None:  # CalcYieldStress(0, 0, T) of the material
         sy = _initial_yield(mattype, c, Fy, T)
     dom.set_array("Sigmay", sy)
-    return Run(dom=dom, integrator=integrator, dt=timestep, sim_time=sim_time, out_time=output_time, thermal=thermal)
+    return Run(dom=dom, integrator=integrator, dt=timestep, sim_time=sim_time, out_time=output_time, thermal=thermal,
+               adaptive=bool(auto_ts[0] or auto_ts[1]))
 
 
 def _initial_yield(mattype, c, Fy, T):
@@ -313,13 +319,38 @@ def run(inp, out_dir: str = ".", make: Callable[[], object] = Domain, precision:
     """Build and solve; write key_NNNN.csv at each output time.  Returns the
     written paths.  The loop control is SolveDiffUpdate*'s
     (while Time <= tf && idx_out <= maxidx; output when Time >= tout), with
-    Time accumulated as the device does (Time += dt per step)."""
+    Time accumulated as the device does (Time += dt per step).  With an
+    adaptive time step, Time is read back: the step never exceeds the initial
+    dt, so floor((limit - Time) / dt) - 1 steps at a time stay inside the next
+    loop or output boundary, and single steps finish the approach."""
     r = build(inp, make, precision)
     d = r.dom
     d.prepare(r.dt)
     os.makedirs(out_dir, exist_ok=True)
     Time, tout, idx_out = 0.0, 0.0, 1
     written = []
+
+    def output():
+        path = os.path.join(out_dir, "%s_%04d.csv" % (key, idx_out))
+        write_csv(d, path)
+        written.append(path)
+
+    if r.adaptive:
+        Time = d.get("Time")
+        while Time <= r.sim_time and idx_out <= max_outputs:
+            lim = min(r.sim_time, tout)
+            n = int((lim - Time) // r.dt) if Time < lim else 0
+            if n > 1:
+                d.step(n - 1)
+                Time = d.get("Time")
+                continue
+            d.step(1)
+            Time = d.get("Time")
+            if Time >= tout:
+                output()
+                idx_out += 1
+                tout += r.out_time
+        return written
     pending = 0
     while Time <= r.sim_time and idx_out <= max_outputs:
         Time += r.dt
@@ -327,9 +358,7 @@ def run(inp, out_dir: str = ".", make: Callable[[], object] = Domain, precision:
         if Time >= tout:
             d.step(pending)
             pending = 0
-            path = os.path.join(out_dir, "%s_%04d.csv" % (key, idx_out))
-            write_csv(d, path)
-            written.append(path)
+            output()
             idx_out += 1
             tout += r.out_time
     if pending:
