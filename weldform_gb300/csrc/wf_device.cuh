@@ -182,7 +182,8 @@ struct DomainConst {
   int id_free_surf;
   int nmeshes;
   int contact_surf_id[MAX_MESHES];
-  int nblocks;         // blocks of the per-particle kernels (partials stride)
+  int pblock;          // threads per block of the per-particle kernels (64, 128 or 256)
+  int nblocks;         // blocks of the per-particle kernels at pblock (partials stride)
   int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
   int gblock;          // thread-block size of the mixed form's gather kernels
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)

@@ -153,8 +153,15 @@ struct wf_domain {
   // adaptive time step (Domain.cpp:107-170 defaults)
   int auto_ts = 0, auto_ts_acc = 0, auto_ts_cont = 0;
   double CFL = 0.7, sqrt_h_a = 0.0025;
-  int gblock = 256;
-  int graph_key() const { return gblock; }
+  int gblock = 0;    // mixed gathers' threads per block (0: chosen by particle count)
+  int pblock = 0;    // per-particle kernels' threads per block (0: chosen by particle count)
+  // Block sizes by particle count: below ~4 blocks of 256 per SM the per-particle
+  // kernels (one thread per particle, FP64 or gather latency bound) leave SMs
+  // idle, so smaller blocks spread the particles over every SM.
+  static int auto_block(long long n) { return n < 78000 ? 64 : (n < 156000 ? 128 : 256); }
+  int gblock_now() const { return gblock ? gblock : auto_block(hp.N); }
+  int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
+  int graph_key() const { return gblock_now() * 1024 + pblock_now(); }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
@@ -605,8 +612,9 @@ struct wf_domain {
       if (hp.i[I_KIND][p] == 0 && F(C_TI, p) > 0.0) K.ti = 1;
     K.nmeshes = (int)meshes.size();
     for (size_t m = 0; m < meshes.size(); ++m) K.contact_surf_id[m] = meshes[m].id;
-    K.nblocks = (N + 255) / 256;
-    P.partials = dalloc<double>((size_t)NSLOTS * K.nblocks);
+    K.pblock = pblock_now();
+    K.nblocks = (N + K.pblock - 1) / K.pblock;
+    P.partials = dalloc<double>((size_t)NSLOTS * ((N + 63) / 64));  // room for the smallest block size
     P.scan_tmp = dalloc<long long>((ncells + 4095) / 4096 + 1);
     // Step state.
     StepState st;
@@ -661,7 +669,9 @@ struct wf_domain {
   wf::DomainConst kconst() const {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
-    k.gblock = gblock;
+    k.gblock = gblock_now();
+    k.pblock = pblock_now();
+    k.nblocks = (int)((hp.N + k.pblock - 1) / k.pblock);
     return k;
   }
   void launch_one_step() {
@@ -869,9 +879,8 @@ struct wf_domain {
       std::vector<std::vector<void*>>& c;
       ~FreeChk() { for (auto& v : c) for (void* p : v) cudaFree(p); }
     } free_chk{chk};
-    DomainConst k = K;
+    DomainConst k = kconst();
     k.mixed = 0;
-    k.gblock = gblock;
 
     // ---- forward pass: loss curve and a checkpoint every kchk steps
     auto t0 = std::chrono::steady_clock::now();
@@ -1185,9 +1194,15 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     return WF_OK;
   }
   if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }
-  if (n == "gather_block") {
-    if (v != 64 && v != 128 && v != 256 && v != 512) return set_err(WF_ERR_ARG, "gather_block must be 64, 128, 256 or 512");
+  if (n == "gather_block") {  // 0: by particle count
+    if (v != 0 && v != 64 && v != 128 && v != 256 && v != 512)
+      return set_err(WF_ERR_ARG, "gather_block must be 0, 64, 128, 256 or 512");
     d->gblock = v;
+    return WF_OK;
+  }
+  if (n == "particle_block") {  // 0: by particle count
+    if (v != 0 && v != 64 && v != 128 && v != 256) return set_err(WF_ERR_ARG, "particle_block must be 0, 64, 128 or 256");
+    d->pblock = v;
     return WF_OK;
   }
   if (n == "device") {
@@ -1258,7 +1273,8 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     std::string n(name ? name : "");
     if (n == "particle_count") { *v = d->hp.N; return WF_OK; }
     if (n == "solid_part_count") { *v = d->solid_part_count; return WF_OK; }
-    if (n == "gather_block") { *v = d->gblock; return WF_OK; }
+    if (n == "gather_block") { *v = d->gblock_now(); return WF_OK; }
+    if (n == "particle_block") { *v = d->pblock_now(); return WF_OK; }
     if (n.size() == 8 && n.rfind("CellNo.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') { *v = d->CellNo[n[7] - 'x']; return WF_OK; }
     if (!d->prepared) { *v = 0; return WF_OK; }
     wf::StepState st = d->read_state();

@@ -778,7 +778,7 @@ __global__ void k_max_pl_final(DevPtrs P, DomainConst K) {
 void launch_prologue(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
   k_initial_pressure<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
   k_refresh_derived<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
-  k_max_pl<<<K.nblocks, BLOCK, 0, s>>>(P, K);
+  k_max_pl<<<K.nblocks, K.pblock, 0, s>>>(P, K);
   k_max_pl_final<<<1, 1, 0, s>>>(P, K);
 }
 void launch_refresh_derived(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
@@ -827,8 +827,8 @@ void launch_step_head(const DevPtrs& P, const DomainConst& K, double* fscratch, 
   mark(s, "k_schedule");
   launch_neighbour_search(P, K, fscratch, iscratch, s);
   if (K.gradcorr) {
-    int b = nblk(K.N, BLOCK);
-    k_grad_corr<<<b < 152 * 4 ? b : 152 * 4, BLOCK, 0, s>>>(P, K);
+    int b = K.nblocks;
+    k_grad_corr<<<b < 152 * 8 ? b : 152 * 8, K.pblock, 0, s>>>(P, K);
     mark(s, "k_grad_corr");
   }
 }
@@ -900,22 +900,22 @@ void launch_bc(const DevPtrs& P, const DomainConst& K, int vcol, cudaStream_t s)
 void launch_contact_kick(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
   bool adapt = K.auto_ts || K.auto_ts_acc;
   if (K.auto_ts && !K.leapfrog) {  // kick-drift: the velocity criterion sees v before the first kick
-    k_dt_tests<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, 1, 0);
+    k_dt_tests<<<K.nblocks, K.pblock, 0, s>>>(P, K, 1, 0);
     mark(s, "k_dt_tests");
   }
-  if (!K.contact) k_contact_kick<0><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
-  else if (K.nmeshes == 1) k_contact_kick<1><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
-  else k_contact_kick<MAX_MESHES><<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  if (!K.contact) k_contact_kick<0><<<K.nblocks, K.pblock, 0, s>>>(P, K);
+  else if (K.nmeshes == 1) k_contact_kick<1><<<K.nblocks, K.pblock, 0, s>>>(P, K);
+  else k_contact_kick<MAX_MESHES><<<K.nblocks, K.pblock, 0, s>>>(P, K);
   mark(s, "k_contact_kick");
   if (K.leapfrog) {  // GeneralAfter, time-step control, then the full kick (the caller's BC pass follows)
     launch_bc(P, K, C_V, s);
     if (adapt) {
-      k_dt_tests<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, K.auto_ts, K.auto_ts_acc);
+      k_dt_tests<<<K.nblocks, K.pblock, 0, s>>>(P, K, K.auto_ts, K.auto_ts_acc);
       mark(s, "k_dt_tests");
       k_adapt_dt<<<1, 256, 0, s>>>(P, K);
       mark(s, "k_adapt_dt");
     }
-    k_kick_leapfrog<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+    k_kick_leapfrog<<<K.nblocks, K.pblock, 0, s>>>(P, K);
     mark(s, "k_kick_leapfrog");
   } else if (adapt) {
     k_adapt_dt<<<1, 256, 0, s>>>(P, K);
@@ -942,22 +942,22 @@ void launch_step_fp64(const DevPtrs& P, const DomainConst& K, double* fscratch, 
 
 void launch_tensile(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
   if (!K.ti) return;
-  k_tensile<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K);
+  k_tensile<<<K.nblocks, K.pblock, 0, s>>>(P, K);
   mark(s, "k_tensile");
 }
 
 void launch_step_fp64_body(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
-  int nb = nblk(K.N, BLOCK);
+  int nb = K.nblocks;
   launch_tensile(P, K, s);
-  k_accel<<<nb, BLOCK, 0, s>>>(P, K);
+  k_accel<<<nb, K.pblock, 0, s>>>(P, K);
   mark(s, "k_accel");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
-  k_density_drift<<<nb, BLOCK, 0, s>>>(P, K);
+  k_density_drift<<<nb, K.pblock, 0, s>>>(P, K);
   mark(s, "k_density_drift");
   launch_bc(P, K, C_VN, s);
-  k_rate_stress<<<nb, BLOCK, 0, s>>>(P, K);
+  k_rate_stress<<<nb, K.pblock, 0, s>>>(P, K);
   mark(s, "k_rate_stress");
   launch_step_tail(P, K, s);
 }

@@ -534,7 +534,7 @@ static void launch_accel_mx(const DevPtrs& P, const DomainConst& K, int ng, int 
 }
 
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
-  int nb = nblk(K.N, BLOCK);
+  int nb = K.nblocks;
   int gb = (K.gblock == 64 || K.gblock == 128 || K.gblock == 512) ? K.gblock : 256;
   int ng = nblk(K.N, gb);
   launch_step_head(P, K, fscratch, iscratch, s);
@@ -564,11 +564,11 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   }
   mark(s, "k_rate_mx");
   if (K.pl_heating) {
-    if (K.thermal_solver) k_stress_mx<true, true><<<nb, BLOCK, 0, s>>>(P, K);
-    else k_stress_mx<true, false><<<nb, BLOCK, 0, s>>>(P, K);
+    if (K.thermal_solver) k_stress_mx<true, true><<<nb, K.pblock, 0, s>>>(P, K);
+    else k_stress_mx<true, false><<<nb, K.pblock, 0, s>>>(P, K);
   } else {
-    if (K.thermal_solver) k_stress_mx<false, true><<<nb, BLOCK, 0, s>>>(P, K);
-    else k_stress_mx<false, false><<<nb, BLOCK, 0, s>>>(P, K);
+    if (K.thermal_solver) k_stress_mx<false, true><<<nb, K.pblock, 0, s>>>(P, K);
+    else k_stress_mx<false, false><<<nb, K.pblock, 0, s>>>(P, K);
   }
   mark(s, "k_stress_mx");
   launch_step_tail(P, K, s);

@@ -21,6 +21,7 @@ def main():
     ap.add_argument("--v-top", type=float, default=-1.0)
     ap.add_argument("--kernels", action="store_true", help="print per-kernel CUDA-event times of the steps")
     ap.add_argument("--gather-block", type=int, default=None, help="mixed gathers: threads per block")
+    ap.add_argument("--particle-block", type=int, default=None, help="per-particle kernels: threads per block")
     a = ap.parse_args()
     dx = configs.dx_for_count(0.010, 0.030, a.n)
     d = Domain()
@@ -29,6 +30,8 @@ def main():
     d.prepare(case.dt)
     if a.gather_block is not None:
         d.set("gather_block", a.gather_block)
+    if a.particle_block is not None:
+        d.set("particle_block", a.particle_block)
     t = time.perf_counter()
     d.step(a.steps)
     el = time.perf_counter() - t
