@@ -734,18 +734,20 @@ __global__ void k_adj_conduction_factor(AdjPtrs A, DomainConst K) {
 }
 
 void launch_adjoint_step(const AdjPtrs& A, const DomainConst& K, cudaStream_t s) {
-  int nb = nblk(K.N, BLOCK);
+  // one thread per particle, no block-level sums: the domain's per-particle block size
+  int tb = K.pblock > 0 ? K.pblock : BLOCK;
+  int nb = nblk(K.N, tb);
   if (K.thermal_solver) {
-    k_adj_conduction_factor<<<nb, BLOCK, 0, s>>>(A, K);
+    k_adj_conduction_factor<<<nb, tb, 0, s>>>(A, K);
     mark(s, "k_adj_conduction_factor");
   }
-  k_adj_thermal_stress<<<nb, BLOCK, 0, s>>>(A, K);
+  k_adj_thermal_stress<<<nb, tb, 0, s>>>(A, K);
   mark(s, "k_adj_thermal_stress");
-  k_adj_rates_drift<<<nb, BLOCK, 0, s>>>(A, K);
+  k_adj_rates_drift<<<nb, tb, 0, s>>>(A, K);
   mark(s, "k_adj_rates_drift");
-  k_adj_density_contact<<<nb, BLOCK, 0, s>>>(A, K);
+  k_adj_density_contact<<<nb, tb, 0, s>>>(A, K);
   mark(s, "k_adj_density_contact");
-  k_adj_accel<<<nb, BLOCK, 0, s>>>(A, K);
+  k_adj_accel<<<nb, tb, 0, s>>>(A, K);
   mark(s, "k_adj_accel");
 }
 void launch_unpermute(const int* perm, const double* src, double* dst, int ncol, int N, cudaStream_t s) {
