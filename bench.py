@@ -47,7 +47,8 @@ ALG_BYTES = {
     "k_rate_stress": lambda nnz: 456 + 4 * nnz + 4,       # x,v,rho,m,h,p,tau,eps,eps_p,pl,sy -> tau,Sigma,..,dkin,dint
     "k_accel_mx": lambda nnz: 108 + 4 * nnz + 4,          # ff x,v; f32 rho,m,h,Sigma/rho^2 -> a (f64)
     "k_density_drift_mx": lambda nnz: 336 + 4 * nnz + 4,  # f64 integration; next-step record written
-    "k_rate_stress_mx": lambda nnz: 512 + 4 * nnz + 4,    # next record -> rates (registers) -> f64 stress state
+    "k_rate_mx": lambda nnz: 72 + 4 * nnz + 4,            # next record -> 9 rates, dkin, conduction
+    "k_stress_mx": lambda nnz: 440,                       # f64 stress state read + written
 }
 # FP64 operations per neighbour entry / per particle (plain form).
 ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (70, 270)}

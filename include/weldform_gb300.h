@@ -93,10 +93,9 @@ int wf_domain_destroy(wf_domain* d);
  * zeroed by StartAcceleration, so h does not change: accepted, no effect),
  * "precision" (WF_PRECISION_*), "device" (CUDA device ordinal, before the
  * prologue), "use_graph" (replay each step as one CUDA graph, default 1),
- * "gather_block" (threads per block of the mixed form's kernels: 64, 128 or
- * 256; 0 = by particle count), "particle_block" (the same for the plain
- * form's per-particle kernels), "cpu_threads" (unused on the GPU path).  Read
- * back with wf_get_domain_i32: "gather_block", "particle_block". */
+ * "gather_block" (threads per block of the mixed form's gathers: 64, 128,
+ * 256 or 512), "cpu_threads" (unused on the GPU path).  Read back with
+ * wf_get_domain_i32: "gather_block". */
 int wf_set_domain_f64(wf_domain* d, const char* name, double value);
 int wf_set_domain_i32(wf_domain* d, const char* name, int value);
 /* Read-back of scalars: "Time", "deltat", "hmax", "int_energy_sum",
@@ -229,8 +228,8 @@ int wf_checkpoint_save(wf_domain* d, int slot);
 int wf_checkpoint_restore(wf_domain* d, int slot);
 int wf_checkpoint_free(wf_domain* d, int slot);
 
-/* Chooses the thread-block size of the mixed form's kernels (64, 128 or 256
- * threads) by timing `steps` steps with each from a
+/* Chooses the thread-block size of the mixed form's three gather kernels
+ * (64, 128, 256 or 512 threads) by timing `steps` steps with each from a
  * checkpoint of the current state, restores that state, keeps the fastest
  * and returns it; results are cached per size bucket (particles rounded to a
  * power of two) for later domains in the process.  The block size is also

@@ -112,7 +112,7 @@ def test_mixed_gather_block_sizes_agree_bitwise():
     order, so a yielding JC + thermal + contact run is bit-identical across
     them (which block handles a particle does not matter)."""
     res = []
-    for block in (256, 64, 128):
+    for block in (256, 64, 128, 512):
         d = gpu_domain()
         d.set("precision", PRECISION_MIXED)
         case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, gap=0.0)

@@ -161,7 +161,7 @@ struct wf_domain {
   static int auto_block(long long n) { return n < 78000 ? 64 : (n < 156000 ? 128 : 256); }
   int gblock_now() const { return gblock ? gblock : auto_block(hp.N); }
   int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
-  int graph_key() const { return gblock_now() * 1024 + pblock_now(); }  // (the form is keyed separately)
+  int graph_key() const { return gblock_now() * 1024 + pblock_now(); }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
@@ -670,9 +670,7 @@ struct wf_domain {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
     k.gblock = gblock_now();
-    // the mixed form's fused rate/stress pass writes block partial sums, so its
-    // per-particle kernels share the gathers' block size
-    k.pblock = k.mixed ? k.gblock : pblock_now();
+    k.pblock = pblock_now();
     k.nblocks = (int)((hp.N + k.pblock - 1) / k.pblock);
     return k;
   }
@@ -1039,7 +1037,7 @@ struct wf_domain {
     checkpoint_save(slot);
     int best = 256;
     double best_ms = 1e300;
-    for (int b : {64, 128, 256}) {
+    for (int b : {64, 128, 256, 512}) {
       gblock = b;
       long long l = 0;
       step(1);  // capture + warm
@@ -1197,8 +1195,8 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   }
   if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }
   if (n == "gather_block") {  // 0: by particle count
-    if (v != 0 && v != 64 && v != 128 && v != 256)
-      return set_err(WF_ERR_ARG, "gather_block must be 0, 64, 128 or 256");
+    if (v != 0 && v != 64 && v != 128 && v != 256 && v != 512)
+      return set_err(WF_ERR_ARG, "gather_block must be 0, 64, 128, 256 or 512");
     d->gblock = v;
     return WF_OK;
   }

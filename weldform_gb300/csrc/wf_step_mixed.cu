@@ -271,11 +271,10 @@ __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainCo
 // 425-450; Thermal.cpp:90-107), weights (float)(m_j / rho_j); the kinetic-energy
 // pair term keeps the plain gradient, as the reference's.
 template <bool THERMAL, bool GC>
-__device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i, float out[9], double& dkin,
-                                        double& cond) {
+__device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
-  for (int c = 0; c < 9; ++c) out[c] = 0.f;
-  dkin = 0.0; cond = 0.0;
+  float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double dkin = 0.0, cond = 0.0;
   if (icol(P, I_KIND, N, i) == 0) {
     const float4* ri = P.rn + i;
     float4 xh = ld4(ri + (size_t)RN_XH * N), xl = ld4(ri + (size_t)RN_XL * N), vh = ld4(ri + (size_t)RN_VH * N), vl = ld4(ri + (size_t)RN_VL * N), e = ld4(ri + (size_t)RN_E * N);
@@ -325,6 +324,13 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
     dkin = kin.value();
     cond = cnd.value();
   }
+  for (int c = 0; c < 9; ++c) P.rates[(size_t)c * N + i] = out[c];
+  colw(P, C_DKIN, N, i) = dkin;
+  colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
+}
+template <bool THERMAL, bool GC>
+__global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
+  run_rows(K, [&](int i) { rate_mx<THERMAL, GC>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- elementwise update
@@ -405,125 +411,104 @@ __device__ __forceinline__ double stress_update_mx(StressMx& s, const float sr[6
   return dep;
 }
 
-// The elementwise update of one particle after its rate gather: next-step
-// buffers become current, radial return, strain columns, plastic heat,
-// temperature, energies, and the next acceleration pass's Sigma/rho^2 groups.
-// sr/rr, dkin and cond come from the gather in registers.
 template <bool HEAT, bool THERMAL>
-__device__ __forceinline__ void stress_mx(const DevPtrs& P, const DomainConst& K, int i, const float rates[9],
-                                          double dkin_in, double cond, double& plw, double& maxpl, double& maxT,
-                                          double& minT, double& dkin, double& dint) {
-  size_t N = K.N;
-  double dt = P.st->deltat;
-  for (int d = 0; d < 3; ++d) {
-    colw(P, C_X + d, N, i) = col(P, C_XN + d, N, i);
-    colw(P, C_V + d, N, i) = col(P, C_VN + d, N, i);
-  }
-  double rho = col(P, C_RHON, N, i);
-  colw(P, C_RHO, N, i) = rho;
-  colw(P, C_MRHO, N, i) = col(P, C_MRHON, N, i);
-  const float4* rn = P.rn + i;
-  float4* rc = P.rc + i;
-  rc[(size_t)RC_XH * N] = rn[(size_t)RN_XH * N];
-  rc[(size_t)RC_XL * N] = rn[(size_t)RN_XL * N];
-  rc[(size_t)RC_VH * N] = rn[(size_t)RN_VH * N];
-  rc[(size_t)RC_VL * N] = rn[(size_t)RN_VL * N];
-  float4 ne = rn[(size_t)RN_E * N];
-  float4 misc = rc[(size_t)RC_MISC * N];
-  maxpl = col(P, C_PLS, N, i);
-  dkin = dkin_in;
-  colw(P, C_DKIN, N, i) = dkin_in;
-  if (icol(P, I_KIND, N, i) == 0) {
-    float sr[6], rr[3];
-    for (int c = 0; c < 6; ++c) sr[c] = rates[c];
-    for (int c = 0; c < 3; ++c) rr[c] = rates[6 + c];
-    StressMx s;
-    for (int c = 0; c < 6; ++c) s.tau[c] = col(P, C_TAU + c, N, i);
-    s.pl_strain = col(P, C_PLS, N, i); s.delta_pl_strain = col(P, C_DPLS, N, i);
-    s.sigmay = col(P, C_SY, N, i); s.Ep = col(P, C_EP, N, i);
-    int mi = icol(P, I_MAT, N, i);
-    const MaterialDev* Mt = (mi >= 0 && mi < P.tab->nmat) ? &P.tab->mat[mi] : nullptr;
-    double T = col(P, C_T, N, i);
-    double dep = stress_update_mx(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i),
-                                  col(P, C_G, N, i), T, icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), Mt, dt);
-    for (int c = 0; c < 6; ++c) {
-      colw(P, C_TAU + c, N, i) = s.tau[c];
-      colw(P, C_SIG + c, N, i) = s.sig[c];
-      colw(P, C_EPS + c, N, i) = dt * (double)sr[c] + col(P, C_EPS + c, N, i);
-    }
-    // Strain_pl_incr = dep / sigma_y (sigma - tr-free part) and Strain_pl += it
-    // (Particle.cpp:1040-1058); kept from the last plastic step otherwise.
-    double epli[6];
-    if (dep > 0.0) {
-      double f = dep / s.sigmay;
-      epli[0] = f * (s.sig[0] - 0.5 * (s.sig[1] + s.sig[2]));
-      epli[1] = f * (s.sig[1] - 0.5 * (s.sig[0] + s.sig[2]));
-      epli[2] = f * (s.sig[2] - 0.5 * (s.sig[0] + s.sig[1]));
-      epli[3] = 1.5 * f * s.sig[3];
-      epli[4] = 1.5 * f * s.sig[4];
-      epli[5] = 1.5 * f * s.sig[5];
-      for (int c = 0; c < 6; ++c) {
-        colw(P, C_EPLI + c, N, i) = epli[c];
-        colw(P, C_EPL + c, N, i) = col(P, C_EPL + c, N, i) + epli[c];
-      }
-    }
-    double srd[6];
-    for (int c = 0; c < 6; ++c) srd[c] = (double)sr[c];
-    double qpl = 0.0;
-    if (HEAT) {
-      qpl = col(P, C_QPL, N, i);
-      if (s.delta_pl_strain > 0.0) {
-        if (!(dep > 0.0))
-          for (int c = 0; c < 6; ++c) epli[c] = col(P, C_EPLI + c, N, i);
-        qpl = plastic_heat(s.sig, epli, dt);
-      }
-      colw(P, C_QPL, N, i) = qpl;
-      colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + qpl * dt;
-      plw = col(P, C_MASS, N, i) / rho * qpl;
-    }
-    if (THERMAL) {  // T(n+1) (already in the next record), then CalcTempInc's dTdt
-      T += dt * col(P, C_DTDT, N, i);
-      colw(P, C_T, N, i) = T;
-      maxT = T; minT = T;
-      if (!HEAT) qpl = col(P, C_QPL, N, i);
-      double f = 1. / (rho * col(P, C_CPT, N, i));
-      double dTdt = f * (cond + col(P, C_QSRC, N, i) + qpl * K.pl_work_heat_frac);
-      colw(P, C_DTDT, N, i) = dTdt;
-      double st = col(P, C_THEXP, N, i) * dTdt;  // CalcThermalExpStrainRate
-      for (int c = 0; c < 3; ++c) srd[c] = srd[c] + st;
-    }
-    for (int c = 0; c < 6; ++c) colw(P, C_SR + c, N, i) = srd[c];
-    for (int c = 0; c < 3; ++c) colw(P, C_RR + c, N, i) = (double)rr[c];
-    colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
-    colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = (double)s.esr;
-    maxpl = s.pl_strain;
-    // CalcIntEnergyEqn (Particle.cpp:941-950)
-    dint = col(P, C_MRHO, N, i) * (s.tau[0] * srd[0] + 2.0 * s.tau[3] * srd[3] + 2.0 * s.tau[4] * srd[4] +
-                                   s.tau[1] * srd[1] + 2.0 * s.tau[5] * srd[5] + s.tau[2] * srd[2]);
-    colw(P, C_DINT, N, i) = dint;
-    float c2 = 1.0f / ((float)rho * (float)rho);
-    float s1w = rc[(size_t)RC_S1 * N].w;
-    rc[(size_t)RC_S0 * N] = make_float4(c2 * (float)s.sig[0], c2 * (float)s.sig[1], c2 * (float)s.sig[2], c2 * (float)s.sig[3]);
-    rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], c2 * (float)s.pressure, s1w);
-  }
-  rc[(size_t)RC_MISC * N] = make_float4(misc.x, misc.y, misc.z, ne.z);
-  rc[(size_t)RC_T2 * N] = make_float4(ne.w, 0.f, 0.f, 0.f);
-}
-
-// Rate gather and elementwise update in one pass: the gather is bound by the
-// L1 data path with DRAM nearly idle, so the update's FP64 work and state
-// traffic overlap it, and the nine rates stay in registers.  The update writes
-// only the current-state groups and columns, which no thread's gather reads.
-template <bool THERMAL, bool GC, bool HEAT>
-__global__ void __launch_bounds__(256, 3) k_rate_stress_mx(DevPtrs P, DomainConst K) {
+__global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K) {
   __shared__ double sh[32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  size_t N = K.N;
+  double dt = P.st->deltat;
   double plw = 0.0, maxpl = 0.0, maxT = -1e300, minT = 1e300, dkin = 0.0, dint = 0.0;
   if (i < K.N) {
-    float rates[9];
-    double dk, cond;
-    rate_mx<THERMAL, GC>(P, K, i, rates, dk, cond);
-    stress_mx<HEAT, THERMAL>(P, K, i, rates, dk, cond, plw, maxpl, maxT, minT, dkin, dint);
+    for (int d = 0; d < 3; ++d) {
+      colw(P, C_X + d, N, i) = col(P, C_XN + d, N, i);
+      colw(P, C_V + d, N, i) = col(P, C_VN + d, N, i);
+    }
+    double rho = col(P, C_RHON, N, i);
+    colw(P, C_RHO, N, i) = rho;
+    colw(P, C_MRHO, N, i) = col(P, C_MRHON, N, i);
+    const float4* rn = P.rn + i;
+    float4* rc = P.rc + i;
+    rc[(size_t)RC_XH * N] = rn[(size_t)RN_XH * N];
+    rc[(size_t)RC_XL * N] = rn[(size_t)RN_XL * N];
+    rc[(size_t)RC_VH * N] = rn[(size_t)RN_VH * N];
+    rc[(size_t)RC_VL * N] = rn[(size_t)RN_VL * N];
+    float4 ne = rn[(size_t)RN_E * N];
+    float4 misc = rc[(size_t)RC_MISC * N];
+    maxpl = col(P, C_PLS, N, i);
+    dkin = col(P, C_DKIN, N, i);
+    if (icol(P, I_KIND, N, i) == 0) {
+      float sr[6], rr[3];
+      for (int c = 0; c < 6; ++c) sr[c] = P.rates[(size_t)c * N + i];
+      for (int c = 0; c < 3; ++c) rr[c] = P.rates[(size_t)(6 + c) * N + i];
+      StressMx s;
+      for (int c = 0; c < 6; ++c) s.tau[c] = col(P, C_TAU + c, N, i);
+      s.pl_strain = col(P, C_PLS, N, i); s.delta_pl_strain = col(P, C_DPLS, N, i);
+      s.sigmay = col(P, C_SY, N, i); s.Ep = col(P, C_EP, N, i);
+      int mi = icol(P, I_MAT, N, i);
+      const MaterialDev* Mt = (mi >= 0 && mi < P.tab->nmat) ? &P.tab->mat[mi] : nullptr;
+      double T = col(P, C_T, N, i);
+      double dep = stress_update_mx(s, sr, rr, rho, col(P, C_RHO0, N, i), col(P, C_CS, N, i), col(P, C_P0, N, i),
+                                    col(P, C_G, N, i), T, icol(P, I_FAIL, N, i), icol(P, I_MODEL, N, i), Mt, dt);
+      for (int c = 0; c < 6; ++c) {
+        colw(P, C_TAU + c, N, i) = s.tau[c];
+        colw(P, C_SIG + c, N, i) = s.sig[c];
+        colw(P, C_EPS + c, N, i) = dt * (double)sr[c] + col(P, C_EPS + c, N, i);
+      }
+      // Strain_pl_incr = dep / sigma_y (sigma - tr-free part) and Strain_pl += it
+      // (Particle.cpp:1040-1058); kept from the last plastic step otherwise.
+      double epli[6];
+      if (dep > 0.0) {
+        double f = dep / s.sigmay;
+        epli[0] = f * (s.sig[0] - 0.5 * (s.sig[1] + s.sig[2]));
+        epli[1] = f * (s.sig[1] - 0.5 * (s.sig[0] + s.sig[2]));
+        epli[2] = f * (s.sig[2] - 0.5 * (s.sig[0] + s.sig[1]));
+        epli[3] = 1.5 * f * s.sig[3];
+        epli[4] = 1.5 * f * s.sig[4];
+        epli[5] = 1.5 * f * s.sig[5];
+        for (int c = 0; c < 6; ++c) {
+          colw(P, C_EPLI + c, N, i) = epli[c];
+          colw(P, C_EPL + c, N, i) = col(P, C_EPL + c, N, i) + epli[c];
+        }
+      }
+      double srd[6];
+      for (int c = 0; c < 6; ++c) srd[c] = (double)sr[c];
+      if (HEAT) {
+        double q = col(P, C_QPL, N, i);
+        if (s.delta_pl_strain > 0.0) {
+          if (!(dep > 0.0))
+            for (int c = 0; c < 6; ++c) epli[c] = col(P, C_EPLI + c, N, i);
+          q = plastic_heat(s.sig, epli, dt);
+        }
+        colw(P, C_QPL, N, i) = q;
+        colw(P, C_PSEN, N, i) = col(P, C_PSEN, N, i) + q * dt;
+        plw = col(P, C_MASS, N, i) / rho * q;
+      }
+      if (THERMAL) {  // T(n+1) (already in the next record), then CalcTempInc's dTdt
+        T += dt * col(P, C_DTDT, N, i);
+        colw(P, C_T, N, i) = T;
+        maxT = T; minT = T;
+        double f = 1. / (rho * col(P, C_CPT, N, i));
+        double dTdt = f * (col(P, C_DINT, N, i) + col(P, C_QSRC, N, i) + col(P, C_QPL, N, i) * K.pl_work_heat_frac);
+        colw(P, C_DTDT, N, i) = dTdt;
+        double st = col(P, C_THEXP, N, i) * dTdt;  // CalcThermalExpStrainRate
+        for (int c = 0; c < 3; ++c) srd[c] = srd[c] + st;
+      }
+      for (int c = 0; c < 6; ++c) colw(P, C_SR + c, N, i) = srd[c];
+      for (int c = 0; c < 3; ++c) colw(P, C_RR + c, N, i) = (double)rr[c];
+      colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
+      colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = (double)s.esr;
+      maxpl = s.pl_strain;
+      // CalcIntEnergyEqn (Particle.cpp:941-950)
+      dint = col(P, C_MRHO, N, i) * (s.tau[0] * srd[0] + 2.0 * s.tau[3] * srd[3] + 2.0 * s.tau[4] * srd[4] +
+                                     s.tau[1] * srd[1] + 2.0 * s.tau[5] * srd[5] + s.tau[2] * srd[2]);
+      colw(P, C_DINT, N, i) = dint;
+      float c2 = 1.0f / ((float)rho * (float)rho);
+      float s1w = rc[(size_t)RC_S1 * N].w;
+      rc[(size_t)RC_S0 * N] = make_float4(c2 * (float)s.sig[0], c2 * (float)s.sig[1], c2 * (float)s.sig[2], c2 * (float)s.sig[3]);
+      rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], c2 * (float)s.pressure, s1w);
+    }
+    rc[(size_t)RC_MISC * N] = make_float4(misc.x, misc.y, misc.z, ne.z);
+    rc[(size_t)RC_T2 * N] = make_float4(ne.w, 0.f, 0.f, 0.f);
   }
   double r;
   r = block_reduce<1>(maxpl, sh); if (threadIdx.x == 0) P.partials[S_MAXPL * K.nblocks + blockIdx.x] = r;
@@ -542,21 +527,6 @@ void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, c
   mark(s, "k_refresh_records");
 }
 
-template <bool THERMAL, bool GC>
-static void launch_rate_stress_heat(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
-  if (K.pl_heating) k_rate_stress_mx<THERMAL, GC, true><<<ng, gb, 0, s>>>(P, K);
-  else k_rate_stress_mx<THERMAL, GC, false><<<ng, gb, 0, s>>>(P, K);
-}
-static void launch_rate_stress_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
-  if (K.thermal_solver) {
-    if (K.gradcorr) launch_rate_stress_heat<true, true>(P, K, ng, gb, s);
-    else launch_rate_stress_heat<true, false>(P, K, ng, gb, s);
-  } else {
-    if (K.gradcorr) launch_rate_stress_heat<false, true>(P, K, ng, gb, s);
-    else launch_rate_stress_heat<false, false>(P, K, ng, gb, s);
-  }
-}
-
 template <bool TI, bool AVU>
 static void launch_accel_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
   if (K.gradcorr) k_accel_mx<TI, AVU, true><<<ng, gb, 0, s>>>(P, K);
@@ -565,7 +535,7 @@ static void launch_accel_mx(const DevPtrs& P, const DomainConst& K, int ng, int 
 
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
   int nb = K.nblocks;
-  int gb = (K.gblock == 64 || K.gblock == 128) ? K.gblock : 256;  // = K.pblock in this form
+  int gb = (K.gblock == 64 || K.gblock == 128 || K.gblock == 512) ? K.gblock : 256;
   int ng = nblk(K.N, gb);
   launch_step_head(P, K, fscratch, iscratch, s);
   launch_refresh_shadows(P, K, 0, s);
@@ -585,8 +555,22 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   else k_density_drift_mx<false><<<ng, gb, 0, s>>>(P, K);
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
-  launch_rate_stress_mx(P, K, ng, gb, s);
-  mark(s, "k_rate_stress_mx");
+  if (K.thermal_solver) {
+    if (K.gradcorr) k_rate_mx<true, true><<<ng, gb, 0, s>>>(P, K);
+    else k_rate_mx<true, false><<<ng, gb, 0, s>>>(P, K);
+  } else {
+    if (K.gradcorr) k_rate_mx<false, true><<<ng, gb, 0, s>>>(P, K);
+    else k_rate_mx<false, false><<<ng, gb, 0, s>>>(P, K);
+  }
+  mark(s, "k_rate_mx");
+  if (K.pl_heating) {
+    if (K.thermal_solver) k_stress_mx<true, true><<<nb, K.pblock, 0, s>>>(P, K);
+    else k_stress_mx<true, false><<<nb, K.pblock, 0, s>>>(P, K);
+  } else {
+    if (K.thermal_solver) k_stress_mx<false, true><<<nb, K.pblock, 0, s>>>(P, K);
+    else k_stress_mx<false, false><<<nb, K.pblock, 0, s>>>(P, K);
+  }
+  mark(s, "k_stress_mx");
   launch_step_tail(P, K, s);
 }
 
