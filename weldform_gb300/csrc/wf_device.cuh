@@ -215,6 +215,8 @@ struct DevPtrs {
   int* row_len;           // neighbours per particle
   int* row_split;         // neighbours with larger original index (row prefix)
   int* nbr;               // ELL: entry k of particle i at k * N + i
+  double* gk;             // plain form: the step's GradKernel per row entry (same ELL layout),
+                          // written by the acceleration pass, read by the density pass
   int* cp_len;            // contact pairs per particle
   int* cp;                // ELL, width MAX_CP
   const int* bc_list;     // original indices of particles carrying a BC zone id

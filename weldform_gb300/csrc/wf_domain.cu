@@ -479,6 +479,7 @@ struct wf_domain {
     P.row_len = dalloc<int>(n);
     P.row_split = dalloc<int>(n);
     P.nbr = dalloc<int>((size_t)MAX_NB * n);
+    P.gk = dalloc<double>((size_t)MAX_NB * n);
     CK(cudaMemsetAsync(P.row_len, 0, sizeof(int) * n, stream));
     CK(cudaMemsetAsync(P.row_split, 0, sizeof(int) * n, stream));
     P.cp_len = dalloc<int>(n);

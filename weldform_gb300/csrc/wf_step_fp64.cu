@@ -8,7 +8,8 @@
 //   k_bc                GeneralAfter (WeldForm.cpp:51-120)
 //   k_contact_kick      CalcContactForcesWang (Contact_Wang.cpp:15-348) + v += a dt/2
 //   k_bc
-//   k_density_drift     CalcDensInc + DensReduction (InteractionAlt.cpp:483-640),
+//   k_density_drift     CalcDensInc + DensReduction (InteractionAlt.cpp:483-640) with the
+//                       acceleration pass's GradKernel per row entry (same x(n), h),
 //                       rho += dt drho, x += v dt, v += a dt/2 (SolverKickDrift.cpp:236-265);
 //                       next-step p/rho^2 and T for the rate gather
 //   k_bc                (on the next-step velocity buffer)
@@ -203,6 +204,7 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
     int j = nb_index(P.nbr[(size_t)k * N + i]);
     PairGeo g = pair_geo(xi0, xi1, xi2, hi, inv_hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
                          col(P, C_H, N, j));
+    P.gk[(size_t)k * N + i] = g.GK;  // the density pass uses the same x(n) and h
     double Alpha = (ai + col(P, C_ALPHA, N, j)) / 2.0, Beta = (bi + col(P, C_BETA, N, j)) / 2.0;
     double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
     double PIs = 0.0;
@@ -435,13 +437,13 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
     P.tx[(size_t)(TX_VH + 2) * N + i] = vi2;
   }
   if (icol(P, I_KIND, N, i) == 0) {
-    double hi = col(P, C_H, N, i);
-    double inv_hi = 1.0 / hi;
     int len = P.row_len[i];
     for (int k = 0; k < len; ++k) {
       int j = nb_index(P.nbr[(size_t)k * N + i]);
-      PairGeo g = pair_geo(xi0, xi1, xi2, hi, inv_hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
-                           col(P, C_H, N, j));
+      // x(n) and h are the acceleration pass's: its GradKernel of this entry is reused
+      PairGeo g;
+      g.x0 = xi0 - col(P, C_X, N, j); g.x1 = xi1 - col(P, C_X + 1, N, j); g.x2 = xi2 - col(P, C_X + 2, N, j);
+      g.GK = P.gk[(size_t)k * N + i];
       double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
       if (K.gradcorr) {  // locking form m_j (rho_i/rho_j) v_ij . vc_i (InteractionAlt.cpp:589-605)
         double vc[3];
