@@ -127,6 +127,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_thermal_stress(AdjPtrs A, DomainC
       int e = S.nbr[(size_t)k * N + i];
       int j = nb_index(e);
       GeoD g = geo_d(xi, hi, inv_hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
+      A.gk_end[(size_t)k * N + i] = g.GK;  // R2 reads the same end-state geometry
+      A.dg_end[(size_t)k * N + i] = g.dGr;
       double lcj = TMP(J_LC, j);
       double d = lci - lcj;
       bool up = nb_up(e);  // j has the larger original index: P2 = j
@@ -331,7 +333,14 @@ __global__ void __launch_bounds__(BLOCK) k_adj_rates_drift(AdjPtrs A, DomainCons
   int len = S.row_len[i];
   for (int k = 0; k < len; ++k) {
     int j = nb_index(S.nbr[(size_t)k * N + i]);
-    GeoD g = geo_d(xi, hi, inv_hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
+    GeoD g;
+    if (K.thermal_solver) {  // R1 formed this entry's end-state geometry
+      g.x0 = xi[0] - FE(C_X, j); g.x1 = xi[1] - FE(C_X + 1, j); g.x2 = xi[2] - FE(C_X + 2, j);
+      g.GK = A.gk_end[(size_t)k * N + i];
+      g.dGr = A.dg_end[(size_t)k * N + i];
+    } else {
+      g = geo_d(xi, hi, inv_hi, FE(C_X, j), FE(C_X + 1, j), FE(C_X + 2, j), col(S, C_H, N, j));
+    }
     double b0 = vi[0] - FE(C_V, j), b1 = vi[1] - FE(C_V + 1, j), b2 = vi[2] - FE(C_V + 2, j);
     double wj = FE(C_MRHO, j);
     double lj[9], L[9];
@@ -390,6 +399,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_density_contact(AdjPtrs A, Domain
   for (int k = 0; k < len; ++k) {
     int j = nb_index(S.nbr[(size_t)k * N + i]);
     GeoD g = geo_d(xi, hi, inv_hi, col(S, C_X, N, j), col(S, C_X + 1, N, j), col(S, C_X + 2, N, j), col(S, C_H, N, j));
+    A.gk_start[(size_t)k * N + i] = g.GK;  // R4 reads the same start-state geometry
+    A.dg_start[(size_t)k * N + i] = g.dGr;
     double b0 = vh[0] - TXV(TX_VH, j), b1 = vh[1] - TXV(TX_VH + 1, j), b2 = vh[2] - TXV(TX_VH + 2, j);
     double bx = b0 * g.x0 + b1 * g.x1 + b2 * g.x2;
     double pd = g.GK * bx;
@@ -600,7 +611,6 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
   double vi[3] = {col(S, C_V, N, i), col(S, C_V + 1, N, i), col(S, C_V + 2, N, i)};
   double hi = col(S, C_H, N, i), rhoi = col(S, C_RHO, N, i), csi = col(S, C_CS, N, i), mi = col(S, C_MASS, N, i);
   double al = col(S, C_ALPHA, N, i), be = col(S, C_BETA, N, i);
-  double inv_hi = 1.0 / hi;
   double Si[6];
   for (int c = 0; c < 6; ++c) Si[c] = col(S, C_SRHO + c, N, i);
   double lai[3] = {TMP(J_AACC, i), TMP(J_AACC + 1, i), TMP(J_AACC + 2, i)};
@@ -612,7 +622,10 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
     double mj = col(S, C_MASS, N, j);
     double Gm[3];
     for (int d = 0; d < 3; ++d) Gm[d] = mj * lai[d] - mi * TMP(J_AACC + d, j);
-    GeoD g = geo_d(xi, hi, inv_hi, col(S, C_X, N, j), col(S, C_X + 1, N, j), col(S, C_X + 2, N, j), col(S, C_H, N, j));
+    GeoD g;  // R3 formed this entry's start-state geometry
+    g.x0 = xi[0] - col(S, C_X, N, j); g.x1 = xi[1] - col(S, C_X + 1, N, j); g.x2 = xi[2] - col(S, C_X + 2, N, j);
+    g.GK = A.gk_start[(size_t)k * N + i];
+    g.dGr = A.dg_start[(size_t)k * N + i];
     double b0 = vi[0] - col(S, C_V, N, j), b1 = vi[1] - col(S, C_V + 1, N, j), b2 = vi[2] - col(S, C_V + 2, N, j);
     double Alpha = (al + col(S, C_ALPHA, N, j)) / 2.0, Beta = (be + col(S, C_BETA, N, j)) / 2.0;
     double PIs = 0.0, MU = 0.0, iDn = 0.0, Cij = 0.0, irbar = 0.0, hh = 0.0;
@@ -621,7 +634,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
       double dvx = b0 * g.x0 + b1 * g.x1 + b2 * g.x2;
       if (dvx < 0) {
         hh = (hi + col(S, C_H, N, j)) / 2;
-        iDn = 1.0 / (g.r * g.r + 0.01 * hh * hh);
+        iDn = 1.0 / (g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2 + 0.01 * hh * hh);
         MU = hh * dvx * iDn;
         Cij = 0.5 * (csi + col(S, C_CS, N, j));
         irbar = 2.0 / (rhoi + col(S, C_RHO, N, j));

@@ -63,6 +63,14 @@ struct AdjPtrs {
   const double* Lin;  // adjoint at the end of the step (AdjState)
   double* Lout;       // adjoint at the start of the step (AdjState)
   double* Tmp;        // AdjTmp
+  // Pair geometry per row entry (ELL, entry k of particle i at k * N + i):
+  // GradKernel and (dGK/dr)/r at the step's start positions, formed by R3 and
+  // read by R4, and at its end positions, formed by R1 (thermal steps) and
+  // read by R2.
+  double* gk_start;
+  double* dg_start;
+  double* gk_end;
+  double* dg_end;
   double* Q;          // AdjParamCol accumulators
   int* err;
   double time;        // Time at the start of the step (velocity-BC amplitudes)

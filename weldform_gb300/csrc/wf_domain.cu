@@ -915,6 +915,7 @@ struct wf_domain {
     double* Lin = sc.get<double>((size_t)NA_STATE * n);
     double* Lout = sc.get<double>((size_t)NA_STATE * n);
     double* Tb = sc.get<double>((size_t)NA_TMP * n);
+    double* geo = sc.get<double>((size_t)4 * MAX_NB * n);  // pair geometry shared by the adjoint kernels
     double* Q = sc.get<double>((size_t)NQ * n);
     double* Q2 = sc.get<double>((size_t)NQ * n);
     int* derr = sc.get<int>(1);
@@ -990,6 +991,10 @@ struct wf_domain {
         A.Lin = Lin;
         A.Lout = Lout;
         A.Tmp = Tb;
+        A.gk_start = geo;
+        A.dg_start = geo + (size_t)MAX_NB * n;
+        A.gk_end = geo + (size_t)2 * MAX_NB * n;
+        A.dg_end = geo + (size_t)3 * MAX_NB * n;
         A.Q = Q;
         A.err = derr;
         A.time = T.time;
