@@ -161,6 +161,9 @@ struct StepState {
   int isfirst, isyielding, ts_i, nb_cleared;
   int do_search;       // set by the schedule kernel for the current step
   int do_gradcorr;     // recompute the kernel-gradient correction this step
+  int gk_valid;        // P.gk holds GradKernel at the current positions and rows (plain form:
+                       // the last step's rate pass formed it; host writes, restores and
+                       // searches clear it)
   int errors;
   int surface_count;
 };
@@ -215,8 +218,10 @@ struct DevPtrs {
   int* row_len;           // neighbours per particle
   int* row_split;         // neighbours with larger original index (row prefix)
   int* nbr;               // ELL: entry k of particle i at k * N + i
-  double* gk;             // plain form: the step's GradKernel per row entry (same ELL layout),
-                          // written by the acceleration pass, read by the density pass
+  double* gk;             // plain form: GradKernel per row entry (same ELL layout) at the
+                          // current positions: written by the rate pass at x(n+1) (or by the
+                          // acceleration pass when stale), read by the next step's
+                          // acceleration and density passes
   int* cp_len;            // contact pairs per particle
   int* cp;                // ELL, width MAX_CP
   const int* bc_list;     // original indices of particles carrying a BC zone id

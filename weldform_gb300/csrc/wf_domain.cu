@@ -790,8 +790,11 @@ struct wf_domain {
   void restore_from(const std::vector<void*>& sl) {
     for (size_t k = 0; k < regions.size(); ++k)
       CK(cudaMemcpyAsync(regions[k].p, sl[k], regions[k].bytes, cudaMemcpyDeviceToDevice, stream));
+    invalidate_gk();  // the per-entry GradKernel is not part of a checkpoint
     CK(cudaStreamSynchronize(stream));
   }
+  // The plain form's per-entry GradKernel (P.gk) no longer matches the state.
+  void invalidate_gk() { CK(cudaMemsetAsync(&P.st->gk_valid, 0, sizeof(int), stream)); }
   void checkpoint_save(int slot) {
     use_device();
     if ((int)slots.size() <= slot) slots.resize(slot + 1);
@@ -1064,6 +1067,7 @@ struct wf_domain {
     wf::launch_force_search(P, stream);
     wf::launch_neighbour_search(P, kconst(), d_fscratch, d_iscratch, stream);
     shadows_valid = false;  // the search reorders particles
+    invalidate_gk();
     int zero = 0;
     CK(cudaMemcpyAsync(&P.st->do_search, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
@@ -1101,6 +1105,7 @@ struct wf_domain {
     CK(cudaFreeAsync(tmp, stream));
     wf::launch_refresh_derived(P, K, stream);
     shadows_valid = false;
+    invalidate_gk();
     CK(cudaStreamSynchronize(stream));
   }
   void get_i32(int c, int* dst) {

@@ -60,6 +60,7 @@ __global__ void k_schedule(DevPtrs P, DomainConst K) {
 
 __global__ void k_step_end(DevPtrs P, DomainConst K) {
   StepState* s = P.st;
+  s->gk_valid = K.mixed ? 0 : 1;  // the plain rate pass left GradKernel at the new positions
   s->steps += 1;
   s->Time += s->deltat;
   s->isfirst = 0;
@@ -200,18 +201,31 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
   for (int c = 0; c < 6; ++c) Si[c] = col(P, C_SRHO + c, N, i);
   double a0 = 0, a1 = 0, a2 = 0;
   int len = P.row_len[i];
+  // The last step's rate pass formed GradKernel at these positions and rows
+  // unless this step searched (or the host touched the state).
+  const bool reuse = P.st->gk_valid && !P.st->do_search;
   for (int k = 0; k < len; ++k) {
     int j = nb_index(P.nbr[(size_t)k * N + i]);
-    PairGeo g = pair_geo(xi0, xi1, xi2, hi, inv_hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
-                         col(P, C_H, N, j));
-    P.gk[(size_t)k * N + i] = g.GK;  // the density pass uses the same x(n) and h
+    PairGeo g;
+    if (reuse) {
+      double hj = col(P, C_H, N, j);
+      g.x0 = xi0 - col(P, C_X, N, j); g.x1 = xi1 - col(P, C_X + 1, N, j); g.x2 = xi2 - col(P, C_X + 2, N, j);
+      g.r2 = g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2;
+      g.hh = hj == hi ? hi : (hi + hj) / 2;
+      g.r = K.ti ? sqrt(g.r2) : 0.0;  // the tensile term alone needs r
+      g.GK = P.gk[(size_t)k * N + i];
+    } else {
+      g = pair_geo(xi0, xi1, xi2, hi, inv_hi, col(P, C_X, N, j), col(P, C_X + 1, N, j), col(P, C_X + 2, N, j),
+                   col(P, C_H, N, j));
+      P.gk[(size_t)k * N + i] = g.GK;  // for the density pass (same x(n), h)
+    }
     double Alpha = (ai + col(P, C_ALPHA, N, j)) / 2.0, Beta = (bi + col(P, C_BETA, N, j)) / 2.0;
     double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
     double PIs = 0.0;
     if (Alpha != 0.0 || Beta != 0.0) {
       double dvx = v0 * g.x0 + v1 * g.x1 + v2 * g.x2;
       if (dvx < 0) {  // MU = h dvx / Dn, PIs = (Alpha Cij MU + Beta MU^2) / rho_bar in one division
-        double Dn = g.r * g.r + 0.01 * g.hh * g.hh;
+        double Dn = g.r2 + 0.01 * g.hh * g.hh;
         double hv = g.hh * dvx;
         double Cij = 0.5 * (csi + col(P, C_CS, N, j));
         PIs = hv * (Alpha * Cij * Dn + Beta * hv) / (Dn * Dn * (0.5 * (rhoi + col(P, C_RHO, N, j))));
@@ -525,6 +539,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
         int j = nb_index(e);
         PairGeo g = pair_geo(x[0], x[1], x[2], hi, inv_hi, col(P, C_XN, N, j), col(P, C_XN + 1, N, j), col(P, C_XN + 2, N, j),
                              col(P, C_H, N, j));
+        P.gk[(size_t)k * N + i] = g.GK;  // x(n+1) is the next step's x(n): its acceleration pass reuses it
         double b0 = v[0] - col(P, C_VN, N, j), b1 = v[1] - col(P, C_VN + 1, N, j), b2 = v[2] - col(P, C_VN + 2, N, j);
         {
           double dv = b0 * (g.GK * g.x0) + b1 * (g.GK * g.x1) + b2 * (g.GK * g.x2);
