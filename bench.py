@@ -46,8 +46,6 @@ ALG_BYTES = {
     "k_density_drift": lambda nnz: 272 + 4 * nnz + 4,     # x,v,a,rho,m,h -> v,rho ; x,v,a -> x,v
     "k_rate_stress": lambda nnz: 456 + 4 * nnz + 4,       # x,v,rho,m,h,p,tau,eps,eps_p,pl,sy -> tau,Sigma,..,dkin,dint
     "k_accel_mx": lambda nnz: 108 + 4 * nnz + 4,          # ff x,v; f32 rho,m,h,Sigma/rho^2 -> a (f64)
-    "k_accel_mx_pairs": lambda nnz: 108 + 36 * nnz / 2 + 4,  # record; per first-part entry: index + 2 float4 shares
-    "k_accel_mx_sum": lambda nnz: 24 + 16 * nnz + 8 * nnz / 2 + 4,  # a share per entry; partner slot lookups
     "k_density_drift_mx": lambda nnz: 336 + 4 * nnz + 4,  # f64 integration; next-step record written
     "k_rate_mx": lambda nnz: 72 + 4 * nnz + 4,            # next record -> 9 rates, dkin, conduction
     "k_stress_mx": lambda nnz: 440,                       # f64 stress state read + written

@@ -149,23 +149,3 @@ def test_mixed_adaptive_time_step():
     _check(m, o, f)
     assert abs(m["deltat"] - o["deltat"]) <= TOL * o["deltat"]
     assert abs(m["Time"] - o["Time"]) <= TOL * o["Time"]
-
-
-def test_mixed_pair_once_matches_the_row_gather():
-    """The pair-once acceleration passes (each pair evaluated at its
-    first-part entry, shares handed over through the partner index) against
-    the one-gather kernel on a yielding run with rebuilds: the same pair
-    terms summed in the same row order (differences only from FMA placement)."""
-    res = []
-    for flag in (1, 0):
-        d = gpu_domain()
-        d.set("precision", PRECISION_MIXED)
-        case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
-        d.prepare(case.dt)
-        d.set("pair_once", flag)
-        d.step(100)
-        assert d.geti("nb_searches") > 3
-        res.append({f: d.get_array(f) for f in ("x", "Sigma", "a")})
-        d.close()
-    for f in res[0]:
-        assert rel_l2(res[0][f], res[1][f]) <= 1e-6, f

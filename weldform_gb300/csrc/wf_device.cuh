@@ -192,7 +192,6 @@ struct DomainConst {
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
   int leapfrog;        // 1: SolveDiffUpdateLeapFrog's update (velocities at half steps)
   int gradcorr;        // 1: kernel-gradient correction (Domain::gradKernelCorr)
-  int pair_once;       // mixed form: evaluate each acceleration pair once (pair-once passes)
   int auto_ts, auto_ts_acc;  // adaptive time step: velocity / acceleration criteria
   double CFL, sqrt_h_a;      // their coefficients (Domain::CFL, Domain::sqrt_h_a)
   int av_uniform;      // 1 when every solid particle has the same Alpha and Beta
@@ -219,10 +218,6 @@ struct DevPtrs {
   int* row_len;           // neighbours per particle
   int* row_split;         // neighbours with larger original index (row prefix)
   int* nbr;               // ELL: entry k of particle i at k * N + i
-  int* rev;               // for an entry of the row's second part (neighbour with the smaller
-                          // original index), its position in the neighbour's row (same ELL layout)
-  float4* pair_a;         // mixed acceleration pair terms at the first-part entry of the pair:
-  float4* pair_b;         //   a: the row particle's share, b: the neighbour's (same ELL layout)
   double* gk;             // plain form: GradKernel per row entry (same ELL layout) at the
                           // current positions: written by the rate pass at x(n+1) (or by the
                           // acceleration pass when stale), read by the next step's

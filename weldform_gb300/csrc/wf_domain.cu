@@ -155,14 +155,13 @@ struct wf_domain {
   double CFL = 0.7, sqrt_h_a = 0.0025;
   int gblock = 0;    // mixed gathers' threads per block (0: chosen by particle count)
   int pblock = 0;    // per-particle kernels' threads per block (0: chosen by particle count)
-  int pair_once = 1; // mixed form: acceleration pairs evaluated once
   // Block sizes by particle count: below ~4 blocks of 256 per SM the per-particle
   // kernels (one thread per particle, FP64 or gather latency bound) leave SMs
   // idle, so smaller blocks spread the particles over every SM.
   static int auto_block(long long n) { return n < 78000 ? 64 : (n < 156000 ? 128 : 256); }
   int gblock_now() const { return gblock ? gblock : auto_block(hp.N); }
   int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
-  int graph_key() const { return (gblock_now() * 1024 + pblock_now()) * 2 + pair_once; }
+  int graph_key() const { return gblock_now() * 1024 + pblock_now(); }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
@@ -481,9 +480,6 @@ struct wf_domain {
     P.row_split = dalloc<int>(n);
     P.nbr = dalloc<int>((size_t)MAX_NB * n);
     P.gk = dalloc<double>((size_t)MAX_NB * n);
-    P.rev = dalloc<int>((size_t)MAX_NB * n);
-    P.pair_a = dalloc<float4>((size_t)MAX_NB * n);
-    P.pair_b = dalloc<float4>((size_t)MAX_NB * n);
     CK(cudaMemsetAsync(P.row_len, 0, sizeof(int) * n, stream));
     CK(cudaMemsetAsync(P.row_split, 0, sizeof(int) * n, stream));
     P.cp_len = dalloc<int>(n);
@@ -631,7 +627,7 @@ struct wf_domain {
     CK(cudaMemcpyAsync(P.st, &st, sizeof(st), cudaMemcpyHostToDevice, stream));
     regions = {{d_f, sizeof(double) * NF64 * n}, {d_i, sizeof(int) * NI32 * n}, {P.g, sizeof(float) * NF32 * n},
                {P.st, sizeof(StepState)}, {P.inv, sizeof(int) * n}, {P.row_len, sizeof(int) * n},
-               {P.row_split, sizeof(int) * n}, {P.nbr, sizeof(int) * MAX_NB * n}, {P.rev, sizeof(int) * MAX_NB * n}, {P.cp_len, sizeof(int) * n},
+               {P.row_split, sizeof(int) * n}, {P.nbr, sizeof(int) * MAX_NB * n}, {P.cp_len, sizeof(int) * n},
                {P.cp, contact ? sizeof(int) * MAX_CP * n : sizeof(int)}, {P.node, sizeof(double) * hnode.size()},
                {P.node_v, sizeof(double) * hnode.size()}, {P.elem_normal, sizeof(double) * hnorm.size()},
                {P.elem_pplane, sizeof(double) * hpp.size()}, {P.elem_particle, sizeof(int) * hep.size()}};
@@ -677,7 +673,6 @@ struct wf_domain {
     k.gblock = gblock_now();
     k.pblock = pblock_now();
     k.nblocks = (int)((hp.N + k.pblock - 1) / k.pblock);
-    k.pair_once = pair_once;
     return k;
   }
   void launch_one_step() {
@@ -1216,7 +1211,6 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     d->gblock = v;
     return WF_OK;
   }
-  if (n == "pair_once") { d->pair_once = v != 0; return WF_OK; }
   if (n == "particle_block") {  // 0: by particle count
     if (v != 0 && v != 64 && v != 128 && v != 256) return set_err(WF_ERR_ARG, "particle_block must be 0, 64, 128 or 256");
     d->pblock = v;

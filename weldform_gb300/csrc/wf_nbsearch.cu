@@ -407,33 +407,6 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   }
 }
 
-// Partner positions: each pair (p, q) with orig p < orig q sits in the first
-// part of p's row (entries with larger original index) and in the second part
-// of q's row.  For every second-part entry of q, store the pair's position in
-// p's row (binary search on original index over p's first part, which is
-// ascending), so a pass that forms each pair once at its first-part entry can
-// hand the share of the second-part particle to it.
-__global__ void k_nbr_rev(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
-  size_t N = K.N;
-  const int* orig = P.i + I_ORIG * N;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
-    int len = P.row_len[i], split = P.row_split[i], oi = orig[i];
-    for (int k = split; k < len; ++k) {
-      int j = nb_index(P.nbr[(size_t)k * N + i]);
-      int lo = 0, hi = P.row_split[j] - 1, pos = -1;
-      while (lo <= hi) {
-        int mid = (lo + hi) >> 1;
-        int om = orig[nb_index(P.nbr[(size_t)mid * N + j])];
-        if (om == oi) { pos = mid; break; }
-        if (om < oi) lo = mid + 1; else hi = mid - 1;
-      }
-      if (pos < 0) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);  // an asymmetric pair: only past a row cap
-      P.rev[(size_t)k * N + i] = pos < 0 ? 0 : pos;
-    }
-  }
-}
-
 // CalculateSurface (Domain.cpp:1415-1491): n_i = sum_j m_j (x_i - x_j) in row
 // order; |n| / totmass >= 0.25 h and Nb <= 46 marks the free surface (ID 1).
 __global__ void k_surface(DevPtrs P, DomainConst K) {
@@ -572,8 +545,6 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
     k_nbr_fill<<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
   }
   mark(s, "k_nbr_fill");
-  k_nbr_rev<<<grid(K.N), T, 0, s>>>(P, K);
-  mark(s, "k_nbr_rev");
   if (K.contact) {
     k_surface<<<grid(K.N), T, 0, s>>>(P, K);
     mark(s, "k_surface");

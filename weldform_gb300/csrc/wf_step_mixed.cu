@@ -113,74 +113,9 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
 }
 
 // ---------------------------------------------------------------- accel
-// A particle's acceleration-pass record: positions and velocities as
-// float-float pairs, Sigma/rho^2, p/rho^2 and Cs, alpha/beta (misc), and the
-// tensile-instability groups.  AVU: every solid particle has the same (alpha,
-// beta), so the pair mean is the value itself and the misc group is not read.
-struct AccRec {
-  float4 xh, xl, vh, vl, s0, s1, mi, t0, t1;
-  float ti;
-};
-template <bool TI, bool AVU>
-__device__ __forceinline__ AccRec load_acc(const DevPtrs& P, size_t N, int p) {
-  const float4* r = P.rc + p;
-  AccRec a;
-  a.xh = ld4(r + (size_t)RC_XH * N); a.xl = ld4(r + (size_t)RC_XL * N);
-  a.vh = ld4(r + (size_t)RC_VH * N); a.vl = ld4(r + (size_t)RC_VL * N);
-  a.s0 = ld4(r + (size_t)RC_S0 * N); a.s1 = ld4(r + (size_t)RC_S1 * N);
-  a.mi = AVU ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(r + (size_t)RC_MISC * N);
-  a.t0 = a.t1 = make_float4(0.f, 0.f, 0.f, 0.f);
-  a.ti = 0.f;
-  if (TI) { a.t0 = ld4(r + (size_t)RC_TI0 * N); a.t1 = ld4(r + (size_t)RC_TI1 * N); a.ti = (float)col(P, C_TI, N, p); }
-  return a;
-}
-// The pair's geometry and stress sum (InteractionAlt.cpp:12-260): x = x_a -
-// x_b, GK, and S = Sigma_a/rho_a^2 + Sigma_b/rho_b^2 + Monaghan viscosity +
-// tensile term.  Swapping a and b negates x and leaves GK and S unchanged.
-template <bool TI, bool AVU>
-__device__ __forceinline__ void acc_pair(const DomainConst& K, const AccRec& a, const AccRec& b, float x[3], float& GK,
-                                         float S[6]) {
-  x[0] = (a.xh.x - b.xh.x) + (a.xl.x - b.xl.x);
-  x[1] = (a.xh.y - b.xh.y) + (a.xl.y - b.xl.y);
-  x[2] = (a.xh.z - b.xh.z) + (a.xl.z - b.xl.z);
-  float v0 = (a.vh.x - b.vh.x) + (a.vl.x - b.vl.x), v1 = (a.vh.y - b.vh.y) + (a.vl.y - b.vl.y),
-        v2 = (a.vh.z - b.vh.z) + (a.vl.z - b.vl.z);
-  float hh = 0.5f * (a.xh.w + b.xh.w);
-  float r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2], r;
-  GK = grad_kernel_f(r2, hh, &r);
-  float Alpha, Beta;
-  if (AVU) { Alpha = K.av_alpha; Beta = K.av_beta; }
-  else { Alpha = 0.5f * (a.mi.x + b.mi.x); Beta = 0.5f * (a.mi.y + b.mi.y); }
-  float PIs = 0.f;
-  if (Alpha != 0.f || Beta != 0.f) {
-    float dvx = v0 * x[0] + v1 * x[1] + v2 * x[2];
-    if (dvx < 0.f) {  // Monaghan viscosity (InteractionAlt.cpp:74-94)
-      float MU = hh * dvx / (r * r + 0.01f * hh * hh);
-      float Cij = 0.5f * (a.s1.w + b.s1.w);
-      PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5f * (a.vh.w + b.vh.w));
-    }
-  }
-  S[0] = a.s0.x + b.s0.x + PIs; S[1] = a.s0.y + b.s0.y + PIs; S[2] = a.s0.z + b.s0.z + PIs;
-  S[3] = a.s0.w + b.s0.w; S[4] = a.s1.x + b.s1.x; S[5] = a.s1.y + b.s1.y;
-  if (TI && (a.ti > 0.f || b.ti > 0.f)) {  // tensile instability (InteractionAlt.cpp:102-109)
-    float q = r / hh, q0 = (a.t1.w + b.t1.w) / (2.f * hh);
-    float wq = q < 1.f ? 1.f - 1.5f * q * q + 0.75f * q * q * q : (q < 2.f ? 0.25f * (2.f - q) * (2.f - q) * (2.f - q) : 0.f);
-    float w0 = q0 < 1.f ? 1.f - 1.5f * q0 * q0 + 0.75f * q0 * q0 * q0
-                        : (q0 < 2.f ? 0.25f * (2.f - q0) * (2.f - q0) * (2.f - q0) : 0.f);
-    float f = powf(wq / w0, 0.5f * (a.t1.z + b.t1.z));
-    S[0] += f * (a.t0.x + b.t0.x); S[1] += f * (a.t0.y + b.t0.y); S[2] += f * (a.t0.z + b.t0.z);
-    S[3] += f * (a.t0.w + b.t0.w); S[4] += f * (a.t1.x + b.t1.x); S[5] += f * (a.t1.y + b.t1.y);
-  }
-}
-__device__ __forceinline__ void acc_term(float g0, float g1, float g2, const float S[6], float t[3]) {
-  t[0] = g0 * S[0] + g1 * S[3] + g2 * S[4];
-  t[1] = g0 * S[3] + g1 * S[1] + g2 * S[5];
-  t[2] = g0 * S[4] + g1 * S[5] + g2 * S[2];
-}
-
-// One gather over the whole row (kernel-gradient correction uses the row
-// particle's own matrix, so its pair terms are not shared; the pair-once form
-// below handles the rest).  GC: temp_c = Mult(vc_i, S), InteractionAlt.cpp:166-170.
+// AVU: every solid particle has the same (alpha, beta), so the pair mean is
+// the value itself and the gather reads neither particle's misc group.
+// GC: kernel-gradient correction (temp_c = Mult(vc_i, S), InteractionAlt.cpp:166-170).
 template <bool TI, bool AVU, bool GC>
 __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
@@ -188,7 +123,13 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
     colw(P, C_A, N, i) = 0.0; colw(P, C_A + 1, N, i) = 0.0; colw(P, C_A + 2, N, i) = 0.0;
     return;
   }
-  AccRec a = load_acc<TI, AVU>(P, N, i);
+  const float4* ri = P.rc + i;
+  float4 xh = ld4(ri + (size_t)RC_XH * N), xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
+  float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1 = ld4(ri + (size_t)RC_S1 * N);
+  float4 mi = AVU ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(ri + (size_t)RC_MISC * N);
+  float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
+  float tii = 0.f;
+  if (TI) { t0 = ld4(ri + (size_t)RC_TI0 * N); t1 = ld4(ri + (size_t)RC_TI1 * N); tii = (float)col(P, C_TI, N, i); }
   CorrM cm;
   if (GC) cm = load_corr(P, N, i);
   KSum a0, a1, a2;
@@ -196,69 +137,56 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   const int* nb = P.nbr + i;
   for (int k = 0; k < len; ++k) {
     int j = nb_index(nb[(size_t)k * N]);
-    AccRec b = load_acc<TI, AVU>(P, N, j);
-    float x[3], GK, S[6], t[3];
-    acc_pair<TI, AVU>(K, a, b, x, GK, S);
-    float g0 = GK * x[0], g1 = GK * x[1], g2 = GK * x[2];
-    if (GC) corr_gk(cm, GK, x[0], x[1], x[2], g0, g1, g2);
-    acc_term(g0, g1, g2, S, t);
-    float mj = b.xl.w;
-    a0.add(mj * t[0]); a1.add(mj * t[1]); a2.add(mj * t[2]);
+    const float4* rj = P.rc + j;
+    float4 jxh = ld4(rj + (size_t)RC_XH * N), jxl = ld4(rj + (size_t)RC_XL * N), jvh = ld4(rj + (size_t)RC_VH * N), jvl = ld4(rj + (size_t)RC_VL * N);
+    float4 js0 = ld4(rj + (size_t)RC_S0 * N), js1 = ld4(rj + (size_t)RC_S1 * N);
+    float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
+    float v0 = (vh.x - jvh.x) + (vl.x - jvl.x), v1 = (vh.y - jvh.y) + (vl.y - jvl.y), v2 = (vh.z - jvh.z) + (vl.z - jvl.z);
+    float hh = 0.5f * (xh.w + jxh.w);
+    float r2 = x0 * x0 + x1 * x1 + x2 * x2, r;
+    float GK = grad_kernel_f(r2, hh, &r);
+    float Alpha, Beta;
+    if (AVU) {
+      Alpha = K.av_alpha; Beta = K.av_beta;
+    } else {
+      float4 jmi = ld4(rj + (size_t)RC_MISC * N);
+      Alpha = 0.5f * (mi.x + jmi.x); Beta = 0.5f * (mi.y + jmi.y);
+    }
+    float PIs = 0.f;
+    if (Alpha != 0.f || Beta != 0.f) {
+      float dvx = v0 * x0 + v1 * x1 + v2 * x2;
+      if (dvx < 0.f) {  // Monaghan viscosity (InteractionAlt.cpp:74-94)
+        float MU = hh * dvx / (r * r + 0.01f * hh * hh);
+        float Cij = 0.5f * (s1.w + js1.w);
+        PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5f * (vh.w + jvh.w));
+      }
+    }
+    float S0 = s0.x + js0.x + PIs, S1 = s0.y + js0.y + PIs, S2 = s0.z + js0.z + PIs;
+    float S3 = s0.w + js0.w, S4 = s1.x + js1.x, S5 = s1.y + js1.y;
+    if (TI) {  // tensile instability (InteractionAlt.cpp:102-109); TIR = 0 where TI = 0
+      float4 jt0 = ld4(rj + (size_t)RC_TI0 * N), jt1 = ld4(rj + (size_t)RC_TI1 * N);
+      if (tii > 0.f || (float)col(P, C_TI, N, j) > 0.f) {
+        float q = r / hh, q0 = (t1.w + jt1.w) / (2.f * hh);
+        float wq = q < 1.f ? 1.f - 1.5f * q * q + 0.75f * q * q * q : (q < 2.f ? 0.25f * (2.f - q) * (2.f - q) * (2.f - q) : 0.f);
+        float w0 = q0 < 1.f ? 1.f - 1.5f * q0 * q0 + 0.75f * q0 * q0 * q0
+                            : (q0 < 2.f ? 0.25f * (2.f - q0) * (2.f - q0) * (2.f - q0) : 0.f);
+        float f = powf(wq / w0, 0.5f * (t1.z + jt1.z));
+        S0 += f * (t0.x + jt0.x); S1 += f * (t0.y + jt0.y); S2 += f * (t0.z + jt0.z);
+        S3 += f * (t0.w + jt0.w); S4 += f * (t1.x + jt1.x); S5 += f * (t1.y + jt1.y);
+      }
+    }
+    float g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
+    if (GC) corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
+    float mj = jxl.w;
+    a0.add(mj * (g0 * S0 + g1 * S3 + g2 * S4));
+    a1.add(mj * (g0 * S3 + g1 * S1 + g2 * S5));
+    a2.add(mj * (g0 * S4 + g1 * S5 + g2 * S2));
   }
   colw(P, C_A, N, i) = a0.value(); colw(P, C_A + 1, N, i) = a1.value(); colw(P, C_A + 2, N, i) = a2.value();
 }
 template <bool TI, bool AVU, bool GC>
 __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
   run_rows(K, [&](int i) { accel_mx<TI, AVU, GC>(P, K, i); });
-}
-
-// Pair-once form.  A pair's term t(x_ab) is odd in x_ab, so the two ends'
-// contributions are m_b t and -m_a t of one evaluation.  Pass 1: every
-// particle evaluates the pairs of its row's first part (neighbours with the
-// larger original index, entries [0, row_split)) and stores both shares at the
-// entry's slot.  Pass 2: every particle sums its row in row order, reading its
-// own slot for first-part entries and the partner's slot (P.rev) for the rest.
-// Half the pair evaluations and half the neighbour-record reads of the gather.
-template <bool TI, bool AVU>
-__global__ void __launch_bounds__(512) k_accel_mx_pairs(DevPtrs P, DomainConst K) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
-  size_t N = K.N;
-  if (icol(P, I_KIND, N, i) != 0) return;
-  AccRec a = load_acc<TI, AVU>(P, N, i);
-  float mi = a.xl.w;
-  int split = P.row_split[i];
-  const int* nb = P.nbr + i;
-  for (int k = 0; k < split; ++k) {
-    int j = nb_index(nb[(size_t)k * N]);
-    AccRec b = load_acc<TI, AVU>(P, N, j);
-    float x[3], GK, S[6], t[3];
-    acc_pair<TI, AVU>(K, a, b, x, GK, S);
-    acc_term(GK * x[0], GK * x[1], GK * x[2], S, t);
-    float mj = b.xl.w;
-    P.pair_a[(size_t)k * N + i] = make_float4(mj * t[0], mj * t[1], mj * t[2], 0.f);
-    P.pair_b[(size_t)k * N + i] = make_float4(-(mi * t[0]), -(mi * t[1]), -(mi * t[2]), 0.f);
-  }
-}
-__global__ void __launch_bounds__(512) k_accel_mx_sum(DevPtrs P, DomainConst K) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
-  size_t N = K.N;
-  KSum a0, a1, a2;
-  if (icol(P, I_KIND, N, i) == 0) {
-    int len = P.row_len[i], split = P.row_split[i];
-    for (int k = 0; k < len; ++k) {
-      float4 v;
-      if (k < split) {
-        v = ld4(P.pair_a + (size_t)k * N + i);
-      } else {
-        int j = nb_index(P.nbr[(size_t)k * N + i]);
-        v = ld4(P.pair_b + (size_t)P.rev[(size_t)k * N + i] * N + j);
-      }
-      a0.add(v.x); a1.add(v.y); a2.add(v.z);
-    }
-  }
-  colw(P, C_A, N, i) = a0.value(); colw(P, C_A + 1, N, i) = a1.value(); colw(P, C_A + 2, N, i) = a2.value();
 }
 
 // ---------------------------------------------------------------- density + drift + kick
@@ -601,18 +529,8 @@ void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, c
 
 template <bool TI, bool AVU>
 static void launch_accel_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
-  if (K.gradcorr) {
-    k_accel_mx<TI, AVU, true><<<ng, gb, 0, s>>>(P, K);
-    mark(s, "k_accel_mx");
-  } else if (K.pair_once) {
-    k_accel_mx_pairs<TI, AVU><<<ng, gb, 0, s>>>(P, K);
-    mark(s, "k_accel_mx_pairs");
-    k_accel_mx_sum<<<ng, gb, 0, s>>>(P, K);
-    mark(s, "k_accel_mx_sum");
-  } else {
-    k_accel_mx<TI, AVU, false><<<ng, gb, 0, s>>>(P, K);
-    mark(s, "k_accel_mx");
-  }
+  if (K.gradcorr) k_accel_mx<TI, AVU, true><<<ng, gb, 0, s>>>(P, K);
+  else k_accel_mx<TI, AVU, false><<<ng, gb, 0, s>>>(P, K);
 }
 
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
@@ -629,6 +547,7 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
     if (K.av_uniform) launch_accel_mx<false, true>(P, K, ng, gb, s);
     else launch_accel_mx<false, false>(P, K, ng, gb, s);
   }
+  mark(s, "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);

@@ -22,7 +22,6 @@ def main():
     ap.add_argument("--kernels", action="store_true", help="print per-kernel CUDA-event times of the steps")
     ap.add_argument("--gather-block", type=int, default=None, help="mixed gathers: threads per block")
     ap.add_argument("--particle-block", type=int, default=None, help="per-particle kernels: threads per block")
-    ap.add_argument("--pair-once", type=int, default=None, help="mixed acceleration: 1 pair-once passes, 0 one gather")
     a = ap.parse_args()
     dx = configs.dx_for_count(0.010, 0.030, a.n)
     d = Domain()
@@ -33,8 +32,6 @@ def main():
         d.set("gather_block", a.gather_block)
     if a.particle_block is not None:
         d.set("particle_block", a.particle_block)
-    if a.pair_once is not None:
-        d.set("pair_once", a.pair_once)
     t = time.perf_counter()
     d.step(a.steps)
     el = time.perf_counter() - t
