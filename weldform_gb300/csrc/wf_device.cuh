@@ -78,7 +78,8 @@ enum RecCur : int {        // current-state groups
 };
 enum RecNext : int {       // next-step groups
   RN_XH = 0, RN_XL = 1,    // as RC_XH / RC_XL at x(n+1)
-  RN_VH = 2, RN_VL = 3,    // v(n+1) hi/lo, rho(n+1), m/rho(n+1)
+  RN_VH = 2, RN_VL = 3,    // v(n+1) hi/lo, p/rho^2 at rho(n+1) (the rate gather's kinetic term;
+                           // the current group carries rho there), m/rho(n+1)
   RN_E = 4,                // p/rho^2 at rho(n+1), k_T, T(n+1) hi, T(n+1) lo
   RN_N = 5
 };

@@ -255,9 +255,10 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   float4* r = P.rn + i;
   r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], xh.w);
   r[(size_t)RN_XL * N] = make_float4(nxl[0], nxl[1], nxl[2], (float)col(P, C_MASS, N, i));
-  r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], (float)rn);
+  float pr2 = solid ? (float)(pn / (rn * rn)) : 0.f;
+  r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], pr2);  // the rate gather reads p/rho^2 here
   r[(size_t)RN_VL * N] = make_float4(nvl[0], nvl[1], nvl[2], (float)mrn);
-  r[(size_t)RN_E * N] = make_float4(solid ? (float)(pn / (rn * rn)) : 0.f, ri[(size_t)RC_MISC * N].z, th, tl);
+  r[(size_t)RN_E * N] = make_float4(pr2, ri[(size_t)RC_MISC * N].z, th, tl);
 }
 template <bool GC>
 __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainConst K) {
@@ -277,7 +278,8 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
   double dkin = 0.0, cond = 0.0;
   if (icol(P, I_KIND, N, i) == 0) {
     const float4* ri = P.rn + i;
-    float4 xh = ld4(ri + (size_t)RN_XH * N), xl = ld4(ri + (size_t)RN_XL * N), vh = ld4(ri + (size_t)RN_VH * N), vl = ld4(ri + (size_t)RN_VL * N), e = ld4(ri + (size_t)RN_E * N);
+    float4 xh = ld4(ri + (size_t)RN_XH * N), xl = ld4(ri + (size_t)RN_XL * N), vh = ld4(ri + (size_t)RN_VH * N), vl = ld4(ri + (size_t)RN_VL * N);
+    float4 e = THERMAL ? ld4(ri + (size_t)RN_E * N) : make_float4(vh.w, 0.f, 0.f, 0.f);
     CorrM cm;
     if (GC) cm = load_corr(P, N, i);
     KSum M[9];  // sum_j (m_j / rho_j) (-GK / 2) (v_i - v_j)_k (x_i - x_j)_l  (GC: gk_l for GK x_l)
@@ -289,7 +291,8 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       int j = nb_index(ent);
       const float4* rj = P.rn + j;
       float4 jxh = ld4(rj + (size_t)RN_XH * N), jxl = ld4(rj + (size_t)RN_XL * N), jvh = ld4(rj + (size_t)RN_VH * N), jvl = ld4(rj + (size_t)RN_VL * N);
-      float4 je = ld4(rj + (size_t)RN_E * N);
+      // p/rho^2 rides in the velocity group; conduction needs the E group (k_T, T)
+      float4 je = THERMAL ? ld4(rj + (size_t)RN_E * N) : make_float4(jvh.w, 0.f, 0.f, 0.f);
       float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
       float b0 = (vh.x - jvh.x) + (vl.x - jvl.x), b1 = (vh.y - jvh.y) + (vl.y - jvl.y), b2 = (vh.z - jvh.z) + (vl.z - jvl.z);
       float r;
@@ -430,7 +433,9 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
     float4* rc = P.rc + i;
     rc[(size_t)RC_XH * N] = rn[(size_t)RN_XH * N];
     rc[(size_t)RC_XL * N] = rn[(size_t)RN_XL * N];
-    rc[(size_t)RC_VH * N] = rn[(size_t)RN_VH * N];
+    float4 nvh = rn[(size_t)RN_VH * N];
+    nvh.w = (float)rho;  // the current group carries rho (the acceleration gather's viscosity)
+    rc[(size_t)RC_VH * N] = nvh;
     rc[(size_t)RC_VL * N] = rn[(size_t)RN_VL * N];
     float4 ne = rn[(size_t)RN_E * N];
     float4 misc = rc[(size_t)RC_MISC * N];
