@@ -72,6 +72,18 @@ def _vec(v, n=3, default=0.0):
 
 
 def build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = None) -> Run:
+    """Build the domain an input file describes (WeldForm.cpp:147-940).  A key
+    the reference driver reads without a default (readValue leaves the
+    variable as it was, uninitialized) raises WF_ERR_UNSUPPORTED."""
+    try:
+        return _build(inp, make, precision)
+    except KeyError as e:
+        raise WFError(WF_ERR_UNSUPPORTED,
+                      f"input lacks {e.args[0]!r}, which the reference driver reads into an uninitialized "
+                      f"variable") from None
+
+
+def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = None) -> Run:
     """Build the domain of a WeldForm JSON input (file path or parsed dict)."""
     j = inp if isinstance(inp, dict) else json.load(open(inp))
     config = j.get("Configuration", {})
