@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from tests._support import gpu_domain, oracle_domain, rel_l2
-from weldform_gb300 import BILINEAR, WFError
+from weldform_gb300 import BILINEAR, PRECISION_MIXED, WFError
 from weldform_gb300 import weldform_json as wj
 
 R, L, r = 0.003, 0.006, 0.00025
@@ -168,3 +168,47 @@ def test_json_run_on_the_gpu_matches_the_oracle(tmp_path):
         assert np.array_equal(g[:, 3], o[:, 3])
         for c in cols:
             assert rel_l2(g[:, c], o[:, c]) <= 2e-6, c   # 6 printed digits
+
+
+HOLLOMON = copy.deepcopy(COMPRESSION)
+HOLLOMON["Materials"] = [{"type": "Hollomon", "density0": rho, "youngsModulus": E, "poissonsRatio": nu,
+                          "yieldStress0": 260e6, "const": [718e6, 0.22]}]
+
+
+def _first_step_sigma(make, precision=None):
+    r = wj.build(HOLLOMON, make=make)
+    if precision is not None:
+        r.dom.set("precision", precision)
+    r.dom.prepare(r.dt)
+    r.dom.step(1)
+    s = r.dom.get_array("Sigma")
+    r.dom.close()
+    return s
+
+
+def test_hollomon_input_starts_with_zero_yield_stress():
+    """The driver gives Hollomon particles mat->CalcYieldStress(0, 0, T)
+    (WeldForm.cpp:912-913), the base class's 0.0 (Material.h:101).  In the
+    first stress update every particle with zero trial stress then takes
+    min(0/0, 1) (Particle.cpp:277), which is NaN: its shear stress becomes
+    NaN.  Particles the moving zone strains have a positive trial stress and
+    stay finite."""
+    r = wj.build(HOLLOMON, make=_oracle)
+    assert np.all(r.dom.get_array("Sigmay") == 0.0)
+    r.dom.close()
+    s = _first_step_sigma(_oracle)
+    bad = ~np.isfinite(s).all(axis=1)
+    assert 0 < bad.sum() < len(bad)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [None, PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_hollomon_nan_pattern_matches_the_oracle(precision):
+    """The GPU stress update keeps std::min's NaN (a NaN ratio is not clamped
+    to 1): the same particles turn NaN as in the oracle, the others agree."""
+    o = _first_step_sigma(_oracle)
+    g = _first_step_sigma(gpu_domain, precision)
+    assert np.array_equal(np.isnan(g), np.isnan(o))
+    ok = np.isfinite(o)
+    tol = 1e-9 if precision is None else 1e-4
+    assert rel_l2(g[ok], o[ok]) <= tol
