@@ -117,6 +117,25 @@ def test_elastic_cylinder_steps():
     _check(g, o, FIELDS, SCALARS)
 
 
+def test_tensor_fields_read_back_as_full_rows():
+    """Symmetric tensors come back as 3x3 rows equal to their transpose,
+    RotationRate antisymmetric with a zero diagonal (both expanded on the
+    device); StrainRate and RotationRate match the oracle, RotationRate's
+    error measured against the velocity gradient's scale (its entries nearly
+    cancel in the upsetting cylinder)."""
+    f = ("Sigma", "ShearStress", "Strain", "StrainRate", "RotationRate")
+    g, o = _pair(configs.cylinder_upsetting, 20, f, R=0.004, L=0.008, dx=0.0005)
+    for k in ("Sigma", "ShearStress", "Strain", "StrainRate"):
+        t = g[k].reshape(-1, 3, 3)
+        assert np.array_equal(t, t.transpose(0, 2, 1)), k
+    w = g["RotationRate"].reshape(-1, 3, 3)
+    assert np.array_equal(w, -w.transpose(0, 2, 1))
+    assert not np.any(w[:, [0, 1, 2], [0, 1, 2]])
+    assert rel_l2(g["StrainRate"], o["StrainRate"]) <= TOL
+    scale = np.linalg.norm(o["StrainRate"]) + np.linalg.norm(o["RotationRate"])
+    assert np.linalg.norm(g["RotationRate"] - o["RotationRate"]) <= TOL * scale
+
+
 def test_yielding_bilinear_with_rebuilds():
     g, o = _pair(configs.cylinder_upsetting, 80, FIELDS + ("Strain_pl", "eff_strain_rate"), SCALARS,
                  R=0.004, L=0.008, dx=0.0005, v_top=-20.0)

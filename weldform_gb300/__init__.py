@@ -338,17 +338,27 @@ class Domain:
         return {"loss": loss.value, "grad": grad, "curve": curve, "fwd_ms": fms.value, "adj_ms": ams.value}
 
     # ------------------------------------------------------------ arrays
-    def get_array(self, field: str) -> np.ndarray:
+    def get_array(self, field: str, out: np.ndarray = None) -> np.ndarray:
+        """Particle field in original particle order.  ``out`` (optional) is a
+        C-contiguous array of the field's dtype and size (e.g. pinned host
+        memory) that receives the values; it is returned as given."""
         n = self.particle_count
-        if field in ("ID", "Nb", "IsFree"):
-            out = np.empty(n, dtype=np.int32)
-            self._call("get_particle_array_i32", self._h, field.encode(),
-                       out.ctypes.data_as(_IP), n)
+        i32 = field in ("ID", "Nb", "IsFree")
+        comps = 1 if i32 else (9 if field in TENSOR_FIELDS else (3 if field in VECTOR_FIELDS else 1))
+        dt = np.int32 if i32 else np.float64
+        if out is None:
+            buf = np.empty(n * comps, dtype=dt)
+        else:
+            if out.dtype != dt or out.size != n * comps or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"{field}: out must be a C-contiguous {np.dtype(dt).name} array of {n * comps} values")
+            buf = out.reshape(-1)
+        if i32:
+            self._call("get_particle_array_i32", self._h, field.encode(), buf.ctypes.data_as(_IP), buf.size)
+        else:
+            self._call("get_particle_array_f64", self._h, field.encode(), buf.ctypes.data_as(_DP), buf.size)
+        if out is not None:
             return out
-        comps = 9 if field in TENSOR_FIELDS else (3 if field in VECTOR_FIELDS else 1)
-        out = np.empty(n * comps, dtype=np.float64)
-        self._call("get_particle_array_f64", self._h, field.encode(), out.ctypes.data_as(_DP), out.size)
-        return out.reshape(n, comps) if comps > 1 else out
+        return buf.reshape(n, comps) if comps > 1 else buf
 
     def set_array(self, field: str, values):
         if field in ("ID", "mat", "Material_model", "Fail", "Material", "not_write_surf_ID"):

@@ -1090,6 +1090,18 @@ struct wf_domain {
     CK(cudaFreeAsync(tmp, stream));
     CK(cudaStreamSynchronize(stream));
   }
+  // Symmetric (6 stored columns) or antisymmetric (3) tensor as 3x3 rows,
+  // expanded on the device so the copy lands straight in dst.
+  void get_f64_tensor(int c, int anti, double* dst) {
+    size_t n = hp.N;
+    use_device();
+    double* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, sizeof(double) * n * 9, stream));
+    wf::launch_gather_orig_tensor(P, K, d_f + (size_t)c * n, tmp, anti, stream);
+    CK(cudaMemcpyAsync(dst, tmp, sizeof(double) * n * 9, cudaMemcpyDeviceToHost, stream));
+    CK(cudaFreeAsync(tmp, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
   void set_f64(int c, int ncomp, const double* src) {
     size_t n = hp.N;
     if (!prepared) {
@@ -1394,6 +1406,10 @@ int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int6
     size_t N = d->hp.N;
     if (nc == 6 || c == wf::C_RR) {
       if (n != (int64_t)N * 9) return set_err(WF_ERR_ARG, "array size mismatch for " + f);
+      if (d->prepared) {
+        d->get_f64_tensor(c, nc == 3, dst);
+        return WF_OK;
+      }
       std::vector<double> t(N * nc);
       d->get_f64(c, nc, t.data());
       for (size_t p = 0; p < N; ++p) {

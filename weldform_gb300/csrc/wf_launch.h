@@ -60,6 +60,9 @@ void launch_gather_orig(const DevPtrs& P, const DomainConst& K, const double* co
                         cudaStream_t s);
 void launch_scatter_orig(const DevPtrs& P, const DomainConst& K, const double* in_orig, double* col, int ncomp,
                          cudaStream_t s);
+// Symmetric (6 stored columns) or antisymmetric (3, anti = 1) tensor as 9 values per particle.
+void launch_gather_orig_tensor(const DevPtrs& P, const DomainConst& K, const double* col, double* out_orig, int anti,
+                               cudaStream_t s);
 void launch_gather_orig_i32(const DevPtrs& P, const DomainConst& K, const int* col, int* out_orig, cudaStream_t s);
 void launch_scatter_orig_i32(const DevPtrs& P, const DomainConst& K, const int* in_orig, int* col, cudaStream_t s);
 // Recompute derived columns after a host write of state (x, v, rho, Sigma...).

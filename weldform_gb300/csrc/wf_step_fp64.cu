@@ -815,6 +815,27 @@ __global__ void k_scatter_orig(DevPtrs P, DomainConst K, const double* in, doubl
   int i = P.inv[o];
   for (int c = 0; c < ncomp; ++c) colp[(size_t)c * K.N + i] = in[(size_t)o * ncomp + c];
 }
+// A stored symmetric tensor (xx, yy, zz, xy, xz, yz) or antisymmetric one
+// (xy, xz, yz) written as full row-major 3x3 rows in original order.
+__global__ void k_gather_orig_tensor(DevPtrs P, DomainConst K, const double* colp, double* out, int anti) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= K.N) return;
+  const size_t N = K.N;
+  int i = P.inv[o];
+  double* r = out + (size_t)o * 9;
+  if (anti) {
+    double a = colp[i], b = colp[N + i], c = colp[2 * N + i];
+    r[0] = 0.0; r[1] = a; r[2] = b;
+    r[3] = -a; r[4] = 0.0; r[5] = c;
+    r[6] = -b; r[7] = -c; r[8] = 0.0;
+  } else {
+    double xx = colp[i], yy = colp[N + i], zz = colp[2 * N + i];
+    double xy = colp[3 * N + i], xz = colp[4 * N + i], yz = colp[5 * N + i];
+    r[0] = xx; r[1] = xy; r[2] = xz;
+    r[3] = xy; r[4] = yy; r[5] = yz;
+    r[6] = xz; r[7] = yz; r[8] = zz;
+  }
+}
 __global__ void k_gather_orig_i32(DevPtrs P, DomainConst K, const int* colp, int* out) {
   int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= K.N) return;
@@ -830,6 +851,10 @@ void launch_gather_orig(const DevPtrs& P, const DomainConst& K, const double* c,
 }
 void launch_scatter_orig(const DevPtrs& P, const DomainConst& K, const double* in, double* c, int n, cudaStream_t s) {
   k_scatter_orig<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, in, c, n);
+}
+void launch_gather_orig_tensor(const DevPtrs& P, const DomainConst& K, const double* c, double* o, int anti,
+                               cudaStream_t s) {
+  k_gather_orig_tensor<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, c, o, anti);
 }
 void launch_gather_orig_i32(const DevPtrs& P, const DomainConst& K, const int* c, int* o, cudaStream_t s) {
   k_gather_orig_i32<<<nblk(K.N, BLOCK), BLOCK, 0, s>>>(P, K, c, o);
