@@ -117,6 +117,38 @@ def test_elastic_cylinder_steps():
     _check(g, o, FIELDS, SCALARS)
 
 
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, 1e-4)], ids=["fp64", "mixed"])
+def test_viscosity_constants_written_after_the_prologue(precision, tol):
+    """Per-particle Alpha/Beta written after prepare: the gathers leave the
+    uniform-constant fast path (the step is recaptured) and match the oracle
+    stepped with the same values; writing uniform values back restores it."""
+    out = {}
+    for name in ("gpu", "oracle"):
+        d = gpu_domain() if name == "gpu" else oracle_domain()
+        if name == "oracle":
+            d.set("cpu_threads", THREADS)
+        else:
+            d.set("precision", precision)
+        case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+        d.prepare(case.dt)
+        d.step(5)
+        n = d.particle_count
+        a = np.random.default_rng(11).uniform(0.5, 1.5, n)
+        d.set_array("Alpha", a)
+        d.set_array("Beta", 0.5 * a)
+        d.step(20)
+        out[name] = {f: d.get_array(f) for f in ("Displacement", "v", "Sigma")}
+        d.set_array("Alpha", np.ones(n))
+        d.set_array("Beta", np.zeros(n))
+        d.step(10)
+        out[name]["Displacement2"] = d.get_array("Displacement")
+        out[name]["Sigma2"] = d.get_array("Sigma")
+        d.close()
+    for f in out["oracle"]:
+        e = rel_l2(out["gpu"][f], out["oracle"][f])
+        assert e <= tol, (f, e)
+
+
 def test_tensor_fields_read_back_as_full_rows():
     """Symmetric tensors come back as 3x3 rows equal to their transpose,
     RotationRate antisymmetric with a zero diagonal (both expanded on the

@@ -37,9 +37,9 @@ static_assert(ADJ_BLOCK == BLOCK, "the finish kernel's partials are sized by ADJ
 // with C = 1 / (pi hh^4):
 //   q < 1:      GK = C/hh (-3 + 9/4 q),     dGK/dr = C/hh^2 9/4
 //   1 <= q < 2: GK = -3/4 C (2 - q)^2 / r,  dGK/dr = 3/4 C (4 - q^2) / r^2
-// formed with one division (1/r) per pair, plus 1/hh when the pair's
-// smoothing lengths differ (inv_hi = 1/h_i is the caller's).  The values
-// equal the forward's to rounding.
+// with r and 1/r from one reciprocal square root per pair, plus 1/hh when
+// the pair's smoothing lengths differ (inv_hi = 1/h_i is the caller's).  The
+// values equal the forward's to rounding.
 struct GeoD {
   double x0, x1, x2, r, GK, dGr;  // dGr = (dGK/dr) / r
 };
@@ -48,12 +48,12 @@ __device__ __forceinline__ GeoD geo_d(const double xi[3], double hi, double inv_
   GeoD g;
   g.x0 = xi[0] - xj0; g.x1 = xi[1] - xj1; g.x2 = xi[2] - xj2;
   double r2 = g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2;
-  g.r = sqrt(r2);
+  double rinv = r2 > 0.0 ? rsqrt(r2) : 0.0;
+  g.r = r2 * rinv;
   double inv_h = hj == hi ? inv_hi : 2.0 / (hi + hj);
   double q = g.r * inv_h;
   double ih2 = inv_h * inv_h;
   double C = ih2 * ih2 * (1.0 / WF_PI);
-  double rinv = g.r > 0.0 ? 1.0 / g.r : 0.0;
   double dG = 0.0;
   if (q == 0.0) g.GK = C * inv_h * -3.0;
   else if (q < 1.0) { g.GK = C * inv_h * (-3.0 + 2.25 * q); dG = C * ih2 * 2.25; }
@@ -627,7 +627,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
     g.GK = A.gk_start[(size_t)k * N + i];
     g.dGr = A.dg_start[(size_t)k * N + i];
     double b0 = vi[0] - col(S, C_V, N, j), b1 = vi[1] - col(S, C_V + 1, N, j), b2 = vi[2] - col(S, C_V + 2, N, j);
-    double Alpha = (al + col(S, C_ALPHA, N, j)) / 2.0, Beta = (be + col(S, C_BETA, N, j)) / 2.0;
+    double Alpha = K.av_uniform ? al : (al + col(S, C_ALPHA, N, j)) / 2.0;
+    double Beta = K.av_uniform ? be : (be + col(S, C_BETA, N, j)) / 2.0;
     double PIs = 0.0, MU = 0.0, iDn = 0.0, Cij = 0.0, irbar = 0.0, hh = 0.0;
     bool av = false;
     if (Alpha != 0.0 || Beta != 0.0) {
@@ -652,12 +653,13 @@ __global__ void __launch_bounds__(BLOCK) k_adj_accel(AdjPtrs A, DomainConst K) {
     lx[0] += g.GK * u0 + xu * g.dGr * g.x0;
     lx[1] += g.GK * u1 + xu * g.dGr * g.x1;
     lx[2] += g.GK * u2 + xu * g.dGr * g.x2;
-    lSs[0] += g.GK * g.x0 * Gm[0]; lSs[1] += g.GK * g.x1 * Gm[1]; lSs[2] += g.GK * g.x2 * Gm[2];
-    lSs[3] += g.GK * (g.x0 * Gm[1] + g.x1 * Gm[0]);
-    lSs[4] += g.GK * (g.x0 * Gm[2] + g.x2 * Gm[0]);
-    lSs[5] += g.GK * (g.x1 * Gm[2] + g.x2 * Gm[1]);
+    double gx0 = g.GK * g.x0, gx1 = g.GK * g.x1, gx2 = g.GK * g.x2;
+    lSs[0] += gx0 * Gm[0]; lSs[1] += gx1 * Gm[1]; lSs[2] += gx2 * Gm[2];
+    lSs[3] += gx0 * Gm[1]; lSs[3] += gx1 * Gm[0];
+    lSs[4] += gx0 * Gm[2]; lSs[4] += gx2 * Gm[0];
+    lSs[5] += gx1 * Gm[2]; lSs[5] += gx2 * Gm[1];
     if (av) {
-      double lPI = g.GK * (g.x0 * Gm[0] + g.x1 * Gm[1] + g.x2 * Gm[2]);
+      double lPI = gx0 * Gm[0] + gx1 * Gm[1] + gx2 * Gm[2];
       double lMU = lPI * (Alpha * Cij + 2.0 * Beta * MU) * irbar;
       lcs += lPI * Alpha * MU * irbar * 0.5;
       lrho += -lPI * PIs * irbar * 0.5;

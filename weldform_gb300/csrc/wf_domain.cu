@@ -591,18 +591,7 @@ struct wf_domain {
     K.totmass_mean = tm / N;
     K.id_free_surf = -999999;
     K.leapfrog = integrator;
-    {
-      K.av_uniform = 1;
-      bool first = true;
-      double a0 = 0, b0 = 0;
-      for (int p = 0; p < N; ++p) {
-        if (hp.i[I_KIND][p] != 0) continue;
-        if (first) { a0 = F(C_ALPHA, p); b0 = F(C_BETA, p); first = false; }
-        else if (F(C_ALPHA, p) != a0 || F(C_BETA, p) != b0) { K.av_uniform = 0; break; }
-      }
-      K.av_alpha = (float)a0;
-      K.av_beta = (float)b0;
-    }
+    set_av_uniform(hp.f[C_ALPHA].data(), hp.f[C_BETA].data(), hp.i[I_KIND].data(), N);
     K.gradcorr = grad_corr;
     if (auto_ts_cont && contact && integrator == 0)
       throw CudaError{WF_ERR_UNSUPPORTED, "auto_ts_cont with contact: the kick-drift solver reads Domain::min_force_ts, "
@@ -795,6 +784,33 @@ struct wf_domain {
   }
   // The plain form's per-entry GradKernel (P.gk) no longer matches the state.
   void invalidate_gk() { CK(cudaMemsetAsync(&P.st->gk_valid, 0, sizeof(int), stream)); }
+  // Whether Alpha and Beta are the same on every SPH particle: the gathers
+  // then take the pair's (a_i + a_j) / 2 = a from K instead of loading a_j.
+  void set_av_uniform(const double* a, const double* b, const int* kind, size_t n) {
+    K.av_uniform = 1;
+    bool first = true;
+    double a0 = 0, b0 = 0;
+    for (size_t p = 0; p < n; ++p) {
+      if (kind[p] != 0) continue;
+      if (first) { a0 = a[p]; b0 = b[p]; first = false; }
+      else if (a[p] != a0 || b[p] != b0) { K.av_uniform = 0; break; }
+    }
+    K.av_alpha = (float)a0;
+    K.av_beta = (float)b0;
+  }
+  // Alpha or Beta written after the prologue: re-evaluate the flag on the
+  // device columns (any order) and recapture the step with the new constants.
+  void refresh_av_uniform() {
+    size_t n = hp.N;
+    std::vector<double> a(n), b(n);
+    std::vector<int> kind(n);
+    CK(cudaMemcpyAsync(a.data(), d_f + (size_t)wf::C_ALPHA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(b.data(), d_f + (size_t)wf::C_BETA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(kind.data(), d_i + (size_t)wf::I_KIND * n, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    set_av_uniform(a.data(), b.data(), kind.data(), n);
+    if (graph) { CK(cudaGraphExecDestroy(graph)); graph = nullptr; }
+  }
   void checkpoint_save(int slot) {
     use_device();
     if ((int)slots.size() <= slot) slots.resize(slot + 1);
@@ -1119,6 +1135,7 @@ struct wf_domain {
     shadows_valid = false;
     invalidate_gk();
     CK(cudaStreamSynchronize(stream));
+    if (c == wf::C_ALPHA || c == wf::C_BETA) refresh_av_uniform();
   }
   void get_i32(int c, int* dst) {
     size_t n = hp.N;

@@ -90,7 +90,10 @@ __device__ __forceinline__ PairGeo pair_geo(double xi0, double xi1, double xi2, 
   PairGeo g;
   g.x0 = xi0 - xj0; g.x1 = xi1 - xj1; g.x2 = xi2 - xj2;
   g.r2 = g.x0 * g.x0 + g.x1 * g.x1 + g.x2 * g.x2;
-  g.r = sqrt(g.r2);
+  // r and 1/r from one reciprocal square root instead of a square root and a
+  // division (r2 = 0 only for coincident particles, where q = 0)
+  double ir = g.r2 > 0.0 ? rsqrt(g.r2) : 0.0;
+  g.r = g.r2 * ir;
   double inv_h;
   if (hj == hi) { g.hh = hi; inv_h = inv_hi; }
   else { g.hh = (hi + hj) / 2; inv_h = 1.0 / g.hh; }
@@ -99,7 +102,7 @@ __device__ __forceinline__ PairGeo pair_geo(double xi0, double xi1, double xi2, 
   double C = ih2 * ih2 * (1.0 / WF_PI);
   if (q == 0.0) g.GK = C * inv_h * -3.0;
   else if (q < 1.0) g.GK = C * inv_h * (-3.0 + 2.25 * q);
-  else if (q < 2.0) { double t = 2.0 - q; g.GK = C / g.r * (-0.75 * t * t); }
+  else if (q < 2.0) { double t = 2.0 - q; g.GK = C * ir * (-0.75 * t * t); }
   else g.GK = 0.0;
   return g;
 }
@@ -219,7 +222,9 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
                    col(P, C_H, N, j));
       P.gk[(size_t)k * N + i] = g.GK;  // for the density pass (same x(n), h)
     }
-    double Alpha = (ai + col(P, C_ALPHA, N, j)) / 2.0, Beta = (bi + col(P, C_BETA, N, j)) / 2.0;
+    // (a + a) / 2 = a exactly, so uniform constants need no per-pair loads
+    double Alpha = K.av_uniform ? ai : (ai + col(P, C_ALPHA, N, j)) / 2.0;
+    double Beta = K.av_uniform ? bi : (bi + col(P, C_BETA, N, j)) / 2.0;
     double v0 = vi0 - col(P, C_V, N, j), v1 = vi1 - col(P, C_V + 1, N, j), v2 = vi2 - col(P, C_V + 2, N, j);
     double PIs = 0.0;
     if (Alpha != 0.0 || Beta != 0.0) {
@@ -248,17 +253,19 @@ __global__ void __launch_bounds__(BLOCK) k_accel(DevPtrs P, DomainConst K) {
       S4 = S4 + f * (col(P, C_TIR + 4, N, i) + col(P, C_TIR + 4, N, j));
       S5 = S5 + f * (col(P, C_TIR + 5, N, i) + col(P, C_TIR + 5, N, j));
     }
-    double g0 = g.GK * g.x0, g1 = g.GK * g.x1, g2 = g.GK * g.x2;
+    double mj = col(P, C_MASS, N, j);
+    double g0, g1, g2;
     if (K.gradcorr) {  // temp_c = Mult(vc_i, S) of the locking sum (InteractionAlt.cpp:166-170)
       double vc[3];
       corr_grad(P, N, i, g.GK, g.x0, g.x1, g.x2, vc);
-      g0 = vc[0]; g1 = vc[1]; g2 = vc[2];
+      g0 = mj * vc[0]; g1 = mj * vc[1]; g2 = mj * vc[2];
+    } else {
+      double gm = mj * g.GK;  // m_j (GK x_ij) . S
+      g0 = gm * g.x0; g1 = gm * g.x1; g2 = gm * g.x2;
     }
-    double t0 = g0 * S0 + g1 * S3 + g2 * S4;
-    double t1 = g0 * S3 + g1 * S1 + g2 * S5;
-    double t2 = g0 * S4 + g1 * S5 + g2 * S2;
-    double mj = col(P, C_MASS, N, j);
-    a0 += mj * t0; a1 += mj * t1; a2 += mj * t2;
+    a0 += g0 * S0 + g1 * S3 + g2 * S4;
+    a1 += g0 * S3 + g1 * S1 + g2 * S5;
+    a2 += g0 * S4 + g1 * S5 + g2 * S2;
   }
   colw(P, C_A, N, i) = a0; colw(P, C_A + 1, N, i) = a1; colw(P, C_A + 2, N, i) = a2;
 }
@@ -542,7 +549,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
         P.gk[(size_t)k * N + i] = g.GK;  // x(n+1) is the next step's x(n): its acceleration pass reuses it
         double b0 = v[0] - col(P, C_VN, N, j), b1 = v[1] - col(P, C_VN + 1, N, j), b2 = v[2] - col(P, C_VN + 2, N, j);
         {
-          double dv = b0 * (g.GK * g.x0) + b1 * (g.GK * g.x1) + b2 * (g.GK * g.x2);
+          double dv = g.GK * (b0 * g.x0 + b1 * g.x1 + b2 * g.x2);
           bool up = nb_up(e);  // original index of j larger than i's
           // pair (P1 = smaller original index): 0.5 m_P2 (p1/d1^2 + p2/d2^2) v12.(GK x12)
           double pk = 0.5 * (up ? col(P, C_MASS, N, j) : massi) * (pri + col(P, C_PR2N, N, j)) * dv;
@@ -577,18 +584,23 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
           rr[2] += wf * (-0.5 * (bv[1] * gk[2] - bv[2] * gk[1]));
           continue;
         }
-        double f = -0.5 * g.GK;
-        double w = col(P, C_MRHON, N, j);
-        sr[0] += w * (f * (2.0 * b0 * g.x0));
-        sr[1] += w * (f * (2.0 * b1 * g.x1));
-        sr[2] += w * (f * (2.0 * b2 * g.x2));
-        sr[3] += w * (f * (b0 * g.x1 + b1 * g.x0));
-        sr[4] += w * (f * (b0 * g.x2 + b2 * g.x0));
-        sr[5] += w * (f * (b1 * g.x2 + b2 * g.x1));
-        rr[0] += w * (f * (b0 * g.x1 - b1 * g.x0));
-        rr[1] += w * (f * (b0 * g.x2 - b2 * g.x0));
-        rr[2] += w * (f * (b1 * g.x2 - b2 * g.x1));
+        // (m_j/rho_j) (-GK/2) (v_ij (x) x_ij +- x_ij (x) v_ij): u = (m_j/rho_j)(-GK/2) v_ij
+        // enters every entry; the diagonal collects u_a x_a and is doubled once
+        // after the loop (exact in binary).
+        double wf = col(P, C_MRHON, N, j) * (-0.5 * g.GK);
+        double u0 = wf * b0, u1 = wf * b1, u2 = wf * b2;
+        sr[0] += u0 * g.x0;
+        sr[1] += u1 * g.x1;
+        sr[2] += u2 * g.x2;
+        sr[3] += u0 * g.x1; sr[3] += u1 * g.x0;
+        sr[4] += u0 * g.x2; sr[4] += u2 * g.x0;
+        sr[5] += u1 * g.x2; sr[5] += u2 * g.x1;
+        rr[0] += u0 * g.x1; rr[0] -= u1 * g.x0;
+        rr[1] += u0 * g.x2; rr[1] -= u2 * g.x0;
+        rr[2] += u1 * g.x2; rr[2] -= u2 * g.x1;
       }
+      if (!K.gradcorr)
+        for (int c = 0; c < 3; ++c) sr[c] = 2.0 * sr[c];
       StressIO s;
       for (int c = 0; c < 6; ++c) {
         s.tau[c] = col(P, C_TAU + c, N, i); s.eps[c] = col(P, C_EPS + c, N, i);
