@@ -62,26 +62,30 @@ enum I32Col : int {
 // better than one record per particle (one line per lane).  Positions,
 // velocities and temperature are float-float pairs (hi = fl(v),
 // lo = fl(v - hi)): the difference of two pairs gives x_i - x_j to FP32
-// accuracy even when |x| >> |x_i - x_j|.
+// accuracy even when |x| >> |x_i - x_j|.  The six low halves of x and v
+// share one group as bf16 values (lo_pack in wf_step_common.cuh): |lo| is at
+// most half an FP32 ulp of hi, so 8 mantissa bits keep it to ~2^-9 of its
+// size, far below the FP32 rounding of the pair difference, and a gather
+// reads three groups per neighbour for x and v instead of four.
 enum RecCur : int {        // current-state groups
   RC_XH = 0,               // x hi (xyz), h
-  RC_XL = 1,               // x lo (xyz), mass
+  RC_L = 1,                // x lo, v lo (bf16 pairs), m/rho
   RC_VH = 2,               // v hi (xyz), rho
-  RC_VL = 3,               // v lo (xyz), m/rho
-  RC_S0 = 4,               // Sigma/rho^2 xx yy zz xy
-  RC_S1 = 5,               // Sigma/rho^2 xz yz, p/rho^2, Cs
-  RC_MISC = 6,             // alpha, beta, k_T, T hi
-  RC_T2 = 7,               // T lo
-  RC_TI0 = 8,              // TIR xx yy zz xy (tensile instability, when any TI > 0)
-  RC_TI1 = 9,              // TIR xz yz, TIn, TIInitDist
-  RC_N = 10
+  RC_S0 = 3,               // Sigma/rho^2 xx yy zz xy
+  RC_S1 = 4,               // Sigma/rho^2 xz yz, mass, Cs
+  RC_MISC = 5,             // alpha, beta, k_T, T hi
+  RC_T2 = 6,               // T lo
+  RC_TI0 = 7,              // TIR xx yy zz xy (tensile instability, when any TI > 0)
+  RC_TI1 = 8,              // TIR xz yz, TIn, TIInitDist
+  RC_N = 9
 };
 enum RecNext : int {       // next-step groups
-  RN_XH = 0, RN_XL = 1,    // as RC_XH / RC_XL at x(n+1)
-  RN_VH = 2, RN_VL = 3,    // v(n+1) hi/lo, p/rho^2 at rho(n+1) (the rate gather's kinetic term;
-                           // the current group carries rho there), m/rho(n+1)
-  RN_E = 4,                // p/rho^2 at rho(n+1), k_T, T(n+1) hi, T(n+1) lo
-  RN_N = 5
+  RN_XH = 0,               // x(n+1) hi, h
+  RN_L = 1,                // x(n+1) lo, v(n+1) lo (bf16 pairs), m/rho(n+1)
+  RN_VH = 2,               // v(n+1) hi, p/rho^2 at rho(n+1) (the rate gather's kinetic term;
+                           // the current group carries rho there)
+  RN_E = 3,                // p/rho^2 at rho(n+1), k_T, T(n+1) hi, T(n+1) lo
+  RN_N = 4
 };
 constexpr int NF32 = 4 * (RC_N + RN_N) + 9;  // floats per particle: records + 9 rate columns
 
@@ -197,6 +201,8 @@ struct DomainConst {
   double CFL, sqrt_h_a;      // their coefficients (Domain::CFL, Domain::sqrt_h_a)
   int av_uniform;      // 1 when every solid particle has the same Alpha and Beta
   float av_alpha, av_beta;  // those values (the mixed acceleration gather skips their loads)
+  int m_uniform;       // 1 when every solid particle has the same mass
+  float mass_f;        // that mass (the mixed rate gather's kinetic-energy term)
 };
 
 // Device pointers, passed by value to every kernel.

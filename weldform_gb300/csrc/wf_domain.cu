@@ -591,7 +591,7 @@ struct wf_domain {
     K.totmass_mean = tm / N;
     K.id_free_surf = -999999;
     K.leapfrog = integrator;
-    set_av_uniform(hp.f[C_ALPHA].data(), hp.f[C_BETA].data(), hp.i[I_KIND].data(), N);
+    set_uniform(hp.f[C_ALPHA].data(), hp.f[C_BETA].data(), hp.f[C_MASS].data(), hp.i[I_KIND].data(), N);
     K.gradcorr = grad_corr;
     if (auto_ts_cont && contact && integrator == 0)
       throw CudaError{WF_ERR_UNSUPPORTED, "auto_ts_cont with contact: the kick-drift solver reads Domain::min_force_ts, "
@@ -784,31 +784,36 @@ struct wf_domain {
   }
   // The plain form's per-entry GradKernel (P.gk) no longer matches the state.
   void invalidate_gk() { CK(cudaMemsetAsync(&P.st->gk_valid, 0, sizeof(int), stream)); }
-  // Whether Alpha and Beta are the same on every SPH particle: the gathers
-  // then take the pair's (a_i + a_j) / 2 = a from K instead of loading a_j.
-  void set_av_uniform(const double* a, const double* b, const int* kind, size_t n) {
+  // Whether Alpha and Beta, and the mass, are the same on every SPH particle:
+  // the gathers then take the pair's (a_i + a_j) / 2 = a, and m_j, from K
+  // instead of loading them.
+  void set_uniform(const double* a, const double* b, const double* m, const int* kind, size_t n) {
     K.av_uniform = 1;
+    K.m_uniform = 1;
     bool first = true;
-    double a0 = 0, b0 = 0;
+    double a0 = 0, b0 = 0, m0 = 0;
     for (size_t p = 0; p < n; ++p) {
       if (kind[p] != 0) continue;
-      if (first) { a0 = a[p]; b0 = b[p]; first = false; }
-      else if (a[p] != a0 || b[p] != b0) { K.av_uniform = 0; break; }
+      if (first) { a0 = a[p]; b0 = b[p]; m0 = m[p]; first = false; continue; }
+      if (a[p] != a0 || b[p] != b0) K.av_uniform = 0;
+      if (m[p] != m0) K.m_uniform = 0;
     }
     K.av_alpha = (float)a0;
     K.av_beta = (float)b0;
+    K.mass_f = (float)m0;
   }
-  // Alpha or Beta written after the prologue: re-evaluate the flag on the
-  // device columns (any order) and recapture the step with the new constants.
-  void refresh_av_uniform() {
+  // Alpha, Beta or mass written after the prologue: re-evaluate the flags on
+  // the device columns (any order) and recapture the step with the new constants.
+  void refresh_uniform() {
     size_t n = hp.N;
-    std::vector<double> a(n), b(n);
+    std::vector<double> a(n), b(n), m(n);
     std::vector<int> kind(n);
     CK(cudaMemcpyAsync(a.data(), d_f + (size_t)wf::C_ALPHA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(b.data(), d_f + (size_t)wf::C_BETA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(m.data(), d_f + (size_t)wf::C_MASS * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(kind.data(), d_i + (size_t)wf::I_KIND * n, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    set_av_uniform(a.data(), b.data(), kind.data(), n);
+    set_uniform(a.data(), b.data(), m.data(), kind.data(), n);
     if (graph) { CK(cudaGraphExecDestroy(graph)); graph = nullptr; }
   }
   void checkpoint_save(int slot) {
@@ -1135,7 +1140,7 @@ struct wf_domain {
     shadows_valid = false;
     invalidate_gk();
     CK(cudaStreamSynchronize(stream));
-    if (c == wf::C_ALPHA || c == wf::C_BETA) refresh_av_uniform();
+    if (c == wf::C_ALPHA || c == wf::C_BETA || c == wf::C_MASS) refresh_uniform();
   }
   void get_i32(int c, int* dst) {
     size_t n = hp.N;

@@ -1,5 +1,7 @@
 // Device helpers shared by the plain and mixed step kernels.
 #pragma once
+#include <cuda_bf16.h>
+
 #include "wf_device.cuh"
 
 namespace wf {
@@ -44,24 +46,46 @@ __device__ __forceinline__ float* rc_f(const DevPtrs& P, size_t N, int i, int q)
 __device__ __forceinline__ float* rn_f(const DevPtrs& P, size_t N, int i, int q) {
   return reinterpret_cast<float*>(P.rn + (size_t)q * N + i);
 }
+// Low-half group: x = (xlo0, xlo1), y = (xlo2, vlo0), z = (vlo1, vlo2) as bf16
+// pairs (first value in the low 16 bits), w = a float.  A bf16 is the upper
+// half of an FP32, so unpacking is a shift or a mask.
+__device__ __forceinline__ unsigned short bf16_bits(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
+__device__ __forceinline__ float bf16_pair(float a, float b) {
+  return __uint_as_float((unsigned)bf16_bits(a) | ((unsigned)bf16_bits(b) << 16));
+}
+__device__ __forceinline__ float bf16_first(float p) { return __uint_as_float(__float_as_uint(p) << 16); }
+__device__ __forceinline__ float bf16_second(float p) { return __uint_as_float(__float_as_uint(p) & 0xffff0000u); }
+__device__ __forceinline__ float4 lo_pack(const float xl[3], const float vl[3], float w) {
+  return make_float4(bf16_pair(xl[0], xl[1]), bf16_pair(xl[2], vl[0]), bf16_pair(vl[1], vl[2]), w);
+}
+__device__ __forceinline__ void lo_unpack(float4 g, float xl[3], float vl[3]) {
+  xl[0] = bf16_first(g.x); xl[1] = bf16_second(g.x); xl[2] = bf16_first(g.y);
+  vl[0] = bf16_second(g.y); vl[1] = bf16_first(g.z); vl[2] = bf16_second(g.z);
+}
+// v lo component d sits in 16-bit half 3 + d of the group.
+__device__ __forceinline__ unsigned short* lo_v_half(float4* group, int d) {
+  return reinterpret_cast<unsigned short*>(group) + 3 + d;
+}
+
 // Velocity component d of particle i into the current (next) float4 groups.
 __device__ __forceinline__ void rec_set_v(const DevPtrs& P, size_t N, int i, int d, double v, bool next) {
   float h, l;
   ff_split(v, h, l);
-  if (next) { rn_f(P, N, i, RN_VH)[d] = h; rn_f(P, N, i, RN_VL)[d] = l; }
-  else { rc_f(P, N, i, RC_VH)[d] = h; rc_f(P, N, i, RC_VL)[d] = l; }
+  if (next) { rn_f(P, N, i, RN_VH)[d] = h; *lo_v_half(P.rn + (size_t)RN_L * N + i, d) = bf16_bits(l); }
+  else { rc_f(P, N, i, RC_VH)[d] = h; *lo_v_half(P.rc + (size_t)RC_L * N + i, d) = bf16_bits(l); }
 }
 
-// The current velocity record of particle i from its three FP64 components,
-// written as whole 16-byte groups (the .w fields carried over).
+// The current velocity record of particle i from its three FP64 components
+// (the .w field and the x lo halves carried over).
 __device__ __forceinline__ void rec_set_v3(const DevPtrs& P, size_t N, int i, const double v[3]) {
   float4* r = P.rc + i;
-  float4 h = r[(size_t)RC_VH * N], l = r[(size_t)RC_VL * N];
-  ff_split(v[0], h.x, l.x);
-  ff_split(v[1], h.y, l.y);
-  ff_split(v[2], h.z, l.z);
+  float4 h = r[(size_t)RC_VH * N];
+  float l[3];
+  ff_split(v[0], h.x, l[0]);
+  ff_split(v[1], h.y, l[1]);
+  ff_split(v[2], h.z, l[2]);
   r[(size_t)RC_VH * N] = h;
-  r[(size_t)RC_VL * N] = l;
+  for (int d = 0; d < 3; ++d) *lo_v_half(r + (size_t)RC_L * N, d) = bf16_bits(l[d]);
 }
 
 // Amplitude lookup (SPH::amplitude::getValAtTime, Source/Domain.h:69-89).

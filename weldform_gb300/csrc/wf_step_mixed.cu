@@ -100,13 +100,12 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
   ff_split(col(P, C_T, N, i), th, tl);
   float4* r = P.rc + i;
   r[(size_t)RC_XH * N] = make_float4(xh[0], xh[1], xh[2], (float)col(P, C_H, N, i));
-  r[(size_t)RC_XL * N] = make_float4(xl[0], xl[1], xl[2], (float)col(P, C_MASS, N, i));
+  r[(size_t)RC_L * N] = lo_pack(xl, vl, solid ? (float)(col(P, C_MASS, N, i) / rho) : 0.f);
   r[(size_t)RC_VH * N] = make_float4(vh[0], vh[1], vh[2], (float)rho);
-  r[(size_t)RC_VL * N] = make_float4(vl[0], vl[1], vl[2], solid ? (float)(col(P, C_MASS, N, i) / rho) : 0.f);
   r[(size_t)RC_S0 * N] = make_float4((float)(c2 * col(P, C_SIG, N, i)), (float)(c2 * col(P, C_SIG + 1, N, i)),
                          (float)(c2 * col(P, C_SIG + 2, N, i)), (float)(c2 * col(P, C_SIG + 3, N, i)));
   r[(size_t)RC_S1 * N] = make_float4((float)(c2 * col(P, C_SIG + 4, N, i)), (float)(c2 * col(P, C_SIG + 5, N, i)),
-                         (float)(c2 * col(P, C_P, N, i)), (float)col(P, C_CS, N, i));
+                         (float)col(P, C_MASS, N, i), (float)col(P, C_CS, N, i));
   r[(size_t)RC_MISC * N] = make_float4((float)col(P, C_ALPHA, N, i), (float)col(P, C_BETA, N, i), (float)col(P, C_KT, N, i), th);
   r[(size_t)RC_T2 * N] = make_float4(tl, 0.f, 0.f, 0.f);
   }
@@ -124,7 +123,9 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
     return;
   }
   const float4* ri = P.rc + i;
-  float4 xh = ld4(ri + (size_t)RC_XH * N), xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
+  float4 xh = ld4(ri + (size_t)RC_XH * N), lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
+  float xl[3], vl[3];
+  lo_unpack(lo, xl, vl);
   float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1 = ld4(ri + (size_t)RC_S1 * N);
   float4 mi = AVU ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(ri + (size_t)RC_MISC * N);
   float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
@@ -138,10 +139,12 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   for (int k = 0; k < len; ++k) {
     int j = nb_index(nb[(size_t)k * N]);
     const float4* rj = P.rc + j;
-    float4 jxh = ld4(rj + (size_t)RC_XH * N), jxl = ld4(rj + (size_t)RC_XL * N), jvh = ld4(rj + (size_t)RC_VH * N), jvl = ld4(rj + (size_t)RC_VL * N);
+    float4 jxh = ld4(rj + (size_t)RC_XH * N), jlo = ld4(rj + (size_t)RC_L * N), jvh = ld4(rj + (size_t)RC_VH * N);
     float4 js0 = ld4(rj + (size_t)RC_S0 * N), js1 = ld4(rj + (size_t)RC_S1 * N);
-    float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
-    float v0 = (vh.x - jvh.x) + (vl.x - jvl.x), v1 = (vh.y - jvh.y) + (vl.y - jvl.y), v2 = (vh.z - jvh.z) + (vl.z - jvl.z);
+    float jxl[3], jvl[3];
+    lo_unpack(jlo, jxl, jvl);
+    float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
+    float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
     float hh = 0.5f * (xh.w + jxh.w);
     float r2 = x0 * x0 + x1 * x1 + x2 * x2, r;
     float GK = grad_kernel_f(r2, hh, &r);
@@ -177,7 +180,7 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
     }
     float g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
     if (GC) corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
-    float mj = jxl.w;
+    float mj = js1.z;
     a0.add(mj * (g0 * S0 + g1 * S3 + g2 * S4));
     a1.add(mj * (g0 * S3 + g1 * S1 + g2 * S5));
     a2.add(mj * (g0 * S4 + g1 * S5 + g2 * S2));
@@ -202,7 +205,9 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   const float4* ri = P.rc + i;
   float4 xh = ld4(ri + (size_t)RC_XH * N);
   if (solid) {
-    float4 xl = ld4(ri + (size_t)RC_XL * N), vh = ld4(ri + (size_t)RC_VH * N), vl = ld4(ri + (size_t)RC_VL * N);
+    float4 lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
+    float xl[3], vl[3];
+    lo_unpack(lo, xl, vl);
     CorrM cm;
     if (GC) cm = load_corr(P, N, i);
     float rhoif = (float)rhoi;
@@ -212,17 +217,19 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
     for (int k = 0; k < len; ++k) {
       int j = nb_index(nb[(size_t)k * N]);
       const float4* rj = P.rc + j;
-      float4 jxh = ld4(rj + (size_t)RC_XH * N), jxl = ld4(rj + (size_t)RC_XL * N), jvh = ld4(rj + (size_t)RC_VH * N), jvl = ld4(rj + (size_t)RC_VL * N);
-      float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
-      float v0 = (vh.x - jvh.x) + (vl.x - jvl.x), v1 = (vh.y - jvh.y) + (vl.y - jvl.y), v2 = (vh.z - jvh.z) + (vl.z - jvl.z);
+      float4 jxh = ld4(rj + (size_t)RC_XH * N), jlo = ld4(rj + (size_t)RC_L * N), jvh = ld4(rj + (size_t)RC_VH * N);
+      float jxl[3], jvl[3];
+      lo_unpack(jlo, jxl, jvl);
+      float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
+      float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
       float r;
       float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
       if (GC) {
         float g0, g1, g2;
         corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
-        s.add(jxl.w * (rhoif / jvh.w) * (v0 * g0 + v1 * g1 + v2 * g2));
+        s.add(jlo.w * rhoif * (v0 * g0 + v1 * g1 + v2 * g2));  // m_j (rho_i / rho_j) = (m_j / rho_j) rho_i
       } else {
-        s.add(jvl.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
+        s.add(jlo.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
       }
     }
     dd = GC ? s.value() : s.value() * rhoi;
@@ -254,10 +261,9 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   ff_split(Tn, th, tl);
   float4* r = P.rn + i;
   r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], xh.w);
-  r[(size_t)RN_XL * N] = make_float4(nxl[0], nxl[1], nxl[2], (float)col(P, C_MASS, N, i));
+  r[(size_t)RN_L * N] = lo_pack(nxl, nvl, (float)mrn);
   float pr2 = solid ? (float)(pn / (rn * rn)) : 0.f;
   r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], pr2);  // the rate gather reads p/rho^2 here
-  r[(size_t)RN_VL * N] = make_float4(nvl[0], nvl[1], nvl[2], (float)mrn);
   r[(size_t)RN_E * N] = make_float4(pr2, ri[(size_t)RC_MISC * N].z, th, tl);
 }
 template <bool GC>
@@ -278,7 +284,9 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
   double dkin = 0.0, cond = 0.0;
   if (icol(P, I_KIND, N, i) == 0) {
     const float4* ri = P.rn + i;
-    float4 xh = ld4(ri + (size_t)RN_XH * N), xl = ld4(ri + (size_t)RN_XL * N), vh = ld4(ri + (size_t)RN_VH * N), vl = ld4(ri + (size_t)RN_VL * N);
+    float4 xh = ld4(ri + (size_t)RN_XH * N), lo = ld4(ri + (size_t)RN_L * N), vh = ld4(ri + (size_t)RN_VH * N);
+    float xl[3], vl[3];
+    lo_unpack(lo, xl, vl);
     float4 e = THERMAL ? ld4(ri + (size_t)RN_E * N) : make_float4(vh.w, 0.f, 0.f, 0.f);
     CorrM cm;
     if (GC) cm = load_corr(P, N, i);
@@ -290,18 +298,20 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       int ent = nb[(size_t)k * N];
       int j = nb_index(ent);
       const float4* rj = P.rn + j;
-      float4 jxh = ld4(rj + (size_t)RN_XH * N), jxl = ld4(rj + (size_t)RN_XL * N), jvh = ld4(rj + (size_t)RN_VH * N), jvl = ld4(rj + (size_t)RN_VL * N);
+      float4 jxh = ld4(rj + (size_t)RN_XH * N), jlo = ld4(rj + (size_t)RN_L * N), jvh = ld4(rj + (size_t)RN_VH * N);
+      float jxl[3], jvl[3];
+      lo_unpack(jlo, jxl, jvl);
       // p/rho^2 rides in the velocity group; conduction needs the E group (k_T, T)
       float4 je = THERMAL ? ld4(rj + (size_t)RN_E * N) : make_float4(jvh.w, 0.f, 0.f, 0.f);
-      float x0 = (xh.x - jxh.x) + (xl.x - jxl.x), x1 = (xh.y - jxh.y) + (xl.y - jxl.y), x2 = (xh.z - jxh.z) + (xl.z - jxl.z);
-      float b0 = (vh.x - jvh.x) + (vl.x - jvl.x), b1 = (vh.y - jvh.y) + (vl.y - jvl.y), b2 = (vh.z - jvh.z) + (vl.z - jvl.z);
+      float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
+      float b0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), b1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), b2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
       float r;
       float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
       float y0 = x0, y1 = x1, y2 = x2;
-      float w = jvl.w * (-0.5f * GK);
+      float w = jlo.w * (-0.5f * GK);
       if (GC) {  // -1/2 (float)(m_j/rho_j) (v_ij (x) gk), gk = M_i GK x_ij
         corr_gk(cm, GK, x0, x1, x2, y0, y1, y2);
-        w = jvl.w * -0.5f;
+        w = jlo.w * -0.5f;
       }
       float wb0 = w * b0, wb1 = w * b1, wb2 = w * b2;
       M[0].add(wb0 * y0); M[1].add(wb0 * y1); M[2].add(wb0 * y2);
@@ -309,10 +319,12 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       M[6].add(wb2 * y0); M[7].add(wb2 * y1); M[8].add(wb2 * y2);
       bool up = nb_up(ent);  // original index of j larger than i's
       float dv = GK * (b0 * x0 + b1 * x1 + b2 * x2);
-      float pk = 0.5f * (up ? jxl.w : xl.w) * (e.x + je.x) * dv;
+      // m_P2 of the pair: the domain's one mass when uniform, else the column
+      float mP2 = K.m_uniform ? K.mass_f : (float)col(P, C_MASS, N, up ? j : i);
+      float pk = 0.5f * mP2 * (e.x + je.x) * dv;
       kin.add(up ? pk : -pk);
       if (THERMAL) {
-        float wt = up ? jvl.w : vl.w;  // m_P2 / rho_P2 for both ends of the pair
+        float wt = up ? jlo.w : lo.w;  // m_P2 / rho_P2 for both ends of the pair
         float dT = (e.z - je.z) + (e.w - je.w);
         // x.(GK x)/r^2 = GK; with the correction x.gk/r^2 (Thermal.cpp:90-107)
         float gr = GC ? (x0 * y0 + x1 * y1 + x2 * y2) / (x0 * x0 + x1 * x1 + x2 * x2) : GK;
@@ -432,11 +444,10 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
     const float4* rn = P.rn + i;
     float4* rc = P.rc + i;
     rc[(size_t)RC_XH * N] = rn[(size_t)RN_XH * N];
-    rc[(size_t)RC_XL * N] = rn[(size_t)RN_XL * N];
+    rc[(size_t)RC_L * N] = rn[(size_t)RN_L * N];
     float4 nvh = rn[(size_t)RN_VH * N];
     nvh.w = (float)rho;  // the current group carries rho (the acceleration gather's viscosity)
     rc[(size_t)RC_VH * N] = nvh;
-    rc[(size_t)RC_VL * N] = rn[(size_t)RN_VL * N];
     float4 ne = rn[(size_t)RN_E * N];
     float4 misc = rc[(size_t)RC_MISC * N];
     maxpl = col(P, C_PLS, N, i);
@@ -508,9 +519,9 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
                                      s.tau[1] * srd[1] + 2.0 * s.tau[5] * srd[5] + s.tau[2] * srd[2]);
       colw(P, C_DINT, N, i) = dint;
       float c2 = 1.0f / ((float)rho * (float)rho);
-      float s1w = rc[(size_t)RC_S1 * N].w;
+      float4 s1o = rc[(size_t)RC_S1 * N];  // mass and Cs carried over
       rc[(size_t)RC_S0 * N] = make_float4(c2 * (float)s.sig[0], c2 * (float)s.sig[1], c2 * (float)s.sig[2], c2 * (float)s.sig[3]);
-      rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], c2 * (float)s.pressure, s1w);
+      rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], s1o.z, s1o.w);
     }
     rc[(size_t)RC_MISC * N] = make_float4(misc.x, misc.y, misc.z, ne.z);
     rc[(size_t)RC_T2 * N] = make_float4(ne.w, 0.f, 0.f, 0.f);
