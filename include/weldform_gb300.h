@@ -94,8 +94,15 @@ int wf_domain_destroy(wf_domain* d);
  * "precision" (WF_PRECISION_*), "device" (CUDA device ordinal, before the
  * prologue), "use_graph" (replay each step as one CUDA graph, default 1),
  * "gather_block" (threads per block of the mixed form's gathers: 64, 128,
- * 256 or 512), "cpu_threads" (unused on the GPU path).  Read back with
- * wf_get_domain_i32: "gather_block". */
+ * 256 or 512), "gather_staging" (1: the mixed acceleration gather reads each
+ * 128-particle block's neighbours from a shared-memory copy of their records,
+ * built at every search; set before the prologue, default 0) and
+ * "stage_cap" (its halo capacity per block, 64..1024, default 896, before
+ * the prologue), "freeze_neighbours" (1: neighbour rows, contact pairs and
+ * surface flags come from the first step's search only, for finite-difference
+ * checks of the adjoint; no reference counterpart), "cpu_threads" (unused on
+ * the GPU path).  Read back with wf_get_domain_i32: "gather_block",
+ * "gather_staging", "stage_cap". */
 int wf_set_domain_f64(wf_domain* d, const char* name, double value);
 int wf_set_domain_i32(wf_domain* d, const char* name, int value);
 /* Read-back of scalars: "Time", "deltat", "hmax", "int_energy_sum",

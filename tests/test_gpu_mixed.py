@@ -149,3 +149,32 @@ def test_mixed_adaptive_time_step():
     _check(m, o, f)
     assert abs(m["deltat"] - o["deltat"]) <= TOL * o["deltat"]
     assert abs(m["Time"] - o["Time"]) <= TOL * o["Time"]
+
+
+def test_mixed_staged_acceleration_gather():
+    """The shared-memory staged acceleration gather (two threads per
+    particle, even and odd row entries, sums added in FP64) on a yielding
+    JC + thermal + contact run with several searches, each rebuilding the
+    block halos: bit-identical for every halo capacity (a block over the
+    capacity runs the same split on global memory), and within FP32
+    summation-order differences of the one-thread gather."""
+    res = []
+    for stage, cap in ((0, 896), (1, 896), (1, 400), (1, 64)):
+        d = gpu_domain()
+        d.set("precision", PRECISION_MIXED)
+        d.set("gather_staging", stage)
+        d.set("stage_cap", cap)
+        case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, gap=0.0)
+        d.prepare(case.dt)
+        assert d.geti("gather_staging") == stage and d.geti("stage_cap") == cap
+        d.step(60)
+        assert d.geti("nb_searches") > 1
+        names = d.profile_steps(2)
+        assert ("k_accel_mx_staged" in names) == bool(stage), names
+        res.append({f: d.get_array(f) for f in ("Displacement", "v", "Sigma", "pl_strain", "T")})
+        d.close()
+    for r in res[2:]:
+        for f in r:
+            assert np.array_equal(r[f], res[1][f]), f
+    for f in res[0]:
+        assert rel_l2(res[1][f], res[0][f]) <= 1e-5, f

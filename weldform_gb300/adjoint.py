@@ -20,11 +20,19 @@ PFAC = 0.1 E / h of the penalty-contact workload).
 u * scale) for checking with ``torch.autograd.gradcheck``.
 
     python -m weldform_gb300.adjoint [--dx-mm 0.55] [--steps 400] [--every 10]
-        [--v-punch -20] [--k 10,20,50] [--fd]
+        [--v-punch -20] [--k 10,20,50] [--fd] [--stencil E,A] [--stencil-points 8]
+        [--scan E] [--freeze-topology]
 
 prints one JSON line: loss, adjoint gradient for every k, the wall time of a
 plain forward run and of the adjoint (forward with checkpoints, reverse
-sweep), and with --fd the central finite differences (relative step 1e-6).
+sweep), with --fd the central finite differences (relative step 1e-6), and
+with --stencil the central differences of the named parameters beside the
+mean of the adjoint derivative over the same stencil, and with --scan the loss
+at 21 points across relative offsets [-1e-5, 1e-5] of one parameter with its
+residual from the adjoint's linear model.  --freeze-topology runs every
+forward pass with the neighbour rows, contact pairs and surface flags of the
+first step's search (the topology the adjoint holds fixed within each step is
+then also fixed across steps), so finite differences see no search decision.
 """
 from __future__ import annotations
 
@@ -58,6 +66,8 @@ class ContactCase:
     jitter_amp: float = 1e-3
     seed: int = SEED
     cfl: float = 0.4
+    freeze: bool = False  # topology searched only at the first step (library option "freeze_neighbours")
+    alpha: float = 1.0    # Monaghan viscosity Alpha of every particle
 
     @property
     def h(self) -> float:
@@ -109,7 +119,7 @@ def build(dom, case: ContactCase, theta) -> int:
     dom.set_particles("G", E / (2. * (1. + mat.nu)))
     dom.set_particles("Cs", math.sqrt(E / (3. * (1. - 2 * mat.nu)) / mat.rho))
     dom.set_particles("Fail", 1)
-    dom.set_particles("Alpha", 1.0)
+    dom.set_particles("Alpha", case.alpha)
     dom.set_particles("Beta", 0.0)
     dom.set_particles("k_T", mat.k_T)
     dom.set_particles("cp_T", mat.cp_T)
@@ -131,6 +141,8 @@ def build(dom, case: ContactCase, theta) -> int:
     if case.thermal:
         dom.set("thermal_solver", 1)
         dom.set("pl_heating", 1)
+    if case.freeze:
+        dom.set("freeze_neighbours", 1)
     return mesh
 
 
@@ -239,6 +251,27 @@ def central_fd(problem: Problem, rel: float = 1e-6) -> np.ndarray:
     return g
 
 
+def stencil_mean_adjoint(problem: Problem, p: int, rel: float = 1e-6, points: int = 8) -> float:
+    """Mean of the adjoint derivative dL/du_p over the central-difference
+    stencil of ``central_fd`` at the same relative step (midpoint rule over
+    ``points`` nodes).
+
+    The step is piecewise smooth in every parameter: each particle's
+    elastic-plastic transition and each pair's viscosity switch is a kink.
+    For a loss that is continuous and piecewise smooth in u_p,
+    (L(+s) - L(-s)) / (2 s) is exactly the mean of dL/du_p over [-s, +s];
+    a kink inside the stencil separates the central difference from the
+    derivative at the centre, not from this mean.  Comparing the two checks
+    the adjoint against finite differences without the kink error."""
+    step = rel * abs(problem.theta0[p]) / problem.scl[p]
+    acc = 0.0
+    for k in range(points):
+        du = np.zeros(len(PARAMS))
+        du[p] = -step + (2 * k + 1) * step / points
+        acc += problem.loss_grad(du)[1][p]
+    return acc / points
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--dx-mm", type=float, default=0.55)
@@ -247,8 +280,23 @@ def main():
     ap.add_argument("--v-punch", type=float, default=-20.0)
     ap.add_argument("--k", default="10,20,50")
     ap.add_argument("--fd", action="store_true")
+    ap.add_argument("--jc-n", type=float, default=None, help="Johnson-Cook hardening exponent of the workload")
+    ap.add_argument("--alpha", type=float, default=1.0, help="artificial viscosity Alpha of the workload")
+    ap.add_argument("--friction", type=float, default=0.2, help="friction coefficient of the workload")
+    ap.add_argument("--freeze-topology", action="store_true",
+                    help="search neighbours and contact pairs only at the first step, for every run")
+    ap.add_argument("--stencil", default="", help="parameters (e.g. E,A) whose stencil-mean adjoint is "
+                    "compared with central differences at relative steps 1e-5 and 1e-6")
+    ap.add_argument("--stencil-points", type=int, default=8)
+    ap.add_argument("--scan", default="", help="parameter (e.g. E) whose loss is sampled at 21 points across "
+                    "relative offsets [-1e-5, 1e-5], with the residual from the adjoint's linear model")
     a = ap.parse_args()
-    case = ContactCase(dx=a.dx_mm * 1e-3, v_punch=a.v_punch)
+    case = ContactCase(dx=a.dx_mm * 1e-3, v_punch=a.v_punch, freeze=a.freeze_topology, alpha=a.alpha,
+                       friction=a.friction)
+    if a.jc_n is not None:
+        jc = list(case.mat.jc)
+        jc[2] = a.jc_n
+        case.mat = Steel(jc=tuple(jc))
     target = perturbed_jc_target(case, a.steps, a.every)
     th0 = case.nominal()
     # plain forward time of the same run (FP64 form, CUDA graph)
@@ -282,6 +330,34 @@ def main():
         out["adjoint_scaled"] = adj.tolist()
         big = np.abs(fd) > 1e-6 * np.abs(fd).max()
         out["fd_rel_err"] = [float(abs(adj[p] - fd[p]) / abs(fd[p])) if big[p] else None for p in range(len(PARAMS))]
+    if a.stencil:
+        prob = Problem(case, a.steps, a.every, target)
+        centre = prob.loss_grad(np.zeros(len(PARAMS)))[1]
+        st = {}
+        for name in a.stencil.split(","):
+            p = PARAMS.index(name)
+            for rel in (1e-5, 1e-6):
+                step = rel * abs(prob.theta0[p]) / prob.scl[p]
+                du = np.zeros(len(PARAMS))
+                du[p] = step
+                fd = (prob.loss(du) - prob.loss(-du)) / (2 * step)
+                mean = stencil_mean_adjoint(prob, p, rel, a.stencil_points)
+                st[f"{name}@{rel:g}"] = {"fd": fd, "adjoint_centre": float(centre[p]), "adjoint_stencil_mean": mean,
+                                         "centre_rel_err": abs(centre[p] - fd) / abs(fd),
+                                         "stencil_rel_err": abs(mean - fd) / abs(fd)}
+        out["stencil"] = st
+    if a.scan:
+        prob = Problem(case, a.steps, a.every, target)
+        p = PARAMS.index(a.scan)
+        l0, g0 = prob.loss_grad(np.zeros(len(PARAMS)))
+        pts = []
+        for k in range(-10, 11):
+            rel = k * 1e-6
+            du = np.zeros(len(PARAMS))
+            du[p] = rel * abs(prob.theta0[p]) / prob.scl[p]
+            lk = prob.loss(du)
+            pts.append({"rel": rel, "loss": lk, "residual": lk - l0 - g0[p] * du[p]})
+        out["scan"] = {"param": a.scan, "loss0": l0, "adjoint": float(g0[p]), "points": pts}
     print(json.dumps(out))
 
 

@@ -113,6 +113,16 @@ constexpr int MAX_NB = 100;  // MAX_NB_PER_PART, Source/Domain.h:49
 
 constexpr int MAX_CP = 64;   // contact pairs per particle
 
+// Shared-memory staging of the mixed form's gathers.  Particles are taken in
+// blocks of STAGE_B consecutive (cell-sorted) particles; at every search each
+// block's distinct neighbours are listed once, sorted by index (its halo,
+// at most stage_cap of them), and every row entry gets its neighbour's slot
+// in that list.  A staged gather copies the halo's float4 groups into shared
+// memory once per block and reads neighbours from there.
+constexpr int STAGE_B = 128;         // particles (threads) per staged block
+constexpr int STAGE_HASH = 4096;     // shared-memory hash set of the halo build
+constexpr int STAGE_CAP_MAX = 1024;  // largest halo a block can stage
+
 // Neighbour-row entries: the neighbour's index, bit 31 set when its original
 // index is larger than the row particle's (the P2 side of the reference's
 // (min, max) pair).  Rows are in the reference's canonical order (j > i
@@ -203,6 +213,8 @@ struct DomainConst {
   float av_alpha, av_beta;  // those values (the mixed acceleration gather skips their loads)
   int m_uniform;       // 1 when every solid particle has the same mass
   float mass_f;        // that mass (the mixed rate gather's kinetic-energy term)
+  int stage_cap;       // halo capacity of the staged gathers (0: staging off)
+  int freeze_nb;       // 1: neighbour and contact topology searched only at the first step
 };
 
 // Device pointers, passed by value to every kernel.
@@ -242,6 +254,9 @@ struct DevPtrs {
   int* elem_particle;     // nelem -> sorted particle index
   const int* node_mesh;   // nnodes
   int nnodes, nelem;
+  int* halo;              // staged gathers: each STAGE_B block's neighbours, sorted (stage_cap per block)
+  int* halo_len;          // per block: halo size, -1 when above stage_cap (that block reads global memory)
+  unsigned short* nslot;  // ELL like nbr: the entry's slot in its block's halo
   double* partials;       // NSLOTS * nblocks
   long long* scan_tmp;
   double* tx;             // step tape of the adjoint's recompute (TapeCol columns), null otherwise

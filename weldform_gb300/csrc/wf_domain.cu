@@ -124,6 +124,7 @@ struct wf_domain {
   double Cellfac = 2.0, pl_work_heat_frac = 0.9, friction_sta = 0.0, friction_dyn = 0.0, PFAC = 0.0, DFAC = 0.0;
   double DomMax[3] = {-100000000000.0, -100000000000.0, -100000000000.0};
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
+  int freeze_nb = 0;  // search only at the first step (finite-difference checks of the adjoint)
   int ts_nb_inc = 5, pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1, contact_alg = 0;
   int precision = WF_PRECISION_FP64, use_graph = 1, device = 0;
   int integrator = 0;  // 0 kick-drift, 1 leapfrog
@@ -155,13 +156,19 @@ struct wf_domain {
   double CFL = 0.7, sqrt_h_a = 0.0025;
   int gblock = 0;    // mixed gathers' threads per block (0: chosen by particle count)
   int pblock = 0;    // per-particle kernels' threads per block (0: chosen by particle count)
+  // Shared-memory staging of the mixed acceleration gather: the halo lists
+  // are allocated at the prologue when it is on; stage_cap is each block's
+  // halo capacity (STAGE_B particles per block, 80 B of shared memory per slot).
+  bool stage = false;
+  int stage_cap = 896;
+  bool stage_ready = false;
   // Block sizes by particle count: below ~4 blocks of 256 per SM the per-particle
   // kernels (one thread per particle, FP64 or gather latency bound) leave SMs
   // idle, so smaller blocks spread the particles over every SM.
   static int auto_block(long long n) { return n < 78000 ? 64 : (n < 156000 ? 128 : 256); }
   int gblock_now() const { return gblock ? gblock : auto_block(hp.N); }
   int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
-  int graph_key() const { return gblock_now() * 1024 + pblock_now(); }
+  int graph_key() const { return (gblock_now() * 1024 + pblock_now()) * 2 + (stage_ready && stage ? 1 : 0); }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
@@ -480,6 +487,15 @@ struct wf_domain {
     P.row_split = dalloc<int>(n);
     P.nbr = dalloc<int>((size_t)MAX_NB * n);
     P.gk = dalloc<double>((size_t)MAX_NB * n);
+    size_t nsb = (n + STAGE_B - 1) / STAGE_B;
+    if (stage) {
+      CK((cudaError_t)configure_staging(stage_cap));
+      P.halo = dalloc<int>(nsb * stage_cap);
+      P.halo_len = dalloc<int>(nsb);
+      P.nslot = dalloc<unsigned short>((size_t)MAX_NB * n);
+      CK(cudaMemsetAsync(P.halo_len, 0, sizeof(int) * nsb, stream));
+      stage_ready = true;
+    }
     CK(cudaMemsetAsync(P.row_len, 0, sizeof(int) * n, stream));
     CK(cudaMemsetAsync(P.row_split, 0, sizeof(int) * n, stream));
     P.cp_len = dalloc<int>(n);
@@ -582,6 +598,7 @@ struct wf_domain {
     double R = Cellfac * hmin;
     double eps = 4.0 * std::sqrt(3.0) * std::ldexp(1.0, -23) * (2.0 * ext) / R + 20.0 * std::ldexp(1.0, -24);
     K.pre_eps = (float)(eps < 0.05 ? std::max(eps, 1e-5) : 2.0);
+    K.freeze_nb = freeze_nb;
     K.ts_nb_inc = ts_nb_inc; K.pl_heating = pl_heating; K.thermal_solver = thermal_solver; K.contact = contact;
     K.contact_mesh_auto_update = contact_mesh_auto_update; K.contact_alg = contact_alg;
     K.pl_work_heat_frac = pl_work_heat_frac; K.friction_sta = friction_sta; K.friction_dyn = friction_dyn;
@@ -620,6 +637,9 @@ struct wf_domain {
                {P.cp, contact ? sizeof(int) * MAX_CP * n : sizeof(int)}, {P.node, sizeof(double) * hnode.size()},
                {P.node_v, sizeof(double) * hnode.size()}, {P.elem_normal, sizeof(double) * hnorm.size()},
                {P.elem_pplane, sizeof(double) * hpp.size()}, {P.elem_particle, sizeof(int) * hep.size()}};
+    if (stage_ready)
+      regions.insert(regions.end(), {{P.halo, sizeof(int) * nsb * stage_cap}, {P.halo_len, sizeof(int) * nsb},
+                                     {P.nslot, sizeof(unsigned short) * MAX_NB * n}});
     launch_prologue(P, K, stream);
     // SolverKickDrift.cpp:72-96: with contact, a search + CalculateSurface(1)
     // before the loop; the first step searches again (ClearNbData).
@@ -662,6 +682,7 @@ struct wf_domain {
     k.gblock = gblock_now();
     k.pblock = pblock_now();
     k.nblocks = (int)((hp.N + k.pblock - 1) / k.pblock);
+    k.stage_cap = stage_ready && stage ? stage_cap : 0;
     return k;
   }
   void launch_one_step() {
@@ -1245,6 +1266,18 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     d->gblock = v;
     return WF_OK;
   }
+  if (n == "gather_staging") {  // shared-memory staged acceleration gather of the mixed form
+    if (d->prepared && v && !d->stage_ready)
+      return set_err(WF_ERR_STATE, "gather_staging must be set before the prologue (it allocates the halo lists)");
+    d->stage = v != 0;
+    return WF_OK;
+  }
+  if (n == "stage_cap") {
+    if (d->prepared) return set_err(WF_ERR_STATE, "stage_cap is fixed after the prologue");
+    if (v < 64 || v > wf::STAGE_CAP_MAX) return set_err(WF_ERR_ARG, "stage_cap must be in [64, 1024]");
+    d->stage_cap = v;
+    return WF_OK;
+  }
   if (n == "particle_block") {  // 0: by particle count
     if (v != 0 && v != 64 && v != 128 && v != 256) return set_err(WF_ERR_ARG, "particle_block must be 0, 64, 128 or 256");
     d->pblock = v;
@@ -1260,6 +1293,7 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   if (n == "cpu_threads" || n == "Nproc" || n == "cpu_mode") return WF_OK;
   if (d->prepared) return set_err(WF_ERR_STATE, "domain fields are fixed after the prologue");
   if (n == "ts_nb_inc") { if (v < 1) return set_err(WF_ERR_ARG, "ts_nb_inc >= 1"); d->ts_nb_inc = v; }
+  else if (n == "freeze_neighbours") d->freeze_nb = v != 0;
   else if (n == "pl_heating") d->pl_heating = v;
   else if (n == "thermal_solver") d->thermal_solver = v;
   else if (n == "contact") d->contact = v;
@@ -1320,6 +1354,8 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     if (n == "solid_part_count") { *v = d->solid_part_count; return WF_OK; }
     if (n == "gather_block") { *v = d->gblock_now(); return WF_OK; }
     if (n == "particle_block") { *v = d->pblock_now(); return WF_OK; }
+    if (n == "gather_staging") { *v = d->stage ? 1 : 0; return WF_OK; }
+    if (n == "stage_cap") { *v = d->stage_cap; return WF_OK; }
     if (n.size() == 8 && n.rfind("CellNo.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') { *v = d->CellNo[n[7] - 'x']; return WF_OK; }
     if (!d->prepared) { *v = 0; return WF_OK; }
     wf::StepState st = d->read_state();

@@ -28,6 +28,11 @@ inline void mark(cudaStream_t s, const char* name) {
 // StepState::do_search.
 void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch,
                              cudaStream_t s);
+// Halo lists and row slots of the staged mixed gathers (wf_step_mixed.cu),
+// after the rows are built; gated on the search flag like the search.
+void launch_halo_build(const DevPtrs& P, const DomainConst& K, cudaStream_t s);
+// Shared-memory limit of the staged gathers for a halo capacity (a cudaError_t).
+int configure_staging(int cap);
 // Forces the search on the next launch (solver prologue and explicit calls).
 void launch_force_search(const DevPtrs& P, cudaStream_t s);
 

@@ -545,6 +545,7 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
     k_nbr_fill<<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
   }
   mark(s, "k_nbr_fill");
+  if (P.halo) launch_halo_build(P, K, s);
   if (K.contact) {
     k_surface<<<grid(K.N), T, 0, s>>>(P, K);
     mark(s, "k_surface");

@@ -51,6 +51,10 @@ __global__ void k_schedule(DevPtrs P, DomainConst K) {
     search = 1;
     regular = 1;
   }
+  // Frozen topology (a library option for finite-difference checks of the
+  // adjoint, which differentiates each step with its topology fixed): after
+  // the first step's search the rows, contact pairs and surface flags stay.
+  if (K.freeze_nb && !s->isfirst) search = regular = 0;
   if (search) s->nb_cleared = 0;
   s->do_search = search;
   // CalcGradCorrMatrix: kick-drift at its first step (SolverKickDrift.cpp:189-191),

@@ -115,13 +115,37 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
 // AVU: every solid particle has the same (alpha, beta), so the pair mean is
 // the value itself and the gather reads neither particle's misc group.
 // GC: kernel-gradient correction (temp_c = Mult(vc_i, S), InteractionAlt.cpp:166-170).
-template <bool TI, bool AVU, bool GC>
-__device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K, int i) {
-  size_t N = K.N;
-  if (icol(P, I_KIND, N, i) != 0) {
-    colw(P, C_A, N, i) = 0.0; colw(P, C_A + 1, N, i) = 0.0; colw(P, C_A + 2, N, i) = 0.0;
-    return;
+// Where a gather reads its neighbours' float4 groups: global memory through
+// the row's indices, or a block's staged halo through the row's slots.
+struct GlobalFetch {
+  const float4* rc;
+  const int* nb;  // P.nbr + i
+  size_t N;
+  __device__ __forceinline__ int get(int k, float4& xh, float4& lo, float4& vh, float4& s0, float4& s1) const {
+    int j = nb_index(nb[(size_t)k * N]);
+    const float4* rj = rc + j;
+    xh = ld4(rj + (size_t)RC_XH * N); lo = ld4(rj + (size_t)RC_L * N); vh = ld4(rj + (size_t)RC_VH * N);
+    s0 = ld4(rj + (size_t)RC_S0 * N); s1 = ld4(rj + (size_t)RC_S1 * N);
+    return j;
   }
+};
+struct StagedFetch {
+  const float4* sh;            // 5 groups of cap records in shared memory
+  const unsigned short* slot;  // P.nslot + i
+  size_t N;
+  int cap;
+  __device__ __forceinline__ int get(int k, float4& xh, float4& lo, float4& vh, float4& s0, float4& s1) const {
+    int q = slot[(size_t)k * N];
+    xh = sh[q]; lo = sh[cap + q]; vh = sh[2 * cap + q]; s0 = sh[3 * cap + q]; s1 = sh[4 * cap + q];
+    return -1;  // the global index is not known here: no misc or TI group (AVU and !TI only)
+  }
+};
+
+// Pair sums of the acceleration of SPH particle i over row entries k0, k0 + dk, ...
+template <bool TI, bool AVU, bool GC, class Fetch>
+__device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainConst& K, int i, const Fetch& F, int k0,
+                                              int dk, KSum& a0, KSum& a1, KSum& a2) {
+  size_t N = K.N;
   const float4* ri = P.rc + i;
   float4 xh = ld4(ri + (size_t)RC_XH * N), lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
   float xl[3], vl[3];
@@ -133,14 +157,11 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
   if (TI) { t0 = ld4(ri + (size_t)RC_TI0 * N); t1 = ld4(ri + (size_t)RC_TI1 * N); tii = (float)col(P, C_TI, N, i); }
   CorrM cm;
   if (GC) cm = load_corr(P, N, i);
-  KSum a0, a1, a2;
   int len = P.row_len[i];
-  const int* nb = P.nbr + i;
-  for (int k = 0; k < len; ++k) {
-    int j = nb_index(nb[(size_t)k * N]);
+  for (int k = k0; k < len; k += dk) {
+    float4 jxh, jlo, jvh, js0, js1;
+    int j = F.get(k, jxh, jlo, jvh, js0, js1);
     const float4* rj = P.rc + j;
-    float4 jxh = ld4(rj + (size_t)RC_XH * N), jlo = ld4(rj + (size_t)RC_L * N), jvh = ld4(rj + (size_t)RC_VH * N);
-    float4 js0 = ld4(rj + (size_t)RC_S0 * N), js1 = ld4(rj + (size_t)RC_S1 * N);
     float jxl[3], jvl[3];
     lo_unpack(jlo, jxl, jvl);
     float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
@@ -185,11 +206,167 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
     a1.add(mj * (g0 * S3 + g1 * S1 + g2 * S5));
     a2.add(mj * (g0 * S4 + g1 * S5 + g2 * S2));
   }
+}
+template <bool TI, bool AVU, bool GC, class Fetch>
+__device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K, int i, const Fetch& F) {
+  size_t N = K.N;
+  if (icol(P, I_KIND, N, i) != 0) {
+    colw(P, C_A, N, i) = 0.0; colw(P, C_A + 1, N, i) = 0.0; colw(P, C_A + 2, N, i) = 0.0;
+    return;
+  }
+  KSum a0, a1, a2;
+  accel_mx_sums<TI, AVU, GC>(P, K, i, F, 0, 1, a0, a1, a2);
   colw(P, C_A, N, i) = a0.value(); colw(P, C_A + 1, N, i) = a1.value(); colw(P, C_A + 2, N, i) = a2.value();
 }
 template <bool TI, bool AVU, bool GC>
 __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { accel_mx<TI, AVU, GC>(P, K, i); });
+  run_rows(K, [&](int i) { accel_mx<TI, AVU, GC>(P, K, i, GlobalFetch{P.rc, P.nbr + i, (size_t)K.N}); });
+}
+
+// Staged acceleration gather (uniform viscosity constants, no tensile
+// instability, no gradient correction): block b copies its halo's five groups
+// into shared memory once, then two threads share each particle's row, which
+// doubles the warps per SM that the shared-memory footprint allows.  The
+// block's first STAGE_B threads sum the even row entries of its particles,
+// the other STAGE_B the odd ones, so a warp's lanes still read the same entry
+// k of consecutive particles (nearly consecutive slots, few bank conflicts);
+// each half is a Kahan sum and the two are added in FP64.  A block whose halo
+// exceeded the capacity (halo_len -1) reads global memory with the same split,
+// so results do not depend on the capacity.
+__global__ void __launch_bounds__(2 * STAGE_B) k_accel_mx_staged(DevPtrs P, DomainConst K) {
+  extern __shared__ float4 sh_rec[];
+  const int b = blockIdx.x, t = threadIdx.x, cap = K.stage_cap;
+  const size_t N = K.N;
+  const int H = P.halo_len[b];
+  if (H > 0) {
+    const int* hl = P.halo + (size_t)b * cap;
+    for (int s = t; s < H; s += 2 * STAGE_B) {
+      const float4* rj = P.rc + hl[s];
+      sh_rec[s] = ld4(rj + (size_t)RC_XH * N);
+      sh_rec[cap + s] = ld4(rj + (size_t)RC_L * N);
+      sh_rec[2 * cap + s] = ld4(rj + (size_t)RC_VH * N);
+      sh_rec[3 * cap + s] = ld4(rj + (size_t)RC_S0 * N);
+      sh_rec[4 * cap + s] = ld4(rj + (size_t)RC_S1 * N);
+    }
+  }
+  __syncthreads();
+  const int p = t % STAGE_B, part = t / STAGE_B;
+  const int i = b * STAGE_B + p;
+  const bool sph = i < K.N && icol(P, I_KIND, N, i) == 0;
+  KSum a0, a1, a2;
+  if (sph) {
+    if (H >= 0) accel_mx_sums<false, true, false>(P, K, i, StagedFetch{sh_rec, P.nslot + i, N, cap}, part, 2, a0, a1, a2);
+    else accel_mx_sums<false, true, false>(P, K, i, GlobalFetch{P.rc, P.nbr + i, N}, part, 2, a0, a1, a2);
+  }
+  double v0 = a0.value(), v1 = a1.value(), v2 = a2.value();
+  __syncthreads();  // halo records no longer read: the odd halves pass through shared memory
+  double* ex = reinterpret_cast<double*>(sh_rec);  // 3 * STAGE_B doubles (stage_cap >= 64)
+  if (part == 1) { ex[p] = v0; ex[STAGE_B + p] = v1; ex[2 * STAGE_B + p] = v2; }
+  __syncthreads();
+  if (part == 0 && i < K.N) {
+    colw(P, C_A, N, i) = sph ? v0 + ex[p] : 0.0;
+    colw(P, C_A + 1, N, i) = sph ? v1 + ex[STAGE_B + p] : 0.0;
+    colw(P, C_A + 2, N, i) = sph ? v2 + ex[2 * STAGE_B + p] : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------- halo build
+// After a search: for each block of STAGE_B consecutive particles, the
+// distinct neighbour indices of its rows (a shared-memory hash set with
+// bounded linear probing), compacted, sorted ascending (bitonic), stored as
+// the block's halo, and each row entry's slot in it (binary search).  A block
+// with more than stage_cap distinct neighbours is marked -1.  Gated on the
+// search flag; a fixed grid strides over the blocks.
+__global__ void __launch_bounds__(STAGE_B) k_halo_build(DevPtrs P, DomainConst K) {
+  if (!P.st->do_search) return;
+  __shared__ int tab[STAGE_HASH];
+  __shared__ int keys[STAGE_CAP_MAX];
+  __shared__ int s_cnt, s_over;
+  __shared__ int s_wsum[STAGE_B / 32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const size_t N = K.N;
+  const int cap = K.stage_cap;
+  const int nsb = (K.N + STAGE_B - 1) / STAGE_B;
+  constexpr int PER = STAGE_HASH / STAGE_B;
+  for (int b = blockIdx.x; b < nsb; b += gridDim.x) {
+    for (int s = t; s < STAGE_HASH; s += STAGE_B) tab[s] = -1;
+    if (t == 0) { s_cnt = 0; s_over = 0; }
+    __syncthreads();
+    const int i = b * STAGE_B + t;
+    const int len = i < K.N ? P.row_len[i] : 0;
+    for (int k = 0; k < len; ++k) {
+      int j = nb_index(P.nbr[(size_t)k * N + i]);
+      unsigned h = ((unsigned)j * 2654435761u) >> 20;  // 12-bit hash
+      int probe = 0;
+      for (; probe < STAGE_HASH; ++probe) {
+        int old = atomicCAS(&tab[h], -1, j);
+        if (old == -1) { atomicAdd(&s_cnt, 1); break; }
+        if (old == j) break;
+        h = (h + 1) & (STAGE_HASH - 1);
+      }
+      if (probe == STAGE_HASH) s_over = 1;
+    }
+    __syncthreads();
+    const int H = s_cnt;
+    if (s_over || H > cap) {
+      if (t == 0) P.halo_len[b] = -1;
+      __syncthreads();
+      continue;
+    }
+    // compaction: thread t owns hash slots [t * PER, (t + 1) * PER)
+    int c = 0;
+    for (int q = 0; q < PER; ++q) c += tab[t * PER + q] >= 0;
+    int x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_wsum[w] = x;
+    __syncthreads();
+    int pos = x - c;
+    for (int q = 0; q < w; ++q) pos += s_wsum[q];
+    for (int q = 0; q < PER; ++q) {
+      int v = tab[t * PER + q];
+      if (v >= 0) keys[pos++] = v;
+    }
+    int P2 = 1;
+    while (P2 < H) P2 <<= 1;
+    for (int q = H + t; q < P2; q += STAGE_B) keys[q] = 0x7fffffff;
+    __syncthreads();
+    for (int size = 2; size <= P2; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int e = t; e < P2 / 2; e += STAGE_B) {
+          int lo = 2 * e - (e & (stride - 1)), hi = lo + stride;
+          bool asc = (lo & size) == 0;
+          int a = keys[lo], bb = keys[hi];
+          if ((a > bb) == asc) { keys[lo] = bb; keys[hi] = a; }
+        }
+        __syncthreads();
+      }
+    for (int q = t; q < H; q += STAGE_B) P.halo[(size_t)b * cap + q] = keys[q];
+    if (t == 0) P.halo_len[b] = H;
+    for (int k = 0; k < len; ++k) {
+      int j = nb_index(P.nbr[(size_t)k * N + i]);
+      int lo = 0, hi = H - 1;
+      while (lo < hi) {
+        int m = (lo + hi) >> 1;
+        if (keys[m] < j) lo = m + 1; else hi = m;
+      }
+      P.nslot[(size_t)k * N + i] = (unsigned short)lo;
+    }
+    __syncthreads();
+  }
+}
+
+void launch_halo_build(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
+  int nsb = nblk(K.N, STAGE_B);
+  k_halo_build<<<nsb < 152 * 4 ? nsb : 152 * 4, STAGE_B, 0, s>>>(P, K);
+  mark(s, "k_halo_build");
+}
+
+int configure_staging(int cap) {
+  size_t bytes = (size_t)5 * cap * sizeof(float4);
+  return (int)cudaFuncSetAttribute(k_accel_mx_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 // ---------------------------------------------------------------- density + drift + kick
@@ -556,14 +733,17 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   launch_step_head(P, K, fscratch, iscratch, s);
   launch_refresh_shadows(P, K, 0, s);
   launch_tensile(P, K, s);
-  if (K.ti) {
+  const bool staged = K.stage_cap > 0 && P.halo && !K.ti && K.av_uniform && !K.gradcorr;
+  if (staged) {
+    k_accel_mx_staged<<<nblk(K.N, STAGE_B), 2 * STAGE_B, (size_t)5 * K.stage_cap * sizeof(float4), s>>>(P, K);
+  } else if (K.ti) {
     if (K.av_uniform) launch_accel_mx<true, true>(P, K, ng, gb, s);
     else launch_accel_mx<true, false>(P, K, ng, gb, s);
   } else {
     if (K.av_uniform) launch_accel_mx<false, true>(P, K, ng, gb, s);
     else launch_accel_mx<false, false>(P, K, ng, gb, s);
   }
-  mark(s, "k_accel_mx");
+  mark(s, staged ? "k_accel_mx_staged" : "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
