@@ -414,7 +414,8 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   colw(P, C_DRHO, N, i) = dd;
   double rn = rhoi + dt * dd;
   colw(P, C_RHON, N, i) = rn;
-  double mrn = solid ? col(P, C_MASS, N, i) / rn : 0.0;
+  const double irn = 1.0 / rn;  // one FP64 division for m/rho and p/rho^2
+  double mrn = solid ? col(P, C_MASS, N, i) * irn : 0.0;
   colw(P, C_MRHON, N, i) = mrn;
   float nxh[3], nxl[3], nvh[3], nvl[3];
   for (int d = 0; d < 3; ++d) {
@@ -439,7 +440,7 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   float4* r = P.rn + i;
   r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], xh.w);
   r[(size_t)RN_L * N] = lo_pack(nxl, nvl, (float)mrn);
-  float pr2 = solid ? (float)(pn / (rn * rn)) : 0.f;
+  float pr2 = solid ? (float)(pn * irn * irn) : 0.f;
   r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], pr2);  // the rate gather reads p/rho^2 here
   r[(size_t)RN_E * N] = make_float4(pr2, ri[(size_t)RC_MISC * N].z, th, tl);
 }
@@ -508,11 +509,13 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
         cnd.add(wt * 4.f * (e.y * je.y) / (e.y + je.y) * dT * gr);
       }
     }
-    double m[9];
-    for (int c = 0; c < 9; ++c) m[c] = M[c].value();
-    out[0] = (float)(2.0 * m[0]); out[1] = (float)(2.0 * m[4]); out[2] = (float)(2.0 * m[8]);
-    out[3] = (float)(m[1] + m[3]); out[4] = (float)(m[2] + m[6]); out[5] = (float)(m[5] + m[7]);
-    out[6] = (float)(m[1] - m[3]); out[7] = (float)(m[2] - m[6]); out[8] = (float)(m[5] - m[7]);
+    // The rate columns are FP32: each compensated sum is rounded to FP32 once
+    // (s - c) and combined in FP32, which keeps the epilogue off the FP64 pipe.
+    float m[9];
+    for (int c = 0; c < 9; ++c) m[c] = M[c].s - M[c].c;
+    out[0] = 2.0f * m[0]; out[1] = 2.0f * m[4]; out[2] = 2.0f * m[8];
+    out[3] = m[1] + m[3]; out[4] = m[2] + m[6]; out[5] = m[5] + m[7];
+    out[6] = m[1] - m[3]; out[7] = m[2] - m[6]; out[8] = m[5] - m[7];
     dkin = kin.value();
     cond = cnd.value();
   }
