@@ -353,3 +353,27 @@ def test_kickdrift_contact_time_step_is_rejected():
     with pytest.raises(WFError):
         d.prepare(case.dt)
     d.close()
+
+
+def test_frozen_topology_searches_once():
+    """freeze_neighbours (a library option for finite-difference checks of
+    the adjoint): a yielding cylinder that rebuilds its rows every 5 steps
+    searches only at the first step, keeps the first search's rows, and its
+    state differs from the regular run only through the stale rows."""
+    res = {}
+    for freeze in (0, 1):
+        d = gpu_domain()
+        if freeze:
+            d.set("freeze_neighbours", 1)
+        case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+        d.prepare(case.dt)
+        d.step(1)
+        first = d.neighbours()
+        d.step(59)
+        res[freeze] = (d.geti("nb_searches"), first, d.neighbours(), d.get_array("Sigma"))
+        d.close()
+    assert res[0][0] > 2 and res[1][0] == 1
+    for k in (0, 1):
+        assert np.array_equal(res[1][1][k], res[1][2][k])
+        assert np.array_equal(res[0][1][k], res[1][1][k])
+    assert rel_l2(res[1][3], res[0][3]) < 1e-2
