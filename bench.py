@@ -14,6 +14,20 @@ The default arm runs the CUDA library; ``--impl reference`` times the CPU
 restatement of the reference's OpenMP structure (per-thread pair lists and the
 Nishimura gather, built from oracle/) on all host cores, on the same workload.
 N > 1 runs N independent replicas (the path does not shard across GPUs).
+
+Measurement modes (each prints its own output instead of the bench line):
+
+    python bench.py --config-table
+        every synthetic configuration on both GPU forms and the CPU restatement
+    python bench.py --case [--n 250000] [--steps 3] [--precision 0|1] [--v-top -1]
+                    [--kernels] [--gather-block B] [--particle-block B]
+        a fixed-size run of the bench cylinder scaled to about n particles, for
+        ncu captures and per-kernel CUDA-event times (--kernels)
+    python bench.py --accuracy [--steps 1000] [--dx-mm 0.3353,0.2112,0.1331]
+                    [--v-top -1] [--contact]
+        the mixed form against the plain FP64 form from the same start
+    python bench.py --pipe-rates
+        FP64/FP32 arithmetic and copy rates of the GPU (roofline ceilings)
 """
 from __future__ import annotations
 
@@ -40,7 +54,7 @@ DX_1M = 0.2112e-3
 # per pass, state read + written once, 4-byte neighbour index per entry and a
 # 4-byte row length), at each form's storage widths: FP64 state; the mixed
 # form's gathers read FP32 float-float shadows (x, v: 24 B each) and FP32
-# Sigma/rho^2, m, rho, h.  the design doc section 5 lists the field sets.
+# Sigma/rho^2, m, rho, h.  The comment of each entry names its fields.
 ALG_BYTES = {
     "k_accel": lambda nnz: 144 + 4 * nnz + 4,             # x,v,rho,m,h,Sigma(6) -> a
     "k_density_drift": lambda nnz: 272 + 4 * nnz + 4,     # x,v,a,rho,m,h -> v,rho ; x,v,a -> x,v
@@ -342,6 +356,193 @@ def adjoint_leg(wfmod, steps=400, every=10, k=20):
             "loss": r["loss"], "grad": dict(zip(wfmod.PARAMS, r["grad"].tolist()))}
 
 
+# ---------------------------------------------------------------- measurement modes
+def case_mode(a):
+    """A fixed-size run of the bench cylinder (R = 10 mm, L = 30 mm, dx chosen
+    for about --n particles) for profilers: prepares, runs --steps steps and
+    prints the particle count and the step time; --kernels adds per-kernel
+    CUDA-event times of the same number of steps."""
+    import weldform_gb300 as wfmod
+    from weldform_gb300 import configs
+    dx = configs.dx_for_count(R, L, a.n)
+    d = wfmod.Domain()
+    d.set("precision", a.precision)
+    case = configs.cylinder_upsetting(d, R=R, L=L, dx=dx, v_top=a.v_top)
+    d.prepare(case.dt)
+    if a.gather_block is not None:
+        d.set("gather_block", a.gather_block)
+    if a.particle_block is not None:
+        d.set("particle_block", a.particle_block)
+    t = time.perf_counter()
+    d.step(a.steps)
+    el = time.perf_counter() - t
+    print(f"n={case.n} dx={dx:.6e} steps={a.steps} s/step={el / max(a.steps, 1):.4e} "
+          f"searches={d.geti('nb_searches')} max_pl={d.get('max_pl_strain'):.3e}")
+    if a.kernels:
+        prof = d.profile_steps(a.steps)
+        tot = sum(v[0] for v in prof.values())
+        for k, (ms, n) in sorted(prof.items(), key=lambda kv: -kv[1][0]):
+            print(f"  {k:24s} {n:4d} launches {ms:9.3f} ms  {100 * ms / tot:5.1f} %")
+    d.close()
+
+
+def accuracy_mode(a):
+    """The mixed form against the plain FP64 form (itself within 1e-9 of the
+    CPU oracle in the parity tests) from the same start after --steps steps,
+    at each --dx-mm: one JSON line per size with the relative L2 errors of
+    displacement, stress, plastic strain and density.  --contact runs the
+    penalty-contact workload (JC, conduction, plastic heating, area penalty
+    0.1 E / h, friction 0.2; dx = 0.2 mm gives 1,150,200 particles) pressed at
+    --v-top and adds the reaction-force curve (every steps / 10 steps) and the
+    temperature rise."""
+    import weldform_gb300 as wfmod
+    from weldform_gb300 import configs
+    fields = ("Displacement", "Sigma", "pl_strain", "Density")
+    dxs = a.dx_mm if a.dx_mm else ("0.2" if a.contact else "0.3353,0.2112,0.1331")
+
+    def run(prec, dx):
+        d = wfmod.Domain()
+        d.set("precision", prec)
+        if a.contact:
+            case = configs.contact_upsetting(d, R=R, L=L, dx=dx, v_punch=a.v_top, stiffness="area")
+        else:
+            case = configs.cylinder_upsetting(d, R=R, L=L, dx=dx, v_top=a.v_top)
+        d.prepare(case.dt)
+        every = max(a.steps // 10, 1)
+        fz = []
+        t = time.perf_counter()
+        for _ in range(a.steps // every):
+            d.step(every)
+            if a.contact:
+                fz.append(d.contact_force(case.mesh)[2])
+        d.step(a.steps - every * (a.steps // every))
+        out = {f: d.get_array(f) for f in fields}
+        out["s"] = time.perf_counter() - t
+        out["n"] = case.n
+        if a.contact:
+            out["reaction_force"] = np.array(fz)
+            out["T_rise"] = d.get_array("T") - configs.Steel().T0
+        d.close()
+        return out
+
+    def rel(x, y):
+        ny = np.linalg.norm(y)
+        return float(np.linalg.norm(x - y) / ny) if ny > 0 else float(np.linalg.norm(x - y))
+
+    for dx in [float(v) * 1e-3 for v in dxs.split(",")]:
+        m = run(wfmod.PRECISION_MIXED, dx)
+        f = run(wfmod.PRECISION_FP64, dx)
+        keys = fields + (("reaction_force", "T_rise") if a.contact else ())
+        print(json.dumps({"particles": m["n"], "dx_mm": dx * 1e3, "steps": a.steps, "v_top": a.v_top,
+                          "contact": a.contact, "max_pl_strain": float(f["pl_strain"].max()),
+                          "mixed_vs_fp64": {k: rel(m[k], f[k]) for k in keys},
+                          "seconds": {"mixed": m["s"], "fp64": f["s"]}}), flush=True)
+
+
+PIPE_RATES_CU = r"""
+// Arithmetic and copy rates: FP64 and FP32 fused multiply-add, FP64 divide
+// and square root, FP64 -> FP32 conversion, device-to-device copy.  Every
+// loop is bounded and every buffer is written in range.
+#include <cstdio>
+#include <cuda_runtime.h>
+#define ITERS 2048
+__global__ void k_dfma(double* out, double a, double b) {
+  double x[8];
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-9 + k;
+  for (int i = 0; i < ITERS; ++i)
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  double s = 0; for (int k = 0; k < 8; ++k) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+__global__ void k_ffma(float* out, float a, float b) {
+  float x[8];
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-9f + k;
+  for (int i = 0; i < ITERS; ++i)
+    for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+  float s = 0; for (int k = 0; k < 8; ++k) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+__global__ void k_ddiv(double* out, double a) {
+  double x[4];
+  for (int k = 0; k < 4; ++k) x[k] = threadIdx.x + 1.5 + k;
+  for (int i = 0; i < ITERS / 8; ++i)
+    for (int k = 0; k < 4; ++k) x[k] = a / x[k] + 1.0;
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x[0] + x[1] + x[2] + x[3];
+}
+__global__ void k_dsqrt(double* out) {
+  double x[4];
+  for (int k = 0; k < 4; ++k) x[k] = threadIdx.x + 1.5 + k;
+  for (int i = 0; i < ITERS / 8; ++i)
+    for (int k = 0; k < 4; ++k) x[k] = sqrt(x[k]) + 1.0;
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x[0] + x[1] + x[2] + x[3];
+}
+__global__ void k_d2f(float* out, double a) {
+  double x0 = threadIdx.x * 1e-3;
+  float s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  for (int i = 0; i < ITERS; ++i) {
+    x0 += a;
+    s0 += (float)x0; s1 += (float)(x0 * 2.0); s2 += (float)(x0 * 3.0); s3 += (float)(x0 * 5.0);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s0 + s1 + s2 + s3;
+}
+__global__ void k_copy(const double4* __restrict__ a, double4* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) b[i] = a[i];
+}
+int main() {
+  int nsm = 0; cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0);
+  int clk = 0; cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, 0);
+  int blocks = nsm * 8, threads = 256;
+  size_t nthreads = (size_t)blocks * threads;
+  double* dout; float* fout;
+  if (cudaMalloc(&dout, nthreads * sizeof(double)) != cudaSuccess) return 1;
+  if (cudaMalloc(&fout, nthreads * sizeof(float)) != cudaSuccess) return 1;
+  cudaEvent_t e0, e1; cudaEventCreate(&e0); cudaEventCreate(&e1);
+  float ms;
+  auto timeit = [&](const char* name, double ops_per_thread, auto launch) {
+    for (int w = 0; w < 3; ++w) launch();
+    cudaEventRecord(e0);
+    for (int r = 0; r < 5; ++r) launch();
+    cudaEventRecord(e1); cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    printf("%-8s %10.3f Gop/s  (%.3f ms/launch)\n", name, ops_per_thread * nthreads * 5 / (ms * 1e-3) / 1e9, ms / 5);
+  };
+  timeit("dfma", 8.0 * ITERS, [&] { k_dfma<<<blocks, threads>>>(dout, 0.999999, 1e-7); });
+  timeit("ffma", 8.0 * ITERS, [&] { k_ffma<<<blocks, threads>>>(fout, 0.999999f, 1e-7f); });
+  timeit("ddiv", 4.0 * ITERS / 8, [&] { k_ddiv<<<blocks, threads>>>(dout, 3.0); });
+  timeit("dsqrt", 4.0 * ITERS / 8, [&] { k_dsqrt<<<blocks, threads>>>(dout); });
+  timeit("d2f", 4.0 * ITERS, [&] { k_d2f<<<blocks, threads>>>(fout, 1e-3); });
+  size_t n4 = (size_t)1 << 27;  // 4 GiB per buffer of 32-byte elements
+  double4 *a = nullptr, *b = nullptr;
+  if (cudaMalloc(&a, n4 * 32) == cudaSuccess && cudaMalloc(&b, n4 * 32) == cudaSuccess) {
+    cudaMemset(a, 0, n4 * 32);
+    for (int w = 0; w < 3; ++w) k_copy<<<nsm * 4, 512>>>(a, b, n4);
+    cudaEventRecord(e0);
+    for (int r = 0; r < 5; ++r) k_copy<<<nsm * 4, 512>>>(a, b, n4);
+    cudaEventRecord(e1); cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    printf("copy     %10.1f GB/s\n", 2.0 * n4 * 32 * 5 / (ms * 1e-3) / 1e9);
+  }
+  printf("SMs %d clock %d kHz; err=%s\n", nsm, clk, cudaGetErrorString(cudaDeviceSynchronize()));
+  return 0;
+}
+"""
+
+
+def pipe_rates_mode():
+    """Compiles PIPE_RATES_CU for sm_103a in a temporary directory and runs it."""
+    nvcc = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+    with tempfile.TemporaryDirectory() as tmp:
+        src, exe = os.path.join(tmp, "rates.cu"), os.path.join(tmp, "rates")
+        with open(src, "w") as f:
+            f.write(PIPE_RATES_CU)
+        subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe, src], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        sys.stdout.write(r.stdout)
+        sys.stderr.write(r.stderr)
+        if r.returncode:
+            sys.exit(r.returncode)
+
+
 def dist_setup(n):
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
@@ -378,10 +579,29 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--config-table", action="store_true",
                     help="time every configuration (GPU forms and CPU restatement) and print one JSON table")
+    ap.add_argument("--case", action="store_true", help="fixed-size run for profilers (see --n, --kernels)")
+    ap.add_argument("--accuracy", action="store_true", help="mixed form against the plain FP64 form")
+    ap.add_argument("--pipe-rates", action="store_true", help="arithmetic and copy rates of the GPU")
+    ap.add_argument("--n", type=int, default=250000, help="--case: particle count")
+    ap.add_argument("--precision", type=int, default=0, help="--case: 0 plain FP64, 1 mixed")
+    ap.add_argument("--v-top", type=float, default=-1.0, help="--case/--accuracy: top or punch velocity (m/s)")
+    ap.add_argument("--kernels", action="store_true", help="--case: per-kernel CUDA-event times")
+    ap.add_argument("--gather-block", type=int, default=None, help="--case: threads per mixed gather block")
+    ap.add_argument("--particle-block", type=int, default=None, help="--case: threads per per-particle block")
+    ap.add_argument("--dx-mm", default=None, help="--accuracy: lattice spacings (mm, comma-separated)")
+    ap.add_argument("--contact", action="store_true", help="--accuracy: penalty-contact workload")
     a = ap.parse_args()
     if a.config_table:
         print(json.dumps(config_table()))
         return
+    if a.case:
+        return case_mode(a)
+    if a.accuracy:
+        if a.steps == ap.get_default("steps"):
+            a.steps = 1000
+        return accuracy_mode(a)
+    if a.pipe_rates:
+        return pipe_rates_mode()
     warmup = max(a.warmup, 3)
     rank, world, local, pg = dist_setup(a.gpus)
 

@@ -100,7 +100,11 @@ int wf_domain_destroy(wf_domain* d);
  * "stage_cap" (its halo capacity per block, 64..1024, default 896, before
  * the prologue), "freeze_neighbours" (1: neighbour rows, contact pairs and
  * surface flags come from the first step's search only, for finite-difference
- * checks of the adjoint; no reference counterpart), "cpu_threads" (unused on
+ * checks of the adjoint; no reference counterpart), "nan_check" (1: a
+ * particle position that is not finite at a neighbour search, or non-finite
+ * energy sums, make the next status-returning call fail with WF_ERR_NAN;
+ * default 0 keeps the reference's behaviour of stepping on with NaN; no
+ * reference counterpart; before the prologue), "cpu_threads" (unused on
  * the GPU path).  Read back with wf_get_domain_i32: "gather_block",
  * "gather_staging", "stage_cap". */
 int wf_set_domain_f64(wf_domain* d, const char* name, double value);
@@ -110,7 +114,11 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int value);
  * "contact_reaction_sum", "ext_forces_work", "max_pl_strain", "m_maxT",
  * "m_minT"; integers: "particle_count", "solid_part_count", "steps",
  * "pair_count", "contact_pair_count", "nb_searches", "CellNo.x|y|z",
- * "surface_count". */
+ * "surface_count", "dynamic_friction_count" (contact-pair evaluations since
+ * the prologue that took the dynamic-friction branch, Contact_Wang.cpp:284-290;
+ * no reference counterpart), "nan_particles" (particles whose position was not
+ * finite at the last neighbour search: they get empty rows and appear in no
+ * row, as CheckRadius decides for them, without being binned into a cell). */
 int wf_get_domain_f64(wf_domain* d, const char* name, double* value);
 int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* value);
 
@@ -134,8 +142,12 @@ int wf_assign_zone(wf_domain* d, const double start[3], const double end[3], int
  * whose ID equals `zone`, or all particles when zone < 0.
  * f64 fields: "G", "Cs", "Sigmay", "Ep", "Alpha", "Beta", "TI", "TIn", "TIInitDist",
  * "k_T", "cp_T", "T", "th_exp", "Density", "RefDensity", "Mass", "h", "P0",
- * "q_source".  i32 fields: "PresEq", "Fail", "Material_model", "mat",
- * "Material", "ID", "IsFree", "print_history". */
+ * "q_source", "T_inf", "h_conv".  i32 fields: "PresEq", "Fail",
+ * "Material_model", "mat", "Material", "ID", "IsFree", "print_history",
+ * "Thermal_BC" (1 = TH_BC_CONVECTION: with the thermal solver on, every step
+ * sets q_conv = rho h_conv (m/rho)^(2/3) (T_inf - T) / m after the temperature
+ * update and adds it to dTdt, CalcConvHeat, Thermal.cpp:339-389; the JSON
+ * driver's "ConvectionBC" sets these three per zone, WeldForm.cpp:793-807). */
 int wf_set_particle_f64(wf_domain* d, const char* field, int zone, double value);
 int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value);
 /* Whole-array transfer in original particle order.  Vector fields ("x", "v",
@@ -143,15 +155,15 @@ int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value);
  * tensor fields ("Sigma", "ShearStress", "StrainRate", "RotationRate",
  * "Strain", "Strain_pl", "TIR" read-only) 9 (row-major, full 3x3, as the reference stores
  * them); scalars 1 ("Density", "Pressure", "pl_strain", "Sigmay", "T",
- * "dTdt", "eff_strain_rate", "q_plheat", "Mass", "h", "delta_pl_strain",
- * "dDensity").  n is the total number of doubles. */
+ * "dTdt", "eff_strain_rate", "q_plheat", "q_conv", "Mass", "h",
+ * "delta_pl_strain", "dDensity").  n is the total number of doubles. */
 int wf_set_particle_array_f64(wf_domain* d, const char* field, const double* src,
                               int64_t n);
 int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int64_t n);
-/* Integer arrays: "ID", "Nb", "IsFree". */
+/* Integer arrays: "ID", "Nb", "IsFree", "Thermal_BC". */
 int wf_get_particle_array_i32(wf_domain* d, const char* field, int32_t* dst, int64_t n);
 /* Per-particle integer fields as whole arrays, before the prologue: "ID",
- * "mat", "Material_model", "Fail", "Material", "not_write_surf_ID"
+ * "mat", "Material_model", "Fail", "Material", "not_write_surf_ID", "Thermal_BC"
  * (Particle.h:50-265; the array form of assigning them in a loop). */
 int wf_set_particle_array_i32(wf_domain* d, const char* field, const int32_t* src, int64_t n);
 
@@ -266,8 +278,8 @@ int wf_autotune(wf_domain* d, int steps, int* block);
  * kernels backwards over it.  On return the domain holds the state after
  * `steps` steps, as if wf_step had run them.  curve (optional, ntarget values)
  * receives F(s); fwd_ms / adj_ms (optional) the wall time of the forward run
- * and of the reverse sweep.  Errors: WF_ERR_UNSUPPORTED for the mixed form or
- * particles with Ep < 0. */
+ * and of the reverse sweep.  Errors: WF_ERR_UNSUPPORTED for the mixed form,
+ * particles with Ep < 0 or convection boundary conditions. */
 #define WF_NPARAM 10
 enum { WF_P_E = 0, WF_P_SY0, WF_P_EP, WF_P_A, WF_P_B, WF_P_N, WF_P_C, WF_P_M, WF_P_MU, WF_P_PFAC };
 int wf_adjoint_reaction_loss(wf_domain* d, int64_t steps, int every, int mesh, int axis, const double* target,

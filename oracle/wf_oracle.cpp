@@ -237,6 +237,8 @@ struct Domain {
   int pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1;
   double pl_work_heat_frac = 0.9;
   double friction_sta = 0.0, friction_dyn = 0.0, PFAC = 0.0, DFAC = 0.0;
+  int64_t dyn_friction_count = 0;  // contact-pair evaluations that took the dynamic-friction branch
+  int nan_count = 0;               // particles with a non-finite position at the last search
   int contact_alg = 0;
   double DomMax[3] = {-100000000000.0, -100000000000.0, -100000000000.0};
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
@@ -254,9 +256,11 @@ struct Domain {
   std::vector<V3> x, v, a, x_prev, disp, normal, contforce;
   std::vector<double> rho, rho0, mass, h, hini, Cs, P0, G, pressure, pl_strain, delta_pl_strain, sigmay, Ep,
       eff_strain_rate, T, dTdt, k_T, cp_T, th_exp, q_plheat, q_conv, q_source, q_cont_conv, ps_energy, alpha,
+      T_inf, h_conv,
       beta, TI, TIn, TIInitDist, dDensity, cont_stiff, delta_cont, dkin, dint;
   std::vector<M3> sigma, tau, srate, rrate, strain, strain_pl, strain_pl_incr, TIR, gcm;
-  std::vector<int> ID, ID_orig, not_write_surf, is_free, material_idx, mat, model, fail_crit, pres_eq, Nb, mesh_of, elem_of;
+  std::vector<int> ID, ID_orig, not_write_surf, is_free, material_idx, mat, model, fail_crit, pres_eq, Nb, mesh_of, elem_of,
+      thermal_bc;
 
   std::vector<Material> materials;
   std::vector<Amplitude> amps;
@@ -306,6 +310,7 @@ struct Domain {
     G.push_back(0); pressure.push_back(0); pl_strain.push_back(0); delta_pl_strain.push_back(0); sigmay.push_back(0);
     Ep.push_back(0); eff_strain_rate.push_back(0); T.push_back(0); dTdt.push_back(0); k_T.push_back(0);
     cp_T.push_back(0); th_exp.push_back(0); q_plheat.push_back(0); q_conv.push_back(0); q_source.push_back(0);
+    T_inf.push_back(0); h_conv.push_back(0); thermal_bc.push_back(0);  // Thermal_BC = TH_BC_NONE (Particle.cpp:102)
     q_cont_conv.push_back(0); ps_energy.push_back(0); alpha.push_back(0); beta.push_back(0); TI.push_back(0);
     TIn.push_back(4.0); TIInitDist.push_back(0); dDensity.push_back(0); cont_stiff.push_back(0); delta_cont.push_back(0);
     dkin.push_back(0); dint.push_back(0);
@@ -722,6 +727,11 @@ struct Domain {
 
   int neighbour_search() {
     if (!cells_ready) return set_err(WF_ERR_STATE, "neighbour search before the solver prologue");
+    // particles with a non-finite coordinate at this search (reported only;
+    // the linked-list search bins them into clamped cells as the reference does)
+    nan_count = 0;
+    for (int i = 0; i < N; ++i)
+      if (!(std::isfinite(x[i].c[0]) && std::isfinite(x[i].c[1]) && std::isfinite(x[i].c[2]))) ++nan_count;
     search_linked_list();
     int rc = build_canonical();
     if (mode == 1) build_nishimura();
@@ -1141,6 +1151,13 @@ struct Domain {
       if (T[i] > m_maxT) m_maxT = T[i];
       if (T[i] < m_minT) m_minT = T[i];
     }
+    // Thermal.cpp:339-389 CalcConvHeat (3D): Fraser Eq. 3-121 with the contact
+    // area dS^2 = (m / rho)^(2/3) of Eq. 3-119
+    for (int i = 0; i < N; i++)
+      if (thermal_bc[i] == 1) {
+        double dS2 = std::pow(mass[i] / rho[i], 2.0 / 3.0);
+        q_conv[i] = rho[i] * h_conv[i] * dS2 * (T_inf[i] - T[i]) / mass[i];
+      }
     std::vector<double> tmp(N, 0.0);
 #pragma omp parallel for schedule(static) num_threads(nthreads)
     for (int i = 0; i < ns; i++) {
@@ -1238,7 +1255,8 @@ struct Domain {
                 V3 q = v3(tgforce.c[0] / mass[P1], tgforce.c[1] / mass[P1], tgforce.c[2] / mass[P1]);
                 contforce[P1] = sub(contforce[P1], q);
                 a[P1] = sub(a[P1], q);
-              } else {
+              } else {  // dynamic branch (Contact_Wang.cpp:284-290)
+                ++dyn_friction_count;
                 double s = friction_dyn * norm(contforce[P1]);
                 double nt = norm(tgforce);
                 V3 td = v3(s * tgforce.c[0] / nt, s * tgforce.c[1] / nt, s * tgforce.c[2] / nt);
@@ -1501,6 +1519,9 @@ std::vector<double>* f64_field(Domain* d, const std::string& f) {
   if (f == "h") return &d->h;
   if (f == "P0") return &d->P0;
   if (f == "q_source") return &d->q_source;
+  if (f == "q_conv") return &d->q_conv;
+  if (f == "T_inf") return &d->T_inf;
+  if (f == "h_conv") return &d->h_conv;
   if (f == "Pressure") return &d->pressure;
   if (f == "pl_strain") return &d->pl_strain;
   if (f == "dTdt") return &d->dTdt;
@@ -1539,6 +1560,7 @@ std::vector<int>* i32_field(Domain* d, const std::string& f) {
   if (f == "ID") return &d->ID;
   if (f == "IsFree") return &d->is_free;
   if (f == "Nb") return &d->Nb;
+  if (f == "Thermal_BC") return &d->thermal_bc;
   return nullptr;
 }
 
@@ -1623,8 +1645,10 @@ int wfo_get_domain_i32(wfo_domain* p, const char* name, int64_t* v) {
   else if (n == "steps") *v = d->steps;
   else if (n == "pair_count") *v = (int64_t)d->sm_pairs.size();
   else if (n == "contact_pair_count") *v = (int64_t)d->cp_idx.size();
+  else if (n == "dynamic_friction_count") *v = d->dyn_friction_count;
   else if (n == "nb_searches") *v = d->nb_searches;
   else if (n == "surface_count") *v = d->surface_count;
+  else if (n == "nan_particles") *v = d->nan_count;
   else if (n.rfind("CellNo.", 0) == 0 && n.size() == 8) *v = d->CellNo[n[7] - 'x'];
   else return set_err(WF_ERR_ARG, "unknown domain i32 read " + n);
   return WF_OK;

@@ -20,6 +20,13 @@ THREADS = os.cpu_count() or 1
 
 JC = adj.ContactCase(R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, model=JOHNSON_COOK, thermal=True, stiffness="area")
 BL = adj.ContactCase(R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, model=BILINEAR, thermal=False, stiffness="wang")
+# The plane also slides along x at 5 m/s: pairs take the dynamic-friction
+# branch (Contact_Wang.cpp:284-290), the only one through which the loss
+# depends on mu.  Wang's stiffness, and the Fraser law (PFAC cont_stiff).
+SL_W = adj.ContactCase(R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, model=JOHNSON_COOK, thermal=True,
+                       stiffness="wang", v_slide=5.0)
+SL_P = adj.ContactCase(R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, model=JOHNSON_COOK, thermal=True,
+                       stiffness="penalty", v_slide=5.0)
 
 
 def _oracle():
@@ -43,8 +50,10 @@ def _target(case, steps, every):
     return adj.perturbed_jc_target(case, steps, every) * 0.9
 
 
-@pytest.mark.parametrize("case,must", [(JC, ("E", "A", "B", "n", "C", "PFAC")), (BL, ("E", "sy0", "Ep"))],
-                         ids=["jc_thermal_area", "bilinear_wang"])
+@pytest.mark.parametrize("case,must", [(JC, ("E", "A", "B", "n", "C", "m", "PFAC")), (BL, ("E", "sy0", "Ep")),
+                                      (SL_W, ("E", "A", "B", "n", "C", "m", "mu")),
+                                      (SL_P, ("E", "A", "B", "n", "C", "m", "mu", "PFAC"))],
+                         ids=["jc_thermal_area", "bilinear_wang", "sliding_wang", "sliding_penalty"])
 def test_adjoint_matches_tangent_linear(case, must):
     steps, every = 60, 5
     t = _target(case, steps, every)
@@ -75,6 +84,31 @@ def test_adjoint_matches_finite_differences():
     fds = {rel: adj.central_fd(prob, rel) for rel in (1e-5, 1e-6, 1e-7)}
     for p in ("E", "A", "B", "n", "C", "PFAC"):
         k = PARAMS.index(p)
+        errs = {rel: abs(g[k] - fd[k]) / abs(fd[k]) for rel, fd in fds.items()}
+        assert min(errs.values()) <= 1e-4, (p, g[k], errs)
+        assert errs[1e-6] <= 1e-2, (p, g[k], errs)
+
+
+@pytest.mark.parametrize("case,params", [(SL_W, ("mu",)), (SL_P, ("mu", "PFAC", "E"))],
+                         ids=["sliding_wang", "sliding_penalty"])
+def test_friction_gradient_matches_finite_differences(case, params):
+    """dL/dmu through the dynamic-friction branch (and the Fraser law's PFAC
+    and E through cont_stiff) against central differences of GPU forward
+    runs, with the bars of the test above."""
+    steps, every = 60, 5
+    t = _target(case, steps, every)
+    prob = adj.Problem(case, steps, every, t)
+    d = gpu_domain()
+    adj.build(d, case, case.nominal())
+    d.prepare(case.dt)
+    d.step(steps)
+    assert d.geti("dynamic_friction_count") > 0
+    d.close()
+    loss, g = prob.loss_grad(np.zeros(len(PARAMS)))
+    fds = {rel: adj.central_fd(prob, rel, only=params) for rel in (1e-5, 1e-6, 1e-7)}
+    for p in params:
+        k = PARAMS.index(p)
+        assert g[k] != 0.0
         errs = {rel: abs(g[k] - fd[k]) / abs(fd[k]) for rel, fd in fds.items()}
         assert min(errs.values()) <= 1e-4, (p, g[k], errs)
         assert errs[1e-6] <= 1e-2, (p, g[k], errs)

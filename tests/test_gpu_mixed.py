@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from tests._support import gpu_domain, oracle_domain, rel_l2
-from weldform_gb300 import configs, JOHNSON_COOK, PRECISION_MIXED
+from weldform_gb300 import configs, HOLLOMON, JOHNSON_COOK, PRECISION_MIXED
 
 pytestmark = pytest.mark.gpu
 
@@ -82,6 +82,57 @@ def test_mixed_contact_reaction_force():
     assert abs(o["cf"][2]) > 0
     assert abs(m["cf"][2] - o["cf"][2]) <= TOL * abs(o["cf"][2])
     _check(m, o, f)
+
+
+def test_mixed_hollomon_yielding():
+    """Hollomon with plateau past its end (Material.cpp:48-64): the mixed
+    form's return evaluates K (eps_p + eps0)^m in FP32."""
+    f = FIELDS + ("pl_strain", "Sigmay")
+    m, o = _run(configs.cylinder_upsetting, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0, model=HOLLOMON)
+    assert o["pl_strain"].max() > 1e-2
+    _check(m, o, f)
+
+
+@pytest.mark.parametrize("stiffness,v_slide", [("penalty", 0.0), ("penalty", 5.0), ("wang", 5.0)],
+                         ids=["penalty", "penalty_sliding", "wang_sliding"])
+def test_mixed_contact_laws_and_sliding(stiffness, v_slide):
+    """The Fraser law kij = PFAC cont_stiff (Contact.cpp:423) and a plane
+    sliding along x, whose pairs take the dynamic-friction branch: the
+    reaction force and the state within the mixed form's bound."""
+    f = FIELDS + ("pl_strain", "T")
+    m, o = _run(configs.contact_upsetting, 150, f, ("contact_force_sum",), R=0.003, L=0.006, dx=0.0003,
+                v_punch=-10.0, gap=0.0, stiffness=stiffness, v_slide=v_slide)
+    assert abs(o["cf"][2]) > 0
+    assert abs(m["cf"][2] - o["cf"][2]) <= TOL * abs(o["cf"][2])
+    if v_slide:
+        assert abs(m["cf"][0] - o["cf"][0]) <= TOL * abs(o["cf"][0])
+    _check(m, o, f)
+
+
+@pytest.mark.parametrize("V", [(1.0, 1.0, 1.0), (-3.0, 0.5, 10.0)], ids=["1m", "10m"])
+def test_mixed_domain_away_from_the_origin(V):
+    """The yielding cylinder placed with its base centre at V (metres).  The
+    mixed form forms x_i - x_j from float-float position records held
+    relative to the cell grid's centre, so its accuracy does not depend on
+    where the domain sits; displacement (not absolute position) and stress
+    stay within the bound."""
+    f = FIELDS + ("pl_strain",)
+    m, o = _run(configs.cylinder_upsetting, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0, V=V)
+    assert o["pl_strain"].max() > 1e-2
+    errs = _check(m, o, f)
+    # the same case at the origin, for scale: the offset costs nothing
+    m0, o0 = _run(configs.cylinder_upsetting, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    errs0 = _check(m0, o0, f)
+    for k in ("Displacement", "Sigma"):
+        assert errs[k] <= 3.0 * errs0[k] + 1e-7, (k, errs[k], errs0[k])
+
+
+def test_mixed_convection_heat():
+    from tests.test_gpu_parity import convection
+    f = FIELDS + ("pl_strain", "T", "q_conv")
+    m, o = _run(convection, 200, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    _check(m, o, f)
+    assert rel_l2(m["T"] - 300.0, o["T"] - 300.0) <= TOL
 
 
 @pytest.mark.slow

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from tests._support import gpu_domain, oracle_domain, rel_l2
-from weldform_gb300 import configs, JOHNSON_COOK
+from weldform_gb300 import configs, HOLLOMON, JOHNSON_COOK
 
 pytestmark = pytest.mark.gpu
 
@@ -183,7 +183,26 @@ def test_johnson_cook_thermal():
     _check(g, o, f, SCALARS + ("plastic_work",))
 
 
-@pytest.mark.parametrize("stiffness", ["wang", "area"])
+def test_hollomon_yielding_past_the_plateau():
+    """Hollomon flow stress with plateau (Material.cpp:48-64) under yielding:
+    sigma_y = sy0 on the plateau, K (eps_p + eps0)^m once eps_p + eps0 > eps1,
+    recomputed in every return with the previous step's sigma_y scaling back
+    (Particle.cpp:995-1011) and Ep held at its initial 0 (quirk Q1).  Most
+    particles pass the plateau end within the run, with rebuilds every 5
+    steps."""
+    mat = configs.Steel()
+    K, m = mat.hollomon
+    eps0, eps1 = mat.sy0 / mat.E, (mat.sy0 / K) ** (1.0 / m)
+    f = FIELDS + ("Strain_pl", "eff_strain_rate")
+    g, o = _pair(configs.cylinder_upsetting, 100, f, SCALARS, R=0.004, L=0.008, dx=0.0005, v_top=-20.0,
+                 model=HOLLOMON)
+    past = o["pl_strain"] + eps0 > eps1
+    assert past.sum() > 0.5 * len(past) and o["searches"] > 10
+    assert (o["Sigmay"] > mat.sy0).sum() > 0.5 * len(past)  # on the power law, above the plateau
+    _check(g, o, f, SCALARS)
+
+
+@pytest.mark.parametrize("stiffness", ["wang", "area", "penalty"])
 def test_rigid_plane_contact(stiffness):
     """Rigid plane closing on the top face (zero initial gap), Johnson-Cook,
     conduction + plastic heating, friction 0.2.  The x/y totals of the
@@ -212,6 +231,41 @@ def test_rigid_plane_contact(stiffness):
     assert rel_l2(cg[:, :2], co[:, :2]) <= 1e-6
 
 
+@pytest.mark.parametrize("stiffness", ["wang", "area", "penalty"])
+def test_sliding_contact_dynamic_friction(stiffness):
+    """The plane slides along x at 5 m/s while closing at 10 m/s: the
+    tangential trial force exceeds mu |F_n| on many pairs, which then take
+    the dynamic-friction branch F_t = mu_d |F_n| t / |t| (Contact_Wang.cpp:
+    284-290).  Both sides count those pair evaluations; the counts and the
+    state must agree."""
+    f = FIELDS + ("T", "contforce")
+    sc = ("int_energy_sum", "contact_force_sum", "ext_forces_work", "plastic_work")
+    out = {}
+    for name in ("gpu", "oracle"):
+        d = gpu_domain() if name == "gpu" else oracle_domain()
+        if name == "oracle":
+            d.set("cpu_threads", THREADS)
+        case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, stiffness=stiffness,
+                                         gap=0.0, v_slide=5.0)
+        d.prepare(case.dt)
+        d.step(100)
+        out[name] = {k: d.get_array(k) for k in f}
+        out[name].update({k: d.get(k) for k in sc})
+        out[name]["dyn"] = d.geti("dynamic_friction_count")
+        out[name]["cf"] = d.contact_force(case.mesh)
+        d.close()
+    g, o = out["gpu"], out["oracle"]
+    assert o["dyn"] > 100 and g["dyn"] == o["dyn"]
+    for k in FIELDS + ("T",):
+        assert rel_l2(g[k], o[k]) <= TOL, k
+    for k in sc:
+        assert abs(g[k] - o[k]) <= 1e-8 * abs(o[k]), (k, g[k], o[k])
+    assert rel_l2(g["cf"], o["cf"]) <= 1e-8
+    # the sliding force's x component is the dynamic friction of the pairs
+    assert abs(o["cf"][0]) > 0
+    assert rel_l2(g["contforce"], o["contforce"]) <= 1e-6
+
+
 def test_solve_loop_matches_reference_loop_control():
     res = {}
     for name in ("gpu", "oracle"):
@@ -230,6 +284,31 @@ def test_config1_full_1000_steps():
     g, o = _pair(configs.cylinder_upsetting, 1000, FIELDS, SCALARS)
     assert g["x"].shape[0] == 8004
     _check(g, o, FIELDS, SCALARS)
+
+
+def convection(dom, h_conv=1e6, T_inf=1000.0, **kw):
+    """Johnson-Cook cylinder with conduction and plastic heating whose
+    lateral surface (the outer lattice ring) carries a convection boundary
+    condition (Thermal_BC = 1, as the JSON driver's ConvectionBC sets it,
+    WeldForm.cpp:793-807) toward a hot ambient."""
+    case = configs.cylinder_upsetting(dom, model=JOHNSON_COOK, thermal=True, **kw)
+    x = dom.get_array("x")
+    R = kw.get("R", 0.010)
+    ring = (np.hypot(x[:, 0], x[:, 1]) > R - 1.5 * case.dx).astype(np.int32)
+    dom.set_array("Thermal_BC", ring)
+    dom.set_particles("h_conv", h_conv)
+    dom.set_particles("T_inf", T_inf)
+    case.info["ring"] = ring
+    return case
+
+
+def test_convection_heat():
+    """CalcConvHeat (Thermal.cpp:339-389): q_conv of the surface ring, the
+    temperature it drives and the state, against the oracle."""
+    f = FIELDS + ("T", "dTdt", "q_conv")
+    g, o = _pair(convection, 100, f, SCALARS, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    assert (o["q_conv"] > 0).sum() > 100 and o["T"].max() > 301.0
+    _check(g, o, f, SCALARS)
 
 
 def _tensile(dom, **kw):

@@ -172,3 +172,21 @@ def test_kickdrift_contact_time_step_is_rejected_by_the_oracle():
     with pytest.raises(WFError):
         d.prepare(case.dt)
     d.close()
+
+
+def test_oracle_convection_source_matches_its_formula():
+    """CalcConvHeat (Thermal.cpp:339-389): after a step, a convection
+    particle's q_conv equals rho h_conv (m/rho)^(2/3) (T_inf - T) / m at its
+    updated density and temperature; other particles keep q_conv = 0."""
+    import numpy as np
+    from tests._support import oracle_domain
+    from tests.test_gpu_parity import convection
+    d = oracle_domain()
+    case = convection(d, R=0.003, L=0.006, dx=0.0005, v_top=-5.0)
+    d.prepare(case.dt)
+    d.step(3)
+    q, rho, m, T = (d.get_array(k) for k in ("q_conv", "Density", "Mass", "T"))
+    ring = case.info["ring"].astype(bool)
+    want = rho * 1e6 * (m / rho) ** (2.0 / 3.0) * (1000.0 - T) / m
+    assert np.allclose(q[ring], want[ring], rtol=1e-13, atol=0)
+    assert not q[~ring].any()

@@ -229,7 +229,7 @@ class Domain:
     def set_particles(self, field: str, value, zone: int = -1):
         """Assign a per-particle public field (Particle.h:50-265) for a zone (or all)."""
         if isinstance(value, (bool, int, np.integer)) and not isinstance(value, float) and field in (
-                "PresEq", "Fail", "Material_model", "mat", "Material", "ID", "IsFree", "print_history"):
+                "PresEq", "Fail", "Material_model", "mat", "Material", "ID", "IsFree", "print_history", "Thermal_BC"):
             self._call("set_particle_i32", self._h, field.encode(), int(zone), int(value))
         else:
             self._call("set_particle_f64", self._h, field.encode(), int(zone), float(value))
@@ -343,7 +343,7 @@ class Domain:
         C-contiguous array of the field's dtype and size (e.g. pinned host
         memory) that receives the values; it is returned as given."""
         n = self.particle_count
-        i32 = field in ("ID", "Nb", "IsFree")
+        i32 = field in ("ID", "Nb", "IsFree", "Thermal_BC")
         comps = 1 if i32 else (9 if field in TENSOR_FIELDS else (3 if field in VECTOR_FIELDS else 1))
         dt = np.int32 if i32 else np.float64
         if out is None:
@@ -361,7 +361,7 @@ class Domain:
         return buf.reshape(n, comps) if comps > 1 else buf
 
     def set_array(self, field: str, values):
-        if field in ("ID", "mat", "Material_model", "Fail", "Material", "not_write_surf_ID"):
+        if field in ("ID", "mat", "Material_model", "Fail", "Material", "not_write_surf_ID", "Thermal_BC"):
             a = np.ascontiguousarray(values, dtype=np.int32).ravel()
             self._call("set_particle_array_i32", self._h, field.encode(), a.ctypes.data_as(_IP), a.size)
             return

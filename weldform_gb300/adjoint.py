@@ -13,7 +13,10 @@ on every particle, the time step fixed by the nominal E, Ep and the initial
 Sigmay (bilinear: sy0; Johnson-Cook: CalcYieldStress(0, 0, T0)) set from the
 parameters, friction_sta = friction_dyn = mu, and the contact stiffness factor
 PFAC (contact_alg 2: k = PFAC (m / rho)^(2/3), with the nominal
-PFAC = 0.1 E / h of the penalty-contact workload).
+PFAC = 0.1 E / h of the penalty-contact workload; contact_alg 1, the Fraser
+law: k = PFAC * 9 K G / (3 K + G) dS, nominal PFAC = 0.6).  ``v_slide`` moves
+the plane along x as well, so sliding contact pairs take the dynamic-friction
+branch, the only one through which the loss depends on mu.
 
 ``ReactionLoss`` wraps the loss and the adjoint gradient as a
 ``torch.autograd.Function`` of dimensionless offsets u (theta = theta0 +
@@ -44,7 +47,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import BILINEAR, CONTACT_AREA, CONTACT_WANG, JOHNSON_COOK, PARAMS, Domain, PRECISION_FP64
+from . import BILINEAR, CONTACT_AREA, CONTACT_PENALTY, CONTACT_WANG, JOHNSON_COOK, PARAMS, Domain, PRECISION_FP64
 from .configs import SEED, Steel, jitter
 
 
@@ -68,6 +71,7 @@ class ContactCase:
     cfl: float = 0.4
     freeze: bool = False  # topology searched only at the first step (library option "freeze_neighbours")
     alpha: float = 1.0    # Monaghan viscosity Alpha of every particle
+    v_slide: float = 0.0  # plane velocity along x: sliding pairs reach the dynamic-friction branch
 
     @property
     def h(self) -> float:
@@ -81,7 +85,10 @@ class ContactCase:
         m = self.mat
         A, B, n, C, e0, mm, Tm, Tt = m.jc
         Ep = m.E * m.Et / (m.E - m.Et) if self.model == BILINEAR else 0.0
-        return np.array([m.E, m.sy0, Ep, A, B, n, C, mm, self.friction, 0.1 * m.E / self.h])
+        # PFAC: the Fraser law's dimensionless factor (0.6, the reference inputs'
+        # penaltyFactor) or the area law's pressure per length 0.1 E / h
+        pfac = 0.6 if self.stiffness == "penalty" else 0.1 * m.E / self.h
+        return np.array([m.E, m.sy0, Ep, A, B, n, C, mm, self.friction, pfac])
 
     def scale(self) -> np.ndarray:
         """Step sizes for parameters whose nominal value is 0 (Ep of JC particles)."""
@@ -129,15 +136,20 @@ def build(dom, case: ContactCase, theta) -> int:
     dens = int(round(2 * half / case.dx))
     zp = z_top + h + case.gap
     mesh = dom.add_rigid_plane(2, False, (-half, -half, zp), (half, half, zp), dens, 10)
-    dom.add_velocity_bc(10, (0.0, 0.0, case.v_punch))
+    dom.add_velocity_bc(10, (case.v_slide, 0.0, case.v_punch))
     dom.set("contact", 1)
     dom.set_f64("friction_sta", mu)
     dom.set_f64("friction_dyn", mu)
     if case.stiffness == "wang":
         dom.set("contact_alg", CONTACT_WANG)
-    else:
+    elif case.stiffness == "penalty":
+        dom.set("contact_alg", CONTACT_PENALTY)
+        dom.set_f64("PFAC", pfac)
+    elif case.stiffness == "area":
         dom.set("contact_alg", CONTACT_AREA)
         dom.set_f64("PFAC", pfac)
+    else:
+        raise ValueError(f"unknown contact stiffness law {case.stiffness!r}")
     if case.thermal:
         dom.set("thermal_solver", 1)
         dom.set("pl_heating", 1)
@@ -230,14 +242,17 @@ def __getattr__(name):
     raise AttributeError(name)
 
 
-def central_fd(problem: Problem, rel: float = 1e-6) -> np.ndarray:
+def central_fd(problem: Problem, rel: float = 1e-6, only=None) -> np.ndarray:
     """Central differences of the (scaled) loss in u, step rel * theta0 / scale.
     A parameter whose nominal value is 0 (Ep of Johnson-Cook particles) gets a
     forward difference: a negative Ep is replaced by E in the step
-    (Particle.cpp:1012-1013), a jump no difference may straddle."""
+    (Particle.cpp:1012-1013), a jump no difference may straddle.  ``only``
+    (parameter names) restricts the differences to those; the rest stay 0."""
     g = np.zeros(len(PARAMS))
     base = None
     for p in range(len(PARAMS)):
+        if only is not None and PARAMS[p] not in only:
+            continue
         du = np.zeros(len(PARAMS))
         if problem.theta0[p] != 0:
             step = rel * abs(problem.theta0[p]) / problem.scl[p]

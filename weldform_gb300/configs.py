@@ -8,8 +8,10 @@ used for parity tests and throughput numbers:
   BCs, Source/WeldForm.cpp:51-120), bilinear or Johnson-Cook material, cubic
   spline with h = 1.2 dx, Monaghan viscosity alpha = 1, dt = 0.4 h / Cs.
 * ``contact_upsetting`` — the same cylinder pressed by a rigid plane
-  (TriMesh::AxisPlaneMesh) moving down, Wang penalty contact with Coulomb
-  friction, Johnson-Cook flow stress, conduction and plastic-work heating.
+  (TriMesh::AxisPlaneMesh) moving down (optionally also sliding along x),
+  penalty contact with Coulomb friction (Wang's 2 m / dt^2, the Fraser
+  PFAC * cont_stiff law or an area penalty), Johnson-Cook flow stress,
+  conduction and plastic-work heating.
 
 Positions receive a seeded, counter-based jitter of +-1e-3 dx per coordinate
 (splitmix64 of (seed, particle, axis)), identical for every implementation
@@ -24,7 +26,7 @@ from typing import Optional
 
 import numpy as np
 
-from . import BILINEAR, JOHNSON_COOK, CONTACT_WANG, CONTACT_AREA
+from . import BILINEAR, HOLLOMON, JOHNSON_COOK, CONTACT_WANG, CONTACT_PENALTY, CONTACT_AREA
 
 SEED = 20261203
 _M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
@@ -58,6 +60,10 @@ class Steel:
     Et: float = 1.5e9
     # Johnson-Cook [A, B, n, C, eps_0, m, T_m, T_t]
     jc: tuple = (350e6, 275e6, 0.36, 0.022, 1.0, 1.0, 1793.0, 300.0)
+    # Hollomon with plateau [K, m] (sigma_y = K (eps_p + eps0)^m past eps1,
+    # eps0 = sy0 / E, eps1 = (sy0 / K)^(1/m); Material.cpp:48-64): with
+    # sy0 = 300 MPa the plateau ends at eps_p = eps1 - eps0 = 9.3e-4
+    hollomon: tuple = (1.0e9, 0.2)
     k_T: float = 50.0
     cp_T: float = 460.0
     T0: float = 300.0
@@ -130,6 +136,11 @@ def _material_setup(dom, mat: Steel, model: int):
         Ep = mat.E * mat.Et / (mat.E - mat.Et)  # WeldForm.cpp:264
         dom.set_particles("Ep", Ep)
         dom.set_particles("Sigmay", mat.sy0)
+    elif model == HOLLOMON:
+        K, m = mat.hollomon
+        mid = dom.add_material(HOLLOMON, [mat.E, mat.nu, mat.sy0, K, m])
+        dom.set_particles("Material_model", HOLLOMON)
+        dom.set_particles("Sigmay", mat.sy0)  # the plateau's flow stress; Ep stays 0 (Particle.cpp:78)
     else:
         A, B, n, C, e0, m, Tm, Tt = mat.jc
         mid = dom.add_material(JOHNSON_COOK, [mat.E, mat.nu, A, B, n, C, e0, m, Tm, Tt])
@@ -151,19 +162,22 @@ def _material_setup(dom, mat: Steel, model: int):
 
 def cylinder_upsetting(dom, R: float = 0.010, L: float = 0.030, dx: float = 0.001, v_top: float = -1.0,
                        model: int = BILINEAR, mat: Optional[Steel] = None, jitter_amp: float = 1e-3,
-                       seed: int = SEED, thermal: bool = False, cfl: float = 0.4) -> Case:
-    """Cylinder upsetting: bottom two layers fixed, top two layers at v_top (z)."""
+                       seed: int = SEED, thermal: bool = False, cfl: float = 0.4,
+                       V: tuple = (0.0, 0.0, 0.0)) -> Case:
+    """Cylinder upsetting: bottom two layers fixed, top two layers at v_top (z).
+    V is the cylinder's base centre (AddCylinderLength's V)."""
     mat = mat or Steel()
     h = 1.2 * dx
     dom.Kernel_Set(0)
-    dom.AddCylinderLength(0, (0.0, 0.0, 0.0), R, L, dx / 2, mat.rho, h, False)
+    dom.AddCylinderLength(0, tuple(V), R, L, dx / 2, mat.rho, h, False)
     n = dom.particle_count
     x = dom.get_array("x")
     if jitter_amp:
         x = x + jitter(n, dx, jitter_amp, seed)
         dom.set_array("x", x)
-    dom.AssignZone((-1.0, -1.0, -1.0), (1.0, 1.0, 2 * dx), 2)
-    dom.AssignZone((-1.0, -1.0, L - 3 * dx), (1.0, 1.0, 1.0), 3)
+    lo, hi = -1.0 + min(V), 1.0 + max(V)
+    dom.AssignZone((lo, lo, lo), (hi, hi, V[2] + 2 * dx), 2)
+    dom.AssignZone((lo, lo, V[2] + L - 3 * dx), (hi, hi, hi), 3)
     dom.add_velocity_bc(2, (0.0, 0.0, 0.0))
     dom.add_velocity_bc(3, (0.0, 0.0, v_top))
     _material_setup(dom, mat, model)
@@ -177,35 +191,50 @@ def cylinder_upsetting(dom, R: float = 0.010, L: float = 0.030, dx: float = 0.00
 def contact_upsetting(dom, R: float = 0.010, L: float = 0.030, dx: float = 0.0002, v_punch: float = -1.0,
                       mat: Optional[Steel] = None, friction: float = 0.2, stiffness: str = "wang",
                       jitter_amp: float = 1e-3, seed: int = SEED, thermal: bool = True, cfl: float = 0.4,
-                      gap: float = 0.0) -> Case:
+                      gap: float = 0.0, v_slide: float = 0.0, pfac: Optional[float] = None,
+                      V: tuple = (0.0, 0.0, 0.0)) -> Case:
     """Rigid top plane pressing a Johnson-Cook cylinder with conduction and
-    plastic-work heating; bottom two layers fixed."""
+    plastic-work heating; bottom two layers fixed.
+
+    stiffness: "wang" (kij = 2 m / dt^2, Contact_Wang.cpp:187), "penalty"
+    (kij = PFAC * cont_stiff, cont_stiff = 9 K G / (3 K + G) dS, Contact.cpp:423
+    and SolverKickDrift.cpp:79-84; PFAC default 0.6, the penaltyFactor of the
+    reference's contact inputs) or "area" (0.1 E / h read as a pressure per
+    length times the contact area (m / rho)^(2/3)).  v_slide moves the plane
+    along x as well, so the contact pairs slide and reach the dynamic-friction
+    branch (Contact_Wang.cpp:284-290).  V is the cylinder's base centre."""
     mat = mat or Steel()
     h = 1.2 * dx
     dom.Kernel_Set(0)
-    dom.AddCylinderLength(0, (0.0, 0.0, 0.0), R, L, dx / 2, mat.rho, h, False)
+    dom.AddCylinderLength(0, tuple(V), R, L, dx / 2, mat.rho, h, False)
     n = dom.particle_count
     x = dom.get_array("x")
     if jitter_amp:
         x = x + jitter(n, dx, jitter_amp, seed)
         dom.set_array("x", x)
-    dom.AssignZone((-1.0, -1.0, -1.0), (1.0, 1.0, 2 * dx), 2)
+    lo, hi = -1.0 + min(V), 1.0 + max(V)
+    dom.AssignZone((lo, lo, lo), (hi, hi, V[2] + 2 * dx), 2)
     dom.add_velocity_bc(2, (0.0, 0.0, 0.0))
     _material_setup(dom, mat, JOHNSON_COOK)
     z_top = float(x[:, 2].max())
     half = R + 2 * dx
     dens = int(round(2 * half / dx))
     zp = z_top + h + gap  # contact engages as the plane closes the last h
-    mesh = dom.add_rigid_plane(2, False, (-half, -half, zp), (half, half, zp), dens, 10)
-    dom.add_velocity_bc(10, (0.0, 0.0, v_punch))
+    mesh = dom.add_rigid_plane(2, False, (V[0] - half, V[1] - half, zp), (V[0] + half, V[1] + half, zp), dens, 10)
+    dom.add_velocity_bc(10, (v_slide, 0.0, v_punch))
     dom.set("contact", 1)
     dom.set_f64("friction_sta", friction)
     dom.set_f64("friction_dyn", friction)
     if stiffness == "wang":
         dom.set("contact_alg", CONTACT_WANG)
-    else:  # 0.1 E / h read as a pressure per length, times the contact area
+    elif stiffness == "penalty":
+        dom.set("contact_alg", CONTACT_PENALTY)
+        dom.set_f64("PFAC", 0.6 if pfac is None else pfac)
+    elif stiffness == "area":  # 0.1 E / h read as a pressure per length, times the contact area
         dom.set("contact_alg", CONTACT_AREA)
-        dom.set_f64("PFAC", 0.1 * mat.E / h)
+        dom.set_f64("PFAC", 0.1 * mat.E / h if pfac is None else pfac)
+    else:
+        raise ValueError(f"unknown contact stiffness law {stiffness!r}")
     if thermal:
         dom.set("thermal_solver", 1)
         dom.set("pl_heating", 1)

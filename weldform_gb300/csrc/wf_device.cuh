@@ -37,20 +37,24 @@ enum F64Col : int {
   C_PR2 = 91,              // Pressure / Density^2
   C_TI = 92, C_TIN, C_TIDIST,  // tensile instability: TI, TIn, TIInitDist (Particle.h:146-149)
   C_GCM = 95,              // kernel-gradient correction matrix gradCorrM (9, row-major)
-  NF64_PERSIST = 104,
+  C_TINF = 104,            // convection: T_inf, h_conv and the last q_conv (Particle.h:187)
+  C_HCONV = 105,
+  C_QCONV = 106,
+  NF64_PERSIST = 107,
   // scratch columns (not permuted): next-step buffers and the
   // tensile-instability stress TIR (6), recomputed at every step start
-  C_XN = 104, C_VN = 107, C_RHON = 110, C_MRHON = 111, C_TIR = 112,
-  C_PR2N = 118,            // next-step Pressure / Density^2 (plain form; read by the fused rate gather)
-  C_TN = 119,              // next-step temperature (plain form)
-  NF64 = 120
+  C_XN = 107, C_VN = 110, C_RHON = 113, C_MRHON = 114, C_TIR = 115,
+  C_PR2N = 121,            // next-step Pressure / Density^2 (plain form; read by the fused rate gather)
+  C_TN = 122,              // next-step temperature (plain form)
+  NF64 = 123
 };
 enum I32Col : int {
   I_ID = 0, I_IDORIG, I_NWS, I_MAT, I_MODEL, I_FAIL, I_MATERIAL, I_NB, I_KIND, I_ELEM, I_MESH, I_ORIG,
-  NI32_PERSIST = 12,
-  I_CELL = 12,             // scratch: cell key (Morton rank) of the particle at its pre-search position
-  I_CLASS = 13,            // scratch: pair-rule class word in sorted order
-  NI32 = 14
+  I_THBC = 12,             // Thermal_BC (Particle.h:69): 1 = convection (TH_BC_CONVECTION)
+  NI32_PERSIST = 13,
+  I_CELL = 13,             // scratch: cell key (Morton rank) of the particle at its pre-search position
+  I_CLASS = 14,            // scratch: pair-rule class word in sorted order
+  NI32 = 15
 };
 
 // ---- float4 field groups of the mixed form -----------------------------------
@@ -61,12 +65,17 @@ enum I32Col : int {
 // lines — better than one column per field (more load instructions) and
 // better than one record per particle (one line per lane).  Positions,
 // velocities and temperature are float-float pairs (hi = fl(v),
-// lo = fl(v - hi)): the difference of two pairs gives x_i - x_j to FP32
-// accuracy even when |x| >> |x_i - x_j|.  The six low halves of x and v
-// share one group as bf16 values (lo_pack in wf_step_common.cuh): |lo| is at
-// most half an FP32 ulp of hi, so 8 mantissa bits keep it to ~2^-9 of its
-// size, far below the FP32 rounding of the pair difference, and a gather
-// reads three groups per neighbour for x and v instead of four.
+// lo = fl(v - hi)); positions are stored relative to a fixed origin O (the
+// cell grid's centre), which leaves every difference unchanged.  The six low
+// halves of x and v share one group as bf16 values (lo_pack in
+// wf_step_common.cuh), so a gather reads three groups per neighbour for x and
+// v instead of four.  |lo| is at most half an FP32 ulp of hi and keeps 8
+// significant bits, so the difference of two pairs, (hi_i - hi_j) +
+// (lo_i - lo_j), carries an absolute error of at most about 2^-33 |x - O|
+// besides its FP32 rounding: for a domain of half-extent D that is
+// 1.2e-10 D / |x_ij| relative (2e-8 for D = 30 mm at a 0.2 mm spacing, below
+// the 6e-8 of the FP32 rounding itself), wherever the domain sits.  A
+// velocity difference carries about 2^-33 |v| in the same way.
 enum RecCur : int {        // current-state groups
   RC_XH = 0,               // x hi (xyz), h
   RC_L = 1,                // x lo, v lo (bf16 pairs), m/rho
@@ -181,6 +190,8 @@ struct StepState {
                        // searches clear it)
   int errors;
   int surface_count;
+  unsigned long long dyn_friction;  // contact-pair evaluations that took the dynamic-friction branch
+  int nan_count;       // particles with a non-finite position at the last search
 };
 
 // Per-domain constants (set once at the solver prologue; small, by value).
@@ -189,6 +200,7 @@ struct DomainConst {
   double Cellfac, hmax, dt;
   double BLPF[3], CellSize[3];
   int CellNo[3];
+  double rec_origin[3];  // the mixed form's position records hold x - rec_origin (the cell grid's centre)
   int ncells;
   float pre_eps;       // relative margin of the FP32 neighbour prefilter
   float cell_skip_r2;  // (Cellfac * hmax + FP32 rounding margin)^2: cells farther hold no neighbour
@@ -215,6 +227,7 @@ struct DomainConst {
   float mass_f;        // that mass (the mixed rate gather's kinetic-energy term)
   int stage_cap;       // halo capacity of the staged gathers (0: staging off)
   int freeze_nb;       // 1: neighbour and contact topology searched only at the first step
+  int nan_check;       // 1: a non-finite position at a search, or non-finite energy sums, raise ERR_NAN
 };
 
 // Device pointers, passed by value to every kernel.

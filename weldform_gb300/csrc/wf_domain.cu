@@ -81,7 +81,7 @@ int col_f64(const std::string& n, int* ncomp) {
       {"dint_energy_dt", C_DINT, 1}, {"dDensity", C_DRHO, 1}, {"TI", C_TI, 1}, {"TIn", C_TIN, 1},
       {"TIInitDist", C_TIDIST, 1}, {"TIR", C_TIR, 6}, {"gradCorrM", C_GCM, 9}, {"Sigma", C_SIG, 6}, {"ShearStress", C_TAU, 6},
       {"Strain", C_EPS, 6}, {"Strain_pl", C_EPL, 6}, {"Strain_pl_incr", C_EPLI, 6}, {"StrainRate", C_SR, 6},
-      {"RotationRate", C_RR, 3}};
+      {"RotationRate", C_RR, 3}, {"T_inf", C_TINF, 1}, {"h_conv", C_HCONV, 1}, {"q_conv", C_QCONV, 1}};
   for (const E& e : tab)
     if (n == e.n) { *ncomp = e.k; return e.c; }
   return -1;
@@ -94,6 +94,7 @@ int col_i32(const std::string& n) {
   if (n == "Fail") return I_FAIL;
   if (n == "Material") return I_MATERIAL;
   if (n == "Nb") return I_NB;
+  if (n == "Thermal_BC") return I_THBC;
   return -1;
 }
 // Fields that exist in the reference but are fixed in this build's scope.
@@ -125,6 +126,7 @@ struct wf_domain {
   double DomMax[3] = {-100000000000.0, -100000000000.0, -100000000000.0};
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int freeze_nb = 0;  // search only at the first step (finite-difference checks of the adjoint)
+  int nan_check = 0;  // raise WF_ERR_NAN on a non-finite position at a search or non-finite energy sums
   int ts_nb_inc = 5, pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1, contact_alg = 0;
   int precision = WF_PRECISION_FP64, use_graph = 1, device = 0;
   int integrator = 0;  // 0 kick-drift, 1 leapfrog
@@ -433,7 +435,7 @@ struct wf_domain {
       cs[d] = (TRPR[d] - BLPF[d]) / CellNo[d];
       ncells *= CellNo[d];
     }
-    if (ncells > (1LL << 30)) throw CudaError{WF_ERR_UNSUPPORTED, "cell grid too large"};
+    if (ncells > (1LL << 29)) throw CudaError{WF_ERR_UNSUPPORTED, "cell grid too large"};
     // Morton rank of each cell (linear index (i * ny + j) * nz + k).
     std::vector<std::pair<uint64_t, int>> mc((size_t)ncells);
     for (int a = 0; a < CellNo[0]; ++a)
@@ -478,8 +480,9 @@ struct wf_domain {
       CK(cudaStreamSynchronize(stream));  // the host vector dies at the end of this scope
       P.cell_lin = clin;
     }
-    P.cell_start = dalloc<int>(ncells + 1);
-    P.cell_count = dalloc<int>(ncells);
+    // grid cells, then as many shadow buckets for particles with a non-finite position
+    P.cell_start = dalloc<int>(2 * ncells + 1);
+    P.cell_count = dalloc<int>(2 * ncells);
     P.perm = dalloc<int>(n);
     P.inv = dalloc<int>(n);
     P.xs = dalloc<float>(4 * n);
@@ -578,6 +581,8 @@ struct wf_domain {
     K.N = N; K.Nsolid = solid_part_count; K.nbc_particles = (int)bl.size();
     K.Cellfac = Cellfac; K.hmax = hmax; K.dt = dt;
     for (int d = 0; d < 3; ++d) { K.BLPF[d] = BLPF[d]; K.CellSize[d] = cs[d]; K.CellNo[d] = CellNo[d]; }
+    // origin of the mixed form's position records: the cell grid's centre
+    for (int d = 0; d < 3; ++d) K.rec_origin[d] = BLPF[d] + 0.5 * CellNo[d] * cs[d];
     {
       // Largest pair radius plus a margin over the FP32 rounding of the
       // prefilter coordinates x - BLPF (the grid's extent at most; clamped
@@ -599,6 +604,7 @@ struct wf_domain {
     double eps = 4.0 * std::sqrt(3.0) * std::ldexp(1.0, -23) * (2.0 * ext) / R + 20.0 * std::ldexp(1.0, -24);
     K.pre_eps = (float)(eps < 0.05 ? std::max(eps, 1e-5) : 2.0);
     K.freeze_nb = freeze_nb;
+    K.nan_check = nan_check;
     K.ts_nb_inc = ts_nb_inc; K.pl_heating = pl_heating; K.thermal_solver = thermal_solver; K.contact = contact;
     K.contact_mesh_auto_update = contact_mesh_auto_update; K.contact_alg = contact_alg;
     K.pl_work_heat_frac = pl_work_heat_frac; K.friction_sta = friction_sta; K.friction_dyn = friction_dyn;
@@ -622,7 +628,7 @@ struct wf_domain {
     K.pblock = pblock_now();
     K.nblocks = (N + K.pblock - 1) / K.pblock;
     P.partials = dalloc<double>((size_t)NSLOTS * ((N + 63) / 64));  // room for the smallest block size
-    P.scan_tmp = dalloc<long long>((ncells + 4095) / 4096 + 1);
+    P.scan_tmp = dalloc<long long>((2 * ncells + 4095) / 4096 + 1);
     // Step state.
     StepState st;
     memset(&st, 0, sizeof(st));
@@ -671,6 +677,8 @@ struct wf_domain {
     if (st.errors & wf::ERR_NBR_OVERFLOW) throw CudaError{WF_ERR_NBR_OVERFLOW, "a particle has more than 100 neighbours (MAX_NB_PER_PART)"};
     if (st.errors & wf::ERR_CONTACT_OVERFLOW) throw CudaError{WF_ERR_NBR_OVERFLOW, "a particle has more than 64 contact pairs"};
     if (st.errors & wf::ERR_TIMEOUT) throw CudaError{WF_ERR_TIMEOUT, "a bounded device wait gave up"};
+    if (st.errors & wf::ERR_NAN)
+      throw CudaError{WF_ERR_NAN, "non-finite state: a particle position at a neighbour search, or the energy sums"};
     if (contact && st.nb_searches > 0 && st.surface_count == 0)
       throw CudaError{WF_ERR_STATE, "No external particles found. Please check particle masses"};
   }
@@ -910,6 +918,12 @@ struct wf_domain {
       get_f64(C_EP, 1, ep.data());
       for (double e : ep)
         if (e < 0.0) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: particles with Ep < 0 are not supported"};
+      if (thermal_solver) {
+        std::vector<int> bc(n);
+        get_i32(I_THBC, bc.data());
+        for (int b : bc)
+          if (b == 1) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: convection boundary conditions are not supported"};
+      }
     }
     use_device();
     if (use_graph && (!graph || graph_precision != precision || graph_block != graph_key())) step(0);
@@ -1294,6 +1308,7 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   if (d->prepared) return set_err(WF_ERR_STATE, "domain fields are fixed after the prologue");
   if (n == "ts_nb_inc") { if (v < 1) return set_err(WF_ERR_ARG, "ts_nb_inc >= 1"); d->ts_nb_inc = v; }
   else if (n == "freeze_neighbours") d->freeze_nb = v != 0;
+  else if (n == "nan_check") d->nan_check = v != 0;
   else if (n == "pl_heating") d->pl_heating = v;
   else if (n == "thermal_solver") d->thermal_solver = v;
   else if (n == "contact") d->contact = v;
@@ -1362,6 +1377,8 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     if (n == "steps") *v = st.steps;
     else if (n == "pair_count") *v = st.pair_count / 2;
     else if (n == "contact_pair_count") *v = st.contact_pair_count;
+    else if (n == "dynamic_friction_count") *v = (int64_t)st.dyn_friction;
+    else if (n == "nan_particles") *v = st.nan_count;
     else if (n == "nb_searches") *v = st.nb_searches;
     else if (n == "surface_count") *v = st.surface_count;
     else return set_err(WF_ERR_ARG, "unknown domain i32 read " + n);
@@ -1433,6 +1450,8 @@ int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value) {
   }
   if (f == "Fail" && value > 1) return set_err(WF_ERR_UNSUPPORTED, "Undefined failure criteria for solids");
   if (f == "Material_model" && (value < 0 || value > 2)) return set_err(WF_ERR_UNSUPPORTED, "material model");
+  if (f == "Thermal_BC" && (value < 0 || value > 1))
+    return set_err(WF_ERR_UNSUPPORTED, "Thermal_BC: only TH_BC_NONE (0) and TH_BC_CONVECTION (1)");
   for (int p = 0; p < d->hp.N; ++p)
     if (zone < 0 || d->hp.i[wf::I_ID][p] == zone) {
       d->hp.i[c][p] = value;
@@ -1509,6 +1528,8 @@ int wf_set_particle_array_i32(wf_domain* d, const char* field, const int32_t* sr
     int v = src[p];
     if (f == "Fail" && v > 1) return set_err(WF_ERR_UNSUPPORTED, "Undefined failure criteria for solids");
     if (f == "Material_model" && (v < 0 || v > 2)) return set_err(WF_ERR_UNSUPPORTED, "material model");
+    if (f == "Thermal_BC" && (v < 0 || v > 1))
+      return set_err(WF_ERR_UNSUPPORTED, "Thermal_BC: only TH_BC_NONE (0) and TH_BC_CONVECTION (1)");
   }
   for (int p = 0; p < d->hp.N; ++p) {
     d->hp.i[c][p] = c == wf::I_NWS ? (src[p] ? 1 : 0) : src[p];

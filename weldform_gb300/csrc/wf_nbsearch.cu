@@ -30,21 +30,41 @@ namespace wf {
 
 __device__ __forceinline__ bool searching(const DevPtrs& P) { return P.st->do_search != 0; }
 
+// A particle with a non-finite coordinate cannot pass CheckRadius with any
+// other (its distance is NaN or infinite), so its row is empty and it is in
+// no other row.  The reference bins it into a clamped edge cell
+// (Neighbour.cpp:185-218), where every later search scans all such particles
+// pairwise.  Here it goes to one of ncells shadow buckets after the grid's
+// (key ncells + original index mod ncells), which no stencil visits: the rows
+// are the same and the search stays linear.  The shadow buckets are sorted
+// like cells, so the order stays deterministic.
 __global__ void k_cell_keys(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
+  int nonfinite = 0;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
   int c[3];
+  bool finite = true;
   for (int d = 0; d < 3; ++d) {
     double xd = P.f[(C_X + d) * (size_t)K.N + p];
+    finite = finite && isfinite(xd);
     int q = (int)floor(__ddiv_rn(__dsub_rn(xd, K.BLPF[d]), K.CellSize[d]));
     if (q < 0) q = 0;
     if (q >= K.CellNo[d]) q = K.CellNo[d] - 1;
     c[d] = q;
   }
-  int lin = (c[0] * K.CellNo[1] + c[1]) * K.CellNo[2] + c[2];
-  int key = P.cell_rank[lin];
+  int key;
+  if (finite) {
+    key = P.cell_rank[(c[0] * K.CellNo[1] + c[1]) * K.CellNo[2] + c[2]];
+  } else {
+    key = K.ncells + P.i[I_ORIG * (size_t)K.N + p] % K.ncells;
+    ++nonfinite;
+  }
   P.i[I_CELL * (size_t)K.N + p] = key;
   atomicAdd(&P.cell_count[key], 1);
+  }
+  if (nonfinite) {
+    atomicAdd(&P.st->nan_count, nonfinite);
+    if (K.nan_check) atomicOr(&P.st->errors, ERR_NAN);
   }
 }
 
@@ -133,10 +153,11 @@ __global__ void k_scatter(DevPtrs P, DomainConst K) {
 }
 
 // Order each cell's slots by original particle index (insertion sort; cells
-// hold ~10-20 particles).
+// hold ~10-20 particles), and likewise the shadow buckets of non-finite
+// particles (at most ceil(N / ncells) each).
 __global__ void k_sort_cells(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < K.ncells; c += gridDim.x * blockDim.x) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < 2 * K.ncells; c += gridDim.x * blockDim.x) {
   int b = P.cell_start[c], e = P.cell_start[c + 1];
   const int* orig = P.i + I_ORIG * (size_t)K.N;
   for (int k = b + 1; k < e; ++k) {
@@ -271,12 +292,14 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   int* ridx = &s_idx[row][0];
   int cnt = 0, split = 0;
   bool overflow = false;
-  if (i < K.N && kind[i] == 0) {
+  // A particle in a shadow bucket (non-finite position) has an empty row.
+  const int key_i = i < K.N ? P.i[I_CELL * N + P.perm[i]] : 0;
+  if (i < K.N && kind[i] == 0 && key_i < K.ncells) {
     float4 pi = reinterpret_cast<const float4*>(P.xs)[i];
     // The particle's cell: the key it was sorted by (k_cell_keys evaluated the
     // reference's FP64 cell formula once per particle), mapped back to grid
     // coordinates.
-    int lin = P.cell_lin[P.i[I_CELL * N + P.perm[i]]];
+    int lin = P.cell_lin[key_i];
     int c[3] = {lin / (K.CellNo[1] * K.CellNo[2]), (lin / K.CellNo[2]) % K.CellNo[1], lin % K.CellNo[2]};
     int idi = ID[i], oi = orig[i], mi = material[i];
     bool ci = K.contact && is_contact_id(K, idi);
@@ -500,6 +523,7 @@ __global__ void k_search_begin(DevPtrs P) {
   P.st->pair_count = 0;
   P.st->contact_pair_count = 0;
   P.st->surface_count = 0;
+  P.st->nan_count = 0;
   P.st->nb_searches += 1;
 }
 
@@ -513,25 +537,27 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   // not search, each launch is a handful of blocks that exit at once.
   const int G = 152 * 4;
   auto grid = [&](long long n) { int b = nblk(n, T); return b < G ? b : G; };
-  int nz = grid(K.ncells);
+  // buckets: ncells grid cells (Morton ranks), then ncells shadow buckets
+  const long long nbk = 2LL * K.ncells;
+  int nz = grid(nbk);
   k_search_begin<<<1, 1, 0, s>>>(P);
   mark(s, "k_search_begin");
-  k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, K.ncells, 1);
+  k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, nbk, 1);
   mark(s, "k_zero_int");
   k_cell_keys<<<grid(K.N), T, 0, s>>>(P, K);
   mark(s, "k_cell_keys");
-  int nb = nblk(K.ncells, SCAN_TILE);
-  k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(P, P.cell_count, K.ncells, P.scan_tmp);
+  int nb = nblk(nbk, SCAN_TILE);
+  k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(P, P.cell_count, nbk, P.scan_tmp);
   mark(s, "k_scan_reduce");
   k_scan_top<<<1, SCAN_THREADS, 0, s>>>(P, P.scan_tmp, nb);
   mark(s, "k_scan_top");
-  k_scan_down<<<nb, SCAN_THREADS, 0, s>>>(P, P.cell_count, K.ncells, P.scan_tmp, P.cell_start, P.cell_start + K.ncells);
+  k_scan_down<<<nb, SCAN_THREADS, 0, s>>>(P, P.cell_count, nbk, P.scan_tmp, P.cell_start, P.cell_start + nbk);
   mark(s, "k_scan_down");
-  k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, K.ncells, 1);
+  k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, nbk, 1);
   mark(s, "k_zero_int");
   k_scatter<<<grid(K.N), T, 0, s>>>(P, K);
   mark(s, "k_scatter");
-  k_sort_cells<<<grid(K.ncells), T, 0, s>>>(P, K);
+  k_sort_cells<<<grid(nbk), T, 0, s>>>(P, K);
   mark(s, "k_sort_cells");
   k_permute<<<152 * 4, 512, 0, s>>>(P, K, fscratch, iscratch);
   mark(s, "k_permute");

@@ -103,6 +103,20 @@ __device__ __forceinline__ double amp_value(const DomainTables* T, int amp_id, d
   return 0.0;
 }
 
+// CalcConvHeat (Thermal.cpp:339-389, 3D; Fraser Eq. 3-121): a particle with
+// Thermal_BC == TH_BC_CONVECTION exchanges heat with the ambient temperature
+// T_inf through its contact area dS^2 = (m / rho)^(2/3):
+// q_conv = rho h_conv dS^2 (T_inf - T) / m, at the step's updated density and
+// temperature.  Other particles keep their q_conv (0 from the constructor).
+__device__ __forceinline__ double conv_heat(const DevPtrs& P, size_t N, int i, double rho, double T) {
+  if (P.i[(size_t)I_THBC * N + i] != 1) return col(P, C_QCONV, N, i);
+  double m = col(P, C_MASS, N, i);
+  double dS2 = pow(m / rho, 2.0 / 3.0);
+  double q = rho * col(P, C_HCONV, N, i) * dS2 * (col(P, C_TINF, N, i) - T) / m;
+  colw(P, C_QCONV, N, i) = q;
+  return q;
+}
+
 // Johnson-Cook flow stress (Source/Material.cpp:6-25).
 __device__ __forceinline__ double jc_yield(const MaterialDev& M, double strain, double strain_rate, double temp) {
   double T_h = (temp - M.T_t) / (M.T_m - M.T_t);

@@ -396,7 +396,8 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
             double ntg = norm3(tg), ncf = norm3(cf);
             if (ntg < K.friction_sta * ncf) {
               for (int d = 0; d < 3; ++d) { double q = tg[d] / m1; cf[d] -= q; a[d] -= q; }
-            } else {
+            } else {  // dynamic branch (Contact_Wang.cpp:284-290)
+              atomicAdd(&P.st->dyn_friction, 1ull);
               double fs = K.friction_dyn * ncf;
               for (int d = 0; d < 3; ++d) { double td = fs * tg[d] / ntg; cf[d] -= td; a[d] -= td / m1; }
             }
@@ -651,7 +652,8 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
         maxT = T; minT = T;
         // CalcTempInc's dTdt and CalcThermalExpStrainRate (after the stress)
         double f = 1. / (rho * col(P, C_CPT, N, i));
-        double dTdt = f * (cond + 0.0 + col(P, C_QSRC, N, i) + qpl * K.pl_work_heat_frac + 0.0);
+        double qconv = conv_heat(P, N, i, rho, T);
+        double dTdt = f * (cond + qconv + col(P, C_QSRC, N, i) + qpl * K.pl_work_heat_frac + 0.0);
         colw(P, C_DTDT, N, i) = dTdt;
         double st = col(P, C_THEXP, N, i) * dTdt;
         for (int c = 0; c < 3; ++c) { sre[c] = sre[c] + st; colw(P, C_SR + c, N, i) = sre[c]; }
@@ -707,8 +709,14 @@ __global__ void k_finalize(DevPtrs P, DomainConst K) {
   StepState* st = P.st;
   double dt = st->deltat;
   switch (slot) {
-    case S_DINT: st->int_energy_sum += v * dt; break;
-    case S_DKIN: st->kin_energy_sum += v * dt; break;
+    case S_DINT:
+      st->int_energy_sum += v * dt;
+      if (K.nan_check && !isfinite(v)) atomicOr(&st->errors, ERR_NAN);
+      break;
+    case S_DKIN:
+      st->kin_energy_sum += v * dt;
+      if (K.nan_check && !isfinite(v)) atomicOr(&st->errors, ERR_NAN);
+      break;
     case S_PLW: st->plastic_work += v * dt; break;
     case S_MAXPL: st->max_pl_next = v; break;
     case S_MAXT: st->m_maxT = v > 0.0 ? v : 0.0; break;

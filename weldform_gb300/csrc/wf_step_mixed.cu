@@ -7,9 +7,12 @@
 //    coalesce across the warp's consecutive particles, instead of one scalar
 //    load from each of ~20 separate columns;
 //  * relative positions, velocities and temperatures come from float-float
-//    pairs, (hi_i - hi_j) + (lo_i - lo_j): accurate to FP32 rounding of the
-//    difference itself — the accuracy of an FP64 difference cast to FP32 —
-//    with FP32 instructions only (GB300 issues FP64 at 1/72 of its FP32 rate);
+//    pairs, (hi_i - hi_j) + (lo_i - lo_j), with FP32 instructions only (GB300
+//    issues FP64 at 1/72 of its FP32 rate).  Temperature low halves are FP32,
+//    which gives the FP32 rounding of the FP64 difference; position and
+//    velocity low halves are bf16, which adds at most ~2^-33 |x - O| (O the
+//    records' origin, the cell grid's centre) or ~2^-33 |v| to the difference
+//    (the bound is in wf_device.cuh beside the record layout);
 //  * kernel gradients, viscosity and pair terms in FP32, every per-particle
 //    pair sum Kahan-compensated;
 //  * FP64 stays in position/velocity/density/temperature integration, the
@@ -94,7 +97,7 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
   double c2 = solid ? 1.0 / (rho * rho) : 0.0;
   float xh[3], xl[3], vh[3], vl[3], th, tl;
   for (int d = 0; d < 3; ++d) {
-    ff_split(col(P, C_X + d, N, i), xh[d], xl[d]);
+    ff_split(col(P, C_X + d, N, i) - K.rec_origin[d], xh[d], xl[d]);
     ff_split(col(P, C_V + d, N, i), vh[d], vl[d]);
   }
   ff_split(col(P, C_T, N, i), th, tl);
@@ -426,7 +429,7 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
     double vn = K.leapfrog ? v : v + col(P, C_A + d, N, i) * dt / 2.;
     colw(P, C_XN + d, N, i) = xn;
     colw(P, C_VN + d, N, i) = vn;
-    ff_split(xn, nxh[d], nxl[d]);
+    ff_split(xn - K.rec_origin[d], nxh[d], nxl[d]);
     ff_split(vn, nvh[d], nvl[d]);
   }
   // Pressure of the updated density (EOS case 0, Functions.cpp:206-212) and the
@@ -684,7 +687,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
         colw(P, C_T, N, i) = T;
         maxT = T; minT = T;
         double f = 1. / (rho * col(P, C_CPT, N, i));
-        double dTdt = f * (col(P, C_DINT, N, i) + col(P, C_QSRC, N, i) + col(P, C_QPL, N, i) * K.pl_work_heat_frac);
+        double qconv = conv_heat(P, N, i, rho, T);
+        double dTdt = f * (col(P, C_DINT, N, i) + qconv + col(P, C_QSRC, N, i) + col(P, C_QPL, N, i) * K.pl_work_heat_frac);
         colw(P, C_DTDT, N, i) = dTdt;
         double st = col(P, C_THEXP, N, i) * dTdt;  // CalcThermalExpStrainRate
         for (int c = 0; c < 3; ++c) srd[c] = srd[c] + st;
