@@ -20,7 +20,7 @@ Measurement modes (each prints its own output instead of the bench line):
     python bench.py --config-table
         every synthetic configuration on both GPU forms and the CPU restatement
     python bench.py --case [--n 250000] [--steps 3] [--precision 0|1] [--v-top -1]
-                    [--kernels] [--gather-block B] [--particle-block B]
+                    [--kernels] [--gather-block B] [--particle-block B] [--gather-lanes L]
         a fixed-size run of the bench cylinder scaled to about n particles, for
         ncu captures and per-kernel CUDA-event times (--kernels)
     python bench.py --accuracy [--steps 1000] [--dx-mm 0.3353,0.2112,0.1331]
@@ -373,6 +373,8 @@ def case_mode(a):
         d.set("gather_block", a.gather_block)
     if a.particle_block is not None:
         d.set("particle_block", a.particle_block)
+    if a.gather_lanes is not None:
+        d.set("gather_lanes", a.gather_lanes)
     t = time.perf_counter()
     d.step(a.steps)
     el = time.perf_counter() - t
@@ -588,6 +590,7 @@ def main():
     ap.add_argument("--kernels", action="store_true", help="--case: per-kernel CUDA-event times")
     ap.add_argument("--gather-block", type=int, default=None, help="--case: threads per mixed gather block")
     ap.add_argument("--particle-block", type=int, default=None, help="--case: threads per per-particle block")
+    ap.add_argument("--gather-lanes", type=int, default=None, help="--case: lanes per particle, acceleration gather")
     ap.add_argument("--dx-mm", default=None, help="--accuracy: lattice spacings (mm, comma-separated)")
     ap.add_argument("--contact", action="store_true", help="--accuracy: penalty-contact workload")
     a = ap.parse_args()

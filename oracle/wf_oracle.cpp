@@ -1616,7 +1616,8 @@ int wfo_set_domain_i32(wfo_domain* p, const char* name, int v) {
   else if (n == "auto_ts_cont") d->auto_ts_cont = v != 0;
   else if (n == "nonlock_sum") { if (!v) return set_err(WF_ERR_UNSUPPORTED, "only the Nishimura sum is supported"); }
   else if (n == "GradientType") { if (v) return set_err(WF_ERR_UNSUPPORTED, "only GradientType 0 is supported"); }
-  else if (n == "precision" || n == "device" || n == "use_graph") {}
+  else if (n == "precision" || n == "device" || n == "use_graph" || n == "gather_block" || n == "gather_lanes" ||
+           n == "particle_block") {}  // GPU launch shapes: no effect on the arithmetic
   else return set_err(WF_ERR_ARG, "unknown domain i32 field " + n);
   return WF_OK;
 }

@@ -178,6 +178,69 @@ def test_mixed_gather_block_sizes_agree_bitwise():
             assert np.array_equal(r[f], res[0][f]), f
 
 
+def test_mixed_particles_of_different_mass_and_smoothing_length():
+    """Masses spread by +-5 % and two smoothing lengths: the gathers read
+    the five-group records (h, mass and Cs per particle) instead of the
+    uniform-particle layout, and stay within the bound; writing uniform
+    masses and h back after the prologue switches to the uniform layout
+    mid-run, still within the bound."""
+    f = FIELDS + ("pl_strain",)
+
+    def build(d, **kw):
+        case = configs.cylinder_upsetting(d, **kw)
+        n = d.particle_count
+        rng = np.random.default_rng(5)
+        d.set_array("Mass", d.get_array("Mass") * (1.0 + 0.05 * rng.uniform(-1, 1, n)))
+        h = d.get_array("h")
+        h[::7] *= 1.02
+        d.set_array("h", h)
+        return case
+    m, o = _run(build, 100, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    _check(m, o, f)
+    out = {}
+    for name in ("mixed", "oracle"):
+        d = gpu_domain() if name == "mixed" else oracle_domain()
+        if name == "mixed":
+            d.set("precision", PRECISION_MIXED)
+        case = build(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+        d.prepare(case.dt)
+        d.step(20)
+        n = d.particle_count
+        d.set_array("Mass", np.full(n, d.get_array("Mass").mean()))
+        d.set_array("h", np.full(n, 1.2 * 0.0005))
+        d.step(40)
+        out[name] = {k: d.get_array(k) for k in f}
+        d.close()
+    _check(out["mixed"], out["oracle"], f)
+
+
+@pytest.mark.parametrize("lanes", [2, 4, 8])
+def test_mixed_acceleration_gather_lanes(lanes):
+    """The acceleration gather with `lanes` lanes per particle (per-lane
+    Kahan sums combined in FP64 by warp shuffles): within the bound against
+    the oracle, and bit-identical across block sizes at a fixed lane count."""
+    f = FIELDS + ("pl_strain",)
+
+    def build(d, **kw):
+        d.set("gather_lanes", lanes)
+        return configs.cylinder_upsetting(d, **kw)
+    m, o = _run(build, 100, f, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    _check(m, o, f)
+    res = []
+    for gb in (64, 256, 512):
+        d = gpu_domain()
+        d.set("precision", PRECISION_MIXED)
+        d.set("gather_lanes", lanes)
+        d.set("gather_block", gb)
+        case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+        d.prepare(case.dt)
+        d.step(30)
+        res.append(d.get_array("a"))
+        d.close()
+    for r in res[1:]:
+        assert np.array_equal(r, res[0])
+
+
 @pytest.mark.parametrize("integrator", [0, 1], ids=["kickdrift", "leapfrog"])
 def test_mixed_kernel_gradient_correction(integrator):
     """gradKernelCorr in the mixed form: corrected FP32 gradients in the

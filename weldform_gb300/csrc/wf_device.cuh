@@ -216,6 +216,7 @@ struct DomainConst {
   int nblocks;         // blocks of the per-particle kernels at pblock (partials stride)
   int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
   int gblock;          // thread-block size of the mixed form's gather kernels
+  int glanes;          // lanes per particle of the mixed acceleration gather (1, 2, 4 or 8)
   int ti;              // 1 when some particle has TI > 0 (tensile-instability term on)
   int leapfrog;        // 1: SolveDiffUpdateLeapFrog's update (velocities at half steps)
   int gradcorr;        // 1: kernel-gradient correction (Domain::gradKernelCorr)
@@ -225,6 +226,16 @@ struct DomainConst {
   float av_alpha, av_beta;  // those values (the mixed acceleration gather skips their loads)
   int m_uniform;       // 1 when every solid particle has the same mass
   float mass_f;        // that mass (the mixed rate gather's kinetic-energy term)
+  // Uniform-particle layout of the mixed records: every solid particle has the
+  // same h, mass and Cs (and the staged gather is off).  The current records
+  // then carry Sigma/rho^2 xz in RC_XH.w and yz in RC_VH.w (instead of h and
+  // rho), so the acceleration gather reads four groups per neighbour instead
+  // of five, rho_j = mass / (m/rho)_j, and every gather uses the kernel
+  // constants of the one h below instead of forming 1/h per pair.
+  int uni;
+  float h_f, cs_f;     // that h and Cs
+  float inv_h_f;       // 1 / h
+  float gk_c_f;        // 1 / (pi h^5): the 3D cubic spline's gradient factor GK = gk_c_f * w(q)
   int stage_cap;       // halo capacity of the staged gathers (0: staging off)
   int freeze_nb;       // 1: neighbour and contact topology searched only at the first step
   int nan_check;       // 1: a non-finite position at a search, or non-finite energy sums, raise ERR_NAN

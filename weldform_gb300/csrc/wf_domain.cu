@@ -157,6 +157,7 @@ struct wf_domain {
   int auto_ts = 0, auto_ts_acc = 0, auto_ts_cont = 0;
   double CFL = 0.7, sqrt_h_a = 0.0025;
   int gblock = 0;    // mixed gathers' threads per block (0: chosen by particle count)
+  int glanes = 1;    // lanes per particle of the mixed acceleration gather (1, 2, 4, 8)
   int pblock = 0;    // per-particle kernels' threads per block (0: chosen by particle count)
   // Shared-memory staging of the mixed acceleration gather: the halo lists
   // are allocated at the prologue when it is on; stage_cap is each block's
@@ -170,7 +171,9 @@ struct wf_domain {
   static int auto_block(long long n) { return n < 78000 ? 64 : (n < 156000 ? 128 : 256); }
   int gblock_now() const { return gblock ? gblock : auto_block(hp.N); }
   int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
-  int graph_key() const { return (gblock_now() * 1024 + pblock_now()) * 2 + (stage_ready && stage ? 1 : 0); }
+  int graph_key() const {
+    return ((gblock_now() * 1024 + pblock_now()) * 16 + glanes) * 2 + (stage_ready && stage ? 1 : 0);
+  }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
@@ -614,7 +617,8 @@ struct wf_domain {
     K.totmass_mean = tm / N;
     K.id_free_surf = -999999;
     K.leapfrog = integrator;
-    set_uniform(hp.f[C_ALPHA].data(), hp.f[C_BETA].data(), hp.f[C_MASS].data(), hp.i[I_KIND].data(), N);
+    set_uniform(hp.f[C_ALPHA].data(), hp.f[C_BETA].data(), hp.f[C_MASS].data(), hp.f[C_H].data(),
+                hp.f[C_CS].data(), hp.i[I_KIND].data(), N);
     K.gradcorr = grad_corr;
     if (auto_ts_cont && contact && integrator == 0)
       throw CudaError{WF_ERR_UNSUPPORTED, "auto_ts_cont with contact: the kick-drift solver reads Domain::min_force_ts, "
@@ -688,6 +692,7 @@ struct wf_domain {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
     k.gblock = gblock_now();
+    k.glanes = glanes;
     k.pblock = pblock_now();
     k.nblocks = (int)((hp.N + k.pblock - 1) / k.pblock);
     k.stage_cap = stage_ready && stage ? stage_cap : 0;
@@ -816,33 +821,52 @@ struct wf_domain {
   // Whether Alpha and Beta, and the mass, are the same on every SPH particle:
   // the gathers then take the pair's (a_i + a_j) / 2 = a, and m_j, from K
   // instead of loading them.
-  void set_uniform(const double* a, const double* b, const double* m, const int* kind, size_t n) {
+  // Flags of the solid particles' uniform fields, which select the mixed
+  // gathers' specialisations and record layout (DomainConst::av_uniform,
+  // m_uniform, uni).
+  void set_uniform(const double* a, const double* b, const double* m, const double* h, const double* cs,
+                   const int* kind, size_t n) {
     K.av_uniform = 1;
     K.m_uniform = 1;
+    bool h_uniform = true, cs_uniform = true;
     bool first = true;
-    double a0 = 0, b0 = 0, m0 = 0;
+    double a0 = 0, b0 = 0, m0 = 0, h0 = 0, c0 = 0;
     for (size_t p = 0; p < n; ++p) {
       if (kind[p] != 0) continue;
-      if (first) { a0 = a[p]; b0 = b[p]; m0 = m[p]; first = false; continue; }
+      if (first) { a0 = a[p]; b0 = b[p]; m0 = m[p]; h0 = h[p]; c0 = cs[p]; first = false; continue; }
       if (a[p] != a0 || b[p] != b0) K.av_uniform = 0;
       if (m[p] != m0) K.m_uniform = 0;
+      if (h[p] != h0) h_uniform = false;
+      if (cs[p] != c0) cs_uniform = false;
     }
     K.av_alpha = (float)a0;
     K.av_beta = (float)b0;
     K.mass_f = (float)m0;
+    // the staged gather copies the five-group layout
+    K.uni = (K.m_uniform && h_uniform && cs_uniform && !stage && h0 > 0) ? 1 : 0;
+    K.h_f = (float)h0;
+    K.cs_f = (float)c0;
+    // the FP32 operations of the per-pair kernel factor at hh = h
+    float ih = 1.0f / K.h_f, ih2 = ih * ih;
+    K.inv_h_f = ih;
+    K.gk_c_f = 0.318309886183790671538f * ih2 * ih2 * ih;
   }
-  // Alpha, Beta or mass written after the prologue: re-evaluate the flags on
-  // the device columns (any order) and recapture the step with the new constants.
+  // Alpha, Beta, mass, h or Cs written after the prologue: re-evaluate the
+  // flags on the device columns (any order) and recapture the step with the
+  // new constants; the mixed records are rebuilt in the layout they select.
   void refresh_uniform() {
     size_t n = hp.N;
-    std::vector<double> a(n), b(n), m(n);
+    std::vector<double> a(n), b(n), m(n), h(n), cs(n);
     std::vector<int> kind(n);
     CK(cudaMemcpyAsync(a.data(), d_f + (size_t)wf::C_ALPHA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(b.data(), d_f + (size_t)wf::C_BETA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(m.data(), d_f + (size_t)wf::C_MASS * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h.data(), d_f + (size_t)wf::C_H * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(cs.data(), d_f + (size_t)wf::C_CS * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(kind.data(), d_i + (size_t)wf::I_KIND * n, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    set_uniform(a.data(), b.data(), m.data(), kind.data(), n);
+    set_uniform(a.data(), b.data(), m.data(), h.data(), cs.data(), kind.data(), n);
+    shadows_valid = false;
     if (graph) { CK(cudaGraphExecDestroy(graph)); graph = nullptr; }
   }
   void checkpoint_save(int slot) {
@@ -1175,7 +1199,7 @@ struct wf_domain {
     shadows_valid = false;
     invalidate_gk();
     CK(cudaStreamSynchronize(stream));
-    if (c == wf::C_ALPHA || c == wf::C_BETA || c == wf::C_MASS) refresh_uniform();
+    if (c == wf::C_ALPHA || c == wf::C_BETA || c == wf::C_MASS || c == wf::C_H || c == wf::C_CS) refresh_uniform();
   }
   void get_i32(int c, int* dst) {
     size_t n = hp.N;
@@ -1280,10 +1304,17 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     d->gblock = v;
     return WF_OK;
   }
+  if (n == "gather_lanes") {  // lanes per particle of the mixed acceleration gather
+    if (v != 1 && v != 2 && v != 4 && v != 8) return set_err(WF_ERR_ARG, "gather_lanes must be 1, 2, 4 or 8");
+    d->glanes = v;
+    return WF_OK;
+  }
   if (n == "gather_staging") {  // shared-memory staged acceleration gather of the mixed form
     if (d->prepared && v && !d->stage_ready)
       return set_err(WF_ERR_STATE, "gather_staging must be set before the prologue (it allocates the halo lists)");
     d->stage = v != 0;
+    if (d->prepared)  // the uniform-particle record layout is off while staging is on
+      return guard([&] { d->refresh_uniform(); return WF_OK; });
     return WF_OK;
   }
   if (n == "stage_cap") {
@@ -1368,6 +1399,7 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     if (n == "particle_count") { *v = d->hp.N; return WF_OK; }
     if (n == "solid_part_count") { *v = d->solid_part_count; return WF_OK; }
     if (n == "gather_block") { *v = d->gblock_now(); return WF_OK; }
+    if (n == "gather_lanes") { *v = d->glanes; return WF_OK; }
     if (n == "particle_block") { *v = d->pblock_now(); return WF_OK; }
     if (n == "gather_staging") { *v = d->stage ? 1 : 0; return WF_OK; }
     if (n == "stage_cap") { *v = d->stage_cap; return WF_OK; }

@@ -69,6 +69,23 @@ __device__ __forceinline__ float grad_kernel_f(float r2, float hh, float* r_out)
   return C * w;
 }
 
+// The same factor for a pair smoothing length hh = h that is uniform over the
+// domain: 1/h and C come precomputed (the same FP32 operations on the host).
+template <bool UNI>
+__device__ __forceinline__ float grad_kernel(const DomainConst& K, float r2, float hh, float* r_out) {
+  if (!UNI) return grad_kernel_f(r2, hh, r_out);
+  float rinv = rsqrtf(r2);
+  float r = r2 * rinv;
+  float q = r * K.inv_h_f;
+  float w;
+  if (q < 1.0f) w = -3.0f + 2.25f * q;
+  else if (q < 2.0f) { float t = 2.0f - q; w = -0.75f * t * t * (K.h_f * rinv); }
+  else w = 0.0f;
+  if (r2 == 0.0f) { w = -3.0f; r = 0.0f; }
+  *r_out = r;
+  return K.gk_c_f * w;
+}
+
 // Kernel-gradient correction of the locking sums (gradKernelCorr): the
 // corrected gradient Mult(GK gradCorrM_i, x_ij) (InteractionAlt.cpp:114-132),
 // with the particle's own matrix in FP32.
@@ -102,9 +119,12 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
   }
   ff_split(col(P, C_T, N, i), th, tl);
   float4* r = P.rc + i;
-  r[(size_t)RC_XH * N] = make_float4(xh[0], xh[1], xh[2], (float)col(P, C_H, N, i));
+  // uniform-particle layout: Sigma/rho^2 xz, yz in the .w slots of the x and v groups
+  float w_x = K.uni ? (float)(c2 * col(P, C_SIG + 4, N, i)) : (float)col(P, C_H, N, i);
+  float w_v = K.uni ? (float)(c2 * col(P, C_SIG + 5, N, i)) : (float)rho;
+  r[(size_t)RC_XH * N] = make_float4(xh[0], xh[1], xh[2], w_x);
   r[(size_t)RC_L * N] = lo_pack(xl, vl, solid ? (float)(col(P, C_MASS, N, i) / rho) : 0.f);
-  r[(size_t)RC_VH * N] = make_float4(vh[0], vh[1], vh[2], (float)rho);
+  r[(size_t)RC_VH * N] = make_float4(vh[0], vh[1], vh[2], w_v);
   r[(size_t)RC_S0 * N] = make_float4((float)(c2 * col(P, C_SIG, N, i)), (float)(c2 * col(P, C_SIG + 1, N, i)),
                          (float)(c2 * col(P, C_SIG + 2, N, i)), (float)(c2 * col(P, C_SIG + 3, N, i)));
   r[(size_t)RC_S1 * N] = make_float4((float)(c2 * col(P, C_SIG + 4, N, i)), (float)(c2 * col(P, C_SIG + 5, N, i)),
@@ -120,15 +140,21 @@ __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
 // GC: kernel-gradient correction (temp_c = Mult(vc_i, S), InteractionAlt.cpp:166-170).
 // Where a gather reads its neighbours' float4 groups: global memory through
 // the row's indices, or a block's staged halo through the row's slots.
+// A fetch splits into the row entry's reference (key) and the records it
+// points at, so a gather can load entry k + dk's key before it consumes
+// entry k's records: the index load then overlaps the record loads instead of
+// adding a second memory latency to every iteration.
 struct GlobalFetch {
   const float4* rc;
   const int* nb;  // P.nbr + i
   size_t N;
-  __device__ __forceinline__ int get(int k, float4& xh, float4& lo, float4& vh, float4& s0, float4& s1) const {
-    int j = nb_index(nb[(size_t)k * N]);
+  __device__ __forceinline__ int key(int k) const { return nb_index(nb[(size_t)k * N]); }
+  template <bool UNI = false>
+  __device__ __forceinline__ int get(int j, float4& xh, float4& lo, float4& vh, float4& s0, float4& s1) const {
     const float4* rj = rc + j;
     xh = ld4(rj + (size_t)RC_XH * N); lo = ld4(rj + (size_t)RC_L * N); vh = ld4(rj + (size_t)RC_VH * N);
-    s0 = ld4(rj + (size_t)RC_S0 * N); s1 = ld4(rj + (size_t)RC_S1 * N);
+    s0 = ld4(rj + (size_t)RC_S0 * N);
+    if (!UNI) s1 = ld4(rj + (size_t)RC_S1 * N);  // uniform layout: xz, yz ride in xh.w, vh.w
     return j;
   }
 };
@@ -137,15 +163,19 @@ struct StagedFetch {
   const unsigned short* slot;  // P.nslot + i
   size_t N;
   int cap;
-  __device__ __forceinline__ int get(int k, float4& xh, float4& lo, float4& vh, float4& s0, float4& s1) const {
-    int q = slot[(size_t)k * N];
+  __device__ __forceinline__ int key(int k) const { return slot[(size_t)k * N]; }
+  template <bool UNI = false>
+  __device__ __forceinline__ int get(int q, float4& xh, float4& lo, float4& vh, float4& s0, float4& s1) const {
     xh = sh[q]; lo = sh[cap + q]; vh = sh[2 * cap + q]; s0 = sh[3 * cap + q]; s1 = sh[4 * cap + q];
     return -1;  // the global index is not known here: no misc or TI group (AVU and !TI only)
   }
 };
 
 // Pair sums of the acceleration of SPH particle i over row entries k0, k0 + dk, ...
-template <bool TI, bool AVU, bool GC, class Fetch>
+// UNI: the uniform-particle layout (DomainConst::uni): h, mass and Cs are the
+// domain's constants, Sigma/rho^2 xz and yz come from the .w slots of the x
+// and v groups, and rho_j = mass / (m/rho)_j.
+template <bool TI, bool AVU, bool GC, bool UNI, class Fetch>
 __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainConst& K, int i, const Fetch& F, int k0,
                                               int dk, KSum& a0, KSum& a1, KSum& a2) {
   size_t N = K.N;
@@ -153,7 +183,11 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
   float4 xh = ld4(ri + (size_t)RC_XH * N), lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
   float xl[3], vl[3];
   lo_unpack(lo, xl, vl);
-  float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1 = ld4(ri + (size_t)RC_S1 * N);
+  float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1;
+  if (UNI) s1 = make_float4(xh.w, vh.w, K.mass_f, K.cs_f);
+  else s1 = ld4(ri + (size_t)RC_S1 * N);
+  const float hi_ = UNI ? K.h_f : xh.w;
+  const float rhoi = UNI ? (float)col(P, C_RHO, N, i) : vh.w;
   float4 mi = AVU ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(ri + (size_t)RC_MISC * N);
   float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
   float tii = 0.f;
@@ -161,17 +195,20 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
   CorrM cm;
   if (GC) cm = load_corr(P, N, i);
   int len = P.row_len[i];
+  int next = k0 < len ? F.key(k0) : 0;
   for (int k = k0; k < len; k += dk) {
     float4 jxh, jlo, jvh, js0, js1;
-    int j = F.get(k, jxh, jlo, jvh, js0, js1);
+    int j = F.template get<UNI>(next, jxh, jlo, jvh, js0, js1);
+    if (k + dk < len) next = F.key(k + dk);
+    if (UNI) js1 = make_float4(jxh.w, jvh.w, K.mass_f, K.cs_f);
     const float4* rj = P.rc + j;
     float jxl[3], jvl[3];
     lo_unpack(jlo, jxl, jvl);
     float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
     float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
-    float hh = 0.5f * (xh.w + jxh.w);
+    float hh = UNI ? hi_ : 0.5f * (hi_ + jxh.w);
     float r2 = x0 * x0 + x1 * x1 + x2 * x2, r;
-    float GK = grad_kernel_f(r2, hh, &r);
+    float GK = grad_kernel<UNI>(K, r2, hh, &r);
     float Alpha, Beta;
     if (AVU) {
       Alpha = K.av_alpha; Beta = K.av_beta;
@@ -185,7 +222,10 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
       if (dvx < 0.f) {  // Monaghan viscosity (InteractionAlt.cpp:74-94)
         float MU = hh * dvx / (r * r + 0.01f * hh * hh);
         float Cij = 0.5f * (s1.w + js1.w);
-        PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5f * (vh.w + jvh.w));
+        if (UNI)  // 1 / (0.5 (rho_i + rho_j)) with rho_j = mass / (m/rho)_j
+          PIs = (Alpha * Cij * MU + Beta * MU * MU) * (2.f * jlo.w) / (rhoi * jlo.w + K.mass_f);
+        else
+          PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5f * (rhoi + jvh.w));
       }
     }
     float S0 = s0.x + js0.x + PIs, S1 = s0.y + js0.y + PIs, S2 = s0.z + js0.z + PIs;
@@ -210,7 +250,7 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
     a2.add(mj * (g0 * S4 + g1 * S5 + g2 * S2));
   }
 }
-template <bool TI, bool AVU, bool GC, class Fetch>
+template <bool TI, bool AVU, bool GC, bool UNI, class Fetch>
 __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K, int i, const Fetch& F) {
   size_t N = K.N;
   if (icol(P, I_KIND, N, i) != 0) {
@@ -218,12 +258,40 @@ __device__ __forceinline__ void accel_mx(const DevPtrs& P, const DomainConst& K,
     return;
   }
   KSum a0, a1, a2;
-  accel_mx_sums<TI, AVU, GC>(P, K, i, F, 0, 1, a0, a1, a2);
+  accel_mx_sums<TI, AVU, GC, UNI>(P, K, i, F, 0, 1, a0, a1, a2);
   colw(P, C_A, N, i) = a0.value(); colw(P, C_A + 1, N, i) = a1.value(); colw(P, C_A + 2, N, i) = a2.value();
 }
-template <bool TI, bool AVU, bool GC>
+template <bool TI, bool AVU, bool GC, bool UNI>
 __global__ void __launch_bounds__(512) k_accel_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { accel_mx<TI, AVU, GC>(P, K, i, GlobalFetch{P.rc, P.nbr + i, (size_t)K.N}); });
+  run_rows(K, [&](int i) { accel_mx<TI, AVU, GC, UNI>(P, K, i, GlobalFetch{P.rc, P.nbr + i, (size_t)K.N}); });
+}
+
+// L consecutive lanes share particle i = thread / L: lane s sums row entries
+// s, s + L, s + 2L, ... with its own Kahan sums, and the L partial sums are
+// combined in FP64 by a butterfly of __shfl_xor_sync (every lane ends with the
+// same total; lane s == 0 writes it).  Each lane walks 1/L of the row, so a
+// warp keeps loads of 32 / L particles' rows in flight with shorter dependent
+// chains.  The result depends on L (summation order) but not on the block size.
+template <bool TI, bool AVU, bool GC, bool UNI, int L>
+__global__ void __launch_bounds__(512) k_accel_mx_lanes(DevPtrs P, DomainConst K) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t / L), sub = (int)(t % L);
+  const size_t N = K.N;
+  const bool live = i < K.N;
+  const bool sph = live && icol(P, I_KIND, N, i) == 0;
+  KSum a0, a1, a2;
+  if (sph) accel_mx_sums<TI, AVU, GC, UNI>(P, K, i, GlobalFetch{P.rc, P.nbr + i, N}, sub, L, a0, a1, a2);
+  double v0 = a0.value(), v1 = a1.value(), v2 = a2.value();
+  for (int off = 1; off < L; off <<= 1) {  // the whole warp takes part; L divides 32
+    v0 += __shfl_xor_sync(0xffffffffu, v0, off);
+    v1 += __shfl_xor_sync(0xffffffffu, v1, off);
+    v2 += __shfl_xor_sync(0xffffffffu, v2, off);
+  }
+  if (live && sub == 0) {
+    colw(P, C_A, N, i) = sph ? v0 : 0.0;
+    colw(P, C_A + 1, N, i) = sph ? v1 : 0.0;
+    colw(P, C_A + 2, N, i) = sph ? v2 : 0.0;
+  }
 }
 
 // Staged acceleration gather (uniform viscosity constants, no tensile
@@ -258,8 +326,8 @@ __global__ void __launch_bounds__(2 * STAGE_B) k_accel_mx_staged(DevPtrs P, Doma
   const bool sph = i < K.N && icol(P, I_KIND, N, i) == 0;
   KSum a0, a1, a2;
   if (sph) {
-    if (H >= 0) accel_mx_sums<false, true, false>(P, K, i, StagedFetch{sh_rec, P.nslot + i, N, cap}, part, 2, a0, a1, a2);
-    else accel_mx_sums<false, true, false>(P, K, i, GlobalFetch{P.rc, P.nbr + i, N}, part, 2, a0, a1, a2);
+    if (H >= 0) accel_mx_sums<false, true, false, false>(P, K, i, StagedFetch{sh_rec, P.nslot + i, N, cap}, part, 2, a0, a1, a2);
+    else accel_mx_sums<false, true, false, false>(P, K, i, GlobalFetch{P.rc, P.nbr + i, N}, part, 2, a0, a1, a2);
   }
   double v0 = a0.value(), v1 = a1.value(), v2 = a2.value();
   __syncthreads();  // halo records no longer read: the odd halves pass through shared memory
@@ -375,7 +443,7 @@ int configure_staging(int cap) {
 // ---------------------------------------------------------------- density + drift + kick
 // GC: the locking sum with corrected gradients, m_j (rho_i / rho_j) v_ij . vc_i
 // (InteractionAlt.cpp:589-605), which carries rho_i inside the sum.
-template <bool GC>
+template <bool GC, bool UNI>
 __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   double dt = P.st->deltat;
@@ -403,7 +471,7 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
       float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
       float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
       float r;
-      float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
+      float GK = grad_kernel<UNI>(K, x0 * x0 + x1 * x1 + x2 * x2, UNI ? K.h_f : 0.5f * (xh.w + jxh.w), &r);
       if (GC) {
         float g0, g1, g2;
         corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
@@ -441,15 +509,15 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   float th, tl;
   ff_split(Tn, th, tl);
   float4* r = P.rn + i;
-  r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], xh.w);
+  r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], UNI ? K.h_f : xh.w);
   r[(size_t)RN_L * N] = lo_pack(nxl, nvl, (float)mrn);
   float pr2 = solid ? (float)(pn * irn * irn) : 0.f;
   r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], pr2);  // the rate gather reads p/rho^2 here
   r[(size_t)RN_E * N] = make_float4(pr2, ri[(size_t)RC_MISC * N].z, th, tl);
 }
-template <bool GC>
+template <bool GC, bool UNI>
 __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { density_drift_mx<GC>(P, K, i); });
+  run_rows(K, [&](int i) { density_drift_mx<GC, UNI>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- rates + energy + conduction
@@ -458,7 +526,7 @@ __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainCo
 // GC: rates and conduction with corrected gradients (InteractionAlt.cpp:330-350,
 // 425-450; Thermal.cpp:90-107), weights (float)(m_j / rho_j); the kinetic-energy
 // pair term keeps the plain gradient, as the reference's.
-template <bool THERMAL, bool GC>
+template <bool THERMAL, bool GC, bool UNI>
 __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i) {
   size_t N = K.N;
   float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -487,7 +555,7 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
       float b0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), b1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), b2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
       float r;
-      float GK = grad_kernel_f(x0 * x0 + x1 * x1 + x2 * x2, 0.5f * (xh.w + jxh.w), &r);
+      float GK = grad_kernel<UNI>(K, x0 * x0 + x1 * x1 + x2 * x2, UNI ? K.h_f : 0.5f * (xh.w + jxh.w), &r);
       float y0 = x0, y1 = x1, y2 = x2;
       float w = jlo.w * (-0.5f * GK);
       if (GC) {  // -1/2 (float)(m_j/rho_j) (v_ij (x) gk), gk = M_i GK x_ij
@@ -526,9 +594,9 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
   colw(P, C_DKIN, N, i) = dkin;
   colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
 }
-template <bool THERMAL, bool GC>
+template <bool THERMAL, bool GC, bool UNI>
 __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { rate_mx<THERMAL, GC>(P, K, i); });
+  run_rows(K, [&](int i) { rate_mx<THERMAL, GC, UNI>(P, K, i); });
 }
 
 // ---------------------------------------------------------------- elementwise update
@@ -626,11 +694,14 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
     colw(P, C_MRHO, N, i) = col(P, C_MRHON, N, i);
     const float4* rn = P.rn + i;
     float4* rc = P.rc + i;
-    rc[(size_t)RC_XH * N] = rn[(size_t)RN_XH * N];
+    float4 nxh = rn[(size_t)RN_XH * N];
     rc[(size_t)RC_L * N] = rn[(size_t)RN_L * N];
     float4 nvh = rn[(size_t)RN_VH * N];
-    nvh.w = (float)rho;  // the current group carries rho (the acceleration gather's viscosity)
-    rc[(size_t)RC_VH * N] = nvh;
+    // the current groups carry h and rho (the acceleration gather's viscosity),
+    // or in the uniform-particle layout Sigma/rho^2 xz and yz (written below
+    // for SPH particles, 0 for the rest)
+    nxh.w = K.uni ? 0.f : nxh.w;
+    nvh.w = K.uni ? 0.f : (float)rho;
     float4 ne = rn[(size_t)RN_E * N];
     float4 misc = rc[(size_t)RC_MISC * N];
     maxpl = col(P, C_PLS, N, i);
@@ -703,10 +774,17 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
                                      s.tau[1] * srd[1] + 2.0 * s.tau[5] * srd[5] + s.tau[2] * srd[2]);
       colw(P, C_DINT, N, i) = dint;
       float c2 = 1.0f / ((float)rho * (float)rho);
-      float4 s1o = rc[(size_t)RC_S1 * N];  // mass and Cs carried over
       rc[(size_t)RC_S0 * N] = make_float4(c2 * (float)s.sig[0], c2 * (float)s.sig[1], c2 * (float)s.sig[2], c2 * (float)s.sig[3]);
-      rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], s1o.z, s1o.w);
+      if (K.uni) {
+        nxh.w = c2 * (float)s.sig[4];
+        nvh.w = c2 * (float)s.sig[5];
+      } else {
+        float4 s1o = rc[(size_t)RC_S1 * N];  // mass and Cs carried over
+        rc[(size_t)RC_S1 * N] = make_float4(c2 * (float)s.sig[4], c2 * (float)s.sig[5], s1o.z, s1o.w);
+      }
     }
+    rc[(size_t)RC_XH * N] = nxh;
+    rc[(size_t)RC_VH * N] = nvh;
     rc[(size_t)RC_MISC * N] = make_float4(misc.x, misc.y, misc.z, ne.z);
     rc[(size_t)RC_T2 * N] = make_float4(ne.w, 0.f, 0.f, 0.f);
   }
@@ -727,10 +805,26 @@ void launch_refresh_shadows(const DevPtrs& P, const DomainConst& K, int force, c
   mark(s, "k_refresh_records");
 }
 
+template <bool TI, bool AVU, bool GC, bool UNI>
+static void launch_accel_mx_u(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
+  // blocks for L lanes per particle: the grid covers L * N threads
+  auto grid = [&](int L) { return (int)(((long long)K.N * L + gb - 1) / gb); };
+  switch (K.glanes) {
+    case 2: k_accel_mx_lanes<TI, AVU, GC, UNI, 2><<<grid(2), gb, 0, s>>>(P, K); break;
+    case 4: k_accel_mx_lanes<TI, AVU, GC, UNI, 4><<<grid(4), gb, 0, s>>>(P, K); break;
+    case 8: k_accel_mx_lanes<TI, AVU, GC, UNI, 8><<<grid(8), gb, 0, s>>>(P, K); break;
+    default: k_accel_mx<TI, AVU, GC, UNI><<<ng, gb, 0, s>>>(P, K);
+  }
+}
 template <bool TI, bool AVU>
 static void launch_accel_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
-  if (K.gradcorr) k_accel_mx<TI, AVU, true><<<ng, gb, 0, s>>>(P, K);
-  else k_accel_mx<TI, AVU, false><<<ng, gb, 0, s>>>(P, K);
+  if (K.gradcorr) {
+    if (K.uni) launch_accel_mx_u<TI, AVU, true, true>(P, K, ng, gb, s);
+    else launch_accel_mx_u<TI, AVU, true, false>(P, K, ng, gb, s);
+  } else {
+    if (K.uni) launch_accel_mx_u<TI, AVU, false, true>(P, K, ng, gb, s);
+    else launch_accel_mx_u<TI, AVU, false, false>(P, K, ng, gb, s);
+  }
 }
 
 void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
@@ -754,16 +848,21 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
-  if (K.gradcorr) k_density_drift_mx<true><<<ng, gb, 0, s>>>(P, K);
-  else k_density_drift_mx<false><<<ng, gb, 0, s>>>(P, K);
+  if (K.gradcorr) {
+    if (K.uni) k_density_drift_mx<true, true><<<ng, gb, 0, s>>>(P, K);
+    else k_density_drift_mx<true, false><<<ng, gb, 0, s>>>(P, K);
+  } else {
+    if (K.uni) k_density_drift_mx<false, true><<<ng, gb, 0, s>>>(P, K);
+    else k_density_drift_mx<false, false><<<ng, gb, 0, s>>>(P, K);
+  }
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
   if (K.thermal_solver) {
-    if (K.gradcorr) k_rate_mx<true, true><<<ng, gb, 0, s>>>(P, K);
-    else k_rate_mx<true, false><<<ng, gb, 0, s>>>(P, K);
+    if (K.gradcorr) { if (K.uni) k_rate_mx<true, true, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<true, true, false><<<ng, gb, 0, s>>>(P, K); }
+    else { if (K.uni) k_rate_mx<true, false, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<true, false, false><<<ng, gb, 0, s>>>(P, K); }
   } else {
-    if (K.gradcorr) k_rate_mx<false, true><<<ng, gb, 0, s>>>(P, K);
-    else k_rate_mx<false, false><<<ng, gb, 0, s>>>(P, K);
+    if (K.gradcorr) { if (K.uni) k_rate_mx<false, true, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<false, true, false><<<ng, gb, 0, s>>>(P, K); }
+    else { if (K.uni) k_rate_mx<false, false, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<false, false, false><<<ng, gb, 0, s>>>(P, K); }
   }
   mark(s, "k_rate_mx");
   if (K.pl_heating) {
