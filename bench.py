@@ -59,7 +59,7 @@ ALG_BYTES = {
     "k_accel": lambda nnz: 144 + 4 * nnz + 4,             # x,v,rho,m,h,Sigma(6) -> a
     "k_density_drift": lambda nnz: 272 + 4 * nnz + 4,     # x,v,a,rho,m,h -> v,rho ; x,v,a -> x,v
     "k_rate_stress": lambda nnz: 456 + 4 * nnz + 4,       # x,v,rho,m,h,p,tau,eps,eps_p,pl,sy -> tau,Sigma,..,dkin,dint
-    "k_accel_mx": lambda nnz: 108 + 4 * nnz + 4,          # ff x,v; f32 rho,m,h,Sigma/rho^2 -> a (f64)
+    "k_accel_mx": lambda nnz: 96 + 4 * nnz + 4,           # four f32 groups (ff x, v; Sigma/rho^2; m/rho), f64 rho -> a
     "k_density_drift_mx": lambda nnz: 336 + 4 * nnz + 4,  # f64 integration; next-step record written
     "k_rate_mx": lambda nnz: 72 + 4 * nnz + 4,            # next record -> 9 rates, dkin, conduction
     "k_stress_mx": lambda nnz: 440,                       # f64 stress state read + written
@@ -140,24 +140,28 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def build_domain(dom, dx=DX_1M):
+V_TOP = -1.0          # the literal configuration: elastic, no rebuild after the first step
+V_TOP_YIELD = -20.0   # the yielding variant: plastic from the first steps, rebuilds every 5 steps
+
+
+def build_domain(dom, dx=DX_1M, v_top=V_TOP):
     from weldform_gb300 import configs
-    return configs.cylinder_upsetting(dom, R=R, L=L, dx=dx, v_top=-1.0)
+    return configs.cylinder_upsetting(dom, R=R, L=L, dx=dx, v_top=v_top)
 
 
-def _workload(n, precision):
+def _workload(n, precision, v_top=V_TOP):
     return {"workload": f"cylinder upsetting R=10mm L=30mm dx={DX_1M * 1e3:.4f}mm N={n}, bilinear steel, "
-                        f"v_top=-1 m/s, alpha=1, dt=0.4h/Cs",
+                        f"v_top={v_top:g} m/s, alpha=1, dt=0.4h/Cs",
             "particles": n, "form": precision, "l2": "state > 129 MB L2 (no flush needed)",
             "parallelism": "replicas"}
 
 
-def time_form(wfmod, precision, steps, warmup, gpu):
+def time_form(wfmod, precision, steps, warmup, gpu, v_top=V_TOP):
     """Headline timing of one precision form: graph-replayed steps between CUDA events."""
     d = wfmod.Domain()
     d.set("device", gpu)
     d.set("precision", precision)
-    case = build_domain(d)
+    case = build_domain(d, v_top=v_top)
     d.prepare(case.dt)
     d.step(max(warmup, 3))
     ms, launches = d.step_timed(steps)
@@ -662,9 +666,11 @@ def main():
         raise
     forms = {}
     head = None
-    for name, prec in (("mixed", wfmod.PRECISION_MIXED), ("fp64", wfmod.PRECISION_FP64)):
-        d, case, _, _, nnz = time_form(wfmod, prec, 1, warmup, gpu)
+    for name, prec, vt in (("mixed", wfmod.PRECISION_MIXED, V_TOP), ("fp64", wfmod.PRECISION_FP64, V_TOP),
+                           ("mixed_yielding", wfmod.PRECISION_MIXED, V_TOP_YIELD)):
+        d, case, _, _, nnz = time_form(wfmod, prec, 1, warmup, gpu, v_top=vt)
         steps = a.steps
+        s0 = d.geti("nb_searches")
         barrier(pg)
         if have_torch_cuda:
             torch.cuda.synchronize()
@@ -675,13 +681,15 @@ def main():
         barrier(pg)
         ms_max = reduce_max(pg, ms)
         val = world * case.n * steps / (ms_max * 1e-3)
+        searches = d.geti("nb_searches") - s0
         rl = roofline(d, case, nnz, steps, peak, peak_kind)
         forms[name] = {"value": val, "ms_per_step": ms_max / steps, "steps": steps, "roofline": rl,
-                       "gpu_launches": launches, "clocks": clk.summary()}
+                       "gpu_launches": launches, "clocks": clk.summary(), "v_top": vt,
+                       "rebuilds_in_timed_steps": searches}
         if name == "mixed":
             head = (case, nnz)
             xm, sm = d.get_array("Displacement"), d.get_array("Sigma")
-        else:
+        elif name == "fp64":
             xf, sf = d.get_array("Displacement"), d.get_array("Sigma")
         d.close()
     case, nnz = head

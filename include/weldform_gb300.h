@@ -298,23 +298,27 @@ int wf_profile_steps(wf_domain* d, int64_t nsteps, char* names, int name_len, do
                      int64_t* launches, int cap, int* nkernels);
 
 /* ---- fixed-footprint neighbour search (no counterpart in the reference) ---
- * For callers that cannot allocate device memory (graph-captured sections
- * that must stay free of allocation nodes, memory pools owned by another
- * library, real-time loops where an allocation may stall or fail): the same
- * cell-list search and radius rule as a domain rebuild, over caller-owned
- * device buffers, with its working memory in one file-scope device array of
- * fixed size (about 10 MB per GPU that loads the library, held until exit).
+ * For callers that cannot allocate device memory (code running inside a
+ * memory pool owned by another library, plugin hosts that forbid device
+ * allocations, real-time loops where an allocation may stall or fail): the
+ * same cell-list search and radius rule as a domain rebuild, over
+ * caller-owned device buffers, with its working memory in one file-scope
+ * device array of fixed size (about 10 MB per GPU that loads the library,
+ * held until exit).
  * x, y, z, h: n device doubles each; the cell grid as CellInitiate computes it
  * (BLPF, CellSize, CellNo; Neighbour.cpp:10-139) and Cellfac.  Outputs:
  * row_len[n] and nbr (device, n * 100 ints, entry k of particle i at
- * k * n + i, rows ordered j > i ascending then j < i ascending); a row
- * length of 101 marks a row cut at 100 entries.  Work is enqueued on
- * `stream` (a cudaStream_t, NULL for the default stream); nothing is
- * allocated or freed.  Limits: n <= WF_STATIC_MAX_PARTICLES and
- * CellNo.x * CellNo.y * CellNo.z <= WF_STATIC_MAX_CELLS, else WF_ERR_ARG.
- * All calls share the one array: calls that overlap on the GPU race.  The
- * first call on a device resolves the array's address with that device
- * current — make it before any stream capture. */
+ * k * n + i, rows ordered j > i ascending then j < i ascending).  A row with
+ * more than 100 neighbours gets length 101 and holds its 100 smallest keys
+ * (the reference writes past its arrays there; a domain rebuild reports
+ * WF_ERR_NBR_OVERFLOW instead).  Work is enqueued on `stream` (a cudaStream_t,
+ * NULL for the default stream); nothing is allocated or freed.  Limits:
+ * n <= WF_STATIC_MAX_PARTICLES and CellNo.x * CellNo.y * CellNo.z <=
+ * WF_STATIC_MAX_CELLS, else WF_ERR_ARG.  All calls share the one array: calls
+ * that overlap on the GPU race.  The first call on a device resolves the
+ * array's address with that device current — make it before any stream
+ * capture; the look-up is repeated after the device's context has been
+ * re-created (cudaDeviceReset). */
 #define WF_STATIC_MAX_PARTICLES 262144
 #define WF_STATIC_MAX_CELLS 1048576
 int wf_neighbour_list_static(const double* x, const double* y, const double* z, const double* h,

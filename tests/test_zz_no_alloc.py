@@ -1,13 +1,16 @@
 """wf_neighbour_list_static: the fixed-footprint neighbour search.
 
-Callers that cannot allocate device memory (a graph-captured section that must
-stay free of allocation nodes, a pool owned by another library, a real-time
-loop) pass their own input and output buffers; the search's working memory is
-a fixed device array inside the library.  This checks, through the C ABI, that
-two calls in a row give exactly the neighbour rows of the domain's own rebuild
-(integer output: the tolerance is equality), and that a size beyond the fixed
-maximum is refused with a clear error.  The file is collected last so a run
-that stops at the first failure has already run every other test.
+Callers that cannot allocate device memory (code inside a memory pool owned
+by another library, a plugin host that forbids device allocations, a
+real-time loop) pass their own input and output buffers; the search's working
+memory is a fixed device array inside the library.  This checks, through the
+C ABI, that two calls in a row give exactly the neighbour rows of the
+domain's own rebuild (integer output: the tolerance is equality), that rows
+with more than 100 neighbours are cut at their 100 smallest keys, and that
+sizes beyond the fixed maximum — including a cell grid whose cell count
+overflows 32 bits — are refused with a clear error.  The file is collected
+last so a run that stops at the first failure has already run every other
+test.
 """
 import ctypes
 import math
@@ -115,3 +118,70 @@ def test_static_search_refuses_sizes_beyond_its_maximum():
             None)
     assert rc == 1
     assert b"cells" in lib.wf_last_error()
+    # three counts near 2^31: their product overflows 64-bit arithmetic too
+    big = 2 ** 31 - 1
+    cn3 = (ctypes.c_int32 * 3)(big, big, big)
+    rc = fn(t.data_ptr(), t.data_ptr(), t.data_ptr(), t.data_ptr(), 8, cb, cc, cn3, 2.0, r.data_ptr(), r.data_ptr(),
+            None)
+    assert rc == 1
+    assert b"cells" in lib.wf_last_error()
+
+
+def _cut_rows_cpu(x, h, cellfac, keep=100):
+    """Rows of all pairs passing CheckRadius (the same IEEE operations as the
+    library: ((dx^2 + dy^2) + dz^2), sqrt, / ((hi + hj) / 2)), each kept at
+    its `keep` smallest canonical keys (j - i - 1 as unsigned)."""
+    n = len(x)
+    rows, lens = [], []
+    for i in range(n):
+        d = x[i] - x
+        r = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2])
+        ok = r / ((h[i] + h) / 2.0) <= cellfac
+        ok[i] = False
+        j = np.nonzero(ok)[0]
+        key = (j - i - 1).astype(np.int64) % (2 ** 32)
+        j = j[np.argsort(key, kind="stable")]
+        lens.append(len(j) if len(j) <= keep else keep + 1)
+        rows.append(j[:keep])
+    return rows, lens
+
+
+def test_static_search_cuts_dense_rows_at_their_smallest_keys():
+    """A cubic lattice with h = 2.5 spacings (pair radius 5 spacings: ~500
+    neighbours per interior particle), one cell spanning the domain so every
+    pair is a candidate: each cut row holds its 100 smallest keys and has
+    length 101; rows that fit are complete.  Two calls agree."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import weldform_gb300 as wf
+    s = 1e-3
+    g = np.arange(8) * s
+    x = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)
+    x = x + np.random.default_rng(3).uniform(-1e-3, 1e-3, x.shape) * s
+    n = len(x)
+    h = np.full(n, 2.5 * s)
+    want_rows, want_len = _cut_rows_cpu(x, h, 2.0)
+    assert max(want_len) == 101 and min(want_len) < 101
+    lib = wf.load_library()
+    fn = _bind(lib)
+    dev = torch.device("cuda:0")
+    X = [torch.tensor(np.ascontiguousarray(x[:, k]), dtype=torch.float64, device=dev) for k in range(3)]
+    H = torch.tensor(h, dtype=torch.float64, device=dev)
+    lo = x.min(axis=0) - 1.5 * s
+    cb = (ctypes.c_double * 3)(*lo)
+    cc = (ctypes.c_double * 3)(*(np.full(3, 11.0 * s)))
+    cn = (ctypes.c_int32 * 3)(1, 1, 1)
+    for call in range(2):
+        rl = torch.full((n,), -7, dtype=torch.int32, device=dev)
+        nb = torch.full((100 * n,), -7, dtype=torch.int32, device=dev)
+        rc = fn(X[0].data_ptr(), X[1].data_ptr(), X[2].data_ptr(), H.data_ptr(), n, cb, cc, cn, 2.0,
+                rl.data_ptr(), nb.data_ptr(), None)
+        assert rc == 0, lib.wf_last_error()
+        torch.cuda.synchronize()
+        rl_h = rl.cpu().numpy()
+        nb_h = nb.cpu().numpy().reshape(100, n)
+        assert np.array_equal(rl_h, np.array(want_len))
+        for i in range(n):
+            k = min(rl_h[i], 100)
+            assert np.array_equal(nb_h[:k, i], want_rows[i]), i

@@ -3,20 +3,22 @@
 // canonical row order), for callers that cannot allocate device memory.
 //
 // Who needs this: code that runs where cudaMalloc is off limits — inside a
-// host callback or a section being captured into a CUDA graph that must not
-// contain allocation nodes, inside another library's memory pool that owns
-// every byte, or in a real-time loop where an allocation could stall or fail.
-// Such a caller owns its input and output buffers; the only working memory
-// this search needs (cell histogram, cell offsets, cell-sorted particle list)
-// lives in one file-scope device array below, reserved when the library is
-// loaded and kept by every GPU that loads it until the process exits.
+// host callback, inside another library's memory pool that owns every byte of
+// the device, in a plugin host that forbids device allocations, or in a
+// real-time loop where an allocation could stall or fail.  Such a caller owns
+// its input and output buffers; the only working memory this search needs
+// (cell histogram, cell offsets, cell-sorted particle list) lives in one
+// file-scope device array below, reserved when the library is loaded and kept
+// by every GPU that loads it until the process exits.
 //
 // Limits: at most WF_STATIC_MAX_PARTICLES particles and WF_STATIC_MAX_CELLS
 // grid cells per call (about 10 MB of scratch per device).  Every call uses
 // the same array, so calls whose work overlaps on the GPU (two streams, or
 // two host threads) race and must be serialised by the caller.  The first call
 // on a device looks up the array's device address (cudaGetSymbolAddress) with
-// that device current; make that first call before any stream capture.
+// that device current; make that first call before any stream capture.  The
+// look-up is repeated when the device's context has been destroyed and
+// re-created since the last call (cudaDeviceReset), which reloads the array.
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -103,18 +105,6 @@ __global__ void k_static_scatter(Scratch* s, int n) {
   s->sorted[s->cell_start[c] + atomicAdd(&s->cell_count[c], 1)] = p;
 }
 
-// Deterministic order inside each cell (ascending particle index).
-__global__ void k_static_sort_cells(Scratch* s, int ncells) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  int b = s->cell_start[c], e = s->cell_start[c + 1];
-  for (int k = b + 1; k < e; ++k) {
-    int v = s->sorted[k], m = k - 1;
-    while (m >= b && s->sorted[m] > v) { s->sorted[m + 1] = s->sorted[m]; --m; }
-    s->sorted[m + 1] = v;
-  }
-}
-
 __global__ void __launch_bounds__(128) k_static_rows(Scratch* s, Grid g, const double* x, const double* y,
                                                      const double* z, const double* h, int n, int32_t* row_len,
                                                      int32_t* nbr) {
@@ -143,25 +133,57 @@ __global__ void __launch_bounds__(128) k_static_rows(Scratch* s, Grid g, const d
           double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
           if (!(__ddiv_rn(r, hh) <= g.cellfac)) continue;
           unsigned kk = (unsigned)(j - i - 1);  // j > i ascending, then j < i ascending
-          if (cnt < kMaxNb) {
-            int m = cnt - 1;
-            while (m >= 0 && keys[m] > kk) { keys[m + 1] = keys[m]; row[m + 1] = row[m]; --m; }
-            keys[m + 1] = kk;
-            row[m + 1] = j;
-            ++cnt;
-          } else {
+          // Sorted insertion that keeps the kMaxNb smallest keys: the row does
+          // not depend on the order in which the cells list their particles.
+          int m = cnt - 1;
+          if (cnt == kMaxNb) {
             over = true;
+            if (kk > keys[kMaxNb - 1]) continue;
+            m = kMaxNb - 2;  // the largest key drops out
+          } else {
+            ++cnt;
           }
+          while (m >= 0 && keys[m] > kk) { keys[m + 1] = keys[m]; row[m + 1] = row[m]; --m; }
+          keys[m + 1] = kk;
+          row[m + 1] = j;
         }
       }
     }
   }
   for (int k = 0; k < cnt; ++k) nbr[(size_t)k * n + i] = row[k];
-  row_len[i] = over ? kMaxNb + 1 : cnt;  // 101: the row was cut at 100 entries
+  row_len[i] = over ? kMaxNb + 1 : cnt;  // 101: the row was cut at its 100 smallest keys
 }
 
+// The array's device address per device, with the identity of the context it
+// was looked up in (cuCtxGetId, reached through the runtime's driver entry
+// points so the library needs no link to the driver library).
 std::mutex g_mu;
 void* g_addr[64] = {nullptr};
+unsigned long long g_ctx_id[64] = {0};
+
+unsigned long long current_context_id() {
+  typedef int (*GetCurrent)(void**);
+  typedef int (*GetId)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;  // unknown: the cached address is kept
+}
 
 }  // namespace
 
@@ -177,11 +199,12 @@ extern "C" int wf_neighbour_list_static(const double* x, const double* y, const 
   long long ncells = 1;
   for (int d = 0; d < 3; ++d) {
     if (cell_no[d] <= 0 || !(cell_size[d] > 0)) return fail(WF_ERR_ARG, "wf_neighbour_list_static: empty cell grid");
+    if (cell_no[d] > kMaxCells / ncells)  // checked before the product can overflow
+      return fail(WF_ERR_ARG, "wf_neighbour_list_static: the cell grid " + std::to_string(cell_no[0]) + " x " +
+                                  std::to_string(cell_no[1]) + " x " + std::to_string(cell_no[2]) +
+                                  " exceeds the fixed maximum of " + std::to_string(kMaxCells) + " cells");
     ncells *= cell_no[d];
   }
-  if (ncells > kMaxCells)
-    return fail(WF_ERR_ARG, "wf_neighbour_list_static: " + std::to_string(ncells) +
-                                " cells exceed the fixed maximum of " + std::to_string(kMaxCells));
   if (n == 0) return WF_OK;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
@@ -189,12 +212,16 @@ extern "C" int wf_neighbour_list_static(const double* x, const double* y, const 
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {  // set-up on the first call on this device (keep it outside stream capture)
+    unsigned long long ctx = current_context_id();
+    // set-up on the first call on this device, and again in a re-created
+    // context (keep the first call outside stream capture)
+    if (!g_addr[dev] || (ctx != 0 && ctx != g_ctx_id[dev])) {
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
       if (e != cudaSuccess)
         return fail(WF_ERR_CUDA, std::string("wf_neighbour_list_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       g_addr[dev] = p;
+      g_ctx_id[dev] = ctx;
     }
     base = g_addr[dev];
   }
@@ -208,7 +235,6 @@ extern "C" int wf_neighbour_list_static(const double* x, const double* y, const 
   k_static_hist<<<(nn + 255) / 256, 256, 0, st>>>(s, g, x, y, z, nn);
   k_static_scan<<<1, 1024, 0, st>>>(s, nc);
   k_static_scatter<<<(nn + 255) / 256, 256, 0, st>>>(s, nn);
-  k_static_sort_cells<<<(nc + 255) / 256, 256, 0, st>>>(s, nc);
   k_static_rows<<<(nn + 127) / 128, 128, 0, st>>>(s, g, x, y, z, h, nn, row_len, nbr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(WF_ERR_CUDA, std::string("wf_neighbour_list_static: ") + cudaGetErrorString(e));
