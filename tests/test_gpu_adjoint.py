@@ -187,15 +187,51 @@ def test_penalty_contact_workload_53k():
         for rel, fd in fds.items():
             print(f"tangent-linear vs central differences (step {rel}):",
                   dict(zip(PARAMS, (np.abs(ga - fd) / np.abs(fd)).round(8))))
-    # E moves every particle's elastic predictor, so the loss has a kink
-    # wherever a particle's trial stress meets its yield stress (load and
-    # unload of the bar waves): central differences of E average the slope
-    # over many such kinks at every step tried (1.5e-3 to 6e-3 measured),
-    # while the adjoint matches the tangent-linear derivative to 1e-11 above.
-    bound = {"E": 2e-3}
-    for p in ("E", "A", "B", "n", "C", "PFAC"):
+    # E is held to the tangent-linear derivative above but not to central
+    # differences here: with plastic heating on, the loss is a smooth function
+    # plus a staircase.  The plastic heat source q = Sigma : Strain_pl_incr /
+    # dt keeps the last plastic increment after a particle turns elastic
+    # (quirk Q3, Particle.cpp:924-938), so a particle whose last plastic step
+    # moves across its yield surface switches between heating from a tiny and
+    # from a full increment for the rest of the run: a jump of the loss.  The
+    # jumps drift in one direction as E grows, so central differences carry a
+    # bias (5.7e-3 to 6e-3 at steps 1e-5 to 1e-4) that no step size removes.
+    # The next test runs the workload with plastic heating off, where the
+    # staircase is gone and E meets 1e-3 at every step.
+    for p in ("A", "B", "n", "C", "PFAC"):
         q = PARAMS.index(p)
-        assert min(abs(ga[q] - fd[q]) / abs(fd[q]) for fd in fds.values()) <= bound.get(p, 1e-3), p
+        assert min(abs(ga[q] - fd[q]) / abs(fd[q]) for fd in fds.values()) <= 1e-3, p
+
+
+@pytest.mark.slow
+def test_e_gradient_finite_differences_without_plastic_heating_53k():
+    """The 53k penalty-contact workload with plastic heating off (conduction
+    on): the loss has no Q3 staircase, and the adjoint's dL/dE agrees with
+    central differences to 1e-3 at every step from 1e-5 to 1e-4 (A too;
+    PFAC at the best step)."""
+    case = adj.ContactCase()
+    steps, every = 400, 10
+    build = adj.build
+
+    def no_heating(dom, c, th):
+        mesh = build(dom, c, th)
+        dom.set("pl_heating", 0)
+        return mesh
+    adj.build = no_heating
+    try:
+        prob = adj.Problem(case, steps, every, adj.perturbed_jc_target(case, steps, every))
+        _, g = prob.loss_grad(np.zeros(len(PARAMS)))
+        fds = {rel: adj.central_fd(prob, rel, only=("E", "A", "PFAC")) for rel in (1e-4, 3e-5, 1e-5)}
+    finally:
+        adj.build = build
+    for p in ("E", "A", "PFAC"):
+        q = PARAMS.index(p)
+        errs = {rel: abs(g[q] - fd[q]) / abs(fd[q]) for rel, fd in fds.items()}
+        print(p, g[q], errs)
+        if p == "PFAC":
+            assert min(errs.values()) <= 1e-3, (p, errs)
+        else:
+            assert max(errs.values()) <= 1e-3, (p, errs)
 
 
 @pytest.mark.slow
