@@ -28,6 +28,9 @@ Measurement modes (each prints its own output instead of the bench line):
         the mixed form against the plain FP64 form from the same start
     python bench.py --pipe-rates
         FP64/FP32 arithmetic and copy rates of the GPU (roofline ceilings)
+    python bench.py --sweep [--specimens 256] [--steps 500] [--precision 1] [--autotune]
+        the batched parameter sweep (uneven specimens in one domain, each with
+        its own rebuild schedule) against every specimen run alone
 """
 from __future__ import annotations
 
@@ -549,6 +552,61 @@ def pipe_rates_mode():
             sys.exit(r.returncode)
 
 
+def sweep_mode(a):
+    """Seeded specimens (radius 4-12 mm, L/D 1-2, dx = 0.5 mm, JC constants
+    within +-20 %, punch speed 0.5-5 m/s) stepped together in one batched
+    domain, then every specimen alone in its own domain for the same steps
+    (CUDA-graph steps between CUDA events after 2 warm-up steps in both).
+    One JSON line: aggregate particle-steps/s of both ways, their ratio, the
+    per-specimen search counts compared with the solo runs', and specimen 0's
+    displacement difference between the two."""
+    import weldform_gb300 as wfmod
+    from weldform_gb300 import batch
+    specs = batch.random_specimens(a.specimens)
+    d = wfmod.Domain()
+    d.set("precision", a.precision)
+    t0 = time.perf_counter()
+    sw = batch.build_sweep(d, specs, dx=0.0005)
+    d.prepare(sw.dt)
+    setup = time.perf_counter() - t0
+    block = d.autotune(3) if a.autotune else d.geti("gather_block")
+    lanes = d.geti("gather_lanes")
+    d.step(2)
+    ms, launches = d.step_timed(a.steps)
+    together = sw.n * a.steps / (ms * 1e-3)
+    a0, b0 = sw.ranges[0]
+    u_together = d.get_array("Displacement")[a0:b0]
+    searches = [d.batch_get(k, "nb_searches") for k in range(len(specs))]
+    d.close()
+    seq_ms, seq_particles, solo_searches, u_alone = 0.0, 0, [], None
+    t1 = time.perf_counter()
+    for k, s in enumerate(specs):
+        e = wfmod.Domain()
+        e.set("precision", a.precision)
+        one = batch.build_single(e, s, k, dx=0.0005)
+        e.prepare(one.dt)
+        e.step(2)
+        ms1, _ = e.step_timed(a.steps)
+        seq_ms += ms1
+        seq_particles += one.n
+        solo_searches.append(e.geti("nb_searches"))
+        if k == 0:
+            u_alone = e.get_array("Displacement")
+        e.close()
+    alone = seq_particles * a.steps / (seq_ms * 1e-3)
+    du = float(np.linalg.norm(u_together - u_alone) / max(np.linalg.norm(u_alone), 1e-300))
+    print(json.dumps({
+        "specimens": len(specs), "particles": sw.n, "steps": a.steps, "precision": a.precision,
+        "gather_block": block, "gather_lanes": lanes, "setup_s": setup,
+        "batched_particle_steps_per_s": together, "batched_ms_per_step": ms / a.steps, "launches": launches,
+        "sequential_specimens_timed": len(specs), "sequential_particle_steps_per_s": alone,
+        "sequential_wall_s": time.perf_counter() - t1,
+        "batched_over_sequential": together / alone,
+        "search_counts_equal_solo": searches == solo_searches,
+        "searches_min_max": [min(searches), max(searches)],
+        "specimen0_displacement_rel_l2_batched_vs_alone": du}))
+
+
 def dist_setup(n):
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
@@ -589,7 +647,8 @@ def main():
     ap.add_argument("--accuracy", action="store_true", help="mixed form against the plain FP64 form")
     ap.add_argument("--pipe-rates", action="store_true", help="arithmetic and copy rates of the GPU")
     ap.add_argument("--n", type=int, default=250000, help="--case: particle count")
-    ap.add_argument("--precision", type=int, default=0, help="--case: 0 plain FP64, 1 mixed")
+    ap.add_argument("--precision", type=int, default=None,
+                    help="--case (default 0) / --sweep (default 1): 0 plain FP64, 1 mixed")
     ap.add_argument("--v-top", type=float, default=-1.0, help="--case/--accuracy: top or punch velocity (m/s)")
     ap.add_argument("--kernels", action="store_true", help="--case: per-kernel CUDA-event times")
     ap.add_argument("--gather-block", type=int, default=None, help="--case: threads per mixed gather block")
@@ -597,11 +656,15 @@ def main():
     ap.add_argument("--gather-lanes", type=int, default=None, help="--case: lanes per particle, acceleration gather")
     ap.add_argument("--dx-mm", default=None, help="--accuracy: lattice spacings (mm, comma-separated)")
     ap.add_argument("--contact", action="store_true", help="--accuracy: penalty-contact workload")
+    ap.add_argument("--sweep", action="store_true", help="batched sweep against every specimen alone")
+    ap.add_argument("--specimens", type=int, default=256, help="--sweep: specimens")
+    ap.add_argument("--autotune", action="store_true", help="--sweep: autotune the batched domain's gathers")
     a = ap.parse_args()
     if a.config_table:
         print(json.dumps(config_table()))
         return
     if a.case:
+        a.precision = 0 if a.precision is None else a.precision
         return case_mode(a)
     if a.accuracy:
         if a.steps == ap.get_default("steps"):
@@ -609,6 +672,11 @@ def main():
         return accuracy_mode(a)
     if a.pipe_rates:
         return pipe_rates_mode()
+    if a.sweep:
+        if a.steps == ap.get_default("steps"):
+            a.steps = 500
+        a.precision = 1 if a.precision is None else a.precision
+        return sweep_mode(a)
     warmup = max(a.warmup, 3)
     rank, world, local, pg = dist_setup(a.gpus)
 

@@ -94,7 +94,9 @@ int wf_domain_destroy(wf_domain* d);
  * "precision" (WF_PRECISION_*), "device" (CUDA device ordinal, before the
  * prologue), "use_graph" (replay each step as one CUDA graph, default 1),
  * "gather_block" (threads per block of the mixed form's gathers: 64, 128,
- * 256 or 512), "gather_staging" (1: the mixed acceleration gather reads each
+ * 256 or 512), "gather_lanes" (lanes per particle of the mixed acceleration
+ * gather: 1, 2, 4 or 8; the lanes walk one row and combine their Kahan
+ * partials by warp shuffles; default 1), "gather_staging" (1: the mixed acceleration gather reads each
  * 128-particle block's neighbours from a shared-memory copy of their records,
  * built at every search; set before the prologue, default 0) and
  * "stage_cap" (its halo capacity per block, 64..1024, default 896, before
@@ -106,7 +108,7 @@ int wf_domain_destroy(wf_domain* d);
  * default 0 keeps the reference's behaviour of stepping on with NaN; no
  * reference counterpart; before the prologue), "cpu_threads" (unused on
  * the GPU path).  Read back with wf_get_domain_i32: "gather_block",
- * "gather_staging", "stage_cap". */
+ * "gather_lanes", "gather_staging", "stage_cap". */
 int wf_set_domain_f64(wf_domain* d, const char* name, double value);
 int wf_set_domain_i32(wf_domain* d, const char* name, int value);
 /* Read-back of scalars: "Time", "deltat", "hmax", "int_energy_sum",
@@ -233,6 +235,23 @@ int wf_get_neighbours(wf_domain* d, int64_t* offsets, int32_t* idx, int64_t cap)
  * entries = rigid-mesh particles, ascending; same calling convention. */
 int wf_get_contact_pairs(wf_domain* d, int64_t* offsets, int32_t* idx, int64_t cap);
 
+/* ---- batched specimens (no counterpart in the reference, which runs one
+ * domain per process) ---------------------------------------------------------
+ * Partitions the particles, by original index, into nspec specimens
+ * [first[s], first[s] + count[s]) that are stepped together in every launch
+ * but each keep the rebuild schedule a run of that specimen alone would have
+ * (SolverKickDrift.cpp:153-186, 315-324: the first step, the first step with a
+ * particle past MIN_PS_FOR_NBSEARCH, then every ts_nb_inc steps while
+ * yielding).  A search serves the specimens that ask for one; the others keep
+ * their rows.  Specimens are meant to be spatially apart (no pair between two
+ * of them).  Every particle must belong to exactly one specimen; before the
+ * prologue; contact and gradKernelCorr are WF_ERR_UNSUPPORTED, and so is the
+ * adjoint on such a domain. */
+int wf_batch_specimens(wf_domain* d, const int64_t* first, const int64_t* count, int nspec);
+/* Per-specimen read-back: "nb_searches" (searches the specimen asked for),
+ * "yielding" (1 once it has yielded), "first", "particle_count". */
+int wf_batch_get_i32(wf_domain* d, int spec, const char* name, int64_t* value);
+
 /* Blocks until the domain's stream is idle and reports deferred device
  * status (non-finite state, neighbour overflow, bounded-wait timeout). */
 int wf_synchronize(wf_domain* d);
@@ -247,12 +266,14 @@ int wf_checkpoint_save(wf_domain* d, int slot);
 int wf_checkpoint_restore(wf_domain* d, int slot);
 int wf_checkpoint_free(wf_domain* d, int slot);
 
-/* Chooses the thread-block size of the mixed form's three gather kernels
- * (64, 128, 256 or 512 threads) by timing `steps` steps with each from a
- * checkpoint of the current state, restores that state, keeps the fastest
- * and returns it; results are cached per size bucket (particles rounded to a
- * power of two) for later domains in the process.  The block size is also
- * domain field "gather_block", settable after the prologue. */
+/* Chooses the launch shape of the mixed form's gather kernels — threads per
+ * block (64, 128, 256 or 512) and lanes per particle of the acceleration
+ * gather (1, 2 or 4) — by timing `steps` steps with every pair from a
+ * checkpoint of the current state, restores that state, keeps the fastest and
+ * returns its block size; results are cached per size bucket (particles
+ * rounded up to a power of two) for later domains in the process.  The choice
+ * is also domain fields "gather_block" and "gather_lanes", settable after the
+ * prologue. */
 int wf_autotune(wf_domain* d, int steps, int* block);
 
 /* ---- reaction-force adjoint (no counterpart in the reference) ------------

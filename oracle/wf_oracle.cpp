@@ -296,6 +296,14 @@ struct Domain {
   double Time = 0, deltat = 0, prev_deltat = 0;
   bool isfirst = true, isyielding = false, nb_cleared = false, check_nb_every_time = false;
   int ts_i = 0;
+  // Batched specimens: particle -> specimen, and each specimen's own rebuild
+  // schedule (the SolverKickDrift.cpp:153-186, 315-324 state of a run of that
+  // specimen alone).  A specimen that does not search keeps its rows.
+  struct SpecSched { bool isyielding = false, nb_cleared = true; int ts_i = 0; double max_pl = 0; int64_t searches = 0; };
+  int nspec = 0;
+  std::vector<int> spec_of;
+  std::vector<int64_t> spec_first, spec_count;
+  std::vector<SpecSched> spec;
   int64_t steps = 0, nb_searches = 0;
   double int_energy_sum = 0, kin_energy_sum = 0, plastic_work = 0, contact_force_sum = 0, contact_reaction_sum = 0,
          ext_forces_work = 0, m_maxT = 0, m_minT = 0, max_pl = 0;
@@ -1291,6 +1299,8 @@ struct Domain {
   // -------------------------------------------------------------- solver
   int prepare(double dt) {  // SolverKickDrift.cpp:23-115
     if (N == 0) return set_err(WF_ERR_STATE, "no particles");
+    if (nspec > 0 && (contact || grad_corr || mode == 1))
+      return set_err(WF_ERR_UNSUPPORTED, "batched specimens: no contact, gradKernelCorr or reference-structured mode");
     if (dim != 3) return set_err(WF_ERR_UNSUPPORTED, "only Dimension = 3 is supported");
     if (grad_corr && mode == 1)
       return set_err(WF_ERR_UNSUPPORTED, "kernel-gradient correction runs the locking sums (cpu_mode 0)");
@@ -1321,6 +1331,7 @@ struct Domain {
     }
     nb_cleared = true;  // ClearNbData
     steps = 0; isfirst = true; isyielding = false; ts_i = 0; check_nb_every_time = false;
+    for (auto& q : spec) q = SpecSched();
     prev_deltat = deltat;
     prepared = true;
     return WF_OK;
@@ -1358,6 +1369,7 @@ struct Domain {
       for (int j = 0; j < 3; j++) if (disp[i].c[j] * disp[i].c[j] > md.c[j]) md.c[j] = disp[i].c[j] * disp[i].c[j];
     for (int j = 0; j < 3; j++) md.c[j] = std::sqrt(md.c[j]);
     check_nb_every_time = norm(md) > 0.1 * hmax;
+    if (nspec > 0) return batch_schedule();
     if (mx > MIN_PS_FOR_NBSEARCH && !isyielding) {
       nb_cleared = true;
       if ((rc = neighbour_search())) return rc;
@@ -1376,6 +1388,47 @@ struct Domain {
     // (SolverKickDrift.cpp:189-191); the leapfrog solver after every regular
     // search and at the first step (SolverLeapfrog.cpp:186-204).
     if (grad_corr && (isfirst || (integrator == 1 && regular))) calc_grad_corr();
+    return WF_OK;
+  }
+  // Each specimen's rebuild decision (first yield, or its own ts_nb_inc
+  // cadence while yielding, SolverKickDrift.cpp:153-186) from the largest
+  // plastic strain of its own particles; one search serves every specimen that
+  // asks, and the others keep their rows.
+  int batch_schedule() {
+    std::vector<double> mxs(nspec, 0.0);
+    for (int i = 0; i < N; i++)
+      if (pl_strain[i] > mxs[spec_of[i]]) mxs[spec_of[i]] = pl_strain[i];
+    std::vector<char> srch(nspec, 0);
+    bool any = false;
+    for (int q = 0; q < nspec; ++q) {
+      SpecSched& sq = spec[q];
+      sq.max_pl = mxs[q];
+      if (mxs[q] > MIN_PS_FOR_NBSEARCH && !sq.isyielding) {
+        srch[q] = 1;
+        sq.isyielding = true;
+      } else if ((mxs[q] > MIN_PS_FOR_NBSEARCH || isfirst) && sq.ts_i == 0 && sq.nb_cleared) {
+        srch[q] = 1;
+      }
+      if (srch[q]) { sq.nb_cleared = false; sq.searches++; any = true; }
+    }
+    if (!any) return WF_OK;
+    std::vector<int64_t> off0 = nb_off;
+    std::vector<int> idx0 = nb_idx;
+    int rc = neighbour_search();
+    if (rc) return rc;
+    std::vector<int64_t> off1(N + 1, 0);
+    std::vector<int> idx1;
+    idx1.reserve(nb_idx.size());
+    for (int i = 0; i < N; ++i) {
+      bool fresh = srch[spec_of[i]] != 0;
+      const std::vector<int64_t>& o = fresh ? nb_off : off0;
+      const std::vector<int>& x = fresh ? nb_idx : idx0;
+      for (int64_t k = o[i]; k < o[i + 1]; ++k) idx1.push_back(x[k]);
+      off1[i + 1] = (int64_t)idx1.size();
+      Nb[i] = (int)(off1[i + 1] - off1[i]);
+    }
+    nb_off.swap(off1);
+    nb_idx.swap(idx1);
     return WF_OK;
   }
   // UpdateSmoothingLength (Domain.cpp:2493-2510): h -= h/3 (dDensity/Density) dt
@@ -1490,6 +1543,12 @@ struct Domain {
       ts_i++;
       if (ts_i > (ts_nb_inc - 1)) ts_i = 0;
     }
+    for (auto& q : spec)  // each specimen's own cadence
+      if (q.max_pl > MIN_PS_FOR_NBSEARCH) {
+        if (q.ts_i == (ts_nb_inc - 1)) q.nb_cleared = true;
+        q.ts_i++;
+        if (q.ts_i > (ts_nb_inc - 1)) q.ts_i = 0;
+      }
   }
 };
 
@@ -1637,6 +1696,36 @@ int wfo_get_domain_f64(wfo_domain* p, const char* name, double* v) {
   else if (n == "m_minT") *v = d->m_minT;
   else if (n == "tangent_mismatch") *v = d->tangent_mismatch;
   else return set_err(WF_ERR_ARG, "unknown domain f64 read " + n);
+  return WF_OK;
+}
+int wfo_batch_specimens(wfo_domain* p, const int64_t* first, const int64_t* count, int nspec) {
+  Domain* d = D(p);
+  if (nspec < 1 || !first || !count) return set_err(WF_ERR_ARG, "batch: nspec >= 1 and both arrays are required");
+  std::vector<int> of(d->N, -1);
+  for (int q = 0; q < nspec; ++q) {
+    if (first[q] < 0 || count[q] < 1 || first[q] + count[q] > d->N) return set_err(WF_ERR_ARG, "batch: range out of bounds");
+    for (int64_t i = first[q]; i < first[q] + count[q]; ++i) {
+      if (of[i] >= 0) return set_err(WF_ERR_ARG, "batch: specimens overlap");
+      of[i] = q;
+    }
+  }
+  for (int v : of) if (v < 0) return set_err(WF_ERR_ARG, "batch: every particle must belong to a specimen");
+  d->nspec = nspec;
+  d->spec_of = of;
+  d->spec_first.assign(first, first + nspec);
+  d->spec_count.assign(count, count + nspec);
+  d->spec.assign(nspec, Domain::SpecSched());
+  return WF_OK;
+}
+int wfo_batch_get_i32(wfo_domain* p, int q, const char* name, int64_t* v) {
+  Domain* d = D(p);
+  std::string n(name ? name : "");
+  if (q < 0 || q >= d->nspec) return set_err(WF_ERR_ARG, "batch: no such specimen");
+  if (n == "nb_searches") *v = d->spec[q].searches;
+  else if (n == "yielding") *v = d->spec[q].isyielding ? 1 : 0;
+  else if (n == "first") *v = d->spec_first[q];
+  else if (n == "particle_count") *v = d->spec_count[q];
+  else return set_err(WF_ERR_ARG, "batch: unknown field " + n);
   return WF_OK;
 }
 int wfo_get_domain_i32(wfo_domain* p, const char* name, int64_t* v) {

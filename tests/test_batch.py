@@ -52,3 +52,57 @@ def test_sweep_equals_single_runs_in_the_oracle():
 def test_sweep_equals_single_runs_on_the_gpu():
     sw, tog, alo = _sweep_vs_single(gpu_domain)
     _check(tog, alo, 1e-9)
+
+
+# Specimens that yield at different times (20, 8 and 0.5 m/s punches): each
+# keeps its own rebuild schedule, so a batched specimen searches exactly when
+# it does alone and its state matches its solo run.
+_JC = SPECS[0].jc
+UNEVEN = [batch.Specimen(R=0.003, L=0.006, v_punch=-20.0, jc=_JC),
+          batch.Specimen(R=0.0035, L=0.005, v_punch=-0.5, jc=_JC),
+          batch.Specimen(R=0.0025, L=0.006, v_punch=-8.0, jc=_JC)]
+
+
+def _uneven(make, steps=60):
+    d = make()
+    sw = batch.build_sweep(d, UNEVEN, dx=DX)
+    d.prepare(sw.dt)
+    d.step(steps)
+    tog = [_fields(d, a, b) for a, b in sw.ranges]
+    searches = [d.batch_get(k, "nb_searches") for k in range(len(UNEVEN))]
+    d.close()
+    alo, solo_searches = [], []
+    for k, s in enumerate(UNEVEN):
+        e = make()
+        one = batch.build_single(e, s, k, dx=DX)
+        e.prepare(one.dt)
+        e.step(steps)
+        alo.append(_fields(e, 0, one.n))
+        solo_searches.append(e.geti("nb_searches"))
+        e.close()
+    return tog, alo, searches, solo_searches
+
+
+def test_each_specimen_keeps_its_own_schedule_in_the_oracle():
+    tog, alo, searches, solo = _uneven(oracle_domain)
+    assert searches == solo
+    assert len(set(searches)) > 1  # the specimens really rebuild at different steps
+    _check(tog, alo, 1e-9)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_each_specimen_keeps_its_own_schedule_on_the_gpu(precision):
+    """Per-specimen search counts equal the solo runs' and the oracle's batch;
+    the batched state matches the solo runs (1e-9 plain; the mixed form's
+    records are kept relative to each domain's own grid centre, so 1e-6) and
+    the oracle's batch (1e-9 plain, 1e-4 mixed)."""
+    def make():
+        d = gpu_domain()
+        d.set("precision", precision)
+        return d
+    tog, alo, searches, solo = _uneven(make)
+    otog, _, osearches, _ = _uneven(oracle_domain)
+    assert searches == solo == osearches
+    _check(tog, alo, 1e-9 if precision == 0 else 1e-6)
+    _check(tog, otog, 1e-9 if precision == 0 else 1e-4)

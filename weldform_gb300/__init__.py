@@ -99,6 +99,8 @@ _SIGS = {
     "autotune": [_P, _I, ctypes.POINTER(_I)],
     "profile_steps": [_P, _I64, ctypes.c_char_p, _I, _DP, _I64P, _I, ctypes.POINTER(_I)],
     "adjoint_reaction_loss": [_P, _I64, _I, _I, _I, _DP, _I64, _I, _DP, _DP, _DP, _DP, _DP],
+    "batch_specimens": [_P, _I64P, _I64P, _I],
+    "batch_get_i32": [_P, _I, _S, _I64P],
 }
 EXPORTS = ["version", "last_error"] + list(_SIGS)
 
@@ -367,6 +369,19 @@ class Domain:
             return
         a = np.ascontiguousarray(values, dtype=np.float64).ravel()
         self._call("set_particle_array_f64", self._h, field.encode(), a.ctypes.data_as(_DP), a.size)
+
+    # ------------------------------------------------------------ batches
+    def batch_specimens(self, ranges):
+        """Specimens as [first, last) ranges of original particle indices,
+        each with its own rebuild schedule (wf_batch_specimens)."""
+        first = np.array([a for a, _ in ranges], dtype=np.int64)
+        count = np.array([b - a for a, b in ranges], dtype=np.int64)
+        self._call("batch_specimens", self._h, first.ctypes.data_as(_I64P), count.ctypes.data_as(_I64P), len(ranges))
+
+    def batch_get(self, spec: int, name: str) -> int:
+        v = ctypes.c_int64()
+        self._call("batch_get_i32", self._h, int(spec), name.encode(), ctypes.byref(v))
+        return int(v.value)
 
     def _rows(self, which: str):
         n = self.particle_count

@@ -8,14 +8,14 @@ specimens; one domain holds them all, so every kernel launch of a step
 advances every specimen and the GPU load-balances across specimens of uneven
 size for free (the unit of work is the particle, not the specimen).
 
-Differences from running each specimen in its own domain:
-  * masses are set per specimen (AddCylinderLength, Domain.cpp:840-855,
-    divides the last cylinder's volume by the count of *all* particles and
-    assigns it to every particle; a multi-body domain needs per-body masses);
-  * the neighbour-rebuild schedule (SolverKickDrift.cpp:153-186, 315-324) is
-    the domain's: once any specimen yields, every specimen's list is rebuilt
-    every ts_nb_inc steps.  A specimen's result changes only if one of its
-    pairs crosses the cutoff between two rebuilds it would otherwise skip.
+Each specimen keeps the neighbour-rebuild schedule a run of it alone would
+have (SolverKickDrift.cpp:153-186, 315-324): the domain is partitioned with
+``Domain.batch_specimens`` (wf_batch_specimens), a search serves only the
+specimens that ask for one, and the others keep their rows.  Masses are set
+per specimen (AddCylinderLength, Domain.cpp:840-855, divides the last
+cylinder's volume by the count of *all* particles and assigns it to every
+particle; a multi-body domain needs per-body masses).  A specimen then evolves
+as it does alone, up to the rounding of its coordinates' offset.
 """
 from __future__ import annotations
 
@@ -123,6 +123,8 @@ def build_sweep(dom, specimens: Sequence[Specimen], dx: float = 0.0005, mat: Ste
     dom.set_particles("T", mat.T0)
     dom.set_particles("k_T", mat.k_T)
     dom.set_particles("cp_T", mat.cp_T)
+    if len(ranges) > 1:
+        dom.batch_specimens(ranges)
     return Sweep(specimens=list(specimens), ranges=ranges, offsets=offsets, dx=dx, h=h, dt=cfl * h / mat.Cs, n=n)
 
 

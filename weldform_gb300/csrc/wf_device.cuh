@@ -51,10 +51,11 @@ enum F64Col : int {
 enum I32Col : int {
   I_ID = 0, I_IDORIG, I_NWS, I_MAT, I_MODEL, I_FAIL, I_MATERIAL, I_NB, I_KIND, I_ELEM, I_MESH, I_ORIG,
   I_THBC = 12,             // Thermal_BC (Particle.h:69): 1 = convection (TH_BC_CONVECTION)
-  NI32_PERSIST = 13,
-  I_CELL = 13,             // scratch: cell key (Morton rank) of the particle at its pre-search position
-  I_CLASS = 14,            // scratch: pair-rule class word in sorted order
-  NI32 = 15
+  I_SPEC = 13,             // specimen of a batched domain (0 otherwise)
+  NI32_PERSIST = 14,
+  I_CELL = 14,             // scratch: cell key (Morton rank) of the particle at its pre-search position
+  I_CLASS = 15,            // scratch: pair-rule class word in sorted order
+  NI32 = 16
 };
 
 // ---- float4 field groups of the mixed form -----------------------------------
@@ -194,6 +195,16 @@ struct StepState {
   int nan_count;       // particles with a non-finite position at the last search
 };
 
+// Rebuild schedule of one specimen of a batched domain: the state a run of
+// that specimen alone keeps (SolverKickDrift.cpp:153-186, 315-324).
+struct SpecState {
+  int yielded_next;    // a particle of the specimen has pl_strain > MIN_PS_FOR_NBSEARCH (after this step)
+  int yielded;         // ... at the start of the current step
+  int isyielding, ts_i, nb_cleared;
+  int do_search;       // the specimen searches this step
+  long long searches;
+};
+
 // Per-domain constants (set once at the solver prologue; small, by value).
 struct DomainConst {
   int N, Nsolid, nbc_particles;
@@ -239,6 +250,7 @@ struct DomainConst {
   int stage_cap;       // halo capacity of the staged gathers (0: staging off)
   int freeze_nb;       // 1: neighbour and contact topology searched only at the first step
   int nan_check;       // 1: a non-finite position at a search, or non-finite energy sums, raise ERR_NAN
+  int nspec;           // batched specimens with their own rebuild schedules (0: one schedule)
 };
 
 // Device pointers, passed by value to every kernel.
@@ -284,6 +296,9 @@ struct DevPtrs {
   double* partials;       // NSLOTS * nblocks
   long long* scan_tmp;
   double* tx;             // step tape of the adjoint's recompute (TapeCol columns), null otherwise
+  SpecState* sp;          // batched domain: one schedule per specimen
+  int* save_len;          // batched domain: rows of the specimens that do not search, kept across
+  int* save_nbr;          // the search's reordering (original indices, ELL by old position)
 };
 
 // Per-step values the plain form writes for the adjoint when DevPtrs::tx is

@@ -127,6 +127,8 @@ struct wf_domain {
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int freeze_nb = 0;  // search only at the first step (finite-difference checks of the adjoint)
   int nan_check = 0;  // raise WF_ERR_NAN on a non-finite position at a search or non-finite energy sums
+  // batched specimens (wf_batch_specimens): [first, first + count) in original order
+  std::vector<int64_t> spec_first, spec_count;
   int ts_nb_inc = 5, pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1, contact_alg = 0;
   int precision = WF_PRECISION_FP64, use_graph = 1, device = 0;
   int integrator = 0;  // 0 kick-drift, 1 leapfrog
@@ -608,6 +610,9 @@ struct wf_domain {
     K.pre_eps = (float)(eps < 0.05 ? std::max(eps, 1e-5) : 2.0);
     K.freeze_nb = freeze_nb;
     K.nan_check = nan_check;
+    K.nspec = (int)spec_first.size();
+    if (K.nspec > 0 && (contact || grad_corr))
+      throw CudaError{WF_ERR_UNSUPPORTED, "batched specimens: contact and gradKernelCorr are not supported"};
     K.ts_nb_inc = ts_nb_inc; K.pl_heating = pl_heating; K.thermal_solver = thermal_solver; K.contact = contact;
     K.contact_mesh_auto_update = contact_mesh_auto_update; K.contact_alg = contact_alg;
     K.pl_work_heat_frac = pl_work_heat_frac; K.friction_sta = friction_sta; K.friction_dyn = friction_dyn;
@@ -641,6 +646,14 @@ struct wf_domain {
     for (size_t m = 0; m < meshes.size(); ++m)
       for (int d = 0; d < 3; ++d) { st.mesh_v[m][d] = meshes[m].mv.c[d]; st.mesh_w[m][d] = meshes[m].mw.c[d]; }
     CK(cudaMemcpyAsync(P.st, &st, sizeof(st), cudaMemcpyHostToDevice, stream));
+    if (K.nspec > 0) {  // one rebuild schedule per specimen, as a run of it alone starts
+      std::vector<SpecState> sp(K.nspec);
+      for (SpecState& q : sp) { memset(&q, 0, sizeof(q)); q.nb_cleared = 1; }
+      P.sp = dalloc<SpecState>(K.nspec);
+      CK(cudaMemcpyAsync(P.sp, sp.data(), sizeof(SpecState) * K.nspec, cudaMemcpyHostToDevice, stream));
+      P.save_len = dalloc<int>(n);
+      P.save_nbr = dalloc<int>((size_t)MAX_NB * n);
+    }
     regions = {{d_f, sizeof(double) * NF64 * n}, {d_i, sizeof(int) * NI32 * n}, {P.g, sizeof(float) * NF32 * n},
                {P.st, sizeof(StepState)}, {P.inv, sizeof(int) * n}, {P.row_len, sizeof(int) * n},
                {P.row_split, sizeof(int) * n}, {P.nbr, sizeof(int) * MAX_NB * n}, {P.cp_len, sizeof(int) * n},
@@ -650,6 +663,7 @@ struct wf_domain {
     if (stage_ready)
       regions.insert(regions.end(), {{P.halo, sizeof(int) * nsb * stage_cap}, {P.halo_len, sizeof(int) * nsb},
                                      {P.nslot, sizeof(unsigned short) * MAX_NB * n}});
+    if (K.nspec > 0) regions.push_back({P.sp, sizeof(SpecState) * K.nspec});
     launch_prologue(P, K, stream);
     // SolverKickDrift.cpp:72-96: with contact, a search + CalculateSurface(1)
     // before the loop; the first step searches again (ClearNbData).
@@ -929,6 +943,7 @@ struct wf_domain {
       throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint runs on the plain FP64 form (precision 0)"};
     if (K.ti) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: tensile instability (TI > 0) is not supported"};
     if (K.leapfrog) throw CudaError{WF_ERR_UNSUPPORTED, "the adjoint differentiates the kick-drift step"};
+    if (K.nspec > 0) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: batched specimens are not supported"};
     if (K.gradcorr) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: kernel-gradient correction is not supported"};
     if (K.auto_ts || K.auto_ts_acc) throw CudaError{WF_ERR_UNSUPPORTED, "adjoint: the time step must be fixed"};
     if (!contact || mesh < 0 || mesh >= (int)meshes.size())
@@ -1112,33 +1127,41 @@ struct wf_domain {
     if (fwd_ms) *fwd_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     if (adj_ms) *adj_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
   }
+  // Launch shape of the mixed gathers: threads per block (64..512) and lanes
+  // per particle of the acceleration gather (1, 2, 4), timed over `steps`
+  // steps from a checkpoint for every pair; the fastest pair is kept, the
+  // state restored, and the choice cached per size bucket (particle count
+  // rounded up to a power of two).
   int autotune(int steps) {
     static std::mutex mu;
-    static std::map<int, int> cache;  // size bucket -> block
+    static std::map<int, std::pair<int, int>> cache;  // size bucket -> (block, lanes)
     int bucket = 0;
     while ((1LL << bucket) < hp.N) ++bucket;
     {
       std::lock_guard<std::mutex> lk(mu);
       auto it = cache.find(bucket);
-      if (it != cache.end()) { gblock = it->second; return gblock; }
+      if (it != cache.end()) { gblock = it->second.first; glanes = it->second.second; return gblock; }
     }
     const int slot = 15;
     checkpoint_save(slot);
-    int best = 256;
+    int best = 256, best_lanes = 1;
     double best_ms = 1e300;
-    for (int b : {64, 128, 256, 512}) {
-      gblock = b;
-      long long l = 0;
-      step(1);  // capture + warm
-      checkpoint_restore(slot);
-      double ms = step_timed(steps, &l);
-      checkpoint_restore(slot);
-      if (ms < best_ms) { best_ms = ms; best = b; }
-    }
+    for (int lanes : {1, 2, 4})
+      for (int b : {64, 128, 256, 512}) {
+        gblock = b;
+        glanes = lanes;
+        long long l = 0;
+        step(1);  // capture + warm
+        checkpoint_restore(slot);
+        double ms = step_timed(steps, &l);
+        checkpoint_restore(slot);
+        if (ms < best_ms) { best_ms = ms; best = b; best_lanes = lanes; }
+      }
     gblock = best;
+    glanes = best_lanes;
     checkpoint_free(slot);
     std::lock_guard<std::mutex> lk(mu);
-    cache[bucket] = best;
+    cache[bucket] = {best, best_lanes};
     return best;
   }
   void search_now() {
@@ -1414,6 +1437,46 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     else if (n == "nb_searches") *v = st.nb_searches;
     else if (n == "surface_count") *v = st.surface_count;
     else return set_err(WF_ERR_ARG, "unknown domain i32 read " + n);
+    return WF_OK;
+  });
+}
+int wf_batch_specimens(wf_domain* d, const int64_t* first, const int64_t* count, int nspec) {
+  NEED(d);
+  if (d->prepared) return set_err(WF_ERR_STATE, "specimens are fixed after the prologue");
+  if (nspec < 1 || !first || !count) return set_err(WF_ERR_ARG, "batch: nspec >= 1 and both arrays are required");
+  const int64_t n = d->hp.N;
+  std::vector<int> of(n, -1);
+  for (int q = 0; q < nspec; ++q) {
+    if (first[q] < 0 || count[q] < 1 || first[q] + count[q] > n) return set_err(WF_ERR_ARG, "batch: range out of bounds");
+    for (int64_t i = first[q]; i < first[q] + count[q]; ++i) {
+      if (of[i] >= 0) return set_err(WF_ERR_ARG, "batch: specimens overlap");
+      of[i] = q;
+    }
+  }
+  for (int v : of)
+    if (v < 0) return set_err(WF_ERR_ARG, "batch: every particle must belong to a specimen");
+  for (int64_t i = 0; i < n; ++i) d->hp.i[wf::I_SPEC][i] = of[i];
+  d->spec_first.assign(first, first + nspec);
+  d->spec_count.assign(count, count + nspec);
+  return WF_OK;
+}
+int wf_batch_get_i32(wf_domain* d, int spec, const char* name, int64_t* v) {
+  NEED(d);
+  return guard([&] {
+    std::string n(name ? name : "");
+    if (spec < 0 || spec >= (int)d->spec_first.size()) return set_err(WF_ERR_ARG, "batch: no such specimen");
+    if (n == "first") { *v = d->spec_first[spec]; return WF_OK; }
+    if (n == "particle_count") { *v = d->spec_count[spec]; return WF_OK; }
+    wf::SpecState q;
+    memset(&q, 0, sizeof(q));
+    if (d->prepared) {
+      d->use_device();
+      CK(cudaMemcpyAsync(&q, d->P.sp + spec, sizeof(q), cudaMemcpyDeviceToHost, d->stream));
+      CK(cudaStreamSynchronize(d->stream));
+    }
+    if (n == "nb_searches") *v = q.searches;
+    else if (n == "yielding") *v = q.isyielding;
+    else return set_err(WF_ERR_ARG, "batch: unknown field " + n);
     return WF_OK;
   });
 }

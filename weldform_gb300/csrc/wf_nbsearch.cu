@@ -68,6 +68,24 @@ __global__ void k_cell_keys(DevPtrs P, DomainConst K) {
   }
 }
 
+// Batched domain, before the reordering: the rows of particles whose specimen
+// does not search this step are saved by old position, each entry as the
+// neighbour's original index (with the larger-index bit), so k_nbr_fill can
+// put them back at the particles' new positions.
+__global__ void k_rows_save(DevPtrs P, DomainConst K) {
+  if (!searching(P)) return;
+  const size_t N = K.N;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
+    if (P.sp[P.i[I_SPEC * N + p]].do_search) continue;
+    int len = P.row_len[p];
+    P.save_len[p] = len;
+    for (int k = 0; k < len; ++k) {
+      int e = P.nbr[(size_t)k * N + p];
+      P.save_nbr[(size_t)k * N + p] = P.i[I_ORIG * N + nb_index(e)] | (int)((unsigned)e & NB_UP);
+    }
+  }
+}
+
 __global__ void k_zero_int(DevPtrs P, int* a, long long n, int gate) {
   if (gate && !searching(P)) return;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) a[k] = 0;
@@ -294,7 +312,19 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   bool overflow = false;
   // A particle in a shadow bucket (non-finite position) has an empty row.
   const int key_i = i < K.N ? P.i[I_CELL * N + P.perm[i]] : 0;
-  if (i < K.N && kind[i] == 0 && key_i < K.ncells) {
+  // Batched domain: a specimen that does not search keeps its rows (saved by
+  // k_rows_save in canonical order; their keys here keep that order).
+  const bool keep = K.nspec > 0 && i < K.N && !P.sp[P.i[I_SPEC * N + i]].do_search;
+  if (keep) {
+    const int old = P.perm[i];
+    cnt = P.save_len[old];
+    for (int e = lane; e < cnt; e += 32) {
+      int v = P.save_nbr[(size_t)e * N + old];
+      rkey[e] = (unsigned)e;
+      ridx[e] = P.inv[v & 0x7fffffff] | (int)((unsigned)v & NB_UP);
+    }
+    __syncwarp();
+  } else if (i < K.N && kind[i] == 0 && key_i < K.ncells) {
     float4 pi = reinterpret_cast<const float4*>(P.xs)[i];
     // The particle's cell: the key it was sorted by (k_cell_keys evaluated the
     // reference's FP64 cell formula once per particle), mapped back to grid
@@ -542,6 +572,10 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   int nz = grid(nbk);
   k_search_begin<<<1, 1, 0, s>>>(P);
   mark(s, "k_search_begin");
+  if (K.nspec > 0) {
+    k_rows_save<<<grid(K.N), T, 0, s>>>(P, K);
+    mark(s, "k_rows_save");
+  }
   k_zero_int<<<nz, T, 0, s>>>(P, P.cell_count, nbk, 1);
   mark(s, "k_zero_int");
   k_cell_keys<<<grid(K.N), T, 0, s>>>(P, K);

@@ -88,6 +88,16 @@ __device__ __forceinline__ void rec_set_v3(const DevPtrs& P, size_t N, int i, co
   for (int d = 0; d < 3; ++d) *lo_v_half(r + (size_t)RC_L * N, d) = bf16_bits(l[d]);
 }
 
+// Batched domain: flag the particle's specimen as yielding once its plastic
+// strain passes the rebuild threshold (Domain.cpp:28), the per-specimen form of
+// the max-plastic-strain test of the rebuild schedule.
+__device__ __forceinline__ void mark_yield(const DevPtrs& P, const DomainConst& K, size_t N, int i, double pl) {
+  if (K.nspec > 0 && pl > MIN_PS_FOR_NBSEARCH) {
+    SpecState* sp = P.sp + icol(P, I_SPEC, N, i);
+    if (!sp->yielded_next) sp->yielded_next = 1;
+  }
+}
+
 // Amplitude lookup (SPH::amplitude::getValAtTime, Source/Domain.h:69-89).
 __device__ __forceinline__ double amp_value(const DomainTables* T, int amp_id, double t, bool* found) {
   for (int k = 0; k < T->namp; ++k) {

@@ -39,8 +39,31 @@ thread_local long long g_launches = 0;
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------- schedule
+// One block.  A batched domain decides per specimen (the same rules on the
+// specimen's own state) and searches when any specimen asks.
 __global__ void k_schedule(DevPtrs P, DomainConst K) {
   StepState* s = P.st;
+  __shared__ int any_search, any_regular;
+  if (threadIdx.x == 0) { any_search = 0; any_regular = 0; }
+  __syncthreads();
+  for (int q = threadIdx.x; q < K.nspec; q += blockDim.x) {
+    SpecState& sp = P.sp[q];
+    sp.yielded = sp.yielded_next;
+    int search = 0, regular = 0;
+    if (sp.yielded && !sp.isyielding) {
+      search = 1;
+      sp.isyielding = 1;
+    } else if ((sp.yielded || s->isfirst) && sp.ts_i == 0 && sp.nb_cleared) {
+      search = 1;
+      regular = 1;
+    }
+    if (K.freeze_nb && !s->isfirst) search = regular = 0;
+    if (search) { sp.nb_cleared = 0; sp.searches += 1; atomicOr(&any_search, 1); }
+    if (regular) atomicOr(&any_regular, 1);
+    sp.do_search = search;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   double mx = s->max_pl_next;
   s->max_pl = mx;
   int search = 0, regular = 0;
@@ -55,6 +78,7 @@ __global__ void k_schedule(DevPtrs P, DomainConst K) {
   // adjoint, which differentiates each step with its topology fixed): after
   // the first step's search the rows, contact pairs and surface flags stay.
   if (K.freeze_nb && !s->isfirst) search = regular = 0;
+  if (K.nspec > 0) { search = any_search; regular = any_regular; }
   if (search) s->nb_cleared = 0;
   s->do_search = search;
   // CalcGradCorrMatrix: kick-drift at its first step (SolverKickDrift.cpp:189-191),
@@ -64,6 +88,16 @@ __global__ void k_schedule(DevPtrs P, DomainConst K) {
 
 __global__ void k_step_end(DevPtrs P, DomainConst K) {
   StepState* s = P.st;
+  for (int q = threadIdx.x; q < K.nspec; q += blockDim.x) {  // each specimen's own cadence
+    SpecState& sp = P.sp[q];
+    if (sp.yielded) {
+      if (sp.ts_i == (K.ts_nb_inc - 1)) sp.nb_cleared = 1;
+      sp.ts_i++;
+      if (sp.ts_i > (K.ts_nb_inc - 1)) sp.ts_i = 0;
+    }
+    sp.do_search = 0;
+  }
+  if (threadIdx.x != 0) return;
   s->gk_valid = K.mixed ? 0 : 1;  // the plain rate pass left GradKernel at the new positions
   s->steps += 1;
   s->Time += s->deltat;
@@ -634,6 +668,7 @@ __global__ void __launch_bounds__(BLOCK) k_rate_stress(DevPtrs P, DomainConst K)
       colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
       colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = s.esr;
       maxpl = s.pl_strain;
+      mark_yield(P, K, N, i, s.pl_strain);
       double c2 = 1.0 / (rho * rho);
       for (int c = 0; c < 6; ++c) colw(P, C_SRHO + c, N, i) = c2 * s.sig[c];
       colw(P, C_PR2, N, i) = s.pressure / (rho * rho);
@@ -889,7 +924,7 @@ void launch_scatter_orig_i32(const DevPtrs& P, const DomainConst& K, const int* 
 
 // ---------------------------------------------------------------- one step
 void launch_step_head(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
-  k_schedule<<<1, 1, 0, s>>>(P, K);
+  k_schedule<<<1, 256, 0, s>>>(P, K);
   mark(s, "k_schedule");
   launch_neighbour_search(P, K, fscratch, iscratch, s);
   if (K.gradcorr) {
@@ -997,7 +1032,7 @@ void launch_step_tail(const DevPtrs& P, const DomainConst& K, cudaStream_t s) {
     k_mesh_elems<<<nblk(P.nelem, BLOCK), BLOCK, 0, s>>>(P, K);
     mark(s, "k_mesh_elems");
   }
-  k_step_end<<<1, 1, 0, s>>>(P, K);
+  k_step_end<<<1, 256, 0, s>>>(P, K);
   mark(s, "k_step_end");
 }
 

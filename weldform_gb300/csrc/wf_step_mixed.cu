@@ -769,6 +769,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_stress_mx(DevPtrs P, DomainConst K
       colw(P, C_P, N, i) = s.pressure; colw(P, C_PLS, N, i) = s.pl_strain; colw(P, C_DPLS, N, i) = s.delta_pl_strain;
       colw(P, C_SY, N, i) = s.sigmay; colw(P, C_EP, N, i) = s.Ep; colw(P, C_ESR, N, i) = (double)s.esr;
       maxpl = s.pl_strain;
+      mark_yield(P, K, N, i, s.pl_strain);
       // CalcIntEnergyEqn (Particle.cpp:941-950)
       dint = col(P, C_MRHO, N, i) * (s.tau[0] * srd[0] + 2.0 * s.tau[3] * srd[3] + 2.0 * s.tau[4] * srd[4] +
                                      s.tau[1] * srd[1] + 2.0 * s.tau[5] * srd[5] + s.tau[2] * srd[2]);
