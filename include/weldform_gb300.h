@@ -74,7 +74,13 @@ int wf_domain_destroy(wf_domain* d);
 /* Domain scalar fields (Source/Domain.h:113-537).  Names are the reference
  * member names: "Cellfac", "pl_work_heat_frac", "friction_sta",
  * "friction_dyn", "PFAC", "DFAC", "CFL", "sqrt_h_a", "DomMax.x|y|z",
- * "DomMin.x|y|z", "contact_force_factor".  Integer fields: "Nproc", "ts_nb_inc",
+ * "DomMin.x|y|z", "contact_force_factor", "nb_skin" (Verlet skin of the
+ * neighbour-search reuse, a fraction of the largest pair radius, default 0.1,
+ * 0 off; no reference counterpart: a full search also lists every particle
+ * within the pair radius plus the skin, and a later search whose particles
+ * have all moved less than half the skin since filters those lists with the
+ * exact pair rules instead of re-sorting — the rows are the same; on without
+ * contact and without batched specimens).  Integer fields: "Nproc", "ts_nb_inc",
  * "nonlock_sum", "pl_heating", "thermal_solver", "contact",
  * "contact_mesh_auto_update", "GradientType", "contact_alg" (WF_CONTACT_*),
  * "integrator" (0 kick-drift, 1 leapfrog; before the prologue),
@@ -116,7 +122,8 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int value);
  * "contact_reaction_sum", "ext_forces_work", "max_pl_strain", "m_maxT",
  * "m_minT"; integers: "particle_count", "solid_part_count", "steps",
  * "pair_count", "contact_pair_count", "nb_searches", "CellNo.x|y|z",
- * "surface_count", "dynamic_friction_count" (contact-pair evaluations since
+ * "surface_count", "nb_full_searches" (searches that re-sorted the particles;
+ * the rest filtered the skin lists), "dynamic_friction_count" (contact-pair evaluations since
  * the prologue that took the dynamic-friction branch, Contact_Wang.cpp:284-290;
  * no reference counterpart), "nan_particles" (particles whose position was not
  * finite at the last neighbour search: they get empty rows and appear in no

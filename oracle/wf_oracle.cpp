@@ -1651,7 +1651,7 @@ int wfo_set_domain_f64(wfo_domain* p, const char* name, double v) {
   else if (n == "CFL") d->CFL = v;
   else if (n == "sqrt_h_a") d->sqrt_h_a = v;
   else if (n == "DFAC") d->DFAC = v;
-  else if (n == "contact_force_factor") {}
+  else if (n == "contact_force_factor" || n == "nb_skin") {}  // nb_skin: a GPU search strategy, same rows
   else if (n.rfind("DomMax.", 0) == 0 && n.size() == 8) d->DomMax[n[7] - 'x'] = v;
   else if (n.rfind("DomMin.", 0) == 0 && n.size() == 8) d->DomMin[n[7] - 'x'] = v;
   else return set_err(WF_ERR_ARG, "unknown domain f64 field " + n);

@@ -266,6 +266,49 @@ def test_sliding_contact_dynamic_friction(stiffness):
     assert rel_l2(g["contforce"], o["contforce"]) <= 1e-6
 
 
+def test_skin_reuse_gives_the_rows_of_a_full_search():
+    """The Verlet-skin reuse of the search (default nb_skin 0.1): most
+    rebuilds of a yielding cylinder filter the skin lists instead of
+    re-sorting, the rows equal the oracle's after every kind of rebuild, and
+    the per-particle state is bit-identical to a run with the reuse off (the
+    particles' memory order differs, a row's summation order does not)."""
+    f = FIELDS + ("Strain_pl",)
+    runs = {}
+    for skin in (0.1, 0.0):
+        d = gpu_domain()
+        d.set_f64("nb_skin", skin)
+        case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+        d.prepare(case.dt)
+        rows = []
+        for _ in range(6):
+            d.step(20)
+            rows.append(d.neighbours())
+        runs[skin] = {k: d.get_array(k) for k in f}
+        runs[skin]["rows"] = rows
+        runs[skin]["searches"] = d.geti("nb_searches")
+        runs[skin]["full"] = d.geti("nb_full_searches")
+        runs[skin]["ie"] = d.get("int_energy_sum")
+        d.close()
+    on, off = runs[0.1], runs[0.0]
+    assert on["searches"] == off["searches"] > 20
+    assert off["full"] == off["searches"] and on["full"] < on["searches"] // 2
+    for k in f:
+        assert np.array_equal(on[k], off[k]), k
+    for a, b in zip(on["rows"], off["rows"]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert abs(on["ie"] - off["ie"]) <= 1e-12 * abs(off["ie"])
+    o = oracle_domain()
+    o.set("cpu_threads", THREADS)
+    case = configs.cylinder_upsetting(o, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+    o.prepare(case.dt)
+    o.step(120)
+    oo, oi = o.neighbours()
+    assert np.array_equal(on["rows"][-1][0], oo) and np.array_equal(on["rows"][-1][1], oi)
+    for k in f:
+        assert rel_l2(on[k], o.get_array(k)) <= TOL, k
+    o.close()
+
+
 def test_solve_loop_matches_reference_loop_control():
     res = {}
     for name in ("gpu", "oracle"):

@@ -122,6 +122,7 @@ constexpr int MAX_MESHES = 8;
 constexpr int MAX_NB = 100;  // MAX_NB_PER_PART, Source/Domain.h:49
 
 constexpr int MAX_CP = 64;   // contact pairs per particle
+constexpr int SUP_W = 128;   // superset entries per particle (skin reuse of the search)
 
 // Shared-memory staging of the mixed form's gathers.  Particles are taken in
 // blocks of STAGE_B consecutive (cell-sorted) particles; at every search each
@@ -192,6 +193,11 @@ struct StepState {
   int errors;
   int surface_count;
   unsigned long long dyn_friction;  // contact-pair evaluations that took the dynamic-friction branch
+  // Verlet-skin reuse of the neighbour search (DomainConst::skin_on)
+  unsigned long long maxdisp2_bits;  // largest squared displacement since the superset was built (as bits)
+  int search_full;     // this step's search re-sorts and rebuilds the superset (else: filter only)
+  int sup_valid;       // a superset exists and every row fitted in SUP_W
+  long long nb_full_searches;
   int nan_count;       // particles with a non-finite position at the last search
 };
 
@@ -251,6 +257,13 @@ struct DomainConst {
   int freeze_nb;       // 1: neighbour and contact topology searched only at the first step
   int nan_check;       // 1: a non-finite position at a search, or non-finite energy sums, raise ERR_NAN
   int nspec;           // batched specimens with their own rebuild schedules (0: one schedule)
+  // Verlet-skin reuse of the search: a full search also lists, per particle,
+  // every particle within its pair radius plus `skin` (canonical order); a
+  // later search whose particles have all moved less than skin / 2 since then
+  // filters those lists with the exact pair rules instead of re-sorting.
+  int skin_on;
+  double skin;         // absolute skin length
+  float sup_skip_r2;   // squared largest superset radius plus margin, in FP32 (cell pruning)
 };
 
 // Device pointers, passed by value to every kernel.
@@ -296,6 +309,10 @@ struct DevPtrs {
   double* partials;       // NSLOTS * nblocks
   long long* scan_tmp;
   double* tx;             // step tape of the adjoint's recompute (TapeCol columns), null otherwise
+  int* sup;               // skin: superset rows (ELL width SUP_W, canonical order, NB_UP flag)
+  int* sup_len;
+  double* xref;           // skin: positions when the superset was built (3 columns)
+  long long* cellc;       // skin: cell coordinates at the current search (21 bits each; -1 if not finite)
   SpecState* sp;          // batched domain: one schedule per specimen
   int* save_len;          // batched domain: rows of the specimens that do not search, kept across
   int* save_nbr;          // the search's reordering (original indices, ELL by old position)

@@ -127,6 +127,7 @@ struct wf_domain {
   double DomMin[3] = {100000000000.0, 100000000000.0, 100000000000.0};
   int freeze_nb = 0;  // search only at the first step (finite-difference checks of the adjoint)
   int nan_check = 0;  // raise WF_ERR_NAN on a non-finite position at a search or non-finite energy sums
+  double nb_skin = 0.1;  // Verlet skin of the search reuse, relative to the largest pair radius (0: off)
   // batched specimens (wf_batch_specimens): [first, first + count) in original order
   std::vector<int64_t> spec_first, spec_count;
   int ts_nb_inc = 5, pl_heating = 0, thermal_solver = 0, contact = 0, contact_mesh_auto_update = 1, contact_alg = 0;
@@ -613,6 +614,21 @@ struct wf_domain {
     K.nspec = (int)spec_first.size();
     if (K.nspec > 0 && (contact || grad_corr))
       throw CudaError{WF_ERR_UNSUPPORTED, "batched specimens: contact and gradKernelCorr are not supported"};
+    // Verlet-skin reuse of the search: on without contact (the contact search
+    // bins rigid-mesh particles that move with their planes) and without
+    // batched specimens; the superset radius must stay within two cells and
+    // each cell coordinate within 21 bits.
+    {
+      double rmax = Cellfac * hmax, skin = nb_skin * rmax;
+      bool fits = true;
+      for (int d = 0; d < 3; ++d) fits = fits && CellNo[d] < (1 << 21) && rmax + skin <= 2.0 * cs[d];
+      K.skin_on = (nb_skin > 0 && !contact && K.nspec == 0 && fits) ? 1 : 0;
+      K.skin = K.skin_on ? skin : 0.0;
+      double ext2 = 0.0;
+      for (int d = 0; d < 3; ++d) ext2 = std::max(ext2, CellNo[d] * cs[d]);
+      double r2 = (rmax + skin) * (1.0 + 1e-5) + 16.0 * 1.1920929e-7 * ext2;
+      K.sup_skip_r2 = (float)(r2 * r2 * (1.0 + 1e-5));
+    }
     K.ts_nb_inc = ts_nb_inc; K.pl_heating = pl_heating; K.thermal_solver = thermal_solver; K.contact = contact;
     K.contact_mesh_auto_update = contact_mesh_auto_update; K.contact_alg = contact_alg;
     K.pl_work_heat_frac = pl_work_heat_frac; K.friction_sta = friction_sta; K.friction_dyn = friction_dyn;
@@ -646,6 +662,12 @@ struct wf_domain {
     for (size_t m = 0; m < meshes.size(); ++m)
       for (int d = 0; d < 3; ++d) { st.mesh_v[m][d] = meshes[m].mv.c[d]; st.mesh_w[m][d] = meshes[m].mw.c[d]; }
     CK(cudaMemcpyAsync(P.st, &st, sizeof(st), cudaMemcpyHostToDevice, stream));
+    if (K.skin_on) {
+      P.sup = dalloc<int>((size_t)SUP_W * n);
+      P.sup_len = dalloc<int>(n);
+      P.xref = dalloc<double>((size_t)3 * n);
+      P.cellc = dalloc<long long>(n);
+    }
     if (K.nspec > 0) {  // one rebuild schedule per specimen, as a run of it alone starts
       std::vector<SpecState> sp(K.nspec);
       for (SpecState& q : sp) { memset(&q, 0, sizeof(q)); q.nb_cleared = 1; }
@@ -664,6 +686,9 @@ struct wf_domain {
       regions.insert(regions.end(), {{P.halo, sizeof(int) * nsb * stage_cap}, {P.halo_len, sizeof(int) * nsb},
                                      {P.nslot, sizeof(unsigned short) * MAX_NB * n}});
     if (K.nspec > 0) regions.push_back({P.sp, sizeof(SpecState) * K.nspec});
+    if (K.skin_on)
+      regions.insert(regions.end(), {{P.sup, sizeof(int) * SUP_W * n}, {P.sup_len, sizeof(int) * n},
+                                     {P.xref, sizeof(double) * 3 * n}});
     launch_prologue(P, K, stream);
     // SolverKickDrift.cpp:72-96: with contact, a search + CalculateSurface(1)
     // before the loop; the first step searches again (ClearNbData).
@@ -1221,6 +1246,7 @@ struct wf_domain {
     wf::launch_refresh_derived(P, K, stream);
     shadows_valid = false;
     invalidate_gk();
+    if (K.skin_on) CK(cudaMemsetAsync(&P.st->sup_valid, 0, sizeof(int), stream));  // positions or h moved
     CK(cudaStreamSynchronize(stream));
     if (c == wf::C_ALPHA || c == wf::C_BETA || c == wf::C_MASS || c == wf::C_H || c == wf::C_CS) refresh_uniform();
   }
@@ -1306,6 +1332,10 @@ int wf_set_domain_f64(wf_domain* d, const char* name, double v) {
   else if (n == "CFL") d->CFL = v;
   else if (n == "sqrt_h_a") d->sqrt_h_a = v;
   else if (n == "DFAC") d->DFAC = v;
+  else if (n == "nb_skin") {
+    if (!(v >= 0.0 && v <= 0.5)) return set_err(WF_ERR_ARG, "nb_skin must be in [0, 0.5]");
+    d->nb_skin = v;
+  }
   else if (n == "contact_force_factor") {}
   else if (n.size() == 8 && n.rfind("DomMax.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') d->DomMax[n[7] - 'x'] = v;
   else if (n.size() == 8 && n.rfind("DomMin.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') d->DomMin[n[7] - 'x'] = v;
@@ -1434,6 +1464,7 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     else if (n == "contact_pair_count") *v = st.contact_pair_count;
     else if (n == "dynamic_friction_count") *v = (int64_t)st.dyn_friction;
     else if (n == "nan_particles") *v = st.nan_count;
+    else if (n == "nb_full_searches") *v = st.nb_full_searches;
     else if (n == "nb_searches") *v = st.nb_searches;
     else if (n == "surface_count") *v = st.surface_count;
     else return set_err(WF_ERR_ARG, "unknown domain i32 read " + n);

@@ -29,6 +29,11 @@
 namespace wf {
 
 __device__ __forceinline__ bool searching(const DevPtrs& P) { return P.st->do_search != 0; }
+// The parts of a search that re-sort the particles run only when the search
+// is a full one (always, unless the Verlet-skin reuse is on).
+__device__ __forceinline__ bool searching_full(const DevPtrs& P) {
+  return P.st->do_search != 0 && P.st->search_full != 0;
+}
 
 // A particle with a non-finite coordinate cannot pass CheckRadius with any
 // other (its distance is NaN or infinite), so its row is empty and it is in
@@ -39,7 +44,7 @@ __device__ __forceinline__ bool searching(const DevPtrs& P) { return P.st->do_se
 // are the same and the search stays linear.  The shadow buckets are sorted
 // like cells, so the order stays deterministic.
 __global__ void k_cell_keys(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   int nonfinite = 0;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
   int c[3];
@@ -87,7 +92,7 @@ __global__ void k_rows_save(DevPtrs P, DomainConst K) {
 }
 
 __global__ void k_zero_int(DevPtrs P, int* a, long long n, int gate) {
-  if (gate && !searching(P)) return;
+  if (gate && !searching_full(P)) return;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) a[k] = 0;
 }
 
@@ -114,7 +119,7 @@ __device__ __forceinline__ long long block_exclusive_scan(long long v, long long
 }
 
 __global__ void k_scan_reduce(DevPtrs P, const int* in, long long n, long long* tot) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   __shared__ long long sh[SCAN_THREADS];
   long long base = (long long)blockIdx.x * SCAN_TILE;
   long long s = 0;
@@ -127,7 +132,7 @@ __global__ void k_scan_reduce(DevPtrs P, const int* in, long long n, long long* 
   if (threadIdx.x == 0) tot[blockIdx.x] = total;
 }
 __global__ void k_scan_top(DevPtrs P, long long* tot, int nb) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   __shared__ long long sh[SCAN_THREADS];
   long long carry = 0;
   for (int base = 0; base < nb; base += SCAN_THREADS) {
@@ -141,7 +146,7 @@ __global__ void k_scan_top(DevPtrs P, long long* tot, int nb) {
   }
 }
 __global__ void k_scan_down(DevPtrs P, const int* in, long long n, const long long* tot, int* out, int* total_out) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   __shared__ long long sh[SCAN_THREADS];
   long long base = (long long)blockIdx.x * SCAN_TILE;
   long long vals[SCAN_ITEMS];
@@ -162,7 +167,7 @@ __global__ void k_scan_down(DevPtrs P, const int* in, long long n, const long lo
 }
 
 __global__ void k_scatter(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
   int key = P.i[I_CELL * (size_t)K.N + p];
   int pos = P.cell_start[key] + atomicAdd(&P.cell_count[key], 1);
@@ -174,7 +179,7 @@ __global__ void k_scatter(DevPtrs P, DomainConst K) {
 // hold ~10-20 particles), and likewise the shadow buckets of non-finite
 // particles (at most ceil(N / ncells) each).
 __global__ void k_sort_cells(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < 2 * K.ncells; c += gridDim.x * blockDim.x) {
   int b = P.cell_start[c], e = P.cell_start[c + 1];
   const int* orig = P.i + I_ORIG * (size_t)K.N;
@@ -192,7 +197,7 @@ __global__ void k_sort_cells(DevPtrs P, DomainConst K) {
 // fixed grid strides over (column, particle) so the launch costs nothing on
 // steps that do not search.
 __global__ void k_permute(DevPtrs P, DomainConst K, double* fdst, int* idst) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   size_t N = K.N;
   size_t total = (size_t)(NF64_PERSIST + NI32_PERSIST) * N;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
@@ -206,7 +211,7 @@ __global__ void k_permute(DevPtrs P, DomainConst K, double* fdst, int* idst) {
   }
 }
 __global__ void k_copy_back(DevPtrs P, DomainConst K, const double* fsrc, const int* isrc) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   size_t nf = (size_t)NF64_PERSIST * K.N, ni = (size_t)NI32_PERSIST * K.N;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < nf + ni; k += (size_t)gridDim.x * blockDim.x) {
     if (k < nf) P.f[k] = fsrc[k];
@@ -223,7 +228,7 @@ __device__ __forceinline__ bool is_contact_id(const DomainConst& K, int id) {
 // Map original -> sorted index, element -> mesh particle, and the FP32
 // prefilter coordinates (relative to BLPF, plus h).
 __global__ void k_after_permute(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
   size_t N = K.N;
   int o = P.i[I_ORIG * N + p];
@@ -286,8 +291,19 @@ constexpr int FILL_WARPS = 8;                    // warps per block
 constexpr int FILL_ROWS = 32;                    // particles (rows) per block group
 constexpr int FILL_PER_WARP = FILL_ROWS / FILL_WARPS;
 constexpr int FILL_SLOTS = 128;
+// SUPER: the Verlet-skin superset instead of the rows: a 5 x 5 x 5 cell
+// stencil, every candidate within the pair radius plus the skin (FP32 with a
+// margin: extra entries are removed by the exact filter later), up to SUP_W
+// entries per particle in canonical order, and the positions they refer to.
+// A row that does not fit marks the superset invalid, and this search's rows
+// come from the exact form instead.
+template <bool SUPER>
 __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
+  if (SUPER) {
+    if (!searching_full(P) || !K.skin_on) return;
+  } else {
+    if (!searching_full(P) || (K.skin_on && P.st->sup_valid)) return;
+  }
   __shared__ __align__(16) unsigned s_key[FILL_ROWS][FILL_SLOTS];
   __shared__ int s_idx[FILL_ROWS][FILL_SLOTS];
   __shared__ int s_len[FILL_ROWS];
@@ -314,7 +330,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   const int key_i = i < K.N ? P.i[I_CELL * N + P.perm[i]] : 0;
   // Batched domain: a specimen that does not search keeps its rows (saved by
   // k_rows_save in canonical order; their keys here keep that order).
-  const bool keep = K.nspec > 0 && i < K.N && !P.sp[P.i[I_SPEC * N + i]].do_search;
+  const bool keep = !SUPER && K.nspec > 0 && i < K.N && !P.sp[P.i[I_SPEC * N + i]].do_search;
   if (keep) {
     const int old = P.perm[i];
     cnt = P.save_len[old];
@@ -340,9 +356,15 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     // the candidates: most corner and some edge cells).  Boxes of the
     // outermost cells extend to infinity outwards, since the cell index is
     // clamped there.
+    // The superset's stencil is 5 x 5 x 5 cells, taken 32 cells per round.
+    constexpr int W = SUPER ? 5 : 3, NC = W * W * W, ROUNDS = (NC + 31) / 32;
+    const float skip_r2 = SUPER ? K.sup_skip_r2 : K.cell_skip_r2;
+    for (int round = 0; round < ROUNDS; ++round) {
+    const int nq = NC - 32 * round < 32 ? NC - 32 * round : 32;  // stencil cells in this round
+    const int qc = 32 * round + lane;
     int cs = 0, cc = 0;
-    if (lane < 27) {
-      int q3[3] = {c[0] + lane / 9 - 1, c[1] + (lane / 3) % 3 - 1, c[2] + lane % 3 - 1};
+    if (lane < nq) {
+      int q3[3] = {c[0] + qc / (W * W) - W / 2, c[1] + (qc / W) % W - W / 2, c[2] + qc % W - W / 2};
       if (q3[0] >= 0 && q3[0] < K.CellNo[0] && q3[1] >= 0 && q3[1] < K.CellNo[1] && q3[2] >= 0 && q3[2] < K.CellNo[2]) {
         // FP32 on the prefilter coordinates x - BLPF (GB300 runs FP64 at 1/64
         // of the FP32 rate); the radius carries a margin above the FP32
@@ -359,7 +381,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
           inside = inside && xf[d] >= 0.f && xf[d] <= (float)K.CellNo[d] * K.CellSizef[d];
         }
         if (!inside) g2 = 0.f;
-        if (g2 <= K.cell_skip_r2) {
+        if (g2 <= skip_r2) {
           int key = P.cell_rank[(q3[0] * K.CellNo[1] + q3[1]) * K.CellNo[2] + q3[2]];
           cs = P.cell_start[key];
           cc = P.cell_start[key + 1] - cs;
@@ -380,8 +402,8 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
       int cell = 0;
       for (int step = 16; step > 0; step >>= 1) {
         int q = cell + step;
-        int ex = __shfl_sync(0xffffffffu, excl, q < 27 ? q : 26);
-        if (q < 27 && ex <= t) cell = q;
+        int ex = __shfl_sync(0xffffffffu, excl, q < nq ? q : nq - 1);
+        if (q < nq && ex <= t) cell = q;
       }
       int cstart = __shfl_sync(0xffffffffu, cs, cell);
       int cexcl = __shfl_sync(0xffffffffu, excl, cell);
@@ -392,8 +414,17 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
         j = cstart + (t - cexcl);
         if (j != i) {
           int cj = cls[j];
-          ok = !(K.contact && (ci || (cj & 2))) && (cj & 1) == 0 && (cj >> 2) == mi &&
-               radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, reinterpret_cast<const float4*>(P.xs)[j]);
+          ok = !(K.contact && (ci || (cj & 2))) && (cj & 1) == 0 && (cj >> 2) == mi;
+          if (ok) {
+            float4 pj = reinterpret_cast<const float4*>(P.xs)[j];
+            if (SUPER) {
+              float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+              float Rs = K.half_cellfac_f * (pi.w + pj.w) + (float)K.skin;
+              ok = dx * dx + dy * dy + dz * dz <= Rs * Rs * (1.0f + 4.0f * K.pre_eps);
+            } else {
+              ok = radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, pj);
+            }
+          }
           if (ok) kk = (unsigned)(orig[j] - oi - 1);
         }
       }
@@ -406,7 +437,8 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
       }
       cnt += __popc(m);
     }
-    if (cnt > MAX_NB) overflow = true;
+    }  // stencil rounds
+    if (cnt > (SUPER ? SUP_W : MAX_NB)) overflow = true;
     if (cnt > FILL_SLOTS) cnt = FILL_SLOTS;
   }
   // Order the row's slots by key.  Keys are distinct (one per neighbour), so
@@ -431,6 +463,17 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   for (int r = 0; r < 4; ++r)
     if (lane + 32 * r < cnt) ridx[rank[r]] = idx[r];
   __syncwarp();
+  if (SUPER) {
+    if (i < K.N && lane == 0) {
+      s_len[row] = cnt;
+      P.sup_len[i] = cnt;
+      if (overflow) P.st->sup_valid = 0;
+      for (int d = 0; d < 3; ++d) P.xref[(size_t)d * N + i] = P.f[(C_X + d) * N + i];
+    } else if (lane == 0) {
+      s_len[row] = 0;
+    }
+    continue;
+  }
   if (cnt > MAX_NB) cnt = MAX_NB;
   if (i < K.N) {
     for (int e = lane; e < cnt; e += 32) split += ridx[e] < 0 ? 1 : 0;
@@ -454,10 +497,118 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   for (int t = 0; t < FILL_ROWS; ++t) maxlen = max(maxlen, s_len[t]);
   for (int q = threadIdx.x; q < maxlen * FILL_ROWS; q += blockDim.x) {
     int k = q / FILL_ROWS, t = q - k * FILL_ROWS;
-    if (k < s_len[t]) P.nbr[(size_t)k * N + i0 + t] = s_idx[t][k];
+    if (k < s_len[t]) (SUPER ? P.sup : P.nbr)[(size_t)k * N + i0 + t] = s_idx[t][k];
   }
   __syncthreads();  // the shared buffers are reused by the next group
   }
+}
+
+// ---- Verlet-skin reuse -------------------------------------------------------
+// Largest squared displacement since the superset was built (a non-finite
+// position gives NaN, whose bit pattern exceeds every finite one: a full
+// search follows).
+__global__ void k_skin_check(DevPtrs P, DomainConst K) {
+  if (!searching(P) || !K.skin_on || !P.st->sup_valid) return;
+  const size_t N = K.N;
+  double m = 0.0;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
+    double d0 = P.f[(C_X + 0) * N + p] - P.xref[p];
+    double d1 = P.f[(C_X + 1) * N + p] - P.xref[N + p];
+    double d2 = P.f[(C_X + 2) * N + p] - P.xref[2 * N + p];
+    double d = d0 * d0 + d1 * d1 + d2 * d2;
+    if (!(d <= m)) m = d;
+  }
+  unsigned long long b = (unsigned long long)__double_as_longlong(m);
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_down_sync(0xffffffffu, b, off);
+    b = o > b ? o : b;
+  }
+  if ((threadIdx.x & 31) == 0 && b) atomicMax(&P.st->maxdisp2_bits, b);
+}
+
+// Full search or filter only: a filter suffices while every particle has
+// moved less than skin / 2 since the superset was built, since a pair within
+// its radius now was then within the radius plus the skin.
+__global__ void k_search_mode(DevPtrs P, DomainConst K) {
+  StepState* s = P.st;
+  if (!s->do_search) return;
+  const double md2 = __longlong_as_double((long long)s->maxdisp2_bits);
+  const double half = 0.5 * K.skin;
+  const bool filter_only = K.skin_on && s->sup_valid && md2 <= half * half;
+  s->search_full = filter_only ? 0 : 1;
+  if (!filter_only) {
+    s->nb_full_searches += 1;
+    if (K.skin_on) s->sup_valid = 1;  // the superset build clears it again if a row does not fit
+  }
+}
+
+// Cell coordinates at the current positions (ListGenerate's clamped cell
+// index, Neighbour.cpp:185-218, the same FP64 expression as k_cell_keys),
+// 21 bits per axis, -1 for a non-finite position; and the FP32 prefilter
+// coordinates.
+__global__ void k_cell_coords(DevPtrs P, DomainConst K) {
+  if (!searching(P) || !K.skin_on || !P.st->sup_valid) return;
+  const size_t N = K.N;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
+    long long code = 0;
+    bool finite = true;
+    for (int d = 0; d < 3; ++d) {
+      double xd = P.f[(C_X + d) * N + p];
+      finite = finite && isfinite(xd);
+      int q = (int)floor(__ddiv_rn(__dsub_rn(xd, K.BLPF[d]), K.CellSize[d]));
+      if (q < 0) q = 0;
+      if (q >= K.CellNo[d]) q = K.CellNo[d] - 1;
+      code = (code << 21) | (long long)q;
+    }
+    P.cellc[p] = finite ? code : -1;
+    reinterpret_cast<float4*>(P.xs)[p] =
+        make_float4((float)(P.f[(C_X + 0) * N + p] - K.BLPF[0]), (float)(P.f[(C_X + 1) * N + p] - K.BLPF[1]),
+                    (float)(P.f[(C_X + 2) * N + p] - K.BLPF[2]), (float)P.f[C_H * N + p]);
+  }
+}
+
+__device__ __forceinline__ bool cells_adjacent(long long a, long long b) {
+  for (int d = 0; d < 3; ++d) {
+    int qa = (int)((a >> (21 * d)) & 0x1fffff), qb = (int)((b >> (21 * d)) & 0x1fffff);
+    if (qa - qb > 1 || qb - qa > 1) return false;
+  }
+  return true;
+}
+
+// Rows from the superset: the entries whose particles sit in adjacent cells
+// now and pass the radius rule (FP32 prefilter, exact FP64 CheckRadius),
+// in the superset's canonical order — the rows a full search gives.
+__global__ void __launch_bounds__(256) k_nbr_filter(DevPtrs P, DomainConst K) {
+  if (!searching(P) || !K.skin_on || !P.st->sup_valid) return;
+  const size_t N = K.N;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K.N) return;
+  int cnt = 0, split = 0;
+  const long long ci = P.cellc[i];
+  if (P.i[I_KIND * N + i] == 0 && ci >= 0) {
+    const float4 pi = reinterpret_cast<const float4*>(P.xs)[i];
+    const int len = P.sup_len[i];
+    for (int k = 0; k < len; ++k) {
+      const int e = P.sup[(size_t)k * N + i];
+      const int j = nb_index(e);
+      const long long cj = P.cellc[j];
+      if (cj < 0 || !cells_adjacent(ci, cj)) continue;
+      if (!radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, reinterpret_cast<const float4*>(P.xs)[j])) continue;
+      if (cnt < MAX_NB) {
+        P.nbr[(size_t)cnt * N + i] = e;
+        split += nb_up(e) ? 1 : 0;
+      }
+      ++cnt;
+    }
+  }
+  if (cnt > MAX_NB) {
+    atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
+    cnt = MAX_NB;
+  }
+  P.row_len[i] = cnt;
+  P.row_split[i] = split;
+  P.i[I_NB * N + i] = cnt;
+  if (cnt) atomicAdd(&P.st->pair_count, (unsigned long long)cnt);
 }
 
 // CalculateSurface (Domain.cpp:1415-1491): n_i = sum_j m_j (x_i - x_j) in row
@@ -554,6 +705,7 @@ __global__ void k_search_begin(DevPtrs P) {
   P.st->contact_pair_count = 0;
   P.st->surface_count = 0;
   P.st->nan_count = 0;
+  P.st->maxdisp2_bits = 0;
   P.st->nb_searches += 1;
 }
 
@@ -572,6 +724,12 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   int nz = grid(nbk);
   k_search_begin<<<1, 1, 0, s>>>(P);
   mark(s, "k_search_begin");
+  if (K.skin_on) {
+    k_skin_check<<<grid(K.N), T, 0, s>>>(P, K);
+    mark(s, "k_skin_check");
+  }
+  k_search_mode<<<1, 1, 0, s>>>(P, K);
+  mark(s, "k_search_mode");
   if (K.nspec > 0) {
     k_rows_save<<<grid(K.N), T, 0, s>>>(P, K);
     mark(s, "k_rows_save");
@@ -602,9 +760,19 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   {
     // a few resident blocks per SM, striding over the row groups
     int groups = nblk(K.N, FILL_ROWS), cap = 152 * 4;
-    k_nbr_fill<<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
+    if (K.skin_on) {
+      k_nbr_fill<true><<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
+      mark(s, "k_sup_build");
+    }
+    k_nbr_fill<false><<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
   }
   mark(s, "k_nbr_fill");
+  if (K.skin_on) {
+    k_cell_coords<<<grid(K.N), T, 0, s>>>(P, K);
+    mark(s, "k_cell_coords");
+    k_nbr_filter<<<nblk(K.N, 256), 256, 0, s>>>(P, K);
+    mark(s, "k_nbr_filter");
+  }
   if (P.halo) launch_halo_build(P, K, s);
   if (K.contact) {
     k_surface<<<grid(K.N), T, 0, s>>>(P, K);
