@@ -266,17 +266,30 @@ def test_sliding_contact_dynamic_friction(stiffness):
     assert rel_l2(g["contforce"], o["contforce"]) <= 1e-6
 
 
-def test_skin_reuse_gives_the_rows_of_a_full_search():
+def _tight_cells(d):
+    """x extent of the cell grid 1e-5 below 9 cells (DomMin.x / DomMax.x):
+    CellInitiate rounds the count up (quirk Q9), so cells are narrower than
+    the pair radius and a pair within the radius can sit two cells apart."""
+    d.set_f64("DomMin.x", -0.005)
+    d.set_f64("DomMax.x", -0.005 - 0.0003 + 0.0012 * (9 - 1e-5) - 0.0003)
+
+
+@pytest.mark.parametrize("grid", [None, _tight_cells], ids=["cells_cover_radius", "tight_cells"])
+def test_skin_reuse_gives_the_rows_of_a_full_search(grid):
     """The Verlet-skin reuse of the search (default nb_skin 0.1): most
     rebuilds of a yielding cylinder filter the skin lists instead of
     re-sorting, the rows equal the oracle's after every kind of rebuild, and
     the per-particle state is bit-identical to a run with the reuse off (the
-    particles' memory order differs, a row's summation order does not)."""
+    particles' memory order differs, a row's summation order does not).
+    With cells narrower than the pair radius the filter also tests that the
+    two cells are adjacent, as the full search's stencil does."""
     f = FIELDS + ("Strain_pl",)
     runs = {}
     for skin in (0.1, 0.0):
         d = gpu_domain()
         d.set_f64("nb_skin", skin)
+        if grid:
+            grid(d)
         case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
         d.prepare(case.dt)
         rows = []
@@ -288,8 +301,11 @@ def test_skin_reuse_gives_the_rows_of_a_full_search():
         runs[skin]["searches"] = d.geti("nb_searches")
         runs[skin]["full"] = d.geti("nb_full_searches")
         runs[skin]["ie"] = d.get("int_energy_sum")
+        runs[skin]["cells_x"] = d.geti("CellNo.x")
         d.close()
     on, off = runs[0.1], runs[0.0]
+    if grid:
+        assert on["cells_x"] == 9
     assert on["searches"] == off["searches"] > 20
     assert off["full"] == off["searches"] and on["full"] < on["searches"] // 2
     for k in f:
@@ -299,6 +315,8 @@ def test_skin_reuse_gives_the_rows_of_a_full_search():
     assert abs(on["ie"] - off["ie"]) <= 1e-12 * abs(off["ie"])
     o = oracle_domain()
     o.set("cpu_threads", THREADS)
+    if grid:
+        grid(o)
     case = configs.cylinder_upsetting(o, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
     o.prepare(case.dt)
     o.step(120)

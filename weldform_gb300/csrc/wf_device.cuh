@@ -264,6 +264,7 @@ struct DomainConst {
   int skin_on;
   double skin;         // absolute skin length
   float sup_skip_r2;   // squared largest superset radius plus margin, in FP32 (cell pruning)
+  int cells_cover;     // every cell is wider than the largest pair radius (with a 1e-9 margin)
 };
 
 // Device pointers, passed by value to every kernel.

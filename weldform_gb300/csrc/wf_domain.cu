@@ -628,6 +628,11 @@ struct wf_domain {
       for (int d = 0; d < 3; ++d) ext2 = std::max(ext2, CellNo[d] * cs[d]);
       double r2 = (rmax + skin) * (1.0 + 1e-5) + 16.0 * 1.1920929e-7 * ext2;
       K.sup_skip_r2 = (float)(r2 * r2 * (1.0 + 1e-5));
+      // two points within the radius of each other then fall in adjacent cells
+      // (ListGenerate's floor((x - BLPF) / CellSize) differs by at most one)
+      K.cells_cover = 1;
+      for (int d = 0; d < 3; ++d)
+        if (!(cs[d] >= rmax * (1.0 + 1e-9))) K.cells_cover = 0;
     }
     K.ts_nb_inc = ts_nb_inc; K.pl_heating = pl_heating; K.thermal_solver = thermal_solver; K.contact = contact;
     K.contact_mesh_auto_update = contact_mesh_auto_update; K.contact_alg = contact_alg;

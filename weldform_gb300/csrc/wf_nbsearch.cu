@@ -315,6 +315,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   const int* material = P.i + I_MATERIAL * N;
   const int* cls = P.i + I_CLASS * N;
   const int ngroups = (K.N + FILL_ROWS - 1) / FILL_ROWS;
+  unsigned long long pairs = 0;  // this warp's entries (lane 0), one atomic at the end
   for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
   const int i0 = grp * FILL_ROWS;
   // Each warp builds FILL_PER_WARP consecutive rows, one after the other, so
@@ -485,7 +486,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
       P.i[I_NB * N + i] = cnt;
       if (K.contact) P.i[I_NWS * N + i] = (P.i[I_NWS * N + i] & 1) | ((ID[i] == K.id_free_surf) ? 2 : 0);
       if (overflow) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
-      atomicAdd(&P.st->pair_count, (unsigned long long)cnt);
+      pairs += (unsigned long long)cnt;
     }
   } else if (lane == 0) {
     s_len[row] = 0;
@@ -495,12 +496,20 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   // Block-wide coalesced ELL write: thread (k, t) stores entry k of particle i0 + t.
   int maxlen = 0;
   for (int t = 0; t < FILL_ROWS; ++t) maxlen = max(maxlen, s_len[t]);
-  for (int q = threadIdx.x; q < maxlen * FILL_ROWS; q += blockDim.x) {
-    int k = q / FILL_ROWS, t = q - k * FILL_ROWS;
-    if (k < s_len[t]) (SUPER ? P.sup : P.nbr)[(size_t)k * N + i0 + t] = s_idx[t][k];
+  if (SUPER) {  // superset rows are row-major (SUP_W entries per particle): a warp reads 32 in one line
+    for (int q = threadIdx.x; q < FILL_ROWS * SUP_W; q += blockDim.x) {
+      int t = q / SUP_W, k = q - t * SUP_W;
+      if (k < s_len[t]) P.sup[(size_t)(i0 + t) * SUP_W + k] = s_idx[t][k];
+    }
+  } else {
+    for (int q = threadIdx.x; q < maxlen * FILL_ROWS; q += blockDim.x) {
+      int k = q / FILL_ROWS, t = q - k * FILL_ROWS;
+      if (k < s_len[t]) P.nbr[(size_t)k * N + i0 + t] = s_idx[t][k];
+    }
   }
   __syncthreads();  // the shared buffers are reused by the next group
   }
+  if (!SUPER && lane == 0 && pairs) atomicAdd(&P.st->pair_count, pairs);
 }
 
 // ---- Verlet-skin reuse -------------------------------------------------------
@@ -578,37 +587,91 @@ __device__ __forceinline__ bool cells_adjacent(long long a, long long b) {
 // Rows from the superset: the entries whose particles sit in adjacent cells
 // now and pass the radius rule (FP32 prefilter, exact FP64 CheckRadius),
 // in the superset's canonical order — the rows a full search gives.
-__global__ void __launch_bounds__(256) k_nbr_filter(DevPtrs P, DomainConst K) {
+// COVER: every cell is wider than the largest pair radius (DomainConst::
+// cells_cover), so a pair that passes the radius rule is in adjacent cells
+// and the cell test is left out (a non-finite position fails the radius rule).
+// One warp per particle, 32 superset entries per round (one coalesced line of
+// the row-major superset); the kept entries are compacted by ballot in order
+// into shared memory, and the block writes its FILL_ROWS rows to the ELL
+// array one coalesced line per entry index.
+template <bool COVER>
+__global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_filter(DevPtrs P, DomainConst K) {
   if (!searching(P) || !K.skin_on || !P.st->sup_valid) return;
+  __shared__ int s_idx[FILL_ROWS][MAX_NB];
+  __shared__ int s_len[FILL_ROWS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const size_t N = K.N;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K.N) return;
-  int cnt = 0, split = 0;
-  const long long ci = P.cellc[i];
-  if (P.i[I_KIND * N + i] == 0 && ci >= 0) {
-    const float4 pi = reinterpret_cast<const float4*>(P.xs)[i];
-    const int len = P.sup_len[i];
-    for (int k = 0; k < len; ++k) {
-      const int e = P.sup[(size_t)k * N + i];
-      const int j = nb_index(e);
-      const long long cj = P.cellc[j];
-      if (cj < 0 || !cells_adjacent(ci, cj)) continue;
-      if (!radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, reinterpret_cast<const float4*>(P.xs)[j])) continue;
-      if (cnt < MAX_NB) {
-        P.nbr[(size_t)cnt * N + i] = e;
-        split += nb_up(e) ? 1 : 0;
+  const float4* xs = reinterpret_cast<const float4*>(P.xs);
+  const int ngroups = (K.N + FILL_ROWS - 1) / FILL_ROWS;
+  unsigned long long pairs = 0;  // this warp's entries (lane 0), one atomic at the end
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int i0 = grp * FILL_ROWS;
+    for (int rr = 0; rr < FILL_PER_WARP; ++rr) {
+      const int row = w * FILL_PER_WARP + rr;
+      const int i = i0 + row;
+      int cnt = 0;
+      const long long ci = i < K.N ? P.cellc[i] : -1;
+      if (i < K.N && P.i[I_KIND * N + i] == 0 && ci >= 0) {
+        const float4 pi = xs[i];
+        const int len = P.sup_len[i];
+        const int* sr = P.sup + (size_t)i * SUP_W;
+        // All of the row's loads are issued before any is used: the lane's up
+        // to four entries (k = lane + 32 r), then their positions, so a row
+        // costs two memory latencies rather than two per 32 entries.
+        constexpr int R = SUP_W / 32;
+        int e[R];
+        float4 pj[R];
+        long long cj[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) e[r] = lane + 32 * r < len ? sr[lane + 32 * r] : 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (lane + 32 * r < len) {
+            pj[r] = xs[nb_index(e[r])];
+            if (!COVER) cj[r] = P.cellc[nb_index(e[r])];
+          }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (32 * r >= len) break;  // warp-uniform
+          bool ok = false;
+          if (lane + 32 * r < len) {
+            ok = COVER || (cj[r] >= 0 && cells_adjacent(ci, cj[r]));
+            if (ok) ok = radius_ok(P, K, N, i, nb_index(e[r]), pi.x, pi.y, pi.z, pi.w, pj[r]);
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, ok);
+          if (ok) {
+            const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+            if (pos < MAX_NB) s_idx[row][pos] = e[r];
+          }
+          cnt += __popc(m);
+        }
       }
-      ++cnt;
+      if (cnt > MAX_NB && lane == 0) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
+      if (cnt > MAX_NB) cnt = MAX_NB;
+      __syncwarp();
+      int split = 0;
+      for (int e = lane; e < cnt; e += 32) split += s_idx[row][e] < 0 ? 1 : 0;
+      for (int off = 16; off > 0; off >>= 1) split += __shfl_down_sync(0xffffffffu, split, off);
+      if (lane == 0) {
+        s_len[row] = i < K.N ? cnt : 0;
+        if (i < K.N) {
+          P.row_len[i] = cnt;
+          P.row_split[i] = split;
+          P.i[I_NB * N + i] = cnt;
+          pairs += (unsigned long long)cnt;
+        }
+      }
     }
+    __syncthreads();
+    int maxlen = 0;
+    for (int t = 0; t < FILL_ROWS; ++t) maxlen = max(maxlen, s_len[t]);
+    for (int q = threadIdx.x; q < maxlen * FILL_ROWS; q += blockDim.x) {
+      int k = q / FILL_ROWS, t = q - k * FILL_ROWS;
+      if (k < s_len[t]) P.nbr[(size_t)k * N + i0 + t] = s_idx[t][k];
+    }
+    __syncthreads();  // the shared rows are reused by the next group
   }
-  if (cnt > MAX_NB) {
-    atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
-    cnt = MAX_NB;
-  }
-  P.row_len[i] = cnt;
-  P.row_split[i] = split;
-  P.i[I_NB * N + i] = cnt;
-  if (cnt) atomicAdd(&P.st->pair_count, (unsigned long long)cnt);
+  if (lane == 0 && pairs) atomicAdd(&P.st->pair_count, pairs);
 }
 
 // CalculateSurface (Domain.cpp:1415-1491): n_i = sum_j m_j (x_i - x_j) in row
@@ -616,6 +679,7 @@ __global__ void __launch_bounds__(256) k_nbr_filter(DevPtrs P, DomainConst K) {
 __global__ void k_surface(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
   size_t N = K.N;
+  unsigned nsurf = 0;  // summed over the warp, one atomic per warp
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
   if (P.i[I_KIND * N + i] != 0) continue;
   double xi = P.f[C_X * N + i], yi = P.f[(C_X + 1) * N + i], zi = P.f[(C_X + 2) * N + i];
@@ -636,10 +700,12 @@ __global__ void k_surface(DevPtrs P, DomainConst K) {
   bool surf = (nn >= __dmul_rn(0.25, P.f[C_H * N + i])) && (len <= 46);
   if (surf) {
     if (!(P.i[I_NWS * N + i] & 1)) id = 1;
-    atomicAdd(&P.st->surface_count, 1);
+    ++nsurf;
   }
   P.i[I_ID * N + i] = id;
   }
+  nsurf = __reduce_add_sync(0xffffffffu, nsurf);
+  if ((threadIdx.x & 31) == 0 && nsurf) atomicAdd(&P.st->surface_count, (int)nsurf);
 }
 
 // ContactNbSearch (Contact.cpp:57-132): surface particle (at search time and
@@ -648,6 +714,7 @@ __global__ void k_surface(DevPtrs P, DomainConst K) {
 __global__ void k_contact_pairs(DevPtrs P, DomainConst K) {
   if (!searching(P)) return;
   size_t N = K.N;
+  unsigned npairs = 0;  // summed over the warp, one atomic per warp
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
   int cnt = 0;
   bool overflow = false;
@@ -692,8 +759,10 @@ __global__ void k_contact_pairs(DevPtrs P, DomainConst K) {
   for (int k = 0; k < cnt; ++k) P.cp[(size_t)k * N + i] = row[k];
   P.cp_len[i] = cnt;
   if (overflow) atomicOr(&P.st->errors, ERR_CONTACT_OVERFLOW);
-  if (cnt) atomicAdd(&P.st->contact_pair_count, (unsigned long long)cnt);
+  npairs += (unsigned)cnt;
   }
+  npairs = __reduce_add_sync(0xffffffffu, npairs);
+  if ((threadIdx.x & 31) == 0 && npairs) atomicAdd(&P.st->contact_pair_count, (unsigned long long)npairs);
 }
 
 __global__ void k_force_search(DevPtrs P) { P.st->do_search = 1; }
@@ -770,7 +839,9 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   if (K.skin_on) {
     k_cell_coords<<<grid(K.N), T, 0, s>>>(P, K);
     mark(s, "k_cell_coords");
-    k_nbr_filter<<<nblk(K.N, 256), 256, 0, s>>>(P, K);
+    int groups = nblk(K.N, FILL_ROWS), cap = 152 * 4;
+    if (K.cells_cover) k_nbr_filter<true><<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
+    else k_nbr_filter<false><<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);
     mark(s, "k_nbr_filter");
   }
   if (P.halo) launch_halo_build(P, K, s);
