@@ -83,7 +83,8 @@ int wf_domain_destroy(wf_domain* d);
  * contact and without batched specimens).  Integer fields: "Nproc", "ts_nb_inc",
  * "nonlock_sum", "pl_heating", "thermal_solver", "contact",
  * "contact_mesh_auto_update", "GradientType", "contact_alg" (WF_CONTACT_*),
- * "integrator" (0 kick-drift, 1 leapfrog; before the prologue),
+ * "integrator" (0 kick-drift, 1 leapfrog; before the prologue; 2, the
+ *   Fraser order of SolveDiffUpdateFraser, is WF_ERR_UNSUPPORTED),
  * "gradKernelCorr" (kernel-gradient correction, Domain.cpp:1832-1940; plain
  * FP64 form; the correction matrix is recomputed at the first step and, for
  * the leapfrog solver, after every rebuild),

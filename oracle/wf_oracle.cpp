@@ -1484,8 +1484,35 @@ struct Domain {
     if (auto_ts_acc) check_min_ts_accel();
     if (auto_ts || auto_ts_acc) adaptive_time_step();
   }
+  // SolverFraser.cpp:212-330 (SolveDiffUpdateFraser): density and rates from
+  // x(n), v(n), the stress update, then the acceleration from the new stress,
+  // contact, x += v dt + a dt^2 / 2 and v += a dt.  The checker of the
+  // reference's own run log of this solver (examples/input/
+  // Contact_Compression.out); the library does not run this integrator.
+  void fraser_body() {
+    pass_density();
+    for (int i = 0; i < N; i++) rho[i] += deltat * dDensity[i];
+    pass_rates();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int i = 0; i < solid_part_count; i++) if (!is_mesh(i)) stress_strain(i, deltat);
+    pass_accel();
+    if (contact) contact_wang();
+    general_after();
+    for (int i = 0; i < N; i++) {
+      x_prev[i] = x[i];
+      V3 du;
+      for (int k = 0; k < 3; ++k) du.c[k] = v[i].c[k] * deltat + 0.5 * a[i].c[k] * deltat * deltat;
+      disp[i] = add(disp[i], du);
+      x[i] = add(x[i], du);
+    }
+    for (int i = 0; i < N; i++) v[i] = add(v[i], scl(deltat, a[i]));
+    general_after();
+  }
   // The rest of the step (force passes, kicks, drift, stress, thermal, bookkeeping).
   void finish_step() {
+    if (integrator == 2) {
+      fraser_body();
+    } else {
     pass_accel();
     general_after();
     if (contact) contact_wang();
@@ -1528,6 +1555,7 @@ struct Domain {
     }
 #pragma omp parallel for schedule(static) num_threads(nthreads)
     for (int i = 0; i < solid_part_count; i++) if (!is_mesh(i)) stress_strain(i, deltat);
+    }  // kick-drift and leapfrog bodies
     plastic_work_heat(deltat);
     thermal_calcs(deltat);
     energies();

@@ -118,8 +118,34 @@ def test_contact_thermal_input_runs_in_the_oracle(tmp_path):
     assert rows[:, 16].max() >= 300.0
 
 
+def test_convection_boundary_condition():
+    """A type-3 BC (WeldForm.cpp:793-807) marks its zone for CalcConvHeat with
+    its convCoeff and infTemp; GeneralAfter leaves it alone.  The zone heats
+    toward T_inf faster than the same run without it."""
+    j = copy.deepcopy(CONTACT)
+    j["BoundaryConditions"].append({"zoneId": 2, "type": 3, "convCoeff": 5e7, "infTemp": 900.0})
+    runs = {}
+    for name, deck in (("conv", j), ("plain", CONTACT)):
+        run = wj.build(deck, make=_oracle)
+        d = run.dom
+        d.prepare(run.dt)
+        d.step(10)
+        runs[name] = (d.get_array("T"), d.get_array("Thermal_BC"), d.get_array("h_conv"), d.get_array("T_inf"),
+                      d.get_array("ID"))
+    T, tbc, hc, tinf, ids = runs["conv"]
+    zone = ids == 2
+    assert zone.sum() > 0
+    assert (tbc[zone] == 1).all() and (tbc[~zone] == 0).all()
+    assert np.allclose(hc[zone], 5e7) and np.allclose(tinf[zone], 900.0)
+    assert (T[zone] > runs["plain"][0][zone] + 1e-3).all()
+    with pytest.raises(WFError) as e:
+        bad = copy.deepcopy(CONTACT)
+        bad["BoundaryConditions"].append({"zoneId": 2, "type": 3, "convCoeff": 5e7})
+        wj.build(bad, make=_oracle)
+    assert e.value.code == 8
+
+
 @pytest.mark.parametrize("patch", [
-    ("Configuration", "solver", "Mech-Fraser"),
     ("Materials", "type", "GMT"),
     ("Materials", "damageModel", "Rankine"),
     ("DomainBlocks", "gridCoordSys", "AxiSymmetric"),
@@ -131,6 +157,18 @@ def test_unsupported_inputs_are_rejected(patch):
     tgt[key] = val
     with pytest.raises(WFError) as e:
         wj.build(j, make=_oracle)
+    assert e.value.code == 8
+
+
+@pytest.mark.gpu
+def test_fraser_solver_is_rejected_by_the_library():
+    """"Mech-Fraser" (SolveDiffUpdateFraser) runs in the oracle, which checks
+    itself against the reference's run log of that solver; the library builds
+    the kick-drift and leapfrog orders only and says so."""
+    j = copy.deepcopy(COMPRESSION)
+    j["Configuration"]["solver"] = "Mech-Fraser"
+    with pytest.raises(WFError) as e:
+        wj.build(j)
     assert e.value.code == 8
 
 

@@ -1404,6 +1404,7 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
   else if (n == "contact_mesh_auto_update") d->contact_mesh_auto_update = v;
   else if (n == "contact_alg") { if (v < 0 || v > 2) return set_err(WF_ERR_ARG, "contact_alg"); d->contact_alg = v; }
   else if (n == "integrator") {  // 0 SolveDiffUpdateKickDrift, 1 SolveDiffUpdateLeapFrog
+    if (v == 2) return set_err(WF_ERR_UNSUPPORTED, "integrator 2 (SolveDiffUpdateFraser) is not built");
     if (v != 0 && v != 1) return set_err(WF_ERR_ARG, "integrator must be 0 (kick-drift) or 1 (leapfrog)");
     d->integrator = v;
   }

@@ -27,9 +27,12 @@ Supported input (everything the kick-drift / leapfrog path covers):
   amplitude, valueAng for rigid bodies), InitialConditions (velocity,
   temperature), RigidBodies of type Plane with Contact[0] (friction
   coefficients, penaltyFactor).
-Anything else (Fraser or Thermal solvers, GMT, damage, file or axisymmetric
-domains and meshes, 2D, heat-conduction contact, convection / temperature
-BCs) raises WFError(WF_ERR_UNSUPPORTED) before any step runs.
+  BoundaryConditions of type 3 (convection: convCoeff, infTemp on the zone).
+"Mech-Fraser" / "Mech-Thermal-Fraser" (SolveDiffUpdateFraser) build for the
+oracle only; the library rejects that integrator.
+Anything else (Thermal-only solvers, GMT, damage, file or axisymmetric
+domains and meshes, 2D, heat-conduction contact, temperature / force BCs)
+raises WFError(WF_ERR_UNSUPPORTED) before any step runs.
 kernelGradCorr is supported in both forms; smoothlenUpdate is accepted (it
 cannot change h in these solvers).
 """
@@ -58,7 +61,7 @@ def _unsupported(msg):
 @dataclass
 class Run:
     dom: object
-    integrator: int      # 0 kick-drift, 1 leapfrog
+    integrator: int      # 0 kick-drift, 1 leapfrog, 2 Fraser (oracle only)
     dt: float
     sim_time: float
     out_time: float
@@ -106,10 +109,14 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
     solver = config.get("solver", "Mech")
     leapfrog = ("Mech", "Mech-Thermal", "Mech-LeapFrog", "Mech-Thermal-LeapFrog")
     kickdrift = ("Mech-KickDrift", "Mech-Thermal-KickDrift")
-    if solver not in leapfrog + kickdrift:
+    # The Fraser solver (SolverFraser.cpp) runs in the oracle only, which
+    # checks itself against the reference's run log of it; the library
+    # rejects integrator 2.
+    fraser = ("Mech-Fraser", "Mech-Thermal-Fraser")
+    if solver not in leapfrog + kickdrift + fraser:
         _unsupported(f"solver {solver!r}")
-    thermal = solver in ("Mech-Thermal", "Mech-Thermal-LeapFrog", "Mech-Thermal-KickDrift")
-    integrator = 1 if solver in leapfrog else 0
+    thermal = solver in ("Mech-Thermal", "Mech-Thermal-LeapFrog", "Mech-Thermal-KickDrift", "Mech-Thermal-Fraser")
+    integrator = 1 if solver in leapfrog else (2 if solver in fraser else 0)
     dom.set("integrator", integrator)
     if thermal:
         dom.set("thermal_solver", 1)
@@ -218,8 +225,15 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
     for ampl in amplitudes:
         dom.add_amplitude(int(ampl["id"]), [float(x) for x in ampl["time"]], [float(x) for x in ampl["value"]])
     for bc in bcs:
-        if int(bc.get("type", 0)) != 0:
-            _unsupported("temperature / convection boundary conditions")
+        btype = int(bc.get("type", 0))  # BC_TYPE, Domain.h:94
+        if btype == 3:  # Convection_BC (WeldForm.cpp:793-807): fields only, GeneralAfter skips it
+            zone = int(bc["zoneId"])
+            dom.set_particles("Thermal_BC", 1, zone)
+            dom.set_particles("T_inf", float(bc["infTemp"]), zone)
+            dom.set_particles("h_conv", float(bc["convCoeff"]), zone)
+            continue
+        if btype != 0:
+            _unsupported("temperature / force / symmetry boundary conditions")
         vt = int(bc.get("valueType", 0))
         value = _vec(bc.get("value", [0, 0, 0]))
         ang = _vec(bc.get("valueAng", [0, 0, 0]))
