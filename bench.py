@@ -572,8 +572,11 @@ def sweep_mode(a):
     block = d.autotune(3) if a.autotune else d.geti("gather_block")
     lanes = d.geti("gather_lanes")
     d.step(2)
+    s0, f0 = d.geti("nb_searches"), d.geti("nb_full_searches")
     ms, launches = d.step_timed(a.steps)
     together = sw.n * a.steps / (ms * 1e-3)
+    dom_searches, dom_full = d.geti("nb_searches") - s0, d.geti("nb_full_searches") - f0
+    layout = {"uniform_layout": d.geti("uniform_layout"), "skin_reuse": d.geti("skin_reuse")}
     a0, b0 = sw.ranges[0]
     u_together = d.get_array("Displacement")[a0:b0]
     searches = [d.batch_get(k, "nb_searches") for k in range(len(specs))]
@@ -599,6 +602,7 @@ def sweep_mode(a):
         "specimens": len(specs), "particles": sw.n, "steps": a.steps, "precision": a.precision,
         "gather_block": block, "gather_lanes": lanes, "setup_s": setup,
         "batched_particle_steps_per_s": together, "batched_ms_per_step": ms / a.steps, "launches": launches,
+        "batched_steps_with_a_search": dom_searches, "batched_full_searches": dom_full, **layout,
         "sequential_specimens_timed": len(specs), "sequential_particle_steps_per_s": alone,
         "sequential_wall_s": time.perf_counter() - t1,
         "batched_over_sequential": together / alone,
@@ -738,7 +742,7 @@ def main():
                            ("mixed_yielding", wfmod.PRECISION_MIXED, V_TOP_YIELD)):
         d, case, _, _, nnz = time_form(wfmod, prec, 1, warmup, gpu, v_top=vt)
         steps = a.steps
-        s0 = d.geti("nb_searches")
+        s0, f0 = d.geti("nb_searches"), d.geti("nb_full_searches")
         barrier(pg)
         if have_torch_cuda:
             torch.cuda.synchronize()
@@ -750,10 +754,11 @@ def main():
         ms_max = reduce_max(pg, ms)
         val = world * case.n * steps / (ms_max * 1e-3)
         searches = d.geti("nb_searches") - s0
+        full = d.geti("nb_full_searches") - f0
         rl = roofline(d, case, nnz, steps, peak, peak_kind)
         forms[name] = {"value": val, "ms_per_step": ms_max / steps, "steps": steps, "roofline": rl,
                        "gpu_launches": launches, "clocks": clk.summary(), "v_top": vt,
-                       "rebuilds_in_timed_steps": searches}
+                       "rebuilds_in_timed_steps": searches, "full_searches_in_timed_steps": full}
         if name == "mixed":
             head = (case, nnz)
             xm, sm = d.get_array("Displacement"), d.get_array("Sigma")

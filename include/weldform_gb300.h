@@ -128,7 +128,11 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int value);
  * the prologue that took the dynamic-friction branch, Contact_Wang.cpp:284-290;
  * no reference counterpart), "nan_particles" (particles whose position was not
  * finite at the last neighbour search: they get empty rows and appear in no
- * row, as CheckRadius decides for them, without being binned into a cell). */
+ * row, as CheckRadius decides for them, without being binned into a cell),
+ * "uniform_layout" (1 when the mixed records take the four-group
+ * uniform-particle layout: h and Cs uniform, and every pair's masses equal —
+ * uniform, or uniform within each batched specimen), "skin_reuse" (1 when the
+ * Verlet-skin reuse of the search is on). */
 int wf_get_domain_f64(wf_domain* d, const char* name, double* value);
 int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* value);
 
@@ -251,10 +255,14 @@ int wf_get_contact_pairs(wf_domain* d, int64_t* offsets, int32_t* idx, int64_t c
  * (SolverKickDrift.cpp:153-186, 315-324: the first step, the first step with a
  * particle past MIN_PS_FOR_NBSEARCH, then every ts_nb_inc steps while
  * yielding).  A search serves the specimens that ask for one; the others keep
- * their rows.  Specimens are meant to be spatially apart (no pair between two
- * of them).  Every particle must belong to exactly one specimen; before the
- * prologue; contact and gradKernelCorr are WF_ERR_UNSUPPORTED, and so is the
- * adjoint on such a domain. */
+ * their rows (with the Verlet-skin reuse, most searches filter the skin lists
+ * of the asking specimens instead of re-sorting the domain).  Specimens must
+ * be spatially apart: a neighbour pair that joins two of them fails the step
+ * with WF_ERR_ARG.  Each specimen may have its own mass; with equal masses
+ * within each one the mixed records keep the uniform-particle layout.  Every
+ * particle must belong to exactly one specimen; before the prologue; contact
+ * and gradKernelCorr are WF_ERR_UNSUPPORTED, and so is the adjoint on such a
+ * domain. */
 int wf_batch_specimens(wf_domain* d, const int64_t* first, const int64_t* count, int nspec);
 /* Per-specimen read-back: "nb_searches" (searches the specimen asked for),
  * "yielding" (1 once it has yielded), "first", "particle_count". */

@@ -106,3 +106,53 @@ def test_each_specimen_keeps_its_own_schedule_on_the_gpu(precision):
     assert searches == solo == osearches
     _check(tog, alo, 1e-9 if precision == 0 else 1e-6)
     _check(tog, otog, 1e-9 if precision == 0 else 1e-4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_batched_skin_reuse_rows_equal_the_oracle(precision):
+    """A batched domain reuses the Verlet-skin lists: most searches filter the
+    lists of the specimens that ask (no re-sort) while the others keep their
+    rows.  The specimens' masses differ, and the mixed records still take the
+    four-group uniform layout (equal masses within each specimen).  After 60
+    steps the rows equal the oracle's batch exactly."""
+    d = gpu_domain()
+    d.set("precision", precision)
+    sw = batch.build_sweep(d, UNEVEN, dx=DX)
+    d.prepare(sw.dt)
+    d.step(60)
+    assert d.geti("skin_reuse") == 1
+    assert d.geti("uniform_layout") == 1
+    m = d.get_array("Mass")
+    assert len({float(m[a]) for a, _ in sw.ranges}) == len(UNEVEN)
+    full, total = d.geti("nb_full_searches"), d.geti("nb_searches")
+    assert 1 <= full < total, (full, total)
+    off, idx = d.neighbours()
+    searches = [d.batch_get(k, "nb_searches") for k in range(len(UNEVEN))]
+    o = oracle_domain()
+    osw = batch.build_sweep(o, UNEVEN, dx=DX)
+    o.prepare(osw.dt)
+    o.step(60)
+    ooff, oidx = o.neighbours()
+    assert searches == [o.batch_get(k, "nb_searches") for k in range(len(UNEVEN))]
+    assert np.array_equal(off, ooff) and np.array_equal(idx, oidx)
+
+
+@pytest.mark.gpu
+def test_specimens_that_touch_are_rejected():
+    """Two specimens side by side, their outer particles about 1.5 dx apart, share
+    neighbour pairs: the first search fails the step with WF_ERR_ARG instead
+    of coupling them silently."""
+    from weldform_gb300 import WFError
+    d = gpu_domain()
+    sw = batch.build_sweep(d, [batch.Specimen(R=0.003, L=0.006, v_punch=-1.0, jc=_JC)] * 2, dx=DX)
+    (a0, b0), (a1, b1) = sw.ranges
+    x = d.get_array("x")
+    width = x[a0:b0, 0].max() - x[a0:b0, 0].min()
+    x[a1:b1] = x[a0:b0] + np.array([width + 1.5 * DX, 0.0, 0.0])  # outer particles ~1.5 dx apart
+    d.set_array("x", x)
+    d.prepare(sw.dt)
+    with pytest.raises(WFError) as e:
+        d.step(1)
+    assert e.value.code == 1  # WF_ERR_ARG
+    d.close()

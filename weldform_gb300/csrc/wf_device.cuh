@@ -159,6 +159,7 @@ constexpr int ERR_NBR_OVERFLOW = 1;
 constexpr int ERR_NAN = 2;
 constexpr int ERR_TIMEOUT = 4;
 constexpr int ERR_CONTACT_OVERFLOW = 8;
+constexpr int ERR_SPEC_LINK = 16;  // a neighbour pair joins two batched specimens
 constexpr int ERR_NO_SURFACE = 16;
 
 // Reduction slots (per-block partials, deterministic tree order).
@@ -241,14 +242,17 @@ struct DomainConst {
   double CFL, sqrt_h_a;      // their coefficients (Domain::CFL, Domain::sqrt_h_a)
   int av_uniform;      // 1 when every solid particle has the same Alpha and Beta
   float av_alpha, av_beta;  // those values (the mixed acceleration gather skips their loads)
-  int m_uniform;       // 1 when every solid particle has the same mass
-  float mass_f;        // that mass (the mixed rate gather's kinetic-energy term)
+  // 1 when the two particles of every pair have the same mass: the mass is
+  // uniform, or uniform within each batched specimen (no pair links two
+  // specimens, ERR_SPEC_LINK).  The gathers then take m_j = m_i.
+  int m_pair;
   // Uniform-particle layout of the mixed records: every solid particle has the
-  // same h, mass and Cs (and the staged gather is off).  The current records
-  // then carry Sigma/rho^2 xz in RC_XH.w and yz in RC_VH.w (instead of h and
-  // rho), so the acceleration gather reads four groups per neighbour instead
-  // of five, rho_j = mass / (m/rho)_j, and every gather uses the kernel
-  // constants of the one h below instead of forming 1/h per pair.
+  // same h and Cs, the pairs' masses agree (m_pair), and the staged gather is
+  // off.  The current records then carry Sigma/rho^2 xz in RC_XH.w and yz in
+  // RC_VH.w (instead of h and rho), so the acceleration gather reads four
+  // groups per neighbour instead of five, rho_j = m_i / (m/rho)_j, and every
+  // gather uses the kernel constants of the one h below instead of forming
+  // 1/h per pair.
   int uni;
   float h_f, cs_f;     // that h and Cs
   float inv_h_f;       // 1 / h

@@ -615,14 +615,14 @@ struct wf_domain {
     if (K.nspec > 0 && (contact || grad_corr))
       throw CudaError{WF_ERR_UNSUPPORTED, "batched specimens: contact and gradKernelCorr are not supported"};
     // Verlet-skin reuse of the search: on without contact (the contact search
-    // bins rigid-mesh particles that move with their planes) and without
-    // batched specimens; the superset radius must stay within two cells and
-    // each cell coordinate within 21 bits.
+    // bins rigid-mesh particles that move with their planes); the superset
+    // radius must stay within two cells and each cell coordinate within 21
+    // bits.
     {
       double rmax = Cellfac * hmax, skin = nb_skin * rmax;
       bool fits = true;
       for (int d = 0; d < 3; ++d) fits = fits && CellNo[d] < (1 << 21) && rmax + skin <= 2.0 * cs[d];
-      K.skin_on = (nb_skin > 0 && !contact && K.nspec == 0 && fits) ? 1 : 0;
+      K.skin_on = (nb_skin > 0 && !contact && fits) ? 1 : 0;
       K.skin = K.skin_on ? skin : 0.0;
       double ext2 = 0.0;
       for (int d = 0; d < 3; ++d) ext2 = std::max(ext2, CellNo[d] * cs[d]);
@@ -644,7 +644,7 @@ struct wf_domain {
     K.id_free_surf = -999999;
     K.leapfrog = integrator;
     set_uniform(hp.f[C_ALPHA].data(), hp.f[C_BETA].data(), hp.f[C_MASS].data(), hp.f[C_H].data(),
-                hp.f[C_CS].data(), hp.i[I_KIND].data(), N);
+                hp.f[C_CS].data(), hp.i[I_KIND].data(), hp.i[I_SPEC].data(), N);
     K.gradcorr = grad_corr;
     if (auto_ts_cont && contact && integrator == 0)
       throw CudaError{WF_ERR_UNSUPPORTED, "auto_ts_cont with contact: the kick-drift solver reads Domain::min_force_ts, "
@@ -724,6 +724,8 @@ struct wf_domain {
     wf::StepState st = read_state();
     if (st.errors & wf::ERR_NBR_OVERFLOW) throw CudaError{WF_ERR_NBR_OVERFLOW, "a particle has more than 100 neighbours (MAX_NB_PER_PART)"};
     if (st.errors & wf::ERR_CONTACT_OVERFLOW) throw CudaError{WF_ERR_NBR_OVERFLOW, "a particle has more than 64 contact pairs"};
+    if (st.errors & wf::ERR_SPEC_LINK)
+      throw CudaError{WF_ERR_ARG, "batch: a neighbour pair links two specimens (they must be spatially apart)"};
     if (st.errors & wf::ERR_TIMEOUT) throw CudaError{WF_ERR_TIMEOUT, "a bounded device wait gave up"};
     if (st.errors & wf::ERR_NAN)
       throw CudaError{WF_ERR_NAN, "non-finite state: a particle position at a neighbour search, or the energy sums"};
@@ -862,32 +864,37 @@ struct wf_domain {
   }
   // The plain form's per-entry GradKernel (P.gk) no longer matches the state.
   void invalidate_gk() { CK(cudaMemsetAsync(&P.st->gk_valid, 0, sizeof(int), stream)); }
-  // Whether Alpha and Beta, and the mass, are the same on every SPH particle:
-  // the gathers then take the pair's (a_i + a_j) / 2 = a, and m_j, from K
-  // instead of loading them.
   // Flags of the solid particles' uniform fields, which select the mixed
-  // gathers' specialisations and record layout (DomainConst::av_uniform,
-  // m_uniform, uni).
+  // gathers' specialisations and record layout: Alpha and Beta the same on
+  // every SPH particle (av_uniform: the pair's (a_i + a_j) / 2 = a from K),
+  // the masses of every pair equal (m_pair), and the uniform-particle layout
+  // (uni).  spec: each particle's batched specimen (all 0 when the domain is
+  // not batched); specimens share no pair, so equal masses within each one
+  // make every pair's masses equal.
   void set_uniform(const double* a, const double* b, const double* m, const double* h, const double* cs,
-                   const int* kind, size_t n) {
+                   const int* kind, const int* spec, size_t n) {
     K.av_uniform = 1;
-    K.m_uniform = 1;
+    K.m_pair = 1;
     bool h_uniform = true, cs_uniform = true;
     bool first = true;
-    double a0 = 0, b0 = 0, m0 = 0, h0 = 0, c0 = 0;
+    double a0 = 0, b0 = 0, h0 = 0, c0 = 0;
+    const size_t nsp = spec_first.empty() ? 1 : spec_first.size();
+    std::vector<double> spec_m(nsp, 0.0);  // first mass seen in each specimen
+    std::vector<char> seen(nsp, 0);
     for (size_t p = 0; p < n; ++p) {
       if (kind[p] != 0) continue;
-      if (first) { a0 = a[p]; b0 = b[p]; m0 = m[p]; h0 = h[p]; c0 = cs[p]; first = false; continue; }
+      const int q = spec[p];
+      if (!seen[q]) { seen[q] = 1; spec_m[q] = m[p]; }
+      else if (m[p] != spec_m[q]) K.m_pair = 0;
+      if (first) { a0 = a[p]; b0 = b[p]; h0 = h[p]; c0 = cs[p]; first = false; continue; }
       if (a[p] != a0 || b[p] != b0) K.av_uniform = 0;
-      if (m[p] != m0) K.m_uniform = 0;
       if (h[p] != h0) h_uniform = false;
       if (cs[p] != c0) cs_uniform = false;
     }
     K.av_alpha = (float)a0;
     K.av_beta = (float)b0;
-    K.mass_f = (float)m0;
     // the staged gather copies the five-group layout
-    K.uni = (K.m_uniform && h_uniform && cs_uniform && !stage && h0 > 0) ? 1 : 0;
+    K.uni = (K.m_pair && h_uniform && cs_uniform && !stage && h0 > 0) ? 1 : 0;
     K.h_f = (float)h0;
     K.cs_f = (float)c0;
     // the FP32 operations of the per-pair kernel factor at hh = h
@@ -901,15 +908,16 @@ struct wf_domain {
   void refresh_uniform() {
     size_t n = hp.N;
     std::vector<double> a(n), b(n), m(n), h(n), cs(n);
-    std::vector<int> kind(n);
+    std::vector<int> kind(n), spec(n);
     CK(cudaMemcpyAsync(a.data(), d_f + (size_t)wf::C_ALPHA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(b.data(), d_f + (size_t)wf::C_BETA * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(m.data(), d_f + (size_t)wf::C_MASS * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(h.data(), d_f + (size_t)wf::C_H * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(cs.data(), d_f + (size_t)wf::C_CS * n, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(kind.data(), d_i + (size_t)wf::I_KIND * n, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(spec.data(), d_i + (size_t)wf::I_SPEC * n, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    set_uniform(a.data(), b.data(), m.data(), h.data(), cs.data(), kind.data(), n);
+    set_uniform(a.data(), b.data(), m.data(), h.data(), cs.data(), kind.data(), spec.data(), n);
     shadows_valid = false;
     if (graph) { CK(cudaGraphExecDestroy(graph)); graph = nullptr; }
   }
@@ -1464,6 +1472,8 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     if (n == "stage_cap") { *v = d->stage_cap; return WF_OK; }
     if (n.size() == 8 && n.rfind("CellNo.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') { *v = d->CellNo[n[7] - 'x']; return WF_OK; }
     if (!d->prepared) { *v = 0; return WF_OK; }
+    if (n == "uniform_layout") { *v = d->K.uni; return WF_OK; }
+    if (n == "skin_reuse") { *v = d->K.skin_on; return WF_OK; }
     wf::StepState st = d->read_state();
     if (n == "steps") *v = st.steps;
     else if (n == "pair_count") *v = st.pair_count / 2;

@@ -73,12 +73,13 @@ __global__ void k_cell_keys(DevPtrs P, DomainConst K) {
   }
 }
 
-// Batched domain, before the reordering: the rows of particles whose specimen
-// does not search this step are saved by old position, each entry as the
-// neighbour's original index (with the larger-index bit), so k_nbr_fill can
-// put them back at the particles' new positions.
+// Batched domain, before the reordering (a full search): the rows of
+// particles whose specimen does not search this step are saved by old
+// position, each entry as the neighbour's original index (with the
+// larger-index bit), so k_nbr_fill can put them back at the particles' new
+// positions.
 __global__ void k_rows_save(DevPtrs P, DomainConst K) {
-  if (!searching(P)) return;
+  if (!searching_full(P)) return;
   const size_t N = K.N;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
     if (P.sp[P.i[I_SPEC * N + p]].do_search) continue;
@@ -302,8 +303,11 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   if (SUPER) {
     if (!searching_full(P) || !K.skin_on) return;
   } else {
-    if (!searching_full(P) || (K.skin_on && P.st->sup_valid)) return;
+    if (!searching_full(P) || (K.skin_on && P.st->sup_valid && K.nspec == 0)) return;
   }
+  // With the superset valid the filter forms the rows of the specimens that
+  // search; this pass then only puts back the rows of those that do not.
+  const bool keep_only = !SUPER && K.skin_on && P.st->sup_valid;
   __shared__ __align__(16) unsigned s_key[FILL_ROWS][FILL_SLOTS];
   __shared__ int s_idx[FILL_ROWS][FILL_SLOTS];
   __shared__ int s_len[FILL_ROWS];
@@ -326,12 +330,16 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
   unsigned* rkey = &s_key[row][0];
   int* ridx = &s_idx[row][0];
   int cnt = 0, split = 0;
-  bool overflow = false;
+  bool overflow = false, link = false;
   // A particle in a shadow bucket (non-finite position) has an empty row.
   const int key_i = i < K.N ? P.i[I_CELL * N + P.perm[i]] : 0;
   // Batched domain: a specimen that does not search keeps its rows (saved by
   // k_rows_save in canonical order; their keys here keep that order).
   const bool keep = !SUPER && K.nspec > 0 && i < K.N && !P.sp[P.i[I_SPEC * N + i]].do_search;
+  if (keep_only && !keep) {
+    if (lane == 0) s_len[row] = 0;
+    continue;
+  }
   if (keep) {
     const int old = P.perm[i];
     cnt = P.save_len[old];
@@ -350,6 +358,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     int c[3] = {lin / (K.CellNo[1] * K.CellNo[2]), (lin / K.CellNo[2]) % K.CellNo[1], lin % K.CellNo[2]};
     int idi = ID[i], oi = orig[i], mi = material[i];
     bool ci = K.contact && is_contact_id(K, idi);
+    const int spec_i = !SUPER && K.nspec > 0 ? P.i[I_SPEC * N + i] : 0;
     // Lane c < 27 fetches the range of neighbour cell c; a warp scan of the
     // counts flattens the candidates so all lanes work on every iteration.
     // A cell whose box lies farther from x_i than the largest pair radius
@@ -424,6 +433,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
               ok = dx * dx + dy * dy + dz * dz <= Rs * Rs * (1.0f + 4.0f * K.pre_eps);
             } else {
               ok = radius_ok(P, K, N, i, j, pi.x, pi.y, pi.z, pi.w, pj);
+              if (ok && K.nspec > 0 && P.i[I_SPEC * N + j] != spec_i) link = true;
             }
           }
           if (ok) kk = (unsigned)(orig[j] - oi - 1);
@@ -441,6 +451,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
     }  // stencil rounds
     if (cnt > (SUPER ? SUP_W : MAX_NB)) overflow = true;
     if (cnt > FILL_SLOTS) cnt = FILL_SLOTS;
+    if (__any_sync(0xffffffffu, link) && lane == 0) atomicOr(&P.st->errors, ERR_SPEC_LINK);
   }
   // Order the row's slots by key.  Keys are distinct (one per neighbour), so
   // each entry's final slot is the number of smaller keys: every lane ranks
@@ -486,7 +497,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_fill(DevPtrs P, DomainC
       P.i[I_NB * N + i] = cnt;
       if (K.contact) P.i[I_NWS * N + i] = (P.i[I_NWS * N + i] & 1) | ((ID[i] == K.id_free_surf) ? 2 : 0);
       if (overflow) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
-      pairs += (unsigned long long)cnt;
+      if (!keep_only) pairs += (unsigned long long)cnt;  // the filter counts the kept rows
     }
   } else if (lane == 0) {
     s_len[row] = 0;
@@ -593,9 +604,11 @@ __device__ __forceinline__ bool cells_adjacent(long long a, long long b) {
 // One warp per particle, 32 superset entries per round (one coalesced line of
 // the row-major superset); the kept entries are compacted by ballot in order
 // into shared memory, and the block writes its FILL_ROWS rows to the ELL
-// array one coalesced line per entry index.
+// array one coalesced line per entry index.  In a batched domain the rows of
+// specimens that do not search stay as they are (untouched, or put back by
+// k_nbr_fill after a reordering).
 template <bool COVER>
-__global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_filter(DevPtrs P, DomainConst K) {
+__global__ void __launch_bounds__(FILL_WARPS * 32, 4) k_nbr_filter(DevPtrs P, DomainConst K) {
   if (!searching(P) || !K.skin_on || !P.st->sup_valid) return;
   __shared__ int s_idx[FILL_ROWS][MAX_NB];
   __shared__ int s_len[FILL_ROWS];
@@ -610,6 +623,12 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_filter(DevPtrs P, Domai
       const int row = w * FILL_PER_WARP + rr;
       const int i = i0 + row;
       int cnt = 0;
+      if (K.nspec > 0 && i < K.N && !P.sp[P.i[I_SPEC * N + i]].do_search) {
+        if (lane == 0) { s_len[row] = 0; pairs += (unsigned long long)P.row_len[i]; }
+        continue;
+      }
+      const int spec_i = K.nspec > 0 && i < K.N ? P.i[I_SPEC * N + i] : 0;
+      bool link = false;
       const long long ci = i < K.N ? P.cellc[i] : -1;
       if (i < K.N && P.i[I_KIND * N + i] == 0 && ci >= 0) {
         const float4 pi = xs[i];
@@ -637,6 +656,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_filter(DevPtrs P, Domai
           if (lane + 32 * r < len) {
             ok = COVER || (cj[r] >= 0 && cells_adjacent(ci, cj[r]));
             if (ok) ok = radius_ok(P, K, N, i, nb_index(e[r]), pi.x, pi.y, pi.z, pi.w, pj[r]);
+            if (ok && K.nspec > 0 && P.i[I_SPEC * N + nb_index(e[r])] != spec_i) link = true;
           }
           const unsigned m = __ballot_sync(0xffffffffu, ok);
           if (ok) {
@@ -647,6 +667,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_nbr_filter(DevPtrs P, Domai
         }
       }
       if (cnt > MAX_NB && lane == 0) atomicOr(&P.st->errors, ERR_NBR_OVERFLOW);
+      if (__any_sync(0xffffffffu, link) && lane == 0) atomicOr(&P.st->errors, ERR_SPEC_LINK);
       if (cnt > MAX_NB) cnt = MAX_NB;
       __syncwarp();
       int split = 0;

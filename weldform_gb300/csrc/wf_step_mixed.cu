@@ -172,9 +172,9 @@ struct StagedFetch {
 };
 
 // Pair sums of the acceleration of SPH particle i over row entries k0, k0 + dk, ...
-// UNI: the uniform-particle layout (DomainConst::uni): h, mass and Cs are the
-// domain's constants, Sigma/rho^2 xz and yz come from the .w slots of the x
-// and v groups, and rho_j = mass / (m/rho)_j.
+// UNI: the uniform-particle layout (DomainConst::uni): h and Cs are the
+// domain's constants, m_j = m_i, Sigma/rho^2 xz and yz come from the .w slots
+// of the x and v groups, and rho_j = m_i / (m/rho)_j.
 template <bool TI, bool AVU, bool GC, bool UNI, class Fetch>
 __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainConst& K, int i, const Fetch& F, int k0,
                                               int dk, KSum& a0, KSum& a1, KSum& a2) {
@@ -184,7 +184,8 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
   float xl[3], vl[3];
   lo_unpack(lo, xl, vl);
   float4 s0 = ld4(ri + (size_t)RC_S0 * N), s1;
-  if (UNI) s1 = make_float4(xh.w, vh.w, K.mass_f, K.cs_f);
+  const float mass_i = UNI ? (float)col(P, C_MASS, N, i) : 0.f;
+  if (UNI) s1 = make_float4(xh.w, vh.w, mass_i, K.cs_f);
   else s1 = ld4(ri + (size_t)RC_S1 * N);
   const float hi_ = UNI ? K.h_f : xh.w;
   const float rhoi = UNI ? (float)col(P, C_RHO, N, i) : vh.w;
@@ -200,7 +201,7 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
     float4 jxh, jlo, jvh, js0, js1;
     int j = F.template get<UNI>(next, jxh, jlo, jvh, js0, js1);
     if (k + dk < len) next = F.key(k + dk);
-    if (UNI) js1 = make_float4(jxh.w, jvh.w, K.mass_f, K.cs_f);
+    if (UNI) js1 = make_float4(jxh.w, jvh.w, mass_i, K.cs_f);
     const float4* rj = P.rc + j;
     float jxl[3], jvl[3];
     lo_unpack(jlo, jxl, jvl);
@@ -222,8 +223,8 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
       if (dvx < 0.f) {  // Monaghan viscosity (InteractionAlt.cpp:74-94)
         float MU = hh * dvx / (r * r + 0.01f * hh * hh);
         float Cij = 0.5f * (s1.w + js1.w);
-        if (UNI)  // 1 / (0.5 (rho_i + rho_j)) with rho_j = mass / (m/rho)_j
-          PIs = (Alpha * Cij * MU + Beta * MU * MU) * (2.f * jlo.w) / (rhoi * jlo.w + K.mass_f);
+        if (UNI)  // 1 / (0.5 (rho_i + rho_j)) with rho_j = m_i / (m/rho)_j
+          PIs = (Alpha * Cij * MU + Beta * MU * MU) * (2.f * jlo.w) / (rhoi * jlo.w + mass_i);
         else
           PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5f * (rhoi + jvh.w));
       }
@@ -541,6 +542,7 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
     if (GC) cm = load_corr(P, N, i);
     KSum M[9];  // sum_j (m_j / rho_j) (-GK / 2) (v_i - v_j)_k (x_i - x_j)_l  (GC: gk_l for GK x_l)
     KSum kin, cnd;
+    const float mass_i = (float)col(P, C_MASS, N, i);
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
     for (int k = 0; k < len; ++k) {
@@ -568,8 +570,8 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
       M[6].add(wb2 * y0); M[7].add(wb2 * y1); M[8].add(wb2 * y2);
       bool up = nb_up(ent);  // original index of j larger than i's
       float dv = GK * (b0 * x0 + b1 * x1 + b2 * x2);
-      // m_P2 of the pair: the domain's one mass when uniform, else the column
-      float mP2 = K.m_uniform ? K.mass_f : (float)col(P, C_MASS, N, up ? j : i);
+      // m_P2 of the pair: m_i when the pairs' masses agree, else the column
+      float mP2 = K.m_pair ? mass_i : (float)col(P, C_MASS, N, up ? j : i);
       float pk = 0.5f * mP2 * (e.x + je.x) * dv;
       kin.add(up ? pk : -pk);
       if (THERMAL) {
