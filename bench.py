@@ -580,6 +580,10 @@ def sweep_mode(a):
     a0, b0 = sw.ranges[0]
     u_together = d.get_array("Displacement")[a0:b0]
     searches = [d.batch_get(k, "nb_searches") for k in range(len(specs))]
+    # per-kernel event timing over 20 more (instrumented) steps: ms per step
+    prof = d.profile_steps(20)
+    layout["kernel_ms_per_step"] = {k: round(v[0] / 20, 3) for k, v in
+                                    sorted(prof.items(), key=lambda kv: -kv[1][0])[:12]}
     d.close()
     seq_ms, seq_particles, solo_searches, u_alone = 0.0, 0, [], None
     t1 = time.perf_counter()

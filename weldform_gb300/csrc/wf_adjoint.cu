@@ -70,8 +70,10 @@ __device__ __forceinline__ GeoD geo_d(const double xi[3], double hi, double inv_
 // its value in vb (the last matching BC wins, as the forward loop).
 __device__ __forceinline__ bool bc_value(const DomainTables* T, int id, double t, double vb[3]) {
   bool hit = false;
-  for (int b = 0; b < T->nbc; ++b) {
-    if (T->bc[b].zone != id) continue;
+  int lo, hi;
+  bc_range(T, id, lo, hi);
+  for (int r = lo; r < hi; ++r) {
+    const int b = T->bc_order[r];
     if (T->bc[b].value_type == 0) {
       hit = true;
       for (int d = 0; d < 3; ++d) vb[d] = T->bc[b].value[d];

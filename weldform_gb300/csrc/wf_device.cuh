@@ -152,7 +152,25 @@ struct DomainTables {
   AmpDev amp[MAX_AMPS];
   double amp_t[MAX_AMP_POINTS], amp_v[MAX_AMP_POINTS];
   int nmat, nbc, namp;
+  // The BCs grouped by zone: bc_zone[0 .. bc_nzone) the distinct zones
+  // ascending; zone z's BCs are bc_order[bc_first[z] .. bc_first[z + 1]) in
+  // the order they were added (a later one overrides an earlier one).
+  int bc_nzone;
+  int bc_zone[MAX_BCS], bc_first[MAX_BCS + 1], bc_order[MAX_BCS];
 };
+
+// The range of bc_order holding the BCs of zone id (empty when it has none):
+// a binary search over the distinct zones, so a BC particle costs log2 of
+// the zone count however many BCs there are.
+__device__ __forceinline__ void bc_range(const DomainTables* T, int id, int& lo, int& hi) {
+  int a = 0, b = T->bc_nzone;
+  while (a < b) {
+    int m = (a + b) >> 1;
+    if (T->bc_zone[m] < id) a = m + 1; else b = m;
+  }
+  if (a < T->bc_nzone && T->bc_zone[a] == id) { lo = T->bc_first[a]; hi = T->bc_first[a + 1]; }
+  else { lo = 0; hi = 0; }
+}
 
 // Error bits raised by kernels (read by the host at synchronisation points).
 constexpr int ERR_NBR_OVERFLOW = 1;
@@ -160,7 +178,6 @@ constexpr int ERR_NAN = 2;
 constexpr int ERR_TIMEOUT = 4;
 constexpr int ERR_CONTACT_OVERFLOW = 8;
 constexpr int ERR_SPEC_LINK = 16;  // a neighbour pair joins two batched specimens
-constexpr int ERR_NO_SURFACE = 16;
 
 // Reduction slots (per-block partials, deterministic tree order).
 enum Slot : int {

@@ -524,6 +524,22 @@ struct wf_domain {
       B.zone = bcs[b].zone; B.value_type = bcs[b].vt; B.amp_id = bcs[b].amp; B.amp_factor = bcs[b].fac;
       for (int d = 0; d < 3; ++d) { B.value[d] = bcs[b].value[d]; B.value_ang[d] = bcs[b].ang[d]; }
     }
+    {
+      std::vector<int> order(bcs.size());
+      std::iota(order.begin(), order.end(), 0);
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return bcs[a].zone < bcs[b].zone; });
+      int nz = 0;
+      for (size_t r = 0; r < order.size(); ++r) {
+        ht.bc_order[r] = order[r];
+        if (r == 0 || bcs[order[r]].zone != bcs[order[r - 1]].zone) {
+          ht.bc_zone[nz] = bcs[order[r]].zone;
+          ht.bc_first[nz] = (int)r;
+          ++nz;
+        }
+      }
+      ht.bc_first[nz] = (int)order.size();
+      ht.bc_nzone = nz;
+    }
     ht.namp = (int)amps.size();
     int off = 0;
     for (size_t a = 0; a < amps.size(); ++a) {
@@ -536,9 +552,11 @@ struct wf_domain {
     std::vector<int> bl;
     bool any_surface_bc = false;
     for (auto& b : bcs) if (b.zone == 1) any_surface_bc = true;
+    const int* zb = ht.bc_zone;
+    const int* ze = ht.bc_zone + ht.bc_nzone;
     for (int p = 0; p < N; ++p) {
       bool hit = any_surface_bc && hp.i[I_KIND][p] == 0;
-      for (auto& b : bcs) if (hp.i[I_ID][p] == b.zone) hit = true;
+      if (std::binary_search(zb, ze, hp.i[I_ID][p])) hit = true;
       if (hit) bl.push_back(p);
     }
     int* dbl = dalloc<int>(bl.size());

@@ -565,20 +565,26 @@ __global__ void k_search_mode(DevPtrs P, DomainConst K) {
 // Cell coordinates at the current positions (ListGenerate's clamped cell
 // index, Neighbour.cpp:185-218, the same FP64 expression as k_cell_keys),
 // 21 bits per axis, -1 for a non-finite position; and the FP32 prefilter
-// coordinates.
+// coordinates.  COVER: the filter leaves the cell test out, so only the
+// finiteness is recorded.  In a batched domain only the particles of the
+// specimens that search are needed (no pair leaves a specimen).
+template <bool COVER>
 __global__ void k_cell_coords(DevPtrs P, DomainConst K) {
   if (!searching(P) || !K.skin_on || !P.st->sup_valid) return;
   const size_t N = K.N;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.N; p += gridDim.x * blockDim.x) {
+    if (K.nspec > 0 && !P.sp[P.i[I_SPEC * N + p]].do_search) continue;
     long long code = 0;
     bool finite = true;
     for (int d = 0; d < 3; ++d) {
       double xd = P.f[(C_X + d) * N + p];
       finite = finite && isfinite(xd);
-      int q = (int)floor(__ddiv_rn(__dsub_rn(xd, K.BLPF[d]), K.CellSize[d]));
-      if (q < 0) q = 0;
-      if (q >= K.CellNo[d]) q = K.CellNo[d] - 1;
-      code = (code << 21) | (long long)q;
+      if (!COVER) {
+        int q = (int)floor(__ddiv_rn(__dsub_rn(xd, K.BLPF[d]), K.CellSize[d]));
+        if (q < 0) q = 0;
+        if (q >= K.CellNo[d]) q = K.CellNo[d] - 1;
+        code = (code << 21) | (long long)q;
+      }
     }
     P.cellc[p] = finite ? code : -1;
     reinterpret_cast<float4*>(P.xs)[p] =
@@ -858,7 +864,8 @@ void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fsc
   }
   mark(s, "k_nbr_fill");
   if (K.skin_on) {
-    k_cell_coords<<<grid(K.N), T, 0, s>>>(P, K);
+    if (K.cells_cover) k_cell_coords<true><<<grid(K.N), T, 0, s>>>(P, K);
+    else k_cell_coords<false><<<grid(K.N), T, 0, s>>>(P, K);
     mark(s, "k_cell_coords");
     int groups = nblk(K.N, FILL_ROWS), cap = 152 * 4;
     if (K.cells_cover) k_nbr_filter<true><<<groups < cap ? groups : cap, FILL_WARPS * 32, 0, s>>>(P, K);

@@ -332,8 +332,10 @@ __global__ void k_bc(DevPtrs P, DomainConst K, int vcol) {
   size_t N = K.N;
   int i = P.inv[P.bc_list[k]];
   int id = icol(P, I_ID, N, i);
-  for (int b = 0; b < T->nbc; ++b) {
-    if (T->bc[b].zone != id) continue;
+  int lo, hi;
+  bc_range(T, id, lo, hi);
+  for (int r = lo; r < hi; ++r) {
+    const int b = T->bc_order[r];
     if (T->bc[b].value_type == 0) {
       for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = T->bc[b].value[d]; }
     } else {

@@ -106,7 +106,9 @@ __device__ __forceinline__ void corr_gk(const CorrM& c, float GK, float x0, floa
 
 // ---------------------------------------------------------------- records
 __global__ void k_refresh_records(DevPtrs P, DomainConst K, int force) {
-  if (!force && !P.st->do_search) return;
+  // After a search that reordered the particles (a filter-only search keeps
+  // the order, and every step writes the records from the FP64 state).
+  if (!force && !(P.st->do_search && P.st->search_full)) return;
   size_t N = K.N;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K.N; i += gridDim.x * blockDim.x) {
   bool solid = icol(P, I_KIND, N, i) == 0;
