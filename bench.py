@@ -69,6 +69,14 @@ ALG_BYTES = {
 }
 # FP64 operations per neighbour entry / per particle (plain form).
 ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (70, 270)}
+# The step kernels of each form: their algorithmic bytes summed give the
+# step's compulsory traffic per particle-step (state read and written once
+# per pass, neighbour re-reads from cache, 4 B per row entry per gather).
+STEP_KERNELS = {"mixed": ("k_accel_mx", "k_density_drift_mx", "k_rate_mx", "k_stress_mx"),
+                "fp64": ("k_accel", "k_density_drift", "k_rate_stress")}
+# FP64 fused multiply-add rate of the GB300 (`python bench.py --pipe-rates`:
+# 503 G FMA/s), the plain form's secondary ceiling.
+FP64_PEAK_TFLOPS = 1.006
 
 
 def _env_int(k, d):
@@ -199,6 +207,22 @@ def roofline(d, case, nnz, steps, peak_gbs, peak_kind):
             "alg_bytes_per_launch": alg, "ms_per_launch": round(ms, 4),
             "fp64_tflops": round(flops / (ms * 1e-3) / 1e12, 4) if flops else None,
             "kernel_time_shares": shares}
+
+
+def step_roofline(form, nnz, particle_steps_per_s, peak_gbs):
+    """The whole step against HBM: the step kernels' algorithmic bytes per
+    particle-step times the particle-steps/s; for the plain form also the
+    algorithmic FP64 flops against the FP64 pipe."""
+    ks = STEP_KERNELS["fp64" if form == "fp64" else "mixed"]
+    b = sum(ALG_BYTES[k](nnz) for k in ks)
+    gbs = b * particle_steps_per_s / 1e9
+    out = {"bytes_per_particle_step": round(b, 1), "achieved_gbs": round(gbs, 1), "frac_hbm": round(gbs / peak_gbs, 4)}
+    if form == "fp64":
+        fl = sum(ALG_FLOPS[k][0] * nnz + ALG_FLOPS[k][1] for k in ks)
+        tf = fl * particle_steps_per_s / 1e12
+        out.update({"flops_per_particle_step": round(fl), "fp64_tflops": round(tf, 3),
+                    "frac_fp64": round(tf / FP64_PEAK_TFLOPS, 4)})
+    return out
 
 
 E2E_OUT_EVERY = 20
@@ -760,6 +784,7 @@ def main():
         searches = d.geti("nb_searches") - s0
         full = d.geti("nb_full_searches") - f0
         rl = roofline(d, case, nnz, steps, peak, peak_kind)
+        rl["step"] = step_roofline(name, nnz, val, peak)
         forms[name] = {"value": val, "ms_per_step": ms_max / steps, "steps": steps, "roofline": rl,
                        "gpu_launches": launches, "clocks": clk.summary(), "v_top": vt,
                        "rebuilds_in_timed_steps": searches, "full_searches_in_timed_steps": full}
