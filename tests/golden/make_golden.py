@@ -18,6 +18,10 @@ before that step's update, SolverFraser.cpp:151-159), contact force and
 reaction sums, external work, internal and kinetic energy, each with the 6
 significant digits of the log.
 
+3. reference_decks.json — the reference's example input decks
+(examples/input/*.json) that the JSON front-end accepts: 3D Cartesian
+domains, Nishimura sums, no damage, no mesh files, no pure-thermal solver.
+
 Run in a tree where the reference is mounted:
 
     python tests/golden/make_golden.py /path/to/WeldForm
@@ -108,9 +112,24 @@ def fraser_log(ref_root: str):
     print("wrote", path, len(rows), "outputs")
 
 
+DECKS = ("Cantilever", "Compression", "Compression_fast_short", "Compression_thermal", "Contact_Compression",
+         "Contact_Compression_Fraser", "Contact_Compression_JC", "Contact_Compression_Rot",
+         "Contact_Compression_Rot_JC", "Contact_Compression_Wang", "Impact_Campos", "Traction")
+
+
+def decks(ref_root: str):
+    out = {"source": "examples/input/<name>.json (WeldForm)",
+           "decks": {n: json.load(open(os.path.join(ref_root, "examples", "input", n + ".json"))) for n in DECKS}}
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_decks.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", path, len(DECKS), "decks")
+
+
 def main(ref_root: str):
     reduction_table(ref_root)
     fraser_log(ref_root)
+    decks(ref_root)
 
 
 if __name__ == "__main__":

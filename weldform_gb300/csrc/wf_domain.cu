@@ -181,7 +181,102 @@ struct wf_domain {
   std::vector<Region> regions;           // every mutable device region of the state
   std::vector<std::vector<void*>> slots; // checkpoint copies, one vector per slot
   bool shadows_valid = false;  // float shadows of the mixed form match the FP64 state
-  long long launches_per_step = 0;
+  long long launches_per_step = 0;     // launches every replay of the step graph makes
+  long long search_launches = 0;       // launches in its conditional search body (0: gated form)
+  bool cond_ok = true;                 // conditional search capture works here (cleared on failure)
+  cudaStream_t body_stream = nullptr;  // captures the conditional search body
+  // wf::SearchCond for one capture: the IF node on a fresh handle of the
+  // capturing graph, its body captured on body_stream.
+  struct CondCapture : wf::SearchCond {
+    cudaStream_t body;
+    cudaGraph_t body_graph = nullptr;
+    cudaGraphConditionalHandle handle = 0;
+    long long l0 = 0, body_launches = 0;
+    explicit CondCapture(cudaStream_t b) : body(b) {}
+    unsigned long long begin(cudaStream_t s) override {
+      cudaStreamCaptureStatus st;
+      cudaGraph_t g;
+      const cudaGraphNode_t* deps;
+      size_t nd;
+      CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+      if (st != cudaStreamCaptureStatusActive) throw CudaError{WF_ERR_CUDA, "conditional search outside a capture"};
+      CK(cudaGraphConditionalHandleCreate(&handle, g, 0, cudaGraphCondAssignDefault));
+      return (unsigned long long)handle;
+    }
+    cudaStream_t open_body(cudaStream_t s) override {
+      cudaStreamCaptureStatus st;
+      cudaGraph_t g;
+      const cudaGraphNode_t* deps;
+      size_t nd;
+      CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeIf;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node;
+      CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
+      body_graph = cp.conditional.phGraph_out[0];
+      CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+      CK(cudaStreamBeginCaptureToGraph(body, body_graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      l0 = wf::g_launches;
+      return body;
+    }
+    void close_body() override {
+      body_launches = wf::g_launches - l0;
+      CK(cudaStreamEndCapture(body, &body_graph));
+    }
+  };
+  // Ends any capture left open on the domain's streams after a failure.
+  void abort_capture() {
+    for (cudaStream_t st : {body_stream, stream}) {
+      if (!st) continue;
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+      }
+    }
+    cudaGetLastError();
+  }
+  // Captures one step into the step graph: with the search in a conditional
+  // node when that works on this device and driver, else in the gated form.
+  void capture_step_graph() {
+    if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+    graph_block = graph_key();
+    for (int attempt = cond_ok ? 0 : 1; attempt < 2; ++attempt) {
+      const bool cond = attempt == 0;
+      try {
+        if (cond && !body_stream) CK(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
+        CondCapture cc(body_stream);
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        long long l0 = wf::g_launches;
+        wf::g_search_cond = cond ? &cc : nullptr;
+        try {
+          launch_one_step();
+        } catch (...) {
+          wf::g_search_cond = nullptr;
+          throw;
+        }
+        wf::g_search_cond = nullptr;
+        search_launches = cond ? cc.body_launches : 0;
+        launches_per_step = wf::g_launches - l0 - search_launches;
+        CK(cudaStreamEndCapture(stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) throw CudaError{WF_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)};
+        graph_precision = precision;
+        return;
+      } catch (CudaError&) {
+        abort_capture();
+        if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+        if (!cond) throw;
+        cond_ok = false;  // capture the gated form from now on
+      }
+    }
+  }
   double hmax = 0;
   double BLPF[3] = {0, 0, 0}, TRPR[3] = {0, 0, 0};
   int CellNo[3] = {0, 0, 0};
@@ -194,6 +289,7 @@ struct wf_domain {
     if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
+    if (body_stream) { cudaStreamDestroy(body_stream); body_stream = nullptr; }
     if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
     prepared = false;
   }
@@ -782,19 +878,7 @@ struct wf_domain {
     use_device();
     ensure_shadows();
     if (use_graph) {
-      if (!graph || graph_precision != precision || graph_block != graph_key()) {
-        if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
-        graph_block = graph_key();
-        cudaGraph_t g;
-        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        long long l0 = wf::g_launches;
-        launch_one_step();
-        launches_per_step = wf::g_launches - l0;
-        CK(cudaStreamEndCapture(stream, &g));
-        CK(cudaGraphInstantiate(&graph, g, 0));
-        CK(cudaGraphDestroy(g));
-        graph_precision = precision;
-      }
+      if (!graph || graph_precision != precision || graph_block != graph_key()) capture_step_graph();
       for (long long s = 0; s < n; ++s) CK(cudaGraphLaunch(graph, stream));
     } else {
       for (long long s = 0; s < n; ++s) launch_one_step();
@@ -812,6 +896,7 @@ struct wf_domain {
     if (use_graph && (!graph || graph_precision != precision || graph_block != graph_key())) step(0);
     ensure_shadows();
     long long l0 = wf::g_launches;
+    const long long s0 = search_launches ? read_state().nb_searches : 0;
     CK(cudaEventRecord(a, stream));
     if (use_graph) {
       for (long long s = 0; s < n; ++s) CK(cudaGraphLaunch(graph, stream));
@@ -824,7 +909,10 @@ struct wf_domain {
     CK(cudaEventElapsedTime(&ms, a, b));
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    *launches = use_graph ? launches_per_step * n : wf::g_launches - l0;
+    // graph replays: every step's launches, plus the search body's on the
+    // steps that searched
+    *launches = use_graph ? launches_per_step * n + (search_launches ? search_launches * (read_state().nb_searches - s0) : 0)
+                          : wf::g_launches - l0;
     check_errors();
     return ms;
   }

@@ -24,6 +24,22 @@ inline void mark(cudaStream_t s, const char* name) {
   }
 }
 
+// Conditional search in a captured step: while a step graph is captured with
+// g_search_cond set, the step head asks it for a graph conditional handle,
+// which k_schedule sets to the step's search decision, and captures the
+// search (and the mixed form's record refresh) into the body of an IF node on
+// that handle.  A step that does not search then launches none of the search
+// kernels instead of launching each to return at once.  Implemented by the
+// domain (it owns the streams); any failure throws and the domain captures
+// the plain gated form instead.
+struct SearchCond {
+  virtual unsigned long long begin(cudaStream_t s) = 0;   // before k_schedule: the handle
+  virtual cudaStream_t open_body(cudaStream_t s) = 0;     // after it: the stream to capture the body on
+  virtual void close_body() = 0;                          // after the body's kernels
+  virtual ~SearchCond() {}
+};
+extern thread_local SearchCond* g_search_cond;
+
 // Neighbour search pipeline (wf_nbsearch.cu); every kernel is gated on
 // StepState::do_search.
 void launch_neighbour_search(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch,

@@ -35,13 +35,15 @@ namespace wf {
 
 thread_local KernelTimer* g_timer = nullptr;
 thread_local long long g_launches = 0;
+thread_local SearchCond* g_search_cond = nullptr;
 
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------- schedule
 // One block.  A batched domain decides per specimen (the same rules on the
-// specimen's own state) and searches when any specimen asks.
-__global__ void k_schedule(DevPtrs P, DomainConst K) {
+// specimen's own state) and searches when any specimen asks.  cond: the
+// captured step's conditional handle of the search (0 outside such a graph).
+__global__ void k_schedule(DevPtrs P, DomainConst K, unsigned long long cond) {
   StepState* s = P.st;
   __shared__ int any_search, any_regular;
   if (threadIdx.x == 0) { any_search = 0; any_regular = 0; }
@@ -84,6 +86,7 @@ __global__ void k_schedule(DevPtrs P, DomainConst K) {
   // CalcGradCorrMatrix: kick-drift at its first step (SolverKickDrift.cpp:189-191),
   // leapfrog after every regular search and at the first step (SolverLeapfrog.cpp:186-204)
   s->do_gradcorr = K.gradcorr && (s->isfirst || (K.leapfrog && regular));
+  if (cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, search ? 1u : 0u);
 }
 
 __global__ void k_step_end(DevPtrs P, DomainConst K) {
@@ -926,9 +929,14 @@ void launch_scatter_orig_i32(const DevPtrs& P, const DomainConst& K, const int* 
 
 // ---------------------------------------------------------------- one step
 void launch_step_head(const DevPtrs& P, const DomainConst& K, double* fscratch, int* iscratch, cudaStream_t s) {
-  k_schedule<<<1, 256, 0, s>>>(P, K);
+  SearchCond* c = g_search_cond;
+  unsigned long long cond = c ? c->begin(s) : 0ull;
+  k_schedule<<<1, 256, 0, s>>>(P, K, cond);
   mark(s, "k_schedule");
-  launch_neighbour_search(P, K, fscratch, iscratch, s);
+  cudaStream_t ss = c ? c->open_body(s) : s;
+  launch_neighbour_search(P, K, fscratch, iscratch, ss);
+  if (K.mixed) launch_refresh_shadows(P, K, 0, ss);  // after a search that reordered the particles
+  if (c) c->close_body();
   if (K.gradcorr) {
     int b = K.nblocks;
     k_grad_corr<<<b < 152 * 8 ? b : 152 * 8, K.pblock, 0, s>>>(P, K);

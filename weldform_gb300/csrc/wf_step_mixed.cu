@@ -837,7 +837,6 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   int gb = (K.gblock == 64 || K.gblock == 128 || K.gblock == 512) ? K.gblock : 256;
   int ng = nblk(K.N, gb);
   launch_step_head(P, K, fscratch, iscratch, s);
-  launch_refresh_shadows(P, K, 0, s);
   launch_tensile(P, K, s);
   const bool staged = K.stage_cap > 0 && P.halo && !K.ti && K.av_uniform && !K.gradcorr;
   if (staged) {

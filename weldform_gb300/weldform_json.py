@@ -17,7 +17,8 @@ Supported input (everything the kick-drift / leapfrog path covers):
                  the contact one with leapfrog), artifViscAlpha/Beta,
                  contAlgorithm ("Wang"; "Fraser" also selects Wang, as the
                  reference), tensileInstability (default 0.3), nbsearchFreq,
-                 sumType "Nishimura", stressGradType 0
+                 sumType "Nishimura" (an unknown value keeps it, as the reference
+                 does), stressGradType 0
   Materials[0]   Bilinear (const[0] = Et), Hollomon (yieldStress0, const = K, m),
                  JohnsonCook (const = A, B, n, C, eps_0, m, T_m, T_t);
                  density0, youngsModulus, poissonsRatio, plasticHeat,
@@ -103,8 +104,11 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
     if precision is not None:
         dom.set("precision", precision)
     # ---- Configuration (WeldForm.cpp:195-226, 345-393)
-    if config.get("sumType", "Nishimura") != "Nishimura":
-        _unsupported("sumType: only the Nishimura sum")
+    # WeldForm.cpp:198-202: "Locking" clears nonlock_sum; any other value but
+    # "Nishimura" only prints a notice and keeps the default (Nishimura,
+    # Domain.cpp:159).
+    if config.get("sumType", "Nishimura") == "Locking":
+        _unsupported("sumType Locking: only the Nishimura sum")
     dom.Kernel_Set(0)
     solver = config.get("solver", "Mech")
     leapfrog = ("Mech", "Mech-Thermal", "Mech-LeapFrog", "Mech-Thermal-LeapFrog")
