@@ -4,8 +4,10 @@ Callers that cannot allocate device memory (code inside a memory pool owned
 by another library, a plugin host that forbids device allocations, a
 real-time loop) pass their own input and output buffers; the search's working
 memory is a fixed device array inside the library.  This checks, through the
-C ABI, that two calls in a row give exactly the neighbour rows of the
-domain's own rebuild (integer output: the tolerance is equality), that rows
+C ABI, that three calls in a row — two on the default stream, one on a
+stream of the caller's — give exactly the neighbour rows of the domain's own
+rebuild (integer output: the tolerance is equality) without taking device
+memory (free memory unchanged across each call after the first), that rows
 with more than 100 neighbours are cut at their 100 smallest keys, and that
 sizes beyond the fixed maximum — including a cell grid whose cell count
 overflows 32 bits — are refused with a clear error.  The file is collected
@@ -49,7 +51,7 @@ def _bind(lib):
     return fn
 
 
-def test_static_search_matches_domain_rebuild_on_two_calls():
+def test_static_search_matches_domain_rebuild_on_three_calls():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no GPU")
@@ -77,14 +79,20 @@ def test_static_search_matches_domain_rebuild_on_two_calls():
     cc = (ctypes.c_double * 3)(*cs)
     cn = (ctypes.c_int32 * 3)(*no)
     results = []
-    for call in range(2):
+    side = torch.cuda.Stream(device=dev)
+    for call in range(3):
         rl = torch.full((n,), -7, dtype=torch.int32, device=dev)
         nb = torch.full((100 * n,), -7, dtype=torch.int32, device=dev)
         torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(dev)[0]
+        # the first two on the default stream, the third on a caller's stream
+        st = ctypes.c_void_p(side.cuda_stream) if call == 2 else None
         rc = fn(X[0].data_ptr(), X[1].data_ptr(), X[2].data_ptr(), H.data_ptr(), n, cb, cc, cn, 2.0,
-                rl.data_ptr(), nb.data_ptr(), None)
+                rl.data_ptr(), nb.data_ptr(), st)
         assert rc == 0, lib.wf_last_error()
         torch.cuda.synchronize()
+        if call > 0:  # after the first call (module load), no call takes device memory
+            assert torch.cuda.mem_get_info(dev)[0] == free0
         rl_h = rl.cpu().numpy()
         nb_h = nb.cpu().numpy().reshape(100, n)
         assert (rl_h >= 0).all() and (rl_h <= 100).all()
