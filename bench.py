@@ -235,7 +235,10 @@ def e2e(wfmod, precision, steps, gpu, pinned):
     last).  20 steps is the dense end of the reference inputs' output
     intervals (1e-6 s at ~5.7e-8 s steps in the impact input; up to ~2000
     steps in the compression inputs), so the read-back cost per step does not
-    shrink with K."""
+    shrink with K.  The reads are the asynchronous form
+    (wf_get_particle_array_f64_async): each output is snapshotted on the
+    device between steps and copied to the host while the next steps run;
+    the timed region ends after wf_synchronize, with every copy landed."""
     d = wfmod.Domain()
     d.set("device", gpu)
     d.set("precision", precision)
@@ -255,9 +258,10 @@ def e2e(wfmod, precision, steps, gpu, pinned):
         k = min(E2E_OUT_EVERY, steps - done)
         d.step(k)
         done += k
-        d.get_array("x", out=xo)
-        d.get_array("Sigma", out=so)
+        d.get_array_async("x", xo)
+        d.get_array_async("Sigma", so)
         reads += 1
+    d.synchronize()
     el = time.perf_counter() - t0
     h2d = (x.nbytes + v.nbytes) / steps
     d2h = reads * (xo.nbytes + so.nbytes) / steps

@@ -174,6 +174,12 @@ int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value);
 int wf_set_particle_array_f64(wf_domain* d, const char* field, const double* src,
                               int64_t n);
 int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int64_t n);
+/* The same read, asynchronous: the field is snapshotted on the device in order
+ * with the steps already enqueued and copied to dst on a copy stream while
+ * later steps run; dst holds the values once wf_synchronize returns (up to
+ * four reads may be in flight; a fifth waits for the oldest).  dst must stay
+ * valid until then; pinned host memory lets the copy overlap the steps. */
+int wf_get_particle_array_f64_async(wf_domain* d, const char* field, double* dst, int64_t n);
 /* Integer arrays: "ID", "Nb", "IsFree", "Thermal_BC". */
 int wf_get_particle_array_i32(wf_domain* d, const char* field, int32_t* dst, int64_t n);
 /* Per-particle integer fields as whole arrays, before the prologue: "ID",
@@ -268,8 +274,9 @@ int wf_batch_specimens(wf_domain* d, const int64_t* first, const int64_t* count,
  * "yielding" (1 once it has yielded), "first", "particle_count". */
 int wf_batch_get_i32(wf_domain* d, int spec, const char* name, int64_t* value);
 
-/* Blocks until the domain's stream is idle and reports deferred device
- * status (non-finite state, neighbour overflow, bounded-wait timeout). */
+/* Blocks until the domain's streams are idle (steps and asynchronous reads)
+ * and reports deferred device status (non-finite state, neighbour overflow,
+ * bounded-wait timeout). */
 int wf_synchronize(wf_domain* d);
 
 /* ---- device checkpoints ----------------------------------------------------

@@ -1941,6 +1941,10 @@ int wfo_get_contact_pairs(wfo_domain* p, int64_t* off, int32_t* idx, int64_t cap
   return WF_OK;
 }
 int wfo_synchronize(wfo_domain*) { return WF_OK; }
+// The oracle reads at once; the asynchronous form is the same read.
+int wfo_get_particle_array_f64_async(wfo_domain* p, const char* field, double* dst, int64_t n) {
+  return wfo_get_particle_array_f64(p, field, dst, n);
+}
 // Checkpoints of the whole oracle state (a copy of the Domain object).
 static std::vector<Domain*> g_slots[1];
 int wfo_checkpoint_save(wfo_domain* p, int slot) {

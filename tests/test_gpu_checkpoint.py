@@ -57,3 +57,40 @@ def test_autotune_keeps_state_and_results():
         res.append(_state(d))
     for k in res[0]:
         assert np.array_equal(res[0][k], res[1][k]), k
+
+
+@pytest.mark.gpu
+def test_asynchronous_reads_snapshot_the_state_at_the_call():
+    """wf_get_particle_array_f64_async: each read holds the field as it was
+    when the read was enqueued, although steps run on while it copies, and
+    more reads than the four snapshot buffers still all land (the fifth
+    waits for the first).  Compared bit for bit with synchronous reads of an
+    identical run."""
+    torch = pytest.importorskip("torch")
+
+    def run(asynchronous):
+        d = gpu_domain()
+        d.set("precision", PRECISION_MIXED)
+        case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+        d.prepare(case.dt)
+        n = d.particle_count
+        out = []
+        for k in range(6):
+            d.step(3)
+            if asynchronous:
+                xo = torch.empty(n * 3, dtype=torch.float64).pin_memory().numpy()
+                so = torch.empty(n * 9, dtype=torch.float64).pin_memory().numpy()
+                out.append((d.get_array_async("x", xo), d.get_array_async("Sigma", so)))
+            else:
+                out.append((d.get_array("x").ravel().copy(), d.get_array("Sigma").ravel().copy()))
+        if asynchronous:
+            d.step(4)  # still running when the last reads are enqueued
+            d.synchronize()
+        out = [(x.copy(), s.copy()) for x, s in out]
+        d.close()
+        return out
+
+    a, b = run(True), run(False)
+    for (xa, sa), (xb, sb) in zip(a, b):
+        assert np.array_equal(xa, xb) and np.array_equal(sa, sb)
+    assert not np.array_equal(a[0][0], a[-1][0])

@@ -76,6 +76,7 @@ _SIGS = {
     "set_particle_i32": [_P, _S, _I, _I],
     "set_particle_array_f64": [_P, _S, _DP, _I64],
     "get_particle_array_f64": [_P, _S, _DP, _I64],
+    "get_particle_array_f64_async": [_P, _S, _DP, _I64],
     "get_particle_array_i32": [_P, _S, _IP, _I64],
     "set_particle_array_i32": [_P, _S, _IP, _I64],
     "add_material": [_P, _I, _DP, _I, ctypes.POINTER(_I)],
@@ -361,6 +362,19 @@ class Domain:
         if out is not None:
             return out
         return buf.reshape(n, comps) if comps > 1 else buf
+
+    def get_array_async(self, field: str, out: np.ndarray) -> np.ndarray:
+        """Enqueues a read of a float particle field into ``out`` (C-contiguous
+        float64 of the field's size; pinned host memory lets the copy overlap
+        later steps) and returns it at once; it holds the values after
+        ``synchronize()`` (wf_get_particle_array_f64_async)."""
+        n = self.particle_count
+        comps = 9 if field in TENSOR_FIELDS else (3 if field in VECTOR_FIELDS else 1)
+        if out.dtype != np.float64 or out.size != n * comps or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"{field}: out must be a C-contiguous float64 array of {n * comps} values")
+        buf = out.reshape(-1)
+        self._call("get_particle_array_f64_async", self._h, field.encode(), buf.ctypes.data_as(_DP), buf.size)
+        return out
 
     def set_array(self, field: str, values):
         if field in ("ID", "mat", "Material_model", "Fail", "Material", "not_write_surf_ID", "Thermal_BC"):

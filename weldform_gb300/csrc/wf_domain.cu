@@ -185,6 +185,18 @@ struct wf_domain {
   long long search_launches = 0;       // launches in its conditional search body (0: gated form)
   bool cond_ok = true;                 // conditional search capture works here (cleared on failure)
   cudaStream_t body_stream = nullptr;  // captures the conditional search body
+  // Asynchronous read-back (wf_get_particle_array_f64_async): the field is
+  // gathered on the domain's stream into a snapshot buffer, and the copy to
+  // the host runs on copy_stream, so steps enqueued after it overlap the copy.
+  cudaStream_t copy_stream = nullptr;
+  struct Snapshot {
+    double* buf = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t ready = nullptr, done = nullptr;  // gathered; copied out
+    bool used = false;
+  };
+  std::vector<Snapshot> snaps = std::vector<Snapshot>(4);  // a ring: four reads in flight
+  size_t snap_next = 0;
   // wf::SearchCond for one capture: the IF node on a fresh handle of the
   // capturing graph, its body captured on body_stream.
   struct CondCapture : wf::SearchCond {
@@ -290,6 +302,13 @@ struct wf_domain {
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
     if (body_stream) { cudaStreamDestroy(body_stream); body_stream = nullptr; }
+    if (copy_stream) { cudaStreamSynchronize(copy_stream); cudaStreamDestroy(copy_stream); copy_stream = nullptr; }
+    for (auto& sn : snaps) {
+      if (sn.buf) cudaFree(sn.buf);
+      if (sn.ready) cudaEventDestroy(sn.ready);
+      if (sn.done) cudaEventDestroy(sn.done);
+      sn = Snapshot();
+    }
     if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
     prepared = false;
   }
@@ -1349,6 +1368,39 @@ struct wf_domain {
     CK(cudaFreeAsync(tmp, stream));
     CK(cudaStreamSynchronize(stream));
   }
+  // Enqueues a read of column c (ncomp components, or a tensor expanded to
+  // 3x3 rows) into dst and returns: the gather runs on the stream in order
+  // with the steps, the copy on copy_stream after it.  dst is complete when
+  // wf_synchronize returns.
+  void get_f64_async(int c, int ncomp, bool tensor, int anti, double* dst) {
+    const size_t n = hp.N;
+    const size_t bytes = sizeof(double) * n * (tensor ? 9 : ncomp);
+    use_device();
+    if (!copy_stream) CK(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+    Snapshot& sn = snaps[snap_next];
+    snap_next = (snap_next + 1) % snaps.size();
+    if (!sn.ready) {
+      CK(cudaEventCreateWithFlags(&sn.ready, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&sn.done, cudaEventDisableTiming));
+    }
+    if (sn.used) CK(cudaStreamWaitEvent(stream, sn.done, 0));  // its last copy has left the buffer
+    if (sn.bytes < bytes) {
+      if (sn.buf) {
+        CK(cudaStreamSynchronize(copy_stream));
+        CK(cudaFree(sn.buf));
+      }
+      sn.buf = nullptr;
+      CK(cudaMalloc((void**)&sn.buf, bytes));
+      sn.bytes = bytes;
+    }
+    if (tensor) wf::launch_gather_orig_tensor(P, K, d_f + (size_t)c * n, sn.buf, anti, stream);
+    else wf::launch_gather_orig(P, K, d_f + (size_t)c * n, sn.buf, ncomp, stream);
+    CK(cudaEventRecord(sn.ready, stream));
+    CK(cudaStreamWaitEvent(copy_stream, sn.ready, 0));
+    CK(cudaMemcpyAsync(dst, sn.buf, bytes, cudaMemcpyDeviceToHost, copy_stream));
+    CK(cudaEventRecord(sn.done, copy_stream));
+    sn.used = true;
+  }
   void set_f64(int c, int ncomp, const double* src) {
     size_t n = hp.N;
     if (!prepared) {
@@ -1753,6 +1805,22 @@ int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int6
     return WF_OK;
   });
 }
+int wf_get_particle_array_f64_async(wf_domain* d, const char* field, double* dst, int64_t n) {
+  NEED(d);
+  return guard([&] {
+    std::string f(field ? field : "");
+    int nc = 0;
+    int c = col_f64(f, &nc);
+    if (c < 0) return set_err(WF_ERR_ARG, "unknown particle array " + f);
+    if (!dst) return set_err(WF_ERR_ARG, "null destination");
+    const size_t N = d->hp.N;
+    const bool tensor = nc == 6 || c == wf::C_RR;
+    if (n != (int64_t)N * (tensor ? 9 : nc)) return set_err(WF_ERR_ARG, "array size mismatch for " + f);
+    if (!d->prepared) return wf_get_particle_array_f64(d, field, dst, n);  // host arrays: read at once
+    d->get_f64_async(c, nc, tensor, nc == 3, dst);
+    return WF_OK;
+  });
+}
 int wf_get_particle_array_i32(wf_domain* d, const char* field, int32_t* dst, int64_t n) {
   NEED(d);
   return guard([&] {
@@ -2024,6 +2092,7 @@ int wf_synchronize(wf_domain* d) {
     if (!d->prepared) return WF_OK;
     d->use_device();
     CK(cudaStreamSynchronize(d->stream));
+    if (d->copy_stream) CK(cudaStreamSynchronize(d->copy_stream));
     d->check_errors();
     return WF_OK;
   });
