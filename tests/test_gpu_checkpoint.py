@@ -94,3 +94,23 @@ def test_asynchronous_reads_snapshot_the_state_at_the_call():
     for (xa, sa), (xb, sb) in zip(a, b):
         assert np.array_equal(xa, xb) and np.array_equal(sa, sb)
     assert not np.array_equal(a[0][0], a[-1][0])
+
+
+@pytest.mark.gpu
+def test_conditional_search_graph_matches_the_gated_graph():
+    """search_conditional: the step graph's search in a conditional node gives
+    bit-identical results to the default gated form, through searches
+    (yielding cylinder, a search every 5 steps)."""
+    out = []
+    for cond in (0, 1):
+        d = gpu_domain()
+        d.set("precision", PRECISION_MIXED)
+        d.set("search_conditional", cond)
+        case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
+        d.prepare(case.dt)
+        d.step(60)
+        assert d.geti("search_conditional") == cond
+        out.append((d.get_array("x"), d.get_array("Sigma"), d.geti("nb_searches")))
+        d.close()
+    assert out[0][2] == out[1][2] > 5
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])

@@ -216,9 +216,10 @@ def test_mixed_particles_of_different_mass_and_smoothing_length():
 
 @pytest.mark.parametrize("lanes", [2, 4, 8])
 def test_mixed_acceleration_gather_lanes(lanes):
-    """The acceleration gather with `lanes` lanes per particle (per-lane
-    Kahan sums combined in FP64 by warp shuffles): within the bound against
-    the oracle, and bit-identical across block sizes at a fixed lane count."""
+    """The acceleration, density and rate gathers with `lanes` lanes per
+    particle (per-lane Kahan sums combined in FP64 by warp shuffles): within
+    the bound against the oracle, and bit-identical across block sizes at a
+    fixed lane count."""
     f = FIELDS + ("pl_strain",)
 
     def build(d, **kw):
@@ -235,7 +236,7 @@ def test_mixed_acceleration_gather_lanes(lanes):
         case = configs.cylinder_upsetting(d, R=0.004, L=0.008, dx=0.0005, v_top=-20.0)
         d.prepare(case.dt)
         d.step(30)
-        res.append(d.get_array("a"))
+        res.append(np.concatenate([d.get_array(f).ravel() for f in ("a", "Density", "Sigma")]))
         d.close()
     for r in res[1:]:
         assert np.array_equal(r, res[0])

@@ -160,7 +160,7 @@ struct wf_domain {
   int auto_ts = 0, auto_ts_acc = 0, auto_ts_cont = 0;
   double CFL = 0.7, sqrt_h_a = 0.0025;
   int gblock = 0;    // mixed gathers' threads per block (0: chosen by particle count)
-  int glanes = 1;    // lanes per particle of the mixed acceleration gather (1, 2, 4, 8)
+  int glanes = 0;    // lanes per particle of the mixed acceleration gather (1, 2, 4, 8; 0: by particle count)
   int pblock = 0;    // per-particle kernels' threads per block (0: chosen by particle count)
   // Shared-memory staging of the mixed acceleration gather: the halo lists
   // are allocated at the prologue when it is on; stage_cap is each block's
@@ -173,9 +173,16 @@ struct wf_domain {
   // idle, so smaller blocks spread the particles over every SM.
   static int auto_block(long long n) { return n < 78000 ? 64 : (n < 156000 ? 128 : 256); }
   int gblock_now() const { return gblock ? gblock : auto_block(hp.N); }
+  // Below ~60k particles a gather's time is its rows' chain of dependent
+  // loads (one thread walks ~55 entries), not throughput: splitting each
+  // row over 4 or 8 lanes shortens the chain (measured on GB300: 8,004
+  // particles 32 -> 12 us for the acceleration gather with 8 lanes, 29,520
+  // particles 34 -> 19 us with 4; from ~100k on one lane is as fast).
+  static int auto_lanes(long long n) { return n < 20000 ? 8 : (n < 60000 ? 4 : 1); }
+  int glanes_now() const { return glanes ? glanes : auto_lanes(hp.N); }
   int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
   int graph_key() const {
-    return ((gblock_now() * 1024 + pblock_now()) * 16 + glanes) * 2 + (stage_ready && stage ? 1 : 0);
+    return ((gblock_now() * 1024 + pblock_now()) * 16 + glanes_now()) * 2 + (stage_ready && stage ? 1 : 0);
   }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
@@ -183,7 +190,11 @@ struct wf_domain {
   bool shadows_valid = false;  // float shadows of the mixed form match the FP64 state
   long long launches_per_step = 0;     // launches every replay of the step graph makes
   long long search_launches = 0;       // launches in its conditional search body (0: gated form)
-  bool cond_ok = true;                 // conditional search capture works here (cleared on failure)
+  // Search in a graph conditional node (opt-in "search_conditional"): fewer
+  // launches on steps without a search, but ncu does not profile the kernel
+  // nodes of a graph that holds conditional nodes, so the gated form is the
+  // default.  Cleared when the capture fails on this device or driver.
+  bool cond_ok = false;
   cudaStream_t body_stream = nullptr;  // captures the conditional search body
   // Asynchronous read-back (wf_get_particle_array_f64_async): the field is
   // gathered on the domain's stream into a snapshot buffer, and the copy to
@@ -871,7 +882,7 @@ struct wf_domain {
     wf::DomainConst k = K;
     k.mixed = precision == WF_PRECISION_MIXED;
     k.gblock = gblock_now();
-    k.glanes = glanes;
+    k.glanes = glanes_now();
     k.pblock = pblock_now();
     k.nblocks = (int)((hp.N + k.pblock - 1) / k.pblock);
     k.stage_cap = stage_ready && stage ? stage_cap : 0;
@@ -1522,6 +1533,11 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     return WF_OK;
   }
   if (n == "use_graph") { d->use_graph = v != 0; return WF_OK; }
+  if (n == "search_conditional") {  // the step graph's search in a conditional IF node
+    d->cond_ok = v != 0;
+    if (d->graph) { cudaGraphExecDestroy(d->graph); d->graph = nullptr; }  // recapture at the next step
+    return WF_OK;
+  }
   if (n == "gather_block") {  // 0: by particle count
     if (v != 0 && v != 64 && v != 128 && v != 256 && v != 512)
       return set_err(WF_ERR_ARG, "gather_block must be 0, 64, 128, 256 or 512");
@@ -1624,7 +1640,8 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     if (n == "particle_count") { *v = d->hp.N; return WF_OK; }
     if (n == "solid_part_count") { *v = d->solid_part_count; return WF_OK; }
     if (n == "gather_block") { *v = d->gblock_now(); return WF_OK; }
-    if (n == "gather_lanes") { *v = d->glanes; return WF_OK; }
+    if (n == "gather_lanes") { *v = d->glanes_now(); return WF_OK; }
+    if (n == "search_conditional") { *v = d->cond_ok ? 1 : 0; return WF_OK; }
     if (n == "particle_block") { *v = d->pblock_now(); return WF_OK; }
     if (n == "gather_staging") { *v = d->stage ? 1 : 0; return WF_OK; }
     if (n == "stage_cap") { *v = d->stage_cap; return WF_OK; }

@@ -186,6 +186,45 @@ __device__ __forceinline__ void eig_sym3(const double s[6], double L[3], double 
   for (int k = 0; k < 3; ++k) L[k] = a[k][k];
 }
 
+// The same cyclic Jacobi iteration in FP32, for the mixed form, whose
+// tensile-instability stress enters the FP32 pair terms: converged to FP32
+// resolution (off-diagonal squares below 1e-14 of the diagonal's).  A rotation
+// angle beyond FP32 range takes t = 1 / (2 theta).
+__device__ __forceinline__ void eig_sym3f(const float s[6], float L[3], float V[3][3]) {
+  float a[3][3] = {{s[0], s[3], s[4]}, {s[3], s[1], s[5]}, {s[4], s[5], s[2]}};
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) V[r][c] = (r == c) ? 1.0f : 0.0f;
+  for (int sweep = 0; sweep < 20; ++sweep) {
+    float off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    float diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (off == 0.0f || off <= 1e-14f * diag) break;
+    for (int e = 0; e < 3; ++e) {
+      int p = e == 2 ? 1 : 0, q = e == 0 ? 1 : 2;
+      if (a[p][q] == 0.0f) continue;
+      float theta = (a[q][q] - a[p][p]) / (2.0f * a[p][q]);
+      float t = fabsf(theta) > 1e15f ? 0.5f / theta
+                                      : (theta >= 0.0f ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+      float c = rsqrtf(t * t + 1.0f), sn = t * c;
+      for (int k = 0; k < 3; ++k) {
+        float akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - sn * akq;
+        a[k][q] = sn * akp + c * akq;
+      }
+      for (int k = 0; k < 3; ++k) {
+        float apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - sn * aqk;
+        a[q][k] = sn * apk + c * aqk;
+      }
+      for (int k = 0; k < 3; ++k) {
+        float vkp = V[k][p], vkq = V[k][q];
+        V[k][p] = c * vkp - sn * vkq;
+        V[k][q] = sn * vkp + c * vkq;
+      }
+    }
+  }
+  for (int k = 0; k < 3; ++k) L[k] = a[k][k];
+}
+
 // Radial-return constitutive update of one particle, Particle::CalcStressStrain
 // (Source/Particle.cpp:960-1067), on symmetric storage (xx yy zz xy xz yz).
 // sr: strain rate (6), rr: rotation rate (xy xz yz of the antisymmetric part).

@@ -151,27 +151,40 @@ __device__ __forceinline__ PairGeo pair_geo(double xi0, double xi1, double xi2, 
 // ---------------------------------------------------------------- tensile instability
 // StartAcceleration's TIR (Domain.cpp:1557-1569): TIR = V diag(f(L)) V^T for
 // the eigen-decomposition of Sigma, f(l) = -TI l / rho^2 for l > 0, else 0;
-// products summed k = 2, 1, 0 as matvec.h's Mult.  Also fills the mixed
-// form's FP32 groups.
+// products summed k = 2, 1, 0 as matvec.h's Mult.  The mixed form, whose pair
+// terms read TIR in FP32, decomposes in FP32 (eig_sym3f): the FP64 Jacobi
+// sweeps' square roots and divisions would cost it more than its whole step
+// at 1M particles.  Also fills the mixed form's FP32 groups.
 __global__ void k_tensile(DevPtrs P, DomainConst K) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K.N) return;
   size_t N = K.N;
   double tir[6] = {0, 0, 0, 0, 0, 0};
   double ti = col(P, C_TI, N, i);
+  const int ui[6] = {0, 1, 2, 0, 0, 1}, uj[6] = {0, 1, 2, 1, 2, 2};
   if (icol(P, I_KIND, N, i) == 0 && ti > 0.0) {
     double rho = col(P, C_RHO, N, i);
     double rho2 = rho * rho;
     double pc = ti / (rho2);
-    double sg[6], L[3], V[3][3];
-    for (int c = 0; c < 6; ++c) sg[c] = col(P, C_SIG + c, N, i);
-    eig_sym3(sg, L, V);
-    double f[3];
-    for (int k = 0; k < 3; ++k) f[k] = (L[k] > 0) ? -pc * L[k] : 0.0;
-    const int ui[6] = {0, 1, 2, 0, 0, 1}, uj[6] = {0, 1, 2, 1, 2, 2};
-    for (int c = 0; c < 6; ++c) {
-      int a = ui[c], b = uj[c];
-      tir[c] = (V[a][2] * f[2]) * V[b][2] + (V[a][1] * f[1]) * V[b][1] + (V[a][0] * f[0]) * V[b][0];
+    if (K.mixed) {
+      float sg[6], L[3], V[3][3], f[3];
+      for (int c = 0; c < 6; ++c) sg[c] = (float)col(P, C_SIG + c, N, i);
+      eig_sym3f(sg, L, V);
+      for (int k = 0; k < 3; ++k) f[k] = (L[k] > 0.0f) ? -(float)pc * L[k] : 0.0f;
+      for (int c = 0; c < 6; ++c) {
+        int a = ui[c], b = uj[c];
+        tir[c] = (double)((V[a][2] * f[2]) * V[b][2] + (V[a][1] * f[1]) * V[b][1] + (V[a][0] * f[0]) * V[b][0]);
+      }
+    } else {
+      double sg[6], L[3], V[3][3];
+      for (int c = 0; c < 6; ++c) sg[c] = col(P, C_SIG + c, N, i);
+      eig_sym3(sg, L, V);
+      double f[3];
+      for (int k = 0; k < 3; ++k) f[k] = (L[k] > 0) ? -pc * L[k] : 0.0;
+      for (int c = 0; c < 6; ++c) {
+        int a = ui[c], b = uj[c];
+        tir[c] = (V[a][2] * f[2]) * V[b][2] + (V[a][1] * f[1]) * V[b][1] + (V[a][0] * f[0]) * V[b][0];
+      }
     }
   }
   for (int c = 0; c < 6; ++c) colw(P, C_TIR + c, N, i) = tir[c];
@@ -368,6 +381,7 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
   size_t N = K.N;
   double dt = P.st->deltat;  // the step's time step before AdaptiveTimeStep (prev_deltat)
   double cfsum = 0, crsum = 0, extw = 0;
+  unsigned ndyn = 0;       // pairs of this thread in the dynamic-friction branch
   double dta = 1.0 / 0.0;  // CheckMinTSAccel candidate (kick-drift, after contact)
   double cfv[NV][3];
   for (int m = 0; m < NV; ++m) cfv[m][0] = cfv[m][1] = cfv[m][2] = 0.0;
@@ -436,7 +450,7 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
             if (ntg < K.friction_sta * ncf) {
               for (int d = 0; d < 3; ++d) { double q = tg[d] / m1; cf[d] -= q; a[d] -= q; }
             } else {  // dynamic branch (Contact_Wang.cpp:284-290)
-              atomicAdd(&P.st->dyn_friction, 1ull);
+              ++ndyn;
               double fs = K.friction_dyn * ncf;
               for (int d = 0; d < 3; ++d) { double td = fs * tg[d] / ntg; cf[d] -= td; a[d] -= td / m1; }
             }
@@ -475,6 +489,10 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
     if (threadIdx.x == 0) P.partials[S_DTA * K.nblocks + blockIdx.x] = r;
   }
   if (CONTACT) {
+    // one counter update per warp (a per-pair atomic on one address serialised
+    // the kernel on contact-heavy steps)
+    unsigned wdyn = __reduce_add_sync(0xffffffffu, ndyn);
+    if ((threadIdx.x & 31) == 0 && wdyn) atomicAdd(&P.st->dyn_friction, (unsigned long long)wdyn);
     double r;
     r = block_reduce<0>(cfsum, sh); if (threadIdx.x == 0) P.partials[S_CFSUM * K.nblocks + blockIdx.x] = r;
     r = block_reduce<0>(crsum, sh); if (threadIdx.x == 0) P.partials[S_CRSUM * K.nblocks + blockIdx.x] = r;

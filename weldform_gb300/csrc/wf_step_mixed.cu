@@ -193,8 +193,7 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
   const float rhoi = UNI ? (float)col(P, C_RHO, N, i) : vh.w;
   float4 mi = AVU ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(ri + (size_t)RC_MISC * N);
   float4 t0 = make_float4(0.f, 0.f, 0.f, 0.f), t1 = t0;
-  float tii = 0.f;
-  if (TI) { t0 = ld4(ri + (size_t)RC_TI0 * N); t1 = ld4(ri + (size_t)RC_TI1 * N); tii = (float)col(P, C_TI, N, i); }
+  if (TI) { t0 = ld4(ri + (size_t)RC_TI0 * N); t1 = ld4(ri + (size_t)RC_TI1 * N); }
   CorrM cm;
   if (GC) cm = load_corr(P, N, i);
   int len = P.row_len[i];
@@ -233,14 +232,21 @@ __device__ __forceinline__ void accel_mx_sums(const DevPtrs& P, const DomainCons
     }
     float S0 = s0.x + js0.x + PIs, S1 = s0.y + js0.y + PIs, S2 = s0.z + js0.z + PIs;
     float S3 = s0.w + js0.w, S4 = s1.x + js1.x, S5 = s1.y + js1.y;
-    if (TI) {  // tensile instability (InteractionAlt.cpp:102-109); TIR = 0 where TI = 0
+    if (TI) {  // tensile instability (InteractionAlt.cpp:102-109)
+      // The reference adds the term when either end has TI > 0; TIR is zero
+      // where TI is, so adding it for every pair with a finite factor (w0 > 0,
+      // TIInitDist within the support) gives the same sums without reading
+      // TI_j.
       float4 jt0 = ld4(rj + (size_t)RC_TI0 * N), jt1 = ld4(rj + (size_t)RC_TI1 * N);
-      if (tii > 0.f || (float)col(P, C_TI, N, j) > 0.f) {
-        float q = r / hh, q0 = (t1.w + jt1.w) / (2.f * hh);
-        float wq = q < 1.f ? 1.f - 1.5f * q * q + 0.75f * q * q * q : (q < 2.f ? 0.25f * (2.f - q) * (2.f - q) * (2.f - q) : 0.f);
-        float w0 = q0 < 1.f ? 1.f - 1.5f * q0 * q0 + 0.75f * q0 * q0 * q0
-                            : (q0 < 2.f ? 0.25f * (2.f - q0) * (2.f - q0) * (2.f - q0) : 0.f);
-        float f = powf(wq / w0, 0.5f * (t1.z + jt1.z));
+      float q = r / hh, q0 = (t1.w + jt1.w) / (2.f * hh);
+      float wq = q < 1.f ? 1.f - 1.5f * q * q + 0.75f * q * q * q : (q < 2.f ? 0.25f * (2.f - q) * (2.f - q) * (2.f - q) : 0.f);
+      float w0 = q0 < 1.f ? 1.f - 1.5f * q0 * q0 + 0.75f * q0 * q0 * q0
+                          : (q0 < 2.f ? 0.25f * (2.f - q0) * (2.f - q0) * (2.f - q0) : 0.f);
+      if (w0 > 0.f) {
+        float fb = wq / w0, fn = 0.5f * (t1.z + jt1.z);
+        float f;
+        if (fn == 4.f) { f = fb * fb; f = f * f; }  // the JSON driver's TIn (WeldForm.cpp:901)
+        else f = powf(fb, fn);
         S0 += f * (t0.x + jt0.x); S1 += f * (t0.y + jt0.y); S2 += f * (t0.z + jt0.z);
         S3 += f * (t0.w + jt0.w); S4 += f * (t1.x + jt1.x); S5 += f * (t1.y + jt1.y);
       }
@@ -446,45 +452,52 @@ int configure_staging(int cap) {
 // ---------------------------------------------------------------- density + drift + kick
 // GC: the locking sum with corrected gradients, m_j (rho_i / rho_j) v_ij . vc_i
 // (InteractionAlt.cpp:589-605), which carries rho_i inside the sum.
+// The row sum of particle i over entries k0, k0 + dk, ... (the whole row for
+// dk = 1): (m_j / rho_j) v_ij . (GK x_ij), or with GC the locking form's
+// m_j (rho_i / rho_j) v_ij . vc_i; the compensated sum's value in FP64.
 template <bool GC, bool UNI>
-__device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainConst& K, int i) {
+__device__ __forceinline__ double density_sum_mx(const DevPtrs& P, const DomainConst& K, int i, int k0, int dk) {
+  size_t N = K.N;
+  const float4* ri = P.rc + i;
+  float4 xh = ld4(ri + (size_t)RC_XH * N), lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
+  float xl[3], vl[3];
+  lo_unpack(lo, xl, vl);
+  CorrM cm;
+  if (GC) cm = load_corr(P, N, i);
+  float rhoif = (float)col(P, C_RHO, N, i);
+  KSum s;
+  int len = P.row_len[i];
+  const int* nb = P.nbr + i;
+  for (int k = k0; k < len; k += dk) {
+    int j = nb_index(nb[(size_t)k * N]);
+    const float4* rj = P.rc + j;
+    float4 jxh = ld4(rj + (size_t)RC_XH * N), jlo = ld4(rj + (size_t)RC_L * N), jvh = ld4(rj + (size_t)RC_VH * N);
+    float jxl[3], jvl[3];
+    lo_unpack(jlo, jxl, jvl);
+    float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
+    float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
+    float r;
+    float GK = grad_kernel<UNI>(K, x0 * x0 + x1 * x1 + x2 * x2, UNI ? K.h_f : 0.5f * (xh.w + jxh.w), &r);
+    if (GC) {
+      float g0, g1, g2;
+      corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
+      s.add(jlo.w * rhoif * (v0 * g0 + v1 * g1 + v2 * g2));  // m_j (rho_i / rho_j) = (m_j / rho_j) rho_i
+    } else {
+      s.add(jlo.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
+    }
+  }
+  return s.value();
+}
+// The rest of the pass for particle i from its row sum: density rate and
+// update, drift, the next-step record.
+template <bool GC, bool UNI>
+__device__ __forceinline__ void density_drift_end_mx(const DevPtrs& P, const DomainConst& K, int i, double sum) {
   size_t N = K.N;
   double dt = P.st->deltat;
   double rhoi = col(P, C_RHO, N, i);
-  double dd = 0.0;
   bool solid = icol(P, I_KIND, N, i) == 0;
   const float4* ri = P.rc + i;
-  float4 xh = ld4(ri + (size_t)RC_XH * N);
-  if (solid) {
-    float4 lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
-    float xl[3], vl[3];
-    lo_unpack(lo, xl, vl);
-    CorrM cm;
-    if (GC) cm = load_corr(P, N, i);
-    float rhoif = (float)rhoi;
-    KSum s;
-    int len = P.row_len[i];
-    const int* nb = P.nbr + i;
-    for (int k = 0; k < len; ++k) {
-      int j = nb_index(nb[(size_t)k * N]);
-      const float4* rj = P.rc + j;
-      float4 jxh = ld4(rj + (size_t)RC_XH * N), jlo = ld4(rj + (size_t)RC_L * N), jvh = ld4(rj + (size_t)RC_VH * N);
-      float jxl[3], jvl[3];
-      lo_unpack(jlo, jxl, jvl);
-      float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
-      float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
-      float r;
-      float GK = grad_kernel<UNI>(K, x0 * x0 + x1 * x1 + x2 * x2, UNI ? K.h_f : 0.5f * (xh.w + jxh.w), &r);
-      if (GC) {
-        float g0, g1, g2;
-        corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
-        s.add(jlo.w * rhoif * (v0 * g0 + v1 * g1 + v2 * g2));  // m_j (rho_i / rho_j) = (m_j / rho_j) rho_i
-      } else {
-        s.add(jlo.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
-      }
-    }
-    dd = GC ? s.value() : s.value() * rhoi;
-  }
+  double dd = solid ? (GC ? sum : sum * rhoi) : 0.0;
   colw(P, C_DRHO, N, i) = dd;
   double rn = rhoi + dt * dd;
   colw(P, C_RHON, N, i) = rn;
@@ -512,7 +525,7 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   float th, tl;
   ff_split(Tn, th, tl);
   float4* r = P.rn + i;
-  r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], UNI ? K.h_f : xh.w);
+  r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], UNI ? K.h_f : ld4(ri + (size_t)RC_XH * N).w);
   r[(size_t)RN_L * N] = lo_pack(nxl, nvl, (float)mrn);
   float pr2 = solid ? (float)(pn * irn * irn) : 0.f;
   r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], pr2);  // the rate gather reads p/rho^2 here
@@ -520,7 +533,23 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
 }
 template <bool GC, bool UNI>
 __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { density_drift_mx<GC, UNI>(P, K, i); });
+  run_rows(K, [&](int i) {
+    double sum = icol(P, I_KIND, K.N, i) == 0 ? density_sum_mx<GC, UNI>(P, K, i, 0, 1) : 0.0;
+    density_drift_end_mx<GC, UNI>(P, K, i, sum);
+  });
+}
+// L lanes per particle, as the acceleration gather's lanes: lane s sums
+// entries s, s + L, ...; the partial sums are added in FP64 by a butterfly of
+// warp shuffles and lane 0 finishes the particle.
+template <bool GC, bool UNI, int L>
+__global__ void __launch_bounds__(512) k_density_drift_mx_lanes(DevPtrs P, DomainConst K) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t / L), sub = (int)(t % L);
+  const bool live = i < K.N;
+  const bool solid = live && icol(P, I_KIND, K.N, i) == 0;
+  double sum = solid ? density_sum_mx<GC, UNI>(P, K, i, sub, L) : 0.0;
+  for (int off = 1; off < L; off <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);  // L divides 32
+  if (live && sub == 0) density_drift_end_mx<GC, UNI>(P, K, i, sum);
 }
 
 // ---------------------------------------------------------------- rates + energy + conduction
@@ -529,12 +558,19 @@ __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainCo
 // GC: rates and conduction with corrected gradients (InteractionAlt.cpp:330-350,
 // 425-450; Thermal.cpp:90-107), weights (float)(m_j / rho_j); the kinetic-energy
 // pair term keeps the plain gradient, as the reference's.
-template <bool THERMAL, bool GC, bool UNI>
-__device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i) {
+// L lanes per particle (L = 1: one thread walks the row): lane `sub` sums
+// entries sub, sub + L, ...; with L > 1 the lanes' compensated values are
+// added in FP64 by a butterfly of warp shuffles (every thread of the warp
+// takes part, so the caller runs this for out-of-range threads too, with
+// live = false) and lane 0 writes the particle.
+template <bool THERMAL, bool GC, bool UNI, int L>
+__device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, int i, int sub, bool live) {
   size_t N = K.N;
   float out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   double dkin = 0.0, cond = 0.0;
-  if (icol(P, I_KIND, N, i) == 0) {
+  const bool sph = live && icol(P, I_KIND, N, i) == 0;
+  double md[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // L > 1: the lane's compensated values
+  if (sph) {
     const float4* ri = P.rn + i;
     float4 xh = ld4(ri + (size_t)RN_XH * N), lo = ld4(ri + (size_t)RN_L * N), vh = ld4(ri + (size_t)RN_VH * N);
     float xl[3], vl[3];
@@ -547,7 +583,7 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
     const float mass_i = (float)col(P, C_MASS, N, i);
     int len = P.row_len[i];
     const int* nb = P.nbr + i;
-    for (int k = 0; k < len; ++k) {
+    for (int k = sub; k < len; k += L) {
       int ent = nb[(size_t)k * N];
       int j = nb_index(ent);
       const float4* rj = P.rn + j;
@@ -584,23 +620,48 @@ __device__ __forceinline__ void rate_mx(const DevPtrs& P, const DomainConst& K, 
         cnd.add(wt * 4.f * (e.y * je.y) / (e.y + je.y) * dT * gr);
       }
     }
-    // The rate columns are FP32: each compensated sum is rounded to FP32 once
-    // (s - c) and combined in FP32, which keeps the epilogue off the FP64 pipe.
-    float m[9];
-    for (int c = 0; c < 9; ++c) m[c] = M[c].s - M[c].c;
-    out[0] = 2.0f * m[0]; out[1] = 2.0f * m[4]; out[2] = 2.0f * m[8];
-    out[3] = m[1] + m[3]; out[4] = m[2] + m[6]; out[5] = m[5] + m[7];
-    out[6] = m[1] - m[3]; out[7] = m[2] - m[6]; out[8] = m[5] - m[7];
+    if constexpr (L == 1) {
+      // The rate columns are FP32: each compensated sum is rounded to FP32 once
+      // (s - c) and combined in FP32, which keeps the epilogue off the FP64 pipe.
+      float m[9];
+      for (int c = 0; c < 9; ++c) m[c] = M[c].s - M[c].c;
+      out[0] = 2.0f * m[0]; out[1] = 2.0f * m[4]; out[2] = 2.0f * m[8];
+      out[3] = m[1] + m[3]; out[4] = m[2] + m[6]; out[5] = m[5] + m[7];
+      out[6] = m[1] - m[3]; out[7] = m[2] - m[6]; out[8] = m[5] - m[7];
+    } else {
+      for (int c = 0; c < 9; ++c) md[c] = M[c].value();
+    }
     dkin = kin.value();
     cond = cnd.value();
   }
+  if constexpr (L > 1) {
+    for (int off = 1; off < L; off <<= 1) {  // L divides 32
+      for (int c = 0; c < 9; ++c) md[c] += __shfl_xor_sync(0xffffffffu, md[c], off);
+      dkin += __shfl_xor_sync(0xffffffffu, dkin, off);
+      if (THERMAL) cond += __shfl_xor_sync(0xffffffffu, cond, off);
+    }
+    if (sph) {
+      float m[9];
+      for (int c = 0; c < 9; ++c) m[c] = (float)md[c];
+      out[0] = 2.0f * m[0]; out[1] = 2.0f * m[4]; out[2] = 2.0f * m[8];
+      out[3] = m[1] + m[3]; out[4] = m[2] + m[6]; out[5] = m[5] + m[7];
+      out[6] = m[1] - m[3]; out[7] = m[2] - m[6]; out[8] = m[5] - m[7];
+    }
+  }
+  if (!live || sub != 0) return;
   for (int c = 0; c < 9; ++c) P.rates[(size_t)c * N + i] = out[c];
   colw(P, C_DKIN, N, i) = dkin;
   colw(P, C_DINT, N, i) = cond;  // conduction sum, consumed by k_stress_mx
 }
 template <bool THERMAL, bool GC, bool UNI>
 __global__ void __launch_bounds__(512) k_rate_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) { rate_mx<THERMAL, GC, UNI>(P, K, i); });
+  run_rows(K, [&](int i) { rate_mx<THERMAL, GC, UNI, 1>(P, K, i, 0, true); });
+}
+template <bool THERMAL, bool GC, bool UNI, int L>
+__global__ void __launch_bounds__(512) k_rate_mx_lanes(DevPtrs P, DomainConst K) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t / L);
+  rate_mx<THERMAL, GC, UNI, L>(P, K, i, (int)(t % L), i < K.N);
 }
 
 // ---------------------------------------------------------------- elementwise update
@@ -821,6 +882,27 @@ static void launch_accel_mx_u(const DevPtrs& P, const DomainConst& K, int ng, in
     default: k_accel_mx<TI, AVU, GC, UNI><<<ng, gb, 0, s>>>(P, K);
   }
 }
+// The density and rate gathers with the acceleration gather's lanes per particle.
+template <bool GC, bool UNI>
+static void launch_density_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
+  auto grid = [&](int L) { return (int)(((long long)K.N * L + gb - 1) / gb); };
+  switch (K.glanes) {
+    case 2: k_density_drift_mx_lanes<GC, UNI, 2><<<grid(2), gb, 0, s>>>(P, K); break;
+    case 4: k_density_drift_mx_lanes<GC, UNI, 4><<<grid(4), gb, 0, s>>>(P, K); break;
+    case 8: k_density_drift_mx_lanes<GC, UNI, 8><<<grid(8), gb, 0, s>>>(P, K); break;
+    default: k_density_drift_mx<GC, UNI><<<ng, gb, 0, s>>>(P, K);
+  }
+}
+template <bool THERMAL, bool GC, bool UNI>
+static void launch_rate_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
+  auto grid = [&](int L) { return (int)(((long long)K.N * L + gb - 1) / gb); };
+  switch (K.glanes) {
+    case 2: k_rate_mx_lanes<THERMAL, GC, UNI, 2><<<grid(2), gb, 0, s>>>(P, K); break;
+    case 4: k_rate_mx_lanes<THERMAL, GC, UNI, 4><<<grid(4), gb, 0, s>>>(P, K); break;
+    case 8: k_rate_mx_lanes<THERMAL, GC, UNI, 8><<<grid(8), gb, 0, s>>>(P, K); break;
+    default: k_rate_mx<THERMAL, GC, UNI><<<ng, gb, 0, s>>>(P, K);
+  }
+}
 template <bool TI, bool AVU>
 static void launch_accel_mx(const DevPtrs& P, const DomainConst& K, int ng, int gb, cudaStream_t s) {
   if (K.gradcorr) {
@@ -853,20 +935,20 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   launch_contact_kick(P, K, s);
   launch_bc(P, K, C_V, s);
   if (K.gradcorr) {
-    if (K.uni) k_density_drift_mx<true, true><<<ng, gb, 0, s>>>(P, K);
-    else k_density_drift_mx<true, false><<<ng, gb, 0, s>>>(P, K);
+    if (K.uni) launch_density_mx<true, true>(P, K, ng, gb, s);
+    else launch_density_mx<true, false>(P, K, ng, gb, s);
   } else {
-    if (K.uni) k_density_drift_mx<false, true><<<ng, gb, 0, s>>>(P, K);
-    else k_density_drift_mx<false, false><<<ng, gb, 0, s>>>(P, K);
+    if (K.uni) launch_density_mx<false, true>(P, K, ng, gb, s);
+    else launch_density_mx<false, false>(P, K, ng, gb, s);
   }
   mark(s, "k_density_drift_mx");
   launch_bc(P, K, C_VN, s);
   if (K.thermal_solver) {
-    if (K.gradcorr) { if (K.uni) k_rate_mx<true, true, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<true, true, false><<<ng, gb, 0, s>>>(P, K); }
-    else { if (K.uni) k_rate_mx<true, false, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<true, false, false><<<ng, gb, 0, s>>>(P, K); }
+    if (K.gradcorr) { if (K.uni) launch_rate_mx<true, true, true>(P, K, ng, gb, s); else launch_rate_mx<true, true, false>(P, K, ng, gb, s); }
+    else { if (K.uni) launch_rate_mx<true, false, true>(P, K, ng, gb, s); else launch_rate_mx<true, false, false>(P, K, ng, gb, s); }
   } else {
-    if (K.gradcorr) { if (K.uni) k_rate_mx<false, true, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<false, true, false><<<ng, gb, 0, s>>>(P, K); }
-    else { if (K.uni) k_rate_mx<false, false, true><<<ng, gb, 0, s>>>(P, K); else k_rate_mx<false, false, false><<<ng, gb, 0, s>>>(P, K); }
+    if (K.gradcorr) { if (K.uni) launch_rate_mx<false, true, true>(P, K, ng, gb, s); else launch_rate_mx<false, true, false>(P, K, ng, gb, s); }
+    else { if (K.uni) launch_rate_mx<false, false, true>(P, K, ng, gb, s); else launch_rate_mx<false, false, false>(P, K, ng, gb, s); }
   }
   mark(s, "k_rate_mx");
   if (K.pl_heating) {
