@@ -452,52 +452,56 @@ int configure_staging(int cap) {
 // ---------------------------------------------------------------- density + drift + kick
 // GC: the locking sum with corrected gradients, m_j (rho_i / rho_j) v_ij . vc_i
 // (InteractionAlt.cpp:589-605), which carries rho_i inside the sum.
-// The row sum of particle i over entries k0, k0 + dk, ... (the whole row for
-// dk = 1): (m_j / rho_j) v_ij . (GK x_ij), or with GC the locking form's
-// m_j (rho_i / rho_j) v_ij . vc_i; the compensated sum's value in FP64.
-template <bool GC, bool UNI>
-__device__ __forceinline__ double density_sum_mx(const DevPtrs& P, const DomainConst& K, int i, int k0, int dk) {
-  size_t N = K.N;
-  const float4* ri = P.rc + i;
-  float4 xh = ld4(ri + (size_t)RC_XH * N), lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
-  float xl[3], vl[3];
-  lo_unpack(lo, xl, vl);
-  CorrM cm;
-  if (GC) cm = load_corr(P, N, i);
-  float rhoif = (float)col(P, C_RHO, N, i);
-  KSum s;
-  int len = P.row_len[i];
-  const int* nb = P.nbr + i;
-  for (int k = k0; k < len; k += dk) {
-    int j = nb_index(nb[(size_t)k * N]);
-    const float4* rj = P.rc + j;
-    float4 jxh = ld4(rj + (size_t)RC_XH * N), jlo = ld4(rj + (size_t)RC_L * N), jvh = ld4(rj + (size_t)RC_VH * N);
-    float jxl[3], jvl[3];
-    lo_unpack(jlo, jxl, jvl);
-    float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
-    float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
-    float r;
-    float GK = grad_kernel<UNI>(K, x0 * x0 + x1 * x1 + x2 * x2, UNI ? K.h_f : 0.5f * (xh.w + jxh.w), &r);
-    if (GC) {
-      float g0, g1, g2;
-      corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
-      s.add(jlo.w * rhoif * (v0 * g0 + v1 * g1 + v2 * g2));  // m_j (rho_i / rho_j) = (m_j / rho_j) rho_i
-    } else {
-      s.add(jlo.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
-    }
-  }
-  return s.value();
-}
-// The rest of the pass for particle i from its row sum: density rate and
-// update, drift, the next-step record.
-template <bool GC, bool UNI>
-__device__ __forceinline__ void density_drift_end_mx(const DevPtrs& P, const DomainConst& K, int i, double sum) {
+// L lanes per particle (L = 1: one thread walks the row): lane `sub` sums
+// entries sub, sub + L, ...; with L > 1 the lanes' compensated values are
+// added in FP64 by a butterfly of warp shuffles (every thread of the warp
+// takes part, so the caller runs this for out-of-range threads too, with
+// live = false) and lane 0 finishes the particle.
+// GC: the locking sum with corrected gradients, m_j (rho_i / rho_j) v_ij . vc_i
+// (InteractionAlt.cpp:589-605), which carries rho_i inside the sum.
+template <bool GC, bool UNI, int L>
+__device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainConst& K, int i, int sub, bool live) {
   size_t N = K.N;
   double dt = P.st->deltat;
-  double rhoi = col(P, C_RHO, N, i);
-  bool solid = icol(P, I_KIND, N, i) == 0;
+  double rhoi = live ? col(P, C_RHO, N, i) : 0.0;
+  double dd = 0.0;
+  bool solid = live && icol(P, I_KIND, N, i) == 0;
   const float4* ri = P.rc + i;
-  double dd = solid ? (GC ? sum : sum * rhoi) : 0.0;
+  float4 xh = live ? ld4(ri + (size_t)RC_XH * N) : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (solid) {
+    float4 lo = ld4(ri + (size_t)RC_L * N), vh = ld4(ri + (size_t)RC_VH * N);
+    float xl[3], vl[3];
+    lo_unpack(lo, xl, vl);
+    CorrM cm;
+    if (GC) cm = load_corr(P, N, i);
+    float rhoif = (float)rhoi;
+    KSum s;
+    int len = P.row_len[i];
+    const int* nb = P.nbr + i;
+    for (int k = sub; k < len; k += L) {
+      int j = nb_index(nb[(size_t)k * N]);
+      const float4* rj = P.rc + j;
+      float4 jxh = ld4(rj + (size_t)RC_XH * N), jlo = ld4(rj + (size_t)RC_L * N), jvh = ld4(rj + (size_t)RC_VH * N);
+      float jxl[3], jvl[3];
+      lo_unpack(jlo, jxl, jvl);
+      float x0 = (xh.x - jxh.x) + (xl[0] - jxl[0]), x1 = (xh.y - jxh.y) + (xl[1] - jxl[1]), x2 = (xh.z - jxh.z) + (xl[2] - jxl[2]);
+      float v0 = (vh.x - jvh.x) + (vl[0] - jvl[0]), v1 = (vh.y - jvh.y) + (vl[1] - jvl[1]), v2 = (vh.z - jvh.z) + (vl[2] - jvl[2]);
+      float r;
+      float GK = grad_kernel<UNI>(K, x0 * x0 + x1 * x1 + x2 * x2, UNI ? K.h_f : 0.5f * (xh.w + jxh.w), &r);
+      if (GC) {
+        float g0, g1, g2;
+        corr_gk(cm, GK, x0, x1, x2, g0, g1, g2);
+        s.add(jlo.w * rhoif * (v0 * g0 + v1 * g1 + v2 * g2));  // m_j (rho_i / rho_j) = (m_j / rho_j) rho_i
+      } else {
+        s.add(jlo.w * (GK * (v0 * x0 + v1 * x1 + v2 * x2)));  // (m_j / rho_j) v_ij . (GK x_ij)
+      }
+    }
+    dd = s.value();
+  }
+  if constexpr (L > 1)
+    for (int off = 1; off < L; off <<= 1) dd += __shfl_xor_sync(0xffffffffu, dd, off);  // L divides 32
+  if (!live || sub != 0) return;
+  if (solid && !GC) dd *= rhoi;
   colw(P, C_DRHO, N, i) = dd;
   double rn = rhoi + dt * dd;
   colw(P, C_RHON, N, i) = rn;
@@ -525,7 +529,7 @@ __device__ __forceinline__ void density_drift_end_mx(const DevPtrs& P, const Dom
   float th, tl;
   ff_split(Tn, th, tl);
   float4* r = P.rn + i;
-  r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], UNI ? K.h_f : ld4(ri + (size_t)RC_XH * N).w);
+  r[(size_t)RN_XH * N] = make_float4(nxh[0], nxh[1], nxh[2], UNI ? K.h_f : xh.w);
   r[(size_t)RN_L * N] = lo_pack(nxl, nvl, (float)mrn);
   float pr2 = solid ? (float)(pn * irn * irn) : 0.f;
   r[(size_t)RN_VH * N] = make_float4(nvh[0], nvh[1], nvh[2], pr2);  // the rate gather reads p/rho^2 here
@@ -533,23 +537,13 @@ __device__ __forceinline__ void density_drift_end_mx(const DevPtrs& P, const Dom
 }
 template <bool GC, bool UNI>
 __global__ void __launch_bounds__(512, 3) k_density_drift_mx(DevPtrs P, DomainConst K) {
-  run_rows(K, [&](int i) {
-    double sum = icol(P, I_KIND, K.N, i) == 0 ? density_sum_mx<GC, UNI>(P, K, i, 0, 1) : 0.0;
-    density_drift_end_mx<GC, UNI>(P, K, i, sum);
-  });
+  run_rows(K, [&](int i) { density_drift_mx<GC, UNI, 1>(P, K, i, 0, true); });
 }
-// L lanes per particle, as the acceleration gather's lanes: lane s sums
-// entries s, s + L, ...; the partial sums are added in FP64 by a butterfly of
-// warp shuffles and lane 0 finishes the particle.
 template <bool GC, bool UNI, int L>
 __global__ void __launch_bounds__(512) k_density_drift_mx_lanes(DevPtrs P, DomainConst K) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = (int)(t / L), sub = (int)(t % L);
-  const bool live = i < K.N;
-  const bool solid = live && icol(P, I_KIND, K.N, i) == 0;
-  double sum = solid ? density_sum_mx<GC, UNI>(P, K, i, sub, L) : 0.0;
-  for (int off = 1; off < L; off <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);  // L divides 32
-  if (live && sub == 0) density_drift_end_mx<GC, UNI>(P, K, i, sum);
+  const int i = (int)(t / L);
+  density_drift_mx<GC, UNI, L>(P, K, i, (int)(t % L), i < K.N);
 }
 
 // ---------------------------------------------------------------- rates + energy + conduction
