@@ -106,8 +106,9 @@ int wf_domain_destroy(wf_domain* d);
  * "gather_block" (threads per block of the mixed form's gathers: 64, 128,
  * 256 or 512), "gather_lanes" (lanes per particle of the mixed acceleration
  * gather: 1, 2, 4 or 8; the lanes walk one row and combine their Kahan
- * partials by warp shuffles; by default 8 below 20,000 particles, 4 below
- * 60,000, else 1), "gather_staging" (1: the mixed acceleration gather reads each
+ * partials by warp shuffles; the density and rate gathers use the same
+ * lanes; by default 8 below 20,000 particles, 4 below 40,000, 2 below
+ * 64,000, else 1), "gather_staging" (1: the mixed acceleration gather reads each
  * 128-particle block's neighbours from a shared-memory copy of their records,
  * built at every search; set before the prologue, default 0) and
  * "stage_cap" (its halo capacity per block, 64..1024, default 896, before

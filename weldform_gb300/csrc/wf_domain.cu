@@ -175,10 +175,10 @@ struct wf_domain {
   int gblock_now() const { return gblock ? gblock : auto_block(hp.N); }
   // Below ~60k particles a gather's time is its rows' chain of dependent
   // loads (one thread walks ~55 entries), not throughput: splitting each
-  // row over 4 or 8 lanes shortens the chain (measured on GB300: 8,004
-  // particles 32 -> 12 us for the acceleration gather with 8 lanes, 29,520
-  // particles 34 -> 19 us with 4; from ~100k on one lane is as fast).
-  static int auto_lanes(long long n) { return n < 20000 ? 8 : (n < 60000 ? 4 : 1); }
+  // row over lanes shortens the chain (measured on GB300, mixed step:
+  // 8,004 particles best with 8 lanes, 29,520 with 4, 44,880 with 2 (135
+  // against 142 us), 79,856 and up with 1).
+  static int auto_lanes(long long n) { return n < 20000 ? 8 : (n < 40000 ? 4 : (n < 64000 ? 2 : 1)); }
   int glanes_now() const { return glanes ? glanes : auto_lanes(hp.N); }
   int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
   int graph_key() const {
