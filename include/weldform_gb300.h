@@ -295,8 +295,8 @@ int wf_checkpoint_restore(wf_domain* d, int slot);
 int wf_checkpoint_free(wf_domain* d, int slot);
 
 /* Chooses the launch shape of the mixed form's gather kernels — threads per
- * block (64, 128, 256 or 512) and lanes per particle of the acceleration
- * gather (1, 2 or 4) — by timing `steps` steps with every pair from a
+ * block (64, 128, 256 or 512) and lanes per particle of the gathers (1, 2,
+ * 4 or 8) — by timing `steps` steps with every pair from a
  * checkpoint of the current state, restores that state, keeps the fastest and
  * returns its block size; results are cached per size bucket (particles
  * rounded up to a power of two) for later domains in the process.  The choice

@@ -1320,7 +1320,7 @@ struct wf_domain {
     checkpoint_save(slot);
     int best = 256, best_lanes = 1;
     double best_ms = 1e300;
-    for (int lanes : {1, 2, 4})
+    for (int lanes : {1, 2, 4, 8})
       for (int b : {64, 128, 256, 512}) {
         gblock = b;
         glanes = lanes;
