@@ -3,7 +3,8 @@
 // Same step, same reference semantics as the plain form (wf_step_fp64.cu);
 // what changes is how the pair gathers compute and what they read:
 //  * the FP32 gather data sits in float4 field-group columns (group q of
-//    particle i at rc[q*N + i]), so a neighbour costs six 16-byte loads that
+//    particle i at rc[q*N + i]), so a neighbour costs four 16-byte loads
+//    (five when h, mass or Cs differ between the particles of a pair) that
 //    coalesce across the warp's consecutive particles, instead of one scalar
 //    load from each of ~20 separate columns;
 //  * relative positions, velocities and temperatures come from float-float
@@ -21,6 +22,8 @@
 // Three gathers per step: acceleration; density (+ drift and second kick);
 // rate tensors fused with the kinetic-energy and conduction sums, which use
 // the same positions, velocities and the pressure of the updated density.
+// Each walks a particle's row with one thread, or on small domains with
+// 2-8 lanes whose partial sums are combined by warp shuffles.
 #include "wf_step_common.cuh"
 #include "wf_launch.h"
 
