@@ -9,20 +9,26 @@
 //   3. k_scatter + k_sort_cells — counting-sort scatter, then each cell's slots
 //                      ordered by original particle index (deterministic order).
 //   4. k_permute / k_copy_back — every persistent state column reordered.
-//   5. k_nbr_fill    — one thread per particle scans the 27 neighbouring cells,
+//   5. k_nbr_fill    — one warp per particle scans the 27 neighbouring cells,
 //                      applies the reference pair rules (AllocateNbPair,
 //                      Neighbour.cpp:374-417: contact-surface pairs, radius test
 //                      CheckRadius :361-372, free + same material) and writes its
 //                      row in canonical order (j > i ascending, then j < i
 //                      ascending by original index) into an ELL array
 //                      (entry k of particle i at k * N + i).
+// With the Verlet-skin reuse, a full search (steps 1-5) also builds each
+// particle's superset over a 5 x 5 x 5 stencil at the pair radius plus the
+// skin (k_nbr_fill<true>), and a later search whose particles all moved less
+// than half the skin skips steps 1-5 and filters the supersets with the same
+// exact rules (k_skin_check, k_search_mode, k_cell_coords, k_nbr_filter).
 // The radius test rij / h <= Cellfac is decided bit-exactly: an FP32 distance
 // prefilter with a proven-safe relative margin accepts or rejects clear cases,
 // and everything inside the margin is decided by the reference's FP64
 // expression evaluated with non-contracted IEEE operations.
 //
-// Every kernel checks st->do_search first, so the search can sit inside a
-// captured step and cost only an empty launch on steps that do not rebuild.
+// Every kernel checks st->do_search first (the re-sorting ones also
+// search_full), so the search can sit inside a captured step and cost only
+// an empty launch on steps that do not rebuild.
 #include "wf_device.cuh"
 #include "wf_launch.h"
 
