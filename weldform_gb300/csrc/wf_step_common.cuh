@@ -113,6 +113,33 @@ __device__ __forceinline__ double amp_value(const DomainTables* T, int amp_id, d
   return 0.0;
 }
 
+// The velocity the BCs of zone id impose at time t (GeneralAfter,
+// WeldForm.cpp:51-120): each of the zone's BCs in the order added, a later one
+// overriding an earlier; an amplitude BC applies only where its table covers
+// t.  False when none applies.  k_bc applies this to its list of BC
+// particles; the kick and drift kernels apply it to their own particle in
+// place of the BC passes that would follow them.
+__device__ __forceinline__ bool bc_velocity(const DomainTables* T, int id, double t, double v[3]) {
+  int lo, hi;
+  bc_range(T, id, lo, hi);
+  bool hit = false;
+  for (int r = lo; r < hi; ++r) {
+    const BCDev& b = T->bc[T->bc_order[r]];
+    if (b.value_type == 0) {
+      hit = true;
+      for (int d = 0; d < 3; ++d) v[d] = b.value[d];
+    } else {
+      bool found = false;
+      double val = b.amp_factor * amp_value(T, b.amp_id, t, &found);
+      if (found) {
+        hit = true;
+        for (int d = 0; d < 3; ++d) v[d] = val * b.value[d];
+      }
+    }
+  }
+  return hit;
+}
+
 // CalcConvHeat (Thermal.cpp:339-389, 3D; Fraser Eq. 3-121): a particle with
 // Thermal_BC == TH_BC_CONVECTION exchanges heat with the ambient temperature
 // T_inf through its contact area dS^2 = (m / rho)^(2/3):

@@ -350,20 +350,9 @@ __global__ void k_bc(DevPtrs P, DomainConst K, int vcol) {
   if (k >= K.nbc_particles) return;
   size_t N = K.N;
   int i = P.inv[P.bc_list[k]];
-  int id = icol(P, I_ID, N, i);
-  int lo, hi;
-  bc_range(T, id, lo, hi);
-  for (int r = lo; r < hi; ++r) {
-    const int b = T->bc_order[r];
-    if (T->bc[b].value_type == 0) {
-      for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = T->bc[b].value[d]; }
-    } else {
-      bool found = false;
-      double val = T->bc[b].amp_factor * amp_value(T, T->bc[b].amp_id, t, &found);
-      if (found)
-        for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = val * T->bc[b].value[d]; }
-    }
-  }
+  double vb[3];
+  if (bc_velocity(T, icol(P, I_ID, N, i), t, vb))
+    for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, vcol + d, N, i) = vb[d]; }
   if (K.mixed)  // keep the float-float velocity in the records in step with the FP64 value
     for (int d = 0; d < 3; ++d) rec_set_v(P, N, i, d, col(P, vcol + d, N, i), vcol == C_VN);
 }
@@ -486,6 +475,15 @@ __global__ void __launch_bounds__(BLOCK) k_contact_kick(DevPtrs P, DomainConst K
       }
       if (K.mixed) rec_set_v3(P, N, i, vn);
     }
+    // GeneralAfter after the kick (SolverKickDrift.cpp:231) on this particle,
+    // in place of a BC pass: it depends on no other particle, and a rigid-mesh
+    // particle another thread reads here keeps the velocity the pass before
+    // the contact gave it.
+    double vb[3];
+    if (!K.leapfrog && bc_velocity(P.tab, icol(P, I_ID, N, i), P.st->Time, vb)) {
+      for (int d = 0; d < 3; ++d) { colw(P, C_A + d, N, i) = 0.0; colw(P, C_V + d, N, i) = vb[d]; }
+      if (K.mixed) rec_set_v3(P, N, i, vb);
+    }
   }
   if (K.auto_ts_acc && !K.leapfrog) {
     double r = block_reduce<2>(dta, sh);
@@ -557,11 +555,16 @@ __global__ void __launch_bounds__(BLOCK) k_density_drift(DevPtrs P, DomainConst 
     if (K.thermal_solver) colw(P, C_TN, N, i) = col(P, C_T, N, i) + dt * col(P, C_DTDT, N, i);
   }
   double v[3] = {vi0, vi1, vi2}, x[3] = {xi0, xi1, xi2};
+  // GeneralAfter on the next-step velocity (SolverKickDrift.cpp:267) applied
+  // here instead of in a BC pass after this kernel
+  double vb[3];
+  const bool bc = bc_velocity(P.tab, icol(P, I_ID, N, i), P.st->Time, vb);
   for (int d = 0; d < 3; ++d) {
     double du = v[d] * dt;
     colw(P, C_DISP + d, N, i) = col(P, C_DISP + d, N, i) + du;
     colw(P, C_XN + d, N, i) = x[d] + du;
-    colw(P, C_VN + d, N, i) = K.leapfrog ? v[d] : v[d] + col(P, C_A + d, N, i) * dt / 2.;
+    colw(P, C_VN + d, N, i) = bc ? vb[d] : (K.leapfrog ? v[d] : v[d] + col(P, C_A + d, N, i) * dt / 2.);
+    if (bc) colw(P, C_A + d, N, i) = 0.0;
   }
 }
 
@@ -1085,10 +1088,9 @@ void launch_step_fp64_body(const DevPtrs& P, const DomainConst& K, cudaStream_t 
   mark(s, "k_accel");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
-  launch_bc(P, K, C_V, s);
-  k_density_drift<<<nb, K.pblock, 0, s>>>(P, K);
+  if (K.leapfrog) launch_bc(P, K, C_V, s);  // kick-drift: applied by the kick kernel
+  k_density_drift<<<nb, K.pblock, 0, s>>>(P, K);  // and the next-step BC by this one
   mark(s, "k_density_drift");
-  launch_bc(P, K, C_VN, s);
   k_rate_stress<<<nb, K.pblock, 0, s>>>(P, K);
   mark(s, "k_rate_stress");
   launch_step_tail(P, K, s);

@@ -512,12 +512,17 @@ __device__ __forceinline__ void density_drift_mx(const DevPtrs& P, const DomainC
   double mrn = solid ? col(P, C_MASS, N, i) * irn : 0.0;
   colw(P, C_MRHON, N, i) = mrn;
   float nxh[3], nxl[3], nvh[3], nvl[3];
+  // GeneralAfter on the next-step velocity (SolverKickDrift.cpp:267) applied
+  // here, records included, instead of in a BC pass after this kernel
+  double vb[3];
+  const bool bc = bc_velocity(P.tab, icol(P, I_ID, N, i), P.st->Time, vb);
   for (int d = 0; d < 3; ++d) {
     double v = col(P, C_V + d, N, i);
     double du = v * dt;
     colw(P, C_DISP + d, N, i) = col(P, C_DISP + d, N, i) + du;
     double xn = col(P, C_X + d, N, i) + du;
-    double vn = K.leapfrog ? v : v + col(P, C_A + d, N, i) * dt / 2.;
+    double vn = bc ? vb[d] : (K.leapfrog ? v : v + col(P, C_A + d, N, i) * dt / 2.);
+    if (bc) colw(P, C_A + d, N, i) = 0.0;
     colw(P, C_XN + d, N, i) = xn;
     colw(P, C_VN + d, N, i) = vn;
     ff_split(xn - K.rec_origin[d], nxh[d], nxl[d]);
@@ -930,7 +935,7 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
   mark(s, staged ? "k_accel_mx_staged" : "k_accel_mx");
   launch_bc(P, K, C_V, s);
   launch_contact_kick(P, K, s);
-  launch_bc(P, K, C_V, s);
+  if (K.leapfrog) launch_bc(P, K, C_V, s);  // kick-drift: applied by the kick kernel
   if (K.gradcorr) {
     if (K.uni) launch_density_mx<true, true>(P, K, ng, gb, s);
     else launch_density_mx<true, false>(P, K, ng, gb, s);
@@ -938,8 +943,7 @@ void launch_step_mixed(const DevPtrs& P, const DomainConst& K, double* fscratch,
     if (K.uni) launch_density_mx<false, true>(P, K, ng, gb, s);
     else launch_density_mx<false, false>(P, K, ng, gb, s);
   }
-  mark(s, "k_density_drift_mx");
-  launch_bc(P, K, C_VN, s);
+  mark(s, "k_density_drift_mx");  // the next-step BC applied by the density kernel
   if (K.thermal_solver) {
     if (K.gradcorr) { if (K.uni) launch_rate_mx<true, true, true>(P, K, ng, gb, s); else launch_rate_mx<true, true, false>(P, K, ng, gb, s); }
     else { if (K.uni) launch_rate_mx<true, false, true>(P, K, ng, gb, s); else launch_rate_mx<true, false, false>(P, K, ng, gb, s); }
