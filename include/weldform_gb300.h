@@ -118,9 +118,12 @@ int wf_domain_destroy(wf_domain* d);
  * particle position that is not finite at a neighbour search, or non-finite
  * energy sums, make the next status-returning call fail with WF_ERR_NAN;
  * default 0 keeps the reference's behaviour of stepping on with NaN; no
- * reference counterpart; before the prologue), "cpu_threads" (unused on
- * the GPU path).  Read back with wf_get_domain_i32: "gather_block",
- * "gather_lanes", "gather_staging", "stage_cap". */
+ * reference counterpart; before the prologue), "particle_block" (threads
+ * per block of the per-particle kernels: 64, 128 or 256; 0, the default,
+ * chooses by particle count), "cpu_threads" and "cpu_mode" (the CPU
+ * restatement's thread count and structure; accepted and unused on the GPU
+ * path).  Read back with wf_get_domain_i32: "gather_block", "gather_lanes",
+ * "particle_block", "gather_staging", "stage_cap", "search_conditional". */
 int wf_set_domain_f64(wf_domain* d, const char* name, double value);
 int wf_set_domain_i32(wf_domain* d, const char* name, int value);
 /* Read-back of scalars: "Time", "deltat", "hmax", "int_energy_sum",

@@ -59,3 +59,14 @@ def test_no_device_is_a_loud_error(cuda_lib_path):
     assert b"device" in lib.wf_last_error()
     with pytest.raises(wf.WFError):
         wf.Domain()
+
+
+def test_header_documents_every_domain_field():
+    """Every field name the library's domain setters and getters accept is
+    documented in the header (the C ABI's only description for a caller)."""
+    src = open(os.path.join(ge.ROOT, "weldform_gb300", "csrc", "wf_domain.cu")).read()
+    hdr = open(HEADER).read()
+    names = set(re.findall(r'n == "([A-Za-z_.|0-9]+)"', src))
+    assert len(names) > 50
+    missing = sorted(n for n in names if '"' + n + '"' not in hdr)
+    assert not missing, missing
