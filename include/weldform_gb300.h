@@ -175,10 +175,14 @@ int wf_set_particle_i32(wf_domain* d, const char* field, int zone, int value);
 /* Whole-array transfer in original particle order.  Vector fields ("x", "v",
  * "a", "Displacement", "normal", "contforce") take 3 values per particle;
  * tensor fields ("Sigma", "ShearStress", "StrainRate", "RotationRate",
- * "Strain", "Strain_pl", "TIR" read-only) 9 (row-major, full 3x3, as the reference stores
- * them); scalars 1 ("Density", "Pressure", "pl_strain", "Sigmay", "T",
- * "dTdt", "eff_strain_rate", "q_plheat", "q_conv", "Mass", "h",
- * "delta_pl_strain", "dDensity").  n is the total number of doubles. */
+ * "Strain", "Strain_pl", "Strain_pl_incr", "TIR" read-only, "gradCorrM"
+ * read-only) 9 (row-major, full 3x3, as the reference stores them); scalars
+ * 1 ("Density", "Pressure", "pl_strain", "Sigmay", "T", "dTdt",
+ * "eff_strain_rate", "q_plheat", "q_conv", "Mass", "h", "delta_pl_strain",
+ * "dDensity", "delta_cont" (contact penetration), "dint_energy_dt",
+ * "dkin_energy_dt" (the particles' energy rates), "ps_energy" (accumulated
+ * plastic work per volume)) and every per-particle f64 field above.  n is the
+ * total number of doubles. */
 int wf_set_particle_array_f64(wf_domain* d, const char* field, const double* src,
                               int64_t n);
 int wf_get_particle_array_f64(wf_domain* d, const char* field, double* dst, int64_t n);

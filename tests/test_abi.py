@@ -70,3 +70,14 @@ def test_header_documents_every_domain_field():
     assert len(names) > 50
     missing = sorted(n for n in names if '"' + n + '"' not in hdr)
     assert not missing, missing
+
+
+def test_header_documents_every_particle_array():
+    """Every per-particle f64 array in the library's column table (the names
+    wf_get/set_particle_array_f64 accept) is named in the header."""
+    src = open(os.path.join(ge.ROOT, "weldform_gb300", "csrc", "wf_domain.cu")).read()
+    hdr = open(HEADER).read()
+    names = set(re.findall(r'\{"([A-Za-z_0-9]+)", C_[A-Z0-9]+, \d\}', src))
+    assert len(names) > 40
+    missing = sorted(n for n in names if '"' + n + '"' not in hdr)
+    assert not missing, missing
