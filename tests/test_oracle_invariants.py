@@ -1,0 +1,112 @@
+"""Physical invariants of the CPU oracle's kick-drift step.
+
+The parity tests hold the GPU forms to the oracle; these hold the oracle to
+properties of the SPH equations themselves, which a misreading of the
+reference's pair terms would break whatever the restatement says:
+
+* the acceleration pair term m_i m_j (Sigma_i/rho_i^2 + Sigma_j/rho_j^2 +
+  Pi_ij) GK x_ij is antisymmetric in (i, j), so with no boundary condition
+  or contact the mass-weighted sum of accelerations vanishes and the total
+  momentum stays put (CalcAccel, InteractionAlt.cpp:35-197);
+* every pair term reads velocities only as v_ij, so a uniform velocity added
+  to every particle shifts v and x and changes nothing else (Galilean
+  invariance of CalcAccel, CalcDensInc and CalcRateTensors,
+  InteractionAlt.cpp:12-640);
+* with kernel-gradient correction (M_i = inverse of -sum_j V_j grad W_ij (x)
+  x_ij, Domain.cpp:1832-1940) the corrected velocity gradient of a linear
+  field v = G x is exactly G at every particle, the free surface included
+  (the corrected rate sums, InteractionAlt.cpp:330-350, 425-450); without it
+  the estimate is off by the lattice's first-moment error.
+"""
+import numpy as np
+
+from tests._support import oracle_domain
+from weldform_gb300 import BILINEAR, configs
+
+DX = 0.0005
+H = 1.2 * DX
+
+
+def _run(v_of_x, steps, alpha=1.0, corr=0, fields=("x", "v", "a", "Sigma", "StrainRate", "Mass", "pl_strain")):
+    """A free cylinder (R 3 mm, L 6 mm, dx 0.5 mm, 968 particles, jittered),
+    bilinear steel, no BC and no contact, initial velocities v_of_x(x);
+    returns the listed fields after each of `steps` steps and dt."""
+    d = oracle_domain()
+    d.set("gradKernelCorr", corr)
+    mat = configs.Steel()
+    d.Kernel_Set(0)
+    d.AddCylinderLength(0, (0.0, 0.0, 0.0), 0.003, 0.006, DX / 2, mat.rho, H, False)
+    n = d.particle_count
+    x = d.get_array("x") + configs.jitter(n, DX)
+    d.set_array("x", x)
+    configs._material_setup(d, mat, BILINEAR)
+    d.set_particles("Alpha", alpha)
+    d.set_array("v", v_of_x(x))
+    dt = 0.4 * H / mat.Cs
+    d.prepare(dt)
+    out = []
+    for _ in range(steps):
+        d.step(1)
+        out.append({k: d.get_array(k) for k in fields})
+    d.close()
+    return out, dt
+
+
+def _random_v(seed, shift=(0.0, 0.0, 0.0)):
+    return lambda x: 50.0 * np.random.default_rng(seed).standard_normal(x.shape) + np.asarray(shift)
+
+
+def test_free_body_conserves_linear_momentum():
+    """Random velocities of 50 m/s: the body yields (plastic strain > 1e-2,
+    which also triggers neighbour rebuilds), yet sum m a = 0 and sum m v stays
+    at its initial value to rounding at every step."""
+    res, _ = _run(_random_v(3), 20)
+    m = res[0]["Mass"][:, None]
+    v0 = _random_v(3)(np.zeros((len(m), 3)))
+    p0 = (m * v0).sum(axis=0)
+    for r in res:
+        force, force_abs = (m * r["a"]).sum(axis=0), (m * np.abs(r["a"])).sum(axis=0)
+        mom_abs = (m * np.abs(r["v"])).sum(axis=0)
+        assert np.abs(force).max() <= 1e-14 * force_abs.max()
+        assert np.abs((m * r["v"]).sum(axis=0) - p0).max() <= 1e-14 * mom_abs.max()
+    assert res[-1]["pl_strain"].max() > 1e-2
+
+
+def test_uniform_velocity_changes_nothing_but_v_and_x():
+    """Adding u = (3, -2, 5) m/s to every initial velocity leaves a, Sigma and
+    StrainRate of the fifth step unchanged to rounding; v is shifted by u and
+    x by 5 dt u."""
+    u = np.array([3.0, -2.0, 5.0])
+    ra, dt = _run(_random_v(7), 5)
+    rb, _ = _run(_random_v(7, u), 5)
+    a, b = ra[-1], rb[-1]
+    for k in ("a", "Sigma", "StrainRate"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-13 * np.abs(a[k]).max(), k
+    assert np.abs((b["v"] - a["v"]) - u).max() <= 1e-12 * np.abs(u).max()
+    assert np.abs((b["x"] - a["x"]) - 5 * dt * u).max() <= 1e-10 * 5 * dt * np.abs(u).max()
+
+
+def test_corrected_gradient_of_a_linear_field_is_exact():
+    """v = G x with no viscosity and zero initial stress: the first step's
+    acceleration is 0, the drift keeps the field linear (v = G' x' with
+    G' = G (I + dt G)^-1), and the step's StrainRate and RotationRate are the
+    symmetric and antisymmetric parts of G' at every particle.  What remains
+    comes from the density and position updates between the correction
+    matrix and the rate sums (relative O(|G| dt)) and the float weights
+    m_j/rho_j of the locking sums (1e-7).  Without correction interior
+    particles read c G with c = 1.376, the lattice's first moment at
+    h = 1.2 dx."""
+    G = 10.0 * np.random.default_rng(0).standard_normal((3, 3))
+    tol = 20.0 * np.abs(G).max() * 0.4 * H / configs.Steel().Cs + 1e-6
+    err = {}
+    for corr in (0, 1):
+        res, dt = _run(lambda x: x @ G.T, 1, alpha=0.0, corr=corr, fields=("a", "StrainRate", "RotationRate"))
+        r = res[0]
+        assert np.abs(r["a"]).max() == 0.0
+        Gp = G @ np.linalg.inv(np.eye(3) + dt * G)
+        S, W = 0.5 * (Gp + Gp.T), 0.5 * (Gp - Gp.T)
+        eS = np.abs(r["StrainRate"].reshape(-1, 3, 3) - S).max(axis=(1, 2)) / np.abs(S).max()
+        eW = np.abs(r["RotationRate"].reshape(-1, 3, 3) - W).max(axis=(1, 2)) / np.abs(W).max()
+        err[corr] = np.maximum(eS, eW)
+    assert err[1].max() <= tol, (err[1].max(), tol)
+    assert np.median(err[0]) > 0.3  # the uncorrected estimate is not exact: the check discriminates
