@@ -16,7 +16,12 @@ reference's pair terms would break whatever the restatement says:
   x_ij, Domain.cpp:1832-1940) the corrected velocity gradient of a linear
   field v = G x is exactly G at every particle, the free surface included
   (the corrected rate sums, InteractionAlt.cpp:330-350, 425-450); without it
-  the estimate is off by the lattice's first-moment error.
+  the estimate is off by the lattice's first-moment error;
+* conduction adds one pair value to the first particle's sum and subtracts
+  it from the second's (Thermal.cpp:72-131), so sum_i rho_i cp_i dT_i/dt
+  vanishes at every step; the weight m_j/rho_j of the pair's second particle
+  is used at both ends, so sum_i m_i cp_i dT_i/dt vanishes only while the
+  density is uniform.
 """
 import numpy as np
 
@@ -110,3 +115,44 @@ def test_corrected_gradient_of_a_linear_field_is_exact():
         err[corr] = np.maximum(eS, eW)
     assert err[1].max() <= tol, (err[1].max(), tol)
     assert np.median(err[0]) > 0.3  # the uncorrected estimate is not exact: the check discriminates
+
+
+def _heat_rates(v_of_x, steps):
+    """Conduction only (no plastic heating): a cylinder with a temperature
+    gradient along z and a ripple along x; returns (rho cp dTdt, m cp dTdt,
+    the density's relative spread) after each step."""
+    d = oracle_domain()
+    mat = configs.Steel()
+    d.Kernel_Set(0)
+    d.AddCylinderLength(0, (0.0, 0.0, 0.0), 0.003, 0.006, DX / 2, mat.rho, H, False)
+    n = d.particle_count
+    x = d.get_array("x") + configs.jitter(n, DX)
+    d.set_array("x", x)
+    configs._material_setup(d, mat, BILINEAR)
+    d.set("thermal_solver", 1)
+    d.set_array("T", 300.0 + 1000.0 * x[:, 2] / 0.006 + 50.0 * np.sin(2000.0 * x[:, 0]))
+    d.set_array("v", v_of_x(x))
+    d.prepare(0.4 * H / mat.Cs)
+    out = []
+    for _ in range(steps):
+        d.step(1)
+        m, cp, rho, dT = (d.get_array(k) for k in ("Mass", "cp_T", "Density", "dTdt"))
+        out.append((rho * cp * dT, m * cp * dT, np.ptp(rho) / rho.mean()))
+    d.close()
+    return out
+
+
+def test_conduction_exchanges_heat_pairwise():
+    """At rest (uniform density) both balances hold to rounding; with the
+    random 50 m/s velocities the density spreads by a few percent and only the
+    density-weighted balance still holds, the mass-weighted one drifting by
+    more than 1e-6 of the exchanged heat."""
+    for rq, mq, spread in _heat_rates(lambda x: np.zeros_like(x), 3):
+        assert spread == 0.0
+        assert abs(rq.sum()) <= 1e-14 * np.abs(rq).sum()
+        assert abs(mq.sum()) <= 1e-14 * np.abs(mq).sum()
+    moving = _heat_rates(_random_v(3), 6)
+    for rq, _, _ in moving:
+        assert abs(rq.sum()) <= 1e-14 * np.abs(rq).sum()
+    rq, mq, spread = moving[-1]
+    assert spread > 1e-2 and abs(mq.sum()) > 1e-6 * np.abs(mq).sum()
