@@ -21,12 +21,19 @@ reference's pair terms would break whatever the restatement says:
   it from the second's (Thermal.cpp:72-131), so sum_i rho_i cp_i dT_i/dt
   vanishes at every step; the weight m_j/rho_j of the pair's second particle
   is used at both ends, so sum_i m_i cp_i dT_i/dt vanishes only while the
-  density is uniform.
+  density is uniform;
+* the flow stress after each step is the material law evaluated at the
+  particle's plastic strain before the step, the step's effective strain
+  rate and its temperature (Johnson-Cook with the rate factor cut at
+  eps_0, Material.cpp:6-23; Hollomon's plateau, Material.cpp:48-64; called
+  from Particle.cpp:997-1000), and the returned deviatoric stress never leaves
+  the yield surface of the step before (the scale factor uses the previous
+  Sigmay, Particle.cpp:995).
 """
 import numpy as np
 
 from tests._support import oracle_domain
-from weldform_gb300 import BILINEAR, configs
+from weldform_gb300 import BILINEAR, HOLLOMON, JOHNSON_COOK, configs
 
 DX = 0.0005
 H = 1.2 * DX
@@ -156,3 +163,44 @@ def test_conduction_exchanges_heat_pairwise():
         assert abs(rq.sum()) <= 1e-14 * np.abs(rq).sum()
     rq, mq, spread = moving[-1]
     assert spread > 1e-2 and abs(mq.sum()) > 1e-6 * np.abs(mq).sum()
+
+
+def _von_mises(tau):
+    t = tau.reshape(-1, 3, 3)
+    return np.sqrt(1.5 * np.einsum("nij,nij->n", t, t))
+
+
+def test_flow_stress_follows_the_material_law():
+    """A cylinder upset at 20 m/s for 40 steps (plastic strain to ~2e-2):
+    Johnson-Cook at 600 K (temperature factor 0.8) and Hollomon, whose
+    plateau end (plastic strain 9.3e-4) is passed by part of the particles
+    while others stay on it."""
+    mat = configs.Steel()
+    for model in (JOHNSON_COOK, HOLLOMON):
+        d = oracle_domain()
+        case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_top=-20.0, model=model)
+        if model == JOHNSON_COOK:
+            d.set_particles("T", 600.0)
+        d.prepare(case.dt)
+        plateau = past = 0
+        for _ in range(40):
+            pl0, sy0 = d.get_array("pl_strain"), d.get_array("Sigmay")
+            d.step(1)
+            sy, esr, T = d.get_array("Sigmay"), d.get_array("eff_strain_rate"), d.get_array("T")
+            if model == JOHNSON_COOK:
+                A, B, n, C, eps_0, m, T_m, T_t = mat.jc
+                f = np.where(esr > eps_0, 1.0 + C * np.log(np.maximum(esr, eps_0) / eps_0), 1.0)
+                law = (A + B * pl0 ** n) * f * (1.0 - ((T - T_t) / (T_m - T_t)) ** m)
+            else:
+                K, m = mat.hollomon
+                eps0, eps1 = mat.sy0 / mat.E, (mat.sy0 / K) ** (1.0 / m)
+                on = pl0 + eps0 > eps1
+                law = np.where(on, K * (pl0 + eps0) ** m, mat.sy0)
+                past += int(on.sum())
+                plateau += int(((pl0 > 0) & ~on).sum())
+            assert np.abs(sy - law).max() <= 1e-14 * law.max()
+            assert (_von_mises(d.get_array("ShearStress")) <= sy0 * (1.0 + 1e-12)).all()
+        assert d.get_array("pl_strain").max() > 1e-2
+        if model == HOLLOMON:
+            assert past > 0 and plateau > 0
+        d.close()
