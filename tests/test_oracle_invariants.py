@@ -102,7 +102,10 @@ def test_corrected_gradient_of_a_linear_field_is_exact():
     """v = G x with no viscosity and zero initial stress: the first step's
     acceleration is 0, the drift keeps the field linear (v = G' x' with
     G' = G (I + dt G)^-1), and the step's StrainRate and RotationRate are the
-    symmetric and antisymmetric parts of G' at every particle.  What remains
+    symmetric and antisymmetric parts of G' at every particle, while the
+    density rate, taken before the drift, is the continuity equation
+    -rho tr(G) (CalcDensInc's corrected locking sum, InteractionAlt.cpp:589-605)
+    to rounding.  What remains in the rates
     comes from the density and position updates between the correction
     matrix and the rate sums (relative O(|G| dt)) and the float weights
     m_j/rho_j of the locking sums (1e-7).  Without correction interior
@@ -112,9 +115,17 @@ def test_corrected_gradient_of_a_linear_field_is_exact():
     tol = 20.0 * np.abs(G).max() * 0.4 * H / configs.Steel().Cs + 1e-6
     err = {}
     for corr in (0, 1):
-        res, dt = _run(lambda x: x @ G.T, 1, alpha=0.0, corr=corr, fields=("a", "StrainRate", "RotationRate"))
+        res, dt = _run(lambda x: x @ G.T, 1, alpha=0.0, corr=corr,
+                       fields=("a", "StrainRate", "RotationRate", "dDensity", "Density"))
         r = res[0]
         assert np.abs(r["a"]).max() == 0.0
+        rho0 = configs.Steel().rho
+        cont = np.abs(r["dDensity"] + rho0 * np.trace(G)) / (rho0 * abs(np.trace(G)))
+        if corr:  # the continuity equation, from the pre-drift state the correction matrix was built on
+            assert cont.max() <= 1e-13
+            assert np.abs(r["Density"] - (rho0 + dt * r["dDensity"])).max() <= 1e-15 * rho0
+        else:
+            assert np.median(cont) > 0.3
         Gp = G @ np.linalg.inv(np.eye(3) + dt * G)
         S, W = 0.5 * (Gp + Gp.T), 0.5 * (Gp - Gp.T)
         eS = np.abs(r["StrainRate"].reshape(-1, 3, 3) - S).max(axis=(1, 2)) / np.abs(S).max()
