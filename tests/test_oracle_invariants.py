@@ -28,7 +28,11 @@ reference's pair terms would break whatever the restatement says:
   eps_0, Material.cpp:6-23; Hollomon's plateau, Material.cpp:48-64; called
   from Particle.cpp:997-1000), and the returned deviatoric stress never leaves
   the yield surface of the step before (the scale factor uses the previous
-  Sigmay, Particle.cpp:995).
+  Sigmay, Particle.cpp:995);
+* the stress rate is objective: a pre-stressed body spinning rigidly
+  carries its stress round with it, dtau/dt = W tau - tau W (the Jaumann
+  terms SRT + RS, Particle.cpp:968-981), which fixes the sign convention of
+  RotationRate against the velocity gradient.
 """
 import numpy as np
 
@@ -110,7 +114,8 @@ def test_corrected_gradient_of_a_linear_field_is_exact():
     matrix and the rate sums (relative O(|G| dt)) and the float weights
     m_j/rho_j of the locking sums (1e-7).  Without correction interior
     particles read c G with c = 1.376, the lattice's first moment at
-    h = 1.2 dx."""
+    h = 1.2 dx with the generator's particle volume m/rho = pi R^2 L / N
+    (Domain.cpp:840-842; 1.40 dx^3 for this cylinder)."""
     G = 10.0 * np.random.default_rng(0).standard_normal((3, 3))
     tol = 20.0 * np.abs(G).max() * 0.4 * H / configs.Steel().Cs + 1e-6
     err = {}
@@ -215,3 +220,60 @@ def test_flow_stress_follows_the_material_law():
         if model == HOLLOMON:
             assert past > 0 and plateau > 0
         d.close()
+
+
+def test_spinning_body_carries_its_stress_round():
+    """A 5,244-particle cylinder (R 5 mm, L 10 mm, no jitter) with a uniform
+    deviatoric stress tau0 (106 MPa von Mises, below yield) spins rigidly,
+    v = Omega x.  The unbalanced stress at the free surface accelerates the
+    outer particles in the first step; particles whose neighbours and
+    neighbours' neighbours were not accelerated (168 here) see only the
+    spin, so their stress rate over the step is 2G dev(S') + W' tau0 -
+    tau0 W' with G' = Omega (I + dt Omega)^-1 the velocity gradient at the
+    drifted positions.  With correction that holds to rounding (measured
+    8e-8); the opposite sign of the rotation terms is off by ~2.  Without
+    correction the same particles read the lattice's first moment c times
+    G', c = 1 / gradCorrM_00 of the corrected run."""
+    tau0 = np.array([[60.0, 30.0, 0.0], [30.0, -20.0, 10.0], [0.0, 10.0, -40.0]]) * 1e6
+    w = np.array([300.0, -500.0, 1000.0])
+    Om = np.array([[0.0, -w[2], w[1]], [w[2], 0.0, -w[0]], [-w[1], w[0], 0.0]])
+    mat = configs.Steel()
+    rate, moment = {}, None
+    for corr in (1, 0):
+        d = oracle_domain()
+        d.set("gradKernelCorr", corr)
+        d.Kernel_Set(0)
+        d.AddCylinderLength(0, (0.0, 0.0, 0.0), 0.005, 0.010, DX / 2, mat.rho, H, False)
+        n = d.particle_count
+        x = d.get_array("x")
+        configs._material_setup(d, mat, BILINEAR)
+        d.set_particles("Alpha", 0.0)
+        d.set_array("v", x @ Om.T)
+        d.set_array("ShearStress", np.tile(tau0.ravel(), (n, 1)))
+        d.set_array("Sigma", np.tile(tau0.ravel(), (n, 1)))
+        dt = 0.4 * H / mat.Cs
+        d.prepare(dt)
+        d.step(1)
+        tau = d.get_array("ShearStress").reshape(-1, 3, 3)
+        a = d.get_array("a")
+        off, idx = d.neighbours()
+        if corr:
+            moment = 1.0 / d.get_array("gradCorrM").reshape(-1, 3, 3)[:, 0, 0]
+        d.close()
+        still = np.abs(a).max(axis=1) < 1e-4
+        calm = still.copy()
+        for _ in range(2):
+            calm = np.array([calm[i] and calm[idx[off[i]:off[i + 1]]].all() for i in range(n)])
+        rate[corr] = (tau - tau0) / dt
+    assert 100 <= calm.sum() < n // 10
+    Gp = Om @ np.linalg.inv(np.eye(3) + dt * Om)
+    S, W = 0.5 * (Gp + Gp.T), 0.5 * (Gp - Gp.T)
+    dev = 2.0 * mat.G * (S - np.trace(S) / 3.0 * np.eye(3))
+    jaumann, opposite = dev + W @ tau0 - tau0 @ W, dev - W @ tau0 + tau0 @ W
+    scale = np.abs(jaumann).max()
+    err = np.abs(rate[1][calm] - jaumann).max(axis=(1, 2)) / scale
+    assert err.max() <= 1e-6
+    assert (np.abs(rate[1][calm] - opposite).max(axis=(1, 2)) / scale).min() > 1.0
+    c = moment[calm]
+    assert np.ptp(c) <= 1e-12 * c[0] and abs(c[0] - 1.0) > 0.1
+    assert (np.abs(rate[0][calm] - c[:, None, None] * jaumann).max(axis=(1, 2)) / scale).max() <= 1e-6
