@@ -296,7 +296,9 @@ class Domain:
         self._call("checkpoint_free", self._h, int(slot))
 
     def autotune(self, steps: int = 5) -> int:
-        """Pick the gather kernels' block size by timing; returns it."""
+        """Pick the mixed gathers' block size and lanes per particle by
+        timing every pair; returns the block size (the lanes are the domain
+        field "gather_lanes")."""
         b = ctypes.c_int()
         self._call("autotune", self._h, int(steps), ctypes.byref(b))
         return b.value
