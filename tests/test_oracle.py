@@ -45,6 +45,38 @@ def test_reference_structured_mode_agrees_with_canonical_mode():
         assert rel_l2(b[f], a[f]) < 1e-9, f
 
 
+@pytest.mark.parametrize("stiffness,ti", [("wang", 0.3), ("area", 0.0)])
+def test_reference_structured_mode_agrees_on_contact_and_heat(stiffness, ti):
+    """The same agreement on the configuration-2 physics the CPU baseline also
+    times: a rigid plane pressing at 20 m/s and sliding at 5 m/s on a
+    Johnson-Cook cylinder with conduction and plastic heating (80 steps,
+    plastic strain to 4e-2, dynamic friction reached), with the tensile-
+    instability term on for the Wang law.  The search schedule and the
+    dynamic-friction count are equal; the contact force agrees to the
+    rounding of the penalty force it sums."""
+    out = []
+    for mode in (0, 1):
+        d = oracle_domain()
+        d.set("cpu_mode", mode)
+        d.set("cpu_threads", 4)
+        case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, stiffness=stiffness,
+                                         v_slide=5.0)
+        d.set_particles("TI", ti)
+        d.prepare(case.dt)
+        d.step(80)
+        r = {f: d.get_array(f) for f in ("x", "Sigma", "pl_strain", "Density", "T")}
+        r["F"] = d.contact_force(case.mesh)
+        r["counts"] = (d.geti("nb_searches"), d.geti("dynamic_friction_count"))
+        out.append(r)
+        d.close()
+    a, b = out
+    assert a["pl_strain"].max() > 1e-2 and a["counts"][1] > 0 and np.ptp(a["T"]) > 1.0
+    assert a["counts"] == b["counts"]
+    for f in ("x", "Sigma", "pl_strain", "Density", "T"):
+        assert rel_l2(b[f], a[f]) < 1e-9, f
+    assert rel_l2(b["F"], a["F"]) < 1e-9
+
+
 def test_kinetic_energy_rate_cancels_pairwise():
     """CalcKinEnergyEqn adds +temp / -temp to the two particles of every pair
     (Domain.cpp:1775-1791), so its global sum is zero up to rounding."""
