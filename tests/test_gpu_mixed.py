@@ -1,6 +1,6 @@
 """Mixed FP32/FP64 form against the FP64 oracle, through the C ABI.
 
-Bar (the benchmark spec): relative L2 error <= 1e-4 in stress and reaction force
+Bar: relative L2 error <= 1e-4 in stress and reaction force
 after the stated steps; the same bound is applied to displacement, plastic
 strain, density and temperature.  Neighbour lists stay bit-exact (the search
 is shared with the plain form and runs on FP64 positions).
