@@ -81,3 +81,40 @@ def test_header_documents_every_particle_array():
     assert len(names) > 40
     missing = sorted(n for n in names if '"' + n + '"' not in hdr)
     assert not missing, missing
+
+
+def _ctype(param):
+    """ctypes type of one C parameter declaration of the header."""
+    stars = param.count("*") + param.count("[")
+    words = re.sub(r"\[.*?\]", "", re.sub(r"\bconst\b", "", param)).replace("*", " ").split()
+    base = words[0] if words else ""
+    if base == "char" and stars == 1:
+        return ctypes.c_char_p
+    if base in ("wf_domain", "void"):
+        return ctypes.c_void_p if stars == 1 else ctypes.POINTER(ctypes.c_void_p)
+    scalar = {"double": ctypes.c_double, "int": ctypes.c_int, "int64_t": ctypes.c_int64,
+              "int32_t": ctypes.c_int32, "float": ctypes.c_float}[base]
+    return ctypes.POINTER(scalar) if stars == 1 else scalar
+
+
+def _header_signatures():
+    txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    txt = re.sub(r"//[^\n]*", "", txt)
+    out = {}
+    for name, args in re.findall(r"\b(?:int|const char\s*\*|double|void)\s+(wf_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", txt):
+        params = [a for a in args.split(",") if a.strip() and a.strip() != "void"]
+        out[name] = [_ctype(a) for a in params]
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every entry point the Python mirror binds has the header's arity and
+    argument types (a width mismatch, int against int64_t, would truncate
+    silently through ctypes)."""
+    assert _ctype("const double V[3]") is ctypes.POINTER(ctypes.c_double)
+    assert _ctype("wf_domain** out") is ctypes.POINTER(ctypes.c_void_p)
+    assert _ctype("int64_t n") is ctypes.c_int64 and _ctype("const char* field") is ctypes.c_char_p
+    sigs = _header_signatures()
+    assert set(declared()) == set(sigs)
+    for key, argtypes in wf._SIGS.items():
+        assert sigs["wf_" + key] == list(argtypes), key
