@@ -118,3 +118,16 @@ def test_ctypes_signatures_match_the_header():
     assert set(declared()) == set(sigs)
     for key, argtypes in wf._SIGS.items():
         assert sigs["wf_" + key] == list(argtypes), key
+
+
+def test_oracle_definitions_match_the_header():
+    """The oracle's wfo_* definitions take the header's argument types, so the
+    same ctypes table drives both libraries."""
+    src = open(os.path.join(ge.ROOT, "oracle", "wf_oracle.cpp")).read()
+    src = re.sub(r"//[^\n]*", "", re.sub(r"/\*.*?\*/", "", src, flags=re.S))
+    defs = dict(re.findall(r"\b(?:int|const char\s*\*|double)\s+wfo_([a-z0-9_]+)\s*\(([^)]*)\)\s*\{", src))
+    for name, sig in _header_signatures().items():
+        if name == "wf_neighbour_list_static":  # product-only helper
+            continue
+        params = [a for a in defs[name[3:]].split(",") if a.strip() and a.strip() != "void"]
+        assert [_ctype(a.replace("wfo_domain", "wf_domain")) for a in params] == sig, name
