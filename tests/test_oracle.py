@@ -142,6 +142,43 @@ def test_leapfrog_first_step_matches_kickdrift_half_kick():
     assert rel_l2(out[1][2], out[0][2]) > 1e-6    # v(n+1/2) against v(n+1)
 
 
+@pytest.mark.parametrize("integrator", [0, 1], ids=["kickdrift", "leapfrog"])
+def test_update_order_of_each_solver(integrator):
+    """One step of a free, yielding cylinder, from the step's own a:
+    kick-drift kicks by a dt/2 before the drift and again after it with the
+    same acceleration (SolverKickDrift.cpp:226-227, 254-263), so
+    x' = x + (v + a dt/2) dt and v' = v + a dt/2 + a dt/2; leapfrog kicks the
+    half-step velocity by a (dt_prev + dt)/2 = a dt and drifts with it
+    (SolverLeapfrog.cpp:269, 296-301).
+    Bit for bit, with Displacement advancing by the same du as x."""
+    from weldform_gb300 import BILINEAR
+    dx, h = 0.0005, 0.0006
+    d = oracle_domain()
+    d.set("integrator", integrator)
+    mat = configs.Steel()
+    d.Kernel_Set(0)
+    d.AddCylinderLength(0, (0.0, 0.0, 0.0), 0.003, 0.006, dx / 2, mat.rho, h, False)
+    x = d.get_array("x") + configs.jitter(d.particle_count, dx)
+    d.set_array("x", x)
+    configs._material_setup(d, mat, BILINEAR)
+    d.set_array("v", 50.0 * np.random.default_rng(3).standard_normal(x.shape))
+    dt = 0.4 * h / mat.Cs
+    d.prepare(dt)
+    d.step(3)
+    x0, v0, u0 = d.get_array("x"), d.get_array("v"), d.get_array("Displacement")
+    d.step(1)
+    a, x1, v1, u1 = d.get_array("a"), d.get_array("x"), d.get_array("v"), d.get_array("Displacement")
+    d.close()
+    if integrator == 0:
+        vh = v0 + a * (0.5 * dt)
+        xe, ve = x0 + vh * dt, vh + a * (dt / 2.0)
+    else:
+        ve = v0 + a * dt
+        xe = x0 + ve * dt
+    assert np.array_equal(x1, xe) and np.array_equal(v1, ve)
+    assert np.abs((u1 - u0) - (x1 - x0)).max() <= 1e-12 * np.abs(x1 - x0).max()
+
+
 def test_kernel_gradient_correction_matrix():
     """CalcGradCorrMatrix (Domain.cpp:1832-1940): isotropic (c I, the same c)
     for interior particles of a regular lattice — at h = 1.2 dx the discrete
