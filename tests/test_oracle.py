@@ -179,6 +179,36 @@ def test_update_order_of_each_solver(integrator):
     assert np.abs((u1 - u0) - (x1 - x0)).max() <= 1e-12 * np.abs(x1 - x0).max()
 
 
+@pytest.mark.parametrize("integrator", [0, 1], ids=["kickdrift", "leapfrog"])
+def test_velocity_bc_zones_move_as_prescribed(integrator):
+    """UserAcc (WeldForm.cpp:51-120) at its call sites: after every step the
+    particles of a BC zone carry exactly the prescribed velocity and zero
+    acceleration, and moved by that velocity times dt.  A constant BC holds
+    v = value; an amplitude BC holds amp_factor * amplitude(t) * value at the
+    step's start time t, since Time advances at the end of the step
+    (SolverKickDrift.cpp:299, SolverLeapfrog.cpp:331)."""
+    d = oracle_domain()
+    d.set("integrator", integrator)
+    case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_top=-20.0)
+    d.add_amplitude(7, [0.0, 1e-5], [0.0, 1.0])
+    d.AssignZone((-1.0, -1.0, 0.0025), (1.0, 1.0, 0.0035), 4)
+    d.add_velocity_bc(4, (3.0, 0.0, 0.0), value_type=1, amp_id=7, amp_factor=2.0)
+    ids = d.get_array("ID")
+    assert all((ids == z).sum() > 100 for z in (2, 3, 4))
+    d.prepare(case.dt)
+    for _ in range(5):
+        x0, t0 = d.get_array("x"), d.Time
+        d.step(1)
+        x1, v, a = d.get_array("x"), d.get_array("v"), d.get_array("a")
+        for zone, value in ((2, (0.0, 0.0, 0.0)), (3, (0.0, 0.0, -20.0)), (4, (2.0 * 3.0 * t0 / 1e-5, 0.0, 0.0))):
+            m = ids == zone
+            assert np.abs(v[m] - value).max() <= 1e-15 * max(1.0, abs(max(value, key=abs))), zone
+            assert np.abs(a[m]).max() == 0.0, zone
+            assert np.abs((x1 - x0)[m] - np.asarray(value) * case.dt).max() <= 1e-15, zone
+    assert d.Time > 4 * case.dt
+    d.close()
+
+
 def test_kernel_gradient_correction_matrix():
     """CalcGradCorrMatrix (Domain.cpp:1832-1940): isotropic (c I, the same c)
     for interior particles of a regular lattice — at h = 1.2 dx the discrete
