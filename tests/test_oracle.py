@@ -209,6 +209,25 @@ def test_velocity_bc_zones_move_as_prescribed(integrator):
     d.close()
 
 
+def test_rigid_plane_moves_as_its_bc_prescribes():
+    """The plane's zone BC sets the mesh velocity m_v (WeldForm.cpp:51-120),
+    and TriMesh::Update (Mesh.cpp:82-293) moves its particles by m_v dt each
+    step: exactly, while contact with friction runs under it."""
+    d = oracle_domain()
+    case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, v_slide=5.0)
+    plane = d.get_array("ID") == 10
+    assert plane.sum() > 100
+    d.prepare(case.dt)
+    for _ in range(4):
+        x0 = d.get_array("x")
+        d.step(1)
+        x1, v = d.get_array("x"), d.get_array("v")
+        assert np.abs(v[plane] - (5.0, 0.0, -20.0)).max() == 0.0
+        assert np.abs((x1 - x0)[plane] - np.array([5.0, 0.0, -20.0]) * case.dt).max() <= 1e-15
+    assert np.abs(d.contact_force(case.mesh)).max() > 0.0
+    d.close()
+
+
 def test_kernel_gradient_correction_matrix():
     """CalcGradCorrMatrix (Domain.cpp:1832-1940): isotropic (c I, the same c)
     for interior particles of a regular lattice — at h = 1.2 dx the discrete
