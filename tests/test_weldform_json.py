@@ -250,3 +250,47 @@ def test_hollomon_nan_pattern_matches_the_oracle(precision):
     ok = np.isfinite(o)
     tol = 1e-9 if precision is None else 1e-4
     assert rel_l2(g[ok], o[ok]) <= tol
+
+
+# Keys of the accepted reference decks the front-end does not read, each one
+# the reference's driver does not act on either (Source/WeldForm.cpp).
+_IGNORED_DECK_KEYS = {
+    "BoundaryConditions[].components": "never read",
+    "BoundaryConditions[].free": "read into bcon.free (WeldForm.cpp:822), never used",
+    "BoundaryConditions[].valuetype": "misspelt in the decks; the driver reads valueType (WeldForm.cpp:777)",
+    "Configuration.Nproc": "OpenMP thread count (WeldForm.cpp:195)",
+    "Contact[].heatCondCoeff": "used only with heatConductance (WeldForm.cpp:689, 714-718), rejected here",
+    "DomainBlocks[].denseMode": "never read",
+    "DomainBlocks[].matID": "read (WeldForm.cpp:404), never used",
+    "DomainBlocks[].scale": "never read",
+    "DomainZones[].denseMode": "never read",
+    "Materials[].const1": "never read (the driver reads const, WeldForm.cpp:252)",
+    "Materials[].const2": "never read (the driver reads const, WeldForm.cpp:252)",
+    "RigidBodies[].scale": "never read",
+}
+
+
+def test_every_key_of_the_accepted_decks_is_read_or_inert():
+    """A key of an accepted deck that the front-end never mentions would be a
+    silent misreading unless the reference's driver ignores it as well."""
+    import json
+    import re
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_decks.json")
+    decks = json.load(open(golden))["decks"]
+    keys = set()
+
+    def walk(o, path):
+        if isinstance(o, dict):
+            for k, v in o.items():
+                p = f"{path}.{k}" if path else k
+                keys.add(p)
+                walk(v, p)
+        elif isinstance(o, list):
+            for x in o:
+                walk(x, path + "[]")
+
+    for deck in decks.values():
+        walk(deck, "")
+    src = open(wj.__file__).read()
+    unread = {k for k in keys if '"%s"' % re.sub(r"\[.*", "", k.split(".")[-1]) not in src}
+    assert unread == set(_IGNORED_DECK_KEYS), sorted(unread ^ set(_IGNORED_DECK_KEYS))
