@@ -145,6 +145,41 @@ def test_convection_boundary_condition():
     assert e.value.code == 8
 
 
+@pytest.mark.parametrize("base,section,key", [
+    ("compression", "Configuration", "cflMethod"),   # int cflMethod (WeldForm.cpp:346-351)
+    ("compression", "DomainBlocks", "start"),        # Vec3_t start (WeldForm.cpp:393, 401)
+    ("box", "DomainBlocks", "id"),                   # int id, the box particles' tag (WeldForm.cpp:394, 434)
+    ("contact", "Materials", "thermalCond"),         # double k_T under a thermal solver (WeldForm.cpp:326-327)
+    ("contact", "Materials", "thermalHeatCap"),      # double cp_T (WeldForm.cpp:326, 328)
+])
+def test_input_without_a_key_the_driver_leaves_uninitialized_is_rejected(base, section, key):
+    """Keys the driver reads into variables it never initialised: an input
+    that omits one has no defined meaning, so the front-end refuses it."""
+    j = copy.deepcopy(CONTACT if base == "contact" else COMPRESSION)
+    if base == "box":
+        j["DomainBlocks"] = [{"type": "Box", "id": 0, "start": [0, 0, 0], "dim": [2 * R, 2 * R, L]}]
+        wj.build(copy.deepcopy(j), make=_oracle).dom.close()  # complete, it builds
+    tgt = j[section][0] if isinstance(j[section], list) else j[section]
+    del tgt[key]
+    with pytest.raises(WFError) as e:
+        wj.build(j, make=_oracle)
+    assert e.value.code == 8 and key in str(e.value)
+
+
+def test_initial_temperature_carries_over_between_conditions():
+    """The driver reads every initial condition's "Temp" into one IniTemp
+    declared outside the loop (WeldForm.cpp:828-833), so a condition without
+    "Temp" applies the previous condition's temperature to its zone."""
+    j = copy.deepcopy(CONTACT)
+    j["DomainZones"].append({"id": 4, "start": [-1, -1, L / 2], "end": [1, 1, 1]})
+    j["InitialConditions"] = [{"Temp": 300.0, "zoneId": -1}, {"Temp": 450.0, "zoneId": 2}, {"zoneId": 4}]
+    run = wj.build(j, make=_oracle)
+    ids, T = run.dom.get_array("ID"), run.dom.get_array("T")
+    assert (T[ids == 2] == 450.0).all() and (T[ids == 4] == 450.0).all()
+    assert (T[ids == 0] == 300.0).all() and (ids == 4).sum() > 0
+    run.dom.close()
+
+
 @pytest.mark.parametrize("patch", [
     ("Materials", "type", "GMT"),
     ("Materials", "damageModel", "Rankine"),

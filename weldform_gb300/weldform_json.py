@@ -138,15 +138,17 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
         dom.set("pl_heating", 1)
     if m0.get("damageModel", ""):
         _unsupported("damage models")
-    k_T = float(m0.get("thermalCond", 0.0))
-    cp_T = float(m0.get("thermalHeatCap", 0.0))
+    # uninitialized doubles in the driver when absent (WeldForm.cpp:326-328);
+    # only the thermal solvers read them
+    k_T = float(m0["thermalCond"]) if thermal else float(m0.get("thermalCond", 0.0))
+    cp_T = float(m0["thermalHeatCap"]) if thermal else float(m0.get("thermalHeatCap", 0.0))
     th_ex = float(m0.get("thermalExp", 0.0))
     K = E / (3. * (1. - 2 * nu))
     G = E / (2. * (1. + nu))
     dx = 2. * r
     h = dx * hfactor
     Cs = math.sqrt(K / rho)
-    if int(config.get("cflMethod", 0)) == 0:
+    if int(config["cflMethod"]) == 0:  # an uninitialized int in the driver when absent (WeldForm.cpp:346)
         timestep = float(config["timeStepSize"])
     else:
         timestep = float(config["cflFactor"]) * h / Cs
@@ -174,8 +176,7 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
     dom.set("ts_nb_inc", int(config.get("nbsearchFreq", 5)))
     # ---- Domain block (WeldForm.cpp:395-560)
     b0 = domblock[0]
-    bid = int(b0.get("id", 0))
-    start = _vec(b0.get("start", [0, 0, 0]))
+    start = _vec(b0["start"])  # an uninitialized Vec3_t in the driver when absent (WeldForm.cpp:393, 401)
     L = _vec(b0["dim"])
     domtype = b0.get("type", "Box")
     if b0.get("gridCoordSys", "Cartesian") != "Cartesian":
@@ -187,7 +188,9 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
     if abs(L[2]) < h:
         _unsupported("2D domains")
     if domtype == "Box":
-        dom.AddBoxLength(bid, start, L[0], L[1], L[2], r, rho, h, 1, 0, False, False)
+        # the block's id tags the particles; an uninitialized int when absent
+        # (WeldForm.cpp:394, 400, 434); cylinders are tagged 0 whatever it is
+        dom.AddBoxLength(int(b0["id"]), start, L[0], L[1], L[2], r, rho, h, 1, 0, False, False)
     elif domtype == "Cylinder":
         if (sym[0] and sym[1]) or sym[2]:
             _unsupported("symmetric / ghost cylinders")
@@ -251,8 +254,11 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
     T = np.zeros(n)
     v = np.zeros((n, 3))
     nsolid = int(dom.geti("solid_part_count"))
+    # The driver keeps one IniTemp across the conditions (WeldForm.cpp:828-833):
+    # a condition without "Temp" applies the previous one's.
+    temp = 0.0
     for ic in ics:
-        temp = float(ic.get("Temp", 0.0))
+        temp = float(ic.get("Temp", temp))
         value = _vec(ic.get("value", [0, 0, 0]))
         zoneid = int(ic.get("zoneId", -1))
         if zoneid == -1:
