@@ -242,6 +242,10 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
         if btype != 0:
             _unsupported("temperature / force / symmetry boundary conditions")
         vt = int(bc.get("valueType", 0))
+        # An absent "value" leaves the driver's Vec3_t uninitialized
+        # (WeldForm.cpp:776-779) and UserAcc multiplies it (WeldForm.cpp:76-77);
+        # the reference's Traction.json has such an amplitude BC.  Zero here:
+        # its zone is held still.
         value = _vec(bc.get("value", [0, 0, 0]))
         ang = _vec(bc.get("valueAng", [0, 0, 0]))
         if vt == 0:
