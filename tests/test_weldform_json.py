@@ -166,6 +166,22 @@ def test_input_without_a_key_the_driver_leaves_uninitialized_is_rejected(base, s
     assert e.value.code == 8 and key in str(e.value)
 
 
+def test_plane_without_start_starts_at_the_block_start():
+    """The driver reads a rigid body's "start" into the domain block's start
+    vector (WeldForm.cpp:393, 595; the zones keep their own), so a plane that
+    gives none is laid from the block's start."""
+    j = copy.deepcopy(CONTACT)
+    j["DomainBlocks"][0]["start"] = [-0.001, -0.002, 0.0075]
+    del j["RigidBodies"][0]["start"]
+    run = wj.build(j, make=_oracle)
+    x, ids = run.dom.get_array("x"), run.dom.get_array("ID")
+    plane = x[ids == 10]
+    assert plane.shape[0] > 0
+    assert np.all(plane[:, 2] == plane[0, 2]) and abs(plane[0, 2] - 0.0075) < 1e-12
+    assert abs(plane[:, 0].min() - (-0.001)) < 2 * r and abs(plane[:, 1].min() - (-0.002)) < 2 * r
+    run.dom.close()
+
+
 def test_initial_temperature_carries_over_between_conditions():
     """The driver reads every initial condition's "Temp" into one IniTemp
     declared outside the loop (WeldForm.cpp:828-833), so a condition without

@@ -206,7 +206,9 @@ def _build(inp, make: Callable[[], object] = Domain, precision: Optional[int] = 
             continue
         if rb["type"] != "Plane":
             _unsupported(f"rigid body type {rb['type']!r}")
-        rstart = _vec(rb["start"])
+        # read into the block's Vec3_t start (WeldForm.cpp:393, 595): absent,
+        # the plane starts where the block does
+        rstart = _vec(rb["start"]) if "start" in rb else list(start)
         rdim = _vec(rb["dim"])
         if rdim[0] != 0. and rdim[1] != 0. and rdim[2] != 0.:
             raise WFError(1, "Contact Plane Surface should have one null dimension")
