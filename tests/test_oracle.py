@@ -228,6 +228,25 @@ def test_rigid_plane_moves_as_its_bc_prescribes():
     d.close()
 
 
+@pytest.mark.parametrize("stiffness", ["wang", "penalty", "area"])
+def test_frictionless_contact_pushes_along_the_plane_normal(stiffness):
+    """With both friction coefficients 0 the friction block is skipped
+    (Contact_Wang.cpp:263, `fr_sta > 0`), so every particle's contact force
+    and the plane's summed force lie along the plane normal (z): their x and y
+    components are exactly 0 while the plane presses ~1e4 N."""
+    d = oracle_domain()
+    case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, friction=0.0,
+                                     stiffness=stiffness)
+    d.prepare(case.dt)
+    d.step(60)
+    cf, F = d.get_array("contforce"), d.contact_force(case.mesh)
+    touching = np.abs(cf).max(axis=1) > 0
+    assert touching.sum() > 20 and abs(F[2]) > 1e3
+    assert np.abs(cf[:, :2]).max() == 0.0 and F[0] == 0.0 and F[1] == 0.0
+    assert d.geti("dynamic_friction_count") == 0
+    d.close()
+
+
 def test_kernel_gradient_correction_matrix():
     """CalcGradCorrMatrix (Domain.cpp:1832-1940): isotropic (c I, the same c)
     for interior particles of a regular lattice — at h = 1.2 dx the discrete
