@@ -29,12 +29,17 @@ reference's pair terms would break whatever the restatement says:
   from Particle.cpp:997-1000), and the returned deviatoric stress never leaves
   the yield surface of the step before (the scale factor uses the previous
   Sigmay, Particle.cpp:995);
+* an unjittered cylinder upset along z keeps the lattice's symmetries
+  (mirrors x -> -x and y -> -y, the swap x <-> y): vectors and tensors at
+  mirrored particles are the mirrored vectors and tensors, through yielding,
+  rebuilds and contact with the plane;
 * the stress rate is objective: a pre-stressed body spinning rigidly
   carries its stress round with it, dtau/dt = W tau - tau W (the Jaumann
   terms SRT + RS, Particle.cpp:968-981), which fixes the sign convention of
   RotationRate against the velocity gradient.
 """
 import numpy as np
+import pytest
 
 from tests._support import oracle_domain
 from weldform_gb300 import BILINEAR, HOLLOMON, JOHNSON_COOK, configs
@@ -277,3 +282,40 @@ def test_spinning_body_carries_its_stress_round():
     c = moment[calm]
     assert np.ptp(c) <= 1e-12 * c[0] and abs(c[0] - 1.0) > 0.1
     assert (np.abs(rate[0][calm] - c[:, None, None] * jaumann).max(axis=(1, 2)) / scale).max() <= 1e-6
+
+
+def _mirror_partner(x, M):
+    """Index of the particle at M x for every particle (-1 where none)."""
+    q = np.round(x * 1e9).astype(np.int64)
+    where = {tuple(p): i for i, p in enumerate(q)}
+    return np.array([where.get(tuple(p), -1) for p in np.round((x @ M.T) * 1e9).astype(np.int64)])
+
+
+@pytest.mark.parametrize("contact", [False, True], ids=["free", "plane"])
+def test_lattice_symmetries_are_kept(contact):
+    """40 steps at 20 m/s (plastic strain ~2e-2, rebuilds; with the plane:
+    Wang contact and friction 0.2): v and Sigma at the mirror partner of
+    every solid particle are M v and M Sigma M^T to 1e-12 of their largest
+    values without the plane and to 1e-10 with it (its triangles, and so
+    the pairs' order, are not mirror-symmetric)."""
+    maps = {"mirror_x": np.diag([-1.0, 1.0, 1.0]), "mirror_y": np.diag([1.0, -1.0, 1.0]),
+            "swap_xy": np.array([[0.0, 1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])}
+    d = oracle_domain()
+    if contact:
+        case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, jitter_amp=0.0)
+    else:
+        case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_top=-20.0, jitter_amp=0.0)
+    x0 = d.get_array("x")
+    solid = d.get_array("ID") != 10
+    partners = {k: _mirror_partner(x0[solid], M) for k, M in maps.items()}
+    d.prepare(case.dt)
+    d.step(40)
+    v, S = d.get_array("v")[solid], d.get_array("Sigma").reshape(-1, 3, 3)[solid]
+    assert d.get_array("pl_strain").max() > 1e-2 and d.geti("nb_searches") > 2
+    d.close()
+    tol = 1e-10 if contact else 1e-12
+    for k, M in maps.items():
+        m = partners[k]
+        assert (m >= 0).all(), k
+        assert np.abs(v[m] - v @ M.T).max() <= tol * np.abs(v).max(), k
+        assert np.abs(S[m] - M @ S @ M.T).max() <= tol * np.abs(S).max(), k
