@@ -291,31 +291,42 @@ def _mirror_partner(x, M):
     return np.array([where.get(tuple(p), -1) for p in np.round((x @ M.T) * 1e9).astype(np.int64)])
 
 
-@pytest.mark.parametrize("contact", [False, True], ids=["free", "plane"])
-def test_lattice_symmetries_are_kept(contact):
-    """40 steps at 20 m/s (plastic strain ~2e-2, rebuilds; with the plane:
-    Wang contact and friction 0.2): v and Sigma at the mirror partner of
-    every solid particle are M v and M Sigma M^T to 1e-12 of their largest
-    values without the plane and to 1e-10 with it (its triangles, and so
-    the pairs' order, are not mirror-symmetric)."""
+@pytest.mark.parametrize("case_name", ["bilinear", "jc_thermal_ti_corr", "plane"])
+def test_lattice_symmetries_are_kept(case_name):
+    """40 steps at 20 m/s (plastic strain ~2e-2, rebuilds): v and Sigma at
+    the mirror partner of every solid particle are M v and M Sigma M^T, to
+    1e-12 of their largest values for the bilinear cylinder; to 1e-10 with
+    Johnson-Cook, conduction and plastic heating, the tensile-instability
+    term (TI = 0.3) and kernel-gradient correction, whose temperature rise
+    agrees to 1e-6 of its range; and to 1e-10 under the plane (Wang contact,
+    friction 0.2), whose triangles, and so the pairs' order, are not
+    mirror-symmetric."""
     maps = {"mirror_x": np.diag([-1.0, 1.0, 1.0]), "mirror_y": np.diag([1.0, -1.0, 1.0]),
             "swap_xy": np.array([[0.0, 1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])}
     d = oracle_domain()
-    if contact:
+    if case_name == "plane":
         case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_punch=-20.0, jitter_amp=0.0)
-    else:
+    elif case_name == "bilinear":
         case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_top=-20.0, jitter_amp=0.0)
+    else:
+        d.set("gradKernelCorr", 1)
+        case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0005, v_top=-20.0, jitter_amp=0.0,
+                                          model=JOHNSON_COOK, thermal=True)
+        d.set_particles("TI", 0.3)
     x0 = d.get_array("x")
     solid = d.get_array("ID") != 10
     partners = {k: _mirror_partner(x0[solid], M) for k, M in maps.items()}
     d.prepare(case.dt)
     d.step(40)
     v, S = d.get_array("v")[solid], d.get_array("Sigma").reshape(-1, 3, 3)[solid]
+    T = d.get_array("T")[solid]
     assert d.get_array("pl_strain").max() > 1e-2 and d.geti("nb_searches") > 2
     d.close()
-    tol = 1e-10 if contact else 1e-12
+    tol = 1e-12 if case_name == "bilinear" else 1e-10
     for k, M in maps.items():
         m = partners[k]
         assert (m >= 0).all(), k
         assert np.abs(v[m] - v @ M.T).max() <= tol * np.abs(v).max(), k
         assert np.abs(S[m] - M @ S @ M.T).max() <= tol * np.abs(S).max(), k
+        if case_name == "jc_thermal_ti_corr":
+            assert np.ptp(T) > 1.0 and np.abs(T[m] - T).max() <= 1e-6 * np.ptp(T), k
