@@ -396,14 +396,29 @@ def case_mode(a):
     """A fixed-size run of the bench cylinder (R = 10 mm, L = 30 mm, dx chosen
     for about --n particles) for profilers: prepares, runs --steps steps and
     prints the particle count and the step time; --kernels adds per-kernel
-    CUDA-event times of the same number of steps."""
+    CUDA-event times of the same number of steps.  --timed times the steps
+    as the bench does (3 untimed steps, then CUDA events around the graph
+    replays) and adds the full and filtered search counts of the timed span;
+    --nb-skin sets the search reuse's skin before the prologue."""
     import weldform_gb300 as wfmod
     from weldform_gb300 import configs
     dx = configs.dx_for_count(R, L, a.n)
     d = wfmod.Domain()
     d.set("precision", a.precision)
     case = configs.cylinder_upsetting(d, R=R, L=L, dx=dx, v_top=a.v_top)
+    if a.nb_skin is not None:
+        d.set("nb_skin", a.nb_skin)
     d.prepare(case.dt)
+    if a.timed:
+        d.step(3)
+        s0, f0 = d.geti("nb_searches"), d.geti("nb_full_searches")
+        ms, launches = d.step_timed(a.steps)
+        print(f"n={case.n} nb_skin={a.nb_skin} skin_reuse={d.geti('skin_reuse')} steps={a.steps} "
+              f"ms/step={ms / max(a.steps, 1):.4f} launches={launches} "
+              f"searches={d.geti('nb_searches') - s0} full={d.geti('nb_full_searches') - f0} "
+              f"max_pl={d.get('max_pl_strain'):.3e}")
+        d.close()
+        return
     if a.gather_block is not None:
         d.set("gather_block", a.gather_block)
     if a.particle_block is not None:
@@ -690,6 +705,10 @@ def main():
     ap.add_argument("--gather-block", type=int, default=None, help="--case: threads per mixed gather block")
     ap.add_argument("--particle-block", type=int, default=None, help="--case: threads per per-particle block")
     ap.add_argument("--gather-lanes", type=int, default=None, help="--case: lanes per particle, acceleration gather")
+    ap.add_argument("--nb-skin", type=float, default=None,
+                    help="--case: Verlet skin of the search reuse, relative to the pair radius (0: off)")
+    ap.add_argument("--timed", action="store_true",
+                    help="--case: 3 untimed steps, then --steps steps between CUDA events")
     ap.add_argument("--dx-mm", default=None, help="--accuracy: lattice spacings (mm, comma-separated)")
     ap.add_argument("--contact", action="store_true", help="--accuracy: penalty-contact workload")
     ap.add_argument("--sweep", action="store_true", help="batched sweep against every specimen alone")
