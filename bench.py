@@ -66,6 +66,8 @@ ALG_BYTES = {
     "k_density_drift_mx": lambda nnz: 336 + 4 * nnz + 4,  # f64 integration; next-step record written
     "k_rate_mx": lambda nnz: 72 + 4 * nnz + 4,            # next record -> 9 rates, dkin, conduction
     "k_stress_mx": lambda nnz: 440,                       # f64 stress state read + written
+    # the two above in one kernel: the nine f32 rates are neither stored nor reloaded (2 x 36 B)
+    "k_rate_stress_mx": lambda nnz: 72 + 4 * nnz + 4 + 440 - 72,
 }
 # FP64 operations per neighbour entry / per particle (plain form).
 ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": (70, 270)}
@@ -73,6 +75,7 @@ ALG_FLOPS = {"k_accel": (95, 10), "k_density_drift": (40, 20), "k_rate_stress": 
 # step's compulsory traffic per particle-step (state read and written once
 # per pass, neighbour re-reads from cache, 4 B per row entry per gather).
 STEP_KERNELS = {"mixed": ("k_accel_mx", "k_density_drift_mx", "k_rate_mx", "k_stress_mx"),
+                "mixed_fused": ("k_accel_mx", "k_density_drift_mx", "k_rate_stress_mx"),
                 "fp64": ("k_accel", "k_density_drift", "k_rate_stress")}
 # FP64 fused multiply-add rate of the GB300 (`python bench.py --pipe-rates`:
 # 503 G FMA/s), the plain form's secondary ceiling.
@@ -209,11 +212,12 @@ def roofline(d, case, nnz, steps, peak_gbs, peak_kind):
             "kernel_time_shares": shares}
 
 
-def step_roofline(form, nnz, particle_steps_per_s, peak_gbs):
+def step_roofline(form, nnz, particle_steps_per_s, peak_gbs, fused=False):
     """The whole step against HBM: the step kernels' algorithmic bytes per
     particle-step times the particle-steps/s; for the plain form also the
-    algorithmic FP64 flops against the FP64 pipe."""
-    ks = STEP_KERNELS["fp64" if form == "fp64" else "mixed"]
+    algorithmic FP64 flops against the FP64 pipe.  fused: the mixed step runs
+    the rate gather and the stress update as one kernel."""
+    ks = STEP_KERNELS["fp64" if form == "fp64" else ("mixed_fused" if fused else "mixed")]
     b = sum(ALG_BYTES[k](nnz) for k in ks)
     gbs = b * particle_steps_per_s / 1e9
     out = {"bytes_per_particle_step": round(b, 1), "achieved_gbs": round(gbs, 1), "frac_hbm": round(gbs / peak_gbs, 4)}
@@ -409,11 +413,13 @@ def case_mode(a):
     if a.nb_skin is not None:
         d.set("nb_skin", a.nb_skin)
     d.prepare(case.dt)
+    if a.fuse_rate_stress is not None:
+        d.set("fuse_rate_stress", a.fuse_rate_stress)
     if a.timed:
         d.step(3)
         s0, f0 = d.geti("nb_searches"), d.geti("nb_full_searches")
         ms, launches = d.step_timed(a.steps)
-        print(f"n={case.n} nb_skin={a.nb_skin} skin_reuse={d.geti('skin_reuse')} steps={a.steps} "
+        print(f"n={case.n} fuse={d.geti('fuse_rate_stress')} nb_skin={a.nb_skin} skin_reuse={d.geti('skin_reuse')} steps={a.steps} "
               f"ms/step={ms / max(a.steps, 1):.4f} launches={launches} "
               f"searches={d.geti('nb_searches') - s0} full={d.geti('nb_full_searches') - f0} "
               f"max_pl={d.get('max_pl_strain'):.3e}")
@@ -425,6 +431,8 @@ def case_mode(a):
         d.set("particle_block", a.particle_block)
     if a.gather_lanes is not None:
         d.set("gather_lanes", a.gather_lanes)
+    if a.fuse_rate_stress is not None:
+        d.set("fuse_rate_stress", a.fuse_rate_stress)
     t = time.perf_counter()
     d.step(a.steps)
     el = time.perf_counter() - t
@@ -707,6 +715,8 @@ def main():
     ap.add_argument("--gather-lanes", type=int, default=None, help="--case: lanes per particle, acceleration gather")
     ap.add_argument("--nb-skin", type=float, default=None,
                     help="--case: Verlet skin of the search reuse, relative to the pair radius (0: off)")
+    ap.add_argument("--fuse-rate-stress", type=int, default=None, choices=[0, 1],
+                    help="--case: mixed form's rate gather and stress update in one kernel (default 1)")
     ap.add_argument("--timed", action="store_true",
                     help="--case: 3 untimed steps, then --steps steps between CUDA events")
     ap.add_argument("--dx-mm", default=None, help="--accuracy: lattice spacings (mm, comma-separated)")
@@ -807,7 +817,8 @@ def main():
         searches = d.geti("nb_searches") - s0
         full = d.geti("nb_full_searches") - f0
         rl = roofline(d, case, nnz, steps, peak, peak_kind)
-        rl["step"] = step_roofline(name, nnz, val, peak)
+        fused = name != "fp64" and d.geti("fuse_rate_stress") == 1 and d.geti("gather_lanes") == 1
+        rl["step"] = step_roofline(name, nnz, val, peak, fused)
         forms[name] = {"value": val, "ms_per_step": ms_max / steps, "steps": steps, "roofline": rl,
                        "gpu_launches": launches, "clocks": clk.summary(), "v_top": vt,
                        "rebuilds_in_timed_steps": searches, "full_searches_in_timed_steps": full}

@@ -120,10 +120,14 @@ int wf_domain_destroy(wf_domain* d);
  * default 0 keeps the reference's behaviour of stepping on with NaN; no
  * reference counterpart; before the prologue), "particle_block" (threads
  * per block of the per-particle kernels: 64, 128 or 256; 0, the default,
- * chooses by particle count), "cpu_threads" and "cpu_mode" (the CPU
+ * chooses by particle count), "fuse_rate_stress" (mixed form with one lane
+ * per particle: 1, the default, runs the rate gather and the stress update as
+ * one kernel, 0 as two; the results are bit-identical; no reference
+ * counterpart; any time), "cpu_threads" and "cpu_mode" (the CPU
  * restatement's thread count and structure; accepted and unused on the GPU
  * path).  Read back with wf_get_domain_i32: "gather_block", "gather_lanes",
- * "particle_block", "gather_staging", "stage_cap", "search_conditional". */
+ * "particle_block", "fuse_rate_stress", "gather_staging", "stage_cap",
+ * "search_conditional". */
 int wf_set_domain_f64(wf_domain* d, const char* name, double value);
 int wf_set_domain_i32(wf_domain* d, const char* name, int value);
 /* Read-back of scalars: "Time", "deltat", "hmax", "int_energy_sum",

@@ -178,6 +178,46 @@ def test_mixed_gather_block_sizes_agree_bitwise():
             assert np.array_equal(r[f], res[0][f]), f
 
 
+@pytest.mark.parametrize("workload", ["wang_contact", "bilinear_yielding", "hollomon_grad_corr"])
+def test_fused_rate_stress_kernel_is_bit_identical(workload):
+    """The fused rate-stress kernel (the rates kept in registers) against
+    k_rate_mx followed by k_stress_mx: same sums in the same order, same
+    update, same block partials, so every field and every reduced scalar
+    agrees bit for bit after a yielding run.  One lane per particle is forced
+    and the thermal solver is off (the fused kernel serves that launch shape
+    only); the workloads take contact with friction, the plain bilinear
+    return and the corrected-gradient variant with Hollomon hardening."""
+    fields = ("x", "v", "Sigma", "pl_strain", "T", "Density", "StrainRate", "RotationRate",
+              "dint_energy_dt", "dkin_energy_dt", "Sigmay", "q_plheat")
+    res = []
+    for fuse in (0, 1):
+        d = gpu_domain()
+        d.set("precision", PRECISION_MIXED)
+        if workload == "wang_contact":
+            case = configs.contact_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_punch=-10.0, gap=0.0,
+                                             thermal=False)
+        elif workload == "bilinear_yielding":
+            case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_top=-20.0)
+        else:
+            case = configs.cylinder_upsetting(d, R=0.003, L=0.006, dx=0.0003, v_top=-20.0, model=HOLLOMON)
+            d.set("gradKernelCorr", 1)
+        d.prepare(case.dt)
+        d.set("gather_lanes", 1)
+        d.set("fuse_rate_stress", fuse)
+        assert d.geti("fuse_rate_stress") == fuse
+        d.step(60)
+        out = {f: d.get_array(f) for f in fields}
+        for k in ("int_energy_sum", "kin_energy_sum", "max_pl_strain", "Time"):
+            out[k] = d.get(k)
+        out["searches"] = d.geti("nb_searches")
+        res.append(out)
+        d.close()
+    if workload != "wang_contact":
+        assert res[0]["max_pl_strain"] > 0.0
+    for f in res[0]:
+        assert np.array_equal(res[0][f], res[1][f]), f
+
+
 def test_mixed_particles_of_different_mass_and_smoothing_length():
     """Masses spread by +-5 % and two smoothing lengths: the gathers read
     the five-group records (h, mass and Cs per particle) instead of the

@@ -249,6 +249,7 @@ struct DomainConst {
   int contact_surf_id[MAX_MESHES];
   int pblock;          // threads per block of the per-particle kernels (64, 128 or 256)
   int nblocks;         // blocks of the per-particle kernels at pblock (partials stride)
+  int fuse_rs;         // mixed form, one lane per particle: rate gather and stress update in one kernel
   int mixed;           // 1 when the step runs the mixed FP32/FP64 kernels
   int gblock;          // thread-block size of the mixed form's gather kernels
   int glanes;          // lanes per particle of the mixed acceleration gather (1, 2, 4 or 8)

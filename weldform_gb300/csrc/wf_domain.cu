@@ -162,6 +162,7 @@ struct wf_domain {
   int gblock = 0;    // mixed gathers' threads per block (0: chosen by particle count)
   int glanes = 0;    // lanes per particle of the mixed acceleration gather (1, 2, 4, 8; 0: by particle count)
   int pblock = 0;    // per-particle kernels' threads per block (0: chosen by particle count)
+  int fuse_rs = 1;   // mixed form: rate gather and stress update fused in one kernel (one lane per particle)
   // Shared-memory staging of the mixed acceleration gather: the halo lists
   // are allocated at the prologue when it is on; stage_cap is each block's
   // halo capacity (STAGE_B particles per block, 80 B of shared memory per slot).
@@ -182,7 +183,8 @@ struct wf_domain {
   int glanes_now() const { return glanes ? glanes : auto_lanes(hp.N); }
   int pblock_now() const { return pblock ? pblock : auto_block(hp.N); }
   int graph_key() const {
-    return ((gblock_now() * 1024 + pblock_now()) * 16 + glanes_now()) * 2 + (stage_ready && stage ? 1 : 0);
+    return (((gblock_now() * 1024 + pblock_now()) * 16 + glanes_now()) * 2 + (stage_ready && stage ? 1 : 0)) * 2 +
+           (fuse_rs ? 1 : 0);
   }
   struct Region { void* p; size_t bytes; };
   std::vector<Region> regions;           // every mutable device region of the state
@@ -800,6 +802,7 @@ struct wf_domain {
     K.nmeshes = (int)meshes.size();
     for (size_t m = 0; m < meshes.size(); ++m) K.contact_surf_id[m] = meshes[m].id;
     K.pblock = pblock_now();
+    K.fuse_rs = fuse_rs;
     K.nblocks = (N + K.pblock - 1) / K.pblock;
     P.partials = dalloc<double>((size_t)NSLOTS * ((N + 63) / 64));  // room for the smallest block size
     P.scan_tmp = dalloc<long long>((2 * ncells + 4095) / 4096 + 1);
@@ -884,6 +887,7 @@ struct wf_domain {
     k.gblock = gblock_now();
     k.glanes = glanes_now();
     k.pblock = pblock_now();
+    k.fuse_rs = fuse_rs;
     k.nblocks = (int)((hp.N + k.pblock - 1) / k.pblock);
     k.stage_cap = stage_ready && stage ? stage_cap : 0;
     return k;
@@ -1563,6 +1567,11 @@ int wf_set_domain_i32(wf_domain* d, const char* name, int v) {
     d->stage_cap = v;
     return WF_OK;
   }
+  if (n == "fuse_rate_stress") {  // the step graph is captured again at the next step
+    if (v != 0 && v != 1) return set_err(WF_ERR_ARG, "fuse_rate_stress must be 0 or 1");
+    d->fuse_rs = v;
+    return WF_OK;
+  }
   if (n == "particle_block") {  // 0: by particle count
     if (v != 0 && v != 64 && v != 128 && v != 256) return set_err(WF_ERR_ARG, "particle_block must be 0, 64, 128 or 256");
     d->pblock = v;
@@ -1643,6 +1652,7 @@ int wf_get_domain_i32(wf_domain* d, const char* name, int64_t* v) {
     if (n == "gather_lanes") { *v = d->glanes_now(); return WF_OK; }
     if (n == "search_conditional") { *v = d->cond_ok ? 1 : 0; return WF_OK; }
     if (n == "particle_block") { *v = d->pblock_now(); return WF_OK; }
+    if (n == "fuse_rate_stress") { *v = d->fuse_rs; return WF_OK; }
     if (n == "gather_staging") { *v = d->stage ? 1 : 0; return WF_OK; }
     if (n == "stage_cap") { *v = d->stage_cap; return WF_OK; }
     if (n.size() == 8 && n.rfind("CellNo.", 0) == 0 && n[7] >= 'x' && n[7] <= 'z') { *v = d->CellNo[n[7] - 'x']; return WF_OK; }
